@@ -1,0 +1,326 @@
+"""ctypes wrapper around the CPU f64 oracle (oracle/rz_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
+and by the CPU-baseline leg of ``bench.py``; the product package never imports
+this module.  Arcs are expanded here exactly like ``PathBuilder::arc_to``
+(src/path.rs:945-972) does at path-build time in the reference, so the oracle
+sees the same Line/Quad/Cubic segments as the reference's rasterizers.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "librz_oracle.so")
+SRC = os.path.join(HERE, "rz_oracle.c")
+
+SEG_LINE, SEG_QUAD, SEG_CUBIC, SEG_ARC = 0, 1, 2, 3
+MAX_STOPS = 32
+
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compiles the oracle with the flags that keep binary64 op order (no FMA contraction)."""
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(SRC):
+        tmp = LIB_PATH + ".tmp.%d" % os.getpid()
+        subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+                               "-o", tmp, SRC, "-lm", "-lpthread"])
+        os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+class Paint(ctypes.Structure):
+    """Mirror of ``rzo_paint`` in rz_oracle.c."""
+
+    _fields_ = [
+        ("kind", ctypes.c_int32), ("units", ctypes.c_int32), ("spread", ctypes.c_int32),
+        ("linear_colors", ctypes.c_int32),
+        ("tr", ctypes.c_double * 6),
+        ("p0", ctypes.c_double * 2), ("p1", ctypes.c_double * 2),
+        ("r0", ctypes.c_double), ("r1", ctypes.c_double),
+        ("nstops", ctypes.c_int32), ("pad", ctypes.c_int32),
+        ("stop_pos", ctypes.c_double * MAX_STOPS),
+        ("stop_col", (ctypes.c_float * 4) * MAX_STOPS),
+        ("solid", ctypes.c_float * 4),
+    ]
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            L = ctypes.CDLL(build())
+            P = ctypes.c_void_p
+            L.rzo_flatten.restype = ctypes.c_long
+            L.rzo_flatten.argtypes = [P, P, P, ctypes.c_long, P, ctypes.c_double, P, ctypes.c_long, P]
+            L.rzo_mask.restype = ctypes.c_int
+            L.rzo_mask.argtypes = [P, P, P, ctypes.c_long, P, ctypes.c_int, ctypes.c_double, P] + [ctypes.c_long] * 6
+            L.rzo_mask_iter.restype = ctypes.c_long
+            L.rzo_mask_iter.argtypes = [P, P, P, ctypes.c_long, P, ctypes.c_int, ctypes.c_double,
+                                        ctypes.c_long, ctypes.c_long, P]
+            L.rzo_mask_ae.restype = ctypes.c_int
+            L.rzo_mask_ae.argtypes = [P, P, P, ctypes.c_long, P, ctypes.c_int, ctypes.c_double, P,
+                                      ctypes.c_long, ctypes.c_long]
+            L.rzo_signed_difference_line.restype = None
+            L.rzo_signed_difference_line.argtypes = [P] + [ctypes.c_long] * 6 + [ctypes.c_double] * 4
+            L.rzo_arc_to_cubics.restype = ctypes.c_int
+            L.rzo_arc_to_cubics.argtypes = [ctypes.c_double] * 7 + [ctypes.c_int, ctypes.c_int, P, ctypes.c_int]
+            L.rzo_alpha_from_winding.restype = ctypes.c_double
+            L.rzo_alpha_from_winding.argtypes = [ctypes.c_int, ctypes.c_double]
+            L.rzo_paint_at.restype = None
+            L.rzo_paint_at.argtypes = [ctypes.POINTER(Paint), ctypes.c_double, ctypes.c_double, P]
+            L.rzo_radial_offset.restype = ctypes.c_int
+            L.rzo_radial_offset.argtypes = [ctypes.POINTER(Paint), ctypes.c_double, ctypes.c_double, P]
+            L.rzo_spread_at.restype = ctypes.c_double
+            L.rzo_spread_at.argtypes = [ctypes.c_int, ctypes.c_double]
+            for name in ("rzo_l2s", "rzo_s2l", "rzo_into_srgb", "rzo_into_linear"):
+                getattr(L, name).restype = None
+                getattr(L, name).argtypes = [P, P]
+            for name in ("rzo_linear_to_srgb", "rzo_srgb_to_linear"):
+                getattr(L, name).restype = ctypes.c_float
+                getattr(L, name).argtypes = [ctypes.c_float]
+            L.rzo_path_bbox.restype = ctypes.c_int
+            L.rzo_path_bbox.argtypes = [P, P, P, ctypes.c_long, P, P]
+            L.rzo_fill.restype = ctypes.c_int
+            L.rzo_fill.argtypes = [P, P, P, ctypes.c_long, P, ctypes.c_int, ctypes.c_double,
+                                   ctypes.POINTER(Paint), P] + [ctypes.c_long] * 5
+            L.rzo_scene_render.restype = ctypes.c_int
+            L.rzo_scene_render.argtypes = [P, P, P, P, P, ctypes.c_long, P, P, ctypes.POINTER(Paint),
+                                           ctypes.c_double, ctypes.c_long, ctypes.c_long, P, P]
+            _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _tr(tr):
+    m = tr.m if hasattr(tr, "m") else tr
+    return np.ascontiguousarray(m, dtype=np.float64)
+
+
+class OraclePath:
+    """Arc-free SoA path as the reference holds it after PathBuilder::build."""
+
+    def __init__(self, kind, pts, sub_off):
+        self.kind = np.ascontiguousarray(kind, dtype=np.uint8)
+        self.pts = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 8)
+        self.sub_off = np.ascontiguousarray(sub_off, dtype=np.uint32)
+
+    @property
+    def nsub(self):
+        return len(self.sub_off) - 1
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+def arc_to_cubics(src, dst, radii, rot, large, sweep):
+    """EllipArc::new_param + to_cubics; returns an (n, 8) array, or None when
+    new_param yields None (PathBuilder then falls back to line_to)."""
+    out = np.zeros((8, 8), dtype=np.float64)
+    n = lib().rzo_arc_to_cubics(src[0], src[1], dst[0], dst[1], radii[0], radii[1], rot,
+                                int(bool(large)), int(bool(sweep)), _ptr(out), 8)
+    if n == -1:
+        return None
+    if n < 0:
+        raise OracleError("arc has no finite cubic count (the reference iterator never terminates)")
+    return out[:n]
+
+
+def expand_path(path) -> OraclePath:
+    """Expands ARC segments into cubics like PathBuilder::arc_to; drops
+    subpaths that end up empty (PathBuilder::subpath_finish records none)."""
+    kind = np.asarray(path.kind)
+    pts = np.asarray(path.pts).reshape(-1, 8)
+    sub = np.asarray(path.subpath_off)
+    if not np.any(kind == SEG_ARC):
+        return OraclePath(kind, pts, sub)
+    ok, op, off = [], [], [0]
+    for s in range(len(sub) - 1):
+        for i in range(int(sub[s]), int(sub[s + 1])):
+            k = int(kind[i])
+            if k != SEG_ARC:
+                ok.append(k)
+                op.append(pts[i])
+                continue
+            p = pts[i]
+            flags = int(p[7])
+            cub = arc_to_cubics((p[0], p[1]), (p[2], p[3]), (p[4], p[5]), p[6], flags & 1, flags & 2)
+            if cub is None:
+                if not (abs(p[0] - p[2]) < 2.220446049250313e-16 and abs(p[1] - p[3]) < 2.220446049250313e-16):
+                    ok.append(SEG_LINE)
+                    op.append(np.array([p[0], p[1], p[2], p[3], 0, 0, 0, 0], dtype=np.float64))
+            else:
+                for c in cub:
+                    ok.append(SEG_CUBIC)
+                    op.append(c)
+        if len(ok) > off[-1]:
+            off.append(len(ok))
+    return OraclePath(np.asarray(ok, np.uint8), np.asarray(op, np.float64).reshape(-1, 8),
+                      np.asarray(off, np.uint32))
+
+
+def flatten(path, tr, flatness=0.05):
+    """Path::flatten(tr, flatness, close=true).  Returns (lines (n,4), counts)
+    where counts holds per-segment line counts then one per subpath closing line."""
+    op = path if isinstance(path, OraclePath) else expand_path(path)
+    L = lib()
+    counts = np.zeros(len(op.kind) + op.nsub, dtype=np.int64)
+    n = L.rzo_flatten(_ptr(op.kind), _ptr(op.pts), _ptr(op.sub_off), op.nsub, _ptr(_tr(tr)), flatness,
+                      None, 0, _ptr(counts))
+    if n < 0:
+        raise OracleError("cannot flatten segment with NaN")
+    out = np.zeros((max(n, 1), 4), dtype=np.float64)
+    L.rzo_flatten(_ptr(op.kind), _ptr(op.pts), _ptr(op.sub_off), op.nsub, _ptr(_tr(tr)), flatness,
+                  _ptr(out), n, _ptr(counts))
+    return out[:n], counts
+
+
+def mask(path, tr, fill_rule, width, height, flatness=0.05, img=None, shape=None):
+    """SignedDifferenceRasterizer::mask into a zeroed (height, width) f64 image,
+    or into ``img`` viewed with ``shape = (start, width, height, row_stride, col_stride)``."""
+    op = path if isinstance(path, OraclePath) else expand_path(path)
+    if img is None:
+        img = np.zeros((height, width), dtype=np.float64)
+        shape = (0, width, height, width, 1)
+    flat = img.reshape(-1)
+    rc = lib().rzo_mask(_ptr(op.kind), _ptr(op.pts), _ptr(op.sub_off), op.nsub, _ptr(_tr(tr)), int(fill_rule),
+                        flatness, _ptr(flat), flat.size, *shape)
+    if rc < 0:
+        raise OracleError("cannot flatten segment with NaN")
+    return img
+
+
+def mask_iter(path, tr, fill_rule, width, height, flatness=0.05):
+    """SignedDifferenceRasterizer::mask_iter materialised as a dense image
+    (pixels the iterator skips stay 0).  Returns (image, yielded pixel count)."""
+    op = path if isinstance(path, OraclePath) else expand_path(path)
+    out = np.zeros((height, width), dtype=np.float64)
+    n = lib().rzo_mask_iter(_ptr(op.kind), _ptr(op.pts), _ptr(op.sub_off), op.nsub, _ptr(_tr(tr)),
+                            int(fill_rule), flatness, width, height, _ptr(out))
+    if n < 0:
+        raise OracleError("cannot flatten segment with NaN")
+    return out, n
+
+
+def mask_ae(path, tr, fill_rule, width, height, flatness=0.05):
+    """ActiveEdgeRasterizer::mask into a zeroed image (independent cross-check)."""
+    op = path if isinstance(path, OraclePath) else expand_path(path)
+    out = np.zeros((height, width), dtype=np.float64)
+    rc = lib().rzo_mask_ae(_ptr(op.kind), _ptr(op.pts), _ptr(op.sub_off), op.nsub, _ptr(_tr(tr)), int(fill_rule),
+                           flatness, _ptr(out), width, height)
+    if rc < 0:
+        raise OracleError("cannot flatten segment with NaN")
+    return out
+
+
+def signed_difference_line(img, line, shape=None):
+    flat = img.reshape(-1)
+    h, w = img.shape
+    if shape is None:
+        shape = (0, w, h, w, 1)
+    lib().rzo_signed_difference_line(_ptr(flat), flat.size, *shape, *[float(v) for v in line])
+    return img
+
+
+def path_bbox(path, tr):
+    op = path if isinstance(path, OraclePath) else expand_path(path)
+    out = np.zeros(4)
+    if not lib().rzo_path_bbox(_ptr(op.kind), _ptr(op.pts), _ptr(op.sub_off), op.nsub, _ptr(_tr(tr)), _ptr(out)):
+        return None
+    return out
+
+
+def make_paint(kind=0, units=0, spread=0, linear_colors=True, tr=None, p0=(0, 0), p1=(0, 0), r0=0.0, r1=0.0,
+               stops=(), solid=(0, 0, 0, 0)) -> Paint:
+    p = Paint()
+    p.kind, p.units, p.spread, p.linear_colors = int(kind), int(units), int(spread), int(bool(linear_colors))
+    m = (1, 0, 0, 0, 1, 0) if tr is None else (tr.m if hasattr(tr, "m") else tr)
+    for i in range(6):
+        p.tr[i] = m[i]
+    p.p0[0], p.p0[1] = p0
+    p.p1[0], p.p1[1] = p1
+    p.r0, p.r1 = r0, r1
+    if len(stops) > MAX_STOPS:
+        raise ValueError("too many stops")
+    p.nstops = len(stops)
+    for i, (pos, col) in enumerate(stops):
+        p.stop_pos[i] = pos
+        for c in range(4):
+            p.stop_col[i][c] = col[c]
+    for c in range(4):
+        p.solid[c] = solid[c]
+    return p
+
+
+def paint_at(paint: Paint, x, y):
+    out = np.zeros(4, dtype=np.float32)
+    lib().rzo_paint_at(ctypes.byref(paint), x, y, _ptr(out))
+    return out
+
+
+def radial_offset(paint: Paint, x, y):
+    out = np.zeros(1)
+    if not lib().rzo_radial_offset(ctypes.byref(paint), x, y, _ptr(out)):
+        return None
+    return float(out[0])
+
+
+def color_fn(name, rgba):
+    a = np.ascontiguousarray(rgba, dtype=np.float32)
+    out = np.zeros(4, dtype=np.float32)
+    getattr(lib(), name)(_ptr(a), _ptr(out))
+    return out
+
+
+def fill(path, tr, fill_rule, paint: Paint, img, shape=None, flatness=0.05):
+    """Rasterizer::fill (default method) into an RGBA f32 image (H, W, 4)."""
+    op = path if isinstance(path, OraclePath) else expand_path(path)
+    h, w = img.shape[:2]
+    if shape is None:
+        shape = (0, w, h, w, 1)
+    rc = lib().rzo_fill(_ptr(op.kind), _ptr(op.pts), _ptr(op.sub_off), op.nsub, _ptr(_tr(tr)), int(fill_rule),
+                        flatness, ctypes.byref(paint), _ptr(img.reshape(-1)), *shape)
+    if rc < 0:
+        raise OracleError("cannot flatten segment with NaN")
+    return img
+
+
+def scene_render(paths, trs, rules, paints, width, height, bg=(0, 0, 0, 0), flatness=0.05):
+    """Scene::render of a Group of Fill nodes in path order over a (height, width)
+    RGBA f32 canvas initialised to ``bg`` (view = the canvas, tr = identity)."""
+    ops = [p if isinstance(p, OraclePath) else expand_path(p) for p in paths]
+    kind = np.ascontiguousarray(np.concatenate([o.kind for o in ops]).astype(np.uint8))
+    pts = np.ascontiguousarray(np.concatenate([o.pts for o in ops]).astype(np.float64))
+    tab, starts, nsubs = [], [], []
+    base = 0
+    for o in ops:
+        starts.append(len(tab))
+        nsubs.append(o.nsub)
+        tab.extend((o.sub_off.astype(np.int64) + base).tolist())
+        base += len(o.kind)
+    tab = np.ascontiguousarray(np.asarray(tab, dtype=np.uint32))
+    starts = np.ascontiguousarray(np.asarray(starts, dtype=np.int64))
+    nsubs = np.ascontiguousarray(np.asarray(nsubs, dtype=np.int64))
+    trs_a = np.ascontiguousarray(np.array([t.m if hasattr(t, "m") else t for t in trs], dtype=np.float64))
+    rules_a = np.ascontiguousarray(np.array([int(r) for r in rules], dtype=np.int32))
+    paints_a = (Paint * len(paints))(*paints)
+    canvas = np.zeros((height, width, 4), dtype=np.float32)
+    bg_a = np.ascontiguousarray(bg, dtype=np.float32)
+    rc = lib().rzo_scene_render(_ptr(kind), _ptr(pts), _ptr(tab), _ptr(starts), _ptr(nsubs), len(ops), _ptr(trs_a),
+                                _ptr(rules_a), paints_a, flatness, width, height, _ptr(bg_a), _ptr(canvas))
+    if rc < 0:
+        raise OracleError("cannot flatten segment with NaN")
+    return canvas
