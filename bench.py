@@ -1,0 +1,362 @@
+#!/usr/bin/env python
+"""Benchmark of the rasterize hot path on GB300.
+
+Workload (default, ``glyphs``): 10,000 independent closed glyph outlines,
+10-400 segments each (log-uniform, 70 % cubic / 30 % quad), square boxes of
+16-256 px (log-uniform), each rendered to its own f32 mask with NonZero fill
+and flatness 0.05 (synthetic, seeded; ~1.07 M segments, ~118 Mpx per step).
+One step = one pass of flatten + coverage + fill rule over the whole batch.
+
+* ``value``      Mpx/s with inputs resident in HBM: the batch plan (one
+  persistent-kernel launch replayed from a CUDA graph) launched back to back.
+* ``e2e``        the same metric through the C ABI with host buffers
+  (``rz_mask_batch``, pinned inputs in, masks back to pinned host memory).
+* ``roofline``   the band kernel against the measured HBM copy bandwidth.
+* ``cpu_baseline``  the CPU f64 oracle on a bounded sample, 1 thread.
+
+``--impl reference`` times the reference's CPU algorithm (the oracle port,
+the reference crate is Rust and cannot be built here) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mpx/s + segments/s, batched vs per-path GPU at ≤1e-4 err; backward ms/step"
+WORKLOAD = "glyph_batch: 10000 closed glyphs, 10-400 segs (70% cubic/30% quad), 16-256 px masks, NonZero, f=0.05"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--glyphs", type=int, default=10000)
+    ap.add_argument("--cpu-seconds", type=float, default=8.0, help="bounded CPU baseline sample")
+    ap.add_argument("--no-per-path", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(name: str):
+    """Per-launch DRAM bytes from the committed ncu summary (profiles/<name>.md)."""
+    p = os.path.join(ROOT, "profiles", name + ".md")
+    try:
+        for line in open(p):
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].strip().split()[0])
+    except Exception:
+        pass
+    return None
+
+
+def make_workload(n):
+    from rasterize_gb300 import MaskBatch
+    from rasterize_gb300 import workloads as W
+    paths, sizes, rules = W.glyph_batch(seed=2, n=n)
+    return paths, sizes, rules, MaskBatch(paths, sizes, fill_rules=rules)
+
+
+# --------------------------------------------------------------------------- CPU
+def _oracle_chunk(args):
+    """Worker: renders glyphs [lo, hi) with the f64 oracle; returns (pixels, seconds)."""
+    lo, hi, n = args
+    sys.path.insert(0, ROOT)
+    from oracle import oracle as O
+    from rasterize_gb300 import Transform
+    from rasterize_gb300 import workloads as W
+    paths, sizes, rules = W.glyph_batch(seed=2, n=n)
+    t = time.perf_counter()
+    px = 0
+    for i in range(lo, hi):
+        w, h = sizes[i]
+        O.mask(paths[i], Transform.identity(), rules[i], w, h)
+        px += w * h
+    return px, time.perf_counter() - t
+
+
+def cpu_baseline_single(paths, sizes, rules, seconds):
+    """The oracle (reference algorithm restated in C, f64) on 1 thread over a
+    bounded prefix sample of the same batch."""
+    from oracle import oracle as O
+    from rasterize_gb300 import Transform
+    O.build()
+    t0 = time.perf_counter()
+    px, segs, n = 0, 0, 0
+    for i in range(len(paths)):
+        w, h = sizes[i]
+        O.mask(paths[i], Transform.identity(), rules[i], w, h)
+        px += w * h
+        segs += paths[i].n_segments
+        n += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": round(px / dt / 1e6, 3), "unit": "Mpx/s", "cores": 1, "kind": "port",
+            "sample": "first %d of 10000 glyphs (%.1f Mpx, %d segments) in %.2f s" % (n, px / 1e6, segs, dt),
+            "masks_per_s": round(n / dt, 2)}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    from oracle import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    paths, sizes, rules, batch = make_workload(args.glyphs)
+    # bounded per-step sample sized to ~seconds of CPU work per step on all cores
+    per_core = 60
+    sample = min(len(paths), cores * per_core)
+    chunks = [(i * sample // cores, (i + 1) * sample // cores, args.glyphs) for i in range(cores)]
+    ctx = mp.get_context("spawn")
+    times = []
+    px_step = sum(sizes[i][0] * sizes[i][1] for i in range(sample))
+    with ctx.Pool(cores) as pool:
+        for s in range(args.warmup + args.steps):
+            t = time.perf_counter()
+            res = pool.map(_oracle_chunk, chunks)
+            dt = time.perf_counter() - t
+            if s >= args.warmup:
+                times.append(dt)
+    dt = sum(times) / len(times)
+    value = px_step / dt / 1e6
+    out = {"metric": METRIC, "value": round(value, 3), "unit": "Mpx/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
+           "config": {"workload": WORKLOAD, "sample_glyphs_per_step": sample},
+           "cpu_baseline": {"value": round(value, 3), "unit": "Mpx/s", "cores": cores, "kind": "port",
+                            "sample": "first %d of 10000 glyphs per step (%.2f Mpx), spawn pool of %d processes"
+                                      % (sample, px_step / 1e6, cores)},
+           "e2e": {"value": round(value, 3), "unit": "Mpx/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+# --------------------------------------------------------------------------- GPU
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    from rasterize_gb300 import GpuRasterizer, Transform
+
+    paths, sizes, rules, batch = make_workload(args.glyphs)
+    R = GpuRasterizer(device=local)
+    stream = torch.cuda.current_stream(dev)
+    R.ctx.set_stream(stream.cuda_stream)
+
+    # ---- device-resident inputs / output
+    d_kind = torch.from_numpy(batch.kind).to(dev)
+    d_pts = torch.from_numpy(batch.pts.reshape(-1)).to(dev)
+    d_sub = torch.from_numpy(batch.sub_off.view(np.int32)).to(dev)
+    d_psub = torch.from_numpy(batch.path_sub.view(np.int32)).to(dev)
+    d_rule = torch.from_numpy(batch.fill_rules).to(dev)
+    d_out = torch.empty(batch.out_len, dtype=torch.float32, device=dev)
+    ptrs = dict(kind=d_kind.data_ptr(), pts=d_pts.data_ptr(), sub_off=d_sub.data_ptr(), path_sub=d_psub.data_ptr(),
+                fill_rules=d_rule.data_ptr())
+    plan = R.plan(batch, ptrs, d_out.data_ptr())
+    for _ in range(args.warmup):
+        plan.launch()
+    plan.status()
+    torch.cuda.synchronize(dev)
+
+    # ---- accuracy on a sample (oracle is the checker)
+    from oracle import oracle as O
+    out_host = d_out.cpu().numpy()
+    err_max, err_sum, err_n = 0.0, 0.0, 0
+    for i in range(0, len(paths), max(1, len(paths) // 200)):
+        w, h = sizes[i]
+        ref = O.mask(paths[i], Transform.identity(), rules[i], w, h)
+        e = np.abs(batch.mask(out_host, i) - ref)
+        err_max = max(err_max, float(e.max()))
+        err_sum += float(e.sum())
+        err_n += e.size
+
+    # ---- timed region: device-resident batch, graph replay
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for s in range(args.steps):
+        ev[s][0].record(stream)
+        plan.launch()
+        ev[s][1].record(stream)
+    t_end.record(stream)
+    torch.cuda.synchronize(dev)
+    clk = clocks.stop()
+    plan.status()
+    total_ms = t_start.elapsed_time(t_end)
+    if world > 1:
+        tt = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    launch_ms = [a.elapsed_time(b) for a, b in ev]
+    kernel_ms = statistics.mean(launch_ms)
+    ms_per_step = total_ms / args.steps
+    px = batch.pixels
+    value = px * world / (ms_per_step / 1e3) / 1e6
+    n_items, fallbacks = plan.info()
+
+    # ---- plain per-path launches (same batch, one launch per glyph)
+    per_path = None
+    if not args.no_per_path:
+        R.mask_batch_device(batch, ptrs, d_out.data_ptr(), per_path=True)
+        torch.cuda.synchronize(dev)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        R.mask_batch_device(batch, ptrs, d_out.data_ptr(), per_path=True)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        pp_ms = a.elapsed_time(b)
+        per_path = {"ms_per_step": round(pp_ms, 3), "masks_per_s": round(len(paths) / (pp_ms / 1e3), 1),
+                    "launches": len(paths)}
+
+    # ---- e2e through the C ABI with host buffers (pinned)
+    h_kind = torch.from_numpy(batch.kind).pin_memory().numpy()
+    h_pts = torch.from_numpy(batch.pts).pin_memory().numpy()
+    h_out = torch.empty(batch.out_len, dtype=torch.float32).pin_memory().numpy()
+    batch.kind, batch.pts = h_kind, h_pts
+    for _ in range(2):
+        R.mask_batch(batch, out=h_out)
+    e_ms = []
+    for _ in range(max(3, min(args.steps, 10))):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        R.mask_batch(batch, out=h_out)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        e_ms.append(a.elapsed_time(b))
+    e2e_ms = statistics.median(e_ms)
+    h2d = batch.kind.nbytes + batch.pts.nbytes + batch.sub_off.nbytes + batch.path_sub.nbytes + batch.fill_rules.nbytes
+    d2h = batch.out_len * 4
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak_hbm()
+    algo_bytes = px * 4 + batch.n_segments * (64 + 1) + (len(batch.sub_off) + len(batch.path_sub)) * 4
+    achieved = algo_bytes / (kernel_ms / 1e3) / 1e9
+    traffic = profile_traffic("mask_bands_glyph_batch")
+    cpu = cpu_baseline_single(paths, sizes, rules, args.cpu_seconds)
+    out = {
+        "metric": METRIC, "value": round(value, 2), "unit": "Mpx/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded glyph outlines)",
+        "config": {"workload": WORKLOAD, "glyphs": len(paths), "segments": batch.n_segments,
+                   "pixels_per_step": px, "flatness": 0.05, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "masks written per step (%.0f MB) exceed the 129 MB L2" % (px * 4 / 1e6)},
+        "segments_per_s": round(batch.n_segments * world / (ms_per_step / 1e3), 1),
+        "masks_per_s": round(len(paths) * world / (ms_per_step / 1e3), 1),
+        "per_path": per_path,
+        "batched_vs_per_path": round(per_path["ms_per_step"] / ms_per_step, 2) if per_path else None,
+        "err": {"max_abs": err_max, "mean_abs": err_sum / max(err_n, 1), "tolerance": 1e-4,
+                "sampled_glyphs": len(range(0, len(paths), max(1, len(paths) // 200)))},
+        "work_items": n_items, "f64_fallbacks_total": fallbacks,
+        "e2e": {"value": round(px / (e2e_ms / 1e3) / 1e6, 2), "unit": "Mpx/s", "ms_per_step": round(e2e_ms, 3),
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+                     "kernel": "k_mask_bands", "algorithmic_bytes_per_launch": int(algo_bytes),
+                     "kernel_ms": round(kernel_ms, 4)},
+        "cpu_baseline": cpu,
+        "gpu_launches": args.steps,
+        "clocks": clk,
+    }
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

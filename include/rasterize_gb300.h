@@ -1,0 +1,185 @@
+/*
+ * rasterize_gb300.h -- C ABI of the GB300 (sm_103a) rasterizer library.
+ *
+ * Drop-in boundary for the `Rasterizer` trait of aslpavel/rasterize v0.6.7
+ * (src/rasterize.rs:44-101): a Rust `GpuRasterizer` (source in INTEGRATION.md)
+ * packs its `Path` (src/path.rs:228-233) into `rz_path`, calls these entry
+ * points and keeps the crate's `Path` / `Transform` / `FillRule` / `ImageMut`
+ * API unchanged.  Every entry point returns a status; nothing traps or
+ * panics.  All functions are callable from any host thread; calls on one
+ * context are serialised on the context's stream.
+ */
+#ifndef RASTERIZE_GB300_H
+#define RASTERIZE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define RZ_API __attribute__((visibility("default")))
+#else
+#define RZ_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+typedef int32_t rz_status;
+#define RZ_OK 0
+#define RZ_ERR_NAN 1          /* a segment holds NaN: the reference panics (src/path.rs:765-767) */
+#define RZ_ERR_INVALID 2      /* bad argument (sizes, pointers, flatness <= 0, ...) */
+#define RZ_ERR_CUDA 3         /* CUDA runtime error; rz_last_error() has the text */
+#define RZ_ERR_NO_DEVICE 4    /* no CUDA device / the library cannot run here */
+#define RZ_ERR_DEPTH 5        /* a curve needs more than 22 bisection levels */
+#define RZ_ERR_ARC 6          /* an arc has no finite cubic count (the reference never terminates) */
+#define RZ_ERR_CAPACITY 7     /* an internal buffer limit was exceeded */
+#define RZ_ERR_SPIN 8         /* a bounded device wait gave up */
+
+/* ---- enums mirroring the reference ------------------------------------- */
+#define RZ_SEG_LINE 0  /* Segment::Line  src/curve.rs:905-909 */
+#define RZ_SEG_QUAD 1  /* Segment::Quad */
+#define RZ_SEG_CUBIC 2 /* Segment::Cubic */
+#define RZ_SEG_ARC 3   /* PathBuilder::arc_to arguments, expanded on the device (src/path.rs:945-972) */
+
+#define RZ_FILL_NONZERO 0 /* FillRule::NonZero src/path.rs:21-47 */
+#define RZ_FILL_EVENODD 1 /* FillRule::EvenOdd */
+
+#define RZ_MEM_HOST 0   /* pointers in a descriptor are host memory */
+#define RZ_MEM_DEVICE 1 /* pointers in a descriptor are device memory of the context's GPU */
+
+/* ---- paths -------------------------------------------------------------- */
+/* One path in the reference's structure-of-arrays form (src/path.rs:228-233).
+ * seg_pts holds 8 doubles per segment: up to four control points
+ * x0 y0 x1 y1 x2 y2 x3 y3; an ARC holds sx sy dx dy rx ry x_axis_rot_deg flags
+ * (flags bit0 = large_arc, bit1 = sweep).  subpath_off has n_subpaths + 1
+ * segment offsets.  closed is informational: rasterizers always close
+ * (src/rasterize.rs:307).  Host memory. */
+typedef struct rz_path {
+    const uint8_t* seg_kind;
+    const double* seg_pts;
+    const uint32_t* subpath_off;
+    const uint8_t* closed;
+    uint32_t n_segments;
+    uint32_t n_subpaths;
+} rz_path;
+
+/* Strided image view, element units (image.rs:6-35 Shape). */
+typedef struct rz_shape {
+    uint64_t start;
+    uint64_t width;
+    uint64_t height;
+    uint64_t row_stride;
+    uint64_t col_stride;
+} rz_shape;
+
+/* Sparse pixel yielded by Rasterizer::mask_iter (src/rasterize.rs:664-672). */
+typedef struct rz_pixel {
+    uint64_t x;
+    uint64_t y;
+    double alpha;
+} rz_pixel;
+
+/* Many independent paths, each rendered into its own mask.  Segments of all
+ * paths are concatenated; subpath_off holds global segment offsets
+ * (n_subpaths + 1); path_subpath_off (n_paths + 1) gives each path's subpath
+ * range.  transforms: n_paths * 6 doubles or NULL (identity).  fill_rules:
+ * n_paths bytes or NULL (NonZero).  `memory` says where seg_kind, seg_pts,
+ * subpath_off, path_subpath_off, transforms and fill_rules live; masks
+ * (descriptors) are always host memory. */
+typedef struct rz_mask_desc {
+    uint64_t offset;     /* element offset of pixel (0,0) in the output buffer */
+    uint32_t width;
+    uint32_t height;
+    uint32_t row_stride; /* elements between rows (>= width) */
+    uint32_t reserved;
+} rz_mask_desc;
+
+typedef struct rz_path_batch {
+    uint32_t n_paths;
+    uint32_t n_segments;
+    uint32_t n_subpaths;
+    int32_t memory;
+    const uint8_t* seg_kind;
+    const double* seg_pts;
+    const uint32_t* subpath_off;
+    const uint32_t* path_subpath_off;
+    const double* transforms;
+    const uint8_t* fill_rules;
+    const rz_mask_desc* masks;
+} rz_path_batch;
+
+typedef struct rz_ctx rz_ctx;
+
+/* ---- context ------------------------------------------------------------ */
+/* Creates a context on `device` with its own non-blocking stream.  Replaces
+ * the constructor `SignedDifferenceRasterizer::new(flatness)`
+ * (src/rasterize.rs:284-296); flatness is passed per call instead. */
+RZ_API rz_ctx* rz_create(int device, rz_status* status);
+RZ_API void rz_destroy(rz_ctx* ctx);
+/* Text of the last error on this context ("" when none). */
+RZ_API const char* rz_last_error(const rz_ctx* ctx);
+/* Runs the context's work on `stream` (a cudaStream_t) instead of its own. */
+RZ_API rz_status rz_set_stream(rz_ctx* ctx, void* stream);
+RZ_API void* rz_get_stream(const rz_ctx* ctx);
+RZ_API rz_status rz_synchronize(rz_ctx* ctx);
+/* Library version string. */
+RZ_API const char* rz_version(void);
+
+/* ---- Rasterizer::mask -------------------------------------------------- */
+/* SignedDifferenceRasterizer::mask (src/rasterize.rs:299-311) followed by the
+ * fill rule (src/rasterize.rs:473-507): rasterises `path` transformed by
+ * `tr` (6 doubles, src/geometry.rs:317) into the host f64 view `img`/`shape`.
+ * The view's pixels are overwritten with the mask the reference produces on a
+ * zeroed image (the reference's contract, src/path.rs:509-512). */
+RZ_API rz_status rz_mask(rz_ctx* ctx, const rz_path* path, const double tr[6], int32_t fill_rule,
+                  double flatness, double* img, rz_shape shape);
+
+/* SignedDifferenceRasterizer::mask_iter (src/rasterize.rs:313-355): writes up
+ * to `cap` pixels with |alpha| >= 1e-6 in row-major order into `pixels` and
+ * their total count into *n_pixels (which may exceed cap). */
+RZ_API rz_status rz_mask_iter(rz_ctx* ctx, const rz_path* path, const double tr[6], int32_t fill_rule,
+                       double flatness, uint64_t width, uint64_t height, rz_pixel* pixels,
+                       uint64_t cap, uint64_t* n_pixels);
+
+/* Renders every path of `batch` into its own f32 mask in `out` (mask
+ * semantics as rz_mask; out has out_len elements, host or device memory per
+ * batch->memory).  One persistent-kernel launch for the whole batch. */
+RZ_API rz_status rz_mask_batch(rz_ctx* ctx, const rz_path_batch* batch, double flatness, float* out,
+                        uint64_t out_len);
+
+/* Same batch rendered the plain way: one rasterisation launch per path, in
+ * path order (the per-path GPU baseline the batched kernel is measured against). */
+RZ_API rz_status rz_mask_batch_per_path(rz_ctx* ctx, const rz_path_batch* batch, double flatness,
+                                 float* out, uint64_t out_len);
+
+/* ---- batch plans: resident work list + CUDA graph replay ---------------- */
+/* A plan fixes one device-memory batch (batch->memory == RZ_MEM_DEVICE), its
+ * output buffer and flatness.  Creating it uploads the work list (bands of
+ * rows, longest first) and mask descriptors once; each launch replays a
+ * captured CUDA graph (queue reset + one persistent-kernel launch) on the
+ * context's stream without any host synchronisation.  The input arrays may be
+ * rewritten between launches (same sizes). */
+typedef struct rz_batch_plan rz_batch_plan;
+RZ_API rz_batch_plan* rz_batch_plan_create(rz_ctx* ctx, const rz_path_batch* batch, double flatness, float* out,
+                                           uint64_t out_len, rz_status* status);
+RZ_API rz_status rz_batch_plan_launch(rz_batch_plan* plan);
+/* Waits for the plan's launches and returns the first device error since the
+ * last call (RZ_ERR_NAN, RZ_ERR_DEPTH, ...), then clears it. */
+RZ_API rz_status rz_batch_plan_status(rz_batch_plan* plan);
+/* Number of work items (bands) and binary64 flatness re-decisions so far. */
+RZ_API rz_status rz_batch_plan_info(rz_batch_plan* plan, uint64_t* n_items, uint64_t* fallbacks);
+RZ_API void rz_batch_plan_destroy(rz_batch_plan* plan);
+
+/* Counts the flattened lines of every segment exactly as
+ * PathFlattenIter (src/path.rs:734-796) emits them: counts[i] for segment i
+ * after arc expansion, then one entry per subpath for the closing line.
+ * n_counts receives the number of entries (may exceed cap). */
+RZ_API rz_status rz_flatten_counts(rz_ctx* ctx, const rz_path* path, const double tr[6], double flatness,
+                            uint32_t* counts, uint64_t cap, uint64_t* n_counts);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RASTERIZE_GB300_H */

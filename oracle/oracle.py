@@ -139,21 +139,27 @@ def arc_to_cubics(src, dst, radii, rot, large, sweep):
     return out[:n]
 
 
-def expand_path(path) -> OraclePath:
+def expand_path(path, with_map: bool = False):
     """Expands ARC segments into cubics like PathBuilder::arc_to; drops
-    subpaths that end up empty (PathBuilder::subpath_finish records none)."""
+    subpaths that end up empty (PathBuilder::subpath_finish records none).
+    With ``with_map`` also returns, per expanded segment, the input segment
+    index it came from, and per expanded subpath the input subpath index."""
     kind = np.asarray(path.kind)
     pts = np.asarray(path.pts).reshape(-1, 8)
     sub = np.asarray(path.subpath_off)
     if not np.any(kind == SEG_ARC):
-        return OraclePath(kind, pts, sub)
-    ok, op, off = [], [], [0]
+        op = OraclePath(kind, pts, sub)
+        if with_map:
+            return op, np.arange(len(kind)), np.arange(len(sub) - 1)
+        return op
+    ok, op, off, seg_map, sub_map = [], [], [0], [], []
     for s in range(len(sub) - 1):
         for i in range(int(sub[s]), int(sub[s + 1])):
             k = int(kind[i])
             if k != SEG_ARC:
                 ok.append(k)
                 op.append(pts[i])
+                seg_map.append(i)
                 continue
             p = pts[i]
             flags = int(p[7])
@@ -162,14 +168,20 @@ def expand_path(path) -> OraclePath:
                 if not (abs(p[0] - p[2]) < 2.220446049250313e-16 and abs(p[1] - p[3]) < 2.220446049250313e-16):
                     ok.append(SEG_LINE)
                     op.append(np.array([p[0], p[1], p[2], p[3], 0, 0, 0, 0], dtype=np.float64))
+                    seg_map.append(i)
             else:
                 for c in cub:
                     ok.append(SEG_CUBIC)
                     op.append(c)
+                    seg_map.append(i)
         if len(ok) > off[-1]:
             off.append(len(ok))
-    return OraclePath(np.asarray(ok, np.uint8), np.asarray(op, np.float64).reshape(-1, 8),
-                      np.asarray(off, np.uint32))
+            sub_map.append(s)
+    res = OraclePath(np.asarray(ok, np.uint8), np.asarray(op, np.float64).reshape(-1, 8),
+                     np.asarray(off, np.uint32))
+    if with_map:
+        return res, np.asarray(seg_map, dtype=np.int64), np.asarray(sub_map, dtype=np.int64)
+    return res
 
 
 def flatten(path, tr, flatness=0.05):
@@ -186,6 +198,19 @@ def flatten(path, tr, flatness=0.05):
     L.rzo_flatten(_ptr(op.kind), _ptr(op.pts), _ptr(op.sub_off), op.nsub, _ptr(_tr(tr)), flatness,
                   _ptr(out), n, _ptr(counts))
     return out[:n], counts
+
+
+def flatten_counts_per_input(path, tr, flatness=0.05):
+    """Line counts per input segment (arcs summed over their cubics), then one
+    entry per input subpath for its closing line (0 if the subpath vanished)."""
+    op, seg_map, sub_map = expand_path(path, with_map=True)
+    _, counts = flatten(op, tr, flatness)
+    n_in = len(np.asarray(path.kind))
+    nsub_in = len(np.asarray(path.subpath_off)) - 1
+    out = np.zeros(n_in + nsub_in, dtype=np.int64)
+    np.add.at(out, seg_map, counts[:len(seg_map)])
+    out[n_in + sub_map] = counts[len(seg_map):]
+    return out
 
 
 def mask(path, tr, fill_rule, width, height, flatness=0.05, img=None, shape=None):

@@ -1,0 +1,118 @@
+"""ctypes binding of the C ABI (include/rasterize_gb300.h).
+
+The library is built in-tree (``python -m rasterize_gb300.build``) and loaded
+from ``rasterize_gb300/_lib``.  There is no fallback: if the library is
+missing or no CUDA device is present, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "librasterize_gb300.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "rasterize_gb300.h")
+
+RZ_OK = 0
+STATUS_NAMES = {0: "RZ_OK", 1: "RZ_ERR_NAN", 2: "RZ_ERR_INVALID", 3: "RZ_ERR_CUDA", 4: "RZ_ERR_NO_DEVICE",
+                5: "RZ_ERR_DEPTH", 6: "RZ_ERR_ARC", 7: "RZ_ERR_CAPACITY", 8: "RZ_ERR_SPIN"}
+RZ_MEM_HOST, RZ_MEM_DEVICE = 0, 1
+
+
+class RasterizeError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s: %s" % (STATUS_NAMES.get(status, status), message))
+        self.status = status
+
+
+class NanError(RasterizeError):
+    """Raised where the reference panics: 'cannot flatten segment with NaN'."""
+
+
+class RzPath(ctypes.Structure):
+    _fields_ = [("seg_kind", ctypes.c_void_p), ("seg_pts", ctypes.c_void_p), ("subpath_off", ctypes.c_void_p),
+                ("closed", ctypes.c_void_p), ("n_segments", ctypes.c_uint32), ("n_subpaths", ctypes.c_uint32)]
+
+
+class RzShape(ctypes.Structure):
+    _fields_ = [("start", ctypes.c_uint64), ("width", ctypes.c_uint64), ("height", ctypes.c_uint64),
+                ("row_stride", ctypes.c_uint64), ("col_stride", ctypes.c_uint64)]
+
+
+class RzPixel(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_uint64), ("y", ctypes.c_uint64), ("alpha", ctypes.c_double)]
+
+
+class RzMaskDesc(ctypes.Structure):
+    _fields_ = [("offset", ctypes.c_uint64), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("row_stride", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class RzPathBatch(ctypes.Structure):
+    _fields_ = [("n_paths", ctypes.c_uint32), ("n_segments", ctypes.c_uint32), ("n_subpaths", ctypes.c_uint32),
+                ("memory", ctypes.c_int32), ("seg_kind", ctypes.c_void_p), ("seg_pts", ctypes.c_void_p),
+                ("subpath_off", ctypes.c_void_p), ("path_subpath_off", ctypes.c_void_p),
+                ("transforms", ctypes.c_void_p), ("fill_rules", ctypes.c_void_p), ("masks", ctypes.c_void_p)]
+
+
+_lock = threading.Lock()
+_lib = None
+
+P = ctypes.c_void_p
+_SIGNATURES = {
+    "rz_version": (ctypes.c_char_p, []),
+    "rz_create": (P, [ctypes.c_int, ctypes.POINTER(ctypes.c_int32)]),
+    "rz_destroy": (None, [P]),
+    "rz_last_error": (ctypes.c_char_p, [P]),
+    "rz_set_stream": (ctypes.c_int32, [P, P]),
+    "rz_get_stream": (P, [P]),
+    "rz_synchronize": (ctypes.c_int32, [P]),
+    "rz_mask": (ctypes.c_int32, [P, ctypes.POINTER(RzPath), P, ctypes.c_int32, ctypes.c_double, P, RzShape]),
+    "rz_mask_iter": (ctypes.c_int32, [P, ctypes.POINTER(RzPath), P, ctypes.c_int32, ctypes.c_double,
+                                      ctypes.c_uint64, ctypes.c_uint64, P, ctypes.c_uint64,
+                                      ctypes.POINTER(ctypes.c_uint64)]),
+    "rz_mask_batch": (ctypes.c_int32, [P, ctypes.POINTER(RzPathBatch), ctypes.c_double, P, ctypes.c_uint64]),
+    "rz_mask_batch_per_path": (ctypes.c_int32, [P, ctypes.POINTER(RzPathBatch), ctypes.c_double, P,
+                                                ctypes.c_uint64]),
+    "rz_flatten_counts": (ctypes.c_int32, [P, ctypes.POINTER(RzPath), P, ctypes.c_double, P, ctypes.c_uint64,
+                                           ctypes.POINTER(ctypes.c_uint64)]),
+    "rz_batch_plan_create": (P, [P, ctypes.POINTER(RzPathBatch), ctypes.c_double, P, ctypes.c_uint64,
+                                 ctypes.POINTER(ctypes.c_int32)]),
+    "rz_batch_plan_launch": (ctypes.c_int32, [P]),
+    "rz_batch_plan_status": (ctypes.c_int32, [P]),
+    "rz_batch_plan_info": (ctypes.c_int32, [P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
+    "rz_batch_plan_destroy": (None, [P]),
+}
+
+
+def header_symbols():
+    """Function names declared in include/rasterize_gb300.h."""
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(rz_[a-z0-9_]+)\s*\(", text)) - {"rz_ctx"})
+
+
+def load(path: str = LIB_PATH):
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(path):
+                raise RasterizeError(4, "CUDA library not built: %s (run python -m rasterize_gb300.build)" % path)
+            L = ctypes.CDLL(path)
+            for name, (res, args) in _SIGNATURES.items():
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = L
+    return _lib
+
+
+def check(lib, ctx, status):
+    if status == RZ_OK:
+        return
+    msg = lib.rz_last_error(ctx)
+    msg = msg.decode() if msg else ""
+    if status == 1:
+        raise NanError(status, msg)
+    raise RasterizeError(status, msg)

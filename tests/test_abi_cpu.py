@@ -1,0 +1,90 @@
+"""CPU-side checks: the C-ABI library builds, loads and exports every symbol
+of include/rasterize_gb300.h; host-side logic (path model, SVG parser, batch
+packing) behaves like the reference.  No compute call needs a GPU here."""
+import ctypes
+import math
+
+import numpy as np
+import pytest
+
+from rasterize_gb300 import FillRule, MaskBatch, Path, PathBuilder, Transform, _ffi, parse_svg_path
+from rasterize_gb300 import workloads as W
+
+
+def test_library_exports_every_header_symbol():
+    lib = _ffi.load()
+    names = _ffi.header_symbols()
+    assert len(names) >= 10
+    for name in names:
+        assert hasattr(lib, name), name
+    assert lib.rz_version().startswith(b"rasterize_gb300")
+
+
+def test_create_without_gpu_reports_no_device():
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    lib = _ffi.load()
+    st = ctypes.c_int32(-1)
+    assert not lib.rz_create(0, ctypes.byref(st))
+    assert st.value == 4  # RZ_ERR_NO_DEVICE
+
+
+def test_null_context_is_invalid():
+    lib = _ffi.load()
+    assert lib.rz_synchronize(None) == 2
+    assert lib.rz_last_error(None) == b"no context"
+
+
+def test_builder_matches_reference_semantics():
+    b = PathBuilder().move_to((1, 1)).line_to((1, 1)).line_to((2, 1)).line_to((2, 2)).close()
+    b.line_to((5, 5))  # after close the position is the subpath start (src/path.rs:857-866)
+    p = b.build()
+    assert p.n_subpaths == 2
+    assert list(p.subpath_off) == [0, 2, 3]
+    assert list(p.closed) == [1, 0]
+    assert tuple(p.pts[2, :2]) == (1.0, 1.0)
+
+
+def test_svg_parser_relative_and_smooth():
+    cmds = list(parse_svg_path("m1,1 l2,0 s1,1 2,2 t3,3 z M0 0 1.5.5"))
+    ops = [c[0] for c in cmds]
+    assert ops == ["M", "L", "C", "Q", "Z", "M", "L"]
+    assert cmds[1][1] == (3.0, 1.0)
+    assert cmds[2][1] == (3.0, 1.0)  # smooth cubic after a line reflects nothing
+    assert cmds[-1][1] == (1.5, 0.5)
+    p = Path.parse("M1,1 v2 h1 v-2 Z")
+    assert p.n_segments == 3 and p.n_subpaths == 1
+
+
+def test_squirrel_parses():
+    import json
+    import os
+    fx = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_fixtures.json")))
+    p = Path.parse(fx["squirrel"])
+    assert p.n_subpaths == 2 and p.n_segments == 26
+
+
+def test_batch_packing():
+    paths, sizes, rules = W.glyph_batch(seed=1, n=50)
+    b = MaskBatch(paths, sizes, fill_rules=rules)
+    assert b.n_paths == 50
+    assert b.sub_off[-1] == b.n_segments
+    assert list(b.path_sub) == list(range(51))
+    for i in range(50):
+        d = b.descs[i]
+        assert d.row_stride % 4 == 0 and d.offset % 4 == 0 and d.row_stride >= d.width
+    last = b.descs[49]
+    assert last.offset + last.row_stride * last.height <= b.out_len
+
+
+def test_workload_shapes():
+    paths, sizes, _ = W.glyph_batch(seed=2, n=2000)
+    segs = np.array([p.n_segments for p in paths])
+    sides = np.array([w for w, _ in sizes])
+    assert segs.min() >= 10 and segs.max() <= 400
+    assert sides.min() >= 16 and sides.max() <= 256
+    path, rule, (w, h) = W.large_path(seed=1, n_segments=2000)
+    kinds = np.bincount(path.kind, minlength=4) / path.n_segments
+    assert abs(kinds[0] - 0.4) < 0.05 and abs(kinds[3] - 0.1) < 0.03
+    assert rule == FillRule.EvenOdd and (w, h) == (4096, 4096)
