@@ -230,7 +230,8 @@ def main():
 
     paths, sizes, rules, batch = make_workload(args.glyphs)
     R = GpuRasterizer(device=local)
-    stream = torch.cuda.current_stream(dev)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     R.ctx.set_stream(stream.cuda_stream)
 
     # ---- device-resident inputs / output

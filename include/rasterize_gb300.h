@@ -120,7 +120,8 @@ RZ_API rz_ctx* rz_create(int device, rz_status* status);
 RZ_API void rz_destroy(rz_ctx* ctx);
 /* Text of the last error on this context ("" when none). */
 RZ_API const char* rz_last_error(const rz_ctx* ctx);
-/* Runs the context's work on `stream` (a cudaStream_t) instead of its own. */
+/* Runs the context's work on `stream` (a cudaStream_t; NULL = the legacy
+ * default stream) instead of the context's own stream. */
 RZ_API rz_status rz_set_stream(rz_ctx* ctx, void* stream);
 RZ_API void* rz_get_stream(const rz_ctx* ctx);
 RZ_API rz_status rz_synchronize(rz_ctx* ctx);

@@ -22,7 +22,9 @@ LIB = os.path.join(LIB_DIR, "librasterize_gb300.so")
 OBJ_DIR = os.path.join(HERE, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code keeps binary64 operation order (no FMA contraction), like the reference
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+              "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"] + ARCH
 
 
@@ -52,7 +54,7 @@ def up_to_date() -> bool:
     if not os.path.exists(LIB):
         return False
     t = os.path.getmtime(LIB)
-    deps = sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.hpp"))
+    deps = sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.inc"))
     deps.append(os.path.join(HERE, "..", "include", "rasterize_gb300.h"))
     deps.append(os.path.abspath(__file__))
     return all(os.path.getmtime(d) <= t for d in deps if os.path.exists(d))

@@ -16,21 +16,21 @@
 #include <vector>
 
 #include "../../include/rasterize_gb300.h"
+#include "rz_host_arc.cpp.inc"
 #include "rz_kernels.cuh"
 
 namespace rz {
 cudaError_t init_kernels();
 cudaError_t launch_mask_bands(const BatchDev& b, const WorkItem* items, int n_items, int32_t* queue, int grid,
-                              int smem_bytes, cudaStream_t stream);
-int mask_bands_occupancy(int smem_bytes);
+                              cudaStream_t stream);
+int mask_bands_occupancy();
+int band_floats();
 cudaError_t launch_flatten_counts(const BatchDev& b, uint32_t n_segments, uint32_t n_subpaths, uint32_t* counts,
                                   cudaStream_t stream);
 }  // namespace rz
 
 namespace {
 
-constexpr int kBandSmemBytes = 64 * 1024;  // shared accumulation band per CTA
-constexpr int kBandFloats = kBandSmemBytes / 4;
 
 struct DevBuf {
     void* p = nullptr;
@@ -86,6 +86,11 @@ struct rz_ctx {
     // device buffers
     DevBuf d_kind, d_pts, d_sub, d_psub, d_tr, d_rule, d_masks, d_items, d_out, d_ctrl, d_counts;
     HostBuf h_stage, h_out;
+    // host-side arc expansion scratch
+    std::vector<uint8_t> x_kind;
+    std::vector<double> x_pts;
+    std::vector<uint32_t> x_sub, x_psub, x_segmap, x_submap;
+    bool expanded = false;  // the last stage_host expanded arcs
 };
 
 namespace {
@@ -121,7 +126,7 @@ bool valid_flatness(double f) { return std::isfinite(f) && 16.0 * f * f > 0.0; }
 // Band height for a mask: as many rows as fit in the shared band.
 int band_rows(int clip_width, int height) {
     const int stride = rz::band_stride(clip_width);
-    int rows = std::max(1, kBandFloats / stride);
+    int rows = std::max(1, rz::band_floats() / stride);
     return std::min(rows, std::max(1, height));
 }
 
@@ -204,7 +209,7 @@ const char* rz_last_error(const rz_ctx* c) { return c ? c->last_error.c_str() : 
 
 rz_status rz_set_stream(rz_ctx* c, void* stream) {
     if (!c) return RZ_ERR_INVALID;
-    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    c->stream = (cudaStream_t)stream;  // NULL selects the legacy default stream
     return RZ_OK;
 }
 
@@ -234,6 +239,21 @@ struct Staged {
 rz_status stage_host(rz_ctx* ctx, const uint8_t* kind, const double* pts, uint32_t n_seg, const uint32_t* sub_off,
                      uint32_t n_sub, const uint32_t* path_sub, uint32_t n_paths, const double* tr,
                      const uint8_t* rule, rz::BatchDev& b) {
+    // arcs are converted to cubics on the host, as PathBuilder::arc_to does
+    bool has_arc = false;
+    for (uint32_t i = 0; i < n_seg && !has_arc; ++i) has_arc = kind[i] == RZ_SEG_ARC;
+    ctx->expanded = has_arc;
+    if (has_arc) {
+        if (!rzhost::expand_batch(kind, pts, sub_off, path_sub, n_paths, ctx->x_kind, ctx->x_pts, ctx->x_sub,
+                                  ctx->x_psub, ctx->x_segmap, ctx->x_submap))
+            return fail(ctx, RZ_ERR_ARC, "an arc has no finite cubic count");
+        kind = ctx->x_kind.data();
+        pts = ctx->x_pts.data();
+        n_seg = (uint32_t)ctx->x_kind.size();
+        sub_off = ctx->x_sub.data();
+        n_sub = (uint32_t)ctx->x_sub.size() - 1;
+        path_sub = ctx->x_psub.data();
+    }
     const size_t sz_kind = n_seg, sz_pts = (size_t)n_seg * 64, sz_sub = ((size_t)n_sub + 1) * 4,
                  sz_psub = ((size_t)n_paths + 1) * 4, sz_tr = tr ? (size_t)n_paths * 48 : 0,
                  sz_rule = rule ? n_paths : 0;
@@ -322,15 +342,15 @@ rz_status run_bands(rz_ctx* ctx, const rz::BatchDev& b, const Items& items, bool
     if (!per_path) {
         const int n = (int)items.items.size();
         if (n == 0) return RZ_OK;
-        const int occ = std::max(1, rz::mask_bands_occupancy(kBandSmemBytes));
+        const int occ = std::max(1, rz::mask_bands_occupancy());
         const int grid = std::min(n, ctx->num_sms * occ);
         RZ_CUDA(cudaMemsetAsync(queue, 0, 4, ctx->stream));
-        RZ_CUDA(rz::launch_mask_bands(b, d_items, n, queue, grid, kBandSmemBytes, ctx->stream));
+        RZ_CUDA(rz::launch_mask_bands(b, d_items, n, queue, grid, ctx->stream));
     } else {
         for (size_t p = 0; p + 1 < items.path_first.size(); ++p) {
             const int f = items.path_first[p], n = items.path_first[p + 1] - f;
             if (n == 0) continue;
-            RZ_CUDA(rz::launch_mask_bands(b, d_items + f, n, nullptr, n, kBandSmemBytes, ctx->stream));
+            RZ_CUDA(rz::launch_mask_bands(b, d_items + f, n, nullptr, n, ctx->stream));
         }
     }
     return RZ_OK;
@@ -369,7 +389,7 @@ rz_status render_single(rz_ctx* ctx, const rz_path* path, const double tr[6], in
     if (st) return st;
     if (!valid_flatness(flatness)) return fail(ctx, RZ_ERR_INVALID, "flatness must be > 0 and finite");
     if (rule != RZ_FILL_NONZERO && rule != RZ_FILL_EVENODD) return fail(ctx, RZ_ERR_INVALID, "bad fill rule");
-    if (width > 16383 || height > 65535) return fail(ctx, RZ_ERR_INVALID, "image too large (max 16383 x 65535)");
+    if (width > 16383 || height > 16383) return fail(ctx, RZ_ERR_INVALID, "image too large (max 16383 x 16383)");
     RZ_CUDA(cudaSetDevice(ctx->device));
     rz::BatchDev b{};
     const uint32_t path_sub[2] = {0, path->n_subpaths};
@@ -461,7 +481,7 @@ static rz_status mask_batch_impl(rz_ctx* ctx, const rz_path_batch* batch, double
     std::vector<rz::MaskDev> masks(P);
     for (uint32_t p = 0; p < P; ++p) {
         const rz_mask_desc& d = batch->masks[p];
-        if (d.width > 16383 || d.height > 65535 || (d.height > 0 && d.row_stride < d.width))
+        if (d.width > 16383 || d.height > 16383 || (d.height > 0 && d.row_stride < d.width))
             return fail(ctx, RZ_ERR_INVALID, "bad mask descriptor");
         if (d.width && d.height && d.offset + (uint64_t)(d.height - 1) * d.row_stride + d.width > out_len)
             return fail(ctx, RZ_ERR_INVALID, "mask exceeds output buffer");
@@ -544,12 +564,22 @@ rz_status rz_flatten_counts(rz_ctx* ctx, const rz_path* path, const double tr[6]
     set_thresholds(b, flatness);
     const uint64_t n = (uint64_t)path->n_segments + path->n_subpaths;
     *n_counts = n;
-    RZ_CUDA(ctx->d_counts.ensure(n * 4 + 4));
-    RZ_CUDA(rz::launch_flatten_counts(b, path->n_segments, path->n_subpaths, (uint32_t*)ctx->d_counts.p,
-                                      ctx->stream));
-    if (counts && cap)
-        RZ_CUDA(cudaMemcpyAsync(counts, ctx->d_counts.p, std::min(cap, n) * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    return read_error(ctx);
+    const uint64_t ne = (uint64_t)b.n_segments + b.n_subpaths;  // after host arc expansion
+    RZ_CUDA(ctx->d_counts.ensure(ne * 4 + 4));
+    RZ_CUDA(rz::launch_flatten_counts(b, b.n_segments, b.n_subpaths, (uint32_t*)ctx->d_counts.p, ctx->stream));
+    std::vector<uint32_t> dev_counts(ne);
+    if (ne) RZ_CUDA(cudaMemcpyAsync(dev_counts.data(), ctx->d_counts.p, ne * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    st = read_error(ctx);
+    if (st) return st;
+    std::vector<uint32_t> agg(n, 0);
+    if (ctx->expanded) {
+        for (uint32_t j = 0; j < b.n_segments; ++j) agg[ctx->x_segmap[j]] += dev_counts[j];
+        for (uint32_t t = 0; t < b.n_subpaths; ++t) agg[path->n_segments + ctx->x_submap[t]] = dev_counts[b.n_segments + t];
+    } else {
+        agg = dev_counts;
+    }
+    if (counts) std::memcpy(counts, agg.data(), std::min(cap, n) * 4);
+    return RZ_OK;
 }
 
 }  // extern "C"
@@ -586,7 +616,7 @@ rz_batch_plan* rz_batch_plan_create(rz_ctx* ctx, const rz_path_batch* batch, dou
     std::vector<rz::MaskDev> masks(P);
     for (uint32_t p = 0; p < P; ++p) {
         const rz_mask_desc& d = batch->masks[p];
-        if (d.width > 16383 || d.height > 65535 || (d.height > 0 && d.row_stride < d.width))
+        if (d.width > 16383 || d.height > 16383 || (d.height > 0 && d.row_stride < d.width))
             return bail(fail(ctx, RZ_ERR_INVALID, "bad mask descriptor"));
         if (d.width && d.height && d.offset + (uint64_t)(d.height - 1) * d.row_stride + d.width > out_len)
             return bail(fail(ctx, RZ_ERR_INVALID, "mask exceeds output buffer"));
@@ -631,7 +661,7 @@ rz_batch_plan* rz_batch_plan_create(rz_ctx* ctx, const rz_path_batch* batch, dou
     b.counters = ctrl + 4;
     set_thresholds(b, flatness);
     const int n = (int)plan->items.items.size();
-    const int occ = std::max(1, rz::mask_bands_occupancy(kBandSmemBytes));
+    const int occ = std::max(1, rz::mask_bands_occupancy());
     plan->grid = std::max(1, std::min(n, ctx->num_sms * occ));
     // capture: reset the queue head, one persistent launch
     int32_t* queue = ctrl + 8;
@@ -639,7 +669,7 @@ rz_batch_plan* rz_batch_plan_create(rz_ctx* ctx, const rz_path_batch* batch, dou
     if (e == cudaSuccess) {
         cudaMemsetAsync(queue, 0, 4, plan->capture_stream);
         if (n > 0)
-            rz::launch_mask_bands(b, (const rz::WorkItem*)plan->d_items.p, n, queue, plan->grid, kBandSmemBytes,
+            rz::launch_mask_bands(b, (const rz::WorkItem*)plan->d_items.p, n, queue, plan->grid,
                                   plan->capture_stream);
         e = cudaStreamEndCapture(plan->capture_stream, &plan->graph);
     }

@@ -97,15 +97,92 @@ __device__ __noinline__ double flatness_chain64(Seg64 s, int d, uint32_t k) {
     return flatness64(s);
 }
 
+struct FlatCoef {
+    float a2x, a2y, a3x, a3y;
+    float mag;  // max |coordinate| of the control points (f64 error term)
+};
+
+// ---------------------------------------------------------------------------
+// Fixed point 16.16 from binary64 with integer instructions only (GB300's
+// FP64 pipe is ~1/64 of FP32).  Deterministic round-half-even of x * 2^16;
+// returns false for |x| >= 16384 px, infinities and NaN.
+// ---------------------------------------------------------------------------
+constexpr double FIX_RANGE = 16384.0;
+
+__device__ __forceinline__ bool d2fix(double x, int32_t& out) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((bits >> 52) & 0x7ffull);
+    if (e == 0) {  // zero or subnormal: below the fixed-point resolution
+        out = 0;
+        return true;
+    }
+    if (e >= 1023 + 14) return false;  // |x| >= 16384, inf, NaN
+    const unsigned long long mant = (bits & 0xfffffffffffffull) | (1ull << 52);
+    const int sh = 1059 - e;  // value * 2^16 = mant * 2^(e - 1059)
+    unsigned long long q;
+    if (sh >= 64) {
+        q = 0;
+    } else {
+        q = mant >> sh;
+        const unsigned long long rem = mant - (q << sh);
+        const unsigned long long half = 1ull << (sh - 1);
+        if (rem > half || (rem == half && (q & 1ull))) ++q;
+    }
+    const int32_t v = (int32_t)q;
+    out = (bits >> 63) ? -v : v;
+    return true;
+}
+
+__device__ __forceinline__ bool is_nan_bits(double x) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    return ((bits >> 52) & 0x7ffull) == 0x7ffull && (bits & 0xfffffffffffffull) != 0ull;
+}
+
+constexpr float FIX_ONE_INV = 1.0f / 65536.0f;
+
+// A reference segment in fixed point (after the path transform).
+struct FixSeg {
+    int kind;
+    int32_t x[4], y[4];
+};
+
+// Flatness coefficients from fixed-point control points, in px, and the
+// bound of their error against the binary64 values (quantisation 2^-17 px per
+// coordinate plus FP32 rounding).
+__device__ inline FlatCoef flat_coef_fix(const FixSeg& s, float& qerr) {
+    FlatCoef c;
+    int32_t mx = 0;
+    #pragma unroll
+    for (int i = 0; i < 4; ++i) mx = max(mx, max(abs(s.x[i]), abs(s.y[i])));  // unused points are 0
+    c.mag = (float)mx * FIX_ONE_INV;
+    const float dx1 = (float)(s.x[1] - s.x[0]) * FIX_ONE_INV, dy1 = (float)(s.y[1] - s.y[0]) * FIX_ONE_INV;
+    if (s.kind == SEG_CUBIC) {
+        const float dx2 = (float)(s.x[2] - s.x[1]) * FIX_ONE_INV, dy2 = (float)(s.y[2] - s.y[1]) * FIX_ONE_INV;
+        const float dx3 = (float)(s.x[3] - s.x[2]) * FIX_ONE_INV, dy3 = (float)(s.y[3] - s.y[2]) * FIX_ONE_INV;
+        c.a2x = 3.f * (dx2 - dx1);
+        c.a2y = 3.f * (dy2 - dy1);
+        c.a3x = (dx1 - 2.f * dx2) + dx3;
+        c.a3y = (dy1 - 2.f * dy2) + dy3;
+        qerr = ldexpf(fmaxf(fabsf(dx1) + fabsf(dx2) + fabsf(dx3), fabsf(dy1) + fabsf(dy2) + fabsf(dy3)), -19) +
+               12.f * ldexpf(1.f, -17);
+    } else if (s.kind == SEG_QUAD) {
+        const float dx2 = (float)(s.x[2] - s.x[1]) * FIX_ONE_INV, dy2 = (float)(s.y[2] - s.y[1]) * FIX_ONE_INV;
+        c.a2x = dx2 - dx1;
+        c.a2y = dy2 - dy1;
+        c.a3x = c.a3y = 0.f;
+        qerr = ldexpf(fmaxf(fabsf(dx1) + fabsf(dx2), fabsf(dy1) + fabsf(dy2)), -21) + 4.f * ldexpf(1.f, -17);
+    } else {
+        c.a2x = c.a2y = c.a3x = c.a3y = 0.f;
+        qerr = 0.f;
+    }
+    return c;
+}
+
 // Per-segment data for exact FP32 flatness decisions.
 //   cubic: sub-curve over [kh, (k+1)h] has u = -h^2 (a2 + a3 h(3k+1)),
 //          v = -h^2 (a2 + a3 h(3k+2)) with a2 = 3(P0 - 2P1 + P2),
 //          a3 = P3 - P0 + 3(P1 - P2); flatness = h^4 G.
 //   quad:  2c1 - c0 - c2 = -h^2 (P0 - 2P1 + P2); flatness = h^4 |a2|^2.
-struct FlatCoef {
-    float a2x, a2y, a3x, a3y;
-    float mag;  // max |coordinate| of the control points (f64 error term)
-};
 
 __device__ inline FlatCoef flat_coef(const Seg64& s) {
     FlatCoef c;
@@ -128,37 +205,47 @@ __device__ inline FlatCoef flat_coef(const Seg64& s) {
     return c;
 }
 
-// Decides `flatness(node) < thr` exactly as the reference.  thr64 = 16 f f.
-// Returns 1 = leaf, 0 = split; `fallbacks` counts binary64 replays.
-__device__ inline int node_is_leaf(const Seg64& root, const FlatCoef& c, int d, uint32_t k, double thr64,
-                                   float thr32, int& fallbacks) {
-    if (root.kind == SEG_LINE) return thr64 > 0.0;  // Line::flatness == 0 (src/curve.rs:233-235)
+// FP32 decision of `flatness(node) < thr` with a rigorous error bound:
+// 1 = leaf, 0 = split, -1 = too close to call (re-decide in binary64).
+// qerr bounds |a2 - a2_true| and |a3 - a3_true| (px) when the coefficients
+// come from rounded inputs.
+__device__ inline int decide_fp32(int kind, const FlatCoef& c, int d, uint32_t k, float thr32, float qerr) {
     const float h = ldexpf(1.0f, -d);
     const float td = ldexpf(thr32, 4 * d);  // thr * 16^d, exact power-of-two scaling
+    const float scale = ldexpf(1.0f, 2 * d);  // chain error grows like 4^d in w units
     float G, E;
-    if (root.kind == SEG_CUBIC) {
+    if (kind == SEG_CUBIC) {
         const float tu = h * (float)(3u * k + 1u);
         const float tv = h * (float)(3u * k + 2u);
         const float wux = fmaf(c.a3x, tu, c.a2x), wvx = fmaf(c.a3x, tv, c.a2x);
         const float wuy = fmaf(c.a3y, tu, c.a2y), wvy = fmaf(c.a3y, tv, c.a2y);
         const float gx = fmaxf(wux * wux, wvx * wvx), gy = fmaxf(wuy * wuy, wvy * wvy);
         G = gx + gy;
-        const float scale = ldexpf(1.0f, 2 * d);  // chain error grows like 4^d in G units
-        const float bx = ldexpf(fabsf(c.a2x) + fabsf(c.a3x) * tv, -21) + ldexpf(c.mag * scale, -40);
-        const float by = ldexpf(fabsf(c.a2y) + fabsf(c.a3y) * tv, -21) + ldexpf(c.mag * scale, -40);
+        const float q = qerr * (1.f + tv);
+        const float bx = ldexpf(fabsf(c.a2x) + fabsf(c.a3x) * tv, -21) + ldexpf(c.mag * scale, -40) + q;
+        const float by = ldexpf(fabsf(c.a2y) + fabsf(c.a3y) * tv, -21) + ldexpf(c.mag * scale, -40) + q;
         const float wx = sqrtf(gx), wy = sqrtf(gy);
         E = (2.f * wx + bx) * bx + (2.f * wy + by) * by + ldexpf(G, -19);
     } else {
         G = c.a2x * c.a2x + c.a2y * c.a2y;
-        const float scale = ldexpf(1.0f, 2 * d);
-        const float bx = ldexpf(fabsf(c.a2x), -21) + ldexpf(c.mag * scale, -40);
-        const float by = ldexpf(fabsf(c.a2y), -21) + ldexpf(c.mag * scale, -40);
+        const float bx = ldexpf(fabsf(c.a2x), -21) + ldexpf(c.mag * scale, -40) + qerr;
+        const float by = ldexpf(fabsf(c.a2y), -21) + ldexpf(c.mag * scale, -40) + qerr;
         E = (2.f * fabsf(c.a2x) + bx) * bx + (2.f * fabsf(c.a2y) + by) * by + ldexpf(G, -19);
     }
     if (isfinite(G) && isfinite(E) && isfinite(td)) {
         if (G + E < td) return 1;
         if (G - E >= td) return 0;
     }
+    return -1;
+}
+
+// Decides `flatness(node) < thr` exactly as the reference.  thr64 = 16 f f.
+// Returns 1 = leaf, 0 = split; `fallbacks` counts binary64 replays.
+__device__ inline int node_is_leaf(const Seg64& root, const FlatCoef& c, int d, uint32_t k, double thr64,
+                                   float thr32, int& fallbacks, float qerr = 0.f) {
+    if (root.kind == SEG_LINE) return thr64 > 0.0;  // Line::flatness == 0 (src/curve.rs:233-235)
+    const int r = decide_fp32(root.kind, c, d, k, thr32, qerr);
+    if (r >= 0) return r;
     ++fallbacks;
     return flatness_chain64(root, d, k) < thr64 ? 1 : 0;
 }
@@ -203,8 +290,9 @@ __device__ inline VertexCoef vertex_coef(const Seg64& s) {
         v.c1x = s.x[1] - s.x[0]; v.c1y = s.y[1] - s.y[0];
         v.c2x = v.c2y = v.c3x = v.c3y = 0.0;
     }
-    double ext = fabs(v.c1x) + fabs(v.c2x) + fabs(v.c3x) + fabs(v.c1y) + fabs(v.c2y) + fabs(v.c3y);
-    v.small = ext < 8.0;
+    // FP32 Horner error is about 3 * 2^-24 * ext: ext < 48 keeps vertices within ~1e-5 px
+    const double ext = fmax(fabs(v.c1x) + fabs(v.c2x) + fabs(v.c3x), fabs(v.c1y) + fabs(v.c2y) + fabs(v.c3y));
+    v.small = ext < 48.0;
     v.f1x = (float)v.c1x; v.f1y = (float)v.c1y;
     v.f2x = (float)v.c2x; v.f2y = (float)v.c2y;
     v.f3x = (float)v.c3x; v.f3y = (float)v.c3y;

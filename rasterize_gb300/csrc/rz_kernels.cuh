@@ -37,7 +37,9 @@ struct WorkItem {
     uint16_t rows;
 };
 
-// Band geometry shared by host and device: row stride in shared memory.
-__host__ __device__ inline int band_stride(int clip_width) { return ((clip_width + 3) + 3) & ~3; }
+// Band geometry shared by host and device: row stride in shared memory.  At
+// least clip_width + 3 columns (two spill columns of the reference's writes
+// past `width`), rounded up to whole 16-pixel scan chunks.
+__host__ __device__ inline int band_stride(int clip_width) { return ((clip_width + 3) + 15) & ~15; }
 
 }  // namespace rz

@@ -10,7 +10,9 @@ the CUDA library or a GPU every call raises ``RasterizeError``.
 from __future__ import annotations
 
 import abc
+import atexit
 import ctypes
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -42,6 +44,24 @@ class Rasterizer(abc.ABC):
     def mask_iter(self, path: Path, tr: Transform, size: Size, fill_rule: FillRule): ...
 
 
+# Plans and contexts are released before interpreter shutdown tears down the
+# CUDA runtime: plans first (they use their context's stream), then contexts.
+_live_plans = weakref.WeakSet()
+_live_contexts = weakref.WeakSet()
+_finalized = [False]
+
+
+def _release_all():
+    for p in list(_live_plans):
+        p.close()
+    for c in list(_live_contexts):
+        c.close()
+    _finalized[0] = True
+
+
+atexit.register(_release_all)
+
+
 def _path_struct(path: Path):
     keep = (path.kind, path.pts, path.subpath_off, path.closed)
     s = _ffi.RzPath(path.kind.ctypes.data, path.pts.ctypes.data, path.subpath_off.ctypes.data,
@@ -64,6 +84,7 @@ class Context:
         if not self.ptr:
             raise _ffi.RasterizeError(st.value or 4, "cannot create a context on CUDA device %d" % device)
         self.device = device
+        _live_contexts.add(self)
 
     def check(self, status):
         _ffi.check(self.lib, self.ptr, status)
@@ -73,15 +94,19 @@ class Context:
         return self.lib.rz_get_stream(self.ptr) or 0
 
     def set_stream(self, stream_ptr: int):
+        """Runs on the given cudaStream_t (0 = the legacy default stream)."""
         self.check(self.lib.rz_set_stream(self.ptr, stream_ptr or None))
 
     def synchronize(self):
         self.check(self.lib.rz_synchronize(self.ptr))
 
     def close(self):
-        if getattr(self, "ptr", None):
+        if getattr(self, "ptr", None) and not _finalized[0]:
+            for p in list(_live_plans):
+                if p.ctx is self:
+                    p.close()
             self.lib.rz_destroy(self.ptr)
-            self.ptr = None
+        self.ptr = None
 
     def __del__(self):
         try:
@@ -183,6 +208,7 @@ class BatchPlan:
                                                 batch.out_len, ctypes.byref(st))
         if not self.ptr:
             ctx.check(st.value or 2)
+        _live_plans.add(self)
 
     def launch(self):
         self.ctx.check(self.ctx.lib.rz_batch_plan_launch(self.ptr))
@@ -196,9 +222,9 @@ class BatchPlan:
         return int(n.value), int(f.value)
 
     def close(self):
-        if getattr(self, "ptr", None):
+        if getattr(self, "ptr", None) and not _finalized[0]:
             self.ctx.lib.rz_batch_plan_destroy(self.ptr)
-            self.ptr = None
+        self.ptr = None
 
     def __del__(self):
         try:

@@ -192,7 +192,8 @@ def test_batch_matches_oracle_and_per_path(R):
         w, h = sizes[i]
         ref = O.mask(paths[i], Transform.identity(), rules[i], w, h)
         assert_close(batch.mask(out, i), ref)
-    assert np.abs(out - out_pp).max() <= 1e-6
+    # shared-memory float atomics add in a different order: equal to rounding
+    assert np.abs(out - out_pp).max() <= 1e-5
 
 
 def test_batch_with_transforms_and_rules(R):
