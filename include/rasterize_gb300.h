@@ -173,6 +173,21 @@ RZ_API rz_status rz_batch_plan_status(rz_batch_plan* plan);
 RZ_API rz_status rz_batch_plan_info(rz_batch_plan* plan, uint64_t* n_items, uint64_t* fallbacks);
 RZ_API void rz_batch_plan_destroy(rz_batch_plan* plan);
 
+/* Allocation-free variant of rz_mask_batch (no counterpart in the reference).
+ * For callers that cannot allocate device memory while rendering: code that
+ * runs inside another framework's memory pool, real-time loops, hosts whose
+ * device memory is reserved up front.  Renders a device-memory batch
+ * (batch->memory == RZ_MEM_DEVICE) into the device buffer `out` on `stream`
+ * (NULL = legacy default stream) of the current device, with no cudaMalloc,
+ * no pinned or heap allocation and no rz_ctx.  The kernel's scratch is one
+ * static 896 KiB device array per GPU (held until the process exits): at most
+ * 16384 paths and 65536 row bands per call, larger batches return
+ * RZ_ERR_CAPACITY.  The first call on a device does a one-time set-up; make
+ * it before any stream capture.  Calls share the array and must not overlap
+ * on the GPU.  Returns after the work has finished (it reads the error word). */
+RZ_API rz_status rz_mask_batch_noalloc(const rz_path_batch* batch, double flatness, float* out, uint64_t out_len,
+                                       void* stream);
+
 /* Counts the flattened lines of every segment exactly as
  * PathFlattenIter (src/path.rs:734-796) emits them: counts[i] for segment i
  * after arc expansion, then one entry per subpath for the closing line.

@@ -84,6 +84,7 @@ _SIGNATURES = {
     "rz_batch_plan_status": (ctypes.c_int32, [P]),
     "rz_batch_plan_info": (ctypes.c_int32, [P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
     "rz_batch_plan_destroy": (None, [P]),
+    "rz_mask_batch_noalloc": (ctypes.c_int32, [ctypes.POINTER(RzPathBatch), ctypes.c_double, P, ctypes.c_uint64, P]),
 }
 
 

@@ -1,0 +1,70 @@
+"""The allocation-free batch entry point, through the C ABI.
+
+rz_mask_batch_noalloc serves callers that cannot allocate device memory
+while rendering (a host framework's memory pool, real-time loops, device
+memory reserved up front): its scratch is a static device array inside the
+library.  This test checks it against rz_mask_batch on the same device-memory
+batch, on two calls in a row (the second call reuses the array left by the
+first), within the tolerance of the other GPU tests.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5  # shared-memory float atomics may add in another order; both are within 1e-4 of the oracle
+
+
+def test_noalloc_matches_mask_batch():
+    torch = pytest.importorskip("torch")
+    from rasterize_gb300 import GpuRasterizer, MaskBatch, _ffi
+    from rasterize_gb300 import workloads as W
+
+    dev = torch.device("cuda", 0)
+    paths, sizes, rules = W.glyph_batch(seed=21, n=400)
+    batch = MaskBatch(paths, sizes, fill_rules=rules)
+    d = dict(kind=torch.from_numpy(batch.kind).to(dev), pts=torch.from_numpy(batch.pts.reshape(-1)).to(dev),
+             sub_off=torch.from_numpy(batch.sub_off.view(np.int32)).to(dev),
+             path_sub=torch.from_numpy(batch.path_sub.view(np.int32)).to(dev),
+             fill_rules=torch.from_numpy(batch.fill_rules).to(dev))
+    ptrs = {k: v.data_ptr() for k, v in d.items()}
+    torch.cuda.synchronize(dev)
+
+    # existing entry point (allocates its scratch through a context)
+    R = GpuRasterizer()
+    ref = torch.zeros(batch.out_len, dtype=torch.float32, device=dev)
+    R.mask_batch_device(batch, ptrs, ref.data_ptr())
+    R.ctx.synchronize()
+    ref_h = ref.cpu().numpy()
+    assert ref_h.any()
+
+    lib = _ffi.load()
+    s = batch.struct(_ffi.RZ_MEM_DEVICE, ptrs)
+    for call in range(2):
+        out = torch.full((batch.out_len,), 7.0, dtype=torch.float32, device=dev)
+        torch.cuda.synchronize(dev)
+        st = lib.rz_mask_batch_noalloc(ctypes.byref(s), R.flatness, out.data_ptr(), batch.out_len, None)
+        assert st == 0, "rz_mask_batch_noalloc returned %d on call %d" % (st, call)
+        got = out.cpu().numpy()
+        for i in range(batch.n_paths):
+            a = batch.mask(got, i)
+            e = batch.mask(ref_h, i)
+            err = float(np.abs(a - e).max())
+            assert err <= TOL, "call %d, path %d: max difference %.3g" % (call, i, err)
+
+
+def test_noalloc_rejects_oversized_batch():
+    pytest.importorskip("torch")
+    from rasterize_gb300 import MaskBatch, _ffi
+    from rasterize_gb300 import workloads as W
+
+    paths, sizes, _ = W.glyph_batch(seed=22, n=2)
+    batch = MaskBatch(paths, sizes)
+    s = batch.struct(_ffi.RZ_MEM_DEVICE, dict(kind=1, pts=1, sub_off=1, path_sub=1))
+    s.n_paths = 16385  # beyond the static scratch; rejected before any memory is touched
+    big = (_ffi.RzMaskDesc * 16385)()
+    s.masks = ctypes.addressof(big)
+    lib = _ffi.load()
+    assert lib.rz_mask_batch_noalloc(ctypes.byref(s), 0.05, 1, 1 << 40, None) == 7  # RZ_ERR_CAPACITY
