@@ -155,6 +155,78 @@ RZ_API rz_status rz_mask_batch(rz_ctx* ctx, const rz_path_batch* batch, double f
 RZ_API rz_status rz_mask_batch_per_path(rz_ctx* ctx, const rz_path_batch* batch, double flatness,
                                  float* out, uint64_t out_len);
 
+/* ---- paints and scenes --------------------------------------------------- */
+#define RZ_PAINT_SOLID 0  /* LinColor (src/color.rs:357-374) */
+#define RZ_PAINT_LINEAR 1 /* GradLinear (src/grad.rs:150-226) */
+#define RZ_PAINT_RADIAL 2 /* GradRadial (src/grad.rs:300-426) */
+#define RZ_UNITS_USER_SPACE 0 /* Units::UserSpaceOnUse (src/rasterize.rs:170-177) */
+#define RZ_UNITS_BOUNDING_BOX 1
+#define RZ_SPREAD_PAD 0 /* GradSpread (src/grad.rs:7-31) */
+#define RZ_SPREAD_REPEAT 1
+#define RZ_SPREAD_REFLECT 2
+
+/* GradStop (src/grad.rs:41-52): position and premultiplied linear RGBA. */
+typedef struct rz_stop {
+    double position;
+    float color[4];
+} rz_stop;
+
+/* A Paint.  Solid: `color` (premultiplied linear RGBA).  Linear: start, end.
+ * Radial: start = center, end = focal center, radius, fradius.  Gradients
+ * take stops (sorted like GradStops::new), units, spread, linear_colors and
+ * their own transform `tr`.  At most 16 stops.  Host memory. */
+typedef struct rz_paint {
+    int32_t kind;
+    int32_t units;
+    int32_t spread;
+    int32_t linear_colors;
+    double tr[6];
+    double start[2];
+    double end[2];
+    double radius;
+    double fradius;
+    float color[4];
+    const rz_stop* stops;
+    uint32_t n_stops;
+    uint32_t reserved;
+} rz_paint;
+
+/* A Scene that is a Group of Fill nodes in drawing order (src/scene.rs:69-200),
+ * rendered with Scene::render(tr = identity, view = the canvas, bg).  Paths of
+ * all fills are concatenated: subpath_off holds global segment offsets
+ * (n_subpaths + 1), fill_subpath_off (n_fills + 1) gives each fill's subpath
+ * range.  transforms: n_fills * 6 (NULL = identity), fill_rules: n_fills (NULL
+ * = NonZero), fill_paint: paint index per fill.  Host memory. */
+typedef struct rz_scene {
+    uint32_t n_fills;
+    uint32_t n_segments;
+    uint32_t n_subpaths;
+    uint32_t n_paints;
+    const uint8_t* seg_kind;
+    const double* seg_pts;
+    const uint32_t* subpath_off;
+    const uint32_t* fill_subpath_off;
+    const double* transforms;
+    const uint8_t* fill_rules;
+    const uint32_t* fill_paint;
+    const rz_paint* paints;
+} rz_scene;
+
+/* Rasterizer::fill (src/rasterize.rs:69-115): paints `path` (transformed by
+ * tr) with `paint` and composites it source-over into the host RGBA f32 view
+ * `img` (4 floats per pixel; shape in pixels), exactly where and how the
+ * reference's signed-difference rasterizer would. */
+RZ_API rz_status rz_fill(rz_ctx* ctx, const rz_path* path, const double tr[6], int32_t fill_rule, double flatness,
+                         const rz_paint* paint, float* img, rz_shape shape);
+
+/* Scene::render (src/scene.rs:186-199, Pipeline::render_rec Fill :407-435)
+ * of a Group of fills over a width x height RGBA f32 canvas (host memory, row
+ * major, 4 floats per pixel) initialised to bg (NULL: transparent).  The
+ * fills are flattened and binned by (fill, row band) once, then one CTA per
+ * row band composites every fill in order. */
+RZ_API rz_status rz_render_scene(rz_ctx* ctx, const rz_scene* scene, double flatness, const float bg[4],
+                                 float* canvas, uint32_t width, uint32_t height);
+
 /* ---- batch plans: resident work list + CUDA graph replay ---------------- */
 /* A plan fixes one device-memory batch (batch->memory == RZ_MEM_DEVICE), its
  * output buffer and flatness.  Creating it uploads the work list (bands of

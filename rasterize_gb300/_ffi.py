@@ -57,6 +57,14 @@ class RzPathBatch(ctypes.Structure):
                 ("transforms", ctypes.c_void_p), ("fill_rules", ctypes.c_void_p), ("masks", ctypes.c_void_p)]
 
 
+class RzScene(ctypes.Structure):
+    _fields_ = [("n_fills", ctypes.c_uint32), ("n_segments", ctypes.c_uint32), ("n_subpaths", ctypes.c_uint32),
+                ("n_paints", ctypes.c_uint32), ("seg_kind", ctypes.c_void_p), ("seg_pts", ctypes.c_void_p),
+                ("subpath_off", ctypes.c_void_p), ("fill_subpath_off", ctypes.c_void_p),
+                ("transforms", ctypes.c_void_p), ("fill_rules", ctypes.c_void_p), ("fill_paint", ctypes.c_void_p),
+                ("paints", ctypes.c_void_p)]
+
+
 _lock = threading.Lock()
 _lib = None
 
@@ -85,6 +93,9 @@ _SIGNATURES = {
     "rz_batch_plan_info": (ctypes.c_int32, [P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
     "rz_batch_plan_destroy": (None, [P]),
     "rz_mask_batch_noalloc": (ctypes.c_int32, [ctypes.POINTER(RzPathBatch), ctypes.c_double, P, ctypes.c_uint64, P]),
+    "rz_fill": (ctypes.c_int32, [P, ctypes.POINTER(RzPath), P, ctypes.c_int32, ctypes.c_double, P, P, RzShape]),
+    "rz_render_scene": (ctypes.c_int32, [P, ctypes.POINTER(RzScene), ctypes.c_double, P, P, ctypes.c_uint32,
+                                         ctypes.c_uint32]),
 }
 
 

@@ -17,7 +17,9 @@
 
 #include "../../include/rasterize_gb300.h"
 #include "rz_host_arc.cpp.inc"
+#include "rz_host_scene.cpp.inc"
 #include "rz_kernels.cuh"
+#include "rz_pipeline.cuh"
 
 namespace rz {
 cudaError_t init_kernels();
@@ -27,6 +29,14 @@ int mask_bands_occupancy();
 int band_floats();
 cudaError_t launch_flatten_counts(const BatchDev& b, uint32_t n_segments, uint32_t n_subpaths, uint32_t* counts,
                                   cudaStream_t stream);
+cudaError_t launch_flatten_count(const SceneDev& S, cudaStream_t st);
+cudaError_t launch_flatten_emit(const SceneDev& S, cudaStream_t st);
+cudaError_t launch_bin_scatter(const SceneDev& S, cudaStream_t st);
+int composite_smem_bytes(int canvas_w, int band_rows, int max_clip_width, bool paint_mode, int* cov_stride,
+                         int* tot_floats);
+cudaError_t launch_composite(const SceneDev& S, int cov_stride, int tot_floats, int smem, cudaStream_t st);
+uint64_t scan_temp_words(uint64_t n);
+cudaError_t scan_u32(uint32_t* data, uint64_t n, uint32_t* temp, cudaStream_t stream);
 }  // namespace rz
 
 namespace {
@@ -85,6 +95,8 @@ struct rz_ctx {
     std::mutex mu;
     // device buffers
     DevBuf d_kind, d_pts, d_sub, d_psub, d_tr, d_rule, d_masks, d_items, d_out, d_ctrl, d_counts;
+    // line pipeline (large paths, scenes)
+    DevBuf p_fills, p_paints, p_slots, p_lines, p_ecount, p_estart, p_ecursor, p_pairs, p_scan, p_canvas;
     HostBuf h_stage, h_out;
     // host-side arc expansion scratch
     std::vector<uint8_t> x_kind;
@@ -123,10 +135,11 @@ rz_status status_from_device(rz_ctx* ctx, int32_t code) {
 
 bool valid_flatness(double f) { return std::isfinite(f) && 16.0 * f * f > 0.0; }
 
-// Band height for a mask: as many rows as fit in the shared band.
+// Band height for a mask: as many rows as fit in the shared band, at most
+// 256 (the fixed-point accumulator holds band-relative y below 511).
 int band_rows(int clip_width, int height) {
     const int stride = rz::band_stride(clip_width);
-    int rows = std::max(1, rz::band_floats() / stride);
+    int rows = std::min(256, std::max(1, rz::band_floats() / stride));
     return std::min(rows, std::max(1, height));
 }
 
@@ -196,8 +209,10 @@ void rz_destroy(rz_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
-    DevBuf* bufs[] = {&c->d_kind, &c->d_pts, &c->d_sub, &c->d_psub, &c->d_tr, &c->d_rule,
-                      &c->d_masks, &c->d_items, &c->d_out, &c->d_ctrl, &c->d_counts};
+    DevBuf* bufs[] = {&c->d_kind,   &c->d_pts,     &c->d_sub,     &c->d_psub,    &c->d_tr,      &c->d_rule,
+                      &c->d_masks,  &c->d_items,   &c->d_out,     &c->d_ctrl,    &c->d_counts,  &c->p_fills,
+                      &c->p_paints, &c->p_slots,   &c->p_lines,   &c->p_ecount,  &c->p_estart,  &c->p_ecursor,
+                      &c->p_pairs,  &c->p_scan,    &c->p_canvas};
     for (DevBuf* b : bufs) b->release();
     c->h_stage.release();
     c->h_out.release();
@@ -417,6 +432,21 @@ rz_status render_single(rz_ctx* ctx, const rz_path* path, const double tr[6], in
 
 }  // namespace
 
+namespace {
+rz_status mask_pipeline(rz_ctx* ctx, const rz_path* path, const double tr[6], int32_t rule, double flatness,
+                        uint64_t width, uint64_t height);
+
+// The band kernel re-walks every segment for each band of rows; paths whose
+// segments x bands product is large go through the line pipeline instead,
+// which flattens every segment once and bins the lines by band.
+bool use_pipeline(const rz_path* path, uint64_t width, uint64_t height) {
+    if (!path) return false;
+    const int rows = band_rows((int)width - 1, (int)height);
+    const uint64_t bands = (height + rows - 1) / rows;
+    return bands * ((uint64_t)path->n_segments + path->n_subpaths) > 2000000ull;
+}
+}  // namespace
+
 extern "C" {
 
 rz_status rz_mask(rz_ctx* ctx, const rz_path* path, const double tr[6], int32_t fill_rule, double flatness,
@@ -425,7 +455,18 @@ rz_status rz_mask(rz_ctx* ctx, const rz_path* path, const double tr[6], int32_t 
     std::lock_guard<std::mutex> lock(ctx->mu);
     if (!tr || !img) return fail(ctx, RZ_ERR_INVALID, "null argument");
     if (shape.width == 0 || shape.height == 0) return RZ_OK;
-    rz_status st = render_single(ctx, path, tr, fill_rule, flatness, shape.width, shape.height, false);
+    rz_status st;
+    if (use_pipeline(path, shape.width, shape.height)) {
+        st = check_path(ctx, path);
+        if (st) return st;
+        if (!valid_flatness(flatness)) return fail(ctx, RZ_ERR_INVALID, "flatness must be > 0 and finite");
+        if (fill_rule != RZ_FILL_NONZERO && fill_rule != RZ_FILL_EVENODD) return fail(ctx, RZ_ERR_INVALID, "bad fill rule");
+        if (shape.width > 16383 || shape.height > 16383) return fail(ctx, RZ_ERR_INVALID, "image too large");
+        RZ_CUDA(cudaSetDevice(ctx->device));
+        st = mask_pipeline(ctx, path, tr, fill_rule, flatness, shape.width, shape.height);
+    } else {
+        st = render_single(ctx, path, tr, fill_rule, flatness, shape.width, shape.height, false);
+    }
     if (st) return st;
     const size_t n = shape.width * shape.height;
     RZ_CUDA(ctx->h_out.ensure(n * 4));
@@ -722,6 +763,409 @@ void rz_batch_plan_destroy(rz_batch_plan* plan) {
     plan->d_items.release();
     plan->d_ctrl.release();
     delete plan;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Line pipeline: large paths and painted scenes
+// ---------------------------------------------------------------------------
+namespace {
+
+// Rasterizer::fill's paint set-up (src/rasterize.rs:78-97) for a fill drawn
+// with transform `tr` (binary64): units transform, its inverse, stops.
+void prepare_paint(const rz_paint& in, const rzhost::Xf& tr, bool have_bbox, const rzhost::Box& bbox0,
+                   rz::PaintDev& out) {
+    std::memset(&out, 0, sizeof(out));
+    out.kind = in.kind;
+    out.spread = in.spread;
+    out.linear_colors = in.linear_colors ? 1 : 0;
+    if (in.kind == RZ_PAINT_SOLID) {
+        for (int i = 0; i < 4; ++i) out.color[i] = in.color[i];
+        return;
+    }
+    rzhost::Xf ptr;
+    std::memcpy(ptr.m, in.tr, sizeof(ptr.m));
+    rzhost::Xf units;
+    if (in.units == RZ_UNITS_USER_SPACE) {
+        units = rzhost::xf_mul(tr, ptr);
+    } else {
+        if (!have_bbox) {
+            out.kind = -1;  // empty path: nothing drawn
+            return;
+        }
+        // BBox::unit_transform: translate(x, y) * scale(width, height) (src/geometry.rs:662-664)
+        const rzhost::Xf t{{1.0, 0.0, bbox0.x0, 0.0, 1.0, bbox0.y0}};
+        const rzhost::Xf sc{{bbox0.x1 - bbox0.x0, 0.0, 0.0, 0.0, bbox0.y1 - bbox0.y0, 0.0}};
+        units = rzhost::xf_mul(rzhost::xf_mul(tr, rzhost::xf_mul(t, sc)), ptr);
+    }
+    rzhost::Xf pix;
+    if (!rzhost::xf_invert(units, pix)) {
+        out.kind = -1;  // not invertible: nothing drawn (src/rasterize.rs:92)
+        return;
+    }
+    // GradStops::new: stable sort by position, a black stop when empty; sRGB stops when !linear_colors
+    struct St {
+        double pos;
+        float c[4];
+    };
+    std::vector<St> stops;
+    for (uint32_t i = 0; i < std::min<uint32_t>(in.n_stops, rz::kMaxStops); ++i) {
+        St t;
+        t.pos = in.stops[i].position;
+        std::memcpy(t.c, in.stops[i].color, sizeof(t.c));
+        stops.push_back(t);
+    }
+    std::stable_sort(stops.begin(), stops.end(), [](const St& a, const St& b) { return a.pos < b.pos; });
+    if (stops.empty()) stops.push_back(St{0.0, {0.f, 0.f, 0.f, 1.f}});
+    out.nstops = (int)stops.size();
+    for (int i = 0; i < out.nstops; ++i) {
+        if (!in.linear_colors) rzhost::into_srgb(stops[i].c);
+        out.pos[i] = (float)stops[i].pos;
+        for (int c = 0; c < 4; ++c) out.col[i][c] = stops[i].c[c];
+    }
+    if (in.kind == RZ_PAINT_LINEAR) {
+        const double dx = in.end[0] - in.start[0], dy = in.end[1] - in.start[1];
+        const double dd = dx * dx + dy * dy;
+        const double ux = dx / dd, uy = dy / dd;
+        // t of a local pixel centre (x, y) = g0 x + g1 y + g2 (GradLinear::at, src/grad.rs:202-211)
+        const double g[3] = {pix.m[0] * ux + pix.m[3] * uy, pix.m[1] * ux + pix.m[4] * uy,
+                             (pix.m[2] - in.start[0]) * ux + (pix.m[5] - in.start[1]) * uy};
+        for (int i = 0; i < 3; ++i) {
+            out.gh[i] = (float)g[i];
+            out.gl[i] = (float)(g[i] - (double)out.gh[i]);
+        }
+    } else {
+        // p - focal centre of a local pixel centre, composed in binary64
+        const double q[6] = {pix.m[0], pix.m[1], pix.m[2] - in.end[0], pix.m[3], pix.m[4], pix.m[5] - in.end[1]};
+        for (int i = 0; i < 6; ++i) {
+            out.q[i] = (float)q[i];
+            out.qd[i] = q[i];
+        }
+        out.cdxd = in.start[0] - in.end[0];
+        out.cdyd = in.start[1] - in.end[1];
+        out.rdd = in.radius - in.fradius;
+        out.frd = in.fradius;
+        out.cdx = (float)out.cdxd;
+        out.cdy = (float)out.cdyd;
+        out.rd = (float)out.rdd;
+        out.fr = (float)out.frd;
+        out.a64 = (out.cdxd * out.cdxd + out.cdyd * out.cdyd) - out.rdd * out.rdd;
+        out.radial_linear = std::fabs(out.a64) < rzhost::kEps ? 1 : 0;
+    }
+}
+
+struct HostScene {
+    std::vector<rz::FillDev> fills;
+    std::vector<rz::PaintDev> paints;
+    const uint8_t* kind = nullptr;
+    const double* pts = nullptr;
+    const uint32_t* sub_off = nullptr;
+    uint32_t n_seg = 0, n_sub = 0;
+    uint32_t n_slots = 0, n_entries = 0;
+    int band_rows = 1, n_bands = 0, max_clip = 1;
+};
+
+int choose_band_rows(int canvas_w, int canvas_h, bool paint_mode) {
+    const int stride = rz::band_stride(canvas_w);
+    const int per_row = 4 * stride + (paint_mode ? 16 * canvas_w : 0) + 4 * ((stride + 15) / 16);
+    int rows = std::max(1, (paint_mode ? 96 * 1024 : 64 * 1024) / per_row);
+    rows = std::min(rows, 64);
+    return std::max(1, std::min(rows, std::max(canvas_h, 1)));
+}
+
+// Adds one fill (its view, transform, paint, slots and bands) to `hs`.
+void add_fill(HostScene& hs, uint32_t sub0, uint32_t sub1, int col0, int row0, int width, int height, int clip_width,
+              const rzhost::Xf& tr, int rule, int paint) {
+    if (width <= 0 || height <= 0) return;
+    rz::FillDev f{};
+    f.sub0 = sub0;
+    f.sub1 = sub1;
+    f.seg0 = hs.sub_off[sub0];
+    f.seg1 = hs.sub_off[sub1];
+    f.slot0 = hs.n_slots;
+    f.col0 = col0;
+    f.row0 = row0;
+    f.width = width;
+    f.height = height;
+    f.clip_width = clip_width;
+    f.rule = rule;
+    f.paint = paint;
+    std::memcpy(f.tr, tr.m, sizeof(f.tr));
+    f.band0 = row0 / hs.band_rows;
+    f.nbands = (row0 + height - 1) / hs.band_rows - f.band0 + 1;
+    f.entry0 = hs.n_entries;
+    hs.n_slots += (f.seg1 - f.seg0) + (sub1 - sub0);
+    hs.n_entries += (uint32_t)f.nbands;
+    hs.max_clip = std::max(hs.max_clip, clip_width);
+    hs.fills.push_back(f);
+}
+
+// Flatten + bin + composite on the device.  canvas: device buffer (RGBA
+// pixels when paints are given, else an f32 mask), stride in pixels.
+rz_status run_pipeline(rz_ctx* ctx, HostScene& hs, double flatness, float* canvas, int64_t canvas_stride, int canvas_w,
+                       int canvas_h, const float* bg_dev, bool load_canvas) {
+    const bool paint_mode = !hs.paints.empty();
+    rz::SceneDev S{};
+    S.kind = (const uint8_t*)ctx->d_kind.p;
+    S.pts = (const double*)ctx->d_pts.p;
+    S.sub_off = (const uint32_t*)ctx->d_sub.p;
+    S.n_fills = (uint32_t)hs.fills.size();
+    S.n_slots = hs.n_slots;
+    S.n_segments = hs.n_seg;
+    S.n_subpaths = hs.n_sub;
+    S.thr64 = 16.0 * flatness * flatness;
+    S.thr32 = (float)S.thr64;
+    S.canvas_w = canvas_w;
+    S.canvas_h = canvas_h;
+    S.band_rows = hs.band_rows;
+    S.n_bands = (canvas_h + hs.band_rows - 1) / hs.band_rows;
+    S.canvas = canvas;
+    S.canvas_stride = canvas_stride;
+    S.bg = bg_dev;
+    S.load_canvas = load_canvas ? 1 : 0;
+    RZ_CUDA(ctx->d_ctrl.ensure(64));
+    RZ_CUDA(cudaMemsetAsync(ctx->d_ctrl.p, 0, 64, ctx->stream));
+    S.err = (int32_t*)ctx->d_ctrl.p;
+    S.counters = (int32_t*)ctx->d_ctrl.p + 4;
+    if (S.n_bands == 0) return read_error(ctx);
+    int cov_stride = 0, tot_floats = 0;
+    const int smem = rz::composite_smem_bytes(canvas_w, hs.band_rows, hs.max_clip, paint_mode, &cov_stride, &tot_floats);
+    if (S.n_fills == 0) {
+        // nothing to draw: the composite still writes the background
+        if (paint_mode) {
+            RZ_CUDA(ctx->p_paints.ensure(sizeof(rz::PaintDev)));
+            S.paints = (const rz::PaintDev*)ctx->p_paints.p;
+            RZ_CUDA(rz::launch_composite(S, cov_stride, tot_floats, smem, ctx->stream));
+        }
+        return read_error(ctx);
+    }
+    RZ_CUDA(ctx->p_fills.ensure(hs.fills.size() * sizeof(rz::FillDev)));
+    RZ_CUDA(cudaMemcpyAsync(ctx->p_fills.p, hs.fills.data(), hs.fills.size() * sizeof(rz::FillDev),
+                            cudaMemcpyHostToDevice, ctx->stream));
+    S.fills = (const rz::FillDev*)ctx->p_fills.p;
+    if (paint_mode) {
+        RZ_CUDA(ctx->p_paints.ensure(hs.paints.size() * sizeof(rz::PaintDev)));
+        RZ_CUDA(cudaMemcpyAsync(ctx->p_paints.p, hs.paints.data(), hs.paints.size() * sizeof(rz::PaintDev),
+                                cudaMemcpyHostToDevice, ctx->stream));
+        S.paints = (const rz::PaintDev*)ctx->p_paints.p;
+    }
+    // 1) lines per slot, 2) offsets (one extra element receives the total)
+    const uint64_t ns = (uint64_t)hs.n_slots + 1;
+    RZ_CUDA(ctx->p_slots.ensure(ns * 4));
+    S.slot_count = (uint32_t*)ctx->p_slots.p;
+    RZ_CUDA(cudaMemsetAsync(S.slot_count, 0, ns * 4, ctx->stream));
+    RZ_CUDA(rz::launch_flatten_count(S, ctx->stream));
+    const uint64_t ne = (uint64_t)hs.n_entries + 1;
+    RZ_CUDA(ctx->p_scan.ensure(rz::scan_temp_words(std::max(ns, ne)) * 4 + 64));
+    RZ_CUDA(rz::scan_u32(S.slot_count, ns, (uint32_t*)ctx->p_scan.p, ctx->stream));
+    uint32_t n_lines = 0;
+    RZ_CUDA(cudaMemcpyAsync(&n_lines, S.slot_count + hs.n_slots, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+    rz_status st = read_error(ctx);
+    if (st) return st;
+    S.n_lines = n_lines;
+    // 3) lines + per-(fill, band) counts
+    RZ_CUDA(ctx->p_lines.ensure((uint64_t)std::max(n_lines, 1u) * 2 * sizeof(int4)));
+    S.lines = (int4*)ctx->p_lines.p;
+    RZ_CUDA(ctx->p_ecount.ensure(ne * 4));
+    RZ_CUDA(ctx->p_estart.ensure(ne * 4));
+    RZ_CUDA(ctx->p_ecursor.ensure(ne * 4));
+    S.entry_count = (uint32_t*)ctx->p_ecount.p;
+    S.entry_start = (uint32_t*)ctx->p_estart.p;
+    S.entry_cursor = (uint32_t*)ctx->p_ecursor.p;
+    RZ_CUDA(cudaMemsetAsync(S.entry_count, 0, ne * 4, ctx->stream));
+    RZ_CUDA(cudaMemsetAsync(S.entry_cursor, 0, ne * 4, ctx->stream));
+    RZ_CUDA(rz::launch_flatten_emit(S, ctx->stream));
+    // 4) list starts per (fill, band)
+    RZ_CUDA(cudaMemcpyAsync(S.entry_start, S.entry_count, ne * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    RZ_CUDA(rz::scan_u32(S.entry_start, ne, (uint32_t*)ctx->p_scan.p, ctx->stream));
+    uint32_t n_pairs = 0;
+    RZ_CUDA(cudaMemcpyAsync(&n_pairs, S.entry_start + hs.n_entries, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+    // 5) line lists
+    RZ_CUDA(ctx->p_pairs.ensure((uint64_t)std::max(n_pairs, 1u) * 4));
+    S.pairs = (uint32_t*)ctx->p_pairs.p;
+    RZ_CUDA(rz::launch_bin_scatter(S, ctx->stream));
+    // 6) composite
+    RZ_CUDA(rz::launch_composite(S, cov_stride, tot_floats, smem, ctx->stream));
+    return read_error(ctx);
+}
+
+// Segments of `hs` staged into the context's device buffers (arcs expanded).
+rz_status stage_scene_segments(rz_ctx* ctx, const uint8_t* kind, const double* pts, uint32_t n_seg,
+                               const uint32_t* sub_off, uint32_t n_sub, const uint32_t* fill_sub, uint32_t n_fills,
+                               HostScene& hs, std::vector<uint32_t>& fill_sub_out) {
+    rz::BatchDev b{};
+    rz_status st = stage_host(ctx, kind, pts, n_seg, sub_off, n_sub, fill_sub, n_fills, nullptr, nullptr, b);
+    if (st) return st;
+    if (ctx->expanded) {
+        hs.kind = ctx->x_kind.data();
+        hs.pts = ctx->x_pts.data();
+        hs.sub_off = ctx->x_sub.data();
+        hs.n_seg = (uint32_t)ctx->x_kind.size();
+        hs.n_sub = (uint32_t)ctx->x_sub.size() - 1;
+        fill_sub_out = ctx->x_psub;
+    } else {
+        hs.kind = kind;
+        hs.pts = pts;
+        hs.sub_off = sub_off;
+        hs.n_seg = n_seg;
+        hs.n_sub = n_sub;
+        fill_sub_out.assign(fill_sub, fill_sub + n_fills + 1);
+    }
+    return RZ_OK;
+}
+
+// Renders one large path as a mask with the line pipeline (mask semantics).
+rz_status mask_pipeline(rz_ctx* ctx, const rz_path* path, const double tr[6], int32_t rule, double flatness,
+                        uint64_t width, uint64_t height) {
+    HostScene hs;
+    std::vector<uint32_t> fsub;
+    const uint32_t psub[2] = {0, path->n_subpaths};
+    rz_status st = stage_scene_segments(ctx, path->seg_kind, path->seg_pts, path->n_segments, path->subpath_off,
+                                        path->n_subpaths, psub, 1, hs, fsub);
+    if (st) return st;
+    hs.band_rows = choose_band_rows((int)width, (int)height, false);
+    rzhost::Xf t;
+    std::memcpy(t.m, tr, sizeof(t.m));
+    add_fill(hs, fsub[0], fsub[1], 0, 0, (int)width, (int)height, (int)width - 1, t, rule, -1);
+    RZ_CUDA(ctx->d_out.ensure(width * height * 4 + 16));
+    RZ_CUDA(cudaMemsetAsync(ctx->d_out.p, 0, width * height * 4, ctx->stream));
+    return run_pipeline(ctx, hs, flatness, (float*)ctx->d_out.p, (int64_t)width, (int)width, (int)height, nullptr,
+                        false);
+}
+
+}  // namespace
+
+extern "C" {
+
+rz_status rz_fill(rz_ctx* ctx, const rz_path* path, const double tr[6], int32_t fill_rule, double flatness,
+                  const rz_paint* paint, float* img, rz_shape shape) {
+    if (!ctx) return RZ_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    rz_status st = check_path(ctx, path);
+    if (st) return st;
+    if (!tr || !paint || !img) return fail(ctx, RZ_ERR_INVALID, "null argument");
+    if (!valid_flatness(flatness)) return fail(ctx, RZ_ERR_INVALID, "flatness must be > 0 and finite");
+    if (shape.width == 0 || shape.height == 0) return RZ_OK;
+    if (shape.width > 16383 || shape.height > 16383) return fail(ctx, RZ_ERR_INVALID, "image too large");
+    if (paint->n_stops > (uint32_t)rz::kMaxStops) return fail(ctx, RZ_ERR_INVALID, "more than 16 stops");
+    RZ_CUDA(cudaSetDevice(ctx->device));
+    HostScene hs;
+    std::vector<uint32_t> fsub;
+    const uint32_t psub[2] = {0, path->n_subpaths};
+    st = stage_scene_segments(ctx, path->seg_kind, path->seg_pts, path->n_segments, path->subpath_off,
+                              path->n_subpaths, psub, 1, hs, fsub);
+    if (st) return st;
+    const int W = (int)shape.width, H = (int)shape.height;
+    hs.band_rows = choose_band_rows(W, H, true);
+    rzhost::Xf t;
+    std::memcpy(t.m, tr, sizeof(t.m));
+    rzhost::Box bb0{};
+    const rzhost::Xf id{{1, 0, 0, 0, 1, 0}};
+    const bool have = rzhost::path_bbox(hs.kind, hs.pts, hs.sub_off, fsub[0], fsub[1], id, bb0);
+    hs.paints.resize(1);
+    prepare_paint(*paint, t, have, bb0, hs.paints[0]);
+    if (hs.paints[0].kind < 0) return RZ_OK;
+    // mask_iter semantics: the view is the image, clip at its width
+    add_fill(hs, fsub[0], fsub[1], 0, 0, W, H, W, t, fill_rule, 0);
+    // dense device copy of the view, blended in place, copied back
+    const size_t n = (size_t)W * H;
+    RZ_CUDA(ctx->h_out.ensure(n * 16));
+    float* h = (float*)ctx->h_out.p;
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x)
+            std::memcpy(h + 4 * ((size_t)y * W + x), img + 4 * (shape.start + y * shape.row_stride + x * shape.col_stride),
+                        16);
+    RZ_CUDA(ctx->p_canvas.ensure(n * 16));
+    RZ_CUDA(cudaMemcpyAsync(ctx->p_canvas.p, h, n * 16, cudaMemcpyHostToDevice, ctx->stream));
+    st = run_pipeline(ctx, hs, flatness, (float*)ctx->p_canvas.p, W, W, H, nullptr, true);
+    if (st) return st;
+    RZ_CUDA(cudaMemcpyAsync(h, ctx->p_canvas.p, n * 16, cudaMemcpyDeviceToHost, ctx->stream));
+    RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x)
+            std::memcpy(img + 4 * (shape.start + y * shape.row_stride + x * shape.col_stride), h + 4 * ((size_t)y * W + x),
+                        16);
+    return RZ_OK;
+}
+
+rz_status rz_render_scene(rz_ctx* ctx, const rz_scene* scene, double flatness, const float bg[4], float* canvas,
+                          uint32_t width, uint32_t height) {
+    if (!ctx) return RZ_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    if (!scene || !canvas || (scene->n_fills && (!scene->fill_subpath_off || !scene->fill_paint || !scene->paints)))
+        return fail(ctx, RZ_ERR_INVALID, "null argument");
+    if (!valid_flatness(flatness)) return fail(ctx, RZ_ERR_INVALID, "flatness must be > 0 and finite");
+    if (width > 16383 || height > 16383) return fail(ctx, RZ_ERR_INVALID, "canvas too large");
+    const uint32_t F = scene->n_fills;
+    for (uint32_t f = 0; f < F; ++f) {
+        if (scene->fill_subpath_off[f] > scene->fill_subpath_off[f + 1] || scene->fill_paint[f] >= scene->n_paints)
+            return fail(ctx, RZ_ERR_INVALID, "bad fill table");
+    }
+    if (F && scene->fill_subpath_off[F] > scene->n_subpaths) return fail(ctx, RZ_ERR_INVALID, "bad fill_subpath_off");
+    for (uint32_t i = 0; i < scene->n_subpaths; ++i)
+        if (scene->subpath_off[i] > scene->subpath_off[i + 1]) return fail(ctx, RZ_ERR_INVALID, "subpath_off decreasing");
+    if (scene->subpath_off[scene->n_subpaths] > scene->n_segments)
+        return fail(ctx, RZ_ERR_INVALID, "subpath_off exceeds n_segments");
+    for (uint32_t p = 0; p < scene->n_paints; ++p)
+        if (scene->paints[p].n_stops > (uint32_t)rz::kMaxStops) return fail(ctx, RZ_ERR_INVALID, "more than 16 stops");
+    RZ_CUDA(cudaSetDevice(ctx->device));
+    HostScene hs;
+    std::vector<uint32_t> fsub;
+    rz_status st = stage_scene_segments(ctx, scene->seg_kind, scene->seg_pts, scene->n_segments, scene->subpath_off,
+                                        scene->n_subpaths, scene->fill_subpath_off, F, hs, fsub);
+    if (st) return st;
+    const int W = (int)width, H = (int)height;
+    hs.band_rows = choose_band_rows(W, H, true);
+    const rzhost::Xf id{{1, 0, 0, 0, 1, 0}};
+    for (uint32_t f = 0; f < F; ++f) {
+        rzhost::Xf t = id;
+        if (scene->transforms) std::memcpy(t.m, scene->transforms + 6ull * f, sizeof(t.m));
+        // Pipeline::build_rec Fill: bbox of the path, intersected with the view (src/scene.rs:288-298)
+        rzhost::Box pb{};
+        if (!rzhost::path_bbox(hs.kind, hs.pts, hs.sub_off, fsub[f], fsub[f + 1], t, pb)) continue;
+        const double vx1 = (double)W, vy1 = (double)H;
+        if (0.0 > pb.x1 || pb.x0 > vx1 || 0.0 > pb.y1 || pb.y0 > vy1) continue;
+        const rzhost::Box nb{std::fmax(0.0, pb.x0), std::fmax(0.0, pb.y0), std::fmin(vx1, pb.x1), std::fmin(vy1, pb.y1)};
+        // render_rec Fill: the view of the layer and the align transform (src/scene.rs:407-430)
+        long col_min = (long)std::floor(nb.x0), col_max = (long)std::ceil(nb.x1) + 1;
+        long row_min = (long)std::floor(nb.y0), row_max = (long)std::ceil(nb.y1) + 1;
+        if (col_min < 0) col_min = W;  // `as usize` wraps; view_shape clamps (src/image.rs:588-605)
+        if (row_min < 0) row_min = H;
+        if (col_max < 0) col_max = W;
+        if (row_max < 0) row_max = H;
+        row_min = std::min<long>(row_min, H);
+        row_max = std::max(std::min<long>(row_max, H), row_min);
+        col_min = std::min<long>(col_min, W);
+        col_max = std::max(std::min<long>(col_max, W), col_min);
+        const rzhost::Xf align{{1.0, 0.0, -std::floor(nb.x0), 0.0, 1.0, -std::floor(nb.y0)}};
+        const rzhost::Xf tr_fill = rzhost::xf_mul(align, t);
+        const int vw = (int)(col_max - col_min), vh = (int)(row_max - row_min);
+        if (vw <= 0 || vh <= 0) continue;
+        rzhost::Box bb0{};
+        const bool have = rzhost::path_bbox(hs.kind, hs.pts, hs.sub_off, fsub[f], fsub[f + 1], id, bb0);
+        rz::PaintDev pd;
+        prepare_paint(scene->paints[scene->fill_paint[f]], tr_fill, have, bb0, pd);
+        if (pd.kind < 0) continue;
+        hs.paints.push_back(pd);
+        const int rule = scene->fill_rules ? scene->fill_rules[f] : 0;
+        add_fill(hs, fsub[f], fsub[f + 1], (int)col_min, (int)row_min, vw, vh, vw, tr_fill, rule,
+                 (int)hs.paints.size() - 1);
+    }
+    if (hs.paints.empty()) hs.paints.resize(1);  // paint mode even with nothing to draw
+    const size_t n = (size_t)W * H;
+    RZ_CUDA(ctx->p_canvas.ensure(n * 16 + 16));
+    RZ_CUDA(ctx->d_counts.ensure(64));
+    float bgv[4] = {0.f, 0.f, 0.f, 0.f};
+    if (bg) std::memcpy(bgv, bg, sizeof(bgv));
+    RZ_CUDA(cudaMemcpyAsync(ctx->d_counts.p, bgv, 16, cudaMemcpyHostToDevice, ctx->stream));
+    st = run_pipeline(ctx, hs, flatness, (float*)ctx->p_canvas.p, W, W, H, (const float*)ctx->d_counts.p, false);
+    if (st) return st;
+    RZ_CUDA(cudaMemcpyAsync(canvas, ctx->p_canvas.p, n * 16, cudaMemcpyDeviceToHost, ctx->stream));
+    RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+    return RZ_OK;
 }
 
 }  // extern "C"

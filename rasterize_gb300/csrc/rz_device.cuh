@@ -92,7 +92,7 @@ __device__ inline double flatness64(const Seg64& s) {
 }
 
 // The reference's flatness of node (d, k): replay the split chain in binary64.
-__device__ __noinline__ double flatness_chain64(Seg64 s, int d, uint32_t k) {
+static __device__ __noinline__ double flatness_chain64(Seg64 s, int d, uint32_t k) {
     for (int i = d - 1; i >= 0; --i) split_half64(s, (k >> i) & 1u);
     return flatness64(s);
 }
@@ -139,6 +139,9 @@ __device__ __forceinline__ bool is_nan_bits(double x) {
 }
 
 constexpr float FIX_ONE_INV = 1.0f / 65536.0f;
+
+// 2^e for -126 <= e <= 127, exact, without a libm call.
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }
 
 // A reference segment in fixed point (after the path transform).
 struct FixSeg {
@@ -210,9 +213,10 @@ __device__ inline FlatCoef flat_coef(const Seg64& s) {
 // qerr bounds |a2 - a2_true| and |a3 - a3_true| (px) when the coefficients
 // come from rounded inputs.
 __device__ inline int decide_fp32(int kind, const FlatCoef& c, int d, uint32_t k, float thr32, float qerr) {
-    const float h = ldexpf(1.0f, -d);
-    const float td = ldexpf(thr32, 4 * d);  // thr * 16^d, exact power-of-two scaling
-    const float scale = ldexpf(1.0f, 2 * d);  // chain error grows like 4^d in w units
+    const float h = pow2f(-d);
+    const float td = thr32 * pow2f(4 * d);     // thr * 16^d, exact power-of-two scaling
+    const float ms = c.mag * pow2f(2 * d - 40);  // chain error grows like 4^d in w units
+    const float e21 = pow2f(-21), e19 = pow2f(-19);
     float G, E;
     if (kind == SEG_CUBIC) {
         const float tu = h * (float)(3u * k + 1u);
@@ -222,15 +226,15 @@ __device__ inline int decide_fp32(int kind, const FlatCoef& c, int d, uint32_t k
         const float gx = fmaxf(wux * wux, wvx * wvx), gy = fmaxf(wuy * wuy, wvy * wvy);
         G = gx + gy;
         const float q = qerr * (1.f + tv);
-        const float bx = ldexpf(fabsf(c.a2x) + fabsf(c.a3x) * tv, -21) + ldexpf(c.mag * scale, -40) + q;
-        const float by = ldexpf(fabsf(c.a2y) + fabsf(c.a3y) * tv, -21) + ldexpf(c.mag * scale, -40) + q;
+        const float bx = (fabsf(c.a2x) + fabsf(c.a3x) * tv) * e21 + ms + q;
+        const float by = (fabsf(c.a2y) + fabsf(c.a3y) * tv) * e21 + ms + q;
         const float wx = sqrtf(gx), wy = sqrtf(gy);
-        E = (2.f * wx + bx) * bx + (2.f * wy + by) * by + ldexpf(G, -19);
+        E = (2.f * wx + bx) * bx + (2.f * wy + by) * by + G * e19;
     } else {
         G = c.a2x * c.a2x + c.a2y * c.a2y;
-        const float bx = ldexpf(fabsf(c.a2x), -21) + ldexpf(c.mag * scale, -40) + qerr;
-        const float by = ldexpf(fabsf(c.a2y), -21) + ldexpf(c.mag * scale, -40) + qerr;
-        E = (2.f * fabsf(c.a2x) + bx) * bx + (2.f * fabsf(c.a2y) + by) * by + ldexpf(G, -19);
+        const float bx = fabsf(c.a2x) * e21 + ms + qerr;
+        const float by = fabsf(c.a2y) * e21 + ms + qerr;
+        E = (2.f * fabsf(c.a2x) + bx) * bx + (2.f * fabsf(c.a2y) + by) * by + G * e19;
     }
     if (isfinite(G) && isfinite(E) && isfinite(td)) {
         if (G + E < td) return 1;
@@ -269,8 +273,6 @@ struct TreeWalk {
 struct VertexCoef {
     double p0x, p0y, pnx, pny;   // first and last control point
     double c1x, c1y, c2x, c2y, c3x, c3y;
-    float f1x, f1y, f2x, f2y, f3x, f3y;  // FP32 copies for small segments
-    bool small;                          // FP32 evaluation error below ~1e-6 px
 };
 
 __device__ inline VertexCoef vertex_coef(const Seg64& s) {
@@ -290,30 +292,10 @@ __device__ inline VertexCoef vertex_coef(const Seg64& s) {
         v.c1x = s.x[1] - s.x[0]; v.c1y = s.y[1] - s.y[0];
         v.c2x = v.c2y = v.c3x = v.c3y = 0.0;
     }
-    // FP32 Horner error is about 3 * 2^-24 * ext: ext < 48 keeps vertices within ~1e-5 px
-    const double ext = fmax(fabs(v.c1x) + fabs(v.c2x) + fabs(v.c3x), fabs(v.c1y) + fabs(v.c2y) + fabs(v.c3y));
-    v.small = ext < 48.0;
-    v.f1x = (float)v.c1x; v.f1y = (float)v.c1y;
-    v.f2x = (float)v.c2x; v.f2y = (float)v.c2y;
-    v.f3x = (float)v.c3x; v.f3y = (float)v.c3y;
     return v;
 }
 
-// Vertex at t = j / 2^d.  Small segments: FP32 relative to (ox, oy) with the
-// exact end point at t = 1.  Otherwise binary64 absolute x, band-relative y.
-__device__ inline void vertex_small(const VertexCoef& v, uint32_t j, int d, double ox, double oy, float p0rx,
-                                    float p0ry, float& rx, float& ry) {
-    if (j == 0) { rx = p0rx; ry = p0ry; return; }
-    if ((j >> d) != 0u) {
-        rx = (float)(v.pnx - ox);
-        ry = (float)(v.pny - oy);
-        return;
-    }
-    const float t = ldexpf((float)j, -d);
-    rx = p0rx + t * fmaf(t, fmaf(t, v.f3x, v.f2x), v.f1x);
-    ry = p0ry + t * fmaf(t, fmaf(t, v.f3y, v.f2y), v.f1y);
-}
-
+// Vertex at t = j / 2^d in binary64: absolute x, y relative to row oy.
 __device__ inline void vertex_big(const VertexCoef& v, uint32_t j, int d, double oy, double& x, double& y) {
     if (j == 0) { x = v.p0x; y = v.p0y - oy; return; }
     if ((j >> d) != 0u) { x = v.pnx; y = v.pny - oy; return; }
@@ -325,8 +307,19 @@ __device__ inline void vertex_big(const VertexCoef& v, uint32_t j, int d, double
 // ---------------------------------------------------------------------------
 // Coverage accumulation into a shared-memory row band
 // ---------------------------------------------------------------------------
+// Signed areas are accumulated in 32-bit fixed point, COV_ONE per unit of
+// winding: shared-memory integer atomics are order independent and the row
+// prefix is exact, so long rows with large windings lose nothing (EvenOdd
+// maps winding error 1:1 into coverage).  Windings wrap modulo 1024 (int32
+// holds +-512 units), which keeps EvenOdd parity and keeps NonZero's |w| >= 1
+// for every winding that is not within one unit of a multiple of 1024.
+// Band-relative y must stay below 511 rows (band heights are capped at 256).
+constexpr int COV_SHIFT = 22;
+constexpr int COV_ONE = 1 << COV_SHIFT;
+constexpr float COV_ONE_F = 4194304.0f;
+
 struct Band {
-    float* acc;     // bh rows x stride floats
+    float* acc;     // bh rows x stride accumulation words (int32 fixed point, COV_ONE per unit)
     int stride;     // >= width_i + 2
     int bh;         // rows in this band
     int y0;         // first image row of the band
@@ -335,73 +328,117 @@ struct Band {
     int width_i;
 };
 
-__device__ __forceinline__ void sadd(float* p, float v) { atomicAdd(p, v); }
+__device__ __forceinline__ void sadd(float* p, int v) {
+    if (v) atomicAdd(reinterpret_cast<int*>(p), v);
+}
 
-// One line (band-relative coordinates, x relative to integer column `xb`)
-// already clipped by the x rules; distributes its signed differences row by
-// row exactly like signed_difference_line (src/rasterize.rs:405-469).
-__device__ inline void accumulate_piece(const Band& B, int xb, float x0, float y0, float x1, float y1) {
-    if (y0 == y1) return;  // no signed coverage (the reference skips |dy| < EPSILON)
-    float dir = 1.f;
-    if (y0 > y1) {
-        float t = x0; x0 = x1; x1 = t;
-        t = y0; y0 = y1; y1 = t;
-        dir = -1.f;
+// Signed height `d` (fixed point) of one row, spread over the pixels the line
+// covers between xa and xn (FP32, relative to integer column xb) as in
+// signed_difference_line (src/rasterize.rs:433-466).  The pixel shares are
+// rounded and the last one takes the remainder, so the row receives exactly
+// `d` and the row prefix telescopes.
+__device__ __forceinline__ void accumulate_row(const Band& B, int r, int xb, float xa, float xn, int d) {
+    const float df = (float)d;
+    const float xlo = fminf(xa, xn), xhi = fmaxf(xa, xn);
+    const float x0_floor = fmaxf(floorf(xlo), -(float)xb);
+    int x0i = (int)x0_floor;
+    const float x1_ceil = fminf(ceilf(xhi), B.width_f - (float)xb);  // the reference's `width`, relative
+    const int x1i = (int)x1_ceil;
+    float* row = B.acc + r * B.stride + xb;
+    x0i = min(x0i, B.width_i + 1 - xb);
+    if (x1i <= x0i + 1) {
+        const float xmf = 0.5f * (xa + xn) - x0_floor;
+        const int c0 = __float2int_rn(df * (1.f - xmf));
+        sadd(row + x0i, c0);
+        sadd(row + x0i + 1, d - c0);
+        return;
     }
-    const float ylim = (float)min(B.bh, B.img_h - B.y0);
-    const float ya_all = fmaxf(y0, fmaxf(0.f, -(float)B.y0));
-    const float yb_all = fminf(y1, ylim);
-    if (!(ya_all < yb_all)) return;
-    const float dxdy = (x1 - x0) / (y1 - y0);
-    const float xmax_rel = B.width_f - (float)xb;  // the reference's `width`, relative
-    const int r0 = (int)floorf(ya_all);
-    const int r1 = (int)ceilf(yb_all);
-    for (int r = max(r0, 0); r < min(r1, B.bh); ++r) {
-        const float ya = fmaxf(ya_all, (float)r);
-        const float yb = fminf(yb_all, (float)(r + 1));
-        if (!(ya < yb)) continue;
-        const float dy = yb - ya;
-        const float d = dir * dy;
-        const float xa = fmaf(ya - y0, dxdy, x0);
-        const float xn = fmaf(yb - y0, dxdy, x0);
-        // in the reference x walks from the lower y end: mean is symmetric
-        const float xlo = fminf(xa, xn), xhi = fmaxf(xa, xn);
-        const float x0_floor = fmaxf(floorf(xlo), -(float)xb);
-        int x0i = (int)x0_floor;
-        const float x1_ceil = fminf(ceilf(xhi), xmax_rel);
-        int x1i = (int)x1_ceil;
-        float* row = B.acc + r * B.stride + xb;
-        x0i = min(x0i, B.width_i + 1 - xb);
-        if (x1i <= x0i + 1) {
-            const float xmf = 0.5f * (xa + xn) - x0_floor;
-            sadd(row + x0i, d * (1.f - xmf));
-            sadd(row + x0i + 1, d * xmf);
-        } else {
-            const float s = 1.f / (xhi - xlo);
-            const float x0f = xlo - x0_floor;
-            const float x1f = xhi - x1_ceil + 1.f;
-            const float a0 = 0.5f * s * (1.f - x0f) * (1.f - x0f);
-            const float am = 0.5f * s * x1f * x1f;
-            sadd(row + x0i, d * a0);
-            if (x1i == x0i + 2) {
-                sadd(row + x0i + 1, d * (1.f - a0 - am));
-            } else {
-                const float a1 = s * (1.5f - x0f);
-                sadd(row + x0i + 1, d * (a1 - a0));
-                const float ds_ = d * s;
-                for (int xi = x0i + 2; xi < x1i - 1; ++xi) sadd(row + xi, ds_);
-                const float a2 = a1 + (float)(x1i - x0i - 3) * s;
-                sadd(row + x1i - 1, d * (1.f - a2 - am));
-            }
-            sadd(row + x1i, d * am);
-        }
+    const float s = 1.f / (xhi - xlo);
+    const float x0f = xlo - x0_floor;
+    const float x1f = xhi - x1_ceil + 1.f;
+    const float a0 = 0.5f * s * (1.f - x0f) * (1.f - x0f);
+    const float am = 0.5f * s * x1f * x1f;
+    const int c0 = __float2int_rn(df * a0);
+    const int cm = __float2int_rn(df * am);
+    sadd(row + x0i, c0);
+    if (x1i == x0i + 2) {
+        sadd(row + x0i + 1, d - c0 - cm);
+    } else {
+        const float a1 = s * (1.5f - x0f);
+        const int c1 = __float2int_rn(df * (a1 - a0));
+        sadd(row + x0i + 1, c1);
+        const int cs = __float2int_rn(df * s);
+        for (int xi = x0i + 2; xi < x1i - 1; ++xi) sadd(row + xi, cs);
+        const int n_mid = max(x1i - x0i - 3, 0);
+        sadd(row + x1i - 1, d - c0 - cm - c1 - n_mid * cs);
+    }
+    sadd(row + x1i, cm);
+}
+
+// A short line piece (a few px each way) already clipped by the x rules: x in
+// FP32 relative to column xb, y band-relative in fixed point.  Walks its rows
+// like signed_difference_line (src/rasterize.rs:405-469); the row crossings
+// are interpolated from the exact fixed-point heights.
+__device__ inline void accumulate_piece(const Band& B, int xb, float x0, int32_t q0, float x1, int32_t q1) {
+    if (q0 == q1) return;  // no signed coverage (the reference skips |dy| < EPSILON)
+    int dir = 1;
+    if (q0 > q1) {
+        const float t = x0; x0 = x1; x1 = t;
+        const int32_t u = q0; q0 = q1; q1 = u;
+        dir = -1;
+    }
+    const int row_lo = max(0, -B.y0);
+    const int row_hi = min(B.bh, B.img_h - B.y0);
+    const int32_t qa_all = max(q0, row_lo << COV_SHIFT);
+    const int32_t qb_all = min(q1, row_hi << COV_SHIFT);
+    if (!(qa_all < qb_all)) return;
+    const float dxq = (x1 - x0) / (float)(q1 - q0);  // px per fixed-point unit of height
+    const int r0 = qa_all >> COV_SHIFT;
+    const int r1 = (qb_all + COV_ONE - 1) >> COV_SHIFT;
+    for (int r = r0; r < r1; ++r) {
+        const int32_t qa = max(qa_all, r << COV_SHIFT);
+        const int32_t qb = min(qb_all, (r + 1) << COV_SHIFT);
+        if (!(qa < qb)) continue;
+        const float xa = qa == q0 ? x0 : fmaf((float)(qa - q0), dxq, x0);
+        const float xn = qb == q1 ? x1 : fmaf((float)(qb - q0), dxq, x0);
+        accumulate_row(B, r, xb, xa, xn, dir * (qb - qa));
+    }
+}
+
+// A long piece: x absolute in binary64, y band-relative in fixed point.  The
+// row crossings are interpolated in binary64 and every row is handed to the
+// FP32 distribution relative to its own integer column.
+static __device__ __noinline__ void accumulate_piece_long(const Band& B, double x0, int32_t q0, double x1,
+                                                          int32_t q1) {
+    if (q0 == q1) return;
+    int dir = 1;
+    if (q0 > q1) {
+        const double t = x0; x0 = x1; x1 = t;
+        const int32_t u = q0; q0 = q1; q1 = u;
+        dir = -1;
+    }
+    const int row_lo = max(0, -B.y0);
+    const int row_hi = min(B.bh, B.img_h - B.y0);
+    const int32_t qa_all = max(q0, row_lo << COV_SHIFT);
+    const int32_t qb_all = min(q1, row_hi << COV_SHIFT);
+    if (!(qa_all < qb_all)) return;
+    const double dxq = (x1 - x0) / (double)(q1 - q0);
+    const int r0 = qa_all >> COV_SHIFT;
+    const int r1 = (qb_all + COV_ONE - 1) >> COV_SHIFT;
+    for (int r = r0; r < r1; ++r) {
+        const int32_t qa = max(qa_all, r << COV_SHIFT);
+        const int32_t qb = min(qb_all, (r + 1) << COV_SHIFT);
+        if (!(qa < qb)) continue;
+        const double xa = qa == q0 ? x0 : x0 + (double)(qa - q0) * dxq;
+        const double xn = qb == q1 ? x1 : x0 + (double)(qb - q0) * dxq;
+        const int col = (int)floor(fmin(xa, xn));
+        accumulate_row(B, r, col, (float)(xa - col), (float)(xn - col), dir * (qb - qa));
     }
 }
 
 // Piece of a line after the x rules, in binary64 (x absolute, y relative to
 // the band).  Clips it to the band's rows (a pure geometric clip, so the area
-// inside is unchanged) and hands a short FP32 copy to accumulate_piece with x
-// relative to an integer column near the piece.
+// inside is unchanged), quantises y (COV_ONE per row) and dispatches it.
 __device__ inline void accumulate_piece64(const Band& B, double x0, double y0, double x1, double y1) {
     if (y0 == y1) return;
     const double lo = fmax(-1.0, -(double)B.y0 - 1.0);
@@ -415,14 +452,19 @@ __device__ inline void accumulate_piece64(const Band& B, double x0, double y0, d
         if (y1 < lo) { x1 = x0 + (lo - y0) * dxdy; y1 = lo; }
         else if (y1 > hi) { x1 = x0 + (hi - y0) * dxdy; y1 = hi; }
     }
-    const int xb = (int)floor(fmin(x0, x1));
-    accumulate_piece(B, xb, (float)(x0 - xb), (float)y0, (float)(x1 - xb), (float)y1);
+    const int32_t q0 = __double2int_rn(y0 * 4194304.0), q1 = __double2int_rn(y1 * 4194304.0);
+    if (fabs(x1 - x0) <= 4.0 && abs(q1 - q0) <= (4 << COV_SHIFT)) {
+        const int xb = (int)floor(fmin(x0, x1));
+        accumulate_piece(B, xb, (float)(x0 - xb), q0, (float)(x1 - xb), q1);
+    } else {
+        accumulate_piece_long(B, x0, q0, x1, q1);
+    }
 }
 
 // A flattened line in binary64 (x absolute, y relative to the band): applies
 // the reference's right-edge rule (src/rasterize.rs:372-387) and
 // split_at_zero_x (:923-937), then accumulates the pieces.
-__device__ __noinline__ void accumulate_line64(const Band& B, double ax, double ay, double bx, double by) {
+static __device__ __noinline__ void accumulate_line64(const Band& B, double ax, double ay, double bx, double by) {
     const double width = (double)B.width_i;
     if (ax > width || bx > width) {
         if (ax > width && bx > width) {
@@ -452,20 +494,36 @@ __device__ __noinline__ void accumulate_line64(const Band& B, double ax, double 
     }
 }
 
-// A short line given relative to integer column xb (y relative to the band):
-// stays in FP32 unless an x rule applies or it is long, then takes the
-// binary64 route.
-__device__ __forceinline__ void accumulate_line(const Band& B, int xb, float x0, float y0, float x1, float y1) {
-    const float xlo = (float)xb + fminf(x0, x1), xhi = (float)xb + fmaxf(x0, x1);
-    if (xlo > 0.01f && xhi < B.width_f - 0.01f && fabsf(x1 - x0) <= 64.f && fabsf(y1 - y0) <= 64.f) {
-        accumulate_piece(B, xb, x0, y0, x1, y1);
-    } else {
-        accumulate_line64(B, (double)xb + (double)x0, (double)y0, (double)xb + (double)x1, (double)y1);
+// A flattened line vertex: integer column and band-relative row plus FP32
+// fractions (a few px at most).  Both ends of every line go through the same
+// quantisation, so a vertex shared by two lines gets one fixed-point height.
+struct VtxQ {
+    int32_t col, row;
+    float fx, fy;
+};
+
+// Line between two vertices.  Short lines away from the x rules stay in FP32
+// with exact fixed-point heights; the rest take the binary64 route, which
+// quantises the same vertex to the same height.
+__device__ __forceinline__ void accumulate_vtx(const Band& B, const VtxQ& a, const VtxQ& b) {
+    const int dc = b.col - a.col, dr = b.row - a.row;
+    if (abs(dc) <= 3 && abs(dr) <= 3) {
+        if (a.row < -8 || a.row > B.bh + 8) return;  // wholly outside the band's rows
+        const float x0 = a.fx, x1 = (float)dc + b.fx;
+        const float xlo = (float)a.col + fminf(x0, x1), xhi = (float)a.col + fmaxf(x0, x1);
+        if (xlo > 0.01f && xhi < B.width_f - 0.01f) {
+            const int32_t q0 = a.row * COV_ONE + __float2int_rn(a.fy * COV_ONE_F);
+            const int32_t q1 = b.row * COV_ONE + __float2int_rn(b.fy * COV_ONE_F);
+            accumulate_piece(B, a.col, x0, q0, x1, q1);
+            return;
+        }
     }
+    accumulate_line64(B, (double)a.col + (double)a.fx, (double)a.row + (double)a.fy, (double)b.col + (double)b.fx,
+                      (double)b.row + (double)b.fy);
 }
 
 // ---------------------------------------------------------------------------
-// Row prefix sum (two-sum compensated warp scan) + fill rule
+// Row prefix sum (exact integer) + fill rule
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     s = a + b;
@@ -482,6 +540,388 @@ __device__ __forceinline__ float alpha_from_winding(int rule, float w) {
     }
     const float v = fabsf(w);
     return v >= 1.f ? 1.f : (v < 1e-6f ? 0.f : v);
+}
+
+// FillRule::alpha_from_winding on a fixed-point winding (COV_ONE per unit):
+// EvenOdd's |((w + 1) rem_euclid 2) - 1| is exact with a mask.
+__device__ __forceinline__ float alpha_from_winding_fix(int rule, int32_t w) {
+    if (rule == 1) {
+        const int32_t r = (int32_t)(((uint32_t)w + (1u << 22)) & ((1u << 23) - 1u));
+        return (float)abs(r - (1 << 22)) * (1.0f / 4194304.0f);
+    }
+    const float v = fabsf((float)w * (1.0f / 4194304.0f));
+    return v >= 1.f ? 1.f : (v < 1e-6f ? 0.f : v);
+}
+
+// The x rules of signed_difference_line (src/rasterize.rs:372-393) on a
+// binary64 line: the part beyond `width` is dropped (a line entirely beyond
+// becomes vertical at width - 0.001), then split_at_zero_x
+// (src/rasterize.rs:923-937) turns the x < 0 part into a vertical line at 0.
+// Returns the number of pieces (0..2); piece i is (px[i][0], py[i][0]) ->
+// (px[i][1], py[i][1]).
+__device__ inline int clip_line_x64(double width, double ax, double ay, double bx, double by, double (&px)[2][2],
+                                    double (&py)[2][2]) {
+    if (ax > width || bx > width) {
+        if (ax > width && bx > width) {
+            ax = width - 0.001;
+            bx = width - 0.001;
+        } else {
+            const double t = (ax - width) / (ax - bx);
+            const double my = (1.0 - t) * ay + t * by;
+            if (ax < width) { bx = width; by = my; }
+            else { ax = width; ay = my; }
+        }
+    }
+    if (ax >= 0.0 && bx >= 0.0) {
+        px[0][0] = ax; py[0][0] = ay; px[0][1] = bx; py[0][1] = by;
+        return 1;
+    }
+    if (ax <= 0.0 && bx <= 0.0) {
+        px[0][0] = 0.0; py[0][0] = ay; px[0][1] = 0.0; py[0][1] = by;
+        return 1;
+    }
+    const double t = ax / (ax - bx);
+    const double mx = (1.0 - t) * ax + t * bx, my = (1.0 - t) * ay + t * by;
+    if (ax < 0.0) {
+        px[0][0] = mx; py[0][0] = my; px[0][1] = bx; py[0][1] = by;
+        px[1][0] = 0.0; py[1][0] = ay; px[1][1] = mx; py[1][1] = my;
+    } else {
+        px[0][0] = ax; py[0][0] = ay; px[0][1] = mx; py[0][1] = my;
+        px[1][0] = mx; py[1][0] = my; px[1][1] = 0.0; py[1][1] = by;
+    }
+    return 2;
+}
+
+// Pure geometric clip of a piece to rows [lo, hi] (the area inside is
+// unchanged); false when nothing is left.
+__device__ inline bool clip_y64(double lo, double hi, double (&x)[2], double (&y)[2]) {
+    const double ymin = fmin(y[0], y[1]), ymax = fmax(y[0], y[1]);
+    if (ymax <= lo || ymin >= hi || y[0] == y[1]) return false;
+    if (ymin < lo || ymax > hi) {
+        const double dxdy = (x[1] - x[0]) / (y[1] - y[0]);
+        const double x0 = x[0], y0 = y[0];
+        for (int i = 0; i < 2; ++i) {
+            if (y[i] < lo) { x[i] = x0 + (lo - y0) * dxdy; y[i] = lo; }
+            else if (y[i] > hi) { x[i] = x0 + (hi - y0) * dxdy; y[i] = hi; }
+        }
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Row prefix of a band (signed differences -> winding) and fill rule
+// (src/rasterize.rs:473-507), in exact fixed-point integer arithmetic.
+// Every thread owns 16-pixel chunks:
+// 1) in-place inclusive prefix of each chunk, chunk totals to `tot`;
+// 2) per row, exclusive scan of the chunk totals (warp shuffles);
+// 3) base + chunk prefix -> fill rule -> epi(row, x0, alpha[16]).
+// `tot` holds at least rows * ceil(width / 16) floats; the band stride is a
+// multiple of 16 (band_stride), so chunk reads stay inside their row.
+// ---------------------------------------------------------------------------
+constexpr int kScanChunk = 16;
+
+template <int THREADS, class Epi>
+__device__ void band_scan(const Band& B, int width, int rule, float* tot_f, const Epi& epi) {
+    int32_t* tot = reinterpret_cast<int32_t*>(tot_f);
+    const int W = width;
+    const int cr = (W + kScanChunk - 1) / kScanChunk;  // chunks per row
+    const int nc = cr * B.bh;
+    for (int c = threadIdx.x; c < nc; c += THREADS) {
+        const int r = c / cr, x0 = (c - r * cr) * kScanChunk;
+        int4* row4 = reinterpret_cast<int4*>(B.acc + r * B.stride + x0);
+        uint32_t run = 0;
+        #pragma unroll
+        for (int q = 0; q < kScanChunk / 4; ++q) {
+            const int4 v = row4[q];
+            const int x = x0 + 4 * q;
+            uint4 u;  // unsigned: the winding wraps by design
+            u.x = (x < W ? (uint32_t)v.x : 0u) + run;
+            u.y = (x + 1 < W ? (uint32_t)v.y : 0u) + u.x;
+            u.z = (x + 2 < W ? (uint32_t)v.z : 0u) + u.y;
+            u.w = (x + 3 < W ? (uint32_t)v.w : 0u) + u.z;
+            run = u.w;
+            row4[q] = make_int4((int)u.x, (int)u.y, (int)u.z, (int)u.w);
+        }
+        tot[c] = (int32_t)run;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    for (int r = threadIdx.x >> 5; r < B.bh; r += THREADS / 32) {
+        uint32_t carry = 0;
+        for (int q0 = 0; q0 < cr; q0 += 32) {
+            const int q = q0 + lane;
+            const uint32_t v = q < cr ? (uint32_t)tot[r * cr + q] : 0u;
+            uint32_t incl = v;
+            #pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t o = __shfl_up_sync(0xffffffffu, incl, off);
+                if (lane >= off) incl += o;
+            }
+            if (q < cr) tot[r * cr + q] = (int32_t)(carry + incl - v);  // exclusive base of the chunk
+            carry += __shfl_sync(0xffffffffu, incl, 31);
+        }
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < nc; c += THREADS) {
+        const int r = c / cr, x0 = (c - r * cr) * kScanChunk;
+        const uint32_t base = (uint32_t)tot[c];
+        const int4* row4 = reinterpret_cast<const int4*>(B.acc + r * B.stride + x0);
+        float a[kScanChunk];
+        #pragma unroll
+        for (int q = 0; q < kScanChunk / 4; ++q) {
+            const int4 v = row4[q];
+            a[4 * q] = alpha_from_winding_fix(rule, (int32_t)(base + (uint32_t)v.x));
+            a[4 * q + 1] = alpha_from_winding_fix(rule, (int32_t)(base + (uint32_t)v.y));
+            a[4 * q + 2] = alpha_from_winding_fix(rule, (int32_t)(base + (uint32_t)v.z));
+            a[4 * q + 3] = alpha_from_winding_fix(rule, (int32_t)(base + (uint32_t)v.w));
+        }
+        epi(r, x0, a);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Segment records shared by the band kernel and the line pipeline
+// ---------------------------------------------------------------------------
+struct SegRec {
+    int32_t xb, yb;  // record origin: integer column and row of P0 (image frame)
+    int8_t anchor;   // anchor level a: vertices are B(m / 2^a) exactly plus an FP32 remainder
+    int8_t scale;    // k: coordinates are integers in units of 2^-k px (16..24)
+    int16_t kind;
+    int32_t p0x, p0y, pnx, pny;           // end points relative to (xb, yb)
+    int32_t d1x, d1y, d2x, d2y, d3x, d3y;  // control point differences
+    float mag;                            // max |absolute coordinate|, px (binary64 chain error term)
+    uint32_t src;                         // input segment, for binary64 re-decisions (~0: a line)
+};
+
+// Power-basis coefficients in px: B(t) - P0 = t (c1 + t (c2 + t c3)).  For a
+// cubic c2 and c3 are also the flatness coefficients a2 and a3; for a quad c2
+// is P0 - 2 P1 + P2.
+__device__ __forceinline__ void rec_coefs(const SegRec& r, int kind, float& c1x, float& c1y, float& c2x, float& c2y,
+                                          float& c3x, float& c3y) {
+    const float u = pow2f(-r.scale);
+    const float d1x = (float)r.d1x * u, d1y = (float)r.d1y * u;
+    const float d2x = (float)r.d2x * u, d2y = (float)r.d2y * u;
+    const float d3x = (float)r.d3x * u, d3y = (float)r.d3y * u;
+    if (kind == SEG_CUBIC) {
+        c1x = 3.f * d1x; c1y = 3.f * d1y;
+        c2x = 3.f * (d2x - d1x); c2y = 3.f * (d2y - d1y);
+        c3x = (d1x - 2.f * d2x) + d3x; c3y = (d1y - 2.f * d2y) + d3y;
+    } else if (kind == SEG_QUAD) {
+        c1x = 2.f * d1x; c1y = 2.f * d1y;
+        c2x = d2x - d1x; c2y = d2y - d1y;
+        c3x = c3y = 0.f;
+    } else {
+        c1x = d1x; c1y = d1y;
+        c2x = c2y = c3x = c3y = 0.f;
+    }
+}
+
+// Decision coefficients of a record and the bound of their error against the
+// binary64 control points (quantisation 2^-(k+1) px per coordinate, plus FP32
+// rounding).
+__device__ __forceinline__ FlatCoef rec_flat(const SegRec& r, float& qerr) {
+    float c1x, c1y, c2x, c2y, c3x, c3y;
+    rec_coefs(r, r.kind, c1x, c1y, c2x, c2y, c3x, c3y);
+    FlatCoef c;
+    c.a2x = c2x; c.a2y = c2y; c.a3x = c3x; c.a3y = c3y;
+    c.mag = r.mag;
+    const float u = pow2f(-r.scale);
+    const float sx = fabsf((float)r.d1x) + fabsf((float)r.d2x) + fabsf((float)r.d3x);
+    const float sy = fabsf((float)r.d1y) + fabsf((float)r.d2y) + fabsf((float)r.d3y);
+    qerr = fmaxf(sx, sy) * u * pow2f(-19) + 6.f * u;
+    return c;
+}
+
+// Control hull of a fixed-point segment against rows [y0 - 1, y0 + rows + 1).
+__device__ __forceinline__ bool hull_meets_rows(const FixSeg& s, int y0, int rows) {
+    int32_t ymin = s.y[0], ymax = s.y[0];
+    #pragma unroll
+    for (int i = 1; i < 4; ++i) {
+        if (i < seg_npts(s.kind)) {
+            ymin = min(ymin, s.y[i]);
+            ymax = max(ymax, s.y[i]);
+        }
+    }
+    const int32_t oy = y0 << 16;  // image heights are limited to 16383 rows
+    return !(ymax < oy - 65536 || ymin > oy + ((rows + 1) << 16));
+}
+
+// x * 2^k rounded half-even, integer instructions only; |x| < 16384 (checked
+// by d2fix), k <= 24.
+__device__ __forceinline__ long long d2fix_k(double x, int k) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((bits >> 52) & 0x7ffull);
+    if (e == 0) return 0;
+    const unsigned long long mant = (bits & 0xfffffffffffffull) | (1ull << 52);
+    const int sh = 1075 - k - e;  // x * 2^k = mant * 2^-sh
+    unsigned long long q;
+    if (sh >= 64) {
+        q = 0;
+    } else if (sh <= 0) {
+        q = mant << (-sh);
+    } else {
+        q = mant >> sh;
+        const unsigned long long rem = mant - (q << sh);
+        const unsigned long long half = 1ull << (sh - 1);
+        if (rem > half || (rem == half && (q & 1ull))) ++q;
+    }
+    return (bits >> 63) ? -(long long)q : (long long)q;
+}
+
+// Record of a segment inside the 16.16 range: binary64 control points `sx`,
+// `sy` (after the transform) and their 16.16 copy `s`.  Coordinates are
+// re-quantised relative to the integer origin at P0 with the finest scale
+// 2^-k that keeps every difference in int32 (2^-24 px for segments up to
+// ~60 px), so the vertices stay within ~1e-7 px of the binary64 curve.
+__device__ inline void make_record(const FixSeg& s, const double (&sx)[4], const double (&sy)[4], SegRec& r) {
+    const int n = seg_npts(s.kind);
+    const int32_t xb = s.x[0] >> 16, yb = s.y[0] >> 16;  // floor
+    int32_t ext16 = 0, mx = 0;
+    #pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        if (i < n) {
+            ext16 = max(ext16, max(abs(s.x[i] - (xb << 16)), abs(s.y[i] - (yb << 16))));
+            mx = max(mx, max(abs(s.x[i]), abs(s.y[i])));
+        }
+    }
+    // 2 * extent * 2^k < 2^31
+    const int bits = 32 - __clz(ext16 + 65536);
+    const int k = min(24, max(16, 46 - bits));
+    long long X[4], Y[4];
+    #pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        X[i] = i < n ? d2fix_k(sx[i], k) : 0;
+        Y[i] = i < n ? d2fix_k(sy[i], k) : 0;
+    }
+    const long long ox = (long long)xb << k, oy = (long long)yb << k;
+    const long long xn = n == 2 ? X[1] : (n == 3 ? X[2] : X[3]);
+    const long long yn = n == 2 ? Y[1] : (n == 3 ? Y[2] : Y[3]);
+    r.xb = xb;
+    r.yb = yb;
+    r.scale = (int8_t)k;
+    r.p0x = (int32_t)(X[0] - ox);
+    r.p0y = (int32_t)(Y[0] - oy);
+    r.pnx = (int32_t)(xn - ox);
+    r.pny = (int32_t)(yn - oy);
+    r.d1x = (int32_t)(X[1] - X[0]);
+    r.d1y = (int32_t)(Y[1] - Y[0]);
+    r.d2x = n > 2 ? (int32_t)(X[2] - X[1]) : 0;
+    r.d2y = n > 2 ? (int32_t)(Y[2] - Y[1]) : 0;
+    r.d3x = n > 3 ? (int32_t)(X[3] - X[2]) : 0;
+    r.d3y = n > 3 ? (int32_t)(Y[3] - Y[2]) : 0;
+    r.kind = (int16_t)s.kind;
+    float c1x, c1y, c2x, c2y, c3x, c3y;
+    rec_coefs(r, s.kind, c1x, c1y, c2x, c2y, c3x, c3y);
+    // Anchor level: sub-curves over 2^-a of the parameter span stay below ~2 px,
+    // so the FP32 remainder keeps ~1e-7 px.  Lines need no anchors (t is 0 or 1).
+    // a <= 9 keeps the integer evaluation below 2^62.
+    const float ext = fmaxf(fabsf(c1x) + fabsf(c2x) + fabsf(c3x), fabsf(c1y) + fabsf(c2y) + fabsf(c3y));
+    int a = 0;
+    if (s.kind != SEG_LINE) {
+        while (a < 9 && ext * pow2f(-a) > 2.f) ++a;
+    }
+    r.mag = (float)mx * FIX_ONE_INV;
+    r.anchor = (int8_t)a;
+}
+
+// Vertex at t = j / 2^d as an exact integer point I (units 2^-k, relative to
+// the record's origin) plus an FP32 remainder R in px.  The anchor depends on
+// t only, so two leaves sharing a vertex compute it identically.
+__device__ __forceinline__ void rec_vertex(const SegRec& r, uint32_t j, int d, int32_t& ix, int32_t& iy, float& rx,
+                                           float& ry) {
+    if (j == 0) {
+        ix = r.p0x; iy = r.p0y; rx = ry = 0.f;
+        return;
+    }
+    if ((j >> d) != 0u) {
+        ix = r.pnx; iy = r.pny; rx = ry = 0.f;
+        return;
+    }
+    const int a = r.anchor;
+    float c1x, c1y, c2x, c2y, c3x, c3y;
+    rec_coefs(r, r.kind, c1x, c1y, c2x, c2y, c3x, c3y);
+    if (a == 0) {
+        const float t = (float)j * pow2f(-d);
+        ix = r.p0x; iy = r.p0y;
+        rx = t * fmaf(t, fmaf(t, c3x, c2x), c1x);
+        ry = t * fmaf(t, fmaf(t, c3y, c2y), c1y);
+        return;
+    }
+    // anchor m / 2^a <= t, exact B(m / 2^a) from integer power-basis coefficients
+    const uint32_t m = d >= a ? (j >> (d - a)) : (j << (a - d));
+    const uint32_t jm = d >= a ? (m << (d - a)) : j;
+    const long long mm = (long long)m;
+    // integer power basis: B(t) - P0 = t (k1 + t (k2 + t k3)) in units of 2^-k
+    long long k1x, k1y, k2x, k2y, k3x, k3y;
+    if (r.kind == SEG_CUBIC) {
+        k1x = 3ll * r.d1x; k1y = 3ll * r.d1y;
+        k2x = 3ll * ((long long)r.d2x - r.d1x); k2y = 3ll * ((long long)r.d2y - r.d1y);
+        k3x = (long long)r.d1x - 2ll * r.d2x + r.d3x; k3y = (long long)r.d1y - 2ll * r.d2y + r.d3y;
+    } else {  // quad (lines never reach here: their vertices are end points)
+        k1x = 2ll * r.d1x; k1y = 2ll * r.d1y;
+        k2x = (long long)r.d2x - r.d1x; k2y = (long long)r.d2y - r.d1y;
+        k3x = k3y = 0;
+    }
+    const long long s1 = 1ll << a, s2 = 1ll << (2 * a);
+    const long long nx = ((k3x * mm + k2x * s1) * mm + k1x * s2) * mm;
+    const long long ny = ((k3y * mm + k2y * s1) * mm + k1y * s2) * mm;
+    const int sh = 3 * a;
+    const long long half = 1ll << (sh - 1);
+    const long long qx = (nx + half) >> sh, qy = (ny + half) >> sh;
+    ix = r.p0x + (int32_t)qx;
+    iy = r.p0y + (int32_t)qy;
+    // the rounding of the anchor (|.| <= 2^(sh-1), an int32), carried in the remainder
+    const float ru = pow2f(-(r.scale + sh));
+    rx = (float)(int32_t)(nx - qx * (1ll << sh)) * ru;
+    ry = (float)(int32_t)(ny - qy * (1ll << sh)) * ru;
+    if (jm == j) return;
+    // remainder over dt = t - m / 2^a with the local power basis at tA
+    const float tA = (float)m * pow2f(-a);
+    const float dt = (float)(j - jm) * pow2f(-d);
+    const float b1x = fmaf(tA, fmaf(3.f * tA, c3x, 2.f * c2x), c1x);
+    const float b1y = fmaf(tA, fmaf(3.f * tA, c3y, 2.f * c2y), c1y);
+    const float b2x = fmaf(3.f * tA, c3x, c2x), b2y = fmaf(3.f * tA, c3y, c2y);
+    rx += dt * fmaf(dt, fmaf(dt, c3x, b2x), b1x);
+    ry += dt * fmaf(dt, fmaf(dt, c3y, b2y), b1y);
+}
+
+// Vertex of a record as an integer column / row (row relative to `row0`)
+// plus FP32 fractions.
+__device__ __forceinline__ VtxQ rec_vtx(const SegRec& r, uint32_t j, int d, int row0) {
+    int32_t ix, iy;
+    float rx, ry;
+    rec_vertex(r, j, d, ix, iy, rx, ry);
+    const int k = r.scale;
+    const int32_t mask = (1 << k) - 1;
+    const float u = pow2f(-k);
+    VtxQ v;
+    v.col = r.xb + (ix >> k);
+    v.row = r.yb + (iy >> k) - row0;
+    v.fx = fmaf((float)(ix & mask), u, rx);
+    v.fy = fmaf((float)(iy & mask), u, ry);
+    return v;
+}
+
+// Reference decision for node (d, k) of a record: FP32 with a rigorous bound,
+// binary64 replay of the split chain when too close to call.  `pts` and
+// `trm` give the record's binary64 source segment.
+__device__ __forceinline__ int decide_node(const SegRec& r, const FlatCoef& c, float qerr, int d, uint32_t k,
+                                           float thr32, double thr64, const double* pts, const double* trm,
+                                           int& fallbacks) {
+    if (r.kind == SEG_LINE) return 1;
+    const int v = decide_fp32(r.kind, c, d, k, thr32, qerr);
+    if (v >= 0) return v;
+    Seg64 S;
+    S.kind = r.kind;
+    const double* p = pts + 8ull * r.src;
+    #pragma unroll
+    for (int j = 0; j < 4; ++j) { S.x[j] = p[2 * j]; S.y[j] = p[2 * j + 1]; }
+    if (trm) {
+        #pragma unroll
+        for (int j = 0; j < 4; ++j) tr_apply64(trm, S.x[j], S.y[j], S.x[j], S.y[j]);
+    }
+    ++fallbacks;
+    return flatness_chain64(S, d, k) < thr64 ? 1 : 0;
 }
 
 }  // namespace rz

@@ -117,7 +117,7 @@ RZ_API rz_status rz_mask_batch_noalloc(const rz_path_batch* batch, double flatne
         m.clip_width = (int32_t)d.width - 1;
         if (m.width <= 0 || m.height <= 0) continue;
         const int stride = rz::band_stride(m.clip_width);
-        const int rows = std::min(std::max(1, rz::band_floats() / stride), m.height);
+        const int rows = std::min(std::min(256, std::max(1, rz::band_floats() / stride)), m.height);
         for (int y = 0; y < m.height; y += rows) {
             if (n_items >= kMaxItems) return RZ_ERR_CAPACITY;
             h_items[n_items].path = p;

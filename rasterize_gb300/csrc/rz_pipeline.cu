@@ -1,0 +1,603 @@
+// rz_pipeline.cu -- line pipeline for large paths and painted scenes.
+//
+// k_flatten_count / k_flatten_emit flatten every segment slot (segments, then
+// one closing line per subpath) with the reference's exact bisection tree
+// (FP32 decisions, binary64 replays) into 16.16 lines in the fill's local
+// frame; the emit pass also counts lines per (fill, band).  k_bin_scatter
+// lists each band's lines per fill (a counting sort keyed by (fill, band)),
+// and k_composite renders one canvas row band per CTA: for every fill in
+// order it accumulates the fill's lines in shared memory, scans the rows,
+// applies the fill rule and blends the fill's paint source-over into an RGBA
+// band kept in shared memory (Rasterizer::fill + Pipeline::render_rec,
+// src/rasterize.rs:69-115, src/scene.rs:407-435).
+#include "rz_device.cuh"
+#include "rz_kernels.cuh"
+#include "rz_pipeline.cuh"
+
+namespace rz {
+
+__device__ __forceinline__ void pset_err(int32_t* err, int code) { atomicCAS(err, 0, code); }
+
+// Fill owning flatten slot s (fills are in slot order).
+__device__ __forceinline__ uint32_t fill_of_slot(const SceneDev& S, uint32_t s) {
+    uint32_t lo = 0, hi = S.n_fills;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (S.fills[mid].slot0 <= s) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// Loads the binary64 segment of slot s (untransformed); false for an empty
+// closing line (empty subpath).  Closing line: Line(subpath.end(), subpath.start()).
+__device__ bool slot_segment(const SceneDev& S, const FillDev& f, uint32_t s, Seg64& g, uint32_t& src) {
+    const uint32_t i = s - f.slot0;
+    const uint32_t nseg = f.seg1 - f.seg0;
+    if (i < nseg) {
+        src = f.seg0 + i;
+        g.kind = S.kind[src];
+        const double2* p2 = reinterpret_cast<const double2*>(S.pts + 8ull * src);
+        #pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const double2 q = __ldg(p2 + j);
+            g.x[j] = q.x;
+            g.y[j] = q.y;
+        }
+        return g.kind != SEG_ARC;  // scenes arrive with arcs expanded
+    }
+    const uint32_t sp = f.sub0 + (i - nseg);
+    const uint32_t s0 = S.sub_off[sp], s1 = min(S.sub_off[sp + 1], S.n_segments);
+    if (s1 <= s0) return false;
+    src = 0xffffffffu;
+    const int kl = S.kind[s1 - 1];
+    const int nl = kl == SEG_LINE ? 1 : (kl == SEG_QUAD ? 2 : 3);
+    g.kind = SEG_LINE;
+    g.x[0] = S.pts[8ull * (s1 - 1) + 2 * nl];
+    g.y[0] = S.pts[8ull * (s1 - 1) + 2 * nl + 1];
+    g.x[1] = S.pts[8ull * s0];
+    g.y[1] = S.pts[8ull * s0 + 1];
+    g.x[2] = g.y[2] = g.x[3] = g.y[3] = 0.0;
+    return true;
+}
+
+struct SlotState {
+    bool ok = false;    // a segment to flatten
+    bool fits = false;  // inside the 16.16 range
+    Seg64 g;            // binary64, transformed
+    FixSeg F;
+    SegRec r;
+    FlatCoef c;
+    float qerr = 0.f;
+};
+
+__device__ void load_slot(const SceneDev& S, const FillDev& f, uint32_t s, SlotState& st) {
+    uint32_t src = 0;
+    st.ok = slot_segment(S, f, s, st.g, src);
+    if (!st.ok) return;
+    const int n = seg_npts(st.g.kind);
+    bool nan = false, fits = true;
+    #pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (j < n) {
+            tr_apply64(f.tr, st.g.x[j], st.g.y[j], st.g.x[j], st.g.y[j]);
+            nan |= is_nan_bits(st.g.x[j]) || is_nan_bits(st.g.y[j]);
+            fits &= d2fix(st.g.x[j], st.F.x[j]) & d2fix(st.g.y[j], st.F.y[j]);
+        } else {
+            st.F.x[j] = st.F.y[j] = 0;
+        }
+    }
+    if (nan) {  // the reference panics on NaN (src/path.rs:765-767)
+        pset_err(S.err, ERR_NAN);
+        st.ok = false;
+        return;
+    }
+    st.F.kind = st.g.kind;
+    st.fits = fits;
+    if (fits) {
+        make_record(st.F, st.g.x, st.g.y, st.r);
+        st.r.src = src;
+        st.c = rec_flat(st.r, st.qerr);
+    }
+}
+
+// Leaves of the slot's tree, in order; `emit(d, k)` per leaf.  Returns false
+// on a tree deeper than MAX_DEPTH.
+template <class Emit>
+__device__ bool walk_slot(const SceneDev& S, const FillDev& f, const SlotState& st, int& fallbacks, Emit& emit) {
+    TreeWalk W;
+    W.start();
+    while (!W.done) {
+        int leaf;
+        if (st.fits) {
+            leaf = decide_node(st.r, st.c, st.qerr, W.d, W.k, S.thr32, S.thr64, S.pts, f.tr, fallbacks);
+        } else {
+            const FlatCoef c = flat_coef(st.g);
+            leaf = node_is_leaf(st.g, c, W.d, W.k, S.thr64, S.thr32, fallbacks);
+        }
+        if (!leaf) {
+            if (W.d >= MAX_DEPTH) return false;
+            ++W.d;
+            W.k <<= 1;
+            continue;
+        }
+        emit(W.d, W.k);
+        W.next_after_leaf();
+    }
+    return true;
+}
+
+struct CountLeaves {
+    uint32_t n = 0;
+    __device__ void operator()(int, uint32_t) { ++n; }
+};
+
+// A slot emits one line per leaf, or two (the reference's x rules split it)
+// when its coordinates are beyond the 16.16 range.
+__global__ void k_flatten_count(SceneDev S) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S.n_slots) return;
+    const FillDev& f = S.fills[fill_of_slot(S, s)];
+    SlotState st;
+    load_slot(S, f, s, st);
+    uint32_t n = 0;
+    int fallbacks = 0;
+    if (st.ok) {
+        CountLeaves c;
+        if (!walk_slot(S, f, st, fallbacks, c)) pset_err(S.err, ERR_DEPTH);
+        n = st.fits ? c.n : 2u * c.n;
+    }
+    S.slot_count[s] = n;
+    if (fallbacks) atomicAdd(&S.counters[1], fallbacks);
+}
+
+// Lines per (fill, band) of one local-frame line.
+__device__ __forceinline__ void count_bands(const SceneDev& S, const FillDev& f, int4 l) {
+    const int32_t ylo = min(l.y, l.w), yhi = max(l.y, l.w);
+    if (ylo == yhi) return;  // no signed coverage
+    int r0 = ylo >> 16;                 // floor
+    int r1 = (yhi + 65535) >> 16;       // ceil (exclusive)
+    r0 = max(r0, 0);
+    r1 = min(r1, f.height);
+    if (r0 >= r1) return;
+    const int b0 = (r0 + f.row0) / S.band_rows, b1 = (r1 - 1 + f.row0) / S.band_rows;
+    for (int b = max(b0, f.band0); b <= min(b1, f.band0 + f.nbands - 1); ++b)
+        atomicAdd(&S.entry_count[f.entry0 + (b - f.band0)], 1u);
+}
+
+__device__ __forceinline__ int32_t fix_add(int32_t a, float d) { return a + __float2int_rn(d * 65536.0f); }
+
+// A line end point: exact 16.16 anchor plus FP32 remainder (px).
+__device__ __forceinline__ int4 end_point(int32_t ax, int32_t ay, float dx, float dy) {
+    return make_int4(ax, ay, __float_as_int(dx), __float_as_int(dy));
+}
+
+struct EmitLines {
+    const SceneDev* S;
+    const FillDev* f;
+    const SlotState* st;
+    uint32_t out;
+    __device__ void write(int4 a, int4 b) {
+        S->lines[2ull * out] = a;
+        S->lines[2ull * out + 1] = b;
+        ++out;
+        count_bands(*S, *f, make_int4(fix_add(a.x, __int_as_float(a.z)), fix_add(a.y, __int_as_float(a.w)),
+                                      fix_add(b.x, __int_as_float(b.z)), fix_add(b.y, __int_as_float(b.w))));
+    }
+    __device__ void operator()(int d, uint32_t k) {
+        if (st->fits) {
+            // integer pixel of the vertex as the 16.16 anchor, its fraction as the remainder
+            const VtxQ a = rec_vtx(st->r, k, d, 0), b = rec_vtx(st->r, k + 1u, d, 0);
+            write(end_point(a.col << 16, a.row << 16, a.fx, a.fy), end_point(b.col << 16, b.row << 16, b.fx, b.fy));
+        } else {
+            // beyond the 16.16 range: the reference's x rules (src/rasterize.rs:372-393)
+            // and a pure y clip in binary64, then anchors + remainders
+            const Seg64& g = st->g;
+            const VertexCoef v = vertex_coef(g);
+            double x0, y0, x1, y1;
+            vertex_big(v, k, d, 0.0, x0, y0);
+            vertex_big(v, k + 1u, d, 0.0, x1, y1);
+            double px[2][2], py[2][2];
+            const int np = clip_line_x64((double)f->clip_width, x0, y0, x1, y1, px, py);
+            for (int i = 0; i < 2; ++i) {
+                int4 e0 = make_int4(0, 0, 0, 0), e1 = make_int4(0, 0, 0, 0);
+                if (i < np && clip_y64(-1.0, (double)f->height + 1.0, px[i], py[i])) {
+                    int32_t a, b2, c, e;
+                    if (d2fix(px[i][0], a) & d2fix(py[i][0], b2) & d2fix(px[i][1], c) & d2fix(py[i][1], e)) {
+                        const double u = 1.0 / 65536.0;
+                        e0 = end_point(a, b2, (float)(px[i][0] - a * u), (float)(py[i][0] - b2 * u));
+                        e1 = end_point(c, e, (float)(px[i][1] - c * u), (float)(py[i][1] - e * u));
+                    }
+                }
+                if (i < np) {
+                    write(e0, e1);
+                } else {
+                    S->lines[2ull * out] = e0;  // unused slot: a degenerate line
+                    S->lines[2ull * out + 1] = e1;
+                    ++out;
+                }
+            }
+        }
+    }
+};
+
+__global__ void k_flatten_emit(SceneDev S) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S.n_slots) return;
+    const FillDev& f = S.fills[fill_of_slot(S, s)];
+    SlotState st;
+    load_slot(S, f, s, st);
+    if (!st.ok) return;
+    int fallbacks = 0;
+    EmitLines e{&S, &f, &st, S.slot_count[s]};
+    walk_slot(S, f, st, fallbacks, e);
+}
+
+// Fill owning line l (slot_count holds the line offsets of the slots).
+__device__ __forceinline__ uint32_t fill_of_line(const SceneDev& S, uint32_t l) {
+    uint32_t lo = 0, hi = S.n_fills;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        const uint32_t first = S.fills[mid].slot0 < S.n_slots ? S.slot_count[S.fills[mid].slot0] : S.n_lines;
+        if (first <= l) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_bin_scatter(SceneDev S) {
+    const uint32_t l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= S.n_lines) return;
+    const FillDev& f = S.fills[fill_of_line(S, l)];
+    const int4 a = S.lines[2ull * l], b = S.lines[2ull * l + 1];
+    const int32_t ya = fix_add(a.y, __int_as_float(a.w)), yb = fix_add(b.y, __int_as_float(b.w));
+    const int32_t ylo = min(ya, yb), yhi = max(ya, yb);
+    if (ylo == yhi) return;
+    int r0 = max(ylo >> 16, 0);
+    int r1 = min((yhi + 65535) >> 16, f.height);
+    if (r0 >= r1) return;
+    const int b0 = (r0 + f.row0) / S.band_rows, b1 = (r1 - 1 + f.row0) / S.band_rows;
+    for (int b = max(b0, f.band0); b <= min(b1, f.band0 + f.nbands - 1); ++b) {
+        const uint32_t e = f.entry0 + (b - f.band0);
+        S.pairs[S.entry_start[e] + atomicAdd(&S.entry_cursor[e], 1u)] = l;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Paint (grad.rs, color.rs) in FP32
+// ---------------------------------------------------------------------------
+// GradSpread::at (src/grad.rs:24-30) on an FP32 offset
+__device__ __forceinline__ float spread_at(int spread, float t) {
+    if (spread == 1) {  // Repeat: rem_euclid(t, 1)
+        float r = fmodf(t, 1.f);
+        return r < 0.f ? r + 1.f : r;
+    }
+    if (spread == 2) {  // Reflect: |rem_euclid(t + 1, 2) - 1|
+        float r = fmodf(t + 1.f, 2.f);
+        if (r < 0.f) r += 2.f;
+        return fabsf(r - 1.f);
+    }
+    return t;
+}
+
+// GradSpread::at on a binary64 offset
+__device__ __forceinline__ float spread_at64(int spread, double t) {
+    if (spread == 1) {
+        const double r = fmod(t, 1.0);
+        return (float)(r < 0.0 ? r + 1.0 : r);
+    }
+    if (spread == 2) {
+        double r = fmod(t + 1.0, 2.0);
+        if (r < 0.0) r += 2.0;
+        return (float)fabs(r - 1.0);
+    }
+    return (float)t;
+}
+
+// GradSpread::at on a double-float offset th + tl (|tl| <= ulp(th)).  The
+// period is removed from th exactly (x - k * period is exact for the k
+// nearest below), so the fraction keeps the low word: repeat and reflect stay
+// accurate however many periods away the pixel is.
+__device__ __forceinline__ float spread_at_df(int spread, float th, float tl) {
+    if (spread == 0) return th + tl;
+    const float period = spread == 1 ? 1.f : 2.f;
+    const float k = floorf(th * (1.f / period)) * period;
+    float r = __fadd_rn(th, -k) + tl;
+    if (r < 0.f) r += period;
+    else if (r >= period) r -= period;
+    if (spread == 1) return r;
+    return r < 1.f ? r : 2.f - r;  // |((t + 1) rem 2) - 1| with r = t rem 2
+}
+
+// Offset of a linear gradient: g0 x + g1 y + g2 in double-float arithmetic
+// (x, y are pixel centres, exact in FP32; products split with an FMA).
+__device__ __forceinline__ float linear_offset(const PaintDev& p, float x, float y) {
+    const float p0 = __fmul_rn(p.gh[0], x), e0 = fmaf(p.gh[0], x, -p0);
+    const float p1 = __fmul_rn(p.gh[1], y), e1 = fmaf(p.gh[1], y, -p1);
+    float s, es, t, et;
+    two_sum(p0, p1, s, es);
+    two_sum(s, p.gh[2], t, et);
+    const float lo = ((e0 + e1) + (es + et)) + fmaf(p.gl[0], x, fmaf(p.gl[1], y, p.gl[2]));
+    const float th = __fadd_rn(t, lo);
+    const float tl = lo - __fadd_rn(th, -t);
+    return spread_at_df(p.spread, th, tl);
+}
+
+// GradRadial::offset (src/grad.rs:361-396) with quadratic_solve
+// (src/utils.rs:205-231) in binary64; false when there is no root.
+static __device__ __noinline__ bool radial_offset64(const PaintDev& p, float px, float py, double& t) {
+    const double pdx = (double)px * p.qd[0] + (double)py * p.qd[1] + p.qd[2];
+    const double pdy = (double)px * p.qd[3] + (double)py * p.qd[4] + p.qd[5];
+    const double a = p.a64;
+    const double b = -2.0 * ((p.cdxd * pdx + p.cdyd * pdy) + p.frd * p.rdd);
+    const double c = (pdx * pdx + pdy * pdy) - p.frd * p.frd;
+    const double eps = 2.220446049250313e-16;
+    if (fabs(a) < eps) {
+        if (fabs(b) > eps) {
+            t = -c / b;
+            return true;
+        }
+        return false;
+    }
+    const double disc = b * b - 4.0 * a * c;
+    if (fabs(disc) < eps) {
+        t = -b / (2.0 * a);
+        return true;
+    }
+    if (disc < 0.0) return false;
+    const double sq = sqrt(disc);
+    double r0, r1;
+    if (b >= 0.0) {
+        const double mul = -b - sq;
+        r0 = mul / (2.0 * a);
+        r1 = 2.0 * c / mul;
+    } else {
+        const double mul = -b + sq;
+        r0 = 2.0 * c / mul;
+        r1 = mul / (2.0 * a);
+    }
+    t = fmax(r0, r1);
+    return true;
+}
+
+// simd/x86.rs:217-244 s2l on all four lanes (the reference's default build)
+__device__ __forceinline__ float s2l(float v) {
+    const float x1 = 2.0843103538116825f * v - 1.0843103538116827f;
+    const float x2 = x1 * x1, x3 = x2 * x1;
+    const float hi = 0.23361048543711943f + 0.4665843122387033f * x1 + 0.26901741378006355f * x2 +
+                     0.031661580753065945f * x3;
+    return v <= 0.04045f ? v * 0.07739938080495357f : hi;
+}
+
+__device__ float4 paint_at(const PaintDev& p, float px, float py) {
+    if (p.kind == 0) return make_float4(p.color[0], p.color[1], p.color[2], p.color[3]);
+    float t;
+    if (p.kind == 1) {
+        t = linear_offset(p, px, py);
+    } else {
+        // FP32 first; binary64 near the cone's edge (root count undecided),
+        // for the degenerate linear case, and where a repeated or reflected
+        // spread needs the fraction of a large offset
+        bool wide = p.radial_linear != 0;
+        if (!wide) {
+            const float pdx = fmaf(px, p.q[0], fmaf(py, p.q[1], p.q[2]));
+            const float pdy = fmaf(px, p.q[3], fmaf(py, p.q[4], p.q[5]));
+            const float b = -2.f * ((p.cdx * pdx + p.cdy * pdy) + p.fr * p.rd);
+            const float c = (pdx * pdx + pdy * pdy) - p.fr * p.fr;
+            const float a = (float)p.a64;
+            const float disc = b * b - 4.f * a * c;
+            if (fabsf(disc) <= 1e-4f * (b * b + fabsf(4.f * a * c))) {
+                wide = true;
+            } else {
+                if (disc < 0.f) return make_float4(0.f, 0.f, 0.f, 0.f);
+                const float sq = sqrtf(disc);
+                float r0, r1;
+                if (b >= 0.f) {
+                    const float mul = -b - sq;
+                    r0 = mul / (2.f * a);
+                    r1 = 2.f * c / mul;
+                } else {
+                    const float mul = -b + sq;
+                    r0 = 2.f * c / mul;
+                    r1 = mul / (2.f * a);
+                }
+                t = fmaxf(r0, r1);
+                if (p.spread != 0 && !(fabsf(t) <= 1.f)) wide = true;
+                else t = spread_at(p.spread, t);
+            }
+        }
+        if (wide) {
+            double t64;
+            if (!radial_offset64(p, px, py, t64)) return make_float4(0.f, 0.f, 0.f, 0.f);
+            t = spread_at64(p.spread, t64);
+        }
+    }
+    // GradStops::at (src/grad.rs:116-139): first stop with position >= t
+    int lo = 0, hi = p.nstops;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (p.pos[mid] < t) lo = mid + 1; else hi = mid;
+    }
+    float4 col;
+    if (lo == 0) {
+        col = make_float4(p.col[0][0], p.col[0][1], p.col[0][2], p.col[0][3]);
+    } else if (lo == p.nstops) {
+        const int i = p.nstops - 1;
+        col = make_float4(p.col[i][0], p.col[i][1], p.col[i][2], p.col[i][3]);
+    } else {
+        const float ratio = (t - p.pos[lo - 1]) / (p.pos[lo] - p.pos[lo - 1]);
+        const float* c0 = p.col[lo - 1];
+        const float* c1 = p.col[lo];
+        col = make_float4(c1[0] * ratio + c0[0] * (1.f - ratio), c1[1] * ratio + c0[1] * (1.f - ratio),
+                          c1[2] * ratio + c0[2] * (1.f - ratio), c1[3] * ratio + c0[3] * (1.f - ratio));
+    }
+    if (!p.linear_colors) {
+        // LinColor::into_linear (src/color.rs:326-333): s2l of the unmultiplied colour, times alpha
+        const float a = col.w;
+        if (a <= 1e-6f) return make_float4(0.f, 0.f, 0.f, 0.f);
+        col = make_float4(s2l(col.x / a) * a, s2l(col.y / a) * a, s2l(col.z / a) * a, s2l(col.w / a) * a);
+    }
+    return col;
+}
+
+// ---------------------------------------------------------------------------
+// Composite
+// ---------------------------------------------------------------------------
+// A stored line end (16.16 anchor + FP32 remainder, fill frame) as a vertex
+// with its row relative to band row `row0`.
+__device__ __forceinline__ VtxQ line_vtx(int4 e, int row0) {
+    VtxQ v;
+    v.col = e.x >> 16;
+    v.row = (e.y >> 16) - row0;
+    v.fx = fmaf((float)(e.x & 0xffff), FIX_ONE_INV, __int_as_float(e.z));
+    v.fy = fmaf((float)(e.y & 0xffff), FIX_ONE_INV, __int_as_float(e.w));
+    return v;
+}
+
+constexpr int kCompThreads = 256;
+
+struct BlendEpi {
+    float4* rgba;        // band colour, canvas_w per row
+    int canvas_w;
+    int col0;            // canvas column of local x = 0
+    int y0_local;        // local row of band row 0
+    int width;           // view width
+    const PaintDev* paint;
+    __device__ __forceinline__ void operator()(int r, int x0, const float (&a)[kScanChunk]) const {
+        #pragma unroll 4
+        for (int i = 0; i < kScanChunk; ++i) {
+            const int x = x0 + i;
+            if (x >= width) break;
+            const float al = a[i];
+            if (fabsf(al) < 1e-6f) continue;  // mask_iter skips these pixels (src/rasterize.rs:347-349)
+            const float4 c = paint_at(*paint, (float)x + 0.5f, (float)(y0_local + r) + 0.5f);
+            float4& d = rgba[r * canvas_w + col0 + x];
+            // dst.blend_over(color.with_alpha(alpha)) = src + dst * (1 - src.a) (src/color.rs:342-349)
+            const float4 s = make_float4(c.x * al, c.y * al, c.z * al, c.w * al);
+            const float inv = 1.f - s.w;
+            d = make_float4(s.x + d.x * inv, s.y + d.y * inv, s.z + d.z * inv, s.w + d.w * inv);
+        }
+    }
+};
+
+struct AlphaEpi {  // coverage-only fills write the mask
+    float* out;
+    int64_t stride;
+    int row_base;  // canvas row of band row 0
+    int col0, width;
+    __device__ __forceinline__ void operator()(int r, int x0, const float (&a)[kScanChunk]) const {
+        float* o = out + (int64_t)(row_base + r) * stride + col0 + x0;
+        #pragma unroll
+        for (int i = 0; i < kScanChunk; ++i)
+            if (x0 + i < width) o[i] = a[i];
+    }
+};
+
+// smem: coverage band (band_rows x cov_stride floats) | RGBA band (band_rows x canvas_w float4) | chunk totals
+__global__ void __launch_bounds__(kCompThreads) k_composite(SceneDev S, int cov_stride, int tot_floats) {
+    extern __shared__ float4 sm4[];
+    float* cov = reinterpret_cast<float*>(sm4);
+    const bool paint_mode = S.paints != nullptr;
+    float4* rgba = reinterpret_cast<float4*>(cov + S.band_rows * cov_stride);
+    float* tot = reinterpret_cast<float*>(rgba + (paint_mode ? S.band_rows * S.canvas_w : 0));
+    const int band = blockIdx.x;
+    const int row_base = band * S.band_rows;
+    const int rows = min(S.band_rows, S.canvas_h - row_base);
+    if (rows <= 0) return;
+    if (paint_mode) {
+        for (int i = threadIdx.x; i < rows * S.canvas_w; i += kCompThreads) {
+            const int r = i / S.canvas_w, x = i - r * S.canvas_w;
+            float4 v;
+            if (S.load_canvas) {
+                v = reinterpret_cast<const float4*>(S.canvas)[(int64_t)(row_base + r) * S.canvas_stride + x];
+            } else if (S.bg) {
+                v = make_float4(S.bg[0], S.bg[1], S.bg[2], S.bg[3]);
+            } else {
+                v = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            rgba[i] = v;
+        }
+    }
+    for (uint32_t fi = 0; fi < S.n_fills; ++fi) {
+        const FillDev& f = S.fills[fi];
+        if (band < f.band0 || band >= f.band0 + f.nbands) continue;
+        const uint32_t e = f.entry0 + (band - f.band0);
+        const uint32_t n = S.entry_count[e];
+        if (n == 0) continue;  // full-width bands: no line, no coverage
+        Band B;
+        B.acc = cov;
+        B.stride = band_stride(f.clip_width);
+        B.bh = rows;
+        B.y0 = row_base - f.row0;  // local row of band row 0
+        B.img_h = f.height;
+        B.width_f = (float)f.clip_width;
+        B.width_i = f.clip_width;
+        __syncthreads();  // previous fill done with the band
+        const int n4 = (rows * B.stride) >> 2;
+        for (int i = threadIdx.x; i < n4; i += kCompThreads) sm4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        __syncthreads();
+        const uint32_t start = S.entry_start[e];
+        for (uint32_t j = threadIdx.x; j < n; j += kCompThreads) {
+            const uint32_t l = S.pairs[start + j];
+            const int4 a = S.lines[2ull * l], b = S.lines[2ull * l + 1];
+            accumulate_vtx(B, line_vtx(a, B.y0), line_vtx(b, B.y0));
+        }
+        __syncthreads();
+        if (paint_mode) {
+            BlendEpi epi{rgba, S.canvas_w, f.col0, B.y0, f.width, S.paints + f.paint};
+            band_scan<kCompThreads>(B, f.width, f.rule, tot, epi);
+        } else {
+            AlphaEpi epi{S.canvas, S.canvas_stride, row_base, f.col0, f.width};
+            band_scan<kCompThreads>(B, f.width, f.rule, tot, epi);
+        }
+    }
+    if (paint_mode) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < rows * S.canvas_w; i += kCompThreads) {
+            const int r = i / S.canvas_w, x = i - r * S.canvas_w;
+            reinterpret_cast<float4*>(S.canvas)[(int64_t)(row_base + r) * S.canvas_stride + x] = rgba[i];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers (declared in rz_api.cu)
+// ---------------------------------------------------------------------------
+cudaError_t launch_flatten_count(const SceneDev& S, cudaStream_t st) {
+    if (S.n_slots == 0) return cudaSuccess;
+    k_flatten_count<<<(S.n_slots + 127) / 128, 128, 0, st>>>(S);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_flatten_emit(const SceneDev& S, cudaStream_t st) {
+    if (S.n_slots == 0) return cudaSuccess;
+    k_flatten_emit<<<(S.n_slots + 127) / 128, 128, 0, st>>>(S);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bin_scatter(const SceneDev& S, cudaStream_t st) {
+    if (S.n_lines == 0) return cudaSuccess;
+    k_bin_scatter<<<(S.n_lines + 255) / 256, 256, 0, st>>>(S);
+    return cudaGetLastError();
+}
+
+// Shared memory of the composite for a canvas width / band height / max view clip width.
+int composite_smem_bytes(int canvas_w, int band_rows, int max_clip_width, bool paint_mode, int* cov_stride,
+                         int* tot_floats) {
+    const int stride = band_stride(max_clip_width);
+    const int tf = band_rows * ((stride + kScanChunk - 1) / kScanChunk);
+    *cov_stride = stride;
+    *tot_floats = tf;
+    return 4 * band_rows * stride + (paint_mode ? 16 * band_rows * canvas_w : 0) + 4 * tf;
+}
+
+cudaError_t launch_composite(const SceneDev& S, int cov_stride, int tot_floats, int smem, cudaStream_t st) {
+    static int configured = 0;
+    if (smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_composite, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    k_composite<<<S.n_bands, kCompThreads, smem, st>>>(S, cov_stride, tot_floats);
+    return cudaGetLastError();
+}
+
+}  // namespace rz

@@ -1,0 +1,86 @@
+// rz_pipeline.cuh -- data layout of the line pipeline (large paths, scenes).
+//
+// Kernels, in launch order:
+//   k_flatten_count  one thread per segment slot: lines its bisection tree emits
+//   scan             exclusive prefix of the counts (line offsets)
+//   k_flatten_emit   walks again, writes 16.16 lines, counts lines per (fill, band)
+//   scan             exclusive prefix of the (fill, band) counts
+//   k_bin_scatter    line indices into their (fill, band) lists
+//   k_composite      one CTA per row band of the canvas: fills in order, signed
+//                    area in shared memory, row prefix, fill rule, paint, source-over
+#pragma once
+#include <stdint.h>
+
+namespace rz {
+
+constexpr int kMaxStops = 16;
+
+// One fill of a scene (or the single path of a large mask), device memory.
+struct FillDev {
+    uint32_t sub0, sub1;     // subpath range (global)
+    uint32_t seg0, seg1;     // segment range (global)
+    uint32_t slot0;          // first flatten slot (segments, then one closing line per subpath)
+    uint32_t entry0;         // first (fill, band) entry
+    int32_t col0, row0;      // canvas position of the fill's local (0, 0)
+    int32_t width, height;   // view: local columns [0, width), rows [0, height)
+    int32_t clip_width;      // the reference's `width` for this view
+    int32_t band0, nbands;   // canvas bands the view touches
+    int32_t rule, paint;     // fill rule, paint index (-1: coverage only)
+    double tr[6];            // transform into local coordinates (binary64)
+};
+
+struct PaintDev {
+    int32_t kind;           // 0 solid, 1 linear, 2 radial, -1 draws nothing
+    int32_t spread;         // 0 pad, 1 repeat, 2 reflect
+    int32_t linear_colors;  // 0: stops are sRGB, results converted back to linear
+    int32_t nstops;
+    int32_t radial_linear;  // radial with |A| < EPSILON: the equation is linear in t
+    int32_t pad;
+    // linear: t of a local pixel centre (x, y) = g0 x + g1 y + g2, each
+    // coefficient a double-float pair gh + gl composed in binary64
+    float gh[3], gl[3];
+    // radial: pd = p - focal centre of a local pixel centre (x, y):
+    // (q0 x + q1 y + q2, q3 x + q4 y + q5), FP32 and binary64
+    float q[6];
+    double qd[6];
+    float cdx, cdy, rd, fr;       // c - fc, r - fr, focal radius
+    double cdxd, cdyd, rdd, frd;  // same in binary64
+    double a64;                   // A = |cd|^2 - rd^2
+    float color[4];               // solid colour
+    float pos[kMaxStops];
+    float col[kMaxStops][4];
+};
+
+struct SceneDev {
+    const uint8_t* kind;
+    const double* pts;
+    const uint32_t* sub_off;
+    const FillDev* fills;
+    const PaintDev* paints;
+    uint32_t n_fills;
+    uint32_t n_slots;
+    uint32_t n_segments;
+    uint32_t n_subpaths;
+    double thr64;
+    float thr32;
+    int32_t canvas_w, canvas_h;
+    int32_t band_rows;       // canvas rows per band
+    int32_t n_bands;
+    // pipeline buffers
+    uint32_t* slot_count;    // [n_slots] lines per slot, then its exclusive prefix
+    int4* lines;             // [2 * n_lines] per end point: exact 16.16 anchor (x, y), FP32 remainder (dx, dy)
+    uint32_t n_lines;
+    uint32_t* entry_count;   // [n_entries]
+    uint32_t* entry_start;   // [n_entries] exclusive prefix of entry_count
+    uint32_t* entry_cursor;  // [n_entries]
+    uint32_t* pairs;         // [n_pairs] line indices grouped by (fill, band)
+    // output
+    float* canvas;           // RGBA f32 (scenes) or f32 mask (coverage only)
+    int64_t canvas_stride;   // elements between rows (pixels for RGBA: 4 floats each)
+    const float* bg;         // background colour or null (canvas already initialised)
+    int32_t load_canvas;     // 1: blend over the canvas content instead of bg
+    int32_t* err;
+    int32_t* counters;
+};
+
+}  // namespace rz

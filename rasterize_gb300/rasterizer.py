@@ -18,6 +18,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _ffi
+from . import paint as _paint
 from .geometry import Size, Transform
 from .path import DEFAULT_FLATNESS, FillRule, Path
 
@@ -195,6 +196,46 @@ class MaskBatch:
         return flat[d.offset:d.offset + d.row_stride * d.height].reshape(d.height, d.row_stride)[:, :d.width]
 
 
+class Scene:
+    """A group of fills drawn in order (the reference's ``Scene::group`` of
+    ``Scene::fill`` nodes, src/scene.rs:69-200), rendered by
+    ``GpuRasterizer.render_scene`` like ``Scene::render`` with view = canvas."""
+
+    def __init__(self):
+        self.fills = []  # (path, transform, fill_rule, paint)
+
+    def fill(self, path: Path, paint, tr: Transform | None = None, fill_rule: FillRule = FillRule.NonZero):
+        self.fills.append((path, tr or Transform.identity(), FillRule(fill_rule), paint))
+        return self
+
+    def pack(self):
+        """(rz_scene struct, keepalive) over host arrays."""
+        paths = [f[0] for f in self.fills]
+        n = len(paths)
+        kind = np.ascontiguousarray(np.concatenate([p.kind for p in paths]) if n else np.zeros(0, np.uint8))
+        pts = np.ascontiguousarray(np.concatenate([p.pts for p in paths]) if n else np.zeros((0, 8)))
+        sub, fsub, base = [0], [0], 0
+        for p in paths:
+            sub.extend((p.subpath_off[1:].astype(np.int64) + base).tolist())
+            base += p.n_segments
+            fsub.append(len(sub) - 1)
+        sub = np.ascontiguousarray(np.asarray(sub, dtype=np.uint32))
+        fsub = np.ascontiguousarray(np.asarray(fsub, dtype=np.uint32))
+        trs = np.ascontiguousarray(np.array([f[1].m for f in self.fills], dtype=np.float64).reshape(-1))
+        rules = np.ascontiguousarray(np.array([int(f[2]) for f in self.fills], dtype=np.uint8))
+        structs, keep = [], []
+        for f in self.fills:
+            st, k = _paint.to_struct(f[3])
+            structs.append(st)
+            keep.append(k)
+        paints = (_paint.RzPaint * max(n, 1))(*structs)
+        fpaint = np.ascontiguousarray(np.arange(n, dtype=np.uint32))
+        s = _ffi.RzScene(n, int(kind.shape[0]), len(sub) - 1, n, kind.ctypes.data, pts.ctypes.data, sub.ctypes.data,
+                         fsub.ctypes.data, trs.ctypes.data if n else None, rules.ctypes.data if n else None,
+                         fpaint.ctypes.data if n else None, ctypes.addressof(paints))
+        return s, (kind, pts, sub, fsub, trs, rules, fpaint, paints, keep)
+
+
 class BatchPlan:
     """A device-resident batch bound to its output: work list uploaded once,
     each ``launch()`` replays a captured CUDA graph (no host synchronisation)."""
@@ -278,6 +319,33 @@ class GpuRasterizer(Rasterizer):
         for p in self.mask_iter(path, tr, size, fill_rule):
             out[p.y, p.x] = p.alpha
         return out
+
+    def fill(self, path: Path, tr: Transform, fill_rule: FillRule, paint, img: np.ndarray) -> None:
+        """Rasterizer::fill: paints ``path`` source-over into a (H, W, 4) float32
+        image of premultiplied linear RGBA (any positive pixel strides)."""
+        if img.dtype != np.float32 or img.ndim != 3 or img.shape[2] != 4 or img.strides[2] != 4:
+            raise TypeError("fill image must be a (H, W, 4) float32 array with contiguous channels")
+        if any(st < 0 or st % 16 for st in img.strides[:2]):
+            raise ValueError("fill image pixel strides must be positive multiples of 16 bytes")
+        h, w = img.shape[:2]
+        shape = _ffi.RzShape(0, w, h, img.strides[0] // 16, img.strides[1] // 16)
+        ps, keep = _path_struct(path)
+        pst, pkeep = _paint.to_struct(paint)
+        tr_a = _tr_array(tr)
+        lib = self.ctx.lib
+        self.ctx.check(lib.rz_fill(self.ctx.ptr, ctypes.byref(ps), tr_a.ctypes.data, int(fill_rule), self.flatness,
+                                   ctypes.addressof(pst), img.ctypes.data, shape))
+
+    def render_scene(self, scene: Scene, width: int, height: int, bg=None) -> np.ndarray:
+        """Scene::render over a (height, width, 4) float32 canvas initialised to bg."""
+        s, keep = scene.pack()
+        canvas = np.zeros((height, width, 4), dtype=np.float32)
+        bg_a = np.ascontiguousarray(bg, dtype=np.float32) if bg is not None else None
+        lib = self.ctx.lib
+        self.ctx.check(lib.rz_render_scene(self.ctx.ptr, ctypes.byref(s), self.flatness,
+                                           bg_a.ctypes.data if bg_a is not None else None, canvas.ctypes.data,
+                                           width, height))
+        return canvas
 
     def flatten_counts(self, path: Path, tr: Transform) -> np.ndarray:
         """Lines per input segment, then one entry per subpath (closing line)."""

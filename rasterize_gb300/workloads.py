@@ -119,3 +119,81 @@ def glyph_batch(seed: int = 2, n: int = 10000, seg_range=(10, 400), side_range=(
 
 def identity():
     return Transform.identity()
+
+
+def _random_stops(rng, n):
+    from .paint import GradStop, LinColor
+    stops = []
+    for _ in range(n):
+        a = float(rng.uniform(0.3, 1.0))
+        r, g, b = rng.uniform(0, 1, 3) * a
+        stops.append(GradStop(float(rng.uniform(0, 1)), LinColor(float(r), float(g), float(b), a)))
+    return stops
+
+
+def random_paint(rng, cx, cy, size, linear_colors=True):
+    """50 % solid, 25 % linear, 25 % radial gradient (2-8 stops uniform in [0,1])."""
+    from .paint import GradLinear, GradRadial, GradSpread, LinColor, Units
+    u = rng.uniform()
+    if u < 0.5:
+        a = float(rng.uniform(0.3, 1.0))
+        r, g, b = rng.uniform(0, 1, 3) * a
+        return LinColor(float(r), float(g), float(b), a)
+    stops = _random_stops(rng, int(rng.integers(2, 9)))
+    spread = GradSpread(int(rng.integers(0, 3)))
+    if u < 0.75:
+        ang = rng.uniform(0, 2 * math.pi)
+        d = size * rng.uniform(0.3, 1.0)
+        start = (cx - 0.5 * d * math.cos(ang), cy - 0.5 * d * math.sin(ang))
+        end = (cx + 0.5 * d * math.cos(ang), cy + 0.5 * d * math.sin(ang))
+        return GradLinear(stops, start, end, Units.UserSpaceOnUse, linear_colors, spread)
+    R = size * rng.uniform(0.3, 0.8)
+    off = R * 0.4 * rng.uniform(0, 1)
+    ang = rng.uniform(0, 2 * math.pi)
+    fc = (cx + off * math.cos(ang), cy + off * math.sin(ang))
+    fr = float(rng.uniform(0.0, 0.5)) * (R - off)
+    return GradRadial(stops, (cx, cy), float(R), fc, fr, Units.UserSpaceOnUse, linear_colors, spread)
+
+
+def contour(rng, n_seg, radius, p_cubic=0.5):
+    """Star-shaped closed outline around the origin: cubic or line segments."""
+    ang = np.sort(rng.uniform(0.0, 2.0 * math.pi, n_seg))
+    rad = radius * rng.uniform(0.55, 1.0, n_seg)
+    v = np.stack([rad * np.cos(ang), rad * np.sin(ang)], axis=1)
+    a, b = v, np.roll(v, -1, axis=0)
+    chord = np.linalg.norm(b - a, axis=1, keepdims=True) + 1e-9
+    kinds = np.where(rng.uniform(size=n_seg) < p_cubic, SEG_CUBIC, SEG_LINE).astype(np.uint8)
+    c1 = a + (b - a) / 3.0 + rng.normal(0.0, 1.0, (n_seg, 2)) * 0.3 * chord
+    c2 = a + 2.0 * (b - a) / 3.0 + rng.normal(0.0, 1.0, (n_seg, 2)) * 0.3 * chord
+    pts = np.zeros((n_seg, 8))
+    pts[:, 0:2] = a
+    cub = kinds == SEG_CUBIC
+    pts[cub, 2:4] = c1[cub]
+    pts[cub, 4:6] = c2[cub]
+    pts[cub, 6:8] = b[cub]
+    pts[~cub, 2:4] = b[~cub]
+    return _path_from_arrays(kinds, pts)
+
+
+def scene(seed: int = 3, n: int = 2000, size: int = 2048, seg_range=(20, 2000), radius_range=(8, 128),
+          linear_colors=True):
+    """``n`` filled star-shaped paths (log-uniform 20-2000 cubic/line segments,
+    radius log-uniform 8-128 px) under random affine transforms (scale
+    0.5-2, any rotation, centre uniform in the canvas), 50 % solid / 25 %
+    linear / 25 % radial paints, NonZero, drawn in order on a size x size
+    canvas.  Returns a Scene and the per-fill (path, tr, rule, paint)."""
+    from .rasterizer import Scene
+    rng = np.random.default_rng(seed)
+    sc = Scene()
+    for _ in range(n):
+        nseg = int(round(math.exp(rng.uniform(math.log(seg_range[0]), math.log(seg_range[1])))))
+        r = math.exp(rng.uniform(math.log(radius_range[0]), math.log(radius_range[1])))
+        path = contour(rng, nseg, r)
+        s = rng.uniform(0.5, 2.0)
+        ang = rng.uniform(0, 2 * math.pi)
+        cx, cy = rng.uniform(0, size, 2)
+        tr = Transform.new_translate(cx, cy) * Transform.new_rotate(ang) * Transform.new_scale(s, s)
+        # gradients live in the path's own coordinates (UserSpaceOnUse, before tr)
+        paint = random_paint(rng, 0.0, 0.0, 2 * r, linear_colors)
+        sc.fill(path, paint, tr, FillRule.NonZero)
+    return sc
