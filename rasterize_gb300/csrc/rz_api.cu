@@ -32,9 +32,8 @@ cudaError_t launch_flatten_counts(const BatchDev& b, uint32_t n_segments, uint32
 cudaError_t launch_flatten_count(const SceneDev& S, cudaStream_t st);
 cudaError_t launch_flatten_emit(const SceneDev& S, cudaStream_t st);
 cudaError_t launch_bin_scatter(const SceneDev& S, cudaStream_t st);
-int composite_smem_bytes(int canvas_w, int band_rows, int max_clip_width, bool paint_mode, int* cov_stride,
-                         int* tot_floats);
-cudaError_t launch_composite(const SceneDev& S, int cov_stride, int tot_floats, int smem, cudaStream_t st);
+int composite_smem_bytes(int canvas_w, int band_rows, int max_clip_width, bool paint_mode, int* cov_stride);
+cudaError_t launch_composite(const SceneDev& S, int cov_stride, int smem, cudaStream_t st);
 uint64_t scan_temp_words(uint64_t n);
 cudaError_t scan_u32(uint32_t* data, uint64_t n, uint32_t* temp, cudaStream_t stream);
 }  // namespace rz
@@ -868,7 +867,7 @@ struct HostScene {
 
 int choose_band_rows(int canvas_w, int canvas_h, bool paint_mode) {
     const int stride = rz::band_stride(canvas_w);
-    const int per_row = 4 * stride + (paint_mode ? 16 * canvas_w : 0) + 4 * ((stride + 15) / 16);
+    const int per_row = 4 * stride + (paint_mode ? 16 * canvas_w : 0);
     int rows = std::max(1, (paint_mode ? 96 * 1024 : 64 * 1024) / per_row);
     rows = std::min(rows, 64);
     return std::max(1, std::min(rows, std::max(canvas_h, 1)));
@@ -929,14 +928,14 @@ rz_status run_pipeline(rz_ctx* ctx, HostScene& hs, double flatness, float* canva
     S.err = (int32_t*)ctx->d_ctrl.p;
     S.counters = (int32_t*)ctx->d_ctrl.p + 4;
     if (S.n_bands == 0) return read_error(ctx);
-    int cov_stride = 0, tot_floats = 0;
-    const int smem = rz::composite_smem_bytes(canvas_w, hs.band_rows, hs.max_clip, paint_mode, &cov_stride, &tot_floats);
+    int cov_stride = 0;
+    const int smem = rz::composite_smem_bytes(canvas_w, hs.band_rows, hs.max_clip, paint_mode, &cov_stride);
     if (S.n_fills == 0) {
         // nothing to draw: the composite still writes the background
         if (paint_mode) {
             RZ_CUDA(ctx->p_paints.ensure(sizeof(rz::PaintDev)));
             S.paints = (const rz::PaintDev*)ctx->p_paints.p;
-            RZ_CUDA(rz::launch_composite(S, cov_stride, tot_floats, smem, ctx->stream));
+            RZ_CUDA(rz::launch_composite(S, cov_stride, smem, ctx->stream));
         }
         return read_error(ctx);
     }
@@ -988,7 +987,7 @@ rz_status run_pipeline(rz_ctx* ctx, HostScene& hs, double flatness, float* canva
     S.pairs = (uint32_t*)ctx->p_pairs.p;
     RZ_CUDA(rz::launch_bin_scatter(S, ctx->stream));
     // 6) composite
-    RZ_CUDA(rz::launch_composite(S, cov_stride, tot_floats, smem, ctx->stream));
+    RZ_CUDA(rz::launch_composite(S, cov_stride, smem, ctx->stream));
     return read_error(ctx);
 }
 

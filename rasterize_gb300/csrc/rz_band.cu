@@ -138,10 +138,8 @@ __device__ __forceinline__ int decide_slot(const BatchDev& b, const SegRec& r, c
 
 constexpr int kSmemBytes = kBandBytes + kThreads * (int)sizeof(SegRec) + kThreads * (int)sizeof(SlotCoef) +
                            kLeafCap * (int)sizeof(LeafCode) + 2 * kLevelCap * (int)sizeof(uint32_t);
-static_assert(kLeafCap * (int)sizeof(LeafCode) >= (kBandFloats / kScanChunk) * (int)sizeof(float),
-              "the leaf buffer doubles as the chunk-total array of the scan");
 
-// Mask epilogue of the row scan: 16-byte streaming stores of the alphas.
+// Mask epilogue of the row scan: a 16-byte streaming store of 4 alphas.
 struct MaskStore {
     float* out;
     uint64_t offset;
@@ -149,11 +147,8 @@ struct MaskStore {
     int y0, width;
     __device__ __forceinline__ void operator()(int r, int x0, const float (&a)[kScanChunk]) const {
         float* o = out + offset + (uint64_t)(y0 + r) * (uint64_t)row_stride + x0;
-        const bool vec = ((reinterpret_cast<uintptr_t>(o) & 15u) == 0) && (x0 + kScanChunk <= width);
-        if (vec) {
-            #pragma unroll
-            for (int q = 0; q < kScanChunk / 4; ++q)
-                __stcs(reinterpret_cast<float4*>(o) + q, make_float4(a[4 * q], a[4 * q + 1], a[4 * q + 2], a[4 * q + 3]));
+        if (((reinterpret_cast<uintptr_t>(o) & 15u) == 0) && (x0 + kScanChunk <= width)) {
+            __stcs(reinterpret_cast<float4*>(o), make_float4(a[0], a[1], a[2], a[3]));
         } else {
             #pragma unroll
             for (int i = 0; i < kScanChunk; ++i)
@@ -391,7 +386,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_mask_bands(BatchDev b, const Wo
 
         const int rule = b.rule ? b.rule[wi.path] : 0;
         MaskStore st{b.out, m.offset, (int64_t)m.row_stride, B.y0, m.width};
-        band_scan<kThreads>(B, m.width, rule, reinterpret_cast<float*>(leaves), st);
+        band_scan<kThreads>(B, m.width, rule, st);
         __syncthreads();
     }
     if (fallbacks) atomicAdd(&b.counters[1], fallbacks);

@@ -328,9 +328,7 @@ struct Band {
     int width_i;
 };
 
-__device__ __forceinline__ void sadd(float* p, int v) {
-    if (v) atomicAdd(reinterpret_cast<int*>(p), v);
-}
+__device__ __forceinline__ void sadd(float* p, int v) { atomicAdd(reinterpret_cast<int*>(p), v); }
 
 // Signed height `d` (fixed point) of one row, spread over the pixels the line
 // covers between xa and xn (FP32, relative to integer column xb) as in
@@ -375,10 +373,13 @@ __device__ __forceinline__ void accumulate_row(const Band& B, int r, int xb, flo
     sadd(row + x1i, cm);
 }
 
-// A short line piece (a few px each way) already clipped by the x rules: x in
-// FP32 relative to column xb, y band-relative in fixed point.  Walks its rows
-// like signed_difference_line (src/rasterize.rs:405-469); the row crossings
-// are interpolated from the exact fixed-point heights.
+constexpr int kShortLine = 32;
+
+// A short line piece (at most kShortLine px each way) already clipped by the
+// x rules: x in FP32 relative to column xb, y band-relative in fixed point.
+// Walks its rows like signed_difference_line (src/rasterize.rs:405-469); the
+// row crossings are interpolated from the exact fixed-point heights, so their
+// x error stays below ~kShortLine * 2^-23 px.
 __device__ inline void accumulate_piece(const Band& B, int xb, float x0, int32_t q0, float x1, int32_t q1) {
     if (q0 == q1) return;  // no signed coverage (the reference skips |dy| < EPSILON)
     int dir = 1;
@@ -453,7 +454,7 @@ __device__ inline void accumulate_piece64(const Band& B, double x0, double y0, d
         else if (y1 > hi) { x1 = x0 + (hi - y0) * dxdy; y1 = hi; }
     }
     const int32_t q0 = __double2int_rn(y0 * 4194304.0), q1 = __double2int_rn(y1 * 4194304.0);
-    if (fabs(x1 - x0) <= 4.0 && abs(q1 - q0) <= (4 << COV_SHIFT)) {
+    if (fabs(x1 - x0) <= (double)kShortLine && abs(q1 - q0) <= (kShortLine << COV_SHIFT)) {
         const int xb = (int)floor(fmin(x0, x1));
         accumulate_piece(B, xb, (float)(x0 - xb), q0, (float)(x1 - xb), q1);
     } else {
@@ -507,8 +508,9 @@ struct VtxQ {
 // quantises the same vertex to the same height.
 __device__ __forceinline__ void accumulate_vtx(const Band& B, const VtxQ& a, const VtxQ& b) {
     const int dc = b.col - a.col, dr = b.row - a.row;
-    if (abs(dc) <= 3 && abs(dr) <= 3) {
-        if (a.row < -8 || a.row > B.bh + 8) return;  // wholly outside the band's rows
+    if (abs(dc) < kShortLine && abs(dr) < kShortLine) {
+        // wholly above or below the band's rows (this also keeps the heights in int32)
+        if (a.row < -kShortLine - 4 || a.row > B.bh + kShortLine + 4) return;
         const float x0 = a.fx, x1 = (float)dc + b.fx;
         const float xlo = (float)a.col + fminf(x0, x1), xhi = (float)a.col + fmaxf(x0, x1);
         if (xlo > 0.01f && xhi < B.width_f - 0.01f) {
@@ -610,72 +612,43 @@ __device__ inline bool clip_y64(double lo, double hi, double (&x)[2], double (&y
 
 // ---------------------------------------------------------------------------
 // Row prefix of a band (signed differences -> winding) and fill rule
-// (src/rasterize.rs:473-507), in exact fixed-point integer arithmetic.
-// Every thread owns 16-pixel chunks:
-// 1) in-place inclusive prefix of each chunk, chunk totals to `tot`;
-// 2) per row, exclusive scan of the chunk totals (warp shuffles);
-// 3) base + chunk prefix -> fill rule -> epi(row, x0, alpha[16]).
-// `tot` holds at least rows * ceil(width / 16) floats; the band stride is a
-// multiple of 16 (band_stride), so chunk reads stay inside their row.
+// (src/rasterize.rs:473-507), in exact fixed-point integer arithmetic.  One
+// warp per row, kScanChunk = 4 pixels per lane: a 16-byte load, the lane's
+// inclusive prefix, a warp shuffle scan of the lane totals and the carry of
+// the previous 128 columns; then epi(row, x0, alpha[4]) per lane.
 // ---------------------------------------------------------------------------
-constexpr int kScanChunk = 16;
+constexpr int kScanChunk = 4;
 
 template <int THREADS, class Epi>
-__device__ void band_scan(const Band& B, int width, int rule, float* tot_f, const Epi& epi) {
-    int32_t* tot = reinterpret_cast<int32_t*>(tot_f);
-    const int W = width;
-    const int cr = (W + kScanChunk - 1) / kScanChunk;  // chunks per row
-    const int nc = cr * B.bh;
-    for (int c = threadIdx.x; c < nc; c += THREADS) {
-        const int r = c / cr, x0 = (c - r * cr) * kScanChunk;
-        int4* row4 = reinterpret_cast<int4*>(B.acc + r * B.stride + x0);
-        uint32_t run = 0;
-        #pragma unroll
-        for (int q = 0; q < kScanChunk / 4; ++q) {
-            const int4 v = row4[q];
-            const int x = x0 + 4 * q;
-            uint4 u;  // unsigned: the winding wraps by design
-            u.x = (x < W ? (uint32_t)v.x : 0u) + run;
-            u.y = (x + 1 < W ? (uint32_t)v.y : 0u) + u.x;
-            u.z = (x + 2 < W ? (uint32_t)v.z : 0u) + u.y;
-            u.w = (x + 3 < W ? (uint32_t)v.w : 0u) + u.z;
-            run = u.w;
-            row4[q] = make_int4((int)u.x, (int)u.y, (int)u.z, (int)u.w);
-        }
-        tot[c] = (int32_t)run;
-    }
-    __syncthreads();
+__device__ void band_scan(const Band& B, int width, int rule, const Epi& epi) {
     const int lane = threadIdx.x & 31;
     for (int r = threadIdx.x >> 5; r < B.bh; r += THREADS / 32) {
-        uint32_t carry = 0;
-        for (int q0 = 0; q0 < cr; q0 += 32) {
-            const int q = q0 + lane;
-            const uint32_t v = q < cr ? (uint32_t)tot[r * cr + q] : 0u;
-            uint32_t incl = v;
+        const int4* row4 = reinterpret_cast<const int4*>(B.acc + r * B.stride);
+        uint32_t carry = 0;  // unsigned: the winding wraps by design
+        for (int x0 = 0; x0 < width; x0 += 32 * kScanChunk) {
+            const int x = x0 + kScanChunk * lane;
+            int4 v = make_int4(0, 0, 0, 0);
+            if (x < width) v = row4[x >> 2];
+            const uint32_t a0 = (uint32_t)v.x;
+            const uint32_t a1 = a0 + (x + 1 < width ? (uint32_t)v.y : 0u);
+            const uint32_t a2 = a1 + (x + 2 < width ? (uint32_t)v.z : 0u);
+            const uint32_t a3 = a2 + (x + 3 < width ? (uint32_t)v.w : 0u);
+            uint32_t incl = a3;
             #pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
                 const uint32_t o = __shfl_up_sync(0xffffffffu, incl, off);
                 if (lane >= off) incl += o;
             }
-            if (q < cr) tot[r * cr + q] = (int32_t)(carry + incl - v);  // exclusive base of the chunk
+            const uint32_t base = carry + incl - a3;
             carry += __shfl_sync(0xffffffffu, incl, 31);
+            if (x < width) {
+                const float a[kScanChunk] = {alpha_from_winding_fix(rule, (int32_t)(base + a0)),
+                                             alpha_from_winding_fix(rule, (int32_t)(base + a1)),
+                                             alpha_from_winding_fix(rule, (int32_t)(base + a2)),
+                                             alpha_from_winding_fix(rule, (int32_t)(base + a3))};
+                epi(r, x, a);
+            }
         }
-    }
-    __syncthreads();
-    for (int c = threadIdx.x; c < nc; c += THREADS) {
-        const int r = c / cr, x0 = (c - r * cr) * kScanChunk;
-        const uint32_t base = (uint32_t)tot[c];
-        const int4* row4 = reinterpret_cast<const int4*>(B.acc + r * B.stride + x0);
-        float a[kScanChunk];
-        #pragma unroll
-        for (int q = 0; q < kScanChunk / 4; ++q) {
-            const int4 v = row4[q];
-            a[4 * q] = alpha_from_winding_fix(rule, (int32_t)(base + (uint32_t)v.x));
-            a[4 * q + 1] = alpha_from_winding_fix(rule, (int32_t)(base + (uint32_t)v.y));
-            a[4 * q + 2] = alpha_from_winding_fix(rule, (int32_t)(base + (uint32_t)v.z));
-            a[4 * q + 3] = alpha_from_winding_fix(rule, (int32_t)(base + (uint32_t)v.w));
-        }
-        epi(r, x0, a);
     }
 }
 

@@ -462,7 +462,7 @@ struct BlendEpi {
     int width;           // view width
     const PaintDev* paint;
     __device__ __forceinline__ void operator()(int r, int x0, const float (&a)[kScanChunk]) const {
-        #pragma unroll 4
+        #pragma unroll
         for (int i = 0; i < kScanChunk; ++i) {
             const int x = x0 + i;
             if (x >= width) break;
@@ -491,13 +491,12 @@ struct AlphaEpi {  // coverage-only fills write the mask
     }
 };
 
-// smem: coverage band (band_rows x cov_stride floats) | RGBA band (band_rows x canvas_w float4) | chunk totals
-__global__ void __launch_bounds__(kCompThreads) k_composite(SceneDev S, int cov_stride, int tot_floats) {
+// smem: coverage band (band_rows x cov_stride words) | RGBA band (band_rows x canvas_w float4)
+__global__ void __launch_bounds__(kCompThreads) k_composite(SceneDev S, int cov_stride) {
     extern __shared__ float4 sm4[];
     float* cov = reinterpret_cast<float*>(sm4);
     const bool paint_mode = S.paints != nullptr;
     float4* rgba = reinterpret_cast<float4*>(cov + S.band_rows * cov_stride);
-    float* tot = reinterpret_cast<float*>(rgba + (paint_mode ? S.band_rows * S.canvas_w : 0));
     const int band = blockIdx.x;
     const int row_base = band * S.band_rows;
     const int rows = min(S.band_rows, S.canvas_h - row_base);
@@ -543,10 +542,10 @@ __global__ void __launch_bounds__(kCompThreads) k_composite(SceneDev S, int cov_
         __syncthreads();
         if (paint_mode) {
             BlendEpi epi{rgba, S.canvas_w, f.col0, B.y0, f.width, S.paints + f.paint};
-            band_scan<kCompThreads>(B, f.width, f.rule, tot, epi);
+            band_scan<kCompThreads>(B, f.width, f.rule, epi);
         } else {
             AlphaEpi epi{S.canvas, S.canvas_stride, row_base, f.col0, f.width};
-            band_scan<kCompThreads>(B, f.width, f.rule, tot, epi);
+            band_scan<kCompThreads>(B, f.width, f.rule, epi);
         }
     }
     if (paint_mode) {
@@ -580,23 +579,20 @@ cudaError_t launch_bin_scatter(const SceneDev& S, cudaStream_t st) {
 }
 
 // Shared memory of the composite for a canvas width / band height / max view clip width.
-int composite_smem_bytes(int canvas_w, int band_rows, int max_clip_width, bool paint_mode, int* cov_stride,
-                         int* tot_floats) {
+int composite_smem_bytes(int canvas_w, int band_rows, int max_clip_width, bool paint_mode, int* cov_stride) {
     const int stride = band_stride(max_clip_width);
-    const int tf = band_rows * ((stride + kScanChunk - 1) / kScanChunk);
     *cov_stride = stride;
-    *tot_floats = tf;
-    return 4 * band_rows * stride + (paint_mode ? 16 * band_rows * canvas_w : 0) + 4 * tf;
+    return 4 * band_rows * stride + (paint_mode ? 16 * band_rows * canvas_w : 0);
 }
 
-cudaError_t launch_composite(const SceneDev& S, int cov_stride, int tot_floats, int smem, cudaStream_t st) {
+cudaError_t launch_composite(const SceneDev& S, int cov_stride, int smem, cudaStream_t st) {
     static int configured = 0;
     if (smem > configured) {
         cudaError_t e = cudaFuncSetAttribute(k_composite, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
-    k_composite<<<S.n_bands, kCompThreads, smem, st>>>(S, cov_stride, tot_floats);
+    k_composite<<<S.n_bands, kCompThreads, smem, st>>>(S, cov_stride);
     return cudaGetLastError();
 }
 
