@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--glyphs", type=int, default=10000)
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="bounded CPU baseline sample")
     ap.add_argument("--no-per-path", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip the C1/C2/C4 legs")
     return ap.parse_args()
 
 
@@ -154,26 +155,120 @@ def _oracle_chunk(args):
     return px, time.perf_counter() - t
 
 
-def cpu_baseline_single(paths, sizes, rules, seconds):
+def cpu_baseline_single(paths, sizes, rules, seconds, gpu_masks=None):
     """The oracle (reference algorithm restated in C, f64) on 1 thread over a
-    bounded prefix sample of the same batch."""
+    bounded prefix sample of the same batch.  With ``gpu_masks(i)`` it also
+    returns the max / mean absolute difference of the GPU masks of that
+    sample against the oracle's."""
+    import numpy as np
     from oracle import oracle as O
     from rasterize_gb300 import Transform
     O.build()
-    t0 = time.perf_counter()
-    px, segs, n = 0, 0, 0
+    px, segs, n, dt = 0, 0, 0, 0.0
+    emax, esum, en = 0.0, 0.0, 0
     for i in range(len(paths)):
         w, h = sizes[i]
-        O.mask(paths[i], Transform.identity(), rules[i], w, h)
+        t = time.perf_counter()
+        ref = O.mask(paths[i], Transform.identity(), rules[i], w, h)
+        dt += time.perf_counter() - t
         px += w * h
         segs += paths[i].n_segments
         n += 1
-        if time.perf_counter() - t0 > seconds:
+        if gpu_masks is not None:
+            e = np.abs(gpu_masks(i).astype(np.float64) - ref)
+            emax = max(emax, float(e.max()))
+            esum += float(e.sum())
+            en += e.size
+        if dt > seconds:
             break
-    dt = time.perf_counter() - t0
-    return {"value": round(px / dt / 1e6, 3), "unit": "Mpx/s", "cores": 1, "kind": "port",
-            "sample": "first %d of 10000 glyphs (%.1f Mpx, %d segments) in %.2f s" % (n, px / 1e6, segs, dt),
-            "masks_per_s": round(n / dt, 2)}
+    out = {"value": round(px / dt / 1e6, 3), "unit": "Mpx/s", "cores": 1, "kind": "port",
+           "sample": "first %d of 10000 glyphs (%.1f Mpx, %d segments) in %.2f s" % (n, px / 1e6, segs, dt),
+           "masks_per_s": round(n / dt, 2)}
+    err = None
+    if gpu_masks is not None:
+        err = {"max_abs": emax, "mean_abs": esum / max(en, 1), "tolerance": 1e-4, "glyphs_checked": n}
+    return out, err
+
+
+def _event_ms(stream, fn, steps):
+    """Median CUDA-event time of ``fn`` on ``stream`` (host buffers in and out)."""
+    import torch
+    ts = []
+    for _ in range(steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b))
+    return statistics.median(ts)
+
+
+def _config_err(gpu, ref):
+    import numpy as np
+    e = np.abs(gpu.astype(np.float64) - ref.astype(np.float64))
+    return {"max_abs": float(e.max()), "mean_abs": float(e.mean()), "tolerance": 1e-4}
+
+
+def run_configs(R, stream):
+    """The other single-GPU configurations, each through the public API with
+    host buffers (the ``gpu`` timing) and a CPU-baseline leg that times the
+    oracle on the same input once and reports the GPU's error against it."""
+    import numpy as np
+    from oracle import oracle as O
+    from rasterize_gb300 import FillRule, Transform
+    from rasterize_gb300 import workloads as W
+    out = {}
+    # C1: one closed path of 200 cubics in [0,512]^2, NonZero, 512x512 f64 mask
+    path, _, _ = W.small_path(seed=0, n_cubics=200, size=512)
+    img = np.zeros((512, 512))
+
+    def c1():
+        img[:] = 0.0
+        R.mask(path, Transform.identity(), img, FillRule.NonZero)
+    c1()
+    ms = _event_ms(stream, c1, 10)
+    t = time.perf_counter()
+    ref = O.mask(path, Transform.identity(), FillRule.NonZero, 512, 512)
+    cpu_s = time.perf_counter() - t
+    out["C1_small_path"] = {"ms": round(ms, 4), "mpx_per_s": round(512 * 512 / ms / 1e3, 1),
+                            "segments_per_s": round(200 / ms * 1e3, 1), "err": _config_err(img, ref),
+                            "cpu_baseline_ms": round(cpu_s * 1e3, 3), "cores": 1}
+    # C2: 20,000 mixed segments in [0,4096]^2 (10 % arcs, 1 % degenerate cubics), EvenOdd, 4096^2
+    path, rule, _ = W.large_path(seed=1, n_segments=20000, size=4096)
+    img = np.zeros((4096, 4096))
+
+    def c2():
+        img[:] = 0.0
+        R.mask(path, Transform.identity(), img, rule)
+    c2()
+    ms = _event_ms(stream, c2, 5)
+    t = time.perf_counter()
+    ref = O.mask(path, Transform.identity(), rule, 4096, 4096)
+    cpu_s = time.perf_counter() - t
+    out["C2_large_path"] = {"ms": round(ms, 3), "mpx_per_s": round(4096 * 4096 / ms / 1e3, 1),
+                            "segments_per_s": round(20000 / ms * 1e3, 1), "err": _config_err(img, ref),
+                            "cpu_baseline_ms": round(cpu_s * 1e3, 1), "cores": 1,
+                            "note": "host f64 image in and out; the time includes the 128 MiB copies"}
+    # C4: 2000 filled paths, affine transforms, 50 % solid / 25 % linear / 25 % radial, 2048^2 RGBA f32
+    sc = W.scene(seed=3, n=2000, size=2048)
+    canvas = {}
+
+    def c4():
+        canvas["c"] = R.render_scene(sc, 2048, 2048, bg=(0.0, 0.0, 0.0, 1.0))
+    c4()
+    ms = _event_ms(stream, c4, 5)
+    paths_ = [f[0] for f in sc.fills]
+    t = time.perf_counter()
+    from tests.paint_oracle import oracle_scene
+    ref = oracle_scene(sc, 2048, 2048, bg=(0.0, 0.0, 0.0, 1.0))
+    cpu_s = time.perf_counter() - t
+    nseg = sum(p.n_segments for p in paths_)
+    out["C4_scene"] = {"ms": round(ms, 3), "mpx_per_s": round(2048 * 2048 / ms / 1e3, 1),
+                       "segments_per_s": round(nseg / ms * 1e3, 1), "err": _config_err(canvas["c"], ref),
+                       "cpu_baseline_ms": round(cpu_s * 1e3, 1), "cores": 1,
+                       "note": "error per colour channel; host canvas in and out"}
+    return out
 
 
 def run_reference(args, rank, world):
@@ -249,17 +344,7 @@ def main():
     plan.status()
     torch.cuda.synchronize(dev)
 
-    # ---- accuracy on a sample (oracle is the checker)
-    from oracle import oracle as O
     out_host = d_out.cpu().numpy()
-    err_max, err_sum, err_n = 0.0, 0.0, 0
-    for i in range(0, len(paths), max(1, len(paths) // 200)):
-        w, h = sizes[i]
-        ref = O.mask(paths[i], Transform.identity(), rules[i], w, h)
-        e = np.abs(batch.mask(out_host, i) - ref)
-        err_max = max(err_max, float(e.max()))
-        err_sum += float(e.sum())
-        err_n += e.size
 
     # ---- timed region: device-resident batch, graph replay
     if world > 1:
@@ -331,7 +416,8 @@ def main():
     algo_bytes = px * 4 + batch.n_segments * (64 + 1) + (len(batch.sub_off) + len(batch.path_sub)) * 4
     achieved = algo_bytes / (kernel_ms / 1e3) / 1e9
     traffic = profile_traffic("mask_bands_glyph_batch")
-    cpu = cpu_baseline_single(paths, sizes, rules, args.cpu_seconds)
+    cpu, err = cpu_baseline_single(paths, sizes, rules, args.cpu_seconds, gpu_masks=lambda i: batch.mask(out_host, i))
+    configs = None if args.no_configs else run_configs(R, stream)
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "Mpx/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
@@ -343,8 +429,7 @@ def main():
         "masks_per_s": round(len(paths) * world / (ms_per_step / 1e3), 1),
         "per_path": per_path,
         "batched_vs_per_path": round(per_path["ms_per_step"] / ms_per_step, 2) if per_path else None,
-        "err": {"max_abs": err_max, "mean_abs": err_sum / max(err_n, 1), "tolerance": 1e-4,
-                "sampled_glyphs": len(range(0, len(paths), max(1, len(paths) // 200)))},
+        "err": err,
         "work_items": n_items, "f64_fallbacks_total": fallbacks,
         "e2e": {"value": round(px / (e2e_ms / 1e3) / 1e6, 2), "unit": "Mpx/s", "ms_per_step": round(e2e_ms, 3),
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
@@ -355,6 +440,7 @@ def main():
         "cpu_baseline": cpu,
         "gpu_launches": args.steps,
         "clocks": clk,
+        "configs": configs,
     }
     print(json.dumps(out))
 

@@ -8,11 +8,14 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/rasterize_gb300.h"
@@ -106,6 +109,69 @@ struct rz_ctx {
 
 namespace {
 
+// Host phase timing of an entry point, printed to stderr when RZ_TRACE is set.
+struct Trace {
+    bool on;
+    const char* name;
+    std::chrono::steady_clock::time_point t0, t;
+    std::string line;
+    explicit Trace(const char* n) : on(std::getenv("RZ_TRACE") != nullptr), name(n) {
+        if (on) t0 = t = std::chrono::steady_clock::now();
+    }
+    // with tracing on, waits for the stream first so the phase includes its GPU work
+    void gpu_mark(cudaStream_t st, const char* phase) {
+        if (!on) return;
+        cudaStreamSynchronize(st);
+        mark(phase);
+    }
+    void mark(const char* phase) {
+        if (!on) return;
+        const auto now = std::chrono::steady_clock::now();
+        char buf[96];
+        std::snprintf(buf, sizeof(buf), " %s %.3f", phase, std::chrono::duration<double, std::milli>(now - t).count());
+        line += buf;
+        t = now;
+    }
+    ~Trace() {
+        if (!on) return;
+        const double total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        std::fprintf(stderr, "[rz] %s ms:%s | total %.3f\n", name, line.c_str(), total);
+    }
+};
+
+// Runs fn(lo, hi) over [0, n) split across the host cores (up to 16
+// threads); small ranges run on the calling thread.
+template <class F>
+void parallel_for(int64_t n, int64_t min_per_thread, F fn) {
+    const int64_t hw = std::max<int64_t>(1, (int64_t)std::thread::hardware_concurrency());
+    const int64_t t = std::min<int64_t>({hw, 16, n / std::max<int64_t>(min_per_thread, 1)});
+    if (t <= 1) {
+        fn((int64_t)0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    th.reserve((size_t)t - 1);
+    const int64_t chunk = (n + t - 1) / t;
+    for (int64_t i = 1; i < t; ++i) {
+        const int64_t lo = i * chunk, hi = std::min(n, lo + chunk);
+        if (lo < hi) th.emplace_back(fn, lo, hi);
+    }
+    fn((int64_t)0, std::min(n, chunk));
+    for (auto& x : th) x.join();
+}
+
+// Device address of page-locked host memory the GPU can write directly
+// (cudaHostAlloc / cudaHostRegister); null for pageable or device memory.
+void* mapped_host(const void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 rz_status fail(rz_ctx* c, rz_status st, const std::string& msg) {
     if (c) c->last_error = msg;
     return st;
@@ -167,11 +233,24 @@ void build_items(const std::vector<rz::MaskDev>& masks, bool grouped, Items& out
     }
     out.path_first[masks.size()] = (int)out.items.size();
     if (!grouped) {
-        std::stable_sort(out.items.begin(), out.items.end(), [&](const rz::WorkItem& a, const rz::WorkItem& b) {
-            const long ca = (long)a.rows * masks[a.path].width;
-            const long cb = (long)b.rows * masks[b.path].width;
-            return ca > cb;
-        });
+        // Decreasing band area on a log scale (16 buckets per octave), by a
+        // stable counting sort: linear time, and path order within a bucket.
+        constexpr int kBuckets = 32 * 16;
+        const size_t n = out.items.size();
+        std::vector<uint16_t> key(n);
+        std::vector<uint32_t> start(kBuckets + 1, 0);
+        for (size_t i = 0; i < n; ++i) {
+            const rz::WorkItem& w = out.items[i];
+            const uint32_t area = std::max<uint32_t>(1u, (uint32_t)w.rows * (uint32_t)masks[w.path].width);
+            const int lz = 31 - __builtin_clz(area);
+            const int frac = (int)(((uint64_t)area << (31 - lz)) >> 27) & 15;  // next 4 bits below the leading one
+            key[i] = (uint16_t)(kBuckets - 1 - std::min(kBuckets - 1, lz * 16 + frac));
+            ++start[key[i] + 1];
+        }
+        for (int k = 0; k < kBuckets; ++k) start[k + 1] += start[k];
+        std::vector<rz::WorkItem> sorted(n);
+        for (size_t i = 0; i < n; ++i) sorted[start[key[i]]++] = out.items[i];
+        out.items.swap(sorted);
     }
 }
 
@@ -254,8 +333,7 @@ rz_status stage_host(rz_ctx* ctx, const uint8_t* kind, const double* pts, uint32
                      uint32_t n_sub, const uint32_t* path_sub, uint32_t n_paths, const double* tr,
                      const uint8_t* rule, rz::BatchDev& b) {
     // arcs are converted to cubics on the host, as PathBuilder::arc_to does
-    bool has_arc = false;
-    for (uint32_t i = 0; i < n_seg && !has_arc; ++i) has_arc = kind[i] == RZ_SEG_ARC;
+    const bool has_arc = n_seg && std::memchr(kind, RZ_SEG_ARC, n_seg) != nullptr;
     ctx->expanded = has_arc;
     if (has_arc) {
         if (!rzhost::expand_batch(kind, pts, sub_off, path_sub, n_paths, ctx->x_kind, ctx->x_pts, ctx->x_sub,
@@ -473,9 +551,17 @@ rz_status rz_mask(rz_ctx* ctx, const rz_path* path, const double tr[6], int32_t 
     st = read_error(ctx);
     if (st) return st;
     const float* src = (const float*)ctx->h_out.p;
-    for (uint64_t y = 0; y < shape.height; ++y)
-        for (uint64_t x = 0; x < shape.width; ++x)
-            img[shape.start + y * shape.row_stride + x * shape.col_stride] = (double)src[y * shape.width + x];
+    parallel_for((int64_t)shape.height, 64, [&](int64_t y0, int64_t y1) {
+        for (int64_t y = y0; y < y1; ++y) {
+            const float* s = src + (uint64_t)y * shape.width;
+            double* d = img + shape.start + (uint64_t)y * shape.row_stride;
+            if (shape.col_stride == 1) {
+                for (uint64_t x = 0; x < shape.width; ++x) d[x] = (double)s[x];
+            } else {
+                for (uint64_t x = 0; x < shape.width; ++x) d[x * shape.col_stride] = (double)s[x];
+            }
+        }
+    });
     return RZ_OK;
 }
 
@@ -517,6 +603,7 @@ static rz_status mask_batch_impl(rz_ctx* ctx, const rz_path_batch* batch, double
     if (!batch || !out || !batch->masks) return fail(ctx, RZ_ERR_INVALID, "null argument");
     if (!valid_flatness(flatness)) return fail(ctx, RZ_ERR_INVALID, "flatness must be > 0 and finite");
     RZ_CUDA(cudaSetDevice(ctx->device));
+    Trace tr("rz_mask_batch");
     const uint32_t P = batch->n_paths;
     std::vector<rz::MaskDev> masks(P);
     for (uint32_t p = 0; p < P; ++p) {
@@ -543,9 +630,11 @@ static rz_status mask_batch_impl(rz_ctx* ctx, const rz_path_batch* batch, double
                 return fail(ctx, RZ_ERR_INVALID, "subpath_off decreasing");
         if (batch->subpath_off[batch->n_subpaths] > batch->n_segments)
             return fail(ctx, RZ_ERR_INVALID, "subpath_off exceeds n_segments");
+        tr.mark("validate");
         st = stage_host(ctx, batch->seg_kind, batch->seg_pts, batch->n_segments, batch->subpath_off,
                         batch->n_subpaths, batch->path_subpath_off, P, batch->transforms, batch->fill_rules, b);
         if (st) return st;
+        tr.mark("stage_inputs");
     } else {
         b.kind = batch->seg_kind;
         b.pts = batch->seg_pts;
@@ -558,20 +647,28 @@ static rz_status mask_batch_impl(rz_ctx* ctx, const rz_path_batch* batch, double
     }
     Items items;
     build_items(masks, per_path, items);
+    tr.mark("items");
     st = stage_plan(ctx, masks, items, b);
     if (st) return st;
     set_thresholds(b, flatness);
-    if (batch->memory == RZ_MEM_HOST) {
+    // page-locked host output: the kernel writes the masks straight into it
+    // (over NVLink-C2C on Grace), so no device copy and no copy back
+    void* direct_out = batch->memory == RZ_MEM_HOST ? mapped_host(out) : nullptr;
+    if (batch->memory == RZ_MEM_HOST && !direct_out) {
         RZ_CUDA(ctx->d_out.ensure(out_len * 4 + 16));
         b.out = (float*)ctx->d_out.p;
     } else {
-        b.out = out;
+        b.out = direct_out ? (float*)direct_out : out;
     }
+    tr.mark("stage_plan");
     st = run_bands(ctx, b, items, per_path);
     if (st) return st;
-    if (batch->memory == RZ_MEM_HOST)
+    if (batch->memory == RZ_MEM_HOST && !direct_out)
         RZ_CUDA(cudaMemcpyAsync(out, b.out, out_len * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    return read_error(ctx);
+    tr.mark("enqueue");
+    st = read_error(ctx);
+    tr.mark("sync");
+    return st;
 }
 
 rz_status rz_mask_batch(rz_ctx* ctx, const rz_path_batch* batch, double flatness, float* out, uint64_t out_len) {
@@ -904,6 +1001,7 @@ void add_fill(HostScene& hs, uint32_t sub0, uint32_t sub1, int col0, int row0, i
 // pixels when paints are given, else an f32 mask), stride in pixels.
 rz_status run_pipeline(rz_ctx* ctx, HostScene& hs, double flatness, float* canvas, int64_t canvas_stride, int canvas_w,
                        int canvas_h, const float* bg_dev, bool load_canvas) {
+    Trace tr("pipeline");
     const bool paint_mode = !hs.paints.empty();
     rz::SceneDev S{};
     S.kind = (const uint8_t*)ctx->d_kind.p;
@@ -954,7 +1052,9 @@ rz_status run_pipeline(rz_ctx* ctx, HostScene& hs, double flatness, float* canva
     RZ_CUDA(ctx->p_slots.ensure(ns * 4));
     S.slot_count = (uint32_t*)ctx->p_slots.p;
     RZ_CUDA(cudaMemsetAsync(S.slot_count, 0, ns * 4, ctx->stream));
+    tr.gpu_mark(ctx->stream, "upload");
     RZ_CUDA(rz::launch_flatten_count(S, ctx->stream));
+    tr.gpu_mark(ctx->stream, "flatten_count");
     const uint64_t ne = (uint64_t)hs.n_entries + 1;
     RZ_CUDA(ctx->p_scan.ensure(rz::scan_temp_words(std::max(ns, ne)) * 4 + 64));
     RZ_CUDA(rz::scan_u32(S.slot_count, ns, (uint32_t*)ctx->p_scan.p, ctx->stream));
@@ -976,6 +1076,7 @@ rz_status run_pipeline(rz_ctx* ctx, HostScene& hs, double flatness, float* canva
     RZ_CUDA(cudaMemsetAsync(S.entry_count, 0, ne * 4, ctx->stream));
     RZ_CUDA(cudaMemsetAsync(S.entry_cursor, 0, ne * 4, ctx->stream));
     RZ_CUDA(rz::launch_flatten_emit(S, ctx->stream));
+    tr.gpu_mark(ctx->stream, "flatten_emit");
     // 4) list starts per (fill, band)
     RZ_CUDA(cudaMemcpyAsync(S.entry_start, S.entry_count, ne * 4, cudaMemcpyDeviceToDevice, ctx->stream));
     RZ_CUDA(rz::scan_u32(S.entry_start, ne, (uint32_t*)ctx->p_scan.p, ctx->stream));
@@ -985,9 +1086,12 @@ rz_status run_pipeline(rz_ctx* ctx, HostScene& hs, double flatness, float* canva
     // 5) line lists
     RZ_CUDA(ctx->p_pairs.ensure((uint64_t)std::max(n_pairs, 1u) * 4));
     S.pairs = (uint32_t*)ctx->p_pairs.p;
+    tr.gpu_mark(ctx->stream, "entry_scan");
     RZ_CUDA(rz::launch_bin_scatter(S, ctx->stream));
+    tr.gpu_mark(ctx->stream, "bin_scatter");
     // 6) composite
     RZ_CUDA(rz::launch_composite(S, cov_stride, smem, ctx->stream));
+    tr.gpu_mark(ctx->stream, "composite");
     return read_error(ctx);
 }
 
@@ -1073,20 +1177,24 @@ rz_status rz_fill(rz_ctx* ctx, const rz_path* path, const double tr[6], int32_t 
     const size_t n = (size_t)W * H;
     RZ_CUDA(ctx->h_out.ensure(n * 16));
     float* h = (float*)ctx->h_out.p;
-    for (int y = 0; y < H; ++y)
-        for (int x = 0; x < W; ++x)
-            std::memcpy(h + 4 * ((size_t)y * W + x), img + 4 * (shape.start + y * shape.row_stride + x * shape.col_stride),
-                        16);
+    parallel_for(H, 64, [&](int64_t y0, int64_t y1) {
+        for (int64_t y = y0; y < y1; ++y)
+            for (int x = 0; x < W; ++x)
+                std::memcpy(h + 4 * ((size_t)y * W + x),
+                            img + 4 * (shape.start + y * shape.row_stride + x * shape.col_stride), 16);
+    });
     RZ_CUDA(ctx->p_canvas.ensure(n * 16));
     RZ_CUDA(cudaMemcpyAsync(ctx->p_canvas.p, h, n * 16, cudaMemcpyHostToDevice, ctx->stream));
     st = run_pipeline(ctx, hs, flatness, (float*)ctx->p_canvas.p, W, W, H, nullptr, true);
     if (st) return st;
     RZ_CUDA(cudaMemcpyAsync(h, ctx->p_canvas.p, n * 16, cudaMemcpyDeviceToHost, ctx->stream));
     RZ_CUDA(cudaStreamSynchronize(ctx->stream));
-    for (int y = 0; y < H; ++y)
-        for (int x = 0; x < W; ++x)
-            std::memcpy(img + 4 * (shape.start + y * shape.row_stride + x * shape.col_stride), h + 4 * ((size_t)y * W + x),
-                        16);
+    parallel_for(H, 64, [&](int64_t y0, int64_t y1) {
+        for (int64_t y = y0; y < y1; ++y)
+            for (int x = 0; x < W; ++x)
+                std::memcpy(img + 4 * (shape.start + y * shape.row_stride + x * shape.col_stride),
+                            h + 4 * ((size_t)y * W + x), 16);
+    });
     return RZ_OK;
 }
 
@@ -1111,20 +1219,36 @@ rz_status rz_render_scene(rz_ctx* ctx, const rz_scene* scene, double flatness, c
     for (uint32_t p = 0; p < scene->n_paints; ++p)
         if (scene->paints[p].n_stops > (uint32_t)rz::kMaxStops) return fail(ctx, RZ_ERR_INVALID, "more than 16 stops");
     RZ_CUDA(cudaSetDevice(ctx->device));
+    Trace tr("rz_render_scene");
     HostScene hs;
     std::vector<uint32_t> fsub;
     rz_status st = stage_scene_segments(ctx, scene->seg_kind, scene->seg_pts, scene->n_segments, scene->subpath_off,
                                         scene->n_subpaths, scene->fill_subpath_off, F, hs, fsub);
     if (st) return st;
+    tr.mark("stage_segments");
     const int W = (int)width, H = (int)height;
     hs.band_rows = choose_band_rows(W, H, true);
     const rzhost::Xf id{{1, 0, 0, 0, 1, 0}};
+    // tight bounding boxes of every fill (transformed; untransformed only for
+    // BoundingBox paint units), computed in parallel
+    std::vector<rzhost::Box> pbox(F), ubox(F);
+    std::vector<uint8_t> have_p(F, 0), have_u(F, 0);
+    parallel_for((int64_t)F, 8, [&](int64_t f0, int64_t f1) {
+        for (int64_t f = f0; f < f1; ++f) {
+            rzhost::Xf t = id;
+            if (scene->transforms) std::memcpy(t.m, scene->transforms + 6ull * f, sizeof(t.m));
+            have_p[f] = rzhost::path_bbox(hs.kind, hs.pts, hs.sub_off, fsub[f], fsub[f + 1], t, pbox[f]);
+            if (have_p[f] && scene->paints[scene->fill_paint[f]].units == RZ_UNITS_BOUNDING_BOX)
+                have_u[f] = rzhost::path_bbox(hs.kind, hs.pts, hs.sub_off, fsub[f], fsub[f + 1], id, ubox[f]);
+        }
+    });
+    tr.mark("bbox");
     for (uint32_t f = 0; f < F; ++f) {
         rzhost::Xf t = id;
         if (scene->transforms) std::memcpy(t.m, scene->transforms + 6ull * f, sizeof(t.m));
         // Pipeline::build_rec Fill: bbox of the path, intersected with the view (src/scene.rs:288-298)
-        rzhost::Box pb{};
-        if (!rzhost::path_bbox(hs.kind, hs.pts, hs.sub_off, fsub[f], fsub[f + 1], t, pb)) continue;
+        if (!have_p[f]) continue;
+        const rzhost::Box pb = pbox[f];
         const double vx1 = (double)W, vy1 = (double)H;
         if (0.0 > pb.x1 || pb.x0 > vx1 || 0.0 > pb.y1 || pb.y0 > vy1) continue;
         const rzhost::Box nb{std::fmax(0.0, pb.x0), std::fmax(0.0, pb.y0), std::fmin(vx1, pb.x1), std::fmin(vy1, pb.y1)};
@@ -1143,10 +1267,8 @@ rz_status rz_render_scene(rz_ctx* ctx, const rz_scene* scene, double flatness, c
         const rzhost::Xf tr_fill = rzhost::xf_mul(align, t);
         const int vw = (int)(col_max - col_min), vh = (int)(row_max - row_min);
         if (vw <= 0 || vh <= 0) continue;
-        rzhost::Box bb0{};
-        const bool have = rzhost::path_bbox(hs.kind, hs.pts, hs.sub_off, fsub[f], fsub[f + 1], id, bb0);
         rz::PaintDev pd;
-        prepare_paint(scene->paints[scene->fill_paint[f]], tr_fill, have, bb0, pd);
+        prepare_paint(scene->paints[scene->fill_paint[f]], tr_fill, have_u[f] != 0, ubox[f], pd);
         if (pd.kind < 0) continue;
         hs.paints.push_back(pd);
         const int rule = scene->fill_rules ? scene->fill_rules[f] : 0;
@@ -1154,6 +1276,7 @@ rz_status rz_render_scene(rz_ctx* ctx, const rz_scene* scene, double flatness, c
                  (int)hs.paints.size() - 1);
     }
     if (hs.paints.empty()) hs.paints.resize(1);  // paint mode even with nothing to draw
+    tr.mark("fills");
     const size_t n = (size_t)W * H;
     RZ_CUDA(ctx->p_canvas.ensure(n * 16 + 16));
     RZ_CUDA(ctx->d_counts.ensure(64));
@@ -1162,8 +1285,21 @@ rz_status rz_render_scene(rz_ctx* ctx, const rz_scene* scene, double flatness, c
     RZ_CUDA(cudaMemcpyAsync(ctx->d_counts.p, bgv, 16, cudaMemcpyHostToDevice, ctx->stream));
     st = run_pipeline(ctx, hs, flatness, (float*)ctx->p_canvas.p, W, W, H, (const float*)ctx->d_counts.p, false);
     if (st) return st;
-    RZ_CUDA(cudaMemcpyAsync(canvas, ctx->p_canvas.p, n * 16, cudaMemcpyDeviceToHost, ctx->stream));
-    RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+    tr.mark("pipeline");
+    if (mapped_host(canvas)) {
+        RZ_CUDA(cudaMemcpyAsync(canvas, ctx->p_canvas.p, n * 16, cudaMemcpyDeviceToHost, ctx->stream));
+        RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+    } else {
+        // pageable canvas: page-locked staging, then a parallel host copy
+        RZ_CUDA(ctx->h_out.ensure(n * 16));
+        RZ_CUDA(cudaMemcpyAsync(ctx->h_out.p, ctx->p_canvas.p, n * 16, cudaMemcpyDeviceToHost, ctx->stream));
+        RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+        const char* src = (const char*)ctx->h_out.p;
+        parallel_for((int64_t)H, 16, [&](int64_t y0, int64_t y1) {
+            std::memcpy((char*)canvas + (size_t)y0 * W * 16, src + (size_t)y0 * W * 16, (size_t)(y1 - y0) * W * 16);
+        });
+    }
+    tr.mark("copy_out");
     return RZ_OK;
 }
 

@@ -332,9 +332,10 @@ __device__ __forceinline__ void sadd(float* p, int v) { atomicAdd(reinterpret_ca
 
 // Signed height `d` (fixed point) of one row, spread over the pixels the line
 // covers between xa and xn (FP32, relative to integer column xb) as in
-// signed_difference_line (src/rasterize.rs:433-466).  The pixel shares are
-// rounded and the last one takes the remainder, so the row receives exactly
-// `d` and the row prefix telescopes.
+// signed_difference_line (src/rasterize.rs:433-466).  Each pixel receives the
+// difference of the rounded cumulative shares, so every pixel is within one
+// fixed-point unit of the exact share however long the span, and the row
+// receives exactly `d` (the row prefix telescopes).
 __device__ __forceinline__ void accumulate_row(const Band& B, int r, int xb, float xa, float xn, int d) {
     const float df = (float)d;
     const float xlo = fminf(xa, xn), xhi = fmaxf(xa, xn);
@@ -354,23 +355,25 @@ __device__ __forceinline__ void accumulate_row(const Band& B, int r, int xb, flo
     const float s = 1.f / (xhi - xlo);
     const float x0f = xlo - x0_floor;
     const float x1f = xhi - x1_ceil + 1.f;
-    const float a0 = 0.5f * s * (1.f - x0f) * (1.f - x0f);
-    const float am = 0.5f * s * x1f * x1f;
+    const float a0 = 0.5f * s * (1.f - x0f) * (1.f - x0f);  // share of the first pixel
+    const float am = 0.5f * s * x1f * x1f;                  // share of the last pixel
     const int c0 = __float2int_rn(df * a0);
-    const int cm = __float2int_rn(df * am);
+    const int c_end = __float2int_rn(df * (1.f - am));  // cumulative through pixel x1i - 1
     sadd(row + x0i, c0);
     if (x1i == x0i + 2) {
-        sadd(row + x0i + 1, d - c0 - cm);
+        sadd(row + x0i + 1, c_end - c0);
     } else {
-        const float a1 = s * (1.5f - x0f);
-        const int c1 = __float2int_rn(df * (a1 - a0));
-        sadd(row + x0i + 1, c1);
-        const int cs = __float2int_rn(df * s);
-        for (int xi = x0i + 2; xi < x1i - 1; ++xi) sadd(row + xi, cs);
-        const int n_mid = max(x1i - x0i - 3, 0);
-        sadd(row + x1i - 1, d - c0 - cm - c1 - n_mid * cs);
+        const float a1 = s * (1.5f - x0f);  // cumulative through pixel x0i + 1
+        int prev = __float2int_rn(df * a1);
+        sadd(row + x0i + 1, prev - c0);
+        for (int xi = x0i + 2; xi < x1i - 1; ++xi) {
+            const int cur = __float2int_rn(df * fmaf((float)(xi - x0i - 1), s, a1));
+            sadd(row + xi, cur - prev);
+            prev = cur;
+        }
+        sadd(row + x1i - 1, c_end - prev);
     }
-    sadd(row + x1i, cm);
+    sadd(row + x1i, d - c_end);
 }
 
 constexpr int kShortLine = 32;

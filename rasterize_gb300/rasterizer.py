@@ -203,24 +203,28 @@ class Scene:
 
     def __init__(self):
         self.fills = []  # (path, transform, fill_rule, paint)
+        self._packed = None
 
     def fill(self, path: Path, paint, tr: Transform | None = None, fill_rule: FillRule = FillRule.NonZero):
         self.fills.append((path, tr or Transform.identity(), FillRule(fill_rule), paint))
+        self._packed = None
         return self
 
     def pack(self):
-        """(rz_scene struct, keepalive) over host arrays."""
+        """(rz_scene struct, keepalive) over host arrays, built once per
+        set of fills (``fill`` invalidates it)."""
+        if self._packed is not None and self._packed[2] == len(self.fills):
+            return self._packed[0], self._packed[1]
         paths = [f[0] for f in self.fills]
         n = len(paths)
         kind = np.ascontiguousarray(np.concatenate([p.kind for p in paths]) if n else np.zeros(0, np.uint8))
         pts = np.ascontiguousarray(np.concatenate([p.pts for p in paths]) if n else np.zeros((0, 8)))
-        sub, fsub, base = [0], [0], 0
-        for p in paths:
-            sub.extend((p.subpath_off[1:].astype(np.int64) + base).tolist())
-            base += p.n_segments
-            fsub.append(len(sub) - 1)
-        sub = np.ascontiguousarray(np.asarray(sub, dtype=np.uint32))
-        fsub = np.ascontiguousarray(np.asarray(fsub, dtype=np.uint32))
+        nseg = np.array([p.n_segments for p in paths], dtype=np.int64)
+        seg_base = np.concatenate([[0], np.cumsum(nseg)[:-1]]) if n else np.zeros(0, np.int64)
+        parts = [np.zeros(1, np.int64)] + [p.subpath_off[1:].astype(np.int64) + b for p, b in zip(paths, seg_base)]
+        sub = np.ascontiguousarray(np.concatenate(parts).astype(np.uint32))
+        nsub = np.array([len(p.subpath_off) - 1 for p in paths], dtype=np.int64)
+        fsub = np.ascontiguousarray(np.concatenate([[0], np.cumsum(nsub)]).astype(np.uint32))
         trs = np.ascontiguousarray(np.array([f[1].m for f in self.fills], dtype=np.float64).reshape(-1))
         rules = np.ascontiguousarray(np.array([int(f[2]) for f in self.fills], dtype=np.uint8))
         structs, keep = [], []
@@ -233,7 +237,9 @@ class Scene:
         s = _ffi.RzScene(n, int(kind.shape[0]), len(sub) - 1, n, kind.ctypes.data, pts.ctypes.data, sub.ctypes.data,
                          fsub.ctypes.data, trs.ctypes.data if n else None, rules.ctypes.data if n else None,
                          fpaint.ctypes.data if n else None, ctypes.addressof(paints))
-        return s, (kind, pts, sub, fsub, trs, rules, fpaint, paints, keep)
+        keepalive = (kind, pts, sub, fsub, trs, rules, fpaint, paints, keep)
+        self._packed = (s, keepalive, n)
+        return s, keepalive
 
 
 class BatchPlan:
