@@ -267,6 +267,44 @@ RZ_API rz_status rz_mask_batch_noalloc(const rz_path_batch* batch, double flatne
 RZ_API rz_status rz_flatten_counts(rz_ctx* ctx, const rz_path* path, const double tr[6], double flatness,
                             uint32_t* counts, uint64_t cap, uint64_t* n_counts);
 
+/* ------------------------------------------------------------------------
+ * Differentiable batch.  The reference has no adjoint; the forward composes
+ * Rasterizer::fill (src/rasterize.rs:69-115: mask_iter with the image size,
+ * then source-over) for closed cubic paths drawn in order with one solid paint
+ * of alpha `paint_alpha`, and keeps the alpha channel of each image.
+ *
+ * Control points are FP32 in device memory: image i, path p, point j at
+ * ctrl[2 * ((i * paths_per_image + p) * 3 * segs_per_path + j)] (x, y).
+ * Segment s of a path is the cubic (V_s, C1_s, C2_s, V_{(s+1) mod segs}) with
+ * V_s = point 3s, C1_s = point 3s + 1, C2_s = point 3s + 2, so every path is
+ * closed.  Images are width x height f32, row-major, image i at offset
+ * i * width * height.
+ * ------------------------------------------------------------------------ */
+typedef struct rz_diff_batch {
+    uint32_t n_images;
+    uint32_t paths_per_image;
+    uint32_t segs_per_path;
+    uint32_t width, height;
+    int32_t fill_rule;   /* RZ_FILL_NONZERO or RZ_FILL_EVENODD */
+    float paint_alpha;   /* 0 < alpha < 1 */
+    const float* ctrl;   /* device memory */
+} rz_diff_batch;
+
+/* Forward: every image (device memory, overwritten). */
+RZ_API rz_status rz_diff_forward(rz_ctx* ctx, const rz_diff_batch* batch, double flatness, float* image);
+
+/* sum over n of (image - target)^2 into *loss (host, binary64 accumulation);
+ * dl_dimage (device, may be null) receives 2 (image - target). */
+RZ_API rz_status rz_l2_loss(rz_ctx* ctx, const float* image, const float* target, uint64_t n, double* loss,
+                            float* dl_dimage);
+
+/* Adjoint: d loss / d control points (device memory, same layout as ctrl,
+ * overwritten) from d loss / d image (device), given the forward `image`.
+ * The bisection tree is held fixed and every flattened line is recomputed
+ * (nothing is stored between the passes). */
+RZ_API rz_status rasterize_backward(rz_ctx* ctx, const rz_diff_batch* batch, double flatness, const float* image,
+                                    const float* dl_dimage, float* dl_dctrl);
+
 #ifdef __cplusplus
 }
 #endif

@@ -349,3 +349,40 @@ def scene_render(paths, trs, rules, paints, width, height, bg=(0, 0, 0, 0), flat
     if rc < 0:
         raise OracleError("cannot flatten segment with NaN")
     return canvas
+
+
+# --------------------------------------------------------------------------- differentiable batch
+def diff_forward(ctrl, n_paths, segs, width, height, alpha=0.5, rule=0, flatness=0.05, frozen=None):
+    """Alpha channel of ``n_paths`` closed cubic paths (``segs`` segments each,
+    control points ``ctrl`` of shape (n_paths, 3*segs, 2)) filled in order with
+    a solid paint of alpha ``alpha`` (source-over).  ``frozen``: control points
+    whose bisection tree is reused (finite differences, tree held fixed)."""
+    c = np.ascontiguousarray(ctrl, dtype=np.float64).reshape(-1)
+    fz = None if frozen is None else np.ascontiguousarray(frozen, dtype=np.float64).reshape(-1)
+    img = np.zeros((height, width))
+    L = lib()
+    L.rzo_diff_forward.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_long, ctypes.c_long, ctypes.c_long,
+                                   ctypes.c_long, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_void_p]
+    rc = L.rzo_diff_forward(_ptr(c), _ptr(fz) if fz is not None else None, n_paths, segs, width, height, alpha,
+                            int(rule), flatness, _ptr(img))
+    if rc < 0:
+        raise OracleError("cannot flatten segment with NaN")
+    return img
+
+
+def diff_backward(ctrl, n_paths, segs, width, height, image, dl_dimage, alpha=0.5, rule=0, flatness=0.05):
+    """d loss / d control points (shape of ``ctrl``) from d loss / d image, the
+    tree held fixed (binary64)."""
+    c = np.ascontiguousarray(ctrl, dtype=np.float64).reshape(-1)
+    img = np.ascontiguousarray(image, dtype=np.float64)
+    dl = np.ascontiguousarray(dl_dimage, dtype=np.float64)
+    out = np.zeros_like(c)
+    L = lib()
+    L.rzo_diff_backward.argtypes = [ctypes.c_void_p, ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.c_long,
+                                    ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_void_p]
+    rc = L.rzo_diff_backward(_ptr(c), n_paths, segs, width, height, alpha, int(rule), flatness, _ptr(img), _ptr(dl),
+                             _ptr(out))
+    if rc < 0:
+        raise OracleError("cannot flatten segment with NaN")
+    return out.reshape(np.shape(ctrl))

@@ -1139,3 +1139,313 @@ int rzo_scene_render(const uint8_t* kind, const double* pts, const uint32_t* sub
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Differentiable batch.  The reference has no adjoint: this composes its   */
+/* Rasterizer::fill (rasterize.rs:69-115, i.e. mask_iter with the image     */
+/* size :313-355, then source-over) for closed cubic paths drawn in order   */
+/* with a solid paint of alpha `a` (the alpha channel of the image), and    */
+/* adds the adjoint of that image with respect to every control point, the  */
+/* bisection tree held fixed.                                               */
+/*                                                                          */
+/* Control points of one image: point j of path p at ctrl[2 * (p * 3 * segs */
+/* + j)]; segment s is the cubic (V_s, C1_s, C2_s, V_{(s+1) mod segs}) with  */
+/* V_s = point 3s, C1_s = 3s + 1, C2_s = 3s + 2.  The closing line of every  */
+/* path starts and ends at V_0 and adds nothing.                            */
+/* ------------------------------------------------------------------------ */
+
+typedef struct { pt a, b; int seg; double t0, t1; } tline_t;
+typedef struct { tline_t* v; long n, cap; } tline_vec;
+
+static void tline_push(tline_vec* lv, tline_t l) {
+    if (lv->n == lv->cap) {
+        lv->cap = lv->cap ? 2 * lv->cap : 1024;
+        lv->v = (tline_t*)realloc(lv->v, sizeof(tline_t) * lv->cap);
+    }
+    lv->v[lv->n++] = l;
+}
+
+static void diff_indices(int s, int segs, int idx[4]) {
+    idx[0] = 3 * s; idx[1] = 3 * s + 1; idx[2] = 3 * s + 2; idx[3] = 3 * ((s + 1) % segs);
+}
+
+static seg diff_segment(const double* ctrl, long p, int segs, int s) {
+    seg c;
+    c.kind = SEG_CUBIC;
+    const double* b = ctrl + 2L * p * 3 * segs;
+    int idx[4];
+    diff_indices(s, segs, idx);
+    for (int k = 0; k < 4; k++) c.p[k] = (pt){b[2 * idx[k]], b[2 * idx[k] + 1]};
+    return c;
+}
+
+static void bernstein3(double t, double b[4]) {
+    double mt = 1.0 - t;
+    b[0] = mt * mt * mt; b[1] = 3.0 * t * mt * mt; b[2] = 3.0 * t * t * mt; b[3] = t * t * t;
+}
+
+static pt bez3(const seg* c, double t) {
+    double b[4];
+    bernstein3(t, b);
+    pt r = {0.0, 0.0};
+    for (int k = 0; k < 4; k++) { r.x += b[k] * c->p[k].x; r.y += b[k] * c->p[k].y; }
+    return r;
+}
+
+/* PathFlattenIter on path p (path.rs:734-796) with every line's segment and
+ * parameter range.  With `frozen`, the tree of the `frozen` control points
+ * is used and the vertices are evaluated on `ctrl` at the same parameters
+ * (finite differences with the tree held fixed). */
+static int diff_flatten(const double* ctrl, const double* frozen, long p, int segs, double flatness, tline_vec* out) {
+    double thr = 16.0 * flatness * flatness;
+    typedef struct { seg s; double t0, t1; } node_t;
+    long cap = 256, top = 0;
+    node_t* stack = (node_t*)malloc(sizeof(node_t) * cap);
+    for (int s = 0; s < segs; s++) {
+        seg root = diff_segment(frozen ? frozen : ctrl, p, segs, s);
+        seg real = diff_segment(ctrl, p, segs, s);
+        top = 0;
+        stack[top++] = (node_t){root, 0.0, 1.0};
+        while (top > 0) {
+            node_t cur = stack[--top];
+            if (seg_has_nans(&cur.s)) { free(stack); return -1; }
+            if (seg_flatness(&cur.s) < thr) {
+                tline_t l;
+                l.seg = s; l.t0 = cur.t0; l.t1 = cur.t1;
+                if (frozen) { l.a = bez3(&real, cur.t0); l.b = bez3(&real, cur.t1); }
+                else { l.a = seg_start(&cur.s); l.b = seg_end(&cur.s); }
+                tline_push(out, l);
+                continue;
+            }
+            seg a, b;
+            seg_split(&cur.s, &a, &b);
+            double tm = 0.5 * (cur.t0 + cur.t1);
+            if (top + 2 > cap) { cap *= 2; stack = (node_t*)realloc(stack, sizeof(node_t) * cap); }
+            stack[top++] = (node_t){b, tm, cur.t1};
+            stack[top++] = (node_t){a, cur.t0, tm};
+        }
+    }
+    free(stack);
+    return 0;
+}
+
+/* Winding of every pixel of a W x H image from the lines of one path
+ * (mask_iter's (W+1)-column buffer and row prefix, rasterize.rs:325-352). */
+static void diff_winding(const tline_vec* lv, long W, long H, double* buf, double* wind) {
+    memset(buf, 0, sizeof(double) * (size_t)((W + 1) * H));
+    img_t im = {buf, (W + 1) * H, 0, W + 1, H, W + 1, 1};
+    for (long i = 0; i < lv->n; i++) {
+        line_t l = {lv->v[i].a, lv->v[i].b};
+        signed_difference_line(&im, l);
+    }
+    for (long y = 0; y < H; y++) {
+        double acc = 0.0;
+        for (long x = 0; x < W; x++) {
+            acc += buf[y * (W + 1) + x];
+            wind[y * W + x] = acc;
+        }
+    }
+}
+
+/* alpha as Rasterizer::fill uses it: pixels with |alpha| < 1e-6 are skipped */
+static double diff_alpha(int rule, double w) {
+    double a = rzo_alpha_from_winding(rule, w);
+    return fabs(a) < 1e-6 ? 0.0 : a;
+}
+
+static double diff_dalpha(int rule, double w) {
+    if (rule == RULE_EVENODD) {
+        double r = rem_euclid(w + 1.0, 2.0) - 1.0;
+        if (fabs(r) < 1e-6) return 0.0;
+        return r > 0.0 ? 1.0 : -1.0;
+    }
+    double v = fabs(w);
+    if (v >= 1.0 || v < 1e-6) return 0.0;
+    return w > 0.0 ? 1.0 : -1.0;
+}
+
+/* Image (alpha channel) of `n_paths` paths drawn in order; image: W x H, written. */
+int rzo_diff_forward(const double* ctrl, const double* frozen, long n_paths, long segs, long W, long H, double a,
+                     int rule, double flatness, double* image) {
+    memset(image, 0, sizeof(double) * (size_t)(W * H));
+    double* buf = (double*)malloc(sizeof(double) * (size_t)((W + 1) * H));
+    double* wind = (double*)malloc(sizeof(double) * (size_t)(W * H));
+    tline_vec lv = {0, 0, 0};
+    int rc = 0;
+    for (long p = 0; p < n_paths && rc == 0; p++) {
+        lv.n = 0;
+        if (diff_flatten(ctrl, frozen, p, (int)segs, flatness, &lv) < 0) { rc = -1; break; }
+        diff_winding(&lv, W, H, buf, wind);
+        for (long i = 0; i < W * H; i++) {
+            double al = diff_alpha(rule, wind[i]);
+            if (al == 0.0) continue;
+            image[i] = a * al + image[i] * (1.0 - a * al);
+        }
+    }
+    free(lv.v); free(buf); free(wind);
+    return rc;
+}
+
+typedef struct { double v, d[4]; } dual4;
+
+static dual4 dv_const(double v) { dual4 r = {v, {0, 0, 0, 0}}; return r; }
+static dual4 dv_add(dual4 a, dual4 b) { for (int k = 0; k < 4; k++) a.d[k] += b.d[k]; a.v += b.v; return a; }
+static dual4 dv_sub(dual4 a, dual4 b) { for (int k = 0; k < 4; k++) a.d[k] -= b.d[k]; a.v -= b.v; return a; }
+static dual4 dv_mul(dual4 a, dual4 b) {
+    dual4 r; r.v = a.v * b.v;
+    for (int k = 0; k < 4; k++) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
+    return r;
+}
+static dual4 dv_div(dual4 a, dual4 b) {
+    dual4 r; r.v = a.v / b.v;
+    for (int k = 0; k < 4; k++) r.d[k] = (a.d[k] - r.v * b.d[k]) / b.v;
+    return r;
+}
+static dual4 dv_lerp(dual4 a, dual4 b, dual4 t) {  /* (1 - t) a + t b */
+    return dv_add(dv_mul(dv_sub(dv_const(1.0), t), a), dv_mul(t, b));
+}
+
+/* Mean of W_row over [lo, hi] and its derivatives; W_row(X) = G[k+1] + (k+1-X) g[k]
+ * on [k, k+1) is the loss change per unit of signed height at X (G: suffix
+ * sums of g, G[W] = 0). */
+static void diff_row_mean(const double* G, const double* g, long W, double lo, double hi, double* I, double* dlo,
+                          double* dhi) {
+    if (lo < 0.0) lo = 0.0;
+    if (hi > (double)W) hi = (double)W;
+    if (hi < lo) hi = lo;
+    double D = hi - lo;
+    if (D < 1e-12) {
+        long k = (long)floor(lo);
+        if (k > W - 1) k = W - 1;
+        if (k < 0) k = 0;
+        *I = G[k + 1] + ((double)(k + 1) - lo) * g[k];
+        *dlo = *dhi = -0.5 * g[k];
+        return;
+    }
+    long k0 = (long)floor(lo), k1 = (long)floor(hi);
+    if (k1 > W - 1) k1 = W - 1;
+    double sI = 0.0, slo = 0.0, shi = 0.0;
+    for (long k = k0; k <= k1; k++) {
+        double a = fmax(lo, (double)k), b = fmin(hi, (double)(k + 1));
+        if (b <= a) continue;
+        double ka = (double)(k + 1) - a, kb = (double)(k + 1) - b;
+        sI += G[k + 1] * (b - a) + g[k] * 0.5 * (ka * ka - kb * kb);
+        shi += -g[k] * 0.5 * ((b - lo) * (b - lo) - (a - lo) * (a - lo));
+        slo += -g[k] * 0.5 * ((hi - a) * (hi - a) - (hi - b) * (hi - b));
+    }
+    *I = sI / D;
+    *dhi = shi / (D * D);
+    *dlo = slo / (D * D);
+}
+
+/* d(sum over pixels of g * winding contribution of the piece p -> q)/d(line ends) */
+static void diff_piece(dual4 px, dual4 py, dual4 qx, dual4 qy, long W, long H, const double* G, const double* g,
+                       double out[4]) {
+    if (fabs(py.v - qy.v) < 1e-300) {
+        /* horizontal: no coverage, but its height derivative moves coverage in */
+        long r = (long)floor(py.v);
+        if (r < 0 || r >= H) return;
+        double I, dlo, dhi;
+        diff_row_mean(G + r * (W + 1), g + r * W, W, fmin(px.v, qx.v), fmax(px.v, qx.v), &I, &dlo, &dhi);
+        for (int k = 0; k < 4; k++) out[k] += I * (qy.d[k] - py.d[k]);
+        return;
+    }
+    double dir = 1.0;
+    if (py.v > qy.v) { dual4 t = px; px = qx; qx = t; t = py; py = qy; qy = t; dir = -1.0; }
+    dual4 k_ = dv_div(dv_sub(qx, px), dv_sub(qy, py));  /* dx/dy */
+    long r0 = (long)floor(py.v), r1 = (long)ceil(qy.v);
+    if (r0 < 0) r0 = 0;
+    if (r1 > H) r1 = H;
+    for (long r = r0; r < r1; r++) {
+        int start_in = py.v >= (double)r, end_in = qy.v <= (double)(r + 1);
+        dual4 sa = start_in ? py : dv_const((double)r);
+        dual4 sb = end_in ? qy : dv_const((double)(r + 1));
+        if (sb.v <= sa.v) continue;
+        dual4 xa = start_in ? px : dv_add(px, dv_mul(dv_sub(sa, py), k_));
+        dual4 xn = end_in ? qx : dv_add(px, dv_mul(dv_sub(sb, py), k_));
+        dual4 h = dv_sub(sb, sa);
+        dual4 lo = xa.v <= xn.v ? xa : xn, hi = xa.v <= xn.v ? xn : xa;
+        double I, dlo, dhi;
+        diff_row_mean(G + r * (W + 1), g + r * W, W, lo.v, hi.v, &I, &dlo, &dhi);
+        for (int k = 0; k < 4; k++)
+            out[k] += dir * (I * h.d[k] + h.v * (dlo * lo.d[k] + dhi * hi.d[k]));
+    }
+}
+
+/* The x rules of signed_difference_line (rasterize.rs:372-393, 923-937) on
+ * dual numbers, then the pieces. */
+static void diff_line(pt a, pt b, long W, long H, const double* G, const double* g, double out[4]) {
+    dual4 x0 = {a.x, {1, 0, 0, 0}}, y0 = {a.y, {0, 1, 0, 0}}, x1 = {b.x, {0, 0, 1, 0}}, y1 = {b.y, {0, 0, 0, 1}};
+    double width = (double)W;
+    if (x0.v > width || x1.v > width) {
+        if (x0.v > width && x1.v > width) {
+            x0 = dv_const(width - 0.001);
+            x1 = dv_const(width - 0.001);
+        } else {
+            dual4 t = dv_div(dv_sub(x0, dv_const(width)), dv_sub(x0, x1));
+            dual4 my = dv_lerp(y0, y1, t);
+            if (x0.v < width) { x1 = dv_const(width); y1 = my; }
+            else { x0 = dv_const(width); y0 = my; }
+        }
+    }
+    if (x0.v >= 0.0 && x1.v >= 0.0) {
+        diff_piece(x0, y0, x1, y1, W, H, G, g, out);
+    } else if (x0.v <= 0.0 && x1.v <= 0.0) {
+        diff_piece(dv_const(0.0), y0, dv_const(0.0), y1, W, H, G, g, out);
+    } else {
+        dual4 t = dv_div(x0, dv_sub(x0, x1));
+        dual4 mx = dv_lerp(x0, x1, t), my = dv_lerp(y0, y1, t);
+        if (x0.v < 0.0) {
+            diff_piece(mx, my, x1, y1, W, H, G, g, out);
+            diff_piece(dv_const(0.0), y0, mx, my, W, H, G, g, out);
+        } else {
+            diff_piece(x0, y0, mx, my, W, H, G, g, out);
+            diff_piece(mx, my, dv_const(0.0), y1, W, H, G, g, out);
+        }
+    }
+}
+
+/* Adjoint: dl_dctrl (same layout as ctrl, overwritten) from dl_dimage, given
+ * the forward image.  d image / d alpha_p = a (1 - image) / (1 - a alpha_p)
+ * for source-over, so every path is independent once the image is known. */
+int rzo_diff_backward(const double* ctrl, long n_paths, long segs, long W, long H, double a, int rule,
+                      double flatness, const double* image, const double* dl_dimage, double* dl_dctrl) {
+    memset(dl_dctrl, 0, sizeof(double) * (size_t)(n_paths * 3 * segs * 2));
+    double* buf = (double*)malloc(sizeof(double) * (size_t)((W + 1) * H));
+    double* wind = (double*)malloc(sizeof(double) * (size_t)(W * H));
+    double* g = (double*)malloc(sizeof(double) * (size_t)(W * H));
+    double* G = (double*)malloc(sizeof(double) * (size_t)((W + 1) * H));
+    tline_vec lv = {0, 0, 0};
+    int rc = 0;
+    for (long p = 0; p < n_paths; p++) {
+        lv.n = 0;
+        if (diff_flatten(ctrl, NULL, p, (int)segs, flatness, &lv) < 0) { rc = -1; break; }
+        diff_winding(&lv, W, H, buf, wind);
+        for (long i = 0; i < W * H; i++) {
+            double al = diff_alpha(rule, wind[i]);
+            double da = al == 0.0 ? 0.0 : diff_dalpha(rule, wind[i]);
+            g[i] = da == 0.0 ? 0.0 : dl_dimage[i] * a * (1.0 - image[i]) / (1.0 - a * al) * da;
+        }
+        for (long y = 0; y < H; y++) {
+            G[y * (W + 1) + W] = 0.0;
+            for (long x = W - 1; x >= 0; x--) G[y * (W + 1) + x] = G[y * (W + 1) + x + 1] + g[y * W + x];
+        }
+        double* out = dl_dctrl + 2L * p * 3 * segs;
+        for (long i = 0; i < lv.n; i++) {
+            const tline_t* l = &lv.v[i];
+            double d4[4] = {0, 0, 0, 0};
+            diff_line(l->a, l->b, W, H, G, g, d4);
+            int idx[4];
+            diff_indices(l->seg, (int)segs, idx);
+            double b0[4], b1[4];
+            bernstein3(l->t0, b0);
+            bernstein3(l->t1, b1);
+            for (int j = 0; j < 4; j++) {
+                out[2 * idx[j]] += d4[0] * b0[j] + d4[2] * b1[j];
+                out[2 * idx[j] + 1] += d4[1] * b0[j] + d4[3] * b1[j];
+            }
+        }
+    }
+    free(lv.v); free(buf); free(wind); free(g); free(G);
+    return rc;
+}

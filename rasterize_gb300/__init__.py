@@ -11,11 +11,12 @@ from .path import (DEFAULT_FLATNESS, SEG_ARC, SEG_CUBIC, SEG_LINE, SEG_QUAD, Fil
                    SvgParserError, parse_svg_path)
 from ._ffi import NanError, RasterizeError
 from .paint import GradLinear, GradRadial, GradSpread, GradStop, LinColor, Units
-from .rasterizer import BatchPlan, Context, GpuRasterizer, MaskBatch, Pixel, Rasterizer, Scene, default_context
+from .rasterizer import (BatchPlan, Context, DiffBatch, GpuRasterizer, MaskBatch, Pixel, Rasterizer, Scene,
+                         default_context)
 
 __all__ = [
     "EPSILON", "EPSILON_SQRT", "Size", "Transform", "DEFAULT_FLATNESS", "SEG_ARC", "SEG_CUBIC", "SEG_LINE",
     "SEG_QUAD", "FillRule", "Path", "PathBuilder", "SvgParserError", "parse_svg_path", "NanError",
-    "RasterizeError", "BatchPlan", "Context", "Scene", "GradLinear", "GradRadial", "GradSpread", "GradStop",
+    "RasterizeError", "BatchPlan", "Context", "DiffBatch", "Scene", "GradLinear", "GradRadial", "GradSpread", "GradStop",
     "LinColor", "Units", "GpuRasterizer", "MaskBatch", "Pixel", "Rasterizer", "default_context",
 ]

@@ -65,6 +65,12 @@ class RzScene(ctypes.Structure):
                 ("paints", ctypes.c_void_p)]
 
 
+class RzDiffBatch(ctypes.Structure):
+    _fields_ = [("n_images", ctypes.c_uint32), ("paths_per_image", ctypes.c_uint32), ("segs_per_path", ctypes.c_uint32),
+                ("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("fill_rule", ctypes.c_int32),
+                ("paint_alpha", ctypes.c_float), ("ctrl", ctypes.c_void_p)]
+
+
 _lock = threading.Lock()
 _lib = None
 
@@ -96,13 +102,16 @@ _SIGNATURES = {
     "rz_fill": (ctypes.c_int32, [P, ctypes.POINTER(RzPath), P, ctypes.c_int32, ctypes.c_double, P, P, RzShape]),
     "rz_render_scene": (ctypes.c_int32, [P, ctypes.POINTER(RzScene), ctypes.c_double, P, P, ctypes.c_uint32,
                                          ctypes.c_uint32]),
+    "rz_diff_forward": (ctypes.c_int32, [P, ctypes.POINTER(RzDiffBatch), ctypes.c_double, P]),
+    "rz_l2_loss": (ctypes.c_int32, [P, P, P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double), P]),
+    "rasterize_backward": (ctypes.c_int32, [P, ctypes.POINTER(RzDiffBatch), ctypes.c_double, P, P, P]),
 }
 
 
 def header_symbols():
     """Function names declared in include/rasterize_gb300.h."""
     text = open(HEADER).read()
-    return sorted(set(re.findall(r"\b(rz_[a-z0-9_]+)\s*\(", text)) - {"rz_ctx"})
+    return sorted(set(re.findall(r"\b((?:rz_|rasterize_)[a-z0-9_]+)\s*\(", text)) - {"rz_ctx"})
 
 
 def load(path: str = LIB_PATH):

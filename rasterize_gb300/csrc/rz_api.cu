@@ -38,6 +38,12 @@ cudaError_t launch_bin_scatter(const SceneDev& S, cudaStream_t st);
 int composite_smem_bytes(int canvas_w, int band_rows, int max_clip_width, bool paint_mode, int* cov_stride);
 cudaError_t launch_composite(const SceneDev& S, int cov_stride, int smem, cudaStream_t st);
 uint64_t scan_temp_words(uint64_t n);
+int diff_smem_bytes(int width, int band_rows, bool backward, int* cov_stride);
+cudaError_t launch_diff_segments(const float* ctrl, uint32_t n_paths, int segs, uint8_t* kind, double* pts,
+                                 cudaStream_t st);
+cudaError_t launch_diff(const DiffDev& D, bool backward, int cov_stride, int smem, cudaStream_t st);
+cudaError_t launch_l2_loss(const float* A, const float* T, uint64_t n, double* loss, float* dl, int num_sms,
+                           cudaStream_t st);
 cudaError_t scan_u32(uint32_t* data, uint64_t n, uint32_t* temp, cudaStream_t stream);
 }  // namespace rz
 
@@ -99,6 +105,8 @@ struct rz_ctx {
     DevBuf d_kind, d_pts, d_sub, d_psub, d_tr, d_rule, d_masks, d_items, d_out, d_ctrl, d_counts;
     // line pipeline (large paths, scenes)
     DevBuf p_fills, p_paints, p_slots, p_lines, p_ecount, p_estart, p_ecursor, p_pairs, p_scan, p_canvas;
+    // differentiable batch
+    DevBuf p_leaf, d_loss;
     HostBuf h_stage, h_out;
     // host-side arc expansion scratch
     std::vector<uint8_t> x_kind;
@@ -997,6 +1005,63 @@ void add_fill(HostScene& hs, uint32_t sub0, uint32_t sub1, int col0, int row0, i
     hs.fills.push_back(f);
 }
 
+// Flatten + bin on the device (pipeline steps 1-5): every fill's lines, the
+// per-(fill, band) counts and starts, and the band lists.  `leaf` (device,
+// may be null) receives each line's segment and tree node.
+rz_status build_lines(rz_ctx* ctx, HostScene& hs, rz::SceneDev& S, Trace& tr, DevBuf* leaf) {
+    RZ_CUDA(ctx->p_fills.ensure(hs.fills.size() * sizeof(rz::FillDev)));
+    RZ_CUDA(cudaMemcpyAsync(ctx->p_fills.p, hs.fills.data(), hs.fills.size() * sizeof(rz::FillDev),
+                            cudaMemcpyHostToDevice, ctx->stream));
+    S.fills = (const rz::FillDev*)ctx->p_fills.p;
+    // 1) lines per slot, 2) offsets (one extra element receives the total)
+    const uint64_t ns = (uint64_t)hs.n_slots + 1;
+    RZ_CUDA(ctx->p_slots.ensure(ns * 4));
+    S.slot_count = (uint32_t*)ctx->p_slots.p;
+    RZ_CUDA(cudaMemsetAsync(S.slot_count, 0, ns * 4, ctx->stream));
+    tr.gpu_mark(ctx->stream, "upload");
+    RZ_CUDA(rz::launch_flatten_count(S, ctx->stream));
+    tr.gpu_mark(ctx->stream, "flatten_count");
+    const uint64_t ne = (uint64_t)hs.n_entries + 1;
+    RZ_CUDA(ctx->p_scan.ensure(rz::scan_temp_words(std::max(ns, ne)) * 4 + 64));
+    RZ_CUDA(rz::scan_u32(S.slot_count, ns, (uint32_t*)ctx->p_scan.p, ctx->stream));
+    uint32_t n_lines = 0;
+    RZ_CUDA(cudaMemcpyAsync(&n_lines, S.slot_count + hs.n_slots, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+    rz_status st = read_error(ctx);
+    if (st) return st;
+    if (leaf) {
+        RZ_CUDA(leaf->ensure((uint64_t)std::max(n_lines, 1u) * sizeof(uint2)));
+        S.leaf = (uint2*)leaf->p;
+    }
+    S.n_lines = n_lines;
+    // 3) lines + per-(fill, band) counts
+    RZ_CUDA(ctx->p_lines.ensure((uint64_t)std::max(n_lines, 1u) * 2 * sizeof(int4)));
+    S.lines = (int4*)ctx->p_lines.p;
+    RZ_CUDA(ctx->p_ecount.ensure(ne * 4));
+    RZ_CUDA(ctx->p_estart.ensure(ne * 4));
+    RZ_CUDA(ctx->p_ecursor.ensure(ne * 4));
+    S.entry_count = (uint32_t*)ctx->p_ecount.p;
+    S.entry_start = (uint32_t*)ctx->p_estart.p;
+    S.entry_cursor = (uint32_t*)ctx->p_ecursor.p;
+    RZ_CUDA(cudaMemsetAsync(S.entry_count, 0, ne * 4, ctx->stream));
+    RZ_CUDA(cudaMemsetAsync(S.entry_cursor, 0, ne * 4, ctx->stream));
+    RZ_CUDA(rz::launch_flatten_emit(S, ctx->stream));
+    tr.gpu_mark(ctx->stream, "flatten_emit");
+    // 4) list starts per (fill, band)
+    RZ_CUDA(cudaMemcpyAsync(S.entry_start, S.entry_count, ne * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    RZ_CUDA(rz::scan_u32(S.entry_start, ne, (uint32_t*)ctx->p_scan.p, ctx->stream));
+    uint32_t n_pairs = 0;
+    RZ_CUDA(cudaMemcpyAsync(&n_pairs, S.entry_start + hs.n_entries, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+    // 5) line lists
+    RZ_CUDA(ctx->p_pairs.ensure((uint64_t)std::max(n_pairs, 1u) * 4));
+    S.pairs = (uint32_t*)ctx->p_pairs.p;
+    tr.gpu_mark(ctx->stream, "entry_scan");
+    RZ_CUDA(rz::launch_bin_scatter(S, ctx->stream));
+    tr.gpu_mark(ctx->stream, "bin_scatter");
+    return RZ_OK;
+}
+
 // Flatten + bin + composite on the device.  canvas: device buffer (RGBA
 // pixels when paints are given, else an f32 mask), stride in pixels.
 rz_status run_pipeline(rz_ctx* ctx, HostScene& hs, double flatness, float* canvas, int64_t canvas_stride, int canvas_w,
@@ -1037,58 +1102,14 @@ rz_status run_pipeline(rz_ctx* ctx, HostScene& hs, double flatness, float* canva
         }
         return read_error(ctx);
     }
-    RZ_CUDA(ctx->p_fills.ensure(hs.fills.size() * sizeof(rz::FillDev)));
-    RZ_CUDA(cudaMemcpyAsync(ctx->p_fills.p, hs.fills.data(), hs.fills.size() * sizeof(rz::FillDev),
-                            cudaMemcpyHostToDevice, ctx->stream));
-    S.fills = (const rz::FillDev*)ctx->p_fills.p;
     if (paint_mode) {
         RZ_CUDA(ctx->p_paints.ensure(hs.paints.size() * sizeof(rz::PaintDev)));
         RZ_CUDA(cudaMemcpyAsync(ctx->p_paints.p, hs.paints.data(), hs.paints.size() * sizeof(rz::PaintDev),
                                 cudaMemcpyHostToDevice, ctx->stream));
         S.paints = (const rz::PaintDev*)ctx->p_paints.p;
     }
-    // 1) lines per slot, 2) offsets (one extra element receives the total)
-    const uint64_t ns = (uint64_t)hs.n_slots + 1;
-    RZ_CUDA(ctx->p_slots.ensure(ns * 4));
-    S.slot_count = (uint32_t*)ctx->p_slots.p;
-    RZ_CUDA(cudaMemsetAsync(S.slot_count, 0, ns * 4, ctx->stream));
-    tr.gpu_mark(ctx->stream, "upload");
-    RZ_CUDA(rz::launch_flatten_count(S, ctx->stream));
-    tr.gpu_mark(ctx->stream, "flatten_count");
-    const uint64_t ne = (uint64_t)hs.n_entries + 1;
-    RZ_CUDA(ctx->p_scan.ensure(rz::scan_temp_words(std::max(ns, ne)) * 4 + 64));
-    RZ_CUDA(rz::scan_u32(S.slot_count, ns, (uint32_t*)ctx->p_scan.p, ctx->stream));
-    uint32_t n_lines = 0;
-    RZ_CUDA(cudaMemcpyAsync(&n_lines, S.slot_count + hs.n_slots, 4, cudaMemcpyDeviceToHost, ctx->stream));
-    RZ_CUDA(cudaStreamSynchronize(ctx->stream));
-    rz_status st = read_error(ctx);
+    rz_status st = build_lines(ctx, hs, S, tr, nullptr);
     if (st) return st;
-    S.n_lines = n_lines;
-    // 3) lines + per-(fill, band) counts
-    RZ_CUDA(ctx->p_lines.ensure((uint64_t)std::max(n_lines, 1u) * 2 * sizeof(int4)));
-    S.lines = (int4*)ctx->p_lines.p;
-    RZ_CUDA(ctx->p_ecount.ensure(ne * 4));
-    RZ_CUDA(ctx->p_estart.ensure(ne * 4));
-    RZ_CUDA(ctx->p_ecursor.ensure(ne * 4));
-    S.entry_count = (uint32_t*)ctx->p_ecount.p;
-    S.entry_start = (uint32_t*)ctx->p_estart.p;
-    S.entry_cursor = (uint32_t*)ctx->p_ecursor.p;
-    RZ_CUDA(cudaMemsetAsync(S.entry_count, 0, ne * 4, ctx->stream));
-    RZ_CUDA(cudaMemsetAsync(S.entry_cursor, 0, ne * 4, ctx->stream));
-    RZ_CUDA(rz::launch_flatten_emit(S, ctx->stream));
-    tr.gpu_mark(ctx->stream, "flatten_emit");
-    // 4) list starts per (fill, band)
-    RZ_CUDA(cudaMemcpyAsync(S.entry_start, S.entry_count, ne * 4, cudaMemcpyDeviceToDevice, ctx->stream));
-    RZ_CUDA(rz::scan_u32(S.entry_start, ne, (uint32_t*)ctx->p_scan.p, ctx->stream));
-    uint32_t n_pairs = 0;
-    RZ_CUDA(cudaMemcpyAsync(&n_pairs, S.entry_start + hs.n_entries, 4, cudaMemcpyDeviceToHost, ctx->stream));
-    RZ_CUDA(cudaStreamSynchronize(ctx->stream));
-    // 5) line lists
-    RZ_CUDA(ctx->p_pairs.ensure((uint64_t)std::max(n_pairs, 1u) * 4));
-    S.pairs = (uint32_t*)ctx->p_pairs.p;
-    tr.gpu_mark(ctx->stream, "entry_scan");
-    RZ_CUDA(rz::launch_bin_scatter(S, ctx->stream));
-    tr.gpu_mark(ctx->stream, "bin_scatter");
     // 6) composite
     RZ_CUDA(rz::launch_composite(S, cov_stride, smem, ctx->stream));
     tr.gpu_mark(ctx->stream, "composite");
@@ -1301,6 +1322,159 @@ rz_status rz_render_scene(rz_ctx* ctx, const rz_scene* scene, double flatness, c
     }
     tr.mark("copy_out");
     return RZ_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Differentiable batch (rz_diff.cu)
+// ---------------------------------------------------------------------------
+namespace {
+
+rz_status diff_check(rz_ctx* ctx, const rz_diff_batch* b, double flatness) {
+    if (!b || !b->ctrl) return fail(ctx, RZ_ERR_INVALID, "null argument");
+    if (!valid_flatness(flatness)) return fail(ctx, RZ_ERR_INVALID, "flatness must be > 0 and finite");
+    if (b->width == 0 || b->height == 0 || b->width > 16383 || b->height > 16383)
+        return fail(ctx, RZ_ERR_INVALID, "image size must be 1..16383");
+    if (b->segs_per_path == 0 || b->segs_per_path > (1u << 20)) return fail(ctx, RZ_ERR_INVALID, "bad segs_per_path");
+    if (b->fill_rule != RZ_FILL_NONZERO && b->fill_rule != RZ_FILL_EVENODD) return fail(ctx, RZ_ERR_INVALID, "bad fill rule");
+    if (!(b->paint_alpha > 0.f && b->paint_alpha < 1.f)) return fail(ctx, RZ_ERR_INVALID, "paint_alpha must be in (0, 1)");
+    const uint64_t paths = (uint64_t)b->n_images * b->paths_per_image;
+    if (paths * b->segs_per_path >= (1ull << 31)) return fail(ctx, RZ_ERR_INVALID, "batch too large");
+    if ((uint64_t)b->n_images * b->height >= (1ull << 30)) return fail(ctx, RZ_ERR_INVALID, "batch too large");
+    return RZ_OK;
+}
+
+// Band height: the largest of 8, 4, 2, 1 rows that divides the image height
+// and keeps the backward kernel's shared memory within 64 KiB.
+int diff_band_rows(int width, int height) {
+    for (int r = 8; r > 1; r >>= 1) {
+        int cs = 0;
+        if (height % r == 0 && rz::diff_smem_bytes(width, r, true, &cs) <= 64 * 1024) return r;
+    }
+    return 1;
+}
+
+// Segments on the device, one fill per path (images stacked in one canvas),
+// lines flattened and binned with their tree nodes.
+rz_status diff_prepare(rz_ctx* ctx, const rz_diff_batch* b, double flatness, rz::DiffDev& D, int& cov_stride,
+                       int& smem, bool backward, Trace& tr) {
+    const uint32_t P = b->paths_per_image, segs = b->segs_per_path;
+    const uint32_t n_paths = b->n_images * P;
+    const uint32_t n_seg = n_paths * segs;
+    RZ_CUDA(ctx->d_kind.ensure((size_t)n_seg + 1));
+    RZ_CUDA(ctx->d_pts.ensure((size_t)n_seg * 64 + 8));
+    RZ_CUDA(ctx->d_sub.ensure(((size_t)n_paths + 1) * 4));
+    std::vector<uint32_t> sub(n_paths + 1);
+    for (uint32_t p = 0; p <= n_paths; ++p) sub[p] = p * segs;
+    RZ_CUDA(cudaMemcpyAsync(ctx->d_sub.p, sub.data(), sub.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    RZ_CUDA(rz::launch_diff_segments(b->ctrl, n_paths, (int)segs, (uint8_t*)ctx->d_kind.p, (double*)ctx->d_pts.p,
+                                     ctx->stream));
+    HostScene hs;
+    hs.sub_off = sub.data();
+    hs.n_seg = n_seg;
+    hs.n_sub = n_paths;
+    const int W = (int)b->width, H = (int)b->height;
+    hs.band_rows = diff_band_rows(W, H);
+    const rzhost::Xf id{{1, 0, 0, 0, 1, 0}};
+    for (uint32_t p = 0; p < n_paths; ++p)
+        add_fill(hs, p, p + 1, 0, (int)(p / P) * H, W, H, W, id, b->fill_rule, 0);  // fill semantics: clip at W
+    rz::SceneDev& S = D.S;
+    S = rz::SceneDev{};
+    S.kind = (const uint8_t*)ctx->d_kind.p;
+    S.pts = (const double*)ctx->d_pts.p;
+    S.sub_off = (const uint32_t*)ctx->d_sub.p;
+    S.n_fills = (uint32_t)hs.fills.size();
+    S.n_slots = hs.n_slots;
+    S.n_segments = hs.n_seg;
+    S.n_subpaths = hs.n_sub;
+    S.thr64 = 16.0 * flatness * flatness;
+    S.thr32 = (float)S.thr64;
+    S.canvas_w = W;
+    S.canvas_h = (int32_t)(b->n_images * b->height);
+    S.band_rows = hs.band_rows;
+    S.n_bands = S.canvas_h / hs.band_rows;
+    RZ_CUDA(ctx->d_ctrl.ensure(64));
+    RZ_CUDA(cudaMemsetAsync(ctx->d_ctrl.p, 0, 64, ctx->stream));
+    S.err = (int32_t*)ctx->d_ctrl.p;
+    S.counters = (int32_t*)ctx->d_ctrl.p + 4;
+    tr.gpu_mark(ctx->stream, "segments");
+    rz_status st = build_lines(ctx, hs, S, tr, &ctx->p_leaf);
+    if (st) return st;
+    D.paths = (int32_t)P;
+    D.segs = (int32_t)segs;
+    D.width = W;
+    D.height = H;
+    D.rule = b->fill_rule;
+    D.alpha = b->paint_alpha;
+    D.ctrl = b->ctrl;
+    smem = rz::diff_smem_bytes(W, hs.band_rows, backward, &cov_stride);
+    return RZ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+rz_status rz_diff_forward(rz_ctx* ctx, const rz_diff_batch* batch, double flatness, float* image) {
+    if (!ctx) return RZ_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    rz_status st = diff_check(ctx, batch, flatness);
+    if (st) return st;
+    if (!image) return fail(ctx, RZ_ERR_INVALID, "null image");
+    if (batch->n_images == 0) return RZ_OK;
+    RZ_CUDA(cudaSetDevice(ctx->device));
+    Trace tr("rz_diff_forward");
+    rz::DiffDev D{};
+    int cov_stride = 0, smem = 0;
+    if (batch->paths_per_image == 0) {
+        RZ_CUDA(cudaMemsetAsync(image, 0, (size_t)batch->n_images * batch->width * batch->height * 4, ctx->stream));
+        return read_error(ctx);
+    }
+    st = diff_prepare(ctx, batch, flatness, D, cov_stride, smem, false, tr);
+    if (st) return st;
+    D.out = image;
+    RZ_CUDA(rz::launch_diff(D, false, cov_stride, smem, ctx->stream));
+    tr.gpu_mark(ctx->stream, "composite");
+    return read_error(ctx);
+}
+
+rz_status rz_l2_loss(rz_ctx* ctx, const float* image, const float* target, uint64_t n, double* loss,
+                     float* dl_dimage) {
+    if (!ctx) return RZ_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    if (!image || !target || !loss) return fail(ctx, RZ_ERR_INVALID, "null argument");
+    RZ_CUDA(cudaSetDevice(ctx->device));
+    RZ_CUDA(ctx->d_loss.ensure(16));
+    RZ_CUDA(cudaMemsetAsync(ctx->d_loss.p, 0, 8, ctx->stream));
+    RZ_CUDA(rz::launch_l2_loss(image, target, n, (double*)ctx->d_loss.p, dl_dimage, ctx->num_sms, ctx->stream));
+    RZ_CUDA(cudaMemcpyAsync(loss, ctx->d_loss.p, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+    return RZ_OK;
+}
+
+rz_status rasterize_backward(rz_ctx* ctx, const rz_diff_batch* batch, double flatness, const float* image,
+                             const float* dl_dimage, float* dl_dctrl) {
+    if (!ctx) return RZ_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    rz_status st = diff_check(ctx, batch, flatness);
+    if (st) return st;
+    if (!image || !dl_dimage || !dl_dctrl) return fail(ctx, RZ_ERR_INVALID, "null argument");
+    const uint64_t n_ctrl = (uint64_t)batch->n_images * batch->paths_per_image * batch->segs_per_path * 3 * 2;
+    RZ_CUDA(cudaSetDevice(ctx->device));
+    RZ_CUDA(cudaMemsetAsync(dl_dctrl, 0, n_ctrl * 4, ctx->stream));
+    if (n_ctrl == 0) return read_error(ctx);
+    Trace tr("rasterize_backward");
+    rz::DiffDev D{};
+    int cov_stride = 0, smem = 0;
+    st = diff_prepare(ctx, batch, flatness, D, cov_stride, smem, true, tr);
+    if (st) return st;
+    D.image = image;
+    D.dl_dimage = dl_dimage;
+    D.out = dl_dctrl;
+    RZ_CUDA(rz::launch_diff(D, true, cov_stride, smem, ctx->stream));
+    tr.gpu_mark(ctx->stream, "adjoint");
+    return read_error(ctx);
 }
 
 }  // extern "C"

@@ -1,0 +1,493 @@
+// rz_diff.cu -- differentiable batch: forward composite and hand-written adjoint.
+//
+// The images are stacked into one tall canvas (image i owns canvas rows
+// [i H, (i + 1) H)) so the line pipeline flattens every path once and bins
+// its lines by (path, band of R rows); R divides H, so a band belongs to one
+// image.  One CTA per band then:
+//
+//   forward   for the paths of its image in order: signed area of the path's
+//             lines in shared memory (exact fixed point), row prefix, fill
+//             rule, A += a alpha (1 - A)  (Rasterizer::fill + source-over,
+//             src/rasterize.rs:69-115, alpha channel of a solid paint);
+//   backward  for every path of its image: the same coverage, then per pixel
+//             g = dL/dA * dA/dalpha * dalpha/dw with dA/dalpha =
+//             a (1 - A) / (1 - a alpha) (so paths are independent once the
+//             forward image is known), the row suffix sums G of g, and for
+//             every line of the path in the band the derivative of
+//             sum_pixels g * (the line's winding contribution) with respect
+//             to the line's end points, restricted to the band's rows.
+//
+// Line derivative.  A line adds to the winding of pixel x in row r the area
+// of the pixel to the right of it, so its loss term over row r is
+// h * mean_{X in [xa, xn]} W_r(X) with h the signed height of its piece in
+// the row and W_r(X) = G[k+1] + (k + 1 - X) g[k] on [k, k+1) (piecewise
+// linear, continuous).  The mean and its derivatives in xa, xn are exact
+// integrals over the pixels the piece spans; xa, xn, h carry forward-mode
+// derivatives (dual numbers) through the reference's x rules
+// (src/rasterize.rs:372-393, 923-937) and the row clipping.  The end points
+// are B(t) at the dyadic parameters of the frozen bisection tree, so the
+// chain to the control points is the cubic Bernstein weights.
+#include "rz_device.cuh"
+#include "rz_kernels.cuh"
+#include "rz_pipeline.cuh"
+
+namespace rz {
+
+// ---------------------------------------------------------------------------
+// FP32 control points -> the pipeline's binary64 cubic segments
+// ---------------------------------------------------------------------------
+__global__ void k_diff_segments(const float* __restrict__ ctrl, uint32_t n_paths, int segs, uint8_t* kind,
+                                double* pts) {
+    const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (uint64_t)n_paths * segs) return;
+    const uint64_t p = g / segs;
+    const int s = (int)(g - p * segs);
+    const float2* c = reinterpret_cast<const float2*>(ctrl) + p * 3ull * segs;
+    const int idx[4] = {3 * s, 3 * s + 1, 3 * s + 2, 3 * ((s + 1) % segs)};
+    #pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const float2 q = c[idx[j]];
+        pts[8 * g + 2 * j] = (double)q.x;
+        pts[8 * g + 2 * j + 1] = (double)q.y;
+    }
+    kind[g] = SEG_CUBIC;
+}
+
+// ---------------------------------------------------------------------------
+// Shared per-band setup
+// ---------------------------------------------------------------------------
+constexpr int kDiffThreads = 256;
+
+__device__ __forceinline__ Band diff_band(const DiffDev& D, const FillDev& f, float* cov, int row_base, int rows) {
+    Band B;
+    B.acc = cov;
+    B.stride = band_stride(f.clip_width);
+    B.bh = rows;
+    B.y0 = row_base - f.row0;
+    B.img_h = f.height;
+    B.width_f = (float)f.clip_width;
+    B.width_i = f.clip_width;
+    return B;
+}
+
+// A stored line end (16.16 anchor + FP32 remainder, fill frame).
+__device__ __forceinline__ VtxQ diff_vtx(int4 e, int row0) {
+    VtxQ v;
+    v.col = e.x >> 16;
+    v.row = (e.y >> 16) - row0;
+    v.fx = fmaf((float)(e.x & 0xffff), FIX_ONE_INV, __int_as_float(e.z));
+    v.fy = fmaf((float)(e.y & 0xffff), FIX_ONE_INV, __int_as_float(e.w));
+    return v;
+}
+
+// Coverage of fill f in the band: clear, accumulate its lines.  Ends with a barrier.
+__device__ void diff_coverage(const DiffDev& D, const FillDev& f, uint32_t e, const Band& B) {
+    const SceneDev& S = D.S;
+    float4* c4 = reinterpret_cast<float4*>(B.acc);
+    const int n4 = (B.bh * B.stride) >> 2;
+    __syncthreads();  // the previous user of the band is done
+    for (int i = threadIdx.x; i < n4; i += kDiffThreads) c4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+    const uint32_t n = S.entry_count[e], start = S.entry_start[e];
+    for (uint32_t j = threadIdx.x; j < n; j += kDiffThreads) {
+        const uint32_t l = S.pairs[start + j];
+        accumulate_vtx(B, diff_vtx(S.lines[2ull * l], B.y0), diff_vtx(S.lines[2ull * l + 1], B.y0));
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Forward
+// ---------------------------------------------------------------------------
+struct DiffBlend {
+    float* A;  // band, width per row
+    int width;
+    float alpha;
+    __device__ __forceinline__ void operator()(int r, int x0, const float (&a)[kScanChunk]) const {
+        #pragma unroll
+        for (int i = 0; i < kScanChunk; ++i) {
+            const int x = x0 + i;
+            if (x >= width || a[i] < 1e-6f) continue;  // fill skips |alpha| < 1e-6 (src/rasterize.rs:347-349)
+            float& d = A[r * width + x];
+            d = fmaf(alpha * a[i], 1.f - d, d);
+        }
+    }
+};
+
+__global__ void __launch_bounds__(kDiffThreads) k_diff_forward(DiffDev D, int cov_stride) {
+    extern __shared__ float4 sm4[];
+    float* cov = reinterpret_cast<float*>(sm4);
+    const SceneDev& S = D.S;
+    const int rows = S.band_rows;
+    float* A = cov + rows * cov_stride;
+    const int band = blockIdx.x;
+    const int row_base = band * rows;
+    const int img = row_base / D.height;
+    for (int i = threadIdx.x; i < rows * D.width; i += kDiffThreads) A[i] = 0.f;
+    for (int p = 0; p < D.paths; ++p) {
+        const FillDev& f = S.fills[img * D.paths + p];
+        const uint32_t e = f.entry0 + (band - f.band0);
+        if (S.entry_count[e] == 0) continue;  // no line in the band: no coverage
+        const Band B = diff_band(D, f, cov, row_base, rows);
+        diff_coverage(D, f, e, B);
+        band_scan<kDiffThreads>(B, D.width, D.rule, DiffBlend{A, D.width, D.alpha});
+    }
+    __syncthreads();
+    float* out = D.out + (uint64_t)row_base * D.width;  // canvas rows are image rows
+    for (int i = threadIdx.x; i < rows * D.width; i += kDiffThreads) out[i] = A[i];
+}
+
+// ---------------------------------------------------------------------------
+// Backward
+// ---------------------------------------------------------------------------
+struct Dual {
+    float v, d[4];
+};
+__device__ __forceinline__ Dual dconst(float v) { return Dual{v, {0.f, 0.f, 0.f, 0.f}}; }
+__device__ __forceinline__ Dual dadd(const Dual& a, const Dual& b) {
+    return Dual{a.v + b.v, {a.d[0] + b.d[0], a.d[1] + b.d[1], a.d[2] + b.d[2], a.d[3] + b.d[3]}};
+}
+__device__ __forceinline__ Dual dsub(const Dual& a, const Dual& b) {
+    return Dual{a.v - b.v, {a.d[0] - b.d[0], a.d[1] - b.d[1], a.d[2] - b.d[2], a.d[3] - b.d[3]}};
+}
+__device__ __forceinline__ Dual dmul(const Dual& a, const Dual& b) {
+    Dual r;
+    r.v = a.v * b.v;
+    #pragma unroll
+    for (int k = 0; k < 4; ++k) r.d[k] = fmaf(a.d[k], b.v, a.v * b.d[k]);
+    return r;
+}
+__device__ __forceinline__ Dual ddiv(const Dual& a, const Dual& b) {
+    Dual r;
+    r.v = a.v / b.v;
+    const float inv = 1.f / b.v;
+    #pragma unroll
+    for (int k = 0; k < 4; ++k) r.d[k] = (a.d[k] - r.v * b.d[k]) * inv;
+    return r;
+}
+__device__ __forceinline__ Dual dlerp(const Dual& a, const Dual& b, const Dual& t) {  // (1 - t) a + t b
+    return dadd(a, dmul(t, dsub(b, a)));
+}
+
+// Mean of W_r over [lo, hi] (x relative to column c0) and its derivatives.
+__device__ void diff_row_mean(const float* G, const float* g, int W, int c0, float lo, float hi, float& I, float& dlo,
+                              float& dhi) {
+    const float wmax = (float)(W - c0), wmin = (float)(-c0);
+    lo = fminf(fmaxf(lo, wmin), wmax);
+    hi = fminf(fmaxf(hi, lo), wmax);
+    const float D = hi - lo;
+    if (D < 1e-6f) {
+        int k = (int)floorf(lo);
+        k = min(max(k + c0, 0), W - 1);
+        const float kr = (float)(k - c0);
+        I = G[k + 1] + (kr + 1.f - lo) * g[k];
+        dlo = dhi = -0.5f * g[k];
+        return;
+    }
+    const int k0 = (int)floorf(lo), k1 = min((int)floorf(hi), W - 1 - c0);
+    float sI = 0.f, slo = 0.f, shi = 0.f;
+    for (int k = k0; k <= k1; ++k) {
+        const float a = fmaxf(lo, (float)k), b = fminf(hi, (float)(k + 1));
+        if (b <= a) continue;
+        const int kk = k + c0;
+        const float gk = g[kk];
+        const float ka = (float)(k + 1) - a, kb = (float)(k + 1) - b;
+        sI += G[kk + 1] * (b - a) + gk * 0.5f * (ka * ka - kb * kb);
+        shi -= gk * 0.5f * ((b - lo) * (b - lo) - (a - lo) * (a - lo));
+        slo -= gk * 0.5f * ((hi - a) * (hi - a) - (hi - b) * (hi - b));
+    }
+    const float inv = 1.f / D;
+    I = sI * inv;
+    dhi = shi * inv * inv;
+    dlo = slo * inv * inv;
+}
+
+// d(sum over the band's pixels of g * winding contribution of the piece p -> q)/d(line ends);
+// x relative to column c0, y relative to band row 0.
+__device__ void diff_piece(Dual px, Dual py, Dual qx, Dual qy, int rows, int W, int c0, const float* G, const float* g,
+                           float (&out)[4]) {
+    const int Gs = W + 1;
+    if (py.v == qy.v) {
+        // horizontal: no coverage, but moving an end vertically brings coverage in
+        const int r = (int)floorf(py.v);
+        if (r < 0 || r >= rows) return;
+        float I, dlo, dhi;
+        diff_row_mean(G + r * Gs, g + r * W, W, c0, fminf(px.v, qx.v), fmaxf(px.v, qx.v), I, dlo, dhi);
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) out[k] += I * (qy.d[k] - py.d[k]);
+        return;
+    }
+    float dir = 1.f;
+    if (py.v > qy.v) {
+        Dual t = px; px = qx; qx = t;
+        t = py; py = qy; qy = t;
+        dir = -1.f;
+    }
+    const Dual kx = ddiv(dsub(qx, px), dsub(qy, py));  // dx/dy
+    const int r0 = max((int)floorf(py.v), 0), r1 = min((int)ceilf(qy.v), rows);
+    for (int r = r0; r < r1; ++r) {
+        const bool start_in = py.v >= (float)r, end_in = qy.v <= (float)(r + 1);
+        const Dual sa = start_in ? py : dconst((float)r);
+        const Dual sb = end_in ? qy : dconst((float)(r + 1));
+        if (!(sb.v > sa.v)) continue;
+        const Dual xa = start_in ? px : dadd(px, dmul(dsub(sa, py), kx));
+        const Dual xn = end_in ? qx : dadd(px, dmul(dsub(sb, py), kx));
+        const Dual h = dsub(sb, sa);
+        const bool ord = xa.v <= xn.v;
+        const Dual& lo = ord ? xa : xn;
+        const Dual& hi = ord ? xn : xa;
+        float I, dlo, dhi;
+        diff_row_mean(G + r * Gs, g + r * W, W, c0, lo.v, hi.v, I, dlo, dhi);
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) out[k] += dir * (I * h.d[k] + h.v * (dlo * lo.d[k] + dhi * hi.d[k]));
+    }
+}
+
+// The reference's x rules on dual numbers (width = W, relative to column c0), then the pieces.
+__device__ void diff_line(float ax, float ay, float bx, float by, int rows, int W, int c0, const float* G,
+                          const float* g, float (&out)[4]) {
+    Dual x0{ax, {1.f, 0.f, 0.f, 0.f}}, y0{ay, {0.f, 1.f, 0.f, 0.f}};
+    Dual x1{bx, {0.f, 0.f, 1.f, 0.f}}, y1{by, {0.f, 0.f, 0.f, 1.f}};
+    const float width = (float)(W - c0), zero = (float)(-c0);
+    if (x0.v > width || x1.v > width) {
+        if (x0.v > width && x1.v > width) {
+            x0 = dconst(width - 0.001f);
+            x1 = dconst(width - 0.001f);
+        } else {
+            const Dual t = ddiv(dsub(x0, dconst(width)), dsub(x0, x1));
+            const Dual my = dlerp(y0, y1, t);
+            if (x0.v < width) { x1 = dconst(width); y1 = my; }
+            else { x0 = dconst(width); y0 = my; }
+        }
+    }
+    if (x0.v >= zero && x1.v >= zero) {
+        diff_piece(x0, y0, x1, y1, rows, W, c0, G, g, out);
+    } else if (x0.v <= zero && x1.v <= zero) {
+        diff_piece(dconst(zero), y0, dconst(zero), y1, rows, W, c0, G, g, out);
+    } else {
+        const Dual t = ddiv(dsub(x0, dconst(zero)), dsub(x0, x1));
+        const Dual mx = dlerp(x0, x1, t), my = dlerp(y0, y1, t);
+        if (x0.v < zero) {
+            diff_piece(mx, my, x1, y1, rows, W, c0, G, g, out);
+            diff_piece(dconst(zero), y0, mx, my, rows, W, c0, G, g, out);
+        } else {
+            diff_piece(x0, y0, mx, my, rows, W, c0, G, g, out);
+            diff_piece(mx, my, dconst(zero), y1, rows, W, c0, G, g, out);
+        }
+    }
+}
+
+// Row scan of the band that hands the fixed-point windings to the epilogue.
+template <class Epi>
+__device__ void band_scan_winding(const Band& B, int width, const Epi& epi) {
+    const int lane = threadIdx.x & 31;
+    for (int r = threadIdx.x >> 5; r < B.bh; r += kDiffThreads / 32) {
+        const int4* row4 = reinterpret_cast<const int4*>(B.acc + r * B.stride);
+        uint32_t carry = 0;
+        for (int x0 = 0; x0 < width; x0 += 32 * kScanChunk) {
+            const int x = x0 + kScanChunk * lane;
+            int4 v = make_int4(0, 0, 0, 0);
+            if (x < width) v = row4[x >> 2];
+            const uint32_t a0 = (uint32_t)v.x;
+            const uint32_t a1 = a0 + (x + 1 < width ? (uint32_t)v.y : 0u);
+            const uint32_t a2 = a1 + (x + 2 < width ? (uint32_t)v.z : 0u);
+            const uint32_t a3 = a2 + (x + 3 < width ? (uint32_t)v.w : 0u);
+            uint32_t incl = a3;
+            #pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t o = __shfl_up_sync(0xffffffffu, incl, off);
+                if (lane >= off) incl += o;
+            }
+            const uint32_t base = carry + incl - a3;
+            carry += __shfl_sync(0xffffffffu, incl, 31);
+            if (x < width) {
+                const int32_t w[kScanChunk] = {(int32_t)(base + a0), (int32_t)(base + a1), (int32_t)(base + a2),
+                                               (int32_t)(base + a3)};
+                epi(r, x, w);
+            }
+        }
+    }
+}
+
+// g = dL/dA * a (1 - A) / (1 - a alpha) * dalpha/dw per pixel of the band.
+struct DiffGrad {
+    float* g;
+    const float* A;   // forward image rows of the band
+    const float* dl;  // d loss / d image rows of the band
+    int width, rule;
+    float alpha;
+    __device__ __forceinline__ void operator()(int r, int x0, const int32_t (&w)[kScanChunk]) const {
+        #pragma unroll
+        for (int i = 0; i < kScanChunk; ++i) {
+            const int x = x0 + i;
+            if (x >= width) continue;
+            float al = alpha_from_winding_fix(rule, w[i]);
+            if (al < 1e-6f) al = 0.f;  // skipped by the forward: no blend, no slope
+            float da = 0.f;
+            if (al != 0.f) {
+                if (rule == 1) {
+                    // EvenOdd: |((w + 1) mod 2) - 1|, slope = sign of the folded value
+                    const int32_t f = (int32_t)(((uint32_t)w[i] + (1u << 22)) & ((1u << 23) - 1u)) - (1 << 22);
+                    da = f > 0 ? 1.f : -1.f;
+                } else if (al < 1.f) {
+                    da = w[i] > 0 ? 1.f : -1.f;
+                }
+            }
+            const int o = r * width + x;
+            g[o] = da == 0.f ? 0.f : dl[o] * alpha * (1.f - A[o]) / (1.f - alpha * al) * da;
+        }
+    }
+};
+
+// G[x] = sum over x' >= x of g[x'] (G[W] = 0), one warp per row.
+__device__ void suffix_rows(const float* g, float* G, int rows, int W) {
+    const int lane = threadIdx.x & 31;
+    for (int r = threadIdx.x >> 5; r < rows; r += kDiffThreads / 32) {
+        const float* gr = g + r * W;
+        float* Gr = G + r * (W + 1);
+        float carry = 0.f;
+        const int nchunk = (W + 127) / 128;
+        for (int c = nchunk - 1; c >= 0; --c) {
+            const int x = c * 128 + 4 * lane;
+            const float v0 = x < W ? gr[x] : 0.f, v1 = x + 1 < W ? gr[x + 1] : 0.f;
+            const float v2 = x + 2 < W ? gr[x + 2] : 0.f, v3 = x + 3 < W ? gr[x + 3] : 0.f;
+            const float s3 = v3, s2 = v2 + s3, s1 = v1 + s2, s0 = v0 + s1;
+            float incl = s0;  // suffix over lanes >= lane
+            #pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const float o = __shfl_down_sync(0xffffffffu, incl, off);
+                if (lane + off < 32) incl += o;
+            }
+            const float base = carry + incl - s0;
+            carry += __shfl_sync(0xffffffffu, incl, 0);
+            if (x < W) Gr[x] = base + s0;
+            if (x + 1 < W) Gr[x + 1] = base + s1;
+            if (x + 2 < W) Gr[x + 2] = base + s2;
+            if (x + 3 < W) Gr[x + 3] = base + s3;
+        }
+        if (lane == 0) Gr[W] = 0.f;
+    }
+}
+
+__global__ void __launch_bounds__(kDiffThreads) k_diff_backward(DiffDev D, int cov_stride) {
+    extern __shared__ float4 sm4[];
+    float* cov = reinterpret_cast<float*>(sm4);
+    const SceneDev& S = D.S;
+    const int rows = S.band_rows;
+    const int W = D.width;
+    float* g = cov + rows * cov_stride;
+    float* G = g + rows * W;
+    const int band = blockIdx.x;
+    const int row_base = band * rows;
+    const int img = row_base / D.height;
+    const float* A = D.image + (uint64_t)row_base * W;
+    const float* dl = D.dl_dimage + (uint64_t)row_base * W;
+    float2* out = reinterpret_cast<float2*>(D.out);
+    for (int p = 0; p < D.paths; ++p) {
+        const uint32_t fi = (uint32_t)(img * D.paths + p);
+        const FillDev& f = S.fills[fi];
+        const uint32_t e = f.entry0 + (band - f.band0);
+        const uint32_t n = S.entry_count[e];
+        if (n == 0) continue;  // no line in the band: zero coverage and no line to move
+        const Band B = diff_band(D, f, cov, row_base, rows);
+        diff_coverage(D, f, e, B);
+        band_scan_winding(B, W, DiffGrad{g, A, dl, W, D.rule, D.alpha});
+        __syncthreads();
+        suffix_rows(g, G, rows, W);
+        __syncthreads();
+        const uint32_t start = S.entry_start[e];
+        for (uint32_t j = threadIdx.x; j < n; j += kDiffThreads) {
+            const uint32_t l = S.pairs[start + j];
+            const uint2 code = S.leaf[l];
+            if (code.x == 0xffffffffu) continue;  // a closing line (zero length here)
+            const VtxQ a = diff_vtx(S.lines[2ull * l], B.y0), b = diff_vtx(S.lines[2ull * l + 1], B.y0);
+            const int c0 = a.col;
+            float d4[4] = {0.f, 0.f, 0.f, 0.f};
+            diff_line(a.fx, (float)a.row + a.fy, (float)(b.col - c0) + b.fx, (float)b.row + b.fy, rows, W, c0, G, g,
+                      d4);
+            if (d4[0] == 0.f && d4[1] == 0.f && d4[2] == 0.f && d4[3] == 0.f) continue;
+            // chain to the control points: Bernstein weights at the frozen tree's parameters
+            const uint32_t seg = code.x;
+            const int d = (int)(code.y >> 27);
+            const uint32_t k = code.y & ((1u << 27) - 1u);
+            const float t0 = (float)k * pow2f(-d), t1 = (float)(k + 1u) * pow2f(-d);
+            const uint64_t path = seg / (uint32_t)D.segs;
+            const int s = (int)(seg - path * (uint32_t)D.segs);
+            const int idx[4] = {3 * s, 3 * s + 1, 3 * s + 2, 3 * ((s + 1) % D.segs)};
+            const float u0 = 1.f - t0, u1 = 1.f - t1;
+            const float b0[4] = {u0 * u0 * u0, 3.f * t0 * u0 * u0, 3.f * t0 * t0 * u0, t0 * t0 * t0};
+            const float b1[4] = {u1 * u1 * u1, 3.f * t1 * u1 * u1, 3.f * t1 * t1 * u1, t1 * t1 * t1};
+            float2* o = out + path * 3ull * D.segs;
+            #pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                atomicAdd(&o[idx[q]].x, d4[0] * b0[q] + d4[2] * b1[q]);
+                atomicAdd(&o[idx[q]].y, d4[1] * b0[q] + d4[3] * b1[q]);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// L2 loss: sum (A - T)^2 in binary64, dL/dA = 2 (A - T)
+// ---------------------------------------------------------------------------
+__global__ void k_l2_loss(const float* __restrict__ A, const float* __restrict__ T, uint64_t n, double* loss,
+                          float* dl) {
+    double acc = 0.0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const float d = A[i] - T[i];
+        acc += (double)d * (double)d;
+        if (dl) dl[i] = 2.f * d;
+    }
+    #pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+    __shared__ double wsum[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) wsum[warp] = acc;
+    __syncthreads();
+    if (warp == 0) {
+        acc = lane < (int)(blockDim.x >> 5) ? wsum[lane] : 0.0;
+        #pragma unroll
+        for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+        if (lane == 0) atomicAdd(loss, acc);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers (declared in rz_api.cu)
+// ---------------------------------------------------------------------------
+int diff_smem_bytes(int width, int band_rows, bool backward, int* cov_stride) {
+    const int stride = band_stride(width);
+    *cov_stride = stride;
+    return 4 * band_rows * stride + 4 * band_rows * width + (backward ? 4 * band_rows * (width + 1) : 0);
+}
+
+cudaError_t launch_diff_segments(const float* ctrl, uint32_t n_paths, int segs, uint8_t* kind, double* pts,
+                                 cudaStream_t st) {
+    const uint64_t n = (uint64_t)n_paths * segs;
+    if (n == 0) return cudaSuccess;
+    k_diff_segments<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(ctrl, n_paths, segs, kind, pts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_diff(const DiffDev& D, bool backward, int cov_stride, int smem, cudaStream_t st) {
+    if (backward) {
+        cudaError_t e = cudaFuncSetAttribute(k_diff_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        k_diff_backward<<<D.S.n_bands, kDiffThreads, smem, st>>>(D, cov_stride);
+    } else {
+        cudaError_t e = cudaFuncSetAttribute(k_diff_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        k_diff_forward<<<D.S.n_bands, kDiffThreads, smem, st>>>(D, cov_stride);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_l2_loss(const float* A, const float* T, uint64_t n, double* loss, float* dl, int num_sms,
+                           cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    const uint64_t blocks = std::min<uint64_t>((n + 255) / 256, (uint64_t)num_sms * 8);
+    k_l2_loss<<<(unsigned)blocks, 256, 0, st>>>(A, T, n, loss, dl);
+    return cudaGetLastError();
+}
+
+}  // namespace rz

@@ -63,6 +63,7 @@ __device__ bool slot_segment(const SceneDev& S, const FillDev& f, uint32_t s, Se
 struct SlotState {
     bool ok = false;    // a segment to flatten
     bool fits = false;  // inside the 16.16 range
+    uint32_t src = 0xffffffffu;  // input segment (~0: a closing line)
     Seg64 g;            // binary64, transformed
     FixSeg F;
     SegRec r;
@@ -74,6 +75,7 @@ __device__ void load_slot(const SceneDev& S, const FillDev& f, uint32_t s, SlotS
     uint32_t src = 0;
     st.ok = slot_segment(S, f, s, st.g, src);
     if (!st.ok) return;
+    st.src = src;
     const int n = seg_npts(st.g.kind);
     bool nan = false, fits = true;
     #pragma unroll
@@ -150,15 +152,25 @@ __global__ void k_flatten_count(SceneDev S) {
     if (fallbacks) atomicAdd(&S.counters[1], fallbacks);
 }
 
+// Rows [r0, r1) of the fill's view a line with 16.16 end heights ya, yb
+// reaches; false when none.  The range is widened by one 16.16 unit so a line
+// whose rounded height sits on a row boundary still reaches the row its exact
+// height enters.  Zero-height lines add no coverage and are skipped, except
+// for the adjoint (leaf codes requested): moving an end vertically still
+// changes the loss.
+__device__ __forceinline__ bool line_rows(const SceneDev& S, const FillDev& f, int32_t ya, int32_t yb, int& r0,
+                                          int& r1) {
+    const int32_t ylo = min(ya, yb), yhi = max(ya, yb);
+    if (ylo == yhi && !S.leaf) return false;  // no signed coverage
+    r0 = max((ylo - 1) >> 16, 0);             // floor
+    r1 = min((yhi + 1 + 65535) >> 16, f.height);  // ceil (exclusive)
+    return r0 < r1;
+}
+
 // Lines per (fill, band) of one local-frame line.
 __device__ __forceinline__ void count_bands(const SceneDev& S, const FillDev& f, int4 l) {
-    const int32_t ylo = min(l.y, l.w), yhi = max(l.y, l.w);
-    if (ylo == yhi) return;  // no signed coverage
-    int r0 = ylo >> 16;                 // floor
-    int r1 = (yhi + 65535) >> 16;       // ceil (exclusive)
-    r0 = max(r0, 0);
-    r1 = min(r1, f.height);
-    if (r0 >= r1) return;
+    int r0, r1;
+    if (!line_rows(S, f, l.y, l.w, r0, r1)) return;
     const int b0 = (r0 + f.row0) / S.band_rows, b1 = (r1 - 1 + f.row0) / S.band_rows;
     for (int b = max(b0, f.band0); b <= min(b1, f.band0 + f.nbands - 1); ++b)
         atomicAdd(&S.entry_count[f.entry0 + (b - f.band0)], 1u);
@@ -184,6 +196,14 @@ struct EmitLines {
                                       fix_add(b.x, __int_as_float(b.z)), fix_add(b.y, __int_as_float(b.w))));
     }
     __device__ void operator()(int d, uint32_t k) {
+        const uint32_t first = out;
+        emit(d, k);
+        if (S->leaf) {
+            const uint2 code = make_uint2(st->src, ((uint32_t)d << 27) | k);
+            for (uint32_t i = first; i < out; ++i) S->leaf[i] = code;
+        }
+    }
+    __device__ void emit(int d, uint32_t k) {
         if (st->fits) {
             // integer pixel of the vertex as the 16.16 anchor, its fraction as the remainder
             const VtxQ a = rec_vtx(st->r, k, d, 0), b = rec_vtx(st->r, k + 1u, d, 0);
@@ -249,11 +269,8 @@ __global__ void k_bin_scatter(SceneDev S) {
     const FillDev& f = S.fills[fill_of_line(S, l)];
     const int4 a = S.lines[2ull * l], b = S.lines[2ull * l + 1];
     const int32_t ya = fix_add(a.y, __int_as_float(a.w)), yb = fix_add(b.y, __int_as_float(b.w));
-    const int32_t ylo = min(ya, yb), yhi = max(ya, yb);
-    if (ylo == yhi) return;
-    int r0 = max(ylo >> 16, 0);
-    int r1 = min((yhi + 65535) >> 16, f.height);
-    if (r0 >= r1) return;
+    int r0, r1;
+    if (!line_rows(S, f, ya, yb, r0, r1)) return;
     const int b0 = (r0 + f.row0) / S.band_rows, b1 = (r1 - 1 + f.row0) / S.band_rows;
     for (int b = max(b0, f.band0); b <= min(b1, f.band0 + f.nbands - 1); ++b) {
         const uint32_t e = f.entry0 + (b - f.band0);

@@ -74,6 +74,7 @@ struct SceneDev {
     uint32_t* entry_start;   // [n_entries] exclusive prefix of entry_count
     uint32_t* entry_cursor;  // [n_entries]
     uint32_t* pairs;         // [n_pairs] line indices grouped by (fill, band)
+    uint2* leaf;             // [n_lines] (input segment or ~0, depth << 27 | index) per line, or null
     // output
     float* canvas;           // RGBA f32 (scenes) or f32 mask (coverage only)
     int64_t canvas_stride;   // elements between rows (pixels for RGBA: 4 floats each)
@@ -81,6 +82,20 @@ struct SceneDev {
     int32_t load_canvas;     // 1: blend over the canvas content instead of bg
     int32_t* err;
     int32_t* counters;
+};
+
+// Differentiable batch (rz_diff.cu): images stacked in one canvas, one fill per path.
+struct DiffDev {
+    SceneDev S;
+    int32_t paths;       // per image
+    int32_t segs;        // per path
+    int32_t width, height;
+    int32_t rule;
+    float alpha;         // paint alpha
+    const float* ctrl;   // control points (FP32)
+    const float* image;  // forward image (backward input)
+    const float* dl_dimage;
+    float* out;          // forward: images; backward: d loss / d ctrl
 };
 
 }  // namespace rz

@@ -242,6 +242,32 @@ class Scene:
         return s, keepalive
 
 
+class DiffBatch:
+    """The differentiable batch: ``n_images`` images of (height, width), each
+    the alpha channel of ``paths`` closed cubic paths of ``segs`` segments
+    filled in order with one solid paint of alpha ``alpha`` (Rasterizer::fill
+    + source-over).  ``ctrl_ptr``: device FP32 control points, shape
+    (n_images, paths, 3 * segs, 2); segment s is (V_s, C1_s, C2_s, V_{s+1})
+    with V_s = point 3s."""
+
+    def __init__(self, n_images, paths, segs, width, height, ctrl_ptr, alpha=0.5, fill_rule=FillRule.NonZero):
+        self.n_images, self.paths, self.segs = int(n_images), int(paths), int(segs)
+        self.width, self.height = int(width), int(height)
+        self.ctrl_ptr, self.alpha, self.fill_rule = int(ctrl_ptr), float(alpha), FillRule(fill_rule)
+
+    @property
+    def n_pixels(self):
+        return self.n_images * self.width * self.height
+
+    @property
+    def n_ctrl(self):
+        return self.n_images * self.paths * self.segs * 3 * 2
+
+    def struct(self):
+        return _ffi.RzDiffBatch(self.n_images, self.paths, self.segs, self.width, self.height, int(self.fill_rule),
+                                self.alpha, self.ctrl_ptr)
+
+
 class BatchPlan:
     """A device-resident batch bound to its output: work list uploaded once,
     each ``launch()`` replays a captured CUDA graph (no host synchronisation)."""
@@ -377,6 +403,25 @@ class GpuRasterizer(Rasterizer):
 
     def plan(self, batch: MaskBatch, device_ptrs: dict, out_ptr: int) -> BatchPlan:
         return BatchPlan(self.ctx, batch, device_ptrs, out_ptr, self.flatness)
+
+    # ---- differentiable batch (device pointers)
+    def diff_forward(self, batch: DiffBatch, image_ptr: int) -> None:
+        """Renders every image of ``batch`` into ``image_ptr`` (device f32)."""
+        s = batch.struct()
+        self.ctx.check(self.ctx.lib.rz_diff_forward(self.ctx.ptr, ctypes.byref(s), self.flatness, image_ptr))
+
+    def l2_loss(self, image_ptr: int, target_ptr: int, n: int, dl_ptr: int | None = None) -> float:
+        """sum (image - target)^2 (binary64); ``dl_ptr`` receives 2 (image - target)."""
+        out = ctypes.c_double(0.0)
+        self.ctx.check(self.ctx.lib.rz_l2_loss(self.ctx.ptr, image_ptr, target_ptr, n, ctypes.byref(out), dl_ptr))
+        return float(out.value)
+
+    def diff_backward(self, batch: DiffBatch, image_ptr: int, dl_ptr: int, out_ptr: int) -> None:
+        """d loss / d control points into ``out_ptr`` (device f32, the layout
+        of the control points) from d loss / d image, tree held fixed."""
+        s = batch.struct()
+        self.ctx.check(self.ctx.lib.rasterize_backward(self.ctx.ptr, ctypes.byref(s), self.flatness, image_ptr,
+                                                       dl_ptr, out_ptr))
 
     def mask_batch_device(self, batch: MaskBatch, device_ptrs: dict, out_ptr: int, per_path: bool = False):
         """Same with inputs and output already in device memory (no copies)."""

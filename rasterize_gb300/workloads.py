@@ -197,3 +197,14 @@ def scene(seed: int = 3, n: int = 2000, size: int = 2048, seg_range=(20, 2000), 
         paint = random_paint(rng, 0.0, 0.0, 2 * r, linear_colors)
         sc.fill(path, paint, tr, FillRule.NonZero)
     return sc
+
+
+def diff_batch(seed: int = 4, n_images: int = 64, paths: int = 256, segs: int = 32, size: int = 1024,
+               jitter: float = 2.0, margin: float = 0.0):
+    """Differentiable batch: control points (n_images, paths, 3*segs, 2)
+    uniform in [-margin, size + margin]^2 (float32) and the jittered copy
+    (N(0, jitter px)) the target images are rendered from."""
+    rng = np.random.default_rng(seed)
+    ctrl = rng.uniform(-margin, size + margin, size=(n_images, paths, 3 * segs, 2)).astype(np.float32)
+    target = (ctrl + rng.normal(0.0, jitter, size=ctrl.shape)).astype(np.float32)
+    return ctrl, target
