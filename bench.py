@@ -268,7 +268,85 @@ def run_configs(R, stream):
                        "segments_per_s": round(nseg / ms * 1e3, 1), "err": _config_err(canvas["c"], ref),
                        "cpu_baseline_ms": round(cpu_s * 1e3, 1), "cores": 1,
                        "note": "error per colour channel; host canvas in and out"}
+    out["C5_diff"] = run_diff(R, stream)
     return out
+
+
+def run_diff(R, stream, n_images=64, paths=256, segs=32, size=1024, fd_coords=100):
+    """Differentiable batch: 64 images of 1024^2, 256 closed cubic paths x 32
+    segments each (FP32 control points uniform in the canvas), solid paint of
+    alpha 0.5; target rendered from the control points jittered by N(0, 2 px);
+    L2 loss; forward and adjoint timed on device-resident inputs.  Central
+    finite differences (h = 1e-3 px) of the GPU loss on 100 random coordinates
+    of image 0, and the CPU-baseline leg's binary64 gradient of image 0."""
+    import numpy as np
+    import torch
+    from oracle import oracle as O
+    from rasterize_gb300 import DiffBatch
+    from rasterize_gb300 import workloads as W
+    dev = torch.device("cuda", torch.cuda.current_device())
+    ctrl, tctrl = W.diff_batch(seed=4, n_images=n_images, paths=paths, segs=segs, size=size)
+    d_ctrl = torch.from_numpy(ctrl).to(dev)
+    d_tctrl = torch.from_numpy(tctrl).to(dev)
+    npx = n_images * size * size
+    img = torch.empty(npx, dtype=torch.float32, device=dev)
+    tgt = torch.empty_like(img)
+    dl = torch.empty_like(img)
+    grad = torch.empty(d_ctrl.numel(), dtype=torch.float32, device=dev)
+    batch = DiffBatch(n_images, paths, segs, size, size, d_ctrl.data_ptr())
+    R.diff_forward(DiffBatch(n_images, paths, segs, size, size, d_tctrl.data_ptr()), tgt.data_ptr())
+
+    def fwd():
+        R.diff_forward(batch, img.data_ptr())
+        return R.l2_loss(img.data_ptr(), tgt.data_ptr(), npx, dl.data_ptr())
+
+    def bwd():
+        R.diff_backward(batch, img.data_ptr(), dl.data_ptr(), grad.data_ptr())
+
+    loss = fwd()
+    bwd()
+    fwd_ms = _event_ms(stream, fwd, 3)
+    bwd_ms = _event_ms(stream, bwd, 3)
+    g = grad.cpu().numpy().reshape(ctrl.shape)
+    # finite differences of the GPU loss of image 0 alone
+    rng = np.random.default_rng(11)
+    c0 = ctrl[:1].copy()
+    d_c0 = torch.from_numpy(c0).to(dev)
+    img0 = torch.empty(size * size, dtype=torch.float32, device=dev)
+    b0 = DiffBatch(1, paths, segs, size, size, d_c0.data_ptr())
+
+    def loss0(c):
+        d_c0.copy_(torch.from_numpy(c))
+        R.diff_forward(b0, img0.data_ptr())
+        return R.l2_loss(img0.data_ptr(), tgt.data_ptr(), size * size)
+
+    rel = []
+    for _ in range(fd_coords):
+        p, j, k = rng.integers(paths), rng.integers(3 * segs), rng.integers(2)
+        cp, cm = c0.copy(), c0.copy()
+        cp[0, p, j, k] += np.float32(1e-3)
+        cm[0, p, j, k] -= np.float32(1e-3)
+        hsum = float(cp[0, p, j, k]) - float(cm[0, p, j, k])
+        fd = (loss0(cp) - loss0(cm)) / hsum
+        an = float(g[0, p, j, k])
+        rel.append(abs(an - fd) / max(abs(fd), 1e-2))
+    rel = np.array(rel)
+    # CPU-baseline leg: the binary64 forward + adjoint of image 0 (timed), and the GPU gradient's error against it
+    t = time.perf_counter()
+    A = O.diff_forward(ctrl[0].astype(np.float64), paths, segs, size, size)
+    T0 = tgt[: size * size].cpu().numpy().reshape(size, size).astype(np.float64)
+    ref = O.diff_backward(ctrl[0].astype(np.float64), paths, segs, size, size, A, 2.0 * (A - T0))
+    cpu_s = time.perf_counter() - t
+    gerr = np.abs(g[0] - ref)
+    return {"forward_ms": round(fwd_ms, 3), "backward_ms_per_step": round(bwd_ms, 3),
+            "mpx_per_s_forward": round(npx / fwd_ms / 1e3, 1), "loss": loss,
+            "fd": {"coords": fd_coords, "h_px": 1e-3, "median_rel_err": float(np.median(rel)),
+                   "p90_rel_err": float(np.percentile(rel, 90)), "within_1e-2": int((rel <= 1e-2).sum())},
+            "grad_vs_f64": {"max_abs": float(gerr.max()), "max_ref": float(np.abs(ref).max()),
+                            "rel_to_max": float(gerr.max() / max(np.abs(ref).max(), 1e-30)), "image": 0},
+            "cpu_baseline_ms_per_image": round(cpu_s * 1e3, 1), "cores": 1,
+            "workload": "%d images %dx%d, %d closed cubic paths x %d segs, alpha 0.5, NonZero" %
+                        (n_images, size, size, paths, segs)}
 
 
 def run_reference(args, rank, world):
