@@ -71,6 +71,15 @@ class RzDiffBatch(ctypes.Structure):
                 ("paint_alpha", ctypes.c_float), ("ctrl", ctypes.c_void_p)]
 
 
+class RzTuneEntry(ctypes.Structure):
+    _fields_ = [("band_rows_cap", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("ms", ctypes.c_float)]
+
+
+class RzTuneResult(ctypes.Structure):
+    _fields_ = [("band_rows_cap", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("ms", ctypes.c_float),
+                ("n_entries", ctypes.c_uint32), ("entries", RzTuneEntry * 16)]
+
+
 _lock = threading.Lock()
 _lib = None
 
@@ -105,6 +114,10 @@ _SIGNATURES = {
     "rz_diff_forward": (ctypes.c_int32, [P, ctypes.POINTER(RzDiffBatch), ctypes.c_double, P]),
     "rz_l2_loss": (ctypes.c_int32, [P, P, P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double), P]),
     "rasterize_backward": (ctypes.c_int32, [P, ctypes.POINTER(RzDiffBatch), ctypes.c_double, P, P, P]),
+    "rz_tune_batch": (ctypes.c_int32, [P, ctypes.POINTER(RzPathBatch), ctypes.c_double, P, ctypes.c_uint64,
+                                       ctypes.POINTER(RzTuneResult)]),
+    "rz_set_tuning": (ctypes.c_int32, [P, ctypes.c_int32, ctypes.c_int32]),
+    "rz_device_name": (ctypes.c_char_p, [P]),
 }
 
 

@@ -107,6 +107,10 @@ struct rz_ctx {
     DevBuf p_fills, p_paints, p_slots, p_lines, p_ecount, p_estart, p_ecursor, p_pairs, p_scan, p_canvas;
     // differentiable batch
     DevBuf p_leaf, d_loss;
+    // batch tuning (rz_tune_batch / rz_set_tuning): band height cap, resident CTAs per SM (0 = occupancy)
+    int tune_rows_cap = 256;
+    int tune_ctas = 0;
+    std::string device_name;
     HostBuf h_stage, h_out;
     // host-side arc expansion scratch
     std::vector<uint8_t> x_kind;
@@ -209,10 +213,10 @@ rz_status status_from_device(rz_ctx* ctx, int32_t code) {
 bool valid_flatness(double f) { return std::isfinite(f) && 16.0 * f * f > 0.0; }
 
 // Band height for a mask: as many rows as fit in the shared band, at most
-// 256 (the fixed-point accumulator holds band-relative y below 511).
-int band_rows(int clip_width, int height) {
+// `cap` (<= 256: the fixed-point accumulator holds band-relative y below 511).
+int band_rows(int clip_width, int height, int cap = 256) {
     const int stride = rz::band_stride(clip_width);
-    int rows = std::min(256, std::max(1, rz::band_floats() / stride));
+    int rows = std::min(std::min(cap, 256), std::max(1, rz::band_floats() / stride));
     return std::min(rows, std::max(1, height));
 }
 
@@ -223,14 +227,14 @@ struct Items {
 
 // Work items sorted by decreasing band area so the persistent CTAs pick the
 // longest items first (LPT order); `grouped` keeps path order instead.
-void build_items(const std::vector<rz::MaskDev>& masks, bool grouped, Items& out) {
+void build_items(const std::vector<rz::MaskDev>& masks, bool grouped, Items& out, int rows_cap = 256) {
     out.items.clear();
     out.path_first.assign(masks.size() + 1, 0);
     for (size_t p = 0; p < masks.size(); ++p) {
         out.path_first[p] = (int)out.items.size();
         const rz::MaskDev& m = masks[p];
         if (m.width <= 0 || m.height <= 0) continue;
-        const int rows = band_rows(m.clip_width, m.height);
+        const int rows = band_rows(m.clip_width, m.height, rows_cap);
         for (int y = 0; y < m.height; y += rows) {
             rz::WorkItem w;
             w.path = (uint32_t)p;
@@ -436,14 +440,20 @@ rz_status stage_plan(rz_ctx* ctx, const std::vector<rz::MaskDev>& masks, const I
     return RZ_OK;
 }
 
+// Persistent grid: resident CTAs per SM from the occupancy, or the tuned count.
+int batch_grid(rz_ctx* ctx, int n_items) {
+    const int occ = std::max(1, rz::mask_bands_occupancy());
+    const int per_sm = ctx->tune_ctas > 0 ? std::min(ctx->tune_ctas, occ) : occ;
+    return std::max(1, std::min(n_items, ctx->num_sms * per_sm));
+}
+
 rz_status run_bands(rz_ctx* ctx, const rz::BatchDev& b, const Items& items, bool per_path) {
     int32_t* queue = (int32_t*)ctx->d_ctrl.p + 8;
     const rz::WorkItem* d_items = (const rz::WorkItem*)ctx->d_items.p;
     if (!per_path) {
         const int n = (int)items.items.size();
         if (n == 0) return RZ_OK;
-        const int occ = std::max(1, rz::mask_bands_occupancy());
-        const int grid = std::min(n, ctx->num_sms * occ);
+        const int grid = batch_grid(ctx, n);
         RZ_CUDA(cudaMemsetAsync(queue, 0, 4, ctx->stream));
         RZ_CUDA(rz::launch_mask_bands(b, d_items, n, queue, grid, ctx->stream));
     } else {
@@ -654,7 +664,7 @@ static rz_status mask_batch_impl(rz_ctx* ctx, const rz_path_batch* batch, double
         b.n_subpaths = batch->n_subpaths;
     }
     Items items;
-    build_items(masks, per_path, items);
+    build_items(masks, per_path, items, ctx->tune_rows_cap);
     tr.mark("items");
     st = stage_plan(ctx, masks, items, b);
     if (st) return st;
@@ -773,7 +783,7 @@ rz_batch_plan* rz_batch_plan_create(rz_ctx* ctx, const rz_path_batch* batch, dou
     }
     rz_batch_plan* plan = new rz_batch_plan();
     plan->ctx = ctx;
-    build_items(masks, false, plan->items);
+    build_items(masks, false, plan->items, ctx->tune_rows_cap);
     const size_t sz_m = std::max<size_t>(masks.size(), 1) * sizeof(rz::MaskDev);
     const size_t sz_i = std::max<size_t>(plan->items.items.size(), 1) * sizeof(rz::WorkItem);
     cudaError_t e = plan->d_masks.ensure(sz_m);
@@ -806,8 +816,7 @@ rz_batch_plan* rz_batch_plan_create(rz_ctx* ctx, const rz_path_batch* batch, dou
     b.counters = ctrl + 4;
     set_thresholds(b, flatness);
     const int n = (int)plan->items.items.size();
-    const int occ = std::max(1, rz::mask_bands_occupancy());
-    plan->grid = std::max(1, std::min(n, ctx->num_sms * occ));
+    plan->grid = batch_grid(ctx, n);
     // capture: reset the queue head, one persistent launch
     int32_t* queue = ctrl + 8;
     e = cudaStreamBeginCapture(plan->capture_stream, cudaStreamCaptureModeThreadLocal);
@@ -1475,6 +1484,122 @@ rz_status rasterize_backward(rz_ctx* ctx, const rz_diff_batch* batch, double fla
     RZ_CUDA(rz::launch_diff(D, true, cov_stride, smem, ctx->stream));
     tr.gpu_mark(ctx->stream, "adjoint");
     return read_error(ctx);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batch autotuner
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* rz_device_name(rz_ctx* ctx) {
+    if (!ctx) return "";
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    if (ctx->device_name.empty()) {
+        cudaDeviceProp prop;
+        if (cudaGetDeviceProperties(&prop, ctx->device) == cudaSuccess) ctx->device_name = prop.name;
+        else cudaGetLastError();
+    }
+    return ctx->device_name.c_str();
+}
+
+rz_status rz_set_tuning(rz_ctx* ctx, int32_t band_rows_cap, int32_t ctas_per_sm) {
+    if (!ctx) return RZ_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    if (band_rows_cap < 0 || band_rows_cap > 256 || ctas_per_sm < 0 || ctas_per_sm > 32)
+        return fail(ctx, RZ_ERR_INVALID, "band_rows_cap must be 0..256 and ctas_per_sm 0..32");
+    ctx->tune_rows_cap = band_rows_cap ? band_rows_cap : 256;
+    ctx->tune_ctas = ctas_per_sm;
+    return RZ_OK;
+}
+
+rz_status rz_tune_batch(rz_ctx* ctx, const rz_path_batch* batch, double flatness, float* out, uint64_t out_len,
+                        rz_tune_result* result) {
+    if (!ctx) return RZ_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    if (!batch || !out || !batch->masks || !result || batch->memory != RZ_MEM_DEVICE)
+        return fail(ctx, RZ_ERR_INVALID, "the tuner needs a device-memory batch and output");
+    if (!valid_flatness(flatness)) return fail(ctx, RZ_ERR_INVALID, "flatness must be > 0 and finite");
+    RZ_CUDA(cudaSetDevice(ctx->device));
+    const uint32_t P = batch->n_paths;
+    std::vector<rz::MaskDev> masks(P);
+    for (uint32_t p = 0; p < P; ++p) {
+        const rz_mask_desc& d = batch->masks[p];
+        if (d.width > 16383 || d.height > 16383 || (d.height > 0 && d.row_stride < d.width))
+            return fail(ctx, RZ_ERR_INVALID, "bad mask descriptor");
+        if (d.width && d.height && d.offset + (uint64_t)(d.height - 1) * d.row_stride + d.width > out_len)
+            return fail(ctx, RZ_ERR_INVALID, "mask exceeds output buffer");
+        masks[p].offset = d.offset;
+        masks[p].width = (int32_t)d.width;
+        masks[p].height = (int32_t)d.height;
+        masks[p].row_stride = (int32_t)d.row_stride;
+        masks[p].clip_width = (int32_t)d.width - 1;
+    }
+    rz::BatchDev b{};
+    b.kind = batch->seg_kind;
+    b.pts = batch->seg_pts;
+    b.sub_off = batch->subpath_off;
+    b.path_sub = batch->path_subpath_off;
+    b.tr = batch->transforms;
+    b.rule = batch->fill_rules;
+    b.n_segments = batch->n_segments;
+    b.n_subpaths = batch->n_subpaths;
+    b.out = out;
+    set_thresholds(b, flatness);
+    const int occ = std::max(1, rz::mask_bands_occupancy());
+    const int caps[5] = {16, 32, 64, 128, 256};
+    const int saved_cap = ctx->tune_rows_cap, saved_ctas = ctx->tune_ctas;
+    std::memset(result, 0, sizeof(*result));
+    result->ms = 1e30f;
+    cudaEvent_t e0, e1;
+    RZ_CUDA(cudaEventCreate(&e0));
+    RZ_CUDA(cudaEventCreate(&e1));
+    rz_status st = RZ_OK;
+    for (int ci = 0; ci < 5 && st == RZ_OK; ++ci) {
+        for (int per_sm = occ; per_sm >= std::max(1, occ - 1) && st == RZ_OK; --per_sm) {
+            ctx->tune_rows_cap = caps[ci];
+            ctx->tune_ctas = per_sm;
+            Items items;
+            build_items(masks, false, items, caps[ci]);
+            rz::BatchDev bb = b;
+            st = stage_plan(ctx, masks, items, bb);
+            if (st) break;
+            float t[3] = {0.f, 0.f, 0.f};
+            for (int rep = 0; rep < 4 && st == RZ_OK; ++rep) {
+                if (cudaEventRecord(e0, ctx->stream) != cudaSuccess) { st = RZ_ERR_CUDA; break; }
+                st = run_bands(ctx, bb, items, false);
+                if (st) break;
+                if (cudaEventRecord(e1, ctx->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+                    st = RZ_ERR_CUDA;
+                    break;
+                }
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (rep > 0) t[rep - 1] = ms;  // the first launch warms up
+            }
+            if (st) break;
+            st = read_error(ctx);
+            if (st) break;
+            std::sort(t, t + 3);
+            if (result->n_entries < 16) result->entries[result->n_entries++] = rz_tune_entry{caps[ci], per_sm, t[1]};
+            if (t[1] < result->ms) {
+                result->ms = t[1];
+                result->band_rows_cap = caps[ci];
+                result->ctas_per_sm = per_sm;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st) {
+        ctx->tune_rows_cap = saved_cap;
+        ctx->tune_ctas = saved_ctas;
+        return st == RZ_ERR_CUDA ? fail(ctx, st, "tuning launch failed") : st;
+    }
+    ctx->tune_rows_cap = result->band_rows_cap;
+    ctx->tune_ctas = result->ctas_per_sm;
+    return RZ_OK;
 }
 
 }  // extern "C"

@@ -12,6 +12,7 @@ from __future__ import annotations
 import abc
 import atexit
 import ctypes
+import os
 import weakref
 from dataclasses import dataclass
 
@@ -242,6 +243,14 @@ class Scene:
         return s, keepalive
 
 
+def _tune_key(device: str, batch: "MaskBatch", flatness: float) -> str:
+    """GPU + batch shape (paths, segments and pixels to two significant digits, flatness)."""
+    def sig2(v):
+        return "%.1e" % float(v) if v else "0"
+    return "%s|paths=%s|segs=%s|px=%s|f=%g" % (device, sig2(len(batch.paths)), sig2(batch.n_segments),
+                                               sig2(batch.pixels), flatness)
+
+
 class DiffBatch:
     """The differentiable batch: ``n_images`` images of (height, width), each
     the alpha channel of ``paths`` closed cubic paths of ``segs`` segments
@@ -403,6 +412,49 @@ class GpuRasterizer(Rasterizer):
 
     def plan(self, batch: MaskBatch, device_ptrs: dict, out_ptr: int) -> BatchPlan:
         return BatchPlan(self.ctx, batch, device_ptrs, out_ptr, self.flatness)
+
+    # ---- batch autotuner
+    def tune(self, batch: MaskBatch, device_ptrs: dict, out_ptr: int, cache: str | None = None,
+             retune: bool = False) -> dict:
+        """Chooses the band-height cap and resident CTAs per SM for batches
+        like ``batch`` (device memory) by timing every candidate, and applies
+        it to this context.  Results are stored in a JSON file (``cache``,
+        default $RZ_TUNE_CACHE or ~/.cache/rasterize_gb300/tune.json) keyed by
+        the GPU and the batch's shape, so later processes apply them without
+        re-timing."""
+        import json
+        lib = self.ctx.lib
+        path = cache or os.environ.get("RZ_TUNE_CACHE") or os.path.join(
+            os.path.expanduser("~"), ".cache", "rasterize_gb300", "tune.json")
+        key = _tune_key(lib.rz_device_name(self.ctx.ptr).decode(), batch, self.flatness)
+        try:
+            with open(path) as f:
+                table = json.load(f)
+        except (OSError, ValueError):
+            table = {}
+        if not retune and key in table:
+            e = table[key]
+            self.ctx.check(lib.rz_set_tuning(self.ctx.ptr, int(e["band_rows_cap"]), int(e["ctas_per_sm"])))
+            return dict(e, cached=True)
+        s = batch.struct(_ffi.RZ_MEM_DEVICE, device_ptrs)
+        res = _ffi.RzTuneResult()
+        self.ctx.check(lib.rz_tune_batch(self.ctx.ptr, ctypes.byref(s), self.flatness, out_ptr, batch.out_len,
+                                         ctypes.byref(res)))
+        entry = {"band_rows_cap": res.band_rows_cap, "ctas_per_sm": res.ctas_per_sm, "ms": res.ms,
+                 "candidates": [[e.band_rows_cap, e.ctas_per_sm, e.ms] for e in res.entries[:res.n_entries]]}
+        table[key] = entry
+        try:
+            os.makedirs(os.path.dirname(path), exist_ok=True)
+            tmp = path + ".tmp.%d" % os.getpid()
+            with open(tmp, "w") as f:
+                json.dump(table, f, indent=1, sort_keys=True)
+            os.replace(tmp, path)
+        except OSError:
+            pass
+        return dict(entry, cached=False)
+
+    def set_tuning(self, band_rows_cap: int = 0, ctas_per_sm: int = 0) -> None:
+        self.ctx.check(self.ctx.lib.rz_set_tuning(self.ctx.ptr, int(band_rows_cap), int(ctas_per_sm)))
 
     # ---- differentiable batch (device pointers)
     def diff_forward(self, batch: DiffBatch, image_ptr: int) -> None:
