@@ -1355,11 +1355,11 @@ rz_status diff_check(rz_ctx* ctx, const rz_diff_batch* b, double flatness) {
 }
 
 // Band height: the largest of 8, 4, 2, 1 rows that divides the image height
-// and keeps the backward kernel's shared memory within 64 KiB.
+// and keeps the backward kernel's shared memory within 72 KiB (3 CTAs per SM).
 int diff_band_rows(int width, int height) {
     for (int r = 8; r > 1; r >>= 1) {
         int cs = 0;
-        if (height % r == 0 && rz::diff_smem_bytes(width, r, true, &cs) <= 64 * 1024) return r;
+        if (height % r == 0 && rz::diff_smem_bytes(width, r, true, &cs) <= 72 * 1024) return r;
     }
     return 1;
 }

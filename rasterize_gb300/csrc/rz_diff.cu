@@ -80,13 +80,11 @@ __device__ __forceinline__ VtxQ diff_vtx(int4 e, int row0) {
     return v;
 }
 
-// Coverage of fill f in the band: clear, accumulate its lines.  Ends with a barrier.
-__device__ void diff_coverage(const DiffDev& D, const FillDev& f, uint32_t e, const Band& B) {
+// Accumulates the lines of (fill, band) entry e into the band, which the
+// previous scan left cleared.  Barriers before (the previous scan is done with
+// the band) and after.
+__device__ void diff_accumulate(const DiffDev& D, uint32_t e, const Band& B) {
     const SceneDev& S = D.S;
-    float4* c4 = reinterpret_cast<float4*>(B.acc);
-    const int n4 = (B.bh * B.stride) >> 2;
-    __syncthreads();  // the previous user of the band is done
-    for (int i = threadIdx.x; i < n4; i += kDiffThreads) c4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
     const uint32_t n = S.entry_count[e], start = S.entry_start[e];
     for (uint32_t j = threadIdx.x; j < n; j += kDiffThreads) {
@@ -96,23 +94,55 @@ __device__ void diff_coverage(const DiffDev& D, const FillDev& f, uint32_t e, co
     __syncthreads();
 }
 
+// Clears the band words of a row past the scanned columns (lines write up to
+// column width + 1).
+__device__ __forceinline__ void clear_row_tail(int4* row4, int width, int stride, int lane) {
+    for (int c = ((width + 3) & ~3) + 4 * lane; c < stride; c += 128) row4[c >> 2] = make_int4(0, 0, 0, 0);
+}
+
 // ---------------------------------------------------------------------------
 // Forward
 // ---------------------------------------------------------------------------
-struct DiffBlend {
-    float* A;  // band, width per row
-    int width;
-    float alpha;
-    __device__ __forceinline__ void operator()(int r, int x0, const float (&a)[kScanChunk]) const {
-        #pragma unroll
-        for (int i = 0; i < kScanChunk; ++i) {
-            const int x = x0 + i;
-            if (x >= width || a[i] < 1e-6f) continue;  // fill skips |alpha| < 1e-6 (src/rasterize.rs:347-349)
-            float& d = A[r * width + x];
-            d = fmaf(alpha * a[i], 1.f - d, d);
+// Row prefix of the band (clearing it as it reads), fill rule, and
+// A += a alpha (1 - A) for the pixels the fill does not skip (|alpha| < 1e-6,
+// src/rasterize.rs:347-349).  One warp per row, 4 pixels per lane.
+__device__ void diff_scan_blend(const Band& B, int width, int rule, float alpha, float* A) {
+    const int lane = threadIdx.x & 31;
+    for (int r = threadIdx.x >> 5; r < B.bh; r += kDiffThreads / 32) {
+        int4* row4 = reinterpret_cast<int4*>(B.acc + r * B.stride);
+        uint32_t carry = 0;
+        for (int x0 = 0; x0 < width; x0 += 128) {
+            const int x = x0 + 4 * lane;
+            int4 v = make_int4(0, 0, 0, 0);
+            if (x < width) {
+                v = row4[x >> 2];
+                row4[x >> 2] = make_int4(0, 0, 0, 0);
+            }
+            const uint32_t a0 = (uint32_t)v.x;
+            const uint32_t a1 = a0 + (x + 1 < width ? (uint32_t)v.y : 0u);
+            const uint32_t a2 = a1 + (x + 2 < width ? (uint32_t)v.z : 0u);
+            const uint32_t a3 = a2 + (x + 3 < width ? (uint32_t)v.w : 0u);
+            uint32_t incl = a3;
+            #pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t o = __shfl_up_sync(0xffffffffu, incl, off);
+                if (lane >= off) incl += o;
+            }
+            const uint32_t base = carry + incl - a3;
+            carry += __shfl_sync(0xffffffffu, incl, 31);
+            const uint32_t wv[4] = {base + a0, base + a1, base + a2, base + a3};
+            #pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                if (x + i >= width) break;
+                const float al = alpha_from_winding_fix(rule, (int32_t)wv[i]);
+                if (al < 1e-6f) continue;
+                float& d = A[r * width + x + i];
+                d = fmaf(alpha * al, 1.f - d, d);
+            }
         }
+        clear_row_tail(row4, width, B.stride, lane);
     }
-};
+}
 
 __global__ void __launch_bounds__(kDiffThreads) k_diff_forward(DiffDev D, int cov_stride) {
     extern __shared__ float4 sm4[];
@@ -124,13 +154,14 @@ __global__ void __launch_bounds__(kDiffThreads) k_diff_forward(DiffDev D, int co
     const int row_base = band * rows;
     const int img = row_base / D.height;
     for (int i = threadIdx.x; i < rows * D.width; i += kDiffThreads) A[i] = 0.f;
+    for (int i = threadIdx.x; i < (rows * cov_stride) >> 2; i += kDiffThreads) sm4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int p = 0; p < D.paths; ++p) {
         const FillDev& f = S.fills[img * D.paths + p];
         const uint32_t e = f.entry0 + (band - f.band0);
         if (S.entry_count[e] == 0) continue;  // no line in the band: no coverage
         const Band B = diff_band(D, f, cov, row_base, rows);
-        diff_coverage(D, f, e, B);
-        band_scan<kDiffThreads>(B, D.width, D.rule, DiffBlend{A, D.width, D.alpha});
+        diff_accumulate(D, e, B);
+        diff_scan_blend(B, D.width, D.rule, D.alpha, A);
     }
     __syncthreads();
     float* out = D.out + (uint64_t)row_base * D.width;  // canvas rows are image rows
@@ -169,10 +200,12 @@ __device__ __forceinline__ Dual dlerp(const Dual& a, const Dual& b, const Dual& 
     return dadd(a, dmul(t, dsub(b, a)));
 }
 
-// Mean of W_r over [lo, hi] (x relative to column c0) and its derivatives.
-__device__ void diff_row_mean(const float* G, const float* g, int W, int c0, float lo, float hi, float& I, float& dlo,
+// Mean of W_r over [lo, hi] (x relative to column c0) and its derivatives;
+// P: exclusive row prefix of g (W + 1 entries), so G[k] = P[W] - P[k].
+__device__ void diff_row_mean(const float* P, const float* g, int W, int c0, float lo, float hi, float& I, float& dlo,
                               float& dhi) {
     const float wmax = (float)(W - c0), wmin = (float)(-c0);
+    const float total = P[W];
     lo = fminf(fmaxf(lo, wmin), wmax);
     hi = fminf(fmaxf(hi, lo), wmax);
     const float D = hi - lo;
@@ -180,7 +213,7 @@ __device__ void diff_row_mean(const float* G, const float* g, int W, int c0, flo
         int k = (int)floorf(lo);
         k = min(max(k + c0, 0), W - 1);
         const float kr = (float)(k - c0);
-        I = G[k + 1] + (kr + 1.f - lo) * g[k];
+        I = (total - P[k + 1]) + (kr + 1.f - lo) * g[k];
         dlo = dhi = -0.5f * g[k];
         return;
     }
@@ -192,7 +225,7 @@ __device__ void diff_row_mean(const float* G, const float* g, int W, int c0, flo
         const int kk = k + c0;
         const float gk = g[kk];
         const float ka = (float)(k + 1) - a, kb = (float)(k + 1) - b;
-        sI += G[kk + 1] * (b - a) + gk * 0.5f * (ka * ka - kb * kb);
+        sI += (total - P[kk + 1]) * (b - a) + gk * 0.5f * (ka * ka - kb * kb);
         shi -= gk * 0.5f * ((b - lo) * (b - lo) - (a - lo) * (a - lo));
         slo -= gk * 0.5f * ((hi - a) * (hi - a) - (hi - b) * (hi - b));
     }
@@ -206,7 +239,7 @@ __device__ void diff_row_mean(const float* G, const float* g, int W, int c0, flo
 // x relative to column c0, y relative to band row 0.
 __device__ void diff_piece(Dual px, Dual py, Dual qx, Dual qy, int rows, int W, int c0, const float* G, const float* g,
                            float (&out)[4]) {
-    const int Gs = W + 1;
+    const int Gs = W + 1;  // G: the exclusive prefix P of the band, W + 1 entries per row
     if (py.v == qy.v) {
         // horizontal: no coverage, but moving an end vertically brings coverage in
         const int r = (int)floorf(py.v);
@@ -277,17 +310,25 @@ __device__ void diff_line(float ax, float ay, float bx, float by, int rows, int 
     }
 }
 
-// Row scan of the band that hands the fixed-point windings to the epilogue.
-template <class Epi>
-__device__ void band_scan_winding(const Band& B, int width, const Epi& epi) {
+// Row prefix of the band (clearing it as it reads), then per pixel
+// g = c / (1 - a alpha) * dalpha/dw with c = dL/dA * a (1 - A) staged per band,
+// and the exclusive row prefix P of g (P[W] = the row total).
+__device__ void diff_scan_grad(const Band& B, int width, int rule, float alpha, const float* c, float* g, float* P) {
     const int lane = threadIdx.x & 31;
     for (int r = threadIdx.x >> 5; r < B.bh; r += kDiffThreads / 32) {
-        const int4* row4 = reinterpret_cast<const int4*>(B.acc + r * B.stride);
+        int4* row4 = reinterpret_cast<int4*>(B.acc + r * B.stride);
+        const float* cr = c + r * width;
+        float* gr = g + r * width;
+        float* Pr = P + r * (width + 1);
         uint32_t carry = 0;
-        for (int x0 = 0; x0 < width; x0 += 32 * kScanChunk) {
-            const int x = x0 + kScanChunk * lane;
+        float gcarry = 0.f;
+        for (int x0 = 0; x0 < width; x0 += 128) {
+            const int x = x0 + 4 * lane;
             int4 v = make_int4(0, 0, 0, 0);
-            if (x < width) v = row4[x >> 2];
+            if (x < width) {
+                v = row4[x >> 2];
+                row4[x >> 2] = make_int4(0, 0, 0, 0);
+            }
             const uint32_t a0 = (uint32_t)v.x;
             const uint32_t a1 = a0 + (x + 1 < width ? (uint32_t)v.y : 0u);
             const uint32_t a2 = a1 + (x + 2 < width ? (uint32_t)v.z : 0u);
@@ -300,72 +341,44 @@ __device__ void band_scan_winding(const Band& B, int width, const Epi& epi) {
             }
             const uint32_t base = carry + incl - a3;
             carry += __shfl_sync(0xffffffffu, incl, 31);
-            if (x < width) {
-                const int32_t w[kScanChunk] = {(int32_t)(base + a0), (int32_t)(base + a1), (int32_t)(base + a2),
-                                               (int32_t)(base + a3)};
-                epi(r, x, w);
-            }
-        }
-    }
-}
-
-// g = dL/dA * a (1 - A) / (1 - a alpha) * dalpha/dw per pixel of the band.
-struct DiffGrad {
-    float* g;
-    const float* A;   // forward image rows of the band
-    const float* dl;  // d loss / d image rows of the band
-    int width, rule;
-    float alpha;
-    __device__ __forceinline__ void operator()(int r, int x0, const int32_t (&w)[kScanChunk]) const {
-        #pragma unroll
-        for (int i = 0; i < kScanChunk; ++i) {
-            const int x = x0 + i;
-            if (x >= width) continue;
-            float al = alpha_from_winding_fix(rule, w[i]);
-            if (al < 1e-6f) al = 0.f;  // skipped by the forward: no blend, no slope
-            float da = 0.f;
-            if (al != 0.f) {
+            const uint32_t wv[4] = {base + a0, base + a1, base + a2, base + a3};
+            float gv[4];
+            #pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                gv[i] = 0.f;
+                if (x + i >= width) continue;
+                const int32_t w = (int32_t)wv[i];
+                const float al = alpha_from_winding_fix(rule, w);
+                if (al < 1e-6f) continue;  // skipped by the forward: no blend, no slope
+                float da = 0.f;
                 if (rule == 1) {
                     // EvenOdd: |((w + 1) mod 2) - 1|, slope = sign of the folded value
-                    const int32_t f = (int32_t)(((uint32_t)w[i] + (1u << 22)) & ((1u << 23) - 1u)) - (1 << 22);
-                    da = f > 0 ? 1.f : -1.f;
+                    const int32_t fo = (int32_t)(((uint32_t)w + (1u << 22)) & ((1u << 23) - 1u)) - (1 << 22);
+                    da = fo > 0 ? 1.f : -1.f;
                 } else if (al < 1.f) {
-                    da = w[i] > 0 ? 1.f : -1.f;
+                    da = w > 0 ? 1.f : -1.f;
                 }
+                if (da != 0.f) gv[i] = cr[x + i] / (1.f - alpha * al) * da;
             }
-            const int o = r * width + x;
-            g[o] = da == 0.f ? 0.f : dl[o] * alpha * (1.f - A[o]) / (1.f - alpha * al) * da;
-        }
-    }
-};
-
-// G[x] = sum over x' >= x of g[x'] (G[W] = 0), one warp per row.
-__device__ void suffix_rows(const float* g, float* G, int rows, int W) {
-    const int lane = threadIdx.x & 31;
-    for (int r = threadIdx.x >> 5; r < rows; r += kDiffThreads / 32) {
-        const float* gr = g + r * W;
-        float* Gr = G + r * (W + 1);
-        float carry = 0.f;
-        const int nchunk = (W + 127) / 128;
-        for (int c = nchunk - 1; c >= 0; --c) {
-            const int x = c * 128 + 4 * lane;
-            const float v0 = x < W ? gr[x] : 0.f, v1 = x + 1 < W ? gr[x + 1] : 0.f;
-            const float v2 = x + 2 < W ? gr[x + 2] : 0.f, v3 = x + 3 < W ? gr[x + 3] : 0.f;
-            const float s3 = v3, s2 = v2 + s3, s1 = v1 + s2, s0 = v0 + s1;
-            float incl = s0;  // suffix over lanes >= lane
+            const float s0 = gv[0], s1 = s0 + gv[1], s2 = s1 + gv[2], s3 = s2 + gv[3];
+            float ginc = s3;
             #pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
-                const float o = __shfl_down_sync(0xffffffffu, incl, off);
-                if (lane + off < 32) incl += o;
+                const float o = __shfl_up_sync(0xffffffffu, ginc, off);
+                if (lane >= off) ginc += o;
             }
-            const float base = carry + incl - s0;
-            carry += __shfl_sync(0xffffffffu, incl, 0);
-            if (x < W) Gr[x] = base + s0;
-            if (x + 1 < W) Gr[x + 1] = base + s1;
-            if (x + 2 < W) Gr[x + 2] = base + s2;
-            if (x + 3 < W) Gr[x + 3] = base + s3;
+            const float gbase = gcarry + ginc - s3;
+            gcarry += __shfl_sync(0xffffffffu, ginc, 31);
+            if (x < width) {
+                gr[x] = gv[0];
+                Pr[x] = gbase;
+            }
+            if (x + 1 < width) { gr[x + 1] = gv[1]; Pr[x + 1] = gbase + s0; }
+            if (x + 2 < width) { gr[x + 2] = gv[2]; Pr[x + 2] = gbase + s1; }
+            if (x + 3 < width) { gr[x + 3] = gv[3]; Pr[x + 3] = gbase + s2; }
         }
-        if (lane == 0) Gr[W] = 0.f;
+        if (lane == 0) Pr[width] = gcarry;
+        clear_row_tail(row4, width, B.stride, lane);
     }
 }
 
@@ -375,14 +388,17 @@ __global__ void __launch_bounds__(kDiffThreads) k_diff_backward(DiffDev D, int c
     const SceneDev& S = D.S;
     const int rows = S.band_rows;
     const int W = D.width;
-    float* g = cov + rows * cov_stride;
-    float* G = g + rows * W;
+    float* c = cov + rows * cov_stride;  // dL/dA * a (1 - A) of the band
+    float* g = c + rows * W;
+    float* G = g + rows * W;             // exclusive row prefix of g, W + 1 per row
     const int band = blockIdx.x;
     const int row_base = band * rows;
     const int img = row_base / D.height;
     const float* A = D.image + (uint64_t)row_base * W;
     const float* dl = D.dl_dimage + (uint64_t)row_base * W;
     float2* out = reinterpret_cast<float2*>(D.out);
+    for (int i = threadIdx.x; i < rows * W; i += kDiffThreads) c[i] = dl[i] * D.alpha * (1.f - A[i]);
+    for (int i = threadIdx.x; i < (rows * cov_stride) >> 2; i += kDiffThreads) sm4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int p = 0; p < D.paths; ++p) {
         const uint32_t fi = (uint32_t)(img * D.paths + p);
         const FillDev& f = S.fills[fi];
@@ -390,10 +406,8 @@ __global__ void __launch_bounds__(kDiffThreads) k_diff_backward(DiffDev D, int c
         const uint32_t n = S.entry_count[e];
         if (n == 0) continue;  // no line in the band: zero coverage and no line to move
         const Band B = diff_band(D, f, cov, row_base, rows);
-        diff_coverage(D, f, e, B);
-        band_scan_winding(B, W, DiffGrad{g, A, dl, W, D.rule, D.alpha});
-        __syncthreads();
-        suffix_rows(g, G, rows, W);
+        diff_accumulate(D, e, B);  // also waits for the previous path's line pass
+        diff_scan_grad(B, W, D.rule, D.alpha, c, g, G);
         __syncthreads();
         const uint32_t start = S.entry_start[e];
         for (uint32_t j = threadIdx.x; j < n; j += kDiffThreads) {
@@ -458,7 +472,9 @@ __global__ void k_l2_loss(const float* __restrict__ A, const float* __restrict__
 int diff_smem_bytes(int width, int band_rows, bool backward, int* cov_stride) {
     const int stride = band_stride(width);
     *cov_stride = stride;
-    return 4 * band_rows * stride + 4 * band_rows * width + (backward ? 4 * band_rows * (width + 1) : 0);
+    // forward: coverage + A; backward: coverage + c + g + prefix (W + 1 per row)
+    return 4 * band_rows * stride + 4 * band_rows * width +
+           (backward ? 4 * band_rows * width + 4 * band_rows * (width + 1) : 0);
 }
 
 cudaError_t launch_diff_segments(const float* ctrl, uint32_t n_paths, int segs, uint8_t* kind, double* pts,
