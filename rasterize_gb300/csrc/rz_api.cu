@@ -38,6 +38,11 @@ cudaError_t launch_bin_scatter(const SceneDev& S, cudaStream_t st);
 int composite_smem_bytes(int canvas_w, int band_rows, int max_clip_width, bool paint_mode, int* cov_stride);
 cudaError_t launch_composite(const SceneDev& S, int cov_stride, int smem, cudaStream_t st);
 uint64_t scan_temp_words(uint64_t n);
+int lines_band_floats();
+cudaError_t init_lines_kernel();
+int mask_lines_occupancy();
+cudaError_t launch_mask_lines(const SceneDev& S, const MaskDev* masks, const WorkItem* items, int n_items,
+                              int32_t* queue, float* out, int grid, cudaStream_t st);
 int diff_smem_bytes(int width, int band_rows, bool backward, int* cov_stride);
 cudaError_t launch_diff_segments(const float* ctrl, uint32_t n_paths, int segs, uint8_t* kind, double* pts,
                                  cudaStream_t st);
@@ -214,9 +219,10 @@ bool valid_flatness(double f) { return std::isfinite(f) && 16.0 * f * f > 0.0; }
 
 // Band height for a mask: as many rows as fit in the shared band, at most
 // `cap` (<= 256: the fixed-point accumulator holds band-relative y below 511).
-int band_rows(int clip_width, int height, int cap = 256) {
+int band_rows(int clip_width, int height, int cap = 256, int band_floats = 0) {
     const int stride = rz::band_stride(clip_width);
-    int rows = std::min(std::min(cap, 256), std::max(1, rz::band_floats() / stride));
+    const int floats = band_floats > 0 ? band_floats : rz::band_floats();
+    int rows = std::min(std::min(cap, 256), std::max(1, floats / stride));
     return std::min(rows, std::max(1, height));
 }
 
@@ -227,14 +233,15 @@ struct Items {
 
 // Work items sorted by decreasing band area so the persistent CTAs pick the
 // longest items first (LPT order); `grouped` keeps path order instead.
-void build_items(const std::vector<rz::MaskDev>& masks, bool grouped, Items& out, int rows_cap = 256) {
+void build_items(const std::vector<rz::MaskDev>& masks, bool grouped, Items& out, int rows_cap = 256,
+                 int band_floats = 0) {
     out.items.clear();
     out.path_first.assign(masks.size() + 1, 0);
     for (size_t p = 0; p < masks.size(); ++p) {
         out.path_first[p] = (int)out.items.size();
         const rz::MaskDev& m = masks[p];
         if (m.width <= 0 || m.height <= 0) continue;
-        const int rows = band_rows(m.clip_width, m.height, rows_cap);
+        const int rows = band_rows(m.clip_width, m.height, rows_cap, band_floats);
         for (int y = 0; y < m.height; y += rows) {
             rz::WorkItem w;
             w.path = (uint32_t)p;
@@ -284,7 +291,7 @@ rz_ctx* rz_create(int device, rz_status* status) {
     if (cudaSetDevice(device) != cudaSuccess ||
         cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
-        rz::init_kernels() != cudaSuccess) {
+        rz::init_kernels() != cudaSuccess || rz::init_lines_kernel() != cudaSuccess) {
         cudaGetLastError();
         delete c;
         if (status) *status = RZ_ERR_NO_DEVICE;
@@ -441,10 +448,106 @@ rz_status stage_plan(rz_ctx* ctx, const std::vector<rz::MaskDev>& masks, const I
 }
 
 // Persistent grid: resident CTAs per SM from the occupancy, or the tuned count.
-int batch_grid(rz_ctx* ctx, int n_items) {
-    const int occ = std::max(1, rz::mask_bands_occupancy());
+int batch_grid(rz_ctx* ctx, int n_items, bool lines = false) {
+    const int occ = std::max(1, lines ? rz::mask_lines_occupancy() : rz::mask_bands_occupancy());
     const int per_sm = ctx->tune_ctas > 0 ? std::min(ctx->tune_ctas, occ) : occ;
     return std::max(1, std::min(n_items, ctx->num_sms * per_sm));
+}
+
+// ---------------------------------------------------------------------------
+// Batches through the line pipeline (k_mask_lines): one fill per path, every
+// segment flattened once, the lines of a path contiguous.
+// ---------------------------------------------------------------------------
+// The band kernel (tree walks per band, overlapped with coverage in one
+// persistent launch) is the default for batches of small paths; the lines
+// kernel (flatten once, then bands) is selected with RZ_BATCH_KERNEL=lines.
+bool use_lines_kernel() {
+    const char* e = std::getenv("RZ_BATCH_KERNEL");
+    return e && std::strcmp(e, "lines") == 0;
+}
+
+// Fills of a batch from host copies of its offsets, rules and transforms.
+uint32_t lines_fills(const std::vector<rz::MaskDev>& masks, const uint32_t* sub_off, const uint32_t* path_sub,
+                     const uint8_t* rules, const double* trs, std::vector<rz::FillDev>& fills) {
+    const size_t P = masks.size();
+    fills.assign(P, rz::FillDev{});
+    uint32_t slot = 0;
+    for (size_t p = 0; p < P; ++p) {
+        rz::FillDev& f = fills[p];
+        f.sub0 = path_sub[p];
+        f.sub1 = path_sub[p + 1];
+        f.seg0 = sub_off[f.sub0];
+        f.seg1 = sub_off[f.sub1];
+        f.slot0 = slot;
+        slot += (f.seg1 - f.seg0) + (f.sub1 - f.sub0);
+        f.width = masks[p].width;
+        f.height = masks[p].height;
+        f.clip_width = masks[p].clip_width;
+        f.rule = rules ? rules[p] : 0;
+        f.paint = -1;
+        const double id[6] = {1, 0, 0, 0, 1, 0};
+        std::memcpy(f.tr, trs ? trs + 6 * p : id, sizeof(f.tr));
+    }
+    return slot;
+}
+
+rz::SceneDev lines_scene(const rz::BatchDev& b, const rz::FillDev* fills, uint32_t n_fills, uint32_t n_slots,
+                         uint32_t* slot_count) {
+    rz::SceneDev S{};
+    S.kind = b.kind;
+    S.pts = b.pts;
+    S.sub_off = b.sub_off;
+    S.fills = fills;
+    S.n_fills = n_fills;
+    S.n_slots = n_slots;
+    S.n_segments = b.n_segments;
+    S.n_subpaths = b.n_subpaths;
+    S.thr64 = b.thr64;
+    S.thr32 = b.thr32;
+    S.slot_count = slot_count;
+    S.err = b.err;
+    S.counters = b.counters;
+    return S;
+}
+
+// Count + scan (lines per slot, then their offsets) on `st`.
+rz_status lines_count(rz_ctx* ctx, rz::SceneDev& S, uint32_t* scan_tmp, cudaStream_t st) {
+    const uint64_t nt = rz::slot_tasks(S.n_slots, S.task_depth) + 1;
+    RZ_CUDA(cudaMemsetAsync(S.slot_count, 0, nt * 4, st));
+    RZ_CUDA(rz::launch_flatten_count(S, st));
+    RZ_CUDA(rz::scan_u32(S.slot_count, nt, scan_tmp, st));
+    return RZ_OK;
+}
+
+// One batch render through the lines kernel (masks and items already staged in b / ctx->d_items).
+rz_status run_lines(rz_ctx* ctx, const rz::BatchDev& b, const std::vector<rz::FillDev>& fills, uint32_t n_slots,
+                    const Items& items, Trace& tr) {
+    const int n = (int)items.items.size();
+    if (n == 0 || fills.empty()) return RZ_OK;
+    RZ_CUDA(ctx->p_fills.ensure(fills.size() * sizeof(rz::FillDev)));
+    RZ_CUDA(cudaMemcpyAsync(ctx->p_fills.p, fills.data(), fills.size() * sizeof(rz::FillDev), cudaMemcpyHostToDevice,
+                            ctx->stream));
+    RZ_CUDA(ctx->p_slots.ensure((rz::slot_tasks(n_slots, 0) + 1) * 4));
+    RZ_CUDA(ctx->p_scan.ensure(rz::scan_temp_words(rz::slot_tasks(n_slots, 0) + 1) * 4 + 64));
+    rz::SceneDev S = lines_scene(b, (const rz::FillDev*)ctx->p_fills.p, (uint32_t)fills.size(), n_slots,
+                                 (uint32_t*)ctx->p_slots.p);
+    rz_status st = lines_count(ctx, S, (uint32_t*)ctx->p_scan.p, ctx->stream);
+    if (st) return st;
+    uint32_t n_lines = 0;
+    RZ_CUDA(cudaMemcpyAsync(&n_lines, S.slot_count + rz::slot_tasks(n_slots, 0), 4, cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+    tr.mark("flatten_count");
+    RZ_CUDA(ctx->p_lines.ensure((uint64_t)std::max(n_lines, 1u) * 2 * sizeof(int4)));
+    S.lines = (int4*)ctx->p_lines.p;
+    S.n_lines = n_lines;
+    S.line_cap = n_lines;
+    RZ_CUDA(rz::launch_flatten_emit(S, ctx->stream));
+    int32_t* queue = (int32_t*)ctx->d_ctrl.p + 8;
+    RZ_CUDA(cudaMemsetAsync(queue, 0, 4, ctx->stream));
+    RZ_CUDA(rz::launch_mask_lines(S, b.masks, (const rz::WorkItem*)ctx->d_items.p, n, queue, b.out,
+                                  batch_grid(ctx, n, true), ctx->stream));
+    return RZ_OK;
 }
 
 rz_status run_bands(rz_ctx* ctx, const rz::BatchDev& b, const Items& items, bool per_path) {
@@ -663,8 +766,9 @@ static rz_status mask_batch_impl(rz_ctx* ctx, const rz_path_batch* batch, double
         b.n_segments = batch->n_segments;
         b.n_subpaths = batch->n_subpaths;
     }
+    const bool lines = !per_path && batch->memory == RZ_MEM_HOST && use_lines_kernel();
     Items items;
-    build_items(masks, per_path, items, ctx->tune_rows_cap);
+    build_items(masks, per_path, items, ctx->tune_rows_cap, lines ? rz::lines_band_floats() : 0);
     tr.mark("items");
     st = stage_plan(ctx, masks, items, b);
     if (st) return st;
@@ -679,7 +783,15 @@ static rz_status mask_batch_impl(rz_ctx* ctx, const rz_path_batch* batch, double
         b.out = direct_out ? (float*)direct_out : out;
     }
     tr.mark("stage_plan");
-    st = run_bands(ctx, b, items, per_path);
+    if (lines) {
+        std::vector<rz::FillDev> fills;
+        const uint32_t n_slots = lines_fills(masks, ctx->expanded ? ctx->x_sub.data() : batch->subpath_off,
+                                             ctx->expanded ? ctx->x_psub.data() : batch->path_subpath_off,
+                                             batch->fill_rules, batch->transforms, fills);
+        st = run_lines(ctx, b, fills, n_slots, items, tr);
+    } else {
+        st = run_bands(ctx, b, items, per_path);
+    }
     if (st) return st;
     if (batch->memory == RZ_MEM_HOST && !direct_out)
         RZ_CUDA(cudaMemcpyAsync(out, b.out, out_len * 4, cudaMemcpyDeviceToHost, ctx->stream));
@@ -747,6 +859,9 @@ struct rz_batch_plan {
     rz::BatchDev b{};
     Items items;
     DevBuf d_masks, d_items, d_ctrl;
+    // lines kernel: fills, line offsets, scan scratch, lines
+    bool lines = false;
+    DevBuf d_fills, d_slots, d_scan, d_lines;
     int grid = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -783,7 +898,41 @@ rz_batch_plan* rz_batch_plan_create(rz_ctx* ctx, const rz_path_batch* batch, dou
     }
     rz_batch_plan* plan = new rz_batch_plan();
     plan->ctx = ctx;
-    build_items(masks, false, plan->items, ctx->tune_rows_cap);
+    // the lines kernel needs the offsets on the host and no raw arcs (those are expanded by the band kernel)
+    std::vector<uint8_t> h_kind;
+    std::vector<uint32_t> h_sub, h_psub;
+    std::vector<uint8_t> h_rule;
+    std::vector<double> h_tr;
+    if (use_lines_kernel() && P > 0) {
+        h_kind.resize(batch->n_segments);
+        h_sub.resize((size_t)batch->n_subpaths + 1);
+        h_psub.resize((size_t)P + 1);
+        cudaError_t ce = cudaSuccess;
+        if (batch->n_segments)
+            ce = cudaMemcpy(h_kind.data(), batch->seg_kind, batch->n_segments, cudaMemcpyDeviceToHost);
+        if (ce == cudaSuccess)
+            ce = cudaMemcpy(h_sub.data(), batch->subpath_off, h_sub.size() * 4, cudaMemcpyDeviceToHost);
+        if (ce == cudaSuccess)
+            ce = cudaMemcpy(h_psub.data(), batch->path_subpath_off, h_psub.size() * 4, cudaMemcpyDeviceToHost);
+        if (ce == cudaSuccess && batch->fill_rules) {
+            h_rule.resize(P);
+            ce = cudaMemcpy(h_rule.data(), batch->fill_rules, P, cudaMemcpyDeviceToHost);
+        }
+        if (ce == cudaSuccess && batch->transforms) {
+            h_tr.resize((size_t)P * 6);
+            ce = cudaMemcpy(h_tr.data(), batch->transforms, h_tr.size() * 8, cudaMemcpyDeviceToHost);
+        }
+        if (ce != cudaSuccess) {
+            delete plan;
+            return bail(cuda_fail(ctx, ce, "plan: reading the batch offsets"));
+        }
+        bool ok = !(batch->n_segments && std::memchr(h_kind.data(), RZ_SEG_ARC, batch->n_segments));
+        for (uint32_t p = 0; ok && p < P; ++p) ok = h_psub[p] <= h_psub[p + 1] && h_psub[p + 1] <= batch->n_subpaths;
+        for (uint32_t i = 0; ok && i < batch->n_subpaths; ++i) ok = h_sub[i] <= h_sub[i + 1];
+        ok = ok && h_sub[batch->n_subpaths] <= batch->n_segments;
+        plan->lines = ok;
+    }
+    build_items(masks, false, plan->items, ctx->tune_rows_cap, plan->lines ? rz::lines_band_floats() : 0);
     const size_t sz_m = std::max<size_t>(masks.size(), 1) * sizeof(rz::MaskDev);
     const size_t sz_i = std::max<size_t>(plan->items.items.size(), 1) * sizeof(rz::WorkItem);
     cudaError_t e = plan->d_masks.ensure(sz_m);
@@ -816,15 +965,54 @@ rz_batch_plan* rz_batch_plan_create(rz_ctx* ctx, const rz_path_batch* batch, dou
     b.counters = ctrl + 4;
     set_thresholds(b, flatness);
     const int n = (int)plan->items.items.size();
-    plan->grid = batch_grid(ctx, n);
-    // capture: reset the queue head, one persistent launch
+    plan->grid = batch_grid(ctx, n, plan->lines);
     int32_t* queue = ctrl + 8;
+    rz::SceneDev S{};
+    if (plan->lines) {
+        // fills, offsets and a first count + scan (outside the graph) to size the line buffer
+        std::vector<rz::FillDev> fills;
+        const uint32_t n_slots = lines_fills(masks, h_sub.data(), h_psub.data(), batch->fill_rules ? h_rule.data() : nullptr,
+                                             batch->transforms ? h_tr.data() : nullptr, fills);
+        e = plan->d_fills.ensure(std::max<size_t>(fills.size(), 1) * sizeof(rz::FillDev));
+        if (e == cudaSuccess && !fills.empty())
+            e = cudaMemcpy(plan->d_fills.p, fills.data(), fills.size() * sizeof(rz::FillDev), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = plan->d_slots.ensure((rz::slot_tasks(n_slots, 0) + 1) * 4);
+        if (e == cudaSuccess) e = plan->d_scan.ensure(rz::scan_temp_words(rz::slot_tasks(n_slots, 0) + 1) * 4 + 64);
+        S = lines_scene(b, (const rz::FillDev*)plan->d_fills.p, (uint32_t)fills.size(), n_slots,
+                        (uint32_t*)plan->d_slots.p);
+        uint32_t n_lines = 0;
+        if (e == cudaSuccess && lines_count(ctx, S, (uint32_t*)plan->d_scan.p, plan->capture_stream) != RZ_OK)
+            e = cudaErrorUnknown;
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&n_lines, S.slot_count + rz::slot_tasks(n_slots, 0), 4, cudaMemcpyDeviceToHost,
+                                plan->capture_stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(plan->capture_stream);
+        if (e == cudaSuccess) e = plan->d_lines.ensure((uint64_t)std::max(n_lines, 1u) * 2 * sizeof(int4));
+        S.lines = (int4*)plan->d_lines.p;
+        S.n_lines = n_lines;
+        // replays of changed geometry get the buffer's slack, then an RZ_ERR_CAPACITY status, never an overrun
+        S.line_cap = (uint32_t)std::min<uint64_t>(plan->d_lines.cap / (2 * sizeof(int4)), 0xffffffffull);
+        if (e != cudaSuccess) {
+            rz_batch_plan_destroy(plan);
+            return bail(cuda_fail(ctx, e, "plan: line buffer"));
+        }
+    }
+    // capture: (lines: count, scan, emit,) reset the queue head, one persistent launch
     e = cudaStreamBeginCapture(plan->capture_stream, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
+        if (plan->lines) {
+            lines_count(ctx, S, (uint32_t*)plan->d_scan.p, plan->capture_stream);
+            rz::launch_flatten_emit(S, plan->capture_stream);
+        }
         cudaMemsetAsync(queue, 0, 4, plan->capture_stream);
-        if (n > 0)
-            rz::launch_mask_bands(b, (const rz::WorkItem*)plan->d_items.p, n, queue, plan->grid,
-                                  plan->capture_stream);
+        if (n > 0) {
+            if (plan->lines)
+                rz::launch_mask_lines(S, (const rz::MaskDev*)plan->d_masks.p, (const rz::WorkItem*)plan->d_items.p, n,
+                                      queue, out, plan->grid, plan->capture_stream);
+            else
+                rz::launch_mask_bands(b, (const rz::WorkItem*)plan->d_items.p, n, queue, plan->grid,
+                                      plan->capture_stream);
+        }
         e = cudaStreamEndCapture(plan->capture_stream, &plan->graph);
     }
     if (e == cudaSuccess) e = cudaGraphInstantiate(&plan->exec, plan->graph, 0);
@@ -875,6 +1063,10 @@ void rz_batch_plan_destroy(rz_batch_plan* plan) {
     plan->d_masks.release();
     plan->d_items.release();
     plan->d_ctrl.release();
+    plan->d_fills.release();
+    plan->d_slots.release();
+    plan->d_scan.release();
+    plan->d_lines.release();
     delete plan;
 }
 
@@ -977,6 +1169,7 @@ struct HostScene {
     uint32_t n_seg = 0, n_sub = 0;
     uint32_t n_slots = 0, n_entries = 0;
     int band_rows = 1, n_bands = 0, max_clip = 1;
+    int task_depth = 0;  // flatten tasks per slot = 2^task_depth (2 for large segments)
 };
 
 int choose_band_rows(int canvas_w, int canvas_h, bool paint_mode) {
@@ -1023,7 +1216,7 @@ rz_status build_lines(rz_ctx* ctx, HostScene& hs, rz::SceneDev& S, Trace& tr, De
                             cudaMemcpyHostToDevice, ctx->stream));
     S.fills = (const rz::FillDev*)ctx->p_fills.p;
     // 1) lines per slot, 2) offsets (one extra element receives the total)
-    const uint64_t ns = (uint64_t)hs.n_slots + 1;
+    const uint64_t ns = rz::slot_tasks(hs.n_slots, hs.task_depth) + 1;
     RZ_CUDA(ctx->p_slots.ensure(ns * 4));
     S.slot_count = (uint32_t*)ctx->p_slots.p;
     RZ_CUDA(cudaMemsetAsync(S.slot_count, 0, ns * 4, ctx->stream));
@@ -1034,7 +1227,8 @@ rz_status build_lines(rz_ctx* ctx, HostScene& hs, rz::SceneDev& S, Trace& tr, De
     RZ_CUDA(ctx->p_scan.ensure(rz::scan_temp_words(std::max(ns, ne)) * 4 + 64));
     RZ_CUDA(rz::scan_u32(S.slot_count, ns, (uint32_t*)ctx->p_scan.p, ctx->stream));
     uint32_t n_lines = 0;
-    RZ_CUDA(cudaMemcpyAsync(&n_lines, S.slot_count + hs.n_slots, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    RZ_CUDA(cudaMemcpyAsync(&n_lines, S.slot_count + rz::slot_tasks(hs.n_slots, hs.task_depth), 4, cudaMemcpyDeviceToHost,
+                            ctx->stream));
     RZ_CUDA(cudaStreamSynchronize(ctx->stream));
     rz_status st = read_error(ctx);
     if (st) return st;
@@ -1046,6 +1240,7 @@ rz_status build_lines(rz_ctx* ctx, HostScene& hs, rz::SceneDev& S, Trace& tr, De
     // 3) lines + per-(fill, band) counts
     RZ_CUDA(ctx->p_lines.ensure((uint64_t)std::max(n_lines, 1u) * 2 * sizeof(int4)));
     S.lines = (int4*)ctx->p_lines.p;
+    S.line_cap = n_lines;
     RZ_CUDA(ctx->p_ecount.ensure(ne * 4));
     RZ_CUDA(ctx->p_estart.ensure(ne * 4));
     RZ_CUDA(ctx->p_ecursor.ensure(ne * 4));
@@ -1085,6 +1280,7 @@ rz_status run_pipeline(rz_ctx* ctx, HostScene& hs, double flatness, float* canva
     S.n_slots = hs.n_slots;
     S.n_segments = hs.n_seg;
     S.n_subpaths = hs.n_sub;
+    S.task_depth = hs.task_depth;
     S.thr64 = 16.0 * flatness * flatness;
     S.thr32 = (float)S.thr64;
     S.canvas_w = canvas_w;
@@ -1160,6 +1356,7 @@ rz_status mask_pipeline(rz_ctx* ctx, const rz_path* path, const double tr[6], in
                                         path->n_subpaths, psub, 1, hs, fsub);
     if (st) return st;
     hs.band_rows = choose_band_rows((int)width, (int)height, false);
+    hs.task_depth = 2;  // a path this large has long segments
     rzhost::Xf t;
     std::memcpy(t.m, tr, sizeof(t.m));
     add_fill(hs, fsub[0], fsub[1], 0, 0, (int)width, (int)height, (int)width - 1, t, rule, -1);
@@ -1385,6 +1582,7 @@ rz_status diff_prepare(rz_ctx* ctx, const rz_diff_batch* b, double flatness, rz:
     hs.n_sub = n_paths;
     const int W = (int)b->width, H = (int)b->height;
     hs.band_rows = diff_band_rows(W, H);
+    hs.task_depth = 2;  // cubics spanning the canvas: hundreds of leaves each
     const rzhost::Xf id{{1, 0, 0, 0, 1, 0}};
     for (uint32_t p = 0; p < n_paths; ++p)
         add_fill(hs, p, p + 1, 0, (int)(p / P) * H, W, H, W, id, b->fill_rule, 0);  // fill semantics: clip at W
@@ -1397,6 +1595,7 @@ rz_status diff_prepare(rz_ctx* ctx, const rz_diff_batch* b, double flatness, rz:
     S.n_slots = hs.n_slots;
     S.n_segments = hs.n_seg;
     S.n_subpaths = hs.n_sub;
+    S.task_depth = hs.task_depth;
     S.thr64 = 16.0 * flatness * flatness;
     S.thr32 = (float)S.thr64;
     S.canvas_w = W;

@@ -139,23 +139,6 @@ __device__ __forceinline__ int decide_slot(const BatchDev& b, const SegRec& r, c
 constexpr int kSmemBytes = kBandBytes + kThreads * (int)sizeof(SegRec) + kThreads * (int)sizeof(SlotCoef) +
                            kLeafCap * (int)sizeof(LeafCode) + 2 * kLevelCap * (int)sizeof(uint32_t);
 
-// Mask epilogue of the row scan: a 16-byte streaming store of 4 alphas.
-struct MaskStore {
-    float* out;
-    uint64_t offset;
-    int64_t row_stride;
-    int y0, width;
-    __device__ __forceinline__ void operator()(int r, int x0, const float (&a)[kScanChunk]) const {
-        float* o = out + offset + (uint64_t)(y0 + r) * (uint64_t)row_stride + x0;
-        if (((reinterpret_cast<uintptr_t>(o) & 15u) == 0) && (x0 + kScanChunk <= width)) {
-            __stcs(reinterpret_cast<float4*>(o), make_float4(a[0], a[1], a[2], a[3]));
-        } else {
-            #pragma unroll
-            for (int i = 0; i < kScanChunk; ++i)
-                if (x0 + i < width) o[i] = a[i];
-        }
-    }
-};
 
 
 __device__ inline void drain_leaf(const Band& B, const SegRec* recs, const LeafCode c) {
@@ -253,6 +236,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_mask_bands(BatchDev b, const Wo
     __shared__ int s_item;
     __shared__ int s_nleaf;
     __shared__ int s_nlevel[2];
+    __shared__ int s_task;  // next subtree to walk (threads that finish early take the next one)
     int fallbacks = 0;
     const int tid = threadIdx.x;
     for (int round = 0;; ++round) {
@@ -289,7 +273,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_mask_bands(BatchDev b, const Wo
             const bool active = i < n_seg + n_close &&
                                 band_load(b, B, seg0, n_seg, sub0, i, trm, recs[tid], coefs[tid], fallbacks);
             // ---- breadth-first over the top levels of every tree, all threads together
-            if (tid == 0) { s_nlevel[0] = 0; s_nlevel[1] = 0; }
+            if (tid == 0) { s_nlevel[0] = 0; s_nlevel[1] = 0; s_task = kThreads; }
             __syncthreads();
             if (active) level[0][atomicAdd(&s_nlevel[0], 1)] = (uint32_t)tid << 24;
             int cur = 0;
@@ -324,7 +308,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_mask_bands(BatchDev b, const Wo
                 cur ^= 1;
             }
             __syncthreads();
-            // ---- the remaining subtrees (roots at depth kSpreadDepth) walked serially, spread over threads
+            // ---- the remaining subtrees (roots at depth kSpreadDepth) walked serially, handed out to threads
+            //      as they finish (subtree sizes vary widely)
             const int n_sub = s_nlevel[cur];
             int task = tid;
             TreeWalk W;
@@ -362,7 +347,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_mask_bands(BatchDev b, const Wo
                         --W.d;
                     }
                     if (W.d == kSpreadDepth) {
-                        task += kThreads;
+                        task = atomicAdd(&s_task, 1);
                         if (task < n_sub) {
                             slot = (int)(level[cur][task] >> 24);
                             W.k = level[cur][task] & 0xffffffu;

@@ -527,6 +527,17 @@ __device__ __forceinline__ void accumulate_vtx(const Band& B, const VtxQ& a, con
                       (double)b.row + (double)b.fy);
 }
 
+// A stored line end (exact 16.16 anchor + FP32 remainder, frame of its view)
+// as a vertex with its row relative to band row `row0`.
+__device__ __forceinline__ VtxQ line_vtx(int4 e, int row0) {
+    VtxQ v;
+    v.col = e.x >> 16;
+    v.row = (e.y >> 16) - row0;
+    v.fx = fmaf((float)(e.x & 0xffff), 1.0f / 65536.0f, __int_as_float(e.z));
+    v.fy = fmaf((float)(e.y & 0xffff), 1.0f / 65536.0f, __int_as_float(e.w));
+    return v;
+}
+
 // ---------------------------------------------------------------------------
 // Row prefix sum (exact integer) + fill rule
 // ---------------------------------------------------------------------------
@@ -654,6 +665,24 @@ __device__ void band_scan(const Band& B, int width, int rule, const Epi& epi) {
         }
     }
 }
+
+// Mask epilogue of the row scan: a 16-byte streaming store of 4 alphas.
+struct MaskStore {
+    float* out;
+    uint64_t offset;
+    int64_t row_stride;
+    int y0, width;
+    __device__ __forceinline__ void operator()(int r, int x0, const float (&a)[kScanChunk]) const {
+        float* o = out + offset + (uint64_t)(y0 + r) * (uint64_t)row_stride + x0;
+        if (((reinterpret_cast<uintptr_t>(o) & 15u) == 0) && (x0 + kScanChunk <= width)) {
+            __stcs(reinterpret_cast<float4*>(o), make_float4(a[0], a[1], a[2], a[3]));
+        } else {
+            #pragma unroll
+            for (int i = 0; i < kScanChunk; ++i)
+                if (x0 + i < width) o[i] = a[i];
+        }
+    }
+};
 
 // ---------------------------------------------------------------------------
 // Segment records shared by the band kernel and the line pipeline

@@ -70,15 +70,6 @@ __device__ __forceinline__ Band diff_band(const DiffDev& D, const FillDev& f, fl
     return B;
 }
 
-// A stored line end (16.16 anchor + FP32 remainder, fill frame).
-__device__ __forceinline__ VtxQ diff_vtx(int4 e, int row0) {
-    VtxQ v;
-    v.col = e.x >> 16;
-    v.row = (e.y >> 16) - row0;
-    v.fx = fmaf((float)(e.x & 0xffff), FIX_ONE_INV, __int_as_float(e.z));
-    v.fy = fmaf((float)(e.y & 0xffff), FIX_ONE_INV, __int_as_float(e.w));
-    return v;
-}
 
 // Accumulates the lines of (fill, band) entry e into the band, which the
 // previous scan left cleared.  Barriers before (the previous scan is done with
@@ -89,7 +80,7 @@ __device__ void diff_accumulate(const DiffDev& D, uint32_t e, const Band& B) {
     const uint32_t n = S.entry_count[e], start = S.entry_start[e];
     for (uint32_t j = threadIdx.x; j < n; j += kDiffThreads) {
         const uint32_t l = S.pairs[start + j];
-        accumulate_vtx(B, diff_vtx(S.lines[2ull * l], B.y0), diff_vtx(S.lines[2ull * l + 1], B.y0));
+        accumulate_vtx(B, line_vtx(S.lines[2ull * l], B.y0), line_vtx(S.lines[2ull * l + 1], B.y0));
     }
     __syncthreads();
 }
@@ -414,7 +405,7 @@ __global__ void __launch_bounds__(kDiffThreads) k_diff_backward(DiffDev D, int c
             const uint32_t l = S.pairs[start + j];
             const uint2 code = S.leaf[l];
             if (code.x == 0xffffffffu) continue;  // a closing line (zero length here)
-            const VtxQ a = diff_vtx(S.lines[2ull * l], B.y0), b = diff_vtx(S.lines[2ull * l + 1], B.y0);
+            const VtxQ a = line_vtx(S.lines[2ull * l], B.y0), b = line_vtx(S.lines[2ull * l + 1], B.y0);
             const int c0 = a.col;
             float d4[4] = {0.f, 0.f, 0.f, 0.f};
             diff_line(a.fx, (float)a.row + a.fy, (float)(b.col - c0) + b.fx, (float)b.row + b.fy, rows, W, c0, G, g,

@@ -102,30 +102,44 @@ __device__ void load_slot(const SceneDev& S, const FillDev& f, uint32_t s, SlotS
     }
 }
 
-// Leaves of the slot's tree, in order; `emit(d, k)` per leaf.  Returns false
-// on a tree deeper than MAX_DEPTH.
+__device__ __forceinline__ int slot_decide(const SceneDev& S, const FillDev& f, const SlotState& st, int d, uint32_t k,
+                                           int& fallbacks) {
+    if (st.fits) return decide_node(st.r, st.c, st.qerr, d, k, S.thr32, S.thr64, S.pts, f.tr, fallbacks);
+    const FlatCoef c = flat_coef(st.g);
+    return node_is_leaf(st.g, c, d, k, S.thr64, S.thr32, fallbacks);
+}
+
+// Leaves of task j of the slot's tree, in order; `emit(d, k)` per leaf.  A
+// leaf above the task depth belongs to the first task under it.  Returns
+// false on a tree deeper than MAX_DEPTH.
 template <class Emit>
-__device__ bool walk_slot(const SceneDev& S, const FillDev& f, const SlotState& st, int& fallbacks, Emit& emit) {
-    TreeWalk W;
-    W.start();
-    while (!W.done) {
-        int leaf;
-        if (st.fits) {
-            leaf = decide_node(st.r, st.c, st.qerr, W.d, W.k, S.thr32, S.thr64, S.pts, f.tr, fallbacks);
-        } else {
-            const FlatCoef c = flat_coef(st.g);
-            leaf = node_is_leaf(st.g, c, W.d, W.k, S.thr64, S.thr32, fallbacks);
+__device__ bool walk_task(const SceneDev& S, const FillDev& f, const SlotState& st, uint32_t j, int& fallbacks,
+                          Emit& emit) {
+    const int td = S.task_depth;
+    for (int d = 0; d < td; ++d) {
+        const int up = td - d;
+        if (slot_decide(S, f, st, d, j >> up, fallbacks)) {
+            if ((j & ((1u << up) - 1u)) == 0u) emit(d, j >> up);
+            return true;
         }
-        if (!leaf) {
-            if (W.d >= MAX_DEPTH) return false;
-            ++W.d;
-            W.k <<= 1;
+    }
+    int d = td;
+    uint32_t k = j;
+    for (;;) {
+        if (!slot_decide(S, f, st, d, k, fallbacks)) {
+            if (d >= MAX_DEPTH) return false;
+            ++d;
+            k <<= 1;
             continue;
         }
-        emit(W.d, W.k);
-        W.next_after_leaf();
+        emit(d, k);
+        while (d > td && (k & 1u)) {
+            k >>= 1;
+            --d;
+        }
+        if (d == td) return true;
+        k += 1u;
     }
-    return true;
 }
 
 struct CountLeaves {
@@ -133,11 +147,12 @@ struct CountLeaves {
     __device__ void operator()(int, uint32_t) { ++n; }
 };
 
-// A slot emits one line per leaf, or two (the reference's x rules split it)
-// when its coordinates are beyond the 16.16 range.
+// A leaf is one line, or two (the reference's x rules split it) when the
+// slot's coordinates are beyond the 16.16 range.
 __global__ void k_flatten_count(SceneDev S) {
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= S.n_slots) return;
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= slot_tasks(S.n_slots, S.task_depth)) return;
+    const uint32_t s = (uint32_t)(t >> S.task_depth), j = (uint32_t)(t & ((1u << S.task_depth) - 1u));
     const FillDev& f = S.fills[fill_of_slot(S, s)];
     SlotState st;
     load_slot(S, f, s, st);
@@ -145,10 +160,10 @@ __global__ void k_flatten_count(SceneDev S) {
     int fallbacks = 0;
     if (st.ok) {
         CountLeaves c;
-        if (!walk_slot(S, f, st, fallbacks, c)) pset_err(S.err, ERR_DEPTH);
+        if (!walk_task(S, f, st, j, fallbacks, c)) pset_err(S.err, ERR_DEPTH);
         n = st.fits ? c.n : 2u * c.n;
     }
-    S.slot_count[s] = n;
+    S.slot_count[t] = n;
     if (fallbacks) atomicAdd(&S.counters[1], fallbacks);
 }
 
@@ -189,24 +204,37 @@ struct EmitLines {
     const SlotState* st;
     uint32_t out;
     __device__ void write(int4 a, int4 b) {
+        if (out >= S->line_cap) {  // the geometry changed since the buffer was sized: report, never overrun
+            pset_err(S->err, ERR_CAPACITY);
+            ++out;
+            return;
+        }
         S->lines[2ull * out] = a;
         S->lines[2ull * out + 1] = b;
         ++out;
-        count_bands(*S, *f, make_int4(fix_add(a.x, __int_as_float(a.z)), fix_add(a.y, __int_as_float(a.w)),
-                                      fix_add(b.x, __int_as_float(b.z)), fix_add(b.y, __int_as_float(b.w))));
+        if (S->entry_count)
+            count_bands(*S, *f, make_int4(fix_add(a.x, __int_as_float(a.z)), fix_add(a.y, __int_as_float(a.w)),
+                                          fix_add(b.x, __int_as_float(b.z)), fix_add(b.y, __int_as_float(b.w))));
     }
     __device__ void operator()(int d, uint32_t k) {
         const uint32_t first = out;
         emit(d, k);
         if (S->leaf) {
             const uint2 code = make_uint2(st->src, ((uint32_t)d << 27) | k);
-            for (uint32_t i = first; i < out; ++i) S->leaf[i] = code;
+            for (uint32_t i = first; i < out && i < S->line_cap; ++i) S->leaf[i] = code;
         }
     }
+    // the last leaf's end vertex, as t * 2^MAX_DEPTH: the next leaf of the walk starts there
+    uint32_t prev_t = 0xffffffffu;
+    VtxQ prev;
     __device__ void emit(int d, uint32_t k) {
         if (st->fits) {
             // integer pixel of the vertex as the 16.16 anchor, its fraction as the remainder
-            const VtxQ a = rec_vtx(st->r, k, d, 0), b = rec_vtx(st->r, k + 1u, d, 0);
+            const uint32_t t0 = k << (MAX_DEPTH - d), t1 = (k + 1u) << (MAX_DEPTH - d);
+            const VtxQ a = t0 == prev_t ? prev : rec_vtx(st->r, k, d, 0);
+            const VtxQ b = rec_vtx(st->r, k + 1u, d, 0);
+            prev_t = t1;
+            prev = b;
             write(end_point(a.col << 16, a.row << 16, a.fx, a.fy), end_point(b.col << 16, b.row << 16, b.fx, b.fy));
         } else {
             // beyond the 16.16 range: the reference's x rules (src/rasterize.rs:372-393)
@@ -230,9 +258,11 @@ struct EmitLines {
                 }
                 if (i < np) {
                     write(e0, e1);
-                } else {
-                    S->lines[2ull * out] = e0;  // unused slot: a degenerate line
+                } else if (out < S->line_cap) {
+                    S->lines[2ull * out] = e0;  // unused slot: a degenerate line, never binned
                     S->lines[2ull * out + 1] = e1;
+                    ++out;
+                } else {
                     ++out;
                 }
             }
@@ -241,23 +271,25 @@ struct EmitLines {
 };
 
 __global__ void k_flatten_emit(SceneDev S) {
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= S.n_slots) return;
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= slot_tasks(S.n_slots, S.task_depth)) return;
+    const uint32_t s = (uint32_t)(t >> S.task_depth), j = (uint32_t)(t & ((1u << S.task_depth) - 1u));
     const FillDev& f = S.fills[fill_of_slot(S, s)];
     SlotState st;
     load_slot(S, f, s, st);
     if (!st.ok) return;
     int fallbacks = 0;
-    EmitLines e{&S, &f, &st, S.slot_count[s]};
-    walk_slot(S, f, st, fallbacks, e);
+    EmitLines e{&S, &f, &st, S.slot_count[t]};
+    walk_task(S, f, st, j, fallbacks, e);
 }
 
-// Fill owning line l (slot_count holds the line offsets of the slots).
+// Fill owning line l (slot_count holds the line offsets of the flatten tasks).
 __device__ __forceinline__ uint32_t fill_of_line(const SceneDev& S, uint32_t l) {
     uint32_t lo = 0, hi = S.n_fills;
     while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) >> 1;
-        const uint32_t first = S.fills[mid].slot0 < S.n_slots ? S.slot_count[S.fills[mid].slot0] : S.n_lines;
+        const uint32_t first =
+            S.fills[mid].slot0 < S.n_slots ? S.slot_count[slot_tasks(S.fills[mid].slot0, S.task_depth)] : S.n_lines;
         if (first <= l) lo = mid; else hi = mid;
     }
     return lo;
@@ -458,16 +490,6 @@ __device__ float4 paint_at(const PaintDev& p, float px, float py) {
 // ---------------------------------------------------------------------------
 // Composite
 // ---------------------------------------------------------------------------
-// A stored line end (16.16 anchor + FP32 remainder, fill frame) as a vertex
-// with its row relative to band row `row0`.
-__device__ __forceinline__ VtxQ line_vtx(int4 e, int row0) {
-    VtxQ v;
-    v.col = e.x >> 16;
-    v.row = (e.y >> 16) - row0;
-    v.fx = fmaf((float)(e.x & 0xffff), FIX_ONE_INV, __int_as_float(e.z));
-    v.fy = fmaf((float)(e.y & 0xffff), FIX_ONE_INV, __int_as_float(e.w));
-    return v;
-}
 
 constexpr int kCompThreads = 256;
 
@@ -578,14 +600,16 @@ __global__ void __launch_bounds__(kCompThreads) k_composite(SceneDev S, int cov_
 // launchers (declared in rz_api.cu)
 // ---------------------------------------------------------------------------
 cudaError_t launch_flatten_count(const SceneDev& S, cudaStream_t st) {
-    if (S.n_slots == 0) return cudaSuccess;
-    k_flatten_count<<<(S.n_slots + 127) / 128, 128, 0, st>>>(S);
+    const uint64_t n = slot_tasks(S.n_slots, S.task_depth);
+    if (n == 0) return cudaSuccess;
+    k_flatten_count<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(S);
     return cudaGetLastError();
 }
 
 cudaError_t launch_flatten_emit(const SceneDev& S, cudaStream_t st) {
-    if (S.n_slots == 0) return cudaSuccess;
-    k_flatten_emit<<<(S.n_slots + 127) / 128, 128, 0, st>>>(S);
+    const uint64_t n = slot_tasks(S.n_slots, S.task_depth);
+    if (n == 0) return cudaSuccess;
+    k_flatten_emit<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(S);
     return cudaGetLastError();
 }
 

@@ -15,6 +15,13 @@ namespace rz {
 
 constexpr int kMaxStops = 16;
 
+// Flattening work is split into 2^task_depth subtree tasks per segment slot
+// (task t = slot * 2^task_depth + j walks the subtree at depth task_depth,
+// index j), so large segments spread over several threads and a warp's
+// threads do similar amounts of work.  Lines stay in tree order.  Small
+// segments use depth 0 (every task loads its segment).
+__host__ __device__ inline uint64_t slot_tasks(uint64_t n_slots, int task_depth) { return n_slots << task_depth; }
+
 // One fill of a scene (or the single path of a large mask), device memory.
 struct FillDev {
     uint32_t sub0, sub1;     // subpath range (global)
@@ -61,15 +68,17 @@ struct SceneDev {
     uint32_t n_slots;
     uint32_t n_segments;
     uint32_t n_subpaths;
+    int32_t task_depth;      // flatten tasks per slot = 2^task_depth
     double thr64;
     float thr32;
     int32_t canvas_w, canvas_h;
     int32_t band_rows;       // canvas rows per band
     int32_t n_bands;
     // pipeline buffers
-    uint32_t* slot_count;    // [n_slots] lines per slot, then its exclusive prefix
+    uint32_t* slot_count;    // [tasks + 1] lines per flatten task, then its exclusive prefix (line offsets)
     int4* lines;             // [2 * n_lines] per end point: exact 16.16 anchor (x, y), FP32 remainder (dx, dy)
     uint32_t n_lines;
+    uint32_t line_cap;       // lines the buffer holds (the emit pass reports more as ERR_CAPACITY)
     uint32_t* entry_count;   // [n_entries]
     uint32_t* entry_start;   // [n_entries] exclusive prefix of entry_count
     uint32_t* entry_cursor;  // [n_entries]

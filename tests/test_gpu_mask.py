@@ -223,3 +223,17 @@ def test_batch_with_transforms_and_rules(R):
     for i in range(len(paths)):
         w, h = sizes[i]
         assert_close(batch.mask(out, i), O.mask(paths[i], trs[i], rules[i], w, h))
+
+
+def test_lines_kernel_matches_band_kernel(R, monkeypatch):
+    """The two batch kernels (the band kernel that walks the trees per band,
+    the default, and flatten once + k_mask_lines) render the same masks."""
+    paths, sizes, rules = W.glyph_batch(seed=31, n=200, side_range=(16, 400))
+    batch = MaskBatch(paths, sizes, fill_rules=rules)
+    bands = R.mask_batch(batch)
+    monkeypatch.setenv("RZ_BATCH_KERNEL", "lines")
+    lines = R.mask_batch(batch)
+    assert np.abs(lines - bands).max() <= 1e-6
+    for i in range(0, 200, 9):
+        w, h = sizes[i]
+        assert_close(batch.mask(lines, i), O.mask(paths[i], Transform.identity(), rules[i], w, h))
