@@ -46,7 +46,12 @@ def parse():
     ap.add_argument("--glyphs", type=int, default=10000)
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="bounded CPU baseline sample")
     ap.add_argument("--no-per-path", action="store_true")
-    ap.add_argument("--no-configs", action="store_true", help="skip the C1/C2/C4 legs")
+    ap.add_argument("--no-configs", action="store_true", help="skip the C1/C2/C4/C5 legs")
+    ap.add_argument("--workload", default="glyphs", choices=["glyphs", "small_path", "large_path", "scene", "diff"],
+                    help="glyphs: the headline line; the others run one configuration leg alone")
+    ap.add_argument("--diff-images", type=int, default=64, help="images of the diff workload")
+    ap.add_argument("--fd-coords", type=int, default=100, help="finite-difference coordinates of the diff workload")
+    ap.add_argument("--scene-fills", type=int, default=2000, help="fills of the scene workload")
     return ap.parse_args()
 
 
@@ -234,12 +239,16 @@ def run_configs(R, stream):
     """The other single-GPU configurations, each through the public API with
     host buffers (the ``gpu`` timing) and a CPU-baseline leg that times the
     oracle on the same input once and reports the GPU's error against it."""
+    return {"C1_small_path": run_small(R, stream), "C2_large_path": run_large(R, stream),
+            "C4_scene": run_scene(R, stream), "C5_diff": run_diff(R, stream)}
+
+
+def run_small(R, stream):
+    """C1: one closed path of 200 cubics in [0,512]^2, NonZero, 512x512 f64 mask."""
     import numpy as np
     from oracle import oracle as O
     from rasterize_gb300 import FillRule, Transform
     from rasterize_gb300 import workloads as W
-    out = {}
-    # C1: one closed path of 200 cubics in [0,512]^2, NonZero, 512x512 f64 mask
     path, _, _ = W.small_path(seed=0, n_cubics=200, size=512)
     img = np.zeros((512, 512))
 
@@ -251,10 +260,17 @@ def run_configs(R, stream):
     t = time.perf_counter()
     ref = O.mask(path, Transform.identity(), FillRule.NonZero, 512, 512)
     cpu_s = time.perf_counter() - t
-    out["C1_small_path"] = {"ms": round(ms, 4), "mpx_per_s": round(512 * 512 / ms / 1e3, 1),
-                            "segments_per_s": round(200 / ms * 1e3, 1), "err": _config_err(img, ref),
-                            "cpu_baseline_ms": round(cpu_s * 1e3, 3), "cores": 1}
-    # C2: 20,000 mixed segments in [0,4096]^2 (10 % arcs, 1 % degenerate cubics), EvenOdd, 4096^2
+    return {"ms": round(ms, 4), "mpx_per_s": round(512 * 512 / ms / 1e3, 1),
+            "segments_per_s": round(200 / ms * 1e3, 1), "err": _config_err(img, ref),
+            "cpu_baseline_ms": round(cpu_s * 1e3, 3), "cores": 1}
+
+
+def run_large(R, stream):
+    """C2: 20,000 mixed segments in [0,4096]^2 (10 % arcs, 1 % degenerate cubics), EvenOdd, 4096^2."""
+    import numpy as np
+    from oracle import oracle as O
+    from rasterize_gb300 import Transform
+    from rasterize_gb300 import workloads as W
     path, rule, _ = W.large_path(seed=1, n_segments=20000, size=4096)
     img = np.zeros((4096, 4096))
 
@@ -266,30 +282,32 @@ def run_configs(R, stream):
     t = time.perf_counter()
     ref = O.mask(path, Transform.identity(), rule, 4096, 4096)
     cpu_s = time.perf_counter() - t
-    out["C2_large_path"] = {"ms": round(ms, 3), "mpx_per_s": round(4096 * 4096 / ms / 1e3, 1),
-                            "segments_per_s": round(20000 / ms * 1e3, 1), "err": _config_err(img, ref),
-                            "cpu_baseline_ms": round(cpu_s * 1e3, 1), "cores": 1,
-                            "note": "host f64 image in and out; the time includes the 128 MiB copies"}
-    # C4: 2000 filled paths, affine transforms, 50 % solid / 25 % linear / 25 % radial, 2048^2 RGBA f32
-    sc = W.scene(seed=3, n=2000, size=2048)
+    return {"ms": round(ms, 3), "mpx_per_s": round(4096 * 4096 / ms / 1e3, 1),
+            "segments_per_s": round(20000 / ms * 1e3, 1), "err": _config_err(img, ref),
+            "cpu_baseline_ms": round(cpu_s * 1e3, 1), "cores": 1,
+            "note": "host f64 image in and out; the time includes the 128 MiB copies"}
+
+
+def run_scene(R, stream, n=2000, size=2048):
+    """C4: 2000 filled paths, affine transforms, 50 % solid / 25 % linear / 25 % radial, 2048^2 RGBA f32."""
+    from rasterize_gb300 import workloads as W
+    sc = W.scene(seed=3, n=n, size=size)
     canvas = {}
 
     def c4():
-        canvas["c"] = R.render_scene(sc, 2048, 2048, bg=(0.0, 0.0, 0.0, 1.0))
+        canvas["c"] = R.render_scene(sc, size, size, bg=(0.0, 0.0, 0.0, 1.0))
     c4()
     ms = _event_ms(stream, c4, 5)
     paths_ = [f[0] for f in sc.fills]
     t = time.perf_counter()
     from tests.paint_oracle import oracle_scene
-    ref = oracle_scene(sc, 2048, 2048, bg=(0.0, 0.0, 0.0, 1.0))
+    ref = oracle_scene(sc, size, size, bg=(0.0, 0.0, 0.0, 1.0))
     cpu_s = time.perf_counter() - t
     nseg = sum(p.n_segments for p in paths_)
-    out["C4_scene"] = {"ms": round(ms, 3), "mpx_per_s": round(2048 * 2048 / ms / 1e3, 1),
-                       "segments_per_s": round(nseg / ms * 1e3, 1), "err": _config_err(canvas["c"], ref),
-                       "cpu_baseline_ms": round(cpu_s * 1e3, 1), "cores": 1,
-                       "note": "error per colour channel; host canvas in and out"}
-    out["C5_diff"] = run_diff(R, stream)
-    return out
+    return {"ms": round(ms, 3), "mpx_per_s": round(size * size / ms / 1e3, 1),
+            "segments_per_s": round(nseg / ms * 1e3, 1), "err": _config_err(canvas["c"], ref),
+            "cpu_baseline_ms": round(cpu_s * 1e3, 1), "cores": 1,
+            "note": "error per colour channel; host canvas in and out"}
 
 
 def run_diff(R, stream, n_images=64, paths=256, segs=32, size=1024, fd_coords=100):
@@ -350,7 +368,7 @@ def run_diff(R, stream, n_images=64, paths=256, segs=32, size=1024, fd_coords=10
         fd = (loss0(cp) - loss0(cm)) / hsum
         an = float(g[0, p, j, k])
         rel.append(abs(an - fd) / max(abs(fd), 1e-2))
-    rel = np.array(rel)
+    rel = np.array(rel) if rel else np.zeros(1)
     # CPU-baseline leg: the binary64 forward + adjoint of image 0 (timed), and the GPU gradient's error against it
     t = time.perf_counter()
     A = O.diff_forward(ctrl[0].astype(np.float64), paths, segs, size, size)
@@ -418,6 +436,18 @@ def main():
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.workload != "glyphs":
+        from rasterize_gb300 import GpuRasterizer
+        R = GpuRasterizer(device=local)
+        stream = torch.cuda.Stream(dev)
+        torch.cuda.set_stream(stream)
+        R.ctx.set_stream(stream.cuda_stream)
+        leg = {"small_path": lambda: run_small(R, stream), "large_path": lambda: run_large(R, stream),
+               "scene": lambda: run_scene(R, stream, n=args.scene_fills),
+               "diff": lambda: run_diff(R, stream, n_images=args.diff_images, fd_coords=args.fd_coords)}[args.workload]()
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "workload": args.workload, "n_gpus": world, **leg}))
+        return
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)

@@ -1356,7 +1356,7 @@ rz_status mask_pipeline(rz_ctx* ctx, const rz_path* path, const double tr[6], in
                                         path->n_subpaths, psub, 1, hs, fsub);
     if (st) return st;
     hs.band_rows = choose_band_rows((int)width, (int)height, false);
-    hs.task_depth = 2;  // a path this large has long segments
+    hs.task_depth = 4;  // a path this large has long segments: 16 subtree tasks each
     rzhost::Xf t;
     std::memcpy(t.m, tr, sizeof(t.m));
     add_fill(hs, fsub[0], fsub[1], 0, 0, (int)width, (int)height, (int)width - 1, t, rule, -1);

@@ -533,6 +533,7 @@ struct AlphaEpi {  // coverage-only fills write the mask
 // smem: coverage band (band_rows x cov_stride words) | RGBA band (band_rows x canvas_w float4)
 __global__ void __launch_bounds__(kCompThreads) k_composite(SceneDev S, int cov_stride) {
     extern __shared__ float4 sm4[];
+    __shared__ PaintDev s_paint;
     float* cov = reinterpret_cast<float*>(sm4);
     const bool paint_mode = S.paints != nullptr;
     float4* rgba = reinterpret_cast<float4*>(cov + S.band_rows * cov_stride);
@@ -568,7 +569,13 @@ __global__ void __launch_bounds__(kCompThreads) k_composite(SceneDev S, int cov_
         B.img_h = f.height;
         B.width_f = (float)f.clip_width;
         B.width_i = f.clip_width;
-        __syncthreads();  // previous fill done with the band
+        __syncthreads();  // previous fill done with the band (and its paint record)
+        if (paint_mode) {
+            // the fill's paint record in shared memory: read by every covered pixel
+            const uint32_t* src = reinterpret_cast<const uint32_t*>(S.paints + f.paint);
+            uint32_t* dst = reinterpret_cast<uint32_t*>(&s_paint);
+            for (int i = threadIdx.x; i < (int)(sizeof(PaintDev) / 4); i += kCompThreads) dst[i] = src[i];
+        }
         const int n4 = (rows * B.stride) >> 2;
         for (int i = threadIdx.x; i < n4; i += kCompThreads) sm4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         __syncthreads();
@@ -580,7 +587,7 @@ __global__ void __launch_bounds__(kCompThreads) k_composite(SceneDev S, int cov_
         }
         __syncthreads();
         if (paint_mode) {
-            BlendEpi epi{rgba, S.canvas_w, f.col0, B.y0, f.width, S.paints + f.paint};
+            BlendEpi epi{rgba, S.canvas_w, f.col0, B.y0, f.width, &s_paint};
             band_scan<kCompThreads>(B, f.width, f.rule, epi);
         } else {
             AlphaEpi epi{S.canvas, S.canvas_stride, row_base, f.col0, f.width};
