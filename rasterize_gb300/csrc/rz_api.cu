@@ -1552,11 +1552,12 @@ rz_status diff_check(rz_ctx* ctx, const rz_diff_batch* b, double flatness) {
 }
 
 // Band height: the largest of 8, 4, 2, 1 rows that divides the image height
-// and keeps the backward kernel's shared memory within 72 KiB (3 CTAs per SM).
-int diff_band_rows(int width, int height) {
+// and keeps the kernel's shared memory within 72 KiB (3 CTAs per SM).  Each
+// call bins its own lines, so the forward and the adjoint choose separately.
+int diff_band_rows(int width, int height, bool backward) {
     for (int r = 8; r > 1; r >>= 1) {
         int cs = 0;
-        if (height % r == 0 && rz::diff_smem_bytes(width, r, true, &cs) <= 72 * 1024) return r;
+        if (height % r == 0 && rz::diff_smem_bytes(width, r, backward, &cs) <= 72 * 1024) return r;
     }
     return 1;
 }
@@ -1581,7 +1582,7 @@ rz_status diff_prepare(rz_ctx* ctx, const rz_diff_batch* b, double flatness, rz:
     hs.n_seg = n_seg;
     hs.n_sub = n_paths;
     const int W = (int)b->width, H = (int)b->height;
-    hs.band_rows = diff_band_rows(W, H);
+    hs.band_rows = diff_band_rows(W, H, backward);
     hs.task_depth = 2;  // cubics spanning the canvas: hundreds of leaves each
     const rzhost::Xf id{{1, 0, 0, 0, 1, 0}};
     for (uint32_t p = 0; p < n_paths; ++p)

@@ -135,7 +135,7 @@ __device__ void diff_scan_blend(const Band& B, int width, int rule, float alpha,
     }
 }
 
-__global__ void __launch_bounds__(kDiffThreads) k_diff_forward(DiffDev D, int cov_stride) {
+__global__ void __launch_bounds__(kDiffThreads, 4) k_diff_forward(DiffDev D, int cov_stride) {
     extern __shared__ float4 sm4[];
     float* cov = reinterpret_cast<float*>(sm4);
     const SceneDev& S = D.S;
@@ -373,7 +373,8 @@ __device__ void diff_scan_grad(const Band& B, int width, int rule, float alpha, 
     }
 }
 
-__global__ void __launch_bounds__(kDiffThreads) k_diff_backward(DiffDev D, int cov_stride) {
+// 3 CTAs per SM (<= 85 registers): the kernel is latency-bound, resident warps hide it
+__global__ void __launch_bounds__(kDiffThreads, 3) k_diff_backward(DiffDev D, int cov_stride) {
     extern __shared__ float4 sm4[];
     float* cov = reinterpret_cast<float*>(sm4);
     const SceneDev& S = D.S;
