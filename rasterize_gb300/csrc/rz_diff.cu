@@ -191,12 +191,88 @@ __device__ __forceinline__ Dual dlerp(const Dual& a, const Dual& b, const Dual& 
     return dadd(a, dmul(t, dsub(b, a)));
 }
 
-// Mean of W_r over [lo, hi] (x relative to column c0) and its derivatives;
-// P: exclusive row prefix of g (W + 1 entries), so G[k] = P[W] - P[k].
-__device__ void diff_row_mean(const float* P, const float* g, int W, int c0, float lo, float hi, float& I, float& dlo,
+// The adjoint's per-row data is sparse.  A pixel's winding is fractional only
+// where a line of the path crosses it, and those pixels are among the
+// accumulation words the lines write.  Every other pixel has an integer
+// winding, so its dalpha/dw is 0.  `bits` marks a superset of the written
+// words.  After diff_sparse_rows, each marked word of the band holds g there
+// (as float bits) and P the inclusive prefix of g along the row; tot[r] is the
+// row's sum.
+struct CellView {
+    const uint32_t* bits;  // rows x wpr
+    const float* g;        // rows x stride (the band)
+    const float* P;        // rows x stride
+    const float* tot;      // rows
+    int wpr, stride, W;
+    // g[k] and G[k+1] = sum of g over the pixels after k, row r
+    __device__ __forceinline__ void at(int r, int k, float& gk, float& Gk1) const {
+        const uint32_t* brow = bits + r * wpr;
+        const int o = r * stride;
+        if ((brow[k >> 5] >> (k & 31)) & 1u) {
+            gk = g[o + k];
+            Gk1 = tot[r] - P[o + k];
+            return;
+        }
+        gk = 0.f;  // an unmarked pixel: integer winding, no slope; G from the next marked one
+        Gk1 = 0.f;
+        int w = (k + 1) >> 5;
+        uint32_t word = w < wpr ? brow[w] & (0xffffffffu << ((k + 1) & 31)) : 0u;
+        while (!word && ++w < wpr) word = brow[w];
+        if (word) {
+            const int m = (w << 5) + __ffs(word) - 1;
+            if (m < W) Gk1 = tot[r] - P[o + m] + g[o + m];
+        }
+    }
+};
+
+// Marks a superset of the accumulation words that accumulate_vtx writes for
+// the line a -> b: in every band row the line reaches (rows widened by 0.01),
+// its x range there clamped to [0, width] like the x rules, one word more on
+// each side and the carry word after it.
+__device__ void diff_mark(const Band& B, const VtxQ& a, const VtxQ& b, uint32_t* bits, int wpr) {
+    const float ax = (float)a.col + a.fx, bx = (float)b.col + b.fx;
+    const float ay = (float)a.row + a.fy, by = (float)b.row + b.fy;
+    if (ay == by) return;  // no signed height
+    const float ylo = fminf(ay, by), yhi = fmaxf(ay, by);
+    const int r0 = max((int)floorf(ylo - 0.01f), 0), r1 = min((int)floorf(yhi + 0.01f), B.bh - 1);
+    const float inv = 1.f / (by - ay), dx = bx - ax;
+    const int cmax = B.width_i + 2;
+    for (int r = r0; r <= r1; ++r) {
+        const float t0 = fminf(fmaxf(((float)r - 0.01f - ay) * inv, 0.f), 1.f);
+        const float t1 = fminf(fmaxf(((float)r + 1.01f - ay) * inv, 0.f), 1.f);
+        const float x0 = fmaf(t0, dx, ax), x1 = fmaf(t1, dx, ax);
+        const float xl = fminf(fmaxf(fminf(x0, x1), 0.f), B.width_f);
+        const float xh = fminf(fmaxf(fmaxf(x0, x1), 0.f), B.width_f);
+        const int c0 = max((int)floorf(xl) - 1, 0), c1 = min((int)floorf(xh) + 2, cmax);
+        uint32_t* row = bits + r * wpr;
+        for (int w = c0 >> 5; w <= (c1 >> 5); ++w) {
+            const int lo = max(c0 - (w << 5), 0), hi = min(c1 - (w << 5), 31);
+            const uint32_t upto = hi == 31 ? 0xffffffffu : ((1u << (hi + 1)) - 1u);
+            atomicOr(&row[w], upto & ~((1u << lo) - 1u));
+        }
+    }
+}
+
+// diff_accumulate, marking the words it writes.
+__device__ void diff_accumulate_marked(const DiffDev& D, uint32_t e, const Band& B, uint32_t* bits, int wpr) {
+    const SceneDev& S = D.S;
+    __syncthreads();
+    const uint32_t n = S.entry_count[e], start = S.entry_start[e];
+    for (uint32_t j = threadIdx.x; j < n; j += kDiffThreads) {
+        const uint32_t l = S.pairs[start + j];
+        const VtxQ a = line_vtx(S.lines[2ull * l], B.y0), b = line_vtx(S.lines[2ull * l + 1], B.y0);
+        accumulate_vtx(B, a, b);
+        diff_mark(B, a, b, bits, wpr);
+    }
+    __syncthreads();
+}
+
+// Mean of W_r over [lo, hi] (x relative to column c0) and its derivatives,
+// W_r(X) = G[k+1] + (k + 1 - X) g[k] on [k, k+1).
+__device__ void diff_row_mean(const CellView& V, int r, int c0, float lo, float hi, float& I, float& dlo,
                               float& dhi) {
+    const int W = V.W;
     const float wmax = (float)(W - c0), wmin = (float)(-c0);
-    const float total = P[W];
     lo = fminf(fmaxf(lo, wmin), wmax);
     hi = fminf(fmaxf(hi, lo), wmax);
     const float D = hi - lo;
@@ -204,8 +280,10 @@ __device__ void diff_row_mean(const float* P, const float* g, int W, int c0, flo
         int k = (int)floorf(lo);
         k = min(max(k + c0, 0), W - 1);
         const float kr = (float)(k - c0);
-        I = (total - P[k + 1]) + (kr + 1.f - lo) * g[k];
-        dlo = dhi = -0.5f * g[k];
+        float gk, Gk1;
+        V.at(r, k, gk, Gk1);
+        I = Gk1 + (kr + 1.f - lo) * gk;
+        dlo = dhi = -0.5f * gk;
         return;
     }
     const int k0 = (int)floorf(lo), k1 = min((int)floorf(hi), W - 1 - c0);
@@ -213,10 +291,10 @@ __device__ void diff_row_mean(const float* P, const float* g, int W, int c0, flo
     for (int k = k0; k <= k1; ++k) {
         const float a = fmaxf(lo, (float)k), b = fminf(hi, (float)(k + 1));
         if (b <= a) continue;
-        const int kk = k + c0;
-        const float gk = g[kk];
+        float gk, Gk1;
+        V.at(r, k + c0, gk, Gk1);
         const float ka = (float)(k + 1) - a, kb = (float)(k + 1) - b;
-        sI += (total - P[kk + 1]) * (b - a) + gk * 0.5f * (ka * ka - kb * kb);
+        sI += Gk1 * (b - a) + gk * 0.5f * (ka * ka - kb * kb);
         shi -= gk * 0.5f * ((b - lo) * (b - lo) - (a - lo) * (a - lo));
         slo -= gk * 0.5f * ((hi - a) * (hi - a) - (hi - b) * (hi - b));
     }
@@ -228,15 +306,13 @@ __device__ void diff_row_mean(const float* P, const float* g, int W, int c0, flo
 
 // d(sum over the band's pixels of g * winding contribution of the piece p -> q)/d(line ends);
 // x relative to column c0, y relative to band row 0.
-__device__ void diff_piece(Dual px, Dual py, Dual qx, Dual qy, int rows, int W, int c0, const float* G, const float* g,
-                           float (&out)[4]) {
-    const int Gs = W + 1;  // G: the exclusive prefix P of the band, W + 1 entries per row
+__device__ void diff_piece(Dual px, Dual py, Dual qx, Dual qy, int rows, int c0, const CellView& V, float (&out)[4]) {
     if (py.v == qy.v) {
         // horizontal: no coverage, but moving an end vertically brings coverage in
         const int r = (int)floorf(py.v);
         if (r < 0 || r >= rows) return;
         float I, dlo, dhi;
-        diff_row_mean(G + r * Gs, g + r * W, W, c0, fminf(px.v, qx.v), fmaxf(px.v, qx.v), I, dlo, dhi);
+        diff_row_mean(V, r, c0, fminf(px.v, qx.v), fmaxf(px.v, qx.v), I, dlo, dhi);
         #pragma unroll
         for (int k = 0; k < 4; ++k) out[k] += I * (qy.d[k] - py.d[k]);
         return;
@@ -261,18 +337,18 @@ __device__ void diff_piece(Dual px, Dual py, Dual qx, Dual qy, int rows, int W, 
         const Dual& lo = ord ? xa : xn;
         const Dual& hi = ord ? xn : xa;
         float I, dlo, dhi;
-        diff_row_mean(G + r * Gs, g + r * W, W, c0, lo.v, hi.v, I, dlo, dhi);
+        diff_row_mean(V, r, c0, lo.v, hi.v, I, dlo, dhi);
         #pragma unroll
         for (int k = 0; k < 4; ++k) out[k] += dir * (I * h.d[k] + h.v * (dlo * lo.d[k] + dhi * hi.d[k]));
     }
 }
 
 // The reference's x rules on dual numbers (width = W, relative to column c0), then the pieces.
-__device__ void diff_line(float ax, float ay, float bx, float by, int rows, int W, int c0, const float* G,
-                          const float* g, float (&out)[4]) {
+__device__ void diff_line(float ax, float ay, float bx, float by, int rows, int c0, const CellView& V,
+                          float (&out)[4]) {
     Dual x0{ax, {1.f, 0.f, 0.f, 0.f}}, y0{ay, {0.f, 1.f, 0.f, 0.f}};
     Dual x1{bx, {0.f, 0.f, 1.f, 0.f}}, y1{by, {0.f, 0.f, 0.f, 1.f}};
-    const float width = (float)(W - c0), zero = (float)(-c0);
+    const float width = (float)(V.W - c0), zero = (float)(-c0);
     if (x0.v > width || x1.v > width) {
         if (x0.v > width && x1.v > width) {
             x0 = dconst(width - 0.001f);
@@ -285,112 +361,120 @@ __device__ void diff_line(float ax, float ay, float bx, float by, int rows, int 
         }
     }
     if (x0.v >= zero && x1.v >= zero) {
-        diff_piece(x0, y0, x1, y1, rows, W, c0, G, g, out);
+        diff_piece(x0, y0, x1, y1, rows, c0, V, out);
     } else if (x0.v <= zero && x1.v <= zero) {
-        diff_piece(dconst(zero), y0, dconst(zero), y1, rows, W, c0, G, g, out);
+        diff_piece(dconst(zero), y0, dconst(zero), y1, rows, c0, V, out);
     } else {
         const Dual t = ddiv(dsub(x0, dconst(zero)), dsub(x0, x1));
         const Dual mx = dlerp(x0, x1, t), my = dlerp(y0, y1, t);
         if (x0.v < zero) {
-            diff_piece(mx, my, x1, y1, rows, W, c0, G, g, out);
-            diff_piece(dconst(zero), y0, mx, my, rows, W, c0, G, g, out);
+            diff_piece(mx, my, x1, y1, rows, c0, V, out);
+            diff_piece(dconst(zero), y0, mx, my, rows, c0, V, out);
         } else {
-            diff_piece(x0, y0, mx, my, rows, W, c0, G, g, out);
-            diff_piece(mx, my, dconst(zero), y1, rows, W, c0, G, g, out);
+            diff_piece(x0, y0, mx, my, rows, c0, V, out);
+            diff_piece(mx, my, dconst(zero), y1, rows, c0, V, out);
         }
     }
 }
 
-// Row prefix of the band (clearing it as it reads), then per pixel
-// g = c / (1 - a alpha) * dalpha/dw with c = dL/dA * a (1 - A) staged per band,
-// and the exclusive row prefix P of g (P[W] = the row total).
-__device__ void diff_scan_grad(const Band& B, int width, int rule, float alpha, const float* c, float* g, float* P) {
+// Sparse row pass, one warp per row, over the marked words in increasing
+// order (32 at a time, skipping empty bitmask words): the exact integer
+// windings there (the prefix of the marked words; the others are 0),
+// g = dL/dA * a (1 - A) / (1 - a alpha) * dalpha/dw, and the inclusive prefix
+// P of g.  g overwrites the coverage word, P goes to its own array.
+__device__ void diff_sparse_rows(const DiffDev& D, const Band& B, int row_base, const uint32_t* bits, float* cov,
+                                 float* P, float* tot) {
     const int lane = threadIdx.x & 31;
+    const int wpr = (B.stride + 31) >> 5, W = D.width;
     for (int r = threadIdx.x >> 5; r < B.bh; r += kDiffThreads / 32) {
-        int4* row4 = reinterpret_cast<int4*>(B.acc + r * B.stride);
-        const float* cr = c + r * width;
-        float* gr = g + r * width;
-        float* Pr = P + r * (width + 1);
-        uint32_t carry = 0;
+        const uint32_t* brow = bits + r * wpr;
+        int32_t* crow = reinterpret_cast<int32_t*>(cov + r * B.stride);
+        float* prow = P + r * B.stride;
+        const float* Arow = D.image + (uint64_t)(row_base + r) * W;
+        const float* dlrow = D.dl_dimage + (uint64_t)(row_base + r) * W;
+        uint32_t wcarry = 0;
         float gcarry = 0.f;
-        for (int x0 = 0; x0 < width; x0 += 128) {
-            const int x = x0 + 4 * lane;
-            int4 v = make_int4(0, 0, 0, 0);
-            if (x < width) {
-                v = row4[x >> 2];
-                row4[x >> 2] = make_int4(0, 0, 0, 0);
-            }
-            const uint32_t a0 = (uint32_t)v.x;
-            const uint32_t a1 = a0 + (x + 1 < width ? (uint32_t)v.y : 0u);
-            const uint32_t a2 = a1 + (x + 2 < width ? (uint32_t)v.z : 0u);
-            const uint32_t a3 = a2 + (x + 3 < width ? (uint32_t)v.w : 0u);
-            uint32_t incl = a3;
-            #pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                const uint32_t o = __shfl_up_sync(0xffffffffu, incl, off);
-                if (lane >= off) incl += o;
-            }
-            const uint32_t base = carry + incl - a3;
-            carry += __shfl_sync(0xffffffffu, incl, 31);
-            const uint32_t wv[4] = {base + a0, base + a1, base + a2, base + a3};
-            float gv[4];
-            #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                gv[i] = 0.f;
-                if (x + i >= width) continue;
-                const int32_t w = (int32_t)wv[i];
-                const float al = alpha_from_winding_fix(rule, w);
-                if (al < 1e-6f) continue;  // skipped by the forward: no blend, no slope
-                float da = 0.f;
-                if (rule == 1) {
-                    // EvenOdd: |((w + 1) mod 2) - 1|, slope = sign of the folded value
-                    const int32_t fo = (int32_t)(((uint32_t)w + (1u << 22)) & ((1u << 23) - 1u)) - (1 << 22);
-                    da = fo > 0 ? 1.f : -1.f;
-                } else if (al < 1.f) {
-                    da = w > 0 ? 1.f : -1.f;
+        for (int w0 = 0; w0 < wpr; w0 += 32) {
+            const uint32_t mine = w0 + lane < wpr ? brow[w0 + lane] : 0u;
+            uint32_t nz = __ballot_sync(0xffffffffu, mine != 0u);
+            while (nz) {
+                const int j = __ffs(nz) - 1;
+                nz &= nz - 1u;
+                const uint32_t word = __shfl_sync(0xffffffffu, mine, j);
+                const int x = ((w0 + j) << 5) + lane;
+                const bool set = (word >> lane) & 1u;
+                const uint32_t d = set ? (uint32_t)crow[x] : 0u;
+                uint32_t wi = d;
+                #pragma unroll
+                for (int off = 1; off < 32; off <<= 1) {
+                    const uint32_t o = __shfl_up_sync(0xffffffffu, wi, off);
+                    if (lane >= off) wi += o;
                 }
-                if (da != 0.f) gv[i] = cr[x + i] / (1.f - alpha * al) * da;
+                const int32_t wn = (int32_t)(wcarry + wi);  // winding at pixel x
+                wcarry += __shfl_sync(0xffffffffu, wi, 31);
+                float gv = 0.f;
+                if (set && x < W) {
+                    const float al = alpha_from_winding_fix(D.rule, wn);
+                    if (al >= 1e-6f) {  // pixels the forward skips have no slope
+                        float da = 0.f;
+                        if (D.rule == 1) {
+                            const int32_t fo = (int32_t)(((uint32_t)wn + (1u << 22)) & ((1u << 23) - 1u)) - (1 << 22);
+                            da = fo > 0 ? 1.f : -1.f;
+                        } else if (al < 1.f) {
+                            da = wn > 0 ? 1.f : -1.f;
+                        }
+                        if (da != 0.f) gv = dlrow[x] * D.alpha * (1.f - Arow[x]) / (1.f - D.alpha * al) * da;
+                    }
+                }
+                float gi = gv;
+                #pragma unroll
+                for (int off = 1; off < 32; off <<= 1) {
+                    const float o = __shfl_up_sync(0xffffffffu, gi, off);
+                    if (lane >= off) gi += o;
+                }
+                if (set) {
+                    crow[x] = __float_as_int(gv);
+                    prow[x] = gcarry + gi;
+                }
+                gcarry += __shfl_sync(0xffffffffu, gi, 31);
             }
-            const float s0 = gv[0], s1 = s0 + gv[1], s2 = s1 + gv[2], s3 = s2 + gv[3];
-            float ginc = s3;
-            #pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                const float o = __shfl_up_sync(0xffffffffu, ginc, off);
-                if (lane >= off) ginc += o;
-            }
-            const float gbase = gcarry + ginc - s3;
-            gcarry += __shfl_sync(0xffffffffu, ginc, 31);
-            if (x < width) {
-                gr[x] = gv[0];
-                Pr[x] = gbase;
-            }
-            if (x + 1 < width) { gr[x + 1] = gv[1]; Pr[x + 1] = gbase + s0; }
-            if (x + 2 < width) { gr[x + 2] = gv[2]; Pr[x + 2] = gbase + s1; }
-            if (x + 3 < width) { gr[x + 3] = gv[3]; Pr[x + 3] = gbase + s2; }
         }
-        if (lane == 0) Pr[width] = gcarry;
-        clear_row_tail(row4, width, B.stride, lane);
+        if (lane == 0) tot[r] = gcarry;
+    }
+}
+
+// Clears the marked words of the band and the bitmask.
+__device__ void diff_sparse_clear(const Band& B, uint32_t* bits, float* cov) {
+    const int wpr = (B.stride + 31) >> 5;
+    for (int i = threadIdx.x; i < B.bh * wpr; i += kDiffThreads) {
+        uint32_t word = bits[i];
+        if (!word) continue;
+        bits[i] = 0u;
+        const int r = i / wpr, x0 = (i - r * wpr) << 5;
+        float* row = cov + r * B.stride + x0;
+        while (word) {
+            row[__ffs(word) - 1] = 0.f;
+            word &= word - 1u;
+        }
     }
 }
 
 // 3 CTAs per SM (<= 85 registers): the kernel is latency-bound, resident warps hide it
 __global__ void __launch_bounds__(kDiffThreads, 3) k_diff_backward(DiffDev D, int cov_stride) {
     extern __shared__ float4 sm4[];
-    float* cov = reinterpret_cast<float*>(sm4);
     const SceneDev& S = D.S;
     const int rows = S.band_rows;
-    const int W = D.width;
-    float* c = cov + rows * cov_stride;  // dL/dA * a (1 - A) of the band
-    float* g = c + rows * W;
-    float* G = g + rows * W;             // exclusive row prefix of g, W + 1 per row
+    const int wpr = (cov_stride + 31) >> 5;
+    float* cov = reinterpret_cast<float*>(sm4);  // coverage words, then g
+    float* P = cov + rows * cov_stride;
+    float* tot = P + rows * cov_stride;
+    uint32_t* bits = reinterpret_cast<uint32_t*>(tot + 8);
     const int band = blockIdx.x;
     const int row_base = band * rows;
     const int img = row_base / D.height;
-    const float* A = D.image + (uint64_t)row_base * W;
-    const float* dl = D.dl_dimage + (uint64_t)row_base * W;
     float2* out = reinterpret_cast<float2*>(D.out);
-    for (int i = threadIdx.x; i < rows * W; i += kDiffThreads) c[i] = dl[i] * D.alpha * (1.f - A[i]);
-    for (int i = threadIdx.x; i < (rows * cov_stride) >> 2; i += kDiffThreads) sm4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int i = threadIdx.x; i < rows * cov_stride; i += kDiffThreads) cov[i] = 0.f;
+    for (int i = threadIdx.x; i < rows * wpr; i += kDiffThreads) bits[i] = 0u;
     for (int p = 0; p < D.paths; ++p) {
         const uint32_t fi = (uint32_t)(img * D.paths + p);
         const FillDev& f = S.fills[fi];
@@ -398,9 +482,10 @@ __global__ void __launch_bounds__(kDiffThreads, 3) k_diff_backward(DiffDev D, in
         const uint32_t n = S.entry_count[e];
         if (n == 0) continue;  // no line in the band: zero coverage and no line to move
         const Band B = diff_band(D, f, cov, row_base, rows);
-        diff_accumulate(D, e, B);  // also waits for the previous path's line pass
-        diff_scan_grad(B, W, D.rule, D.alpha, c, g, G);
+        diff_accumulate_marked(D, e, B, bits, wpr);  // also waits for the previous path's clear
+        diff_sparse_rows(D, B, row_base, bits, cov, P, tot);
         __syncthreads();
+        const CellView V{bits, cov, P, tot, wpr, cov_stride, D.width};
         const uint32_t start = S.entry_start[e];
         for (uint32_t j = threadIdx.x; j < n; j += kDiffThreads) {
             const uint32_t l = S.pairs[start + j];
@@ -409,8 +494,7 @@ __global__ void __launch_bounds__(kDiffThreads, 3) k_diff_backward(DiffDev D, in
             const VtxQ a = line_vtx(S.lines[2ull * l], B.y0), b = line_vtx(S.lines[2ull * l + 1], B.y0);
             const int c0 = a.col;
             float d4[4] = {0.f, 0.f, 0.f, 0.f};
-            diff_line(a.fx, (float)a.row + a.fy, (float)(b.col - c0) + b.fx, (float)b.row + b.fy, rows, W, c0, G, g,
-                      d4);
+            diff_line(a.fx, (float)a.row + a.fy, (float)(b.col - c0) + b.fx, (float)b.row + b.fy, rows, c0, V, d4);
             if (d4[0] == 0.f && d4[1] == 0.f && d4[2] == 0.f && d4[3] == 0.f) continue;
             // chain to the control points: Bernstein weights at the frozen tree's parameters
             const uint32_t seg = code.x;
@@ -430,6 +514,8 @@ __global__ void __launch_bounds__(kDiffThreads, 3) k_diff_backward(DiffDev D, in
                 atomicAdd(&o[idx[q]].y, d4[1] * b0[q] + d4[3] * b1[q]);
             }
         }
+        __syncthreads();
+        diff_sparse_clear(B, bits, cov);
     }
 }
 
@@ -464,9 +550,9 @@ __global__ void k_l2_loss(const float* __restrict__ A, const float* __restrict__
 int diff_smem_bytes(int width, int band_rows, bool backward, int* cov_stride) {
     const int stride = band_stride(width);
     *cov_stride = stride;
-    // forward: coverage + A; backward: coverage + c + g + prefix (W + 1 per row)
-    return 4 * band_rows * stride + 4 * band_rows * width +
-           (backward ? 4 * band_rows * width + 4 * band_rows * (width + 1) : 0);
+    if (!backward) return 4 * band_rows * stride + 4 * band_rows * width;  // coverage + A
+    // coverage words (then g), the prefix of g, row sums, the bitmask of marked words
+    return 8 * band_rows * stride + 32 + 4 * band_rows * ((stride + 31) >> 5);
 }
 
 cudaError_t launch_diff_segments(const float* ctrl, uint32_t n_paths, int segs, uint8_t* kind, double* pts,
