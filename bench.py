@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="bounded CPU baseline sample")
     ap.add_argument("--no-per-path", action="store_true")
     ap.add_argument("--no-configs", action="store_true", help="skip the C1/C2/C4/C5 legs")
-    ap.add_argument("--workload", default="glyphs", choices=["glyphs", "small_path", "large_path", "scene", "diff"],
+    ap.add_argument("--workload", default="glyphs", choices=["glyphs", "small_path", "large_path", "scene", "diff", "encode"],
                     help="glyphs: the headline line; the others run one configuration leg alone")
     ap.add_argument("--diff-images", type=int, default=64, help="images of the diff workload")
     ap.add_argument("--fd-coords", type=int, default=100, help="finite-difference coordinates of the diff workload")
@@ -240,7 +240,7 @@ def run_configs(R, stream):
     host buffers (the ``gpu`` timing) and a CPU-baseline leg that times the
     oracle on the same input once and reports the GPU's error against it."""
     return {"C1_small_path": run_small(R, stream), "C2_large_path": run_large(R, stream),
-            "C4_scene": run_scene(R, stream), "C5_diff": run_diff(R, stream)}
+            "C4_scene": run_scene(R, stream), "C5_diff": run_diff(R, stream), "encode": run_encode(R, stream)}
 
 
 def run_small(R, stream):
@@ -304,10 +304,55 @@ def run_scene(R, stream, n=2000, size=2048):
     ref = oracle_scene(sc, size, size, bg=(0.0, 0.0, 0.0, 1.0))
     cpu_s = time.perf_counter() - t
     nseg = sum(p.n_segments for p in paths_)
+    # the same scene straight to sRGB8 bytes (encode fused into the composite)
+    import numpy as np
+    from oracle import oracle as O
+
+    def c4_rgba8():
+        canvas["b"] = R.render_scene_rgba8(sc, size, size, bg=(0.0, 0.0, 0.0, 1.0))
+    c4_rgba8()
+    ms8 = _event_ms(stream, c4_rgba8, 5)
+    lsb = np.abs(canvas["b"].astype(np.int32) - O.encode_rgba8(ref.astype(np.float32)).astype(np.int32))
     return {"ms": round(ms, 3), "mpx_per_s": round(size * size / ms / 1e3, 1),
             "segments_per_s": round(nseg / ms * 1e3, 1), "err": _config_err(canvas["c"], ref),
+            "rgba8_ms": round(ms8, 3), "rgba8_err_lsb": {"max": int(lsb.max()), "frac_off": float((lsb > 0).mean())},
             "cpu_baseline_ms": round(cpu_s * 1e3, 1), "cores": 1,
-            "note": "error per colour channel; host canvas in and out"}
+            "note": "error per colour channel; host canvas in and out; rgba8: sRGB8 bytes out, encode fused"}
+
+
+def run_encode(R, stream, size=8192):
+    """Output encode (to_rgba of every pixel): a size x size premultiplied linear
+    RGBA f32 canvas in device memory (1 GiB at 8192^2, larger than L2, so no
+    flush is needed) to sRGB8 RGBA; 20 algorithmic bytes a pixel."""
+    import numpy as np
+    import torch
+    from oracle import oracle as O
+    dev = torch.device("cuda", torch.cuda.current_device())
+    n = size * size
+    g = torch.Generator(device=dev)
+    g.manual_seed(9)
+    a = torch.rand(n, 1, generator=g, device=dev)
+    canvas = torch.cat([torch.rand(n, 3, generator=g, device=dev) * a, a], dim=1).contiguous()
+    out = torch.empty(n * 4, dtype=torch.uint8, device=dev)
+    lib = R.ctx.lib
+
+    def enc():
+        R.ctx.check(lib.rz_encode_rgba8(R.ctx.ptr, canvas.data_ptr(), n, out.data_ptr(), 1))
+    enc()
+    ms = _event_ms(stream, enc, 10)
+    sample = 1 << 20
+    c_host = canvas[:sample].cpu().numpy()
+    exact = bool((out[:4 * sample].cpu().numpy().reshape(-1, 4) == O.encode_rgba8(c_host)).all())
+    t = time.perf_counter()
+    O.encode_rgba8(c_host)
+    cpu_s = time.perf_counter() - t
+    gbs = 20.0 * n / ms / 1e6
+    peak, kind = measured_peak_hbm()
+    del canvas, out
+    return {"ms": round(ms, 4), "gpx_per_s": round(n / ms / 1e6, 2), "achieved_gbs": round(gbs, 1),
+            "roofline_frac": round(gbs / peak, 3), "peak_gbs": peak, "peak_kind": kind, "bit_exact_sample_px": sample,
+            "bit_exact": exact, "cpu_baseline_mpx_per_s": round(sample / cpu_s / 1e6, 1), "cores": 1,
+            "workload": "%dx%d RGBA f32 canvas -> sRGB8, device memory" % (size, size)}
 
 
 def run_diff(R, stream, n_images=64, paths=256, segs=32, size=1024, fd_coords=100):
@@ -444,7 +489,8 @@ def main():
         R.ctx.set_stream(stream.cuda_stream)
         leg = {"small_path": lambda: run_small(R, stream), "large_path": lambda: run_large(R, stream),
                "scene": lambda: run_scene(R, stream, n=args.scene_fills),
-               "diff": lambda: run_diff(R, stream, n_images=args.diff_images, fd_coords=args.fd_coords)}[args.workload]()
+               "diff": lambda: run_diff(R, stream, n_images=args.diff_images, fd_coords=args.fd_coords),
+               "encode": lambda: run_encode(R, stream)}[args.workload]()
         if rank == 0:
             print(json.dumps({"metric": METRIC, "workload": args.workload, "n_gpus": world, **leg}))
         return

@@ -227,6 +227,35 @@ RZ_API rz_status rz_fill(rz_ctx* ctx, const rz_path* path, const double tr[6], i
 RZ_API rz_status rz_render_scene(rz_ctx* ctx, const rz_scene* scene, double flatness, const float bg[4],
                                  float* canvas, uint32_t width, uint32_t height);
 
+/* ---- output encode: premultiplied linear RGBA f32 -> sRGB8 RGBA ---------- */
+/* Scene::render followed by `to_rgba` of every pixel (From<LinColor> for RGBA,
+ * src/color.rs:164-175), what Image::write_bmp / write_png / write_rgba store
+ * (src/image.rs:136-229).  The encode runs in the composite's epilogue, so only
+ * 4 bytes a pixel leave the GPU.  rgba8: width * height * 4 bytes, host memory. */
+RZ_API rz_status rz_render_scene_rgba8(rz_ctx* ctx, const rz_scene* scene, double flatness, const float bg[4],
+                                       uint8_t* rgba8, uint32_t width, uint32_t height);
+/* `to_rgba` of n premultiplied linear RGBA f32 pixels: unmultiply (alpha <= 1e-6
+ * gives 0), the x86 l2s fit (src/simd/x86.rs:197-214), (c * 255 + 0.5) as u8;
+ * alpha is not unmultiplied.  memory: RZ_MEM_HOST or RZ_MEM_DEVICE for both
+ * arrays (device arrays 16-byte aligned; the call is then asynchronous on the
+ * context's stream). */
+RZ_API rz_status rz_encode_rgba8(rz_ctx* ctx, const float* canvas, uint64_t n_pixels, uint8_t* rgba8,
+                                 int32_t memory);
+/* `to_rgba` of a mask (Scalar, src/color.rs:429-432): grey linear_to_srgb(1 - m),
+ * alpha 255.  elem_size 8: f64 masks (converted to f32 first, as the reference
+ * does), 4: f32. */
+RZ_API rz_status rz_encode_mask_rgba8(rz_ctx* ctx, const void* mask, int32_t elem_size, uint64_t n_pixels,
+                                      uint8_t* rgba8, int32_t memory);
+
+#define RZ_IMAGE_BMP 0  /* Image::write_bmp (src/image.rs:165-212) */
+#define RZ_IMAGE_RGBA 1 /* Image::write_rgba (src/image.rs:136-149) */
+#define RZ_IMAGE_PPM 2  /* Image::write_ppm (src/image.rs:151-163) */
+/* Host-only: the file bytes of an sRGB8 RGBA image (row major, 4 bytes a pixel)
+ * in `format`.  *len receives the size; out NULL asks for the size only, a
+ * smaller cap returns RZ_ERR_CAPACITY.  Needs no context or GPU. */
+RZ_API rz_status rz_write_image(const uint8_t* rgba8, uint32_t width, uint32_t height, int32_t format,
+                                uint8_t* out, uint64_t cap, uint64_t* len);
+
 /* ---- batch plans: resident work list + CUDA graph replay ---------------- */
 /* A plan fixes one device-memory batch (batch->memory == RZ_MEM_DEVICE), its
  * output buffer and flatness.  Creating it uploads the work list (bands of

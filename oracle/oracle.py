@@ -88,6 +88,12 @@ def lib():
             for name in ("rzo_linear_to_srgb", "rzo_srgb_to_linear"):
                 getattr(L, name).restype = ctypes.c_float
                 getattr(L, name).argtypes = [ctypes.c_float]
+            L.rzo_encode_rgba8.restype = None
+            L.rzo_encode_rgba8.argtypes = [P, ctypes.c_long, P]
+            L.rzo_encode_mask_rgba8.restype = None
+            L.rzo_encode_mask_rgba8.argtypes = [P, ctypes.c_long, P]
+            L.rzo_lin_from_rgba8.restype = None
+            L.rzo_lin_from_rgba8.argtypes = [P, P]
             L.rzo_path_bbox.restype = ctypes.c_int
             L.rzo_path_bbox.argtypes = [P, P, P, ctypes.c_long, P, P]
             L.rzo_fill.restype = ctypes.c_int
@@ -386,3 +392,54 @@ def diff_backward(ctrl, n_paths, segs, width, height, image, dl_dimage, alpha=0.
     if rc < 0:
         raise OracleError("cannot flatten segment with NaN")
     return out.reshape(np.shape(ctrl))
+
+
+def encode_rgba8(canvas):
+    """From<LinColor> for RGBA of every pixel: (..., 4) f32 -> (..., 4) uint8."""
+    c = np.ascontiguousarray(canvas, dtype=np.float32)
+    out = np.zeros(c.shape, dtype=np.uint8)
+    lib().rzo_encode_rgba8(_ptr(c), c.size // 4, _ptr(out))
+    return out
+
+
+def encode_mask_rgba8(mask):
+    """Scalar::to_rgba of every mask value (f64): (...) -> (..., 4) uint8."""
+    m = np.ascontiguousarray(mask, dtype=np.float64)
+    out = np.zeros(m.shape + (4,), dtype=np.uint8)
+    lib().rzo_encode_mask_rgba8(_ptr(m), m.size, _ptr(out))
+    return out
+
+
+def lin_from_rgba8(rgba):
+    """From<RGBA> for LinColor."""
+    a = np.ascontiguousarray(rgba, dtype=np.uint8)
+    out = np.zeros(4, dtype=np.float32)
+    lib().rzo_lin_from_rgba8(_ptr(a), _ptr(out))
+    return out
+
+
+def write_bmp(rgba8):
+    """Image::write_bmp (src/image.rs:165-212) restated byte by byte."""
+    img = np.ascontiguousarray(rgba8, dtype=np.uint8)
+    h, w = img.shape[:2]
+    size = w * h * 4
+    head = b"BM" + (size + 122).to_bytes(4, "little") + bytes(4) + (122).to_bytes(4, "little")
+    dib = ((108).to_bytes(4, "little") + w.to_bytes(4, "little") + h.to_bytes(4, "little") + bytes([1, 0, 0x20, 0])
+           + bytes([3, 0, 0, 0]) + size.to_bytes(4, "little") + bytes([0x13, 0x0B, 0, 0]) * 2 + bytes(8)
+           + bytes([0xFF, 0, 0, 0]) + bytes([0, 0xFF, 0, 0]) + bytes([0, 0, 0xFF, 0]) + bytes([0, 0, 0, 0xFF])
+           + bytes([0x42, 0x47, 0x52, 0x73]) + bytes(48))
+    return head + dib + img[::-1].tobytes()
+
+
+def write_rgba(rgba8):
+    """Image::write_rgba (src/image.rs:136-149)."""
+    img = np.ascontiguousarray(rgba8, dtype=np.uint8)
+    h, w = img.shape[:2]
+    return h.to_bytes(4, "little") + w.to_bytes(4, "little") + img.tobytes()
+
+
+def write_ppm(rgba8):
+    """Image::write_ppm (src/image.rs:151-163)."""
+    img = np.ascontiguousarray(rgba8, dtype=np.uint8)
+    h, w = img.shape[:2]
+    return ("P6 %d %d 255 " % (w, h)).encode() + img[..., :3].tobytes()

@@ -845,6 +845,43 @@ void rzo_into_linear(const float* in, float* out) { col4 c; memcpy(c.v, in, 16);
 void rzo_l2s(const float* in, float* out) { col4 c; memcpy(c.v, in, 16); c = l2s_x86(c); memcpy(out, c.v, 16); }
 void rzo_s2l(const float* in, float* out) { col4 c; memcpy(c.v, in, 16); c = s2l_x86(c); memcpy(out, c.v, 16); }
 
+/* Rust `(v * 255.0 + 0.5) as u8`: saturating, truncating, NaN -> 0 (color.rs:169-172) */
+static uint8_t u8_sat(float v) {
+    float t = v * 255.0f;
+    float s = t + 0.5f;
+    if (!(s > 0.0f)) return 0;
+    if (s >= 255.0f) return 255;
+    return (uint8_t)s;
+}
+/* From<LinColor> for RGBA color.rs:164-175: l2s of the unmultiplied colour, alpha as is */
+void rzo_encode_rgba8(const float* canvas, long n, uint8_t* out) {
+    for (long i = 0; i < n; i++) {
+        col4 c;
+        memcpy(c.v, canvas + 4 * i, 16);
+        col4 u = l2s_x86(unmultiply(c));
+        out[4 * i + 0] = u8_sat(u.v[0]);
+        out[4 * i + 1] = u8_sat(u.v[1]);
+        out[4 * i + 2] = u8_sat(u.v[2]);
+        out[4 * i + 3] = u8_sat(c.v[3]);
+    }
+}
+/* Scalar::to_rgba color.rs:429-432 (f64 mask, cast to f32 first) */
+void rzo_encode_mask_rgba8(const double* mask, long n, uint8_t* out) {
+    for (long i = 0; i < n; i++) {
+        uint8_t v = u8_sat(rzo_linear_to_srgb(1.0f - (float)mask[i]));
+        out[4 * i + 0] = out[4 * i + 1] = out[4 * i + 2] = v;
+        out[4 * i + 3] = 255;
+    }
+}
+/* From<RGBA> for LinColor color.rs:394-406 */
+void rzo_lin_from_rgba8(const uint8_t* rgba, float* out) {
+    float a = (float)rgba[3] / 255.0f;
+    out[0] = rzo_srgb_to_linear((float)rgba[0] / 255.0f) * a;
+    out[1] = rzo_srgb_to_linear((float)rgba[1] / 255.0f) * a;
+    out[2] = rzo_srgb_to_linear((float)rgba[2] / 255.0f) * a;
+    out[3] = a;
+}
+
 /* ------------------------------------------------------------------------ */
 /* grad.rs -- spread, stops, linear and radial gradients                    */
 /* ------------------------------------------------------------------------ */

@@ -111,6 +111,12 @@ _SIGNATURES = {
     "rz_fill": (ctypes.c_int32, [P, ctypes.POINTER(RzPath), P, ctypes.c_int32, ctypes.c_double, P, P, RzShape]),
     "rz_render_scene": (ctypes.c_int32, [P, ctypes.POINTER(RzScene), ctypes.c_double, P, P, ctypes.c_uint32,
                                          ctypes.c_uint32]),
+    "rz_render_scene_rgba8": (ctypes.c_int32, [P, ctypes.POINTER(RzScene), ctypes.c_double, P, P, ctypes.c_uint32,
+                                               ctypes.c_uint32]),
+    "rz_encode_rgba8": (ctypes.c_int32, [P, P, ctypes.c_uint64, P, ctypes.c_int32]),
+    "rz_encode_mask_rgba8": (ctypes.c_int32, [P, P, ctypes.c_int32, ctypes.c_uint64, P, ctypes.c_int32]),
+    "rz_write_image": (ctypes.c_int32, [P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int32, P, ctypes.c_uint64,
+                                        ctypes.POINTER(ctypes.c_uint64)]),
     "rz_diff_forward": (ctypes.c_int32, [P, ctypes.POINTER(RzDiffBatch), ctypes.c_double, P]),
     "rz_l2_loss": (ctypes.c_int32, [P, P, P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double), P]),
     "rasterize_backward": (ctypes.c_int32, [P, ctypes.POINTER(RzDiffBatch), ctypes.c_double, P, P, P]),

@@ -50,6 +50,8 @@ cudaError_t launch_diff(const DiffDev& D, bool backward, int cov_stride, int sme
 cudaError_t launch_l2_loss(const float* A, const float* T, uint64_t n, double* loss, float* dl, int num_sms,
                            cudaStream_t st);
 cudaError_t scan_u32(uint32_t* data, uint64_t n, uint32_t* temp, cudaStream_t stream);
+cudaError_t launch_encode_rgba8(const float* in, uint8_t* out, uint64_t n, cudaStream_t st);
+cudaError_t launch_encode_mask_rgba8(const void* in, int elem_size, uint8_t* out, uint64_t n, cudaStream_t st);
 }  // namespace rz
 
 namespace {
@@ -112,6 +114,8 @@ struct rz_ctx {
     DevBuf p_fills, p_paints, p_slots, p_lines, p_ecount, p_estart, p_ecursor, p_pairs, p_scan, p_canvas;
     // differentiable batch
     DevBuf p_leaf, d_loss;
+    // output encode (sRGB8 RGBA) and its input staging
+    DevBuf p_rgba8, p_encode_in;
     // batch tuning (rz_tune_batch / rz_set_tuning): band height cap, resident CTAs per SM (0 = occupancy)
     int tune_rows_cap = 256;
     int tune_ctas = 0;
@@ -309,7 +313,8 @@ void rz_destroy(rz_ctx* c) {
     DevBuf* bufs[] = {&c->d_kind,   &c->d_pts,     &c->d_sub,     &c->d_psub,    &c->d_tr,      &c->d_rule,
                       &c->d_masks,  &c->d_items,   &c->d_out,     &c->d_ctrl,    &c->d_counts,  &c->p_fills,
                       &c->p_paints, &c->p_slots,   &c->p_lines,   &c->p_ecount,  &c->p_estart,  &c->p_ecursor,
-                      &c->p_pairs,  &c->p_scan,    &c->p_canvas};
+                      &c->p_pairs,  &c->p_scan,    &c->p_canvas,  &c->p_leaf,    &c->d_loss,    &c->p_rgba8,
+                      &c->p_encode_in};
     for (DevBuf* b : bufs) b->release();
     c->h_stage.release();
     c->h_out.release();
@@ -1269,7 +1274,7 @@ rz_status build_lines(rz_ctx* ctx, HostScene& hs, rz::SceneDev& S, Trace& tr, De
 // Flatten + bin + composite on the device.  canvas: device buffer (RGBA
 // pixels when paints are given, else an f32 mask), stride in pixels.
 rz_status run_pipeline(rz_ctx* ctx, HostScene& hs, double flatness, float* canvas, int64_t canvas_stride, int canvas_w,
-                       int canvas_h, const float* bg_dev, bool load_canvas) {
+                       int canvas_h, const float* bg_dev, bool load_canvas, uint32_t* rgba8 = nullptr) {
     Trace tr("pipeline");
     const bool paint_mode = !hs.paints.empty();
     rz::SceneDev S{};
@@ -1291,6 +1296,7 @@ rz_status run_pipeline(rz_ctx* ctx, HostScene& hs, double flatness, float* canva
     S.canvas_stride = canvas_stride;
     S.bg = bg_dev;
     S.load_canvas = load_canvas ? 1 : 0;
+    S.rgba8 = rgba8;
     RZ_CUDA(ctx->d_ctrl.ensure(64));
     RZ_CUDA(cudaMemsetAsync(ctx->d_ctrl.p, 0, 64, ctx->stream));
     S.err = (int32_t*)ctx->d_ctrl.p;
@@ -1343,6 +1349,26 @@ rz_status stage_scene_segments(rz_ctx* ctx, const uint8_t* kind, const double* p
         hs.n_sub = n_sub;
         fill_sub_out.assign(fill_sub, fill_sub + n_fills + 1);
     }
+    return RZ_OK;
+}
+
+// Device bytes to host memory: directly when `dst` is page-locked, else through
+// the page-locked staging buffer and a parallel host copy.  Synchronises.
+rz_status copy_out_bytes(rz_ctx* ctx, void* dst, const void* src_dev, uint64_t bytes) {
+    if (mapped_host(dst)) {
+        RZ_CUDA(cudaMemcpyAsync(dst, src_dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+        return RZ_OK;
+    }
+    RZ_CUDA(ctx->h_out.ensure(bytes));
+    RZ_CUDA(cudaMemcpyAsync(ctx->h_out.p, src_dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+    const char* src = (const char*)ctx->h_out.p;
+    const int64_t chunks = (int64_t)((bytes + (1u << 20) - 1) >> 20);
+    parallel_for(chunks, 4, [&](int64_t c0, int64_t c1) {
+        const uint64_t b0 = (uint64_t)c0 << 20, b1 = std::min<uint64_t>((uint64_t)c1 << 20, bytes);
+        std::memcpy((char*)dst + b0, src + b0, b1 - b0);
+    });
     return RZ_OK;
 }
 
@@ -1425,11 +1451,13 @@ rz_status rz_fill(rz_ctx* ctx, const rz_path* path, const double tr[6], int32_t 
     return RZ_OK;
 }
 
-rz_status rz_render_scene(rz_ctx* ctx, const rz_scene* scene, double flatness, const float bg[4], float* canvas,
-                          uint32_t width, uint32_t height) {
+// Scene::render into an RGBA f32 canvas, or (rgba8 non-null) straight into
+// sRGB8 RGBA bytes with the encode fused into the composite's epilogue.
+static rz_status render_scene_impl(rz_ctx* ctx, const rz_scene* scene, double flatness, const float bg[4],
+                                   float* canvas, uint8_t* rgba8, uint32_t width, uint32_t height) {
     if (!ctx) return RZ_ERR_INVALID;
     std::lock_guard<std::mutex> lock(ctx->mu);
-    if (!scene || !canvas || (scene->n_fills && (!scene->fill_subpath_off || !scene->fill_paint || !scene->paints)))
+    if (!scene || (!canvas && !rgba8) || (scene->n_fills && (!scene->fill_subpath_off || !scene->fill_paint || !scene->paints)))
         return fail(ctx, RZ_ERR_INVALID, "null argument");
     if (!valid_flatness(flatness)) return fail(ctx, RZ_ERR_INVALID, "flatness must be > 0 and finite");
     if (width > 16383 || height > 16383) return fail(ctx, RZ_ERR_INVALID, "canvas too large");
@@ -1510,6 +1538,16 @@ rz_status rz_render_scene(rz_ctx* ctx, const rz_scene* scene, double flatness, c
     float bgv[4] = {0.f, 0.f, 0.f, 0.f};
     if (bg) std::memcpy(bgv, bg, sizeof(bgv));
     RZ_CUDA(cudaMemcpyAsync(ctx->d_counts.p, bgv, 16, cudaMemcpyHostToDevice, ctx->stream));
+    if (rgba8) {
+        RZ_CUDA(ctx->p_rgba8.ensure(n * 4 + 16));
+        st = run_pipeline(ctx, hs, flatness, (float*)ctx->p_canvas.p, W, W, H, (const float*)ctx->d_counts.p, false,
+                          (uint32_t*)ctx->p_rgba8.p);
+        if (st) return st;
+        tr.mark("pipeline");
+        st = copy_out_bytes(ctx, rgba8, ctx->p_rgba8.p, n * 4);
+        tr.mark("copy_out");
+        return st;
+    }
     st = run_pipeline(ctx, hs, flatness, (float*)ctx->p_canvas.p, W, W, H, (const float*)ctx->d_counts.p, false);
     if (st) return st;
     tr.mark("pipeline");
@@ -1528,6 +1566,138 @@ rz_status rz_render_scene(rz_ctx* ctx, const rz_scene* scene, double flatness, c
     }
     tr.mark("copy_out");
     return RZ_OK;
+}
+
+rz_status rz_render_scene(rz_ctx* ctx, const rz_scene* scene, double flatness, const float bg[4], float* canvas,
+                          uint32_t width, uint32_t height) {
+    if (ctx && !canvas) return fail(ctx, RZ_ERR_INVALID, "null argument");
+    return render_scene_impl(ctx, scene, flatness, bg, canvas, nullptr, width, height);
+}
+
+rz_status rz_render_scene_rgba8(rz_ctx* ctx, const rz_scene* scene, double flatness, const float bg[4],
+                                uint8_t* rgba8, uint32_t width, uint32_t height) {
+    if (ctx && !rgba8) return fail(ctx, RZ_ERR_INVALID, "null argument");
+    return render_scene_impl(ctx, scene, flatness, bg, nullptr, rgba8, width, height);
+}
+
+rz_status rz_write_image(const uint8_t* rgba8, uint32_t width, uint32_t height, int32_t format, uint8_t* out,
+                         uint64_t cap, uint64_t* len) {
+    if (!len || (!rgba8 && (uint64_t)width * height)) return RZ_ERR_INVALID;
+    const uint64_t npx = (uint64_t)width * height;
+    char ppm_head[64];
+    int ppm_len = 0;
+    uint64_t need = 0;
+    switch (format) {
+        case RZ_IMAGE_BMP:
+            if (npx * 4 + 122 > 0xffffffffull) return RZ_ERR_INVALID;  // sizes are u32 in the header
+            need = 122 + npx * 4;
+            break;
+        case RZ_IMAGE_RGBA: need = 8 + npx * 4; break;
+        case RZ_IMAGE_PPM:
+            ppm_len = std::snprintf(ppm_head, sizeof(ppm_head), "P6 %u %u 255 ", width, height);
+            need = (uint64_t)ppm_len + npx * 3;
+            break;
+        default: return RZ_ERR_INVALID;
+    }
+    *len = need;
+    if (!out) return RZ_OK;
+    if (cap < need) return RZ_ERR_CAPACITY;
+    uint8_t* o = out;
+    auto u32 = [&o](uint32_t v) {
+        for (int i = 0; i < 4; ++i) *o++ = (uint8_t)(v >> (8 * i));
+    };
+    if (format == RZ_IMAGE_BMP) {
+        // Image::write_bmp (src/image.rs:165-212): file header, BITMAPV4HEADER with
+        // bit fields and the sRGB colour space, rows bottom-up, 4 bytes a pixel
+        const uint32_t data = (uint32_t)(npx * 4), off = 14 + 108;
+        *o++ = 'B';
+        *o++ = 'M';
+        u32(data + off);
+        u32(0);
+        u32(off);
+        u32(108);
+        u32(width);
+        u32(height);
+        u32(0x00200001u);  // 1 plane, 32 bits per pixel
+        u32(3);            // BI_BITFIELDS
+        u32(data);
+        u32(2835);  // 72 dpi, both directions
+        u32(2835);
+        u32(0);
+        u32(0);
+        u32(0x000000ffu);  // the four channel masks, in the reference's order
+        u32(0x0000ff00u);
+        u32(0x00ff0000u);
+        u32(0xff000000u);
+        u32(0x73524742u);  // 'sRGB'
+        std::memset(o, 0, 48);
+        o += 48;
+        for (uint32_t r = height; r-- > 0;) {
+            std::memcpy(o, rgba8 + (uint64_t)r * width * 4, (size_t)width * 4);
+            o += (size_t)width * 4;
+        }
+    } else if (format == RZ_IMAGE_RGBA) {
+        // Image::write_rgba (src/image.rs:136-149): height, width, pixels
+        u32(height);
+        u32(width);
+        std::memcpy(o, rgba8, npx * 4);
+    } else {
+        // Image::write_ppm (src/image.rs:151-163): the alpha byte is dropped
+        std::memcpy(o, ppm_head, (size_t)ppm_len);
+        o += ppm_len;
+        for (uint64_t i = 0; i < npx; ++i) {
+            *o++ = rgba8[4 * i];
+            *o++ = rgba8[4 * i + 1];
+            *o++ = rgba8[4 * i + 2];
+        }
+    }
+    return RZ_OK;
+}
+
+rz_status rz_encode_rgba8(rz_ctx* ctx, const float* canvas, uint64_t n_pixels, uint8_t* rgba8, int32_t memory) {
+    if (!ctx) return RZ_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    if (n_pixels == 0) return RZ_OK;
+    if (!canvas || !rgba8) return fail(ctx, RZ_ERR_INVALID, "null argument");
+    if (memory != RZ_MEM_HOST && memory != RZ_MEM_DEVICE) return fail(ctx, RZ_ERR_INVALID, "bad memory kind");
+    if (n_pixels > (1ull << 36)) return fail(ctx, RZ_ERR_INVALID, "too many pixels");
+    RZ_CUDA(cudaSetDevice(ctx->device));
+    if (memory == RZ_MEM_DEVICE) {
+        if (((uintptr_t)canvas & 15) || ((uintptr_t)rgba8 & 15))
+            return fail(ctx, RZ_ERR_INVALID, "device buffers must be 16-byte aligned");
+        RZ_CUDA(rz::launch_encode_rgba8(canvas, rgba8, n_pixels, ctx->stream));
+        return RZ_OK;
+    }
+    RZ_CUDA(ctx->p_encode_in.ensure(n_pixels * 16 + 16));
+    RZ_CUDA(ctx->p_rgba8.ensure(n_pixels * 4 + 16));
+    RZ_CUDA(cudaMemcpyAsync(ctx->p_encode_in.p, canvas, n_pixels * 16, cudaMemcpyHostToDevice, ctx->stream));
+    RZ_CUDA(rz::launch_encode_rgba8((const float*)ctx->p_encode_in.p, (uint8_t*)ctx->p_rgba8.p, n_pixels, ctx->stream));
+    return copy_out_bytes(ctx, rgba8, ctx->p_rgba8.p, n_pixels * 4);
+}
+
+rz_status rz_encode_mask_rgba8(rz_ctx* ctx, const void* mask, int32_t elem_size, uint64_t n_pixels, uint8_t* rgba8,
+                               int32_t memory) {
+    if (!ctx) return RZ_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    if (n_pixels == 0) return RZ_OK;
+    if (!mask || !rgba8) return fail(ctx, RZ_ERR_INVALID, "null argument");
+    if (elem_size != 4 && elem_size != 8) return fail(ctx, RZ_ERR_INVALID, "elem_size must be 4 or 8");
+    if (memory != RZ_MEM_HOST && memory != RZ_MEM_DEVICE) return fail(ctx, RZ_ERR_INVALID, "bad memory kind");
+    if (n_pixels > (1ull << 36)) return fail(ctx, RZ_ERR_INVALID, "too many pixels");
+    RZ_CUDA(cudaSetDevice(ctx->device));
+    if (memory == RZ_MEM_DEVICE) {
+        if (((uintptr_t)mask & (uintptr_t)(elem_size - 1)) || ((uintptr_t)rgba8 & 15))
+            return fail(ctx, RZ_ERR_INVALID, "misaligned device buffer");
+        RZ_CUDA(rz::launch_encode_mask_rgba8(mask, elem_size, rgba8, n_pixels, ctx->stream));
+        return RZ_OK;
+    }
+    RZ_CUDA(ctx->p_encode_in.ensure(n_pixels * (uint64_t)elem_size + 16));
+    RZ_CUDA(ctx->p_rgba8.ensure(n_pixels * 4 + 16));
+    RZ_CUDA(cudaMemcpyAsync(ctx->p_encode_in.p, mask, n_pixels * (uint64_t)elem_size, cudaMemcpyHostToDevice,
+                            ctx->stream));
+    RZ_CUDA(rz::launch_encode_mask_rgba8(ctx->p_encode_in.p, elem_size, (uint8_t*)ctx->p_rgba8.p, n_pixels,
+                                         ctx->stream));
+    return copy_out_bytes(ctx, rgba8, ctx->p_rgba8.p, n_pixels * 4);
 }
 
 }  // extern "C"

@@ -10,6 +10,7 @@
 // applies the fill rule and blends the fill's paint source-over into an RGBA
 // band kept in shared memory (Rasterizer::fill + Pipeline::render_rec,
 // src/rasterize.rs:69-115, src/scene.rs:407-435).
+#include "rz_color.cuh"
 #include "rz_device.cuh"
 #include "rz_kernels.cuh"
 #include "rz_pipeline.cuh"
@@ -596,9 +597,15 @@ __global__ void __launch_bounds__(kCompThreads) k_composite(SceneDev S, int cov_
     }
     if (paint_mode) {
         __syncthreads();
-        for (int i = threadIdx.x; i < rows * S.canvas_w; i += kCompThreads) {
-            const int r = i / S.canvas_w, x = i - r * S.canvas_w;
-            reinterpret_cast<float4*>(S.canvas)[(int64_t)(row_base + r) * S.canvas_stride + x] = rgba[i];
+        if (S.rgba8) {
+            // fused output encode: From<LinColor> for RGBA per pixel, 4 bytes out instead of 16
+            uint32_t* o = S.rgba8 + (int64_t)row_base * S.canvas_w;
+            for (int i = threadIdx.x; i < rows * S.canvas_w; i += kCompThreads) __stcs(o + i, encode_lin_rgba8(rgba[i]));
+        } else {
+            for (int i = threadIdx.x; i < rows * S.canvas_w; i += kCompThreads) {
+                const int r = i / S.canvas_w, x = i - r * S.canvas_w;
+                reinterpret_cast<float4*>(S.canvas)[(int64_t)(row_base + r) * S.canvas_stride + x] = rgba[i];
+            }
         }
     }
 }

@@ -89,6 +89,7 @@ struct SceneDev {
     int64_t canvas_stride;   // elements between rows (pixels for RGBA: 4 floats each)
     const float* bg;         // background colour or null (canvas already initialised)
     int32_t load_canvas;     // 1: blend over the canvas content instead of bg
+    uint32_t* rgba8;         // non-null: the band is written as sRGB8 RGBA (canvas_w words a row) instead of f32
     int32_t* err;
     int32_t* counters;
 };

@@ -388,6 +388,38 @@ class GpuRasterizer(Rasterizer):
                                            width, height))
         return canvas
 
+    def render_scene_rgba8(self, scene: Scene, width: int, height: int, bg=None) -> np.ndarray:
+        """Scene::render, then `to_rgba` of every pixel: (height, width, 4) uint8
+        sRGB, encoded in the composite's epilogue on the GPU."""
+        s, keep = scene.pack()
+        out = np.zeros((height, width, 4), dtype=np.uint8)
+        bg_a = np.ascontiguousarray(bg, dtype=np.float32) if bg is not None else None
+        lib = self.ctx.lib
+        self.ctx.check(lib.rz_render_scene_rgba8(self.ctx.ptr, ctypes.byref(s), self.flatness,
+                                                 bg_a.ctypes.data if bg_a is not None else None, out.ctypes.data,
+                                                 width, height))
+        return out
+
+    def encode_rgba8(self, canvas: np.ndarray) -> np.ndarray:
+        """`to_rgba` of premultiplied linear RGBA f32 pixels (..., 4) -> uint8 (..., 4)."""
+        c = np.ascontiguousarray(canvas, dtype=np.float32)
+        if c.shape[-1] != 4:
+            raise ValueError("canvas must end in 4 channels")
+        out = np.zeros(c.shape, dtype=np.uint8)
+        lib = self.ctx.lib
+        self.ctx.check(lib.rz_encode_rgba8(self.ctx.ptr, c.ctypes.data, c.size // 4, out.ctypes.data, 0))
+        return out
+
+    def encode_mask_rgba8(self, mask: np.ndarray) -> np.ndarray:
+        """`to_rgba` of a mask (f64 or f32): grey sRGB of 1 - m, opaque; shape (..., 4) uint8."""
+        m = np.ascontiguousarray(mask)
+        if m.dtype not in (np.float32, np.float64):
+            m = m.astype(np.float64)
+        out = np.zeros(m.shape + (4,), dtype=np.uint8)
+        lib = self.ctx.lib
+        self.ctx.check(lib.rz_encode_mask_rgba8(self.ctx.ptr, m.ctypes.data, m.itemsize, m.size, out.ctypes.data, 0))
+        return out
+
     def flatten_counts(self, path: Path, tr: Transform) -> np.ndarray:
         """Lines per input segment, then one entry per subpath (closing line)."""
         ps, keep = _path_struct(path)

@@ -88,3 +88,51 @@ def test_workload_shapes():
     kinds = np.bincount(path.kind, minlength=4) / path.n_segments
     assert abs(kinds[0] - 0.4) < 0.05 and abs(kinds[3] - 0.1) < 0.03
     assert rule == FillRule.EvenOdd and (w, h) == (4096, 4096)
+
+
+@pytest.mark.parametrize("fmt", ["bmp", "rgba", "ppm"])
+def test_image_writers_match_reference_layout(fmt):
+    """rz_write_image against the oracle's byte-for-byte restatement of
+    Image::write_bmp / write_rgba / write_ppm (src/image.rs:136-212)."""
+    from oracle import oracle as O
+    from rasterize_gb300 import image
+    rng = np.random.default_rng(3)
+    for h, w in [(1, 1), (3, 5), (17, 9), (0, 4)]:
+        img = rng.integers(0, 256, size=(h, w, 4), dtype=np.uint8)
+        got = image.encode(img, fmt)
+        want = {"bmp": O.write_bmp, "rgba": O.write_rgba, "ppm": O.write_ppm}[fmt](img)
+        assert got == want, (fmt, h, w)
+
+
+def test_png_writer_decodes_back():
+    import struct
+    import zlib
+    from rasterize_gb300 import image
+    rng = np.random.default_rng(4)
+    img = rng.integers(0, 256, size=(7, 11, 4), dtype=np.uint8)
+    data = image.encode(img, "png")
+    assert data[:8] == b"\x89PNG\r\n\x1a\n"
+    pos, idat, ihdr = 8, b"", None
+    while pos < len(data):
+        n, = struct.unpack(">I", data[pos:pos + 4])
+        tag, body = data[pos + 4:pos + 8], data[pos + 8:pos + 8 + n]
+        assert struct.unpack(">I", data[pos + 8 + n:pos + 12 + n])[0] == zlib.crc32(tag + body) & 0xFFFFFFFF
+        if tag == b"IHDR":
+            ihdr = struct.unpack(">IIBBBBB", body)
+        elif tag == b"IDAT":
+            idat += body
+        pos += 12 + n
+    assert ihdr == (11, 7, 8, 6, 0, 0, 0)
+    raw = np.frombuffer(zlib.decompress(idat), dtype=np.uint8).reshape(7, 1 + 11 * 4)
+    assert (raw[:, 0] == 0).all()
+    assert (raw[:, 1:].reshape(7, 11, 4) == img).all()
+
+
+def test_image_writer_rejects_bad_format():
+    lib = _ffi.load()
+    n = ctypes.c_uint64(0)
+    img = np.zeros(4, dtype=np.uint8)
+    assert lib.rz_write_image(img.ctypes.data, 1, 1, 9, None, 0, ctypes.byref(n)) == 2
+    assert lib.rz_write_image(img.ctypes.data, 1, 1, 0, None, 0, ctypes.byref(n)) == 0 and n.value == 126
+    small = np.zeros(10, dtype=np.uint8)
+    assert lib.rz_write_image(img.ctypes.data, 1, 1, 0, small.ctypes.data, 10, ctypes.byref(n)) == 7

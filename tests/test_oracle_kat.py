@@ -256,3 +256,40 @@ def test_arc_expansion_and_nan():
     bad = PathBuilder().move_to((0, 0)).line_to((float("nan"), 1)).line_to((3, 3)).close().build()
     with pytest.raises(O.OracleError):
         O.mask(bad, Transform.identity(), FillRule.NonZero, 8, 8)
+
+
+def test_color_conversion_roundtrip():
+    """src/color.rs:538-545: "#ff804010" -> LinColor -> RGBA is the identity."""
+    c = np.array([0xFF, 0x80, 0x40, 0x10], dtype=np.uint8)
+    lin = O.lin_from_rgba8(c)
+    assert list(O.encode_rgba8(lin.reshape(1, 4))[0]) == list(c)
+
+
+def test_encode_roundtrip_every_byte():
+    """Every opaque sRGB byte survives RGBA -> LinColor -> RGBA (the same path
+    as the KAT above, over all 256 values of each channel)."""
+    lin = np.stack([O.lin_from_rgba8(np.array([v, 255 - v, v // 2, 255], dtype=np.uint8)) for v in range(256)])
+    out = O.encode_rgba8(lin)
+    assert (out[:, 0] == np.arange(256)).all()
+    assert (out[:, 1] == 255 - np.arange(256)).all()
+    assert (out[:, 2] == np.arange(256) // 2).all()
+    assert (out[:, 3] == 255).all()
+
+
+def test_encode_edges():
+    """unmultiply's alpha <= 1e-6 cut (src/color.rs:308-316), Rust's saturating
+    `as u8` (negative and NaN -> 0, >= 255 -> 255) and the mask grey."""
+    f = np.float32
+    canvas = np.array([[0, 0, 0, 0], [0.5, 0.5, 0.5, f(1e-6)], [1, 1, 1, 1], [2, -1, np.nan, 1],
+                       [0.25, 0.5, 1.0, 0.5], [0.001, 0.002, 0.003, 1.0]], dtype=np.float32)
+    out = O.encode_rgba8(canvas)
+    assert list(out[0]) == [0, 0, 0, 0]
+    assert list(out[1]) == [0, 0, 0, 0]
+    assert list(out[2]) == [255, 255, 255, 255]
+    assert list(out[3]) == [255, 0, 0, 255]
+    assert list(out[4][[2, 3]]) == [255, 128]
+    m = O.encode_mask_rgba8(np.array([0.0, 1.0, 0.5, -1.0, 2.0]))
+    assert list(m[0]) == [255, 255, 255, 255]
+    assert list(m[1]) == [0, 0, 0, 255]
+    assert m[2][0] == int(np.float32(O.lib().rzo_linear_to_srgb(0.5)) * np.float32(255) + np.float32(0.5))
+    assert list(m[3][:3]) == [255] * 3 and list(m[4][:3]) == [0] * 3
