@@ -237,8 +237,8 @@ RZ_API rz_status rz_render_scene_rgba8(rz_ctx* ctx, const rz_scene* scene, doubl
 /* `to_rgba` of n premultiplied linear RGBA f32 pixels: unmultiply (alpha <= 1e-6
  * gives 0), the x86 l2s fit (src/simd/x86.rs:197-214), (c * 255 + 0.5) as u8;
  * alpha is not unmultiplied.  memory: RZ_MEM_HOST or RZ_MEM_DEVICE for both
- * arrays (device arrays 16-byte aligned; the call is then asynchronous on the
- * context's stream). */
+ * arrays (a device canvas 16-byte aligned, rgba8 4-byte aligned; the call is
+ * then asynchronous on the context's stream). */
 RZ_API rz_status rz_encode_rgba8(rz_ctx* ctx, const float* canvas, uint64_t n_pixels, uint8_t* rgba8,
                                  int32_t memory);
 /* `to_rgba` of a mask (Scalar, src/color.rs:429-432): grey linear_to_srgb(1 - m),

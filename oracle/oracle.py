@@ -92,6 +92,8 @@ def lib():
             L.rzo_encode_rgba8.argtypes = [P, ctypes.c_long, P]
             L.rzo_encode_mask_rgba8.restype = None
             L.rzo_encode_mask_rgba8.argtypes = [P, ctypes.c_long, P]
+            L.rzo_l2s_byte_thresholds.restype = ctypes.c_int
+            L.rzo_l2s_byte_thresholds.argtypes = [P]
             L.rzo_lin_from_rgba8.restype = None
             L.rzo_lin_from_rgba8.argtypes = [P, P]
             L.rzo_path_bbox.restype = ctypes.c_int
@@ -443,3 +445,10 @@ def write_ppm(rgba8):
     img = np.ascontiguousarray(rgba8, dtype=np.uint8)
     h, w = img.shape[:2]
     return ("P6 %d %d 255 " % (w, h)).encode() + img[..., :3].tobytes()
+
+
+def l2s_byte_thresholds():
+    """(T[0..255], monotone): the smallest f32 in [0, 1] reaching each sRGB byte."""
+    T = np.zeros(256, dtype=np.float32)
+    mono = lib().rzo_l2s_byte_thresholds(_ptr(T))
+    return T, bool(mono)

@@ -873,6 +873,24 @@ void rzo_encode_mask_rgba8(const double* mask, long n, uint8_t* out) {
         out[4 * i + 3] = 255;
     }
 }
+/* The l2s byte thresholds: T[k] = the smallest f32 u in [0, 1] whose byte
+   u8_sat(linear_to_srgb(u)) is >= k (k = 1..255; T[0] = 0), by a scan of
+   every f32 in [0, 1].  Returns 1 when the byte never decreases on [0, 1]
+   (then byte(u) = k exactly when T[k] <= u < T[k + 1]). */
+int rzo_l2s_byte_thresholds(float* T) {
+    int prev = 0, mono = 1;
+    T[0] = 0.0f;
+    for (int k = 1; k < 256; k++) T[k] = INFINITY;
+    for (uint32_t b = 0; b <= 0x3F800000u; b++) {
+        float u;
+        memcpy(&u, &b, 4);
+        int v = u8_sat(rzo_linear_to_srgb(u));
+        if (v < prev) mono = 0;
+        for (int k = prev + 1; k <= v; k++) T[k] = u;
+        if (v > prev) prev = v;
+    }
+    return mono;
+}
 /* From<RGBA> for LinColor color.rs:394-406 */
 void rzo_lin_from_rgba8(const uint8_t* rgba, float* out) {
     float a = (float)rgba[3] / 255.0f;

@@ -1663,8 +1663,8 @@ rz_status rz_encode_rgba8(rz_ctx* ctx, const float* canvas, uint64_t n_pixels, u
     if (n_pixels > (1ull << 36)) return fail(ctx, RZ_ERR_INVALID, "too many pixels");
     RZ_CUDA(cudaSetDevice(ctx->device));
     if (memory == RZ_MEM_DEVICE) {
-        if (((uintptr_t)canvas & 15) || ((uintptr_t)rgba8 & 15))
-            return fail(ctx, RZ_ERR_INVALID, "device buffers must be 16-byte aligned");
+        if (((uintptr_t)canvas & 15) || ((uintptr_t)rgba8 & 3))
+            return fail(ctx, RZ_ERR_INVALID, "misaligned device buffer (canvas 16 bytes, rgba8 4 bytes)");
         RZ_CUDA(rz::launch_encode_rgba8(canvas, rgba8, n_pixels, ctx->stream));
         return RZ_OK;
     }
@@ -1686,7 +1686,7 @@ rz_status rz_encode_mask_rgba8(rz_ctx* ctx, const void* mask, int32_t elem_size,
     if (n_pixels > (1ull << 36)) return fail(ctx, RZ_ERR_INVALID, "too many pixels");
     RZ_CUDA(cudaSetDevice(ctx->device));
     if (memory == RZ_MEM_DEVICE) {
-        if (((uintptr_t)mask & (uintptr_t)(elem_size - 1)) || ((uintptr_t)rgba8 & 15))
+        if (((uintptr_t)mask & (uintptr_t)(elem_size - 1)) || ((uintptr_t)rgba8 & 3))
             return fail(ctx, RZ_ERR_INVALID, "misaligned device buffer");
         RZ_CUDA(rz::launch_encode_mask_rgba8(mask, elem_size, rgba8, n_pixels, ctx->stream));
         return RZ_OK;

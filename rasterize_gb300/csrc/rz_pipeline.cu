@@ -600,7 +600,8 @@ __global__ void __launch_bounds__(kCompThreads) k_composite(SceneDev S, int cov_
         if (S.rgba8) {
             // fused output encode: From<LinColor> for RGBA per pixel, 4 bytes out instead of 16
             uint32_t* o = S.rgba8 + (int64_t)row_base * S.canvas_w;
-            for (int i = threadIdx.x; i < rows * S.canvas_w; i += kCompThreads) __stcs(o + i, encode_lin_rgba8(rgba[i]));
+            for (int i = threadIdx.x; i < rows * S.canvas_w; i += kCompThreads)
+                __stcs(o + i, encode_lin_rgba8(rgba[i]));
         } else {
             for (int i = threadIdx.x; i < rows * S.canvas_w; i += kCompThreads) {
                 const int r = i / S.canvas_w, x = i - r * S.canvas_w;

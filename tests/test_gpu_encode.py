@@ -97,3 +97,32 @@ def test_scene_rgba8_empty(R):
     out = R.render_scene_rgba8(Scene(), 9, 5, bg=(0.5, 0.25, 0.0, 1.0))
     want = O.encode_rgba8(np.array([[0.5, 0.25, 0.0, 1.0]], dtype=np.float32))[0]
     assert (out == want).all()
+
+
+def test_encode_at_every_byte_threshold(R):
+    """Channel values a few ulps either side of every place the byte changes
+    (the oracle's scan of every f32 in [0, 1]), where the hardware square
+    roots and the IEEE route could disagree: opaque and through the division."""
+    T, mono = O.l2s_byte_thresholds()
+    assert not mono  # the rounded fit steps back by one byte in a dozen places
+    vals = []
+    for t in T[1:]:
+        b = int(np.float32(t).view(np.uint32))
+        vals += [np.uint32(b + d).view(np.float32) for d in range(-64, 65)]
+    v = np.array(vals, dtype=np.float32)
+    v = v[(v >= 0) & (v <= 1)]
+    for a in (np.float32(1.0), np.float32(0.5), np.float32(0.7)):
+        c = np.stack([v * a, v[::-1] * a, np.full_like(v, 0.25) * a, np.full_like(v, a)], axis=1).astype(np.float32)
+        assert (R.encode_rgba8(c) == O.encode_rgba8(c)).all()
+    m = (np.float32(1.0) - v).astype(np.float32)
+    assert (R.encode_mask_rgba8(m) == O.encode_mask_rgba8(m.astype(np.float64))).all()
+
+
+def test_encode_strided_sweep_of_unit_interval(R):
+    """Every 64th f32 in [0, 1] as an opaque channel (16.6 M values)."""
+    bits = np.arange(0, 0x3F800001, 64, dtype=np.uint32)
+    v = bits.view(np.float32)
+    n = (len(v) + 2) // 3 * 3
+    v = np.concatenate([v, np.zeros(n - len(v), dtype=np.float32)]).reshape(-1, 3)
+    c = np.concatenate([v, np.ones((len(v), 1), dtype=np.float32)], axis=1)
+    assert (R.encode_rgba8(c) == O.encode_rgba8(c)).all()
