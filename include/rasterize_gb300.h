@@ -227,6 +227,38 @@ RZ_API rz_status rz_fill(rz_ctx* ctx, const rz_path* path, const double tr[6], i
 RZ_API rz_status rz_render_scene(rz_ctx* ctx, const rz_scene* scene, double flatness, const float bg[4],
                                  float* canvas, uint32_t width, uint32_t height);
 
+/* ---- scene trees: groups, transforms, opacity and clip layers ----------- */
+/* One node of a scene tree (SceneInner, src/scene.rs:19-62), in pre-order: a
+ * node, then the subtrees of its children.  Fill entries are those of the
+ * rz_scene the nodes come with; an entry's own transform (scene->transforms,
+ * NULL = identity) applies first, under the transforms of its ancestors. */
+#define RZ_NODE_FILL 0      /* Fill: arg = fill entry (path, rule, paint) */
+#define RZ_NODE_GROUP 1     /* Group: arg = number of child subtrees that follow */
+#define RZ_NODE_TRANSFORM 2 /* Transform: tr, then one child subtree */
+#define RZ_NODE_OPACITY 3   /* Opacity: opacity (clamped to [0, 1] as Scene::opacity does), one child */
+#define RZ_NODE_CLIP 4      /* Clip: arg = fill entry of the clip path (its rule; paint unused), units, one child */
+typedef struct rz_scene_node {
+    int32_t kind;
+    uint32_t arg;
+    int32_t units;   /* RZ_UNITS_USER_SPACE or RZ_UNITS_BOUNDING_BOX (Clip) */
+    int32_t reserved;
+    double opacity;  /* Opacity */
+    double tr[6];    /* Transform */
+} rz_scene_node;
+
+/* Scene::render (src/scene.rs:186-199) of the tree nodes[0 .. n_nodes) with
+ * view = the width x height canvas and tr = identity: Pipeline::build_rec
+ * (:268-357) on the host, then render_rec (:397-458).  Fills queued for one
+ * layer go through the line pipeline together; an Opacity or Clip node renders
+ * its child into a layer of its own (device memory, per nesting depth), a Clip
+ * renders its path's mask with the same pipeline, and one compose kernel
+ * blends the child onto its parent layer (Layer::compose, :532-565).  Output:
+ * the RGBA f32 canvas (host), the sRGB8 RGBA bytes (host), or both (either
+ * may be NULL).  With nothing in view the canvas is the background. */
+RZ_API rz_status rz_render_scene_tree(rz_ctx* ctx, const rz_scene* scene, const rz_scene_node* nodes,
+                                      uint32_t n_nodes, double flatness, const float bg[4], float* canvas,
+                                      uint8_t* rgba8, uint32_t width, uint32_t height);
+
 /* ---- output encode: premultiplied linear RGBA f32 -> sRGB8 RGBA ---------- */
 /* Scene::render followed by `to_rgba` of every pixel (From<LinColor> for RGBA,
  * src/color.rs:164-175), what Image::write_bmp / write_png / write_rgba store

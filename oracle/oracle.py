@@ -9,6 +9,7 @@ sees the same Line/Quad/Cubic segments as the reference's rasterizers.
 from __future__ import annotations
 
 import ctypes
+import math
 import os
 import subprocess
 import threading
@@ -452,3 +453,245 @@ def l2s_byte_thresholds():
     T = np.zeros(256, dtype=np.float32)
     mono = lib().rzo_l2s_byte_thresholds(_ptr(T))
     return T, bool(mono)
+
+
+# ---------------------------------------------------------------------------
+# Scene trees: Pipeline::build_rec / render_rec and Layer (src/scene.rs:153-565)
+# restated over the C primitives above.  A tree is nested tuples:
+#   ("fill", path, tr, rule, paint)      tr: the fill's own transform (applied first)
+#   ("group", [children])
+#   ("transform", child, tr)
+#   ("opacity", child, opacity)          already clamped (Scene::opacity)
+#   ("clip", child, path, units, rule)   units 0 UserSpaceOnUse, 1 BoundingBox
+# Bounding boxes are (x0, y0, x1, y1) tuples of Python floats (binary64).
+# ---------------------------------------------------------------------------
+_ID = (1.0, 0.0, 0.0, 0.0, 1.0, 0.0)
+
+
+def _m(tr):
+    return tuple(tr.m) if hasattr(tr, "m") else tuple(tr)
+
+
+def _xf_mul(s, o):
+    """Transform * Transform (src/geometry.rs:519-539)."""
+    return (s[0] * o[0] + s[1] * o[3], s[0] * o[1] + s[1] * o[4], s[0] * o[2] + s[1] * o[5] + s[2],
+            s[3] * o[0] + s[4] * o[3], s[3] * o[1] + s[4] * o[4], s[3] * o[2] + s[4] * o[5] + s[5])
+
+
+def _bbox_new(x0, y0, x1, y1):
+    """BBox::new (src/geometry.rs:552-561)."""
+    if not x0 <= x1:
+        x0, x1 = x1, x0
+    if not y0 <= y1:
+        y0, y1 = y1, y0
+    return (x0, y0, x1, y1)
+
+
+def _bbox_extend(b, x, y):
+    """BBox::extend (src/geometry.rs:611-633)."""
+    x0, y0, x1, y1 = b
+    if x < x0:
+        x0 = x
+    elif x > x1:
+        x1 = x
+    if y < y0:
+        y0 = y
+    elif y > y1:
+        y1 = y
+    return (x0, y0, x1, y1)
+
+
+def _bbox_union(a, b):
+    return _bbox_extend(_bbox_extend(a, b[0], b[1]), b[2], b[3])
+
+
+def _bbox_intersect(a, b):
+    """BBox::intersect with range_intersect (src/geometry.rs:648-657, 677-688)."""
+    if a[0] > b[2] or b[0] > a[2] or a[1] > b[3] or b[1] > a[3]:
+        return None
+    return _bbox_new(max(a[0], b[0]), max(a[1], b[1]), min(a[2], b[2]), min(a[3], b[3]))
+
+
+def _unit_transform(b):
+    """BBox::unit_transform (src/geometry.rs:662-664)."""
+    return _xf_mul((1.0, 0.0, b[0], 0.0, 1.0, b[1]), (b[2] - b[0], 0.0, 0.0, 0.0, b[3] - b[1], 0.0))
+
+
+def _path_bbox(path, tr):
+    b = path_bbox(path, tr)
+    return None if b is None else tuple(float(v) for v in b)
+
+
+def _scene_bbox(node, tr):
+    """Scene::bbox (src/scene.rs:153-182)."""
+    k = node[0]
+    if k == "fill":
+        return _path_bbox(node[1], _xf_mul(tr, _m(node[2])))
+    if k == "group":
+        acc = None
+        for c in node[1]:
+            cb = _scene_bbox(c, tr)
+            acc = cb if acc is None else (acc if cb is None else _bbox_union(acc, cb))
+        return acc
+    if k == "transform":
+        return _scene_bbox(node[1], _xf_mul(tr, _m(node[2])))
+    if k == "opacity":
+        return _scene_bbox(node[1], tr)
+    clip_tr = tr
+    if node[3] == 1:
+        cb = _scene_bbox(node[1], _ID)
+        if cb is None:
+            return None
+        clip_tr = _xf_mul(tr, _unit_transform(cb))
+    child = _scene_bbox(node[1], tr)
+    if child is None:
+        return None
+    clip = _path_bbox(node[2], clip_tr)
+    if clip is None:
+        return None
+    return _bbox_intersect(child, clip)
+
+
+def _view_apply(view, bbox):
+    if view is None:
+        return bbox
+    if bbox is None:
+        return None
+    return _bbox_intersect(view, bbox)
+
+
+def _build_rec(node, view, tr, out):
+    """Pipeline::build_rec (src/scene.rs:268-357): appends pipeline nodes
+    (children first) and returns the index of this one, or None."""
+    k = node[0]
+    if k == "fill":
+        b = _view_apply(view, _path_bbox(node[1], _xf_mul(tr, _m(node[2]))))
+        if b is None:
+            return None
+        out.append({"kind": "fill", "bbox": b, "tr": tr, "node": node})
+    elif k == "group":
+        ids = [i for i in (_build_rec(c, view, tr, out) for c in node[1]) if i is not None]
+        if not ids:
+            return None
+        acc = None
+        for i in ids:
+            acc = out[i]["bbox"] if acc is None else _bbox_union(out[i]["bbox"], acc)
+        out.append({"kind": "group", "bbox": acc, "tr": tr, "children": ids})
+    elif k == "clip":
+        clip_tr = tr
+        if node[3] == 1:
+            cb = _scene_bbox(node[1], _ID)
+            if cb is None:
+                return None
+            clip_tr = _xf_mul(tr, _unit_transform(cb))
+        clip_bbox = _view_apply(view, _path_bbox(node[2], clip_tr))
+        if clip_bbox is None:
+            return None
+        cid = _build_rec(node[1], clip_bbox, tr, out)
+        if cid is None:
+            return None
+        b = _bbox_intersect(clip_bbox, out[cid]["bbox"])
+        if b is None:
+            return None
+        out.append({"kind": "clip", "bbox": b, "tr": tr, "child": cid, "clip": node[2], "clip_tr": clip_tr,
+                    "rule": node[4]})
+    elif k == "opacity":
+        cid = _build_rec(node[1], view, tr, out)
+        if cid is None:
+            return None
+        out.append({"kind": "opacity", "bbox": out[cid]["bbox"], "tr": tr, "child": cid, "opacity": node[2]})
+    else:
+        return _build_rec(node[1], view, _xf_mul(tr, _m(node[2])), out)
+    return len(out) - 1
+
+
+def _layer_new(b, color=None):
+    """Layer::new (src/scene.rs:483-501)."""
+    x0, x1 = math.floor(b[0]), math.ceil(b[2])
+    y0, y1 = math.floor(b[1]), math.ceil(b[3])
+    img = np.zeros((y1 - y0, x1 - x0, 4), dtype=np.float32)
+    if color is not None:
+        img[:] = np.asarray(color, dtype=np.float32)
+    return {"x": x0, "y": y0, "img": img}
+
+
+def _layer_compose(dst, src, fn):
+    """Layer::compose (src/scene.rs:532-565) over the intersection."""
+    dh, dw = dst["img"].shape[:2]
+    sh, sw = src["img"].shape[:2]
+    x0, x1 = max(dst["x"], src["x"]), min(dst["x"] + dw, src["x"] + sw)
+    y0, y1 = max(dst["y"], src["y"]), min(dst["y"] + dh, src["y"] + sh)
+    if x1 <= x0 or y1 <= y0:
+        return
+    d = dst["img"][y0 - dst["y"]:y1 - dst["y"], x0 - dst["x"]:x1 - dst["x"]]
+    s = src["img"][y0 - src["y"]:y1 - src["y"], x0 - src["x"]:x1 - src["x"]]
+    d[...] = fn(d, s)
+
+
+def _blend_over(dst, src):
+    """LinColor::blend_over (src/color.rs:342-344): src + dst * (1 - src.alpha), in f32."""
+    return src + dst * (np.float32(1.0) - src[..., 3:4])
+
+
+def _render(nodes, pid, view, bg, flatness):
+    """Pipeline::render (src/scene.rs:384-395)."""
+    layer = _layer_new(view if view is not None else nodes[pid]["bbox"], bg)
+    _render_rec(nodes, pid, layer, flatness)
+    return layer
+
+
+def _render_rec(nodes, pid, layer, flatness):
+    """Pipeline::render_rec (src/scene.rs:397-458)."""
+    nd = nodes[pid]
+    k = nd["kind"]
+    if k == "fill":
+        b = nd["bbox"]
+        h, w = layer["img"].shape[:2]
+        col_min = math.floor(b[0]) - layer["x"]
+        col_max = math.ceil(b[2]) - layer["x"] + 1
+        row_min = math.floor(b[1]) - layer["y"]
+        row_max = math.ceil(b[3]) - layer["y"] + 1
+        # `i32 as usize` wraps negatives to huge values; view_shape clamps (src/image.rs:588-605)
+        wrap = lambda v, lim: lim if v < 0 else v  # noqa: E731
+        row_min = min(wrap(row_min, h), h)
+        row_max = max(min(wrap(row_max, h), h), row_min)
+        col_min = min(wrap(col_min, w), w)
+        col_max = max(min(wrap(col_max, w), w), col_min)
+        vw, vh = col_max - col_min, row_max - row_min
+        if vw <= 0 or vh <= 0:
+            return
+        align = (1.0, 0.0, -math.floor(b[0]), 0.0, 1.0, -math.floor(b[1]))
+        node = nd["node"]
+        tr = _xf_mul(_xf_mul(align, nd["tr"]), _m(node[2]))
+        fill(node[1], tr, node[3], node[4], layer["img"], shape=(row_min * w + col_min, vw, vh, w, 1),
+             flatness=flatness)
+    elif k == "group":
+        for c in nd["children"]:
+            _render_rec(nodes, c, layer, flatness)
+    elif k == "opacity":
+        child = _render(nodes, nd["child"], None, None, flatness)
+        op = np.float32(nd["opacity"])
+        _layer_compose(layer, child, lambda d, s: _blend_over(d, s * op))
+    else:
+        mlay = _layer_new(nd["bbox"])
+        mh, mw = mlay["img"].shape[:2]
+        align = (1.0, 0.0, -float(mlay["x"]), 0.0, 1.0, -float(mlay["y"]))
+        child = _render(nodes, nd["child"], None, None, flatness)
+        m = mask(nd["clip"], _xf_mul(align, nd["clip_tr"]), nd["rule"], mw, mh, flatness=flatness)
+        mlayer = {"x": mlay["x"], "y": mlay["y"], "img": m.astype(np.float32)[..., None]}
+        _layer_compose(child, mlayer, lambda d, s: d * s)
+        _layer_compose(layer, child, _blend_over)
+
+
+def scene_tree_render(tree, width, height, bg=(0, 0, 0, 0), flatness=0.05):
+    """Scene::render (src/scene.rs:186-199) of ``tree`` with view = the canvas
+    (0, 0, width, height) and tr = identity: the (height, width, 4) f32 canvas.
+    With nothing in view the reference returns an empty layer; the canvas is
+    then the background."""
+    nodes = []
+    root = _build_rec(tree, (0.0, 0.0, float(width), float(height)), _ID, nodes)
+    if root is None:
+        img = np.zeros((height, width, 4), dtype=np.float32)
+        img[:] = np.asarray(bg, dtype=np.float32)
+        return img
+    return _render(nodes, root, (0.0, 0.0, float(width), float(height)), bg, flatness)["img"]

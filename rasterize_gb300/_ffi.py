@@ -65,6 +65,14 @@ class RzScene(ctypes.Structure):
                 ("paints", ctypes.c_void_p)]
 
 
+class RzSceneNode(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("arg", ctypes.c_uint32), ("units", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("opacity", ctypes.c_double), ("tr", ctypes.c_double * 6)]
+
+
+NODE_FILL, NODE_GROUP, NODE_TRANSFORM, NODE_OPACITY, NODE_CLIP = 0, 1, 2, 3, 4
+
+
 class RzDiffBatch(ctypes.Structure):
     _fields_ = [("n_images", ctypes.c_uint32), ("paths_per_image", ctypes.c_uint32), ("segs_per_path", ctypes.c_uint32),
                 ("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("fill_rule", ctypes.c_int32),
@@ -113,6 +121,8 @@ _SIGNATURES = {
                                          ctypes.c_uint32]),
     "rz_render_scene_rgba8": (ctypes.c_int32, [P, ctypes.POINTER(RzScene), ctypes.c_double, P, P, ctypes.c_uint32,
                                                ctypes.c_uint32]),
+    "rz_render_scene_tree": (ctypes.c_int32, [P, ctypes.POINTER(RzScene), P, ctypes.c_uint32, ctypes.c_double, P, P,
+                                              P, ctypes.c_uint32, ctypes.c_uint32]),
     "rz_encode_rgba8": (ctypes.c_int32, [P, P, ctypes.c_uint64, P, ctypes.c_int32]),
     "rz_encode_mask_rgba8": (ctypes.c_int32, [P, P, ctypes.c_int32, ctypes.c_uint64, P, ctypes.c_int32]),
     "rz_write_image": (ctypes.c_int32, [P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int32, P, ctypes.c_uint64,

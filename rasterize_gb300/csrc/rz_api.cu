@@ -52,6 +52,10 @@ cudaError_t launch_l2_loss(const float* A, const float* T, uint64_t n, double* l
 cudaError_t scan_u32(uint32_t* data, uint64_t n, uint32_t* temp, cudaStream_t stream);
 cudaError_t launch_encode_rgba8(const float* in, uint8_t* out, uint64_t n, cudaStream_t st);
 cudaError_t launch_encode_mask_rgba8(const void* in, int elem_size, uint8_t* out, uint64_t n, cudaStream_t st);
+cudaError_t launch_layer_fill(float* buf, uint64_t n_pixels, const float v[4], cudaStream_t st);
+cudaError_t launch_layer_compose(float* dst, const int32_t d[4], const float* src, const int32_t s[4],
+                                 const float* mask, const int32_t m[4], float opacity, bool scale_opacity, int x0,
+                                 int y0, int x1, int y1, cudaStream_t st);
 }  // namespace rz
 
 namespace {
@@ -116,6 +120,8 @@ struct rz_ctx {
     DevBuf p_leaf, d_loss;
     // output encode (sRGB8 RGBA) and its input staging
     DevBuf p_rgba8, p_encode_in;
+    // scene-tree layers by nesting depth: colour layers and clip masks
+    std::vector<DevBuf> layer_pool, mask_pool;
     // batch tuning (rz_tune_batch / rz_set_tuning): band height cap, resident CTAs per SM (0 = occupancy)
     int tune_rows_cap = 256;
     int tune_ctas = 0;
@@ -316,6 +322,8 @@ void rz_destroy(rz_ctx* c) {
                       &c->p_pairs,  &c->p_scan,    &c->p_canvas,  &c->p_leaf,    &c->d_loss,    &c->p_rgba8,
                       &c->p_encode_in};
     for (DevBuf* b : bufs) b->release();
+    for (DevBuf& b : c->layer_pool) b.release();
+    for (DevBuf& b : c->mask_pool) b.release();
     c->h_stage.release();
     c->h_out.release();
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -1392,6 +1400,391 @@ rz_status mask_pipeline(rz_ctx* ctx, const rz_path* path, const double tr[6], in
                         false);
 }
 
+// ---------------------------------------------------------------------------
+// Scene trees: Pipeline::build_rec / render_rec and Layer (src/scene.rs:222-565)
+// ---------------------------------------------------------------------------
+// A pipeline node (src/scene.rs:222-246): the node's rendering bbox and
+// transform; FILL and CLIP name a fill entry of the scene (CLIP: its path and
+// rule), OPACITY and CLIP have one child.
+struct PNode {
+    int kind = 0;
+    rzhost::Box bbox{};
+    rzhost::Xf tr{};
+    uint32_t entry = 0;
+    std::vector<int> children;
+    float opacity = 1.0f;
+    rzhost::Xf clip_tr{};
+};
+
+struct OptBox {
+    bool ok = false;
+    rzhost::Box b{};
+};
+
+const rzhost::Xf kIdentity{{1, 0, 0, 0, 1, 0}};
+
+// BBox::intersect (src/geometry.rs:648-657 with range_intersect :677-688)
+OptBox box_intersect(const rzhost::Box& a, const rzhost::Box& o) {
+    OptBox r;
+    if (a.x0 > o.x1 || o.x0 > a.x1 || a.y0 > o.y1 || o.y0 > a.y1) return r;
+    r.ok = true;
+    r.b = rzhost::box_new(rzhost::P2{std::fmax(a.x0, o.x0), std::fmax(a.y0, o.y0)},
+                          rzhost::P2{std::fmin(a.x1, o.x1), std::fmin(a.y1, o.y1)});
+    return r;
+}
+
+// BBox::union (src/geometry.rs:636-638)
+rzhost::Box box_union(const rzhost::Box& a, const rzhost::Box& o) {
+    return rzhost::box_extend(rzhost::box_extend(a, rzhost::P2{o.x0, o.y0}), rzhost::P2{o.x1, o.y1});
+}
+
+// BBox::unit_transform (src/geometry.rs:662-664): translate(x, y).pre_scale(w, h)
+rzhost::Xf unit_transform(const rzhost::Box& b) {
+    const rzhost::Xf t{{1, 0, b.x0, 0, 1, b.y0}}, s{{b.x1 - b.x0, 0, 0, 0, b.y1 - b.y0, 0}};
+    return rzhost::xf_mul(t, s);
+}
+
+// view_apply (src/scene.rs:276-282)
+OptBox view_apply(const OptBox& view, const OptBox& bbox) {
+    if (!view.ok) return bbox;
+    if (!bbox.ok) return OptBox{};
+    return box_intersect(view.b, bbox.b);
+}
+
+struct SceneTree {
+    const rz_scene* sc = nullptr;
+    const rz_scene_node* nodes = nullptr;
+    uint32_t n = 0;
+    std::vector<uint32_t> end;  // end[i]: the index after node i's subtree
+    HostScene base;             // staged segment arrays
+    std::vector<uint32_t> fsub;
+    std::vector<PNode> P;
+};
+
+// Checks the pre-order node array and records every subtree's end.
+rz_status parse_tree(rz_ctx* ctx, SceneTree& T, uint32_t i, int depth, uint32_t& out_end) {
+    if (i >= T.n) return fail(ctx, RZ_ERR_INVALID, "scene tree: a node's children run past n_nodes");
+    if (depth > 256) return fail(ctx, RZ_ERR_INVALID, "scene tree deeper than 256");
+    const rz_scene_node& nd = T.nodes[i];
+    uint32_t e = i + 1;
+    switch (nd.kind) {
+        case RZ_NODE_FILL:
+            if (nd.arg >= T.sc->n_fills) return fail(ctx, RZ_ERR_INVALID, "scene tree: fill entry out of range");
+            break;
+        case RZ_NODE_GROUP:
+            for (uint32_t c = 0; c < nd.arg; ++c) {
+                rz_status st = parse_tree(ctx, T, e, depth + 1, e);
+                if (st) return st;
+            }
+            break;
+        case RZ_NODE_CLIP:
+            if (nd.arg >= T.sc->n_fills) return fail(ctx, RZ_ERR_INVALID, "scene tree: clip entry out of range");
+            if (nd.units != RZ_UNITS_USER_SPACE && nd.units != RZ_UNITS_BOUNDING_BOX)
+                return fail(ctx, RZ_ERR_INVALID, "scene tree: bad clip units");
+            // fallthrough: one child
+        case RZ_NODE_TRANSFORM:
+        case RZ_NODE_OPACITY: {
+            if (nd.kind == RZ_NODE_OPACITY && std::isnan(nd.opacity))
+                return fail(ctx, RZ_ERR_INVALID, "scene tree: opacity is NaN");
+            rz_status st = parse_tree(ctx, T, e, depth + 1, e);
+            if (st) return st;
+            break;
+        }
+        default: return fail(ctx, RZ_ERR_INVALID, "scene tree: unknown node kind");
+    }
+    T.end[i] = e;
+    out_end = e;
+    return RZ_OK;
+}
+
+rzhost::Xf entry_tr(const SceneTree& T, uint32_t f) {
+    rzhost::Xf t = kIdentity;
+    if (T.sc->transforms) std::memcpy(t.m, T.sc->transforms + 6ull * f, sizeof(t.m));
+    return t;
+}
+
+// Path::bbox(tr) of fill entry f (its own transform applied first)
+OptBox entry_bbox(const SceneTree& T, uint32_t f, const rzhost::Xf& tr) {
+    OptBox r;
+    r.ok = rzhost::path_bbox(T.base.kind, T.base.pts, T.base.sub_off, T.fsub[f], T.fsub[f + 1],
+                             rzhost::xf_mul(tr, entry_tr(T, f)), r.b);
+    return r;
+}
+
+rzhost::Xf node_tr(const rz_scene_node& nd) {
+    rzhost::Xf t;
+    std::memcpy(t.m, nd.tr, sizeof(t.m));
+    return t;
+}
+
+// Scene::bbox (src/scene.rs:153-182)
+OptBox scene_bbox(const SceneTree& T, uint32_t i, const rzhost::Xf& tr) {
+    const rz_scene_node& nd = T.nodes[i];
+    switch (nd.kind) {
+        case RZ_NODE_FILL: return entry_bbox(T, nd.arg, tr);
+        case RZ_NODE_GROUP: {
+            OptBox acc;
+            uint32_t c = i + 1;
+            for (uint32_t k = 0; k < nd.arg; ++k, c = T.end[c]) {
+                const OptBox cb = scene_bbox(T, c, tr);
+                if (acc.ok) {
+                    if (cb.ok) acc.b = box_union(acc.b, cb.b);
+                } else {
+                    acc = cb;
+                }
+            }
+            return acc;
+        }
+        case RZ_NODE_TRANSFORM: return scene_bbox(T, i + 1, rzhost::xf_mul(tr, node_tr(nd)));
+        case RZ_NODE_OPACITY: return scene_bbox(T, i + 1, tr);
+        default: {  // CLIP
+            rzhost::Xf clip_tr = tr;
+            if (nd.units == RZ_UNITS_BOUNDING_BOX) {
+                const OptBox cb = scene_bbox(T, i + 1, kIdentity);
+                if (!cb.ok) return OptBox{};
+                clip_tr = rzhost::xf_mul(tr, unit_transform(cb.b));
+            }
+            const OptBox child = scene_bbox(T, i + 1, tr);
+            if (!child.ok) return OptBox{};
+            const OptBox clip = entry_bbox(T, nd.arg, clip_tr);
+            if (!clip.ok) return OptBox{};
+            return box_intersect(child.b, clip.b);
+        }
+    }
+}
+
+// Pipeline::build_rec (src/scene.rs:268-357); -1 for None.  Children are
+// allocated before their parent, so the root is the last node.
+int build_rec(SceneTree& T, uint32_t i, const OptBox& view, const rzhost::Xf& tr) {
+    const rz_scene_node& nd = T.nodes[i];
+    PNode p;
+    p.tr = tr;
+    switch (nd.kind) {
+        case RZ_NODE_FILL: {
+            const OptBox b = view_apply(view, entry_bbox(T, nd.arg, tr));
+            if (!b.ok) return -1;
+            p.kind = RZ_NODE_FILL;
+            p.bbox = b.b;
+            p.entry = nd.arg;
+            break;
+        }
+        case RZ_NODE_GROUP: {
+            OptBox acc;
+            uint32_t c = i + 1;
+            for (uint32_t k = 0; k < nd.arg; ++k, c = T.end[c]) {
+                const int id = build_rec(T, c, view, tr);
+                if (id < 0) continue;
+                p.children.push_back(id);
+                // fold(None, |acc, bbox| Some(bbox.union_opt(acc)))
+                acc.b = acc.ok ? box_union(T.P[id].bbox, acc.b) : T.P[id].bbox;
+                acc.ok = true;
+            }
+            if (!acc.ok) return -1;
+            p.kind = RZ_NODE_GROUP;
+            p.bbox = acc.b;
+            break;
+        }
+        case RZ_NODE_CLIP: {
+            rzhost::Xf clip_tr = tr;
+            if (nd.units == RZ_UNITS_BOUNDING_BOX) {
+                const OptBox cb = scene_bbox(T, i + 1, kIdentity);
+                if (!cb.ok) return -1;
+                clip_tr = rzhost::xf_mul(tr, unit_transform(cb.b));
+            }
+            const OptBox clip_bbox = view_apply(view, entry_bbox(T, nd.arg, clip_tr));
+            if (!clip_bbox.ok) return -1;
+            const int cid = build_rec(T, i + 1, clip_bbox, tr);
+            if (cid < 0) return -1;
+            const OptBox b = box_intersect(clip_bbox.b, T.P[cid].bbox);
+            if (!b.ok) return -1;
+            p.kind = RZ_NODE_CLIP;
+            p.bbox = b.b;
+            p.children.push_back(cid);
+            p.entry = nd.arg;
+            p.clip_tr = clip_tr;
+            break;
+        }
+        case RZ_NODE_OPACITY: {
+            const int cid = build_rec(T, i + 1, view, tr);
+            if (cid < 0) return -1;
+            p.kind = RZ_NODE_OPACITY;
+            p.bbox = T.P[cid].bbox;
+            p.children.push_back(cid);
+            // Scene::opacity clamps to [0, 1]; render_rec uses it as f32
+            p.opacity = (float)std::fmin(std::fmax(nd.opacity, 0.0), 1.0);
+            break;
+        }
+        default:  // TRANSFORM
+            return build_rec(T, i + 1, view, rzhost::xf_mul(tr, node_tr(nd)));
+    }
+    T.P.push_back(std::move(p));
+    return (int)T.P.size() - 1;
+}
+
+// A layer: a rectangle of the canvas grid with its device pixels, and the
+// fills queued for it (flushed through the line pipeline before anything
+// reads the layer).
+struct LayerState {
+    int32_t x = 0, y = 0, w = 0, h = 0;
+    float* buf = nullptr;
+    HostScene hs;
+};
+
+// Layer::new (src/scene.rs:483-501): floor of min, ceil of max.
+void layer_rect(const rzhost::Box& b, LayerState& L) {
+    L.x = (int32_t)std::floor(b.x0);
+    L.y = (int32_t)std::floor(b.y0);
+    L.w = std::max<int32_t>((int32_t)std::ceil(b.x1) - L.x, 0);
+    L.h = std::max<int32_t>((int32_t)std::ceil(b.y1) - L.y, 0);
+}
+
+void layer_begin(const SceneTree& T, LayerState& L) {
+    L.hs = HostScene{};
+    L.hs.kind = T.base.kind;
+    L.hs.pts = T.base.pts;
+    L.hs.sub_off = T.base.sub_off;
+    L.hs.n_seg = T.base.n_seg;
+    L.hs.n_sub = T.base.n_sub;
+    L.hs.band_rows = choose_band_rows(std::max(L.w, 1), std::max(L.h, 1), true);
+}
+
+rz_status layer_flush(rz_ctx* ctx, LayerState& L, double flatness) {
+    if (L.hs.fills.empty()) return RZ_OK;
+    rz_status st = run_pipeline(ctx, L.hs, flatness, L.buf, L.w, L.w, L.h, nullptr, true);
+    const int band_rows = L.hs.band_rows;
+    L.hs.fills.clear();
+    L.hs.paints.clear();
+    L.hs.n_slots = L.hs.n_entries = 0;
+    L.hs.max_clip = 1;
+    L.hs.band_rows = band_rows;
+    return st;
+}
+
+rz_status render_rec(rz_ctx* ctx, SceneTree& T, int pid, LayerState& L, int depth, double flatness);
+
+// Pipeline::render (src/scene.rs:384-395) of a child node into a fresh
+// transparent layer at nesting depth `depth`, flushed.
+rz_status render_child(rz_ctx* ctx, SceneTree& T, int pid, LayerState& C, int depth, double flatness) {
+    layer_rect(T.P[pid].bbox, C);
+    if ((int)ctx->layer_pool.size() <= depth) ctx->layer_pool.resize(depth + 1);
+    const uint64_t n = (uint64_t)C.w * (uint64_t)C.h;
+    RZ_CUDA(ctx->layer_pool[depth].ensure(n * 16 + 16));
+    C.buf = (float*)ctx->layer_pool[depth].p;
+    if (n) RZ_CUDA(cudaMemsetAsync(C.buf, 0, n * 16, ctx->stream));
+    layer_begin(T, C);
+    if (n == 0) return RZ_OK;
+    rz_status st = render_rec(ctx, T, pid, C, depth, flatness);
+    if (st) return st;
+    return layer_flush(ctx, C, flatness);
+}
+
+// Pipeline::render_rec (src/scene.rs:397-458).
+rz_status render_rec(rz_ctx* ctx, SceneTree& T, int pid, LayerState& L, int depth, double flatness) {
+    const PNode& p = T.P[pid];
+    if (p.kind == RZ_NODE_FILL) {
+        // the fill's view of the layer (max bounds are exclusive: max + 1) and the align transform
+        long col_min = (long)std::floor(p.bbox.x0) - L.x, col_max = (long)std::ceil(p.bbox.x1) - L.x + 1;
+        long row_min = (long)std::floor(p.bbox.y0) - L.y, row_max = (long)std::ceil(p.bbox.y1) - L.y + 1;
+        if (col_min < 0) col_min = L.w;  // `as usize` wraps; view_shape clamps (src/image.rs:588-605)
+        if (row_min < 0) row_min = L.h;
+        if (col_max < 0) col_max = L.w;
+        if (row_max < 0) row_max = L.h;
+        row_min = std::min<long>(row_min, L.h);
+        row_max = std::max(std::min<long>(row_max, L.h), row_min);
+        col_min = std::min<long>(col_min, L.w);
+        col_max = std::max(std::min<long>(col_max, L.w), col_min);
+        const int vw = (int)(col_max - col_min), vh = (int)(row_max - row_min);
+        if (vw <= 0 || vh <= 0) return RZ_OK;
+        const rzhost::Xf align{{1.0, 0.0, -std::floor(p.bbox.x0), 0.0, 1.0, -std::floor(p.bbox.y0)}};
+        const rzhost::Xf tr_fill = rzhost::xf_mul(rzhost::xf_mul(align, p.tr), entry_tr(T, p.entry));
+        const rz_paint& paint = T.sc->paints[T.sc->fill_paint[p.entry]];
+        rzhost::Box ubox{};
+        bool have_u = false;
+        if (paint.units == RZ_UNITS_BOUNDING_BOX)
+            have_u = rzhost::path_bbox(T.base.kind, T.base.pts, T.base.sub_off, T.fsub[p.entry], T.fsub[p.entry + 1],
+                                       kIdentity, ubox);
+        rz::PaintDev pd;
+        prepare_paint(paint, tr_fill, have_u, ubox, pd);
+        if (pd.kind < 0) return RZ_OK;
+        L.hs.paints.push_back(pd);
+        const int rule = T.sc->fill_rules ? T.sc->fill_rules[p.entry] : 0;
+        add_fill(L.hs, T.fsub[p.entry], T.fsub[p.entry + 1], (int)col_min, (int)row_min, vw, vh, vw, tr_fill, rule,
+                 (int)L.hs.paints.size() - 1);
+        return RZ_OK;
+    }
+    if (p.kind == RZ_NODE_GROUP) {
+        for (int c : p.children) {
+            rz_status st = render_rec(ctx, T, c, L, depth, flatness);
+            if (st) return st;
+        }
+        return RZ_OK;
+    }
+    // Opacity and Clip: the child renders into its own layer, then composes onto L
+    rz_status st = layer_flush(ctx, L, flatness);
+    if (st) return st;
+    LayerState C;
+    st = render_child(ctx, T, p.children[0], C, depth + 1, flatness);
+    if (st) return st;
+    const int32_t drect[4] = {L.x, L.y, L.w, L.h}, srect[4] = {C.x, C.y, C.w, C.h};
+    const int x0 = std::max(L.x, C.x), x1 = std::min(L.x + L.w, C.x + C.w);
+    const int y0 = std::max(L.y, C.y), y1 = std::min(L.y + L.h, C.y + C.h);
+    if (p.kind == RZ_NODE_OPACITY) {
+        RZ_CUDA(rz::launch_layer_compose(L.buf, drect, C.buf, srect, nullptr, drect, p.opacity, true, x0, y0, x1, y1,
+                                         ctx->stream));
+        return RZ_OK;
+    }
+    // Clip: the clip path's mask over the clip node's bbox (Path::mask, mask semantics)
+    LayerState M;
+    layer_rect(p.bbox, M);
+    const uint64_t nm = (uint64_t)M.w * (uint64_t)M.h;
+    if ((int)ctx->mask_pool.size() <= depth) ctx->mask_pool.resize(depth + 1);
+    RZ_CUDA(ctx->mask_pool[depth].ensure(nm * 4 + 16));
+    float* mask = (float*)ctx->mask_pool[depth].p;
+    if (nm) {
+        RZ_CUDA(cudaMemsetAsync(mask, 0, nm * 4, ctx->stream));
+        HostScene mh;
+        mh.kind = T.base.kind;
+        mh.pts = T.base.pts;
+        mh.sub_off = T.base.sub_off;
+        mh.n_seg = T.base.n_seg;
+        mh.n_sub = T.base.n_sub;
+        mh.band_rows = choose_band_rows(M.w, M.h, false);
+        const rzhost::Xf align{{1.0, 0.0, -(double)M.x, 0.0, 1.0, -(double)M.y}};
+        const rzhost::Xf t = rzhost::xf_mul(rzhost::xf_mul(align, p.clip_tr), entry_tr(T, p.entry));
+        const int rule = T.sc->fill_rules ? T.sc->fill_rules[p.entry] : 0;
+        add_fill(mh, T.fsub[p.entry], T.fsub[p.entry + 1], 0, 0, M.w, M.h, M.w - 1, t, rule, -1);
+        st = run_pipeline(ctx, mh, flatness, mask, M.w, M.w, M.h, nullptr, false);
+        if (st) return st;
+    }
+    const int32_t mrect[4] = {M.x, M.y, M.w, M.h};
+    RZ_CUDA(rz::launch_layer_compose(L.buf, drect, C.buf, srect, mask, mrect, 1.0f, false, x0, y0, x1, y1,
+                                     ctx->stream));
+    return RZ_OK;
+}
+
+// Scene-table checks shared by the flat and tree renders.
+rz_status check_scene(rz_ctx* ctx, const rz_scene* scene, double flatness, uint32_t width, uint32_t height) {
+    if (!scene || (scene->n_fills && (!scene->fill_subpath_off || !scene->fill_paint || !scene->paints)))
+        return fail(ctx, RZ_ERR_INVALID, "null argument");
+    if (!valid_flatness(flatness)) return fail(ctx, RZ_ERR_INVALID, "flatness must be > 0 and finite");
+    if (width > 16383 || height > 16383) return fail(ctx, RZ_ERR_INVALID, "canvas too large");
+    if ((scene->n_segments && (!scene->seg_kind || !scene->seg_pts)) || (scene->n_subpaths && !scene->subpath_off))
+        return fail(ctx, RZ_ERR_INVALID, "null segment arrays");
+    const uint32_t F = scene->n_fills;
+    for (uint32_t f = 0; f < F; ++f) {
+        if (scene->fill_subpath_off[f] > scene->fill_subpath_off[f + 1] || scene->fill_paint[f] >= scene->n_paints)
+            return fail(ctx, RZ_ERR_INVALID, "bad fill table");
+    }
+    if (F && scene->fill_subpath_off[F] > scene->n_subpaths) return fail(ctx, RZ_ERR_INVALID, "bad fill_subpath_off");
+    for (uint32_t i = 0; i < scene->n_subpaths; ++i)
+        if (scene->subpath_off[i] > scene->subpath_off[i + 1]) return fail(ctx, RZ_ERR_INVALID, "subpath_off decreasing");
+    if (scene->n_subpaths && scene->subpath_off[scene->n_subpaths] > scene->n_segments)
+        return fail(ctx, RZ_ERR_INVALID, "subpath_off exceeds n_segments");
+    for (uint32_t p = 0; p < scene->n_paints; ++p)
+        if (scene->paints[p].n_stops > (uint32_t)rz::kMaxStops) return fail(ctx, RZ_ERR_INVALID, "more than 16 stops");
+    return RZ_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1457,22 +1850,10 @@ static rz_status render_scene_impl(rz_ctx* ctx, const rz_scene* scene, double fl
                                    float* canvas, uint8_t* rgba8, uint32_t width, uint32_t height) {
     if (!ctx) return RZ_ERR_INVALID;
     std::lock_guard<std::mutex> lock(ctx->mu);
-    if (!scene || (!canvas && !rgba8) || (scene->n_fills && (!scene->fill_subpath_off || !scene->fill_paint || !scene->paints)))
-        return fail(ctx, RZ_ERR_INVALID, "null argument");
-    if (!valid_flatness(flatness)) return fail(ctx, RZ_ERR_INVALID, "flatness must be > 0 and finite");
-    if (width > 16383 || height > 16383) return fail(ctx, RZ_ERR_INVALID, "canvas too large");
+    if (!canvas && !rgba8) return fail(ctx, RZ_ERR_INVALID, "null argument");
+    rz_status st0 = check_scene(ctx, scene, flatness, width, height);
+    if (st0) return st0;
     const uint32_t F = scene->n_fills;
-    for (uint32_t f = 0; f < F; ++f) {
-        if (scene->fill_subpath_off[f] > scene->fill_subpath_off[f + 1] || scene->fill_paint[f] >= scene->n_paints)
-            return fail(ctx, RZ_ERR_INVALID, "bad fill table");
-    }
-    if (F && scene->fill_subpath_off[F] > scene->n_subpaths) return fail(ctx, RZ_ERR_INVALID, "bad fill_subpath_off");
-    for (uint32_t i = 0; i < scene->n_subpaths; ++i)
-        if (scene->subpath_off[i] > scene->subpath_off[i + 1]) return fail(ctx, RZ_ERR_INVALID, "subpath_off decreasing");
-    if (scene->subpath_off[scene->n_subpaths] > scene->n_segments)
-        return fail(ctx, RZ_ERR_INVALID, "subpath_off exceeds n_segments");
-    for (uint32_t p = 0; p < scene->n_paints; ++p)
-        if (scene->paints[p].n_stops > (uint32_t)rz::kMaxStops) return fail(ctx, RZ_ERR_INVALID, "more than 16 stops");
     RZ_CUDA(cudaSetDevice(ctx->device));
     Trace tr("rz_render_scene");
     HostScene hs;
@@ -1652,6 +2033,68 @@ rz_status rz_write_image(const uint8_t* rgba8, uint32_t width, uint32_t height, 
         }
     }
     return RZ_OK;
+}
+
+rz_status rz_render_scene_tree(rz_ctx* ctx, const rz_scene* scene, const rz_scene_node* nodes, uint32_t n_nodes,
+                               double flatness, const float bg[4], float* canvas, uint8_t* rgba8, uint32_t width,
+                               uint32_t height) {
+    if (!ctx) return RZ_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    rz_status st = check_scene(ctx, scene, flatness, width, height);
+    if (st) return st;
+    if ((!nodes && n_nodes) || (!canvas && !rgba8)) return fail(ctx, RZ_ERR_INVALID, "null argument");
+    RZ_CUDA(cudaSetDevice(ctx->device));
+    Trace tr("rz_render_scene_tree");
+    SceneTree T;
+    T.sc = scene;
+    T.nodes = nodes;
+    T.n = n_nodes;
+    T.end.assign(n_nodes, 0);
+    if (n_nodes) {
+        uint32_t e = 0;
+        st = parse_tree(ctx, T, 0, 0, e);
+        if (st) return st;
+        if (e != n_nodes) return fail(ctx, RZ_ERR_INVALID, "scene tree: nodes after the root's subtree");
+    }
+    st = stage_scene_segments(ctx, scene->seg_kind, scene->seg_pts, scene->n_segments, scene->subpath_off,
+                              scene->n_subpaths, scene->fill_subpath_off, scene->n_fills, T.base, T.fsub);
+    if (st) return st;
+    tr.mark("stage_segments");
+    // Pipeline::build with view = the canvas, tr = identity (src/scene.rs:186-199)
+    const int W = (int)width, H = (int)height;
+    int root = -1;
+    if (n_nodes) root = build_rec(T, 0, OptBox{true, rzhost::Box{0.0, 0.0, (double)W, (double)H}}, kIdentity);
+    tr.mark("build");
+    // the root layer is the view: Layer::new(view, bg)
+    const uint64_t n = (uint64_t)W * (uint64_t)H;
+    if (n == 0) return RZ_OK;
+    RZ_CUDA(ctx->p_canvas.ensure(n * 16 + 16));
+    LayerState R;
+    R.w = W;
+    R.h = H;
+    R.buf = (float*)ctx->p_canvas.p;
+    const float zero[4] = {0.f, 0.f, 0.f, 0.f};
+    RZ_CUDA(rz::launch_layer_fill(R.buf, n, bg ? bg : zero, ctx->stream));
+    layer_begin(T, R);
+    if (root >= 0) {
+        st = render_rec(ctx, T, root, R, 0, flatness);
+        if (st) return st;
+        st = layer_flush(ctx, R, flatness);
+        if (st) return st;
+    }
+    tr.mark("render");
+    if (canvas) {
+        st = copy_out_bytes(ctx, canvas, R.buf, n * 16);
+        if (st) return st;
+    }
+    if (rgba8) {
+        RZ_CUDA(ctx->p_rgba8.ensure(n * 4 + 16));
+        RZ_CUDA(rz::launch_encode_rgba8(R.buf, (uint8_t*)ctx->p_rgba8.p, n, ctx->stream));
+        st = copy_out_bytes(ctx, rgba8, ctx->p_rgba8.p, n * 4);
+        if (st) return st;
+    }
+    tr.mark("copy_out");
+    return read_error(ctx);
 }
 
 rz_status rz_encode_rgba8(rz_ctx* ctx, const float* canvas, uint64_t n_pixels, uint8_t* rgba8, int32_t memory) {

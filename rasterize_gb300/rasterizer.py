@@ -198,49 +198,165 @@ class MaskBatch:
 
 
 class Scene:
-    """A group of fills drawn in order (the reference's ``Scene::group`` of
-    ``Scene::fill`` nodes, src/scene.rs:69-200), rendered by
-    ``GpuRasterizer.render_scene`` like ``Scene::render`` with view = canvas."""
+    """A scene tree (SceneInner, src/scene.rs:19-62).  A Scene made with
+    ``Scene()`` is a Group: ``fill`` appends a Fill (with the fill's own
+    transform) and ``add`` a child scene; ``opacity``, ``clip`` and
+    ``transform`` wrap a scene like the reference's builders (src/scene.rs:85-150,
+    nested opacities and transforms merged, a group of one child is the child).
+    ``GpuRasterizer.render_scene`` renders it like ``Scene::render`` with
+    view = canvas: a Group of Fills goes through ``rz_render_scene``, anything
+    else through ``rz_render_scene_tree``."""
 
-    def __init__(self):
-        self.fills = []  # (path, transform, fill_rule, paint)
+    def __init__(self, kind: str = "group", children=None, **params):
+        self.kind = kind
+        self.children = list(children or [])  # fills as (path, tr, rule, paint) tuples, or Scenes
+        self.params = params
         self._packed = None
 
+    # ---- builders
     def fill(self, path: Path, paint, tr: Transform | None = None, fill_rule: FillRule = FillRule.NonZero):
-        self.fills.append((path, tr or Transform.identity(), FillRule(fill_rule), paint))
+        """Appends a Fill to this Group (``tr``: the fill's own transform)."""
+        if self.kind != "group":
+            raise TypeError("fill() appends to a group")
+        self.children.append((path, tr or Transform.identity(), FillRule(fill_rule), paint))
         self._packed = None
         return self
 
+    def add(self, child: "Scene"):
+        """Appends a child scene to this Group."""
+        if self.kind != "group":
+            raise TypeError("add() appends to a group")
+        self.children.append(child)
+        self._packed = None
+        return self
+
+    @staticmethod
+    def group(children) -> "Scene":
+        """Scene::group (src/scene.rs:101-107): one child is the child itself."""
+        children = list(children)
+        if len(children) == 1 and isinstance(children[0], Scene):
+            return children[0]
+        return Scene("group", children)
+
+    def opacity(self, opacity: float) -> "Scene":
+        """Scene::opacity (src/scene.rs:110-125): clamped to [0, 1], nested opacities multiply."""
+        opacity = min(max(float(opacity), 0.0), 1.0)
+        if self.kind == "opacity":
+            return self.children[0].opacity(opacity * self.params["opacity"])
+        return Scene("opacity", [self], opacity=opacity)
+
+    def clip(self, path: Path, units=_paint.Units.UserSpaceOnUse, fill_rule: FillRule = FillRule.NonZero) -> "Scene":
+        """Scene::clip (src/scene.rs:128-136)."""
+        return Scene("clip", [self], path=path, units=int(units), rule=FillRule(fill_rule))
+
+    def transform(self, tr: Transform) -> "Scene":
+        """Scene::transform (src/scene.rs:139-150): nested transforms compose."""
+        if self.kind == "transform":
+            return self.children[0].transform(tr * self.params["tr"])
+        return Scene("transform", [self], tr=tr)
+
+    # ---- views
+    @property
+    def fills(self):
+        """Every Fill in drawing order as (path, tr, rule, paint)."""
+        if self.kind == "group" and all(isinstance(c, tuple) for c in self.children):
+            return self.children
+        out = []
+        for c in self.children:
+            out.extend([c] if isinstance(c, tuple) else c.fills)
+        return out
+
+    def is_flat(self) -> bool:
+        return self.kind == "group" and all(isinstance(c, tuple) for c in self.children)
+
+    def entries_and_nodes(self):
+        """The fill entries (fills in drawing order, then clip paths with a
+        transparent paint) and the pre-order node list of rz_render_scene_tree."""
+        entries, nodes = [], []
+
+        def walk(sc):
+            if isinstance(sc, tuple):
+                nodes.append(("fill", len(entries)))
+                entries.append(sc)
+                return
+            if sc.kind == "group":
+                nodes.append(("group", len(sc.children)))
+                for c in sc.children:
+                    walk(c)
+            elif sc.kind == "opacity":
+                nodes.append(("opacity", sc.params["opacity"]))
+                walk(sc.children[0])
+            elif sc.kind == "transform":
+                nodes.append(("transform", sc.params["tr"]))
+                walk(sc.children[0])
+            else:
+                i = len(nodes)
+                nodes.append(None)
+                clip_entry = (sc.params["path"], Transform.identity(), sc.params["rule"], _paint.LinColor(0, 0, 0, 0))
+                walk(sc.children[0])
+                nodes[i] = ("clip", clip_entry, sc.params["units"])
+
+        walk(self)
+        # clip paths become entries after the fills
+        out = (_ffi.RzSceneNode * max(len(nodes), 1))()
+        for i, nd in enumerate(nodes):
+            k = nd[0]
+            if k == "fill":
+                out[i].kind, out[i].arg = _ffi.NODE_FILL, nd[1]
+            elif k == "group":
+                out[i].kind, out[i].arg = _ffi.NODE_GROUP, nd[1]
+            elif k == "opacity":
+                out[i].kind, out[i].opacity = _ffi.NODE_OPACITY, nd[1]
+            elif k == "transform":
+                out[i].kind = _ffi.NODE_TRANSFORM
+                for j in range(6):
+                    out[i].tr[j] = nd[1].m[j]
+            else:
+                out[i].kind, out[i].arg, out[i].units = _ffi.NODE_CLIP, len(entries), nd[2]
+                entries.append(nd[1])
+        return entries, out, len(nodes)
+
     def pack(self):
-        """(rz_scene struct, keepalive) over host arrays, built once per
-        set of fills (``fill`` invalidates it)."""
-        if self._packed is not None and self._packed[2] == len(self.fills):
+        """(rz_scene struct, keepalive) over host arrays; for a tree also the
+        node array: (struct, keepalive, nodes, n_nodes)."""
+        key = (len(self.children), self.is_flat())
+        if self._packed is not None and self._packed[2] == key:
             return self._packed[0], self._packed[1]
-        paths = [f[0] for f in self.fills]
-        n = len(paths)
-        kind = np.ascontiguousarray(np.concatenate([p.kind for p in paths]) if n else np.zeros(0, np.uint8))
-        pts = np.ascontiguousarray(np.concatenate([p.pts for p in paths]) if n else np.zeros((0, 8)))
-        nseg = np.array([p.n_segments for p in paths], dtype=np.int64)
-        seg_base = np.concatenate([[0], np.cumsum(nseg)[:-1]]) if n else np.zeros(0, np.int64)
-        parts = [np.zeros(1, np.int64)] + [p.subpath_off[1:].astype(np.int64) + b for p, b in zip(paths, seg_base)]
-        sub = np.ascontiguousarray(np.concatenate(parts).astype(np.uint32))
-        nsub = np.array([len(p.subpath_off) - 1 for p in paths], dtype=np.int64)
-        fsub = np.ascontiguousarray(np.concatenate([[0], np.cumsum(nsub)]).astype(np.uint32))
-        trs = np.ascontiguousarray(np.array([f[1].m for f in self.fills], dtype=np.float64).reshape(-1))
-        rules = np.ascontiguousarray(np.array([int(f[2]) for f in self.fills], dtype=np.uint8))
-        structs, keep = [], []
-        for f in self.fills:
-            st, k = _paint.to_struct(f[3])
-            structs.append(st)
-            keep.append(k)
-        paints = (_paint.RzPaint * max(n, 1))(*structs)
-        fpaint = np.ascontiguousarray(np.arange(n, dtype=np.uint32))
-        s = _ffi.RzScene(n, int(kind.shape[0]), len(sub) - 1, n, kind.ctypes.data, pts.ctypes.data, sub.ctypes.data,
-                         fsub.ctypes.data, trs.ctypes.data if n else None, rules.ctypes.data if n else None,
-                         fpaint.ctypes.data if n else None, ctypes.addressof(paints))
-        keepalive = (kind, pts, sub, fsub, trs, rules, fpaint, paints, keep)
-        self._packed = (s, keepalive, n)
-        return s, keepalive
+        if self.is_flat():
+            entries, nodes, n_nodes = self.children, None, 0
+        else:
+            entries, nodes, n_nodes = self.entries_and_nodes()
+        s, keep = _pack_entries(entries)
+        keep = (keep, nodes, n_nodes)
+        self._packed = (s, keep, key)
+        return s, keep
+
+
+def _pack_entries(entries):
+    """rz_scene over fill entries (path, tr, rule, paint)."""
+    paths = [f[0] for f in entries]
+    n = len(paths)
+    kind = np.ascontiguousarray(np.concatenate([p.kind for p in paths]) if n else np.zeros(0, np.uint8))
+    pts = np.ascontiguousarray(np.concatenate([p.pts for p in paths]) if n else np.zeros((0, 8)))
+    nseg = np.array([p.n_segments for p in paths], dtype=np.int64)
+    seg_base = np.concatenate([[0], np.cumsum(nseg)[:-1]]) if n else np.zeros(0, np.int64)
+    parts = [np.zeros(1, np.int64)] + [p.subpath_off[1:].astype(np.int64) + b for p, b in zip(paths, seg_base)]
+    sub = np.ascontiguousarray(np.concatenate(parts).astype(np.uint32))
+    nsub = np.array([len(p.subpath_off) - 1 for p in paths], dtype=np.int64)
+    fsub = np.ascontiguousarray(np.concatenate([[0], np.cumsum(nsub)]).astype(np.uint32))
+    trs = np.ascontiguousarray(np.array([f[1].m for f in entries], dtype=np.float64).reshape(-1))
+    rules = np.ascontiguousarray(np.array([int(f[2]) for f in entries], dtype=np.uint8))
+    structs, keep = [], []
+    for f in entries:
+        st, k = _paint.to_struct(f[3])
+        structs.append(st)
+        keep.append(k)
+    paints = (_paint.RzPaint * max(n, 1))(*structs)
+    fpaint = np.ascontiguousarray(np.arange(n, dtype=np.uint32))
+    s = _ffi.RzScene(n, int(kind.shape[0]), len(sub) - 1, n, kind.ctypes.data, pts.ctypes.data, sub.ctypes.data,
+                     fsub.ctypes.data, trs.ctypes.data if n else None, rules.ctypes.data if n else None,
+                     fpaint.ctypes.data if n else None, ctypes.addressof(paints))
+    return s, (kind, pts, sub, fsub, trs, rules, fpaint, paints, keep)
 
 
 def _tune_key(device: str, batch: "MaskBatch", flatness: float) -> str:
@@ -377,28 +493,41 @@ class GpuRasterizer(Rasterizer):
         self.ctx.check(lib.rz_fill(self.ctx.ptr, ctypes.byref(ps), tr_a.ctypes.data, int(fill_rule), self.flatness,
                                    ctypes.addressof(pst), img.ctypes.data, shape))
 
-    def render_scene(self, scene: Scene, width: int, height: int, bg=None) -> np.ndarray:
-        """Scene::render over a (height, width, 4) float32 canvas initialised to bg."""
-        s, keep = scene.pack()
+    def render_scene(self, scene: Scene, width: int, height: int, bg=None, tree: bool | None = None) -> np.ndarray:
+        """Scene::render over a (height, width, 4) float32 canvas initialised to bg
+        (``tree=True`` sends a flat group through the scene-tree path too)."""
         canvas = np.zeros((height, width, 4), dtype=np.float32)
-        bg_a = np.ascontiguousarray(bg, dtype=np.float32) if bg is not None else None
-        lib = self.ctx.lib
-        self.ctx.check(lib.rz_render_scene(self.ctx.ptr, ctypes.byref(s), self.flatness,
-                                           bg_a.ctypes.data if bg_a is not None else None, canvas.ctypes.data,
-                                           width, height))
+        self._render(scene, width, height, bg, canvas, None, tree)
         return canvas
 
-    def render_scene_rgba8(self, scene: Scene, width: int, height: int, bg=None) -> np.ndarray:
+    def render_scene_rgba8(self, scene: Scene, width: int, height: int, bg=None, tree: bool | None = None) -> np.ndarray:
         """Scene::render, then `to_rgba` of every pixel: (height, width, 4) uint8
-        sRGB, encoded in the composite's epilogue on the GPU."""
-        s, keep = scene.pack()
+        sRGB, encoded on the GPU (in the composite's epilogue for a flat group)."""
         out = np.zeros((height, width, 4), dtype=np.uint8)
-        bg_a = np.ascontiguousarray(bg, dtype=np.float32) if bg is not None else None
-        lib = self.ctx.lib
-        self.ctx.check(lib.rz_render_scene_rgba8(self.ctx.ptr, ctypes.byref(s), self.flatness,
-                                                 bg_a.ctypes.data if bg_a is not None else None, out.ctypes.data,
-                                                 width, height))
+        self._render(scene, width, height, bg, None, out, tree)
         return out
+
+    def _render(self, scene, width, height, bg, canvas, rgba8, tree):
+        bg_a = np.ascontiguousarray(bg, dtype=np.float32) if bg is not None else None
+        bg_p = bg_a.ctypes.data if bg_a is not None else None
+        lib = self.ctx.lib
+        if tree is None:
+            tree = not scene.is_flat()
+        if not tree:
+            s, keep = scene.pack()
+            if canvas is not None:
+                self.ctx.check(lib.rz_render_scene(self.ctx.ptr, ctypes.byref(s), self.flatness, bg_p,
+                                                   canvas.ctypes.data, width, height))
+            else:
+                self.ctx.check(lib.rz_render_scene_rgba8(self.ctx.ptr, ctypes.byref(s), self.flatness, bg_p,
+                                                         rgba8.ctypes.data, width, height))
+            return
+        entries, nodes, n_nodes = scene.entries_and_nodes()
+        s, keep = _pack_entries(entries)
+        self.ctx.check(lib.rz_render_scene_tree(self.ctx.ptr, ctypes.byref(s), ctypes.addressof(nodes), n_nodes,
+                                                self.flatness, bg_p,
+                                                canvas.ctypes.data if canvas is not None else None,
+                                                rgba8.ctypes.data if rgba8 is not None else None, width, height))
 
     def encode_rgba8(self, canvas: np.ndarray) -> np.ndarray:
         """`to_rgba` of premultiplied linear RGBA f32 pixels (..., 4) -> uint8 (..., 4)."""

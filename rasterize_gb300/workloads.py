@@ -155,8 +155,8 @@ def random_paint(rng, cx, cy, size, linear_colors=True):
     return GradRadial(stops, (cx, cy), float(R), fc, fr, Units.UserSpaceOnUse, linear_colors, spread)
 
 
-def contour(rng, n_seg, radius, p_cubic=0.5):
-    """Star-shaped closed outline around the origin: cubic or line segments."""
+def contour(rng, n_seg, radius, p_cubic=0.5, center=(0.0, 0.0)):
+    """Star-shaped closed outline around ``center`` (the origin by default): cubic or line segments."""
     ang = np.sort(rng.uniform(0.0, 2.0 * math.pi, n_seg))
     rad = radius * rng.uniform(0.55, 1.0, n_seg)
     v = np.stack([rad * np.cos(ang), rad * np.sin(ang)], axis=1)
@@ -172,6 +172,10 @@ def contour(rng, n_seg, radius, p_cubic=0.5):
     pts[cub, 4:6] = c2[cub]
     pts[cub, 6:8] = b[cub]
     pts[~cub, 2:4] = b[~cub]
+    if center[0] or center[1]:
+        pts[:, 0:2] += center
+        pts[cub, 2:8] += np.tile(np.asarray(center, dtype=np.float64), 3)
+        pts[~cub, 2:4] += center
     return _path_from_arrays(kinds, pts)
 
 
@@ -197,6 +201,48 @@ def scene(seed: int = 3, n: int = 2000, size: int = 2048, seg_range=(20, 2000), 
         paint = random_paint(rng, 0.0, 0.0, 2 * r, linear_colors)
         sc.fill(path, paint, tr, FillRule.NonZero)
     return sc
+
+
+def scene_tree(seed: int = 6, n_groups: int = 40, fills_per_group: int = 10, size: int = 512, seg_range=(20, 200),
+               radius_range=(8, 64), linear_colors=True):
+    """A layered scene: ``n_groups`` groups of ``fills_per_group`` fills (as
+    ``scene``), each group either plain, under Opacity U[0.2, 0.95], clipped by
+    a star path (UserSpaceOnUse or BoundingBox units, NonZero or EvenOdd), or a
+    clip inside an opacity; every third group under an extra Transform node
+    (a small rotation about the canvas centre)."""
+    from .paint import Units
+    from .rasterizer import Scene
+    rng = np.random.default_rng(seed)
+    root = Scene()
+    for g in range(n_groups):
+        grp = Scene()
+        gx, gy = rng.uniform(0.1 * size, 0.9 * size, 2)
+        for _ in range(fills_per_group):
+            nseg = int(round(math.exp(rng.uniform(math.log(seg_range[0]), math.log(seg_range[1])))))
+            r = math.exp(rng.uniform(math.log(radius_range[0]), math.log(radius_range[1])))
+            path = contour(rng, nseg, r)
+            s = rng.uniform(0.5, 2.0)
+            ang = rng.uniform(0, 2 * math.pi)
+            cx, cy = np.array([gx, gy]) + rng.normal(0, 0.08 * size, 2)
+            tr = Transform.new_translate(cx, cy) * Transform.new_rotate(ang) * Transform.new_scale(s, s)
+            grp.fill(path, random_paint(rng, 0.0, 0.0, 2 * r, linear_colors), tr, FillRule.NonZero)
+        mode = g % 4
+        node = grp
+        if mode in (2, 3):
+            units = Units(int(rng.integers(2)))
+            if units == Units.BoundingBox:
+                clip = contour(rng, 24, 0.5, center=(0.5, 0.5))  # in the unit square of the group's bbox
+            else:
+                clip = contour(rng, 24, rng.uniform(0.1, 0.25) * size, center=(gx, gy))
+            node = node.clip(clip, units, FillRule(int(rng.integers(2))))
+        if mode in (1, 3):
+            node = node.opacity(rng.uniform(0.2, 0.95))
+        if g % 3 == 2:
+            c = size / 2.0
+            node = node.transform(Transform.new_translate(c, c) * Transform.new_rotate(rng.uniform(-0.2, 0.2))
+                                  * Transform.new_translate(-c, -c))
+        root.add(node)
+    return root
 
 
 def diff_batch(seed: int = 4, n_images: int = 64, paths: int = 256, segs: int = 32, size: int = 1024,

@@ -22,3 +22,21 @@ def oracle_scene(sc, width, height, bg=(0, 0, 0, 0)):
     rules = [f[2] for f in sc.fills]
     paints = [oracle_paint(f[3]) for f in sc.fills]
     return O.scene_render(paths, trs, rules, paints, width, height, bg=bg)
+
+
+def oracle_tree(sc):
+    """The oracle's nested-tuple form of a product Scene tree."""
+    if isinstance(sc, tuple):
+        path, tr, rule, paint = sc
+        return ("fill", path, tr, int(rule), oracle_paint(paint))
+    if sc.kind == "group":
+        return ("group", [oracle_tree(c) for c in sc.children])
+    if sc.kind == "opacity":
+        return ("opacity", oracle_tree(sc.children[0]), sc.params["opacity"])
+    if sc.kind == "transform":
+        return ("transform", oracle_tree(sc.children[0]), sc.params["tr"])
+    return ("clip", oracle_tree(sc.children[0]), sc.params["path"], int(sc.params["units"]), int(sc.params["rule"]))
+
+
+def oracle_scene_tree(sc, width, height, bg=(0, 0, 0, 0)):
+    return O.scene_tree_render(oracle_tree(sc), width, height, bg=bg)

@@ -1,0 +1,97 @@
+"""GPU parity of scene trees (rz_render_scene_tree): Opacity and Clip layers,
+Transform and Group nodes, against the oracle's restatement of
+Pipeline::build_rec / render_rec / Layer::compose (src/scene.rs:153-565)."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from rasterize_gb300 import FillRule, GpuRasterizer, LinColor, RasterizeError, Scene, Transform, Units
+from rasterize_gb300 import workloads as W
+from tests.paint_oracle import oracle_scene_tree
+
+pytestmark = pytest.mark.gpu
+
+TOL = 2e-4  # per colour channel, as the flat scenes (clip masks add their own 1e-4 at most)
+
+
+@pytest.fixture(scope="module")
+def R():
+    return GpuRasterizer()
+
+
+def assert_close(gpu, ref, tol=TOL):
+    err = np.abs(gpu.astype(np.float64) - ref.astype(np.float64))
+    i = np.unravel_index(err.argmax(), err.shape)
+    assert err.max() <= tol, "max err %.3g at %s: gpu %r ref %r" % (err.max(), i, gpu[i], ref[i])
+
+
+def test_flat_group_through_the_tree_path_is_identical(R):
+    sc = W.scene(seed=5, n=40, size=256, seg_range=(20, 200), radius_range=(8, 64))
+    bg = (0.1, 0.1, 0.12, 1.0)
+    assert np.array_equal(R.render_scene(sc, 256, 200, bg=bg, tree=True), R.render_scene(sc, 256, 200, bg=bg))
+
+
+@pytest.mark.parametrize("seed", [6, 7])
+def test_layered_scene_matches_oracle(R, seed):
+    st = W.scene_tree(seed=seed, n_groups=16, fills_per_group=6, size=256)
+    bg = (0.0, 0.0, 0.0, 1.0)
+    assert_close(R.render_scene(st, 256, 256, bg=bg), oracle_scene_tree(st, 256, 256, bg=bg))
+
+
+def test_opacity_clip_nesting_and_units(R):
+    rng = np.random.default_rng(3)
+    paint = [LinColor(0.8, 0.2, 0.1, 1.0), LinColor(0.1, 0.5, 0.2, 0.7), LinColor(0.0, 0.2, 0.6, 0.9)]
+    inner = Scene()
+    for i in range(3):
+        inner.fill(W.contour(rng, 20, 30.0, center=(40.0 + 25 * i, 50.0)), paint[i])
+    clip_u = W.contour(rng, 16, 35.0, center=(70.0, 55.0))
+    clip_b = W.contour(rng, 16, 0.45, center=(0.5, 0.5))
+    root = Scene()
+    root.fill(W.contour(rng, 30, 60.0, center=(64.0, 64.0)), LinColor(0.2, 0.2, 0.2, 1.0))
+    root.add(inner.clip(clip_u, Units.UserSpaceOnUse, FillRule.NonZero).opacity(0.6))
+    root.add(inner.clip(clip_b, Units.BoundingBox, FillRule.EvenOdd)
+             .transform(Transform.new_translate(10, 30)))
+    root.add(inner.opacity(0.5).clip(clip_u, fill_rule=FillRule.EvenOdd).opacity(0.8))
+    bg = (1.0, 1.0, 1.0, 1.0)
+    assert_close(R.render_scene(root, 160, 128, bg=bg), oracle_scene_tree(root, 160, 128, bg=bg))
+
+
+def test_nodes_out_of_view_and_empty_groups(R):
+    far = Scene().fill(W.contour(np.random.default_rng(0), 8, 5.0, center=(900.0, 900.0)), LinColor(1, 1, 1, 1))
+    root = Scene().add(far.opacity(0.5)).add(Scene()).add(
+        Scene().fill(W.contour(np.random.default_rng(1), 8, 10.0, center=(16.0, 8.0)), LinColor(1, 0, 0, 1))
+        .clip(W.contour(np.random.default_rng(2), 8, 3.0, center=(500.0, 8.0))))
+    bg = (0.25, 0.0, 0.0, 1.0)
+    got = R.render_scene(root, 32, 16, bg=bg)
+    assert (got == np.float32(bg)).all()
+    assert_close(got, oracle_scene_tree(root, 32, 16, bg=bg))
+
+
+def test_tree_rgba8_is_the_encoded_canvas(R):
+    st = W.scene_tree(seed=8, n_groups=8, fills_per_group=4, size=128)
+    canvas = R.render_scene(st, 128, 100, bg=(0, 0, 0, 1))
+    assert (R.render_scene_rgba8(st, 128, 100, bg=(0, 0, 0, 1)) == O.encode_rgba8(canvas)).all()
+
+
+def test_invalid_trees_are_rejected(R):
+    import ctypes
+    from rasterize_gb300 import _ffi
+    from rasterize_gb300.rasterizer import _pack_entries
+    s, keep = _pack_entries([(W.contour(np.random.default_rng(0), 8, 5.0, center=(8.0, 8.0)), Transform.identity(),
+                              FillRule.NonZero, LinColor(1, 1, 1, 1))])
+    canvas = np.zeros((16, 16, 4), dtype=np.float32)
+    lib = R.ctx.lib
+
+    def call(nodes):
+        arr = (_ffi.RzSceneNode * len(nodes))()
+        for i, (k, a) in enumerate(nodes):
+            arr[i].kind, arr[i].arg = k, a
+        return lib.rz_render_scene_tree(R.ctx.ptr, ctypes.byref(s), ctypes.addressof(arr), len(nodes), 0.05, None,
+                                        canvas.ctypes.data, None, 16, 16)
+
+    assert call([(_ffi.NODE_FILL, 0)]) == 0
+    assert call([(_ffi.NODE_FILL, 1)]) == 2          # entry out of range
+    assert call([(_ffi.NODE_GROUP, 2), (_ffi.NODE_FILL, 0)]) == 2  # children run past the array
+    assert call([(_ffi.NODE_FILL, 0), (_ffi.NODE_FILL, 0)]) == 2   # nodes after the root's subtree
+    assert call([(9, 0)]) == 2
+    assert call([(_ffi.NODE_OPACITY, 0)]) == 2       # opacity without its child
