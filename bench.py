@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="bounded CPU baseline sample")
     ap.add_argument("--no-per-path", action="store_true")
     ap.add_argument("--no-configs", action="store_true", help="skip the C1/C2/C4/C5 legs")
-    ap.add_argument("--workload", default="glyphs", choices=["glyphs", "small_path", "large_path", "scene", "diff", "encode"],
+    ap.add_argument("--workload", default="glyphs", choices=["glyphs", "small_path", "large_path", "scene", "diff", "encode", "scene_tree"],
                     help="glyphs: the headline line; the others run one configuration leg alone")
     ap.add_argument("--diff-images", type=int, default=64, help="images of the diff workload")
     ap.add_argument("--fd-coords", type=int, default=100, help="finite-difference coordinates of the diff workload")
@@ -240,7 +240,8 @@ def run_configs(R, stream):
     host buffers (the ``gpu`` timing) and a CPU-baseline leg that times the
     oracle on the same input once and reports the GPU's error against it."""
     return {"C1_small_path": run_small(R, stream), "C2_large_path": run_large(R, stream),
-            "C4_scene": run_scene(R, stream), "C5_diff": run_diff(R, stream), "encode": run_encode(R, stream)}
+            "C4_scene": run_scene(R, stream), "C5_diff": run_diff(R, stream), "encode": run_encode(R, stream),
+            "scene_tree": run_scene_tree(R, stream)}
 
 
 def run_small(R, stream):
@@ -318,6 +319,29 @@ def run_scene(R, stream, n=2000, size=2048):
             "rgba8_ms": round(ms8, 3), "rgba8_err_lsb": {"max": int(lsb.max()), "frac_off": float((lsb > 0).mean())},
             "cpu_baseline_ms": round(cpu_s * 1e3, 1), "cores": 1,
             "note": "error per colour channel; host canvas in and out; rgba8: sRGB8 bytes out, encode fused"}
+
+
+def run_scene_tree(R, stream, n_groups=200, fills_per_group=10, size=2048):
+    """Layered scene: 200 groups of 10 fills on a 2048^2 RGBA f32 canvas, a
+    quarter plain, a quarter under Opacity, a quarter clipped, a quarter a clip
+    inside an opacity (every third group under a Transform node)."""
+    from rasterize_gb300 import workloads as W
+    from tests.paint_oracle import oracle_scene_tree
+    st = W.scene_tree(seed=6, n_groups=n_groups, fills_per_group=fills_per_group, size=size,
+                      seg_range=(20, 2000), radius_range=(8, 128))
+    out = {}
+
+    def run():
+        out["c"] = R.render_scene(st, size, size, bg=(0.0, 0.0, 0.0, 1.0))
+    run()
+    ms = _event_ms(stream, run, 5)
+    t = time.perf_counter()
+    ref = oracle_scene_tree(st, size, size, bg=(0.0, 0.0, 0.0, 1.0))
+    cpu_s = time.perf_counter() - t
+    return {"ms": round(ms, 3), "mpx_per_s": round(size * size / ms / 1e3, 1), "err": _config_err(out["c"], ref),
+            "cpu_baseline_ms": round(cpu_s * 1e3, 1), "cores": 1, "layers": n_groups // 2 + n_groups // 4,
+            "workload": "%d groups x %d fills, opacity / clip layers, %dx%d RGBA f32, host canvas in and out" %
+                        (n_groups, fills_per_group, size, size)}
 
 
 def run_encode(R, stream, size=8192):
@@ -490,7 +514,8 @@ def main():
         leg = {"small_path": lambda: run_small(R, stream), "large_path": lambda: run_large(R, stream),
                "scene": lambda: run_scene(R, stream, n=args.scene_fills),
                "diff": lambda: run_diff(R, stream, n_images=args.diff_images, fd_coords=args.fd_coords),
-               "encode": lambda: run_encode(R, stream)}[args.workload]()
+               "encode": lambda: run_encode(R, stream),
+               "scene_tree": lambda: run_scene_tree(R, stream)}[args.workload]()
         if rank == 0:
             print(json.dumps({"metric": METRIC, "workload": args.workload, "n_gpus": world, **leg}))
         return

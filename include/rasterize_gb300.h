@@ -227,6 +227,31 @@ RZ_API rz_status rz_fill(rz_ctx* ctx, const rz_path* path, const double tr[6], i
 RZ_API rz_status rz_render_scene(rz_ctx* ctx, const rz_scene* scene, double flatness, const float bg[4],
                                  float* canvas, uint32_t width, uint32_t height);
 
+/* ---- stroking ------------------------------------------------------------ */
+#define RZ_JOIN_MITER 0 /* LineJoin::Miter(miter_limit) (src/path.rs:78-95; default, limit 4) */
+#define RZ_JOIN_BEVEL 1
+#define RZ_JOIN_ROUND 2
+#define RZ_CAP_BUTT 0 /* LineCap (src/path.rs:103-117; default Butt) */
+#define RZ_CAP_SQUARE 1
+#define RZ_CAP_ROUND 2
+/* StrokeStyle (src/path.rs:121-137). */
+typedef struct rz_stroke_style {
+    double width;
+    double miter_limit; /* LineJoin::Miter's limit */
+    int32_t line_join;
+    int32_t line_cap;
+} rz_stroke_style;
+
+/* Host-only: Path::stroke (src/path.rs:374-415), the outline path of `path`
+ * stroked with `style` (path->closed says which subpaths are closed; NULL:
+ * all open).  Every outline subpath is closed.  Call once with NULL arrays
+ * for *n_segments / *n_subpaths, then with arrays of those sizes
+ * (subpath_off: n_subpaths + 1); smaller caps return RZ_ERR_CAPACITY.  Arcs
+ * are expanded first.  Needs no context or GPU. */
+RZ_API rz_status rz_stroke_path(const rz_path* path, const rz_stroke_style* style, uint8_t* seg_kind,
+                                double* seg_pts, uint32_t seg_cap, uint32_t* subpath_off, uint32_t sub_cap,
+                                uint32_t* n_segments, uint32_t* n_subpaths);
+
 /* ---- scene trees: groups, transforms, opacity and clip layers ----------- */
 /* One node of a scene tree (SceneInner, src/scene.rs:19-62), in pre-order: a
  * node, then the subtrees of its children.  Fill entries are those of the

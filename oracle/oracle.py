@@ -695,3 +695,34 @@ def scene_tree_render(tree, width, height, bg=(0, 0, 0, 0), flatness=0.05):
         img[:] = np.asarray(bg, dtype=np.float32)
         return img
     return _render(nodes, root, (0.0, 0.0, float(width), float(height)), bg, flatness)["img"]
+
+
+def stroke(path, width, line_join=0, miter_limit=4.0, line_cap=0):
+    """Path::stroke (src/path.rs:374-415): the outline as an OraclePath (every
+    subpath closed).  ``path`` carries ``closed`` flags per subpath (arcs
+    are expanded first, keeping the flag of the subpath they came from)."""
+    op, _, sub_map = expand_path(path, with_map=True)
+    closed_in = np.asarray(getattr(path, "closed", np.zeros(0)), dtype=np.uint8)
+    closed = np.ascontiguousarray(np.array([closed_in[s] if s < len(closed_in) else 0 for s in sub_map],
+                                           dtype=np.uint8))
+    L = lib()
+    if not hasattr(L, "_stroke_ready"):
+        L.rzo_stroke.restype = ctypes.c_long
+        L.rzo_stroke.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_long, ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
+                                                          ctypes.c_double, ctypes.c_int, ctypes.c_void_p,
+                                                          ctypes.c_void_p, ctypes.c_long, ctypes.c_void_p,
+                                                          ctypes.c_long, ctypes.POINTER(ctypes.c_long)]
+        L._stroke_ready = True
+    cap = max(64, 64 * len(op.kind))
+    while True:
+        okind = np.zeros(cap, dtype=np.uint8)
+        opts = np.zeros((cap, 8), dtype=np.float64)
+        osub = np.zeros(cap + 1, dtype=np.uint32)
+        nsub = ctypes.c_long(0)
+        n = L.rzo_stroke(_ptr(op.kind), _ptr(op.pts), _ptr(op.sub_off), op.nsub, _ptr(closed), float(width),
+                         int(line_join), float(miter_limit), int(line_cap), _ptr(okind), _ptr(opts), cap, _ptr(osub),
+                         cap + 1, ctypes.byref(nsub))
+        if n >= 0:
+            break
+        cap *= 4
+    return OraclePath(okind[:n].copy(), opts[:n].copy(), osub[:nsub.value + 1].copy())

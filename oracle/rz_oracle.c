@@ -781,6 +781,314 @@ int rzo_mask_ae(const uint8_t* kind, const double* pts, const uint32_t* sub_off,
 }
 
 /* ------------------------------------------------------------------------ */
+/* path.rs:374-415, 692-732 Path::stroke; curve.rs:977-1076 line_join /     */
+/* line_cap; curve.rs:1290-1433 offsets (Tiller-Hanson)                     */
+/* ------------------------------------------------------------------------ */
+typedef struct { seg* v; long n, cap; } segvec;
+static void sv_push(segvec* s, seg x) {
+    if (s->n == s->cap) { s->cap = s->cap ? 2 * s->cap : 16; s->v = (seg*)realloc(s->v, (size_t)s->cap * sizeof(seg)); }
+    s->v[s->n++] = x;
+}
+/* inserts b (all of it) at position at of a */
+static void sv_insert(segvec* a, long at, const segvec* b) {
+    for (long i = 0; i < b->n; i++) sv_push(a, b->v[0]);
+    memmove(a->v + at + b->n, a->v + at, (size_t)(a->n - b->n - at) * sizeof(seg));
+    memcpy(a->v + at, b->v, (size_t)b->n * sizeof(seg));
+}
+static pt p_sub(pt a, pt b) { pt r = { a.x - b.x, a.y - b.y }; return r; }
+static pt p_add(pt a, pt b) { pt r = { a.x + b.x, a.y + b.y }; return r; }
+static pt p_scale(double s, pt a) { pt r = { s * a.x, s * a.y }; return r; }
+static double p_dot(pt a, pt b) { return a.x * b.x + a.y * b.y; }           /* geometry.rs:155-159 */
+static double p_cross(pt a, pt b) { return a.x * b.y - a.y * b.x; }         /* geometry.rs:162-166 */
+static double p_length(pt a) { return hypot(a.x, a.y); }                     /* geometry.rs:144-147 */
+static int p_close(pt a, pt b) { return fabs(a.x - b.x) < RZO_EPSILON && fabs(a.y - b.y) < RZO_EPSILON; }
+static int p_normalize(pt a, pt* out) {                                      /* geometry.rs:175-183 */
+    double l = p_length(a);
+    if (l < RZO_EPSILON) return 0;
+    out->x = a.x / l; out->y = a.y / l;
+    return 1;
+}
+static seg mk_line(pt a, pt b) { seg s; memset(&s, 0, sizeof(s)); s.kind = SEG_LINE; s.p[0] = a; s.p[1] = b; return s; }
+static pt l_at(line_t l, double t) { pt r = { (1.0 - t) * l.a.x + t * l.b.x, (1.0 - t) * l.a.y + t * l.b.y }; return r; }
+/* Line::intersect curve.rs:204-215 */
+static int l_intersect(line_t s, line_t o, double* t0, double* t1) {
+    double x1 = s.a.x, y1 = s.a.y, x2 = s.b.x, y2 = s.b.y, x3 = o.a.x, y3 = o.a.y, x4 = o.b.x, y4 = o.b.y;
+    double det = (x4 - x3) * (y1 - y2) - (x1 - x2) * (y4 - y3);
+    if (fabs(det) < RZO_EPSILON) return 0;
+    *t0 = ((y3 - y4) * (x1 - x3) + (x4 - x3) * (y1 - y3)) / det;
+    *t1 = ((y1 - y2) * (x1 - x3) + (x2 - x1) * (y1 - y3)) / det;
+    return 1;
+}
+static int unit01(double t) { return t >= 0.0 && t <= 1.0; }
+/* Segment::ends curve.rs:195-197 (line), 377-388 (quad), 647-666 (cubic) */
+static void s_ends(const seg* s, line_t* start, line_t* end) {
+    const pt* p = s->p;
+    if (s->kind == SEG_LINE) { start->a = end->a = p[0]; start->b = end->b = p[1]; return; }
+    if (s->kind == SEG_QUAD) {
+        line_t a = { p[0], p[1] }, b = { p[1], p[2] };
+        if (p_close(p[0], p[1])) { *start = b; *end = b; }
+        else if (p_close(p[1], p[2])) { *start = a; *end = a; }
+        else { *start = a; *end = b; }
+        return;
+    }
+    int st = 0, en = 0;
+    for (int i = 0; i < 3; i++) if (!p_close(p[i], p[i + 1])) { st = i; break; }
+    for (int i = 3; i >= 1; i--) if (!p_close(p[i], p[i - 1])) { en = i; break; }
+    if (en == 0) en = 1;
+    start->a = p[st]; start->b = p[st + 1];
+    end->a = p[en - 1]; end->b = p[en];
+}
+/* line_offset curve.rs:1290-1295 */
+static int l_offset(line_t l, double dist, line_t* out) {
+    pt d = p_sub(l.b, l.a), nrm = { d.y, -d.x }, u;
+    if (!p_normalize(nrm, &u)) return 0;
+    pt off = p_scale(dist, u);
+    out->a = p_add(l.a, off); out->b = p_add(l.b, off);
+    return 1;
+}
+/* polyline_offset curve.rs:1302-1352 */
+static int polyline_offset(pt* ps, int n, double dist) {
+    if (n == 0) return 1;
+    int have = 0, index = 0;
+    line_t prev = { {0, 0}, {0, 0} };
+    for (;;) {
+        int repeats = 1;
+        for (int i = index; i < n - 1; i++) { if (!p_close(ps[i], ps[i + 1])) break; repeats++; }
+        if (index + repeats >= n) break;
+        index += repeats;
+        line_t src = { ps[index - 1], ps[index] }, next;
+        l_offset(src, dist, &next);
+        pt point = next.a;
+        double t0, t1;
+        if (have && l_intersect(prev, next, &t0, &t1)) point = l_at(prev, t0);
+        for (int i = index - repeats; i < index; i++) ps[i] = point;
+        prev = next;
+        have = 1;
+    }
+    if (!have) return 0;
+    for (int i = index; i < n; i++) ps[i] = prev.b;
+    return 1;
+}
+static double diag_length(const seg* s) {  /* bbox(None).diag().length() */
+    bbox_t b = seg_bbox(s, NULL);
+    return p_length(p_sub(b.min, b.max));
+}
+/* quad_offset_should_split curve.rs:1355-1368 */
+static int quad_split_needed(const seg* q) {
+    pt p0 = q->p[0], p1 = q->p[1], p2 = q->p[2];
+    if (p_dot(p_sub(p0, p1), p_sub(p2, p1)) > 0.0) return 1;
+    pt mass = { (p0.x + p1.x + p2.x) / 3.0, (p0.y + p1.y + p2.y) / 3.0 };
+    double dist = p_length(p_sub(mass, seg_at(q, 0.5)));
+    return diag_length(q) * 0.1 < dist;
+}
+/* cubic_offset_should_split curve.rs:1412-1431 */
+static int cubic_split_needed(const seg* c) {
+    pt p0 = c->p[0], p1 = c->p[1], p2 = c->p[2], p3 = c->p[3];
+    if (p_dot(p_sub(p3, p0), p_sub(p2, p1)) < 0.0) return 1;
+    double a0 = p_cross(p_sub(p3, p0), p_sub(p1, p0)), a1 = p_cross(p_sub(p3, p0), p_sub(p2, p0));
+    if (a0 * a1 < 0.0) return 1;
+    pt mass = { (p0.x + p1.x + p2.x + p3.x) / 4.0, (p0.y + p1.y + p2.y + p3.y) / 4.0 };
+    double dist = p_length(p_sub(mass, seg_at(c, 0.5)));
+    return diag_length(c) * 0.1 < dist;
+}
+typedef struct { double width, miter; int join, cap; } stroke_t;
+enum { J_MITER = 0, J_BEVEL = 1, J_ROUND = 2 };
+enum { C_BUTT = 0, C_SQUARE = 1, C_ROUND = 2 };
+/* Segment::line_join curve.rs:977-1047 */
+static void line_join(const seg* self, const seg* other, const stroke_t* st, segvec* out) {
+    pt e = seg_end(self), s = seg_start(other);
+    if (p_close(e, s)) return;
+    seg bevel = mk_line(e, s);
+    line_t t0l, start, end, t1l;
+    s_ends(self, &t0l, &start);
+    s_ends(other, &end, &t1l);
+    double t0, t1;
+    if (st->join == J_BEVEL) { sv_push(out, bevel); return; }
+    if (st->join == J_MITER) {
+        if (!l_intersect(start, end, &t0, &t1) || (unit01(t0) && unit01(t1))) { sv_push(out, bevel); return; }
+        pt p0 = p_sub(start.b, start.a), p1 = p_sub(end.a, end.b);
+        double lengths = p_length(p0) * p_length(p1);             /* cos_between geometry.rs:196-203 */
+        if (lengths < RZO_EPSILON) { sv_push(out, bevel); return; }
+        double c = p_dot(p0, p1) / lengths;
+        double miter_length = st->width / sqrt((1.0 - c) / 2.0);
+        if (miter_length < st->miter) {
+            pt p = l_at(start, t0);
+            sv_push(out, mk_line(start.b, p));
+            sv_push(out, mk_line(p, end.a));
+        } else {
+            sv_push(out, bevel);
+        }
+        return;
+    }
+    if (l_intersect(start, end, &t0, &t1) && unit01(t0) && unit01(t1)) { sv_push(out, bevel); return; }
+    int sweep = p_cross(p_sub(start.b, start.a), p_sub(s, e)) >= 0.0;
+    double r = st->width / 2.0, cub[64];
+    int n = rzo_arc_to_cubics(start.b.x, start.b.y, end.a.x, end.a.y, r, r, 0.0, 0, sweep, cub, 8);
+    if (n < 0) { sv_push(out, bevel); return; }
+    for (int i = 0; i < n; i++) {
+        seg c; c.kind = SEG_CUBIC;
+        for (int j = 0; j < 4; j++) { c.p[j].x = cub[8 * i + 2 * j]; c.p[j].y = cub[8 * i + 2 * j + 1]; }
+        sv_push(out, c);
+    }
+}
+/* Segment::line_cap curve.rs:1050-1076 */
+static void line_cap(const seg* self, const seg* other, const stroke_t* st, segvec* out) {
+    pt e = seg_end(self), s = seg_start(other);
+    if (p_close(e, s)) return;
+    if (st->cap == C_BUTT) { sv_push(out, mk_line(e, s)); return; }
+    if (st->cap == C_SQUARE) {
+        line_t t0l, from;
+        s_ends(self, &t0l, &from);
+        pt tang;
+        if (p_normalize(p_sub(from.b, from.a), &tang)) {
+            seg l0 = mk_line(e, p_add(e, p_scale(st->width / 2.0, tang)));
+            seg l1 = mk_line(l0.p[1], p_add(l0.p[1], p_sub(s, e)));
+            sv_push(out, l0);
+            sv_push(out, l1);
+            sv_push(out, mk_line(l1.p[1], s));
+        }
+        return;
+    }
+    stroke_t r = *st;
+    r.join = J_ROUND;
+    line_join(self, other, &r, out);
+}
+/* quad_offset_rec curve.rs:1371-1383 (split_at(0.5)) */
+static void quad_offset_rec(seg q, double dist, segvec* out, int depth) {
+    if (quad_split_needed(&q) && depth < 3) {
+        const pt* p = q.p;
+        double t = 0.5, t1 = t, t_1 = 1.0 - t, t2 = t1 * t1, t_2 = t_1 * t_1;
+        pt mid = { t_2 * p[0].x + 2.0 * t1 * t_1 * p[1].x + t2 * p[2].x,
+                   t_2 * p[0].y + 2.0 * t1 * t_1 * p[1].y + t2 * p[2].y };
+        seg a = q, b = q;
+        a.p[1].x = t_1 * p[0].x + t * p[1].x; a.p[1].y = t_1 * p[0].y + t * p[1].y; a.p[2] = mid;
+        b.p[0] = mid; b.p[1].x = t_1 * p[1].x + t * p[2].x; b.p[1].y = t_1 * p[1].y + t * p[2].y;
+        quad_offset_rec(a, dist, out, depth + 1);
+        quad_offset_rec(b, dist, out, depth + 1);
+        return;
+    }
+    if (polyline_offset(q.p, 3, dist)) sv_push(out, q);
+}
+/* cubic_offset_rec curve.rs:1386-1409 (Cubic::split) */
+static int cubic_offset_rec(seg c, int have_last, seg last, double dist, segvec* out, int depth, seg* res) {
+    if (cubic_split_needed(&c) && depth < 3) {
+        seg a, b, l;
+        seg_split(&c, &a, &b);
+        int h = cubic_offset_rec(a, have_last, last, dist, out, depth + 1, &l);
+        return cubic_offset_rec(b, h, l, dist, out, depth + 1, res);
+    }
+    seg r = c;
+    if (polyline_offset(r.p, 4, dist)) {
+        if (have_last && !p_close(seg_end(&last), seg_start(&r))) {
+            stroke_t st = { dist * 2.0, 0.0, J_ROUND, C_ROUND };
+            line_join(&last, &r, &st, out);
+        }
+        sv_push(out, r);
+        *res = r;
+        return 1;
+    }
+    *res = last;
+    return have_last;
+}
+static void seg_offset(const seg* s, double dist, segvec* out) {
+    if (s->kind == SEG_LINE) {
+        line_t l = { s->p[0], s->p[1] }, o;
+        if (l_offset(l, dist, &o)) sv_push(out, mk_line(o.a, o.b));
+    } else if (s->kind == SEG_QUAD) {
+        quad_offset_rec(*s, dist, out, 0);
+    } else {
+        seg last, res;
+        memset(&last, 0, sizeof(last));
+        cubic_offset_rec(*s, 0, last, dist, out, 0, &res);
+    }
+}
+/* stroke_segment path.rs:692-705 */
+static void stroke_segment(segvec* segs, const seg* s, const stroke_t* st, int cap) {
+    long offset = segs->n;
+    seg_offset(s, st->width / 2.0, segs);
+    if (offset != 0 && segs->n > offset) {
+        segvec j = { NULL, 0, 0 };
+        seg src = segs->v[offset - 1], dst = segs->v[offset];
+        if (cap) line_cap(&src, &dst, st, &j); else line_join(&src, &dst, st, &j);
+        if (j.n) sv_insert(segs, offset, &j);
+        free(j.v);
+    }
+}
+/* stroke_close path.rs:708-732 */
+static void stroke_close(pt sp_start, pt sp_end, segvec* segs, const stroke_t* st, int forward) {
+    if (segs->n == 0) return;
+    seg first = segs->v[0], last = segs->v[segs->n - 1];
+    line_t close = forward ? (line_t){ sp_end, sp_start } : (line_t){ sp_start, sp_end }, off;
+    if (l_offset(close, st->width / 2.0, &off) && p_length(p_sub(off.a, off.b)) * 100.0 > st->width) {
+        seg c = mk_line(off.a, off.b);
+        line_join(&last, &c, st, segs);
+        sv_push(segs, c);
+        line_join(&c, &first, st, segs);
+    } else {
+        line_join(&last, &first, st, segs);
+    }
+}
+static seg reversed(const seg* s) {
+    seg r = *s;
+    int n = seg_npts(s->kind);
+    for (int i = 0; i < n; i++) r.p[i] = s->p[n - 1 - i];
+    return r;
+}
+/* Path::stroke path.rs:374-415 of an arc-free path.  Writes up to seg_cap
+ * segments (kind, 8 doubles) and the subpath offsets (n_sub + 1); returns
+ * the segment count (and *n_sub), or -1 when a cap is too small. */
+long rzo_stroke(const uint8_t* kind, const double* pts, const uint32_t* sub_off, long nsub, const uint8_t* closed,
+                double width, int join, double miter, int cap, uint8_t* okind, double* opts, long seg_cap,
+                uint32_t* osub, long sub_cap, long* n_sub) {
+    stroke_t st = { width, miter, join, cap };
+    segvec segs = { NULL, 0, 0 }, fwd = { NULL, 0, 0 };
+    long nseg = 0, ns = 0;
+    if (sub_cap < 1) return -1;
+    osub[0] = 0;
+    for (long sp = 0; sp < nsub; sp++) {
+        fwd.n = 0;
+        for (uint32_t i = sub_off[sp]; i < sub_off[sp + 1]; i++) sv_push(&fwd, load_seg(kind, pts, i));
+        if (fwd.n == 0) continue;
+        int is_closed = closed && closed[sp];
+        pt sp_start = seg_start(&fwd.v[0]), sp_end = seg_end(&fwd.v[fwd.n - 1]);
+        for (long i = 0; i < fwd.n; i++) stroke_segment(&segs, &fwd.v[i], &st, 0);
+        long back = fwd.n;
+        for (int pass = 0; pass < 2; pass++) {
+            if (pass == 1) {
+                while (back > 0) { back--; seg r = reversed(&fwd.v[back]); stroke_segment(&segs, &r, &st, 0); }
+            }
+            if (is_closed) {
+                stroke_close(sp_start, sp_end, &segs, &st, pass == 0);
+            } else if (pass == 0) {
+                back--;
+                seg r = reversed(&fwd.v[back]);
+                stroke_segment(&segs, &r, &st, 1);
+                continue;
+            } else if (segs.n) {
+                seg last = segs.v[segs.n - 1], first = segs.v[0];
+                line_cap(&last, &first, &st, &segs);
+            }
+            if (segs.n) {  /* Path::push(&segments, true) */
+                if (nseg + segs.n > seg_cap || ns + 2 > sub_cap) { free(segs.v); free(fwd.v); return -1; }
+                for (long i = 0; i < segs.n; i++) {
+                    okind[nseg] = (uint8_t)segs.v[i].kind;
+                    double* o = opts + 8 * nseg;
+                    memset(o, 0, 8 * sizeof(double));
+                    for (int j = 0; j < seg_npts(segs.v[i].kind); j++) { o[2 * j] = segs.v[i].p[j].x; o[2 * j + 1] = segs.v[i].p[j].y; }
+                    nseg++;
+                }
+                osub[++ns] = (uint32_t)nseg;
+                segs.n = 0;
+            }
+        }
+    }
+    free(segs.v);
+    free(fwd.v);
+    *n_sub = ns;
+    return nseg;
+}
+
+/* ------------------------------------------------------------------------ */
 /* color.rs / simd -- premultiplied linear colors                           */
 /* ------------------------------------------------------------------------ */
 

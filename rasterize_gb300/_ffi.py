@@ -65,6 +65,11 @@ class RzScene(ctypes.Structure):
                 ("paints", ctypes.c_void_p)]
 
 
+class RzStrokeStyle(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_double), ("miter_limit", ctypes.c_double), ("line_join", ctypes.c_int32),
+                ("line_cap", ctypes.c_int32)]
+
+
 class RzSceneNode(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("arg", ctypes.c_uint32), ("units", ctypes.c_int32),
                 ("reserved", ctypes.c_int32), ("opacity", ctypes.c_double), ("tr", ctypes.c_double * 6)]
@@ -125,6 +130,9 @@ _SIGNATURES = {
                                               P, ctypes.c_uint32, ctypes.c_uint32]),
     "rz_encode_rgba8": (ctypes.c_int32, [P, P, ctypes.c_uint64, P, ctypes.c_int32]),
     "rz_encode_mask_rgba8": (ctypes.c_int32, [P, P, ctypes.c_int32, ctypes.c_uint64, P, ctypes.c_int32]),
+    "rz_stroke_path": (ctypes.c_int32, [ctypes.POINTER(RzPath), ctypes.POINTER(RzStrokeStyle), P, P, ctypes.c_uint32,
+                                        P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32),
+                                        ctypes.POINTER(ctypes.c_uint32)]),
     "rz_write_image": (ctypes.c_int32, [P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int32, P, ctypes.c_uint64,
                                         ctypes.POINTER(ctypes.c_uint64)]),
     "rz_diff_forward": (ctypes.c_int32, [P, ctypes.POINTER(RzDiffBatch), ctypes.c_double, P]),

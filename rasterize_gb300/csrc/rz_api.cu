@@ -21,6 +21,7 @@
 #include "../../include/rasterize_gb300.h"
 #include "rz_host_arc.cpp.inc"
 #include "rz_host_scene.cpp.inc"
+#include "rz_host_stroke.cpp.inc"
 #include "rz_kernels.cuh"
 #include "rz_pipeline.cuh"
 
@@ -1400,6 +1401,39 @@ rz_status mask_pipeline(rz_ctx* ctx, const rz_path* path, const double tr[6], in
                         false);
 }
 
+// Path::stroke of subpaths [sub0, sub1) of a host path that may hold arcs
+// (expanded first, as PathBuilder::arc_to would have).  Appends the outline
+// (segments and subpath ends relative to what it appends).
+rz_status stroke_subpaths(const uint8_t* kind, const double* pts, const uint32_t* sub_off, const uint8_t* closed,
+                          uint32_t sub0, uint32_t sub1, const rz_stroke_style& style, std::vector<uint8_t>& okind,
+                          std::vector<double>& opts, std::vector<uint32_t>& oends) {
+    if (!(style.width >= 0.0) || !std::isfinite(style.width) || std::isnan(style.miter_limit) ||
+        style.line_join < RZ_JOIN_MITER || style.line_join > RZ_JOIN_ROUND || style.line_cap < RZ_CAP_BUTT ||
+        style.line_cap > RZ_CAP_ROUND)
+        return RZ_ERR_INVALID;
+    const rzhost::Style st{style.width, style.line_join, style.line_cap, style.miter_limit};
+    std::vector<uint8_t> k;
+    std::vector<double> p;
+    std::vector<uint32_t> so{0};
+    std::vector<uint8_t> cl;
+    for (uint32_t sp = sub0; sp < sub1; ++sp) {
+        for (uint32_t i = sub_off[sp]; i < sub_off[sp + 1]; ++i) {
+            if (kind[i] == RZ_SEG_ARC) {
+                if (!rzhost::expand_arc(pts + 8ull * i, k, p)) return RZ_ERR_ARC;
+            } else if (kind[i] <= RZ_SEG_CUBIC) {
+                k.push_back(kind[i]);
+                p.insert(p.end(), pts + 8ull * i, pts + 8ull * i + 8);
+            } else {
+                return RZ_ERR_INVALID;
+            }
+        }
+        so.push_back((uint32_t)k.size());
+        cl.push_back(closed ? closed[sp] : 0);
+    }
+    rzhost::stroke_path(k.data(), p.data(), so.data(), cl.data(), 0, (uint32_t)cl.size(), st, okind, opts, oends);
+    return RZ_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Scene trees: Pipeline::build_rec / render_rec and Layer (src/scene.rs:222-565)
 // ---------------------------------------------------------------------------
@@ -1959,6 +1993,32 @@ rz_status rz_render_scene_rgba8(rz_ctx* ctx, const rz_scene* scene, double flatn
                                 uint8_t* rgba8, uint32_t width, uint32_t height) {
     if (ctx && !rgba8) return fail(ctx, RZ_ERR_INVALID, "null argument");
     return render_scene_impl(ctx, scene, flatness, bg, nullptr, rgba8, width, height);
+}
+
+rz_status rz_stroke_path(const rz_path* path, const rz_stroke_style* style, uint8_t* seg_kind, double* seg_pts,
+                         uint32_t seg_cap, uint32_t* subpath_off, uint32_t sub_cap, uint32_t* n_segments,
+                         uint32_t* n_subpaths) {
+    if (!path || !style || !n_segments || !n_subpaths) return RZ_ERR_INVALID;
+    if (path->n_segments && (!path->seg_kind || !path->seg_pts)) return RZ_ERR_INVALID;
+    if (!path->subpath_off || path->subpath_off[path->n_subpaths] > path->n_segments) return RZ_ERR_INVALID;
+    for (uint32_t i = 0; i < path->n_subpaths; ++i)
+        if (path->subpath_off[i] > path->subpath_off[i + 1]) return RZ_ERR_INVALID;
+    std::vector<uint8_t> okind;
+    std::vector<double> opts;
+    std::vector<uint32_t> oends;
+    const rz_status st = stroke_subpaths(path->seg_kind, path->seg_pts, path->subpath_off, path->closed, 0,
+                                         path->n_subpaths, *style, okind, opts, oends);
+    if (st) return st;
+    *n_segments = (uint32_t)okind.size();
+    *n_subpaths = (uint32_t)oends.size();
+    if (!seg_kind && !seg_pts && !subpath_off) return RZ_OK;
+    if (seg_cap < okind.size() || sub_cap < oends.size() + 1 || !seg_kind || !seg_pts || !subpath_off)
+        return RZ_ERR_CAPACITY;
+    std::memcpy(seg_kind, okind.data(), okind.size());
+    std::memcpy(seg_pts, opts.data(), opts.size() * sizeof(double));
+    subpath_off[0] = 0;
+    for (size_t i = 0; i < oends.size(); ++i) subpath_off[i + 1] = oends[i];
+    return RZ_OK;
 }
 
 rz_status rz_write_image(const uint8_t* rgba8, uint32_t width, uint32_t height, int32_t format, uint8_t* out,

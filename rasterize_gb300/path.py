@@ -50,6 +50,33 @@ def _close_to(p, q) -> bool:
     return abs(p[0] - q[0]) < EPSILON and abs(p[1] - q[1]) < EPSILON
 
 
+class LineJoin(enum.IntEnum):
+    """LineJoin (src/path.rs:78-95); Miter carries StrokeStyle.miter_limit."""
+    Miter = 0
+    Bevel = 1
+    Round = 2
+
+
+class LineCap(enum.IntEnum):
+    """LineCap (src/path.rs:103-117)."""
+    Butt = 0
+    Square = 1
+    Round = 2
+
+
+class StrokeStyle:
+    """StrokeStyle (src/path.rs:121-137): width, join (Miter(4.0) by default), cap (Butt)."""
+
+    __slots__ = ("width", "line_join", "miter_limit", "line_cap")
+
+    def __init__(self, width: float = 0.0, line_join: LineJoin = LineJoin.Miter, miter_limit: float = 4.0,
+                 line_cap: LineCap = LineCap.Butt):
+        self.width = float(width)
+        self.line_join = LineJoin(line_join)
+        self.miter_limit = float(miter_limit)
+        self.line_cap = LineCap(line_cap)
+
+
 class Path:
     """Immutable path in SoA form (src/path.rs:228-233)."""
 
@@ -90,6 +117,29 @@ class Path:
 
     def is_empty(self) -> bool:
         return self.n_subpaths == 0
+
+    def stroke(self, style: StrokeStyle) -> "Path":
+        """Path::stroke (src/path.rs:374-415) on the host, through the library's
+        rz_stroke_path: the outline, every subpath closed."""
+        import ctypes
+        from . import _ffi
+        lib = _ffi.load()
+        ps = _ffi.RzPath(self.kind.ctypes.data, self.pts.ctypes.data, self.subpath_off.ctypes.data,
+                         self.closed.ctypes.data if self.closed.size else None, self.n_segments, self.n_subpaths)
+        st = _ffi.RzStrokeStyle(style.width, style.miter_limit, int(style.line_join), int(style.line_cap))
+        ns, nsub = ctypes.c_uint32(0), ctypes.c_uint32(0)
+        rc = lib.rz_stroke_path(ctypes.byref(ps), ctypes.byref(st), None, None, 0, None, 0, ctypes.byref(ns),
+                                ctypes.byref(nsub))
+        if rc != 0:
+            raise _ffi.RasterizeError(rc, "rz_stroke_path failed")
+        kind = np.zeros(ns.value, dtype=np.uint8)
+        pts = np.zeros((ns.value, 8), dtype=np.float64)
+        sub = np.zeros(nsub.value + 1, dtype=np.uint32)
+        rc = lib.rz_stroke_path(ctypes.byref(ps), ctypes.byref(st), kind.ctypes.data, pts.ctypes.data, ns.value,
+                                sub.ctypes.data, nsub.value + 1, ctypes.byref(ns), ctypes.byref(nsub))
+        if rc != 0:
+            raise _ffi.RasterizeError(rc, "rz_stroke_path failed")
+        return Path(kind, pts, sub, np.ones(nsub.value, dtype=np.uint8))
 
     def has_arcs(self) -> bool:
         return bool(np.any(self.kind == SEG_ARC))

@@ -6,7 +6,8 @@ Run in a checkout that has the reference crate mounted (default
 * the SVG path strings of the reference's unit tests (SQUIRREL in
   src/path.rs, the star/boxes path of test_fill_rule and the 9x4 polygon of
   test_rasterizer in src/rasterize.rs);
-* the small SVG path files of the reference's data/ directory.
+* the small SVG path files of the reference's data/ directory;
+* the input paths and expected outlines of test_stroke (src/path.rs).
 
 Expected numbers of the known-answer tests are restated in
 tests/test_oracle_kat.py next to the assertions that use them.
@@ -40,6 +41,11 @@ def main():
         "square_on_pixel_edges": re.search(r'let path: Path = "(M1,1 v2 h1 v-2 Z)"', rast_rs).group(1),
         "data": {},
     }
+    # test_stroke (src/path.rs): the input paths and the three expected outlines
+    body = path_rs[path_rs.index("fn test_stroke"):]
+    body = body[:body.index("#[test]")]
+    fx["stroke_inputs"] = re.findall(r'let path: Path = "([^"]+)"\.parse', body)
+    fx["stroke_expected"] = [" ".join(t.split()) for t in re.findall(r'r#"(.*?)"#', body, re.S)]
     for name in ("squirrel.path", "tv.path", "rust.path"):
         fx["data"][name] = open(os.path.join(REF, "data", name)).read().strip()
     with open(OUT, "w") as f:

@@ -136,3 +136,36 @@ def test_image_writer_rejects_bad_format():
     assert lib.rz_write_image(img.ctypes.data, 1, 1, 0, None, 0, ctypes.byref(n)) == 0 and n.value == 126
     small = np.zeros(10, dtype=np.uint8)
     assert lib.rz_write_image(img.ctypes.data, 1, 1, 0, small.ctypes.data, 10, ctypes.byref(n)) == 7
+
+
+@pytest.mark.parametrize("join,cap", [(0, 0), (1, 1), (2, 2), (0, 2), (2, 1)])
+def test_stroke_path_matches_oracle_bit_for_bit(join, cap):
+    """rz_stroke_path (host C++) against the oracle's restatement of
+    Path::stroke on random open and closed paths with lines, quads, cubics
+    and arcs, every join and cap."""
+    from oracle import oracle as O
+    from rasterize_gb300 import LineCap, LineJoin, StrokeStyle
+    rng = np.random.default_rng(10 + 3 * join + cap)
+    for trial in range(6):
+        b = PathBuilder().move_to(tuple(rng.uniform(0, 50, 2)))
+        for _ in range(int(rng.integers(1, 9))):
+            k = rng.integers(4)
+            p = [tuple(rng.uniform(0, 50, 2)) for _ in range(3)]
+            if k == 0:
+                b.line_to(p[0])
+            elif k == 1:
+                b.quad_to(p[0], p[1])
+            elif k == 2:
+                b.cubic_to(p[0], p[1], p[2])
+            else:
+                b.arc_to(tuple(rng.uniform(5, 20, 2)), float(rng.uniform(0, 90)), bool(rng.integers(2)),
+                         bool(rng.integers(2)), p[0])
+        if trial % 2:
+            b.close()
+        path = b.build()
+        width = float(rng.uniform(0.5, 6.0))
+        got = path.stroke(StrokeStyle(width, LineJoin(join), 4.0, LineCap(cap)))
+        want = O.stroke(path, width, join, 4.0, cap)
+        assert list(got.kind) == list(want.kind)
+        assert list(got.subpath_off) == list(want.sub_off)
+        assert np.array_equal(got.pts, want.pts)

@@ -293,3 +293,18 @@ def test_encode_edges():
     assert list(m[1]) == [0, 0, 0, 255]
     assert m[2][0] == int(np.float32(O.lib().rzo_linear_to_srgb(0.5)) * np.float32(255) + np.float32(0.5))
     assert list(m[3][:3]) == [255] * 3 and list(m[4][:3]) == [0] * 3
+
+
+STROKE_STYLES = [(1.0, 0, 4.0, 0), (1.0, 2, 4.0, 2), (1.0, 2, 4.0, 2)]  # (width, join, miter, cap) per case
+
+
+def test_stroke():
+    """src/path.rs:1224-1273: the three outlines of test_stroke, compared as
+    the reference does (its Display prints 5 decimals)."""
+    inputs = [FIX["stroke_inputs"][0], FIX["stroke_inputs"][0], FIX["stroke_inputs"][1]]
+    for src, want_svg, (w, j, m, c) in zip(inputs, FIX["stroke_expected"], STROKE_STYLES):
+        got = O.stroke(Path.parse(src), w, j, m, c)
+        want = Path.parse(want_svg)
+        assert list(got.kind) == list(want.kind), (src, list(got.kind), list(want.kind))
+        assert list(got.sub_off) == list(want.subpath_off)
+        assert np.abs(got.pts - want.pts).max() < 1e-5
