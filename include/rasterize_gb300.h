@@ -210,6 +210,7 @@ typedef struct rz_scene {
     const uint8_t* fill_rules;
     const uint32_t* fill_paint;
     const rz_paint* paints;
+    const uint8_t* subpath_closed; /* n_subpaths flags or NULL (all open): only strokes read them */
 } rz_scene;
 
 /* Rasterizer::fill (src/rasterize.rs:69-115): paints `path` (transformed by
@@ -262,13 +263,18 @@ RZ_API rz_status rz_stroke_path(const rz_path* path, const rz_stroke_style* styl
 #define RZ_NODE_TRANSFORM 2 /* Transform: tr, then one child subtree */
 #define RZ_NODE_OPACITY 3   /* Opacity: opacity (clamped to [0, 1] as Scene::opacity does), one child */
 #define RZ_NODE_CLIP 4      /* Clip: arg = fill entry of the clip path (its rule; paint unused), units, one child */
+#define RZ_NODE_STROKE 5    /* Stroke: arg = fill entry (path, paint; rule unused), stroke style; filled NonZero */
 typedef struct rz_scene_node {
     int32_t kind;
     uint32_t arg;
-    int32_t units;   /* RZ_UNITS_USER_SPACE or RZ_UNITS_BOUNDING_BOX (Clip) */
+    int32_t units;        /* RZ_UNITS_USER_SPACE or RZ_UNITS_BOUNDING_BOX (Clip) */
+    int32_t line_join;    /* Stroke: RZ_JOIN_* */
+    int32_t line_cap;     /* Stroke: RZ_CAP_* */
     int32_t reserved;
-    double opacity;  /* Opacity */
-    double tr[6];    /* Transform */
+    double opacity;       /* Opacity */
+    double width;         /* Stroke */
+    double miter_limit;   /* Stroke, RZ_JOIN_MITER */
+    double tr[6];         /* Transform */
 } rz_scene_node;
 
 /* Scene::render (src/scene.rs:186-199) of the tree nodes[0 .. n_nodes) with

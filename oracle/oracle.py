@@ -463,6 +463,7 @@ def l2s_byte_thresholds():
 #   ("transform", child, tr)
 #   ("opacity", child, opacity)          already clamped (Scene::opacity)
 #   ("clip", child, path, units, rule)   units 0 UserSpaceOnUse, 1 BoundingBox
+#   ("stroke", path, tr, (width, join, miter_limit, cap), paint)
 # Bounding boxes are (x0, y0, x1, y1) tuples of Python floats (binary64).
 # ---------------------------------------------------------------------------
 _ID = (1.0, 0.0, 0.0, 0.0, 1.0, 0.0)
@@ -525,7 +526,7 @@ def _path_bbox(path, tr):
 def _scene_bbox(node, tr):
     """Scene::bbox (src/scene.rs:153-182)."""
     k = node[0]
-    if k == "fill":
+    if k in ("fill", "stroke"):  # a stroke's bbox does not include the stroke width
         return _path_bbox(node[1], _xf_mul(tr, _m(node[2])))
     if k == "group":
         acc = None
@@ -564,6 +565,10 @@ def _build_rec(node, view, tr, out):
     """Pipeline::build_rec (src/scene.rs:268-357): appends pipeline nodes
     (children first) and returns the index of this one, or None."""
     k = node[0]
+    if k == "stroke":  # the Fill of the outline, NonZero (src/scene.rs:297-306)
+        w, j, m, c = node[3]
+        node = ("fill", stroke(node[1], w, j, m, c), node[2], 0, node[4])
+        k = "fill"
     if k == "fill":
         b = _view_apply(view, _path_bbox(node[1], _xf_mul(tr, _m(node[2]))))
         if b is None:

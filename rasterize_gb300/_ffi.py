@@ -62,7 +62,7 @@ class RzScene(ctypes.Structure):
                 ("n_paints", ctypes.c_uint32), ("seg_kind", ctypes.c_void_p), ("seg_pts", ctypes.c_void_p),
                 ("subpath_off", ctypes.c_void_p), ("fill_subpath_off", ctypes.c_void_p),
                 ("transforms", ctypes.c_void_p), ("fill_rules", ctypes.c_void_p), ("fill_paint", ctypes.c_void_p),
-                ("paints", ctypes.c_void_p)]
+                ("paints", ctypes.c_void_p), ("subpath_closed", ctypes.c_void_p)]
 
 
 class RzStrokeStyle(ctypes.Structure):
@@ -72,10 +72,12 @@ class RzStrokeStyle(ctypes.Structure):
 
 class RzSceneNode(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("arg", ctypes.c_uint32), ("units", ctypes.c_int32),
-                ("reserved", ctypes.c_int32), ("opacity", ctypes.c_double), ("tr", ctypes.c_double * 6)]
+                ("line_join", ctypes.c_int32), ("line_cap", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("opacity", ctypes.c_double), ("width", ctypes.c_double), ("miter_limit", ctypes.c_double),
+                ("tr", ctypes.c_double * 6)]
 
 
-NODE_FILL, NODE_GROUP, NODE_TRANSFORM, NODE_OPACITY, NODE_CLIP = 0, 1, 2, 3, 4
+NODE_FILL, NODE_GROUP, NODE_TRANSFORM, NODE_OPACITY, NODE_CLIP, NODE_STROKE = 0, 1, 2, 3, 4, 5
 
 
 class RzDiffBatch(ctypes.Structure):

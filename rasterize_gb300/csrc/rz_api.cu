@@ -1485,13 +1485,23 @@ OptBox view_apply(const OptBox& view, const OptBox& bbox) {
     return box_intersect(view.b, bbox.b);
 }
 
+// A fill entry of the tree: the scene's fill entries, then one per Stroke
+// node holding its outline (filled NonZero with the stroked entry's paint).
+struct TreeEntry {
+    rzhost::Xf own;   // the entry's own transform
+    int rule;
+    uint32_t paint;
+};
+
 struct SceneTree {
     const rz_scene* sc = nullptr;
     const rz_scene_node* nodes = nullptr;
     uint32_t n = 0;
-    std::vector<uint32_t> end;  // end[i]: the index after node i's subtree
-    HostScene base;             // staged segment arrays
-    std::vector<uint32_t> fsub;
+    std::vector<uint32_t> end;        // end[i]: the index after node i's subtree
+    std::vector<TreeEntry> E;
+    std::vector<uint32_t> stroke_of;  // Stroke node -> its outline's entry
+    HostScene base;                   // staged segment arrays
+    std::vector<uint32_t> fsub;       // entry e: staged subpaths [fsub[e], fsub[e + 1])
     std::vector<PNode> P;
 };
 
@@ -1504,6 +1514,13 @@ rz_status parse_tree(rz_ctx* ctx, SceneTree& T, uint32_t i, int depth, uint32_t&
     switch (nd.kind) {
         case RZ_NODE_FILL:
             if (nd.arg >= T.sc->n_fills) return fail(ctx, RZ_ERR_INVALID, "scene tree: fill entry out of range");
+            break;
+        case RZ_NODE_STROKE:
+            if (nd.arg >= T.sc->n_fills) return fail(ctx, RZ_ERR_INVALID, "scene tree: stroke entry out of range");
+            if (!(nd.width >= 0.0) || !std::isfinite(nd.width) || std::isnan(nd.miter_limit) ||
+                nd.line_join < RZ_JOIN_MITER || nd.line_join > RZ_JOIN_ROUND || nd.line_cap < RZ_CAP_BUTT ||
+                nd.line_cap > RZ_CAP_ROUND)
+                return fail(ctx, RZ_ERR_INVALID, "scene tree: bad stroke style");
             break;
         case RZ_NODE_GROUP:
             for (uint32_t c = 0; c < nd.arg; ++c) {
@@ -1531,11 +1548,7 @@ rz_status parse_tree(rz_ctx* ctx, SceneTree& T, uint32_t i, int depth, uint32_t&
     return RZ_OK;
 }
 
-rzhost::Xf entry_tr(const SceneTree& T, uint32_t f) {
-    rzhost::Xf t = kIdentity;
-    if (T.sc->transforms) std::memcpy(t.m, T.sc->transforms + 6ull * f, sizeof(t.m));
-    return t;
-}
+rzhost::Xf entry_tr(const SceneTree& T, uint32_t f) { return T.E[f].own; }
 
 // Path::bbox(tr) of fill entry f (its own transform applied first)
 OptBox entry_bbox(const SceneTree& T, uint32_t f, const rzhost::Xf& tr) {
@@ -1556,6 +1569,7 @@ OptBox scene_bbox(const SceneTree& T, uint32_t i, const rzhost::Xf& tr) {
     const rz_scene_node& nd = T.nodes[i];
     switch (nd.kind) {
         case RZ_NODE_FILL: return entry_bbox(T, nd.arg, tr);
+        case RZ_NODE_STROKE: return entry_bbox(T, nd.arg, tr);  // not including the stroke width
         case RZ_NODE_GROUP: {
             OptBox acc;
             uint32_t c = i + 1;
@@ -1594,12 +1608,15 @@ int build_rec(SceneTree& T, uint32_t i, const OptBox& view, const rzhost::Xf& tr
     PNode p;
     p.tr = tr;
     switch (nd.kind) {
-        case RZ_NODE_FILL: {
-            const OptBox b = view_apply(view, entry_bbox(T, nd.arg, tr));
+        case RZ_NODE_FILL:
+        case RZ_NODE_STROKE: {
+            // a Stroke is the Fill of its outline, NonZero (src/scene.rs:297-306)
+            const uint32_t e = nd.kind == RZ_NODE_FILL ? nd.arg : T.stroke_of[i];
+            const OptBox b = view_apply(view, entry_bbox(T, e, tr));
             if (!b.ok) return -1;
             p.kind = RZ_NODE_FILL;
             p.bbox = b.b;
-            p.entry = nd.arg;
+            p.entry = e;
             break;
         }
         case RZ_NODE_GROUP: {
@@ -1731,7 +1748,7 @@ rz_status render_rec(rz_ctx* ctx, SceneTree& T, int pid, LayerState& L, int dept
         if (vw <= 0 || vh <= 0) return RZ_OK;
         const rzhost::Xf align{{1.0, 0.0, -std::floor(p.bbox.x0), 0.0, 1.0, -std::floor(p.bbox.y0)}};
         const rzhost::Xf tr_fill = rzhost::xf_mul(rzhost::xf_mul(align, p.tr), entry_tr(T, p.entry));
-        const rz_paint& paint = T.sc->paints[T.sc->fill_paint[p.entry]];
+        const rz_paint& paint = T.sc->paints[T.E[p.entry].paint];
         rzhost::Box ubox{};
         bool have_u = false;
         if (paint.units == RZ_UNITS_BOUNDING_BOX)
@@ -1741,9 +1758,8 @@ rz_status render_rec(rz_ctx* ctx, SceneTree& T, int pid, LayerState& L, int dept
         prepare_paint(paint, tr_fill, have_u, ubox, pd);
         if (pd.kind < 0) return RZ_OK;
         L.hs.paints.push_back(pd);
-        const int rule = T.sc->fill_rules ? T.sc->fill_rules[p.entry] : 0;
-        add_fill(L.hs, T.fsub[p.entry], T.fsub[p.entry + 1], (int)col_min, (int)row_min, vw, vh, vw, tr_fill, rule,
-                 (int)L.hs.paints.size() - 1);
+        add_fill(L.hs, T.fsub[p.entry], T.fsub[p.entry + 1], (int)col_min, (int)row_min, vw, vh, vw, tr_fill,
+                 T.E[p.entry].rule, (int)L.hs.paints.size() - 1);
         return RZ_OK;
     }
     if (p.kind == RZ_NODE_GROUP) {
@@ -1785,8 +1801,7 @@ rz_status render_rec(rz_ctx* ctx, SceneTree& T, int pid, LayerState& L, int dept
         mh.band_rows = choose_band_rows(M.w, M.h, false);
         const rzhost::Xf align{{1.0, 0.0, -(double)M.x, 0.0, 1.0, -(double)M.y}};
         const rzhost::Xf t = rzhost::xf_mul(rzhost::xf_mul(align, p.clip_tr), entry_tr(T, p.entry));
-        const int rule = T.sc->fill_rules ? T.sc->fill_rules[p.entry] : 0;
-        add_fill(mh, T.fsub[p.entry], T.fsub[p.entry + 1], 0, 0, M.w, M.h, M.w - 1, t, rule, -1);
+        add_fill(mh, T.fsub[p.entry], T.fsub[p.entry + 1], 0, 0, M.w, M.h, M.w - 1, t, T.E[p.entry].rule, -1);
         st = run_pipeline(ctx, mh, flatness, mask, M.w, M.w, M.h, nullptr, false);
         if (st) return st;
     }
@@ -2116,8 +2131,54 @@ rz_status rz_render_scene_tree(rz_ctx* ctx, const rz_scene* scene, const rz_scen
         if (st) return st;
         if (e != n_nodes) return fail(ctx, RZ_ERR_INVALID, "scene tree: nodes after the root's subtree");
     }
-    st = stage_scene_segments(ctx, scene->seg_kind, scene->seg_pts, scene->n_segments, scene->subpath_off,
-                              scene->n_subpaths, scene->fill_subpath_off, scene->n_fills, T.base, T.fsub);
+    // the entry table; every Stroke node's outline becomes one more entry,
+    // appended after the fills' subpaths
+    const uint32_t F = scene->n_fills;
+    T.E.resize(F);
+    for (uint32_t f = 0; f < F; ++f) {
+        T.E[f].own = kIdentity;
+        if (scene->transforms) std::memcpy(T.E[f].own.m, scene->transforms + 6ull * f, sizeof(T.E[f].own.m));
+        T.E[f].rule = scene->fill_rules ? scene->fill_rules[f] : 0;
+        T.E[f].paint = scene->fill_paint[f];
+    }
+    T.stroke_of.assign(n_nodes, 0);
+    std::vector<uint8_t> mk;
+    std::vector<double> mp;
+    std::vector<uint32_t> ms, mfs;
+    bool strokes = false;
+    for (uint32_t i = 0; i < n_nodes; ++i) strokes = strokes || nodes[i].kind == RZ_NODE_STROKE;
+    if (strokes) {
+        const uint32_t S0 = F ? scene->fill_subpath_off[F] : 0;
+        const uint32_t seg_end = scene->n_subpaths ? scene->subpath_off[S0] : 0;
+        mk.assign(scene->seg_kind, scene->seg_kind + seg_end);
+        mp.assign(scene->seg_pts, scene->seg_pts + 8ull * seg_end);
+        if (scene->n_subpaths) ms.assign(scene->subpath_off, scene->subpath_off + S0 + 1);
+        else ms.push_back(0);
+        mfs.assign(scene->fill_subpath_off, scene->fill_subpath_off + F + 1);
+        if (!F) mfs.assign(1, 0);
+        for (uint32_t i = 0; i < n_nodes; ++i) {
+            const rz_scene_node& nd = nodes[i];
+            if (nd.kind != RZ_NODE_STROKE) continue;
+            const rz_stroke_style style{nd.width, nd.miter_limit, nd.line_join, nd.line_cap};
+            std::vector<uint32_t> ends;
+            const size_t base = mk.size();
+            st = stroke_subpaths(scene->seg_kind, scene->seg_pts, scene->subpath_off, scene->subpath_closed,
+                                 scene->fill_subpath_off[nd.arg], scene->fill_subpath_off[nd.arg + 1], style, mk, mp,
+                                 ends);
+            if (st) return fail(ctx, st, "scene tree: cannot stroke a path");
+            for (uint32_t e : ends) ms.push_back((uint32_t)base + e);
+            mfs.push_back((uint32_t)ms.size() - 1);
+            T.stroke_of[i] = (uint32_t)T.E.size();
+            T.E.push_back(TreeEntry{T.E[nd.arg].own, RZ_FILL_NONZERO, T.E[nd.arg].paint});
+        }
+        if (mk.size() > 0xffffffffull || ms.size() > 0xffffffffull)
+            return fail(ctx, RZ_ERR_INVALID, "scene tree: stroke outlines too large");
+        st = stage_scene_segments(ctx, mk.data(), mp.data(), (uint32_t)mk.size(), ms.data(), (uint32_t)ms.size() - 1,
+                                  mfs.data(), (uint32_t)T.E.size(), T.base, T.fsub);
+    } else {
+        st = stage_scene_segments(ctx, scene->seg_kind, scene->seg_pts, scene->n_segments, scene->subpath_off,
+                                  scene->n_subpaths, scene->fill_subpath_off, F, T.base, T.fsub);
+    }
     if (st) return st;
     tr.mark("stage_segments");
     // Pipeline::build with view = the canvas, tr = identity (src/scene.rs:186-199)

@@ -222,6 +222,15 @@ class Scene:
         self._packed = None
         return self
 
+    def stroke(self, path: Path, paint, style, tr: Transform | None = None):
+        """Appends a Stroke (src/scene.rs:29-35) to this Group: ``path``
+        stroked with ``style`` (a StrokeStyle), filled NonZero with ``paint``."""
+        if self.kind != "group":
+            raise TypeError("stroke() appends to a group")
+        self.children.append(Scene("stroke", path=path, paint=paint, style=style, tr=tr or Transform.identity()))
+        self._packed = None
+        return self
+
     def add(self, child: "Scene"):
         """Appends a child scene to this Group."""
         if self.kind != "group":
@@ -289,6 +298,9 @@ class Scene:
             elif sc.kind == "transform":
                 nodes.append(("transform", sc.params["tr"]))
                 walk(sc.children[0])
+            elif sc.kind == "stroke":
+                nodes.append(("stroke", len(entries), sc.params["style"]))
+                entries.append((sc.params["path"], sc.params["tr"], FillRule.NonZero, sc.params["paint"]))
             else:
                 i = len(nodes)
                 nodes.append(None)
@@ -311,6 +323,11 @@ class Scene:
                 out[i].kind = _ffi.NODE_TRANSFORM
                 for j in range(6):
                     out[i].tr[j] = nd[1].m[j]
+            elif k == "stroke":
+                st = nd[2]
+                out[i].kind, out[i].arg = _ffi.NODE_STROKE, nd[1]
+                out[i].width, out[i].miter_limit = st.width, st.miter_limit
+                out[i].line_join, out[i].line_cap = int(st.line_join), int(st.line_cap)
             else:
                 out[i].kind, out[i].arg, out[i].units = _ffi.NODE_CLIP, len(entries), nd[2]
                 entries.append(nd[1])
@@ -353,10 +370,14 @@ def _pack_entries(entries):
         keep.append(k)
     paints = (_paint.RzPaint * max(n, 1))(*structs)
     fpaint = np.ascontiguousarray(np.arange(n, dtype=np.uint32))
+    closed = np.ascontiguousarray(np.concatenate(
+        [np.resize(np.asarray(p.closed, np.uint8), len(p.subpath_off) - 1) if len(p.closed) else
+         np.zeros(len(p.subpath_off) - 1, np.uint8) for p in paths]) if n else np.zeros(0, np.uint8))
     s = _ffi.RzScene(n, int(kind.shape[0]), len(sub) - 1, n, kind.ctypes.data, pts.ctypes.data, sub.ctypes.data,
                      fsub.ctypes.data, trs.ctypes.data if n else None, rules.ctypes.data if n else None,
-                     fpaint.ctypes.data if n else None, ctypes.addressof(paints))
-    return s, (kind, pts, sub, fsub, trs, rules, fpaint, paints, keep)
+                     fpaint.ctypes.data if n else None, ctypes.addressof(paints),
+                     closed.ctypes.data if closed.size else None)
+    return s, (kind, pts, sub, fsub, trs, rules, fpaint, paints, keep, closed)
 
 
 def _tune_key(device: str, batch: "MaskBatch", flatness: float) -> str:

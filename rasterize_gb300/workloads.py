@@ -204,13 +204,15 @@ def scene(seed: int = 3, n: int = 2000, size: int = 2048, seg_range=(20, 2000), 
 
 
 def scene_tree(seed: int = 6, n_groups: int = 40, fills_per_group: int = 10, size: int = 512, seg_range=(20, 200),
-               radius_range=(8, 64), linear_colors=True):
+               radius_range=(8, 64), linear_colors=True, stroke_fraction=0.2):
     """A layered scene: ``n_groups`` groups of ``fills_per_group`` fills (as
     ``scene``), each group either plain, under Opacity U[0.2, 0.95], clipped by
     a star path (UserSpaceOnUse or BoundingBox units, NonZero or EvenOdd), or a
     clip inside an opacity; every third group under an extra Transform node
-    (a small rotation about the canvas centre)."""
+    (a small rotation about the canvas centre).  ``stroke_fraction`` of the
+    paths are stroked instead of filled (width 1-6, any join and cap)."""
     from .paint import Units
+    from .path import LineCap, LineJoin, Path, StrokeStyle
     from .rasterizer import Scene
     rng = np.random.default_rng(seed)
     root = Scene()
@@ -225,7 +227,15 @@ def scene_tree(seed: int = 6, n_groups: int = 40, fills_per_group: int = 10, siz
             ang = rng.uniform(0, 2 * math.pi)
             cx, cy = np.array([gx, gy]) + rng.normal(0, 0.08 * size, 2)
             tr = Transform.new_translate(cx, cy) * Transform.new_rotate(ang) * Transform.new_scale(s, s)
-            grp.fill(path, random_paint(rng, 0.0, 0.0, 2 * r, linear_colors), tr, FillRule.NonZero)
+            if rng.uniform() < stroke_fraction:
+                # an open outline stroked (closed every other time), any join and cap
+                style = StrokeStyle(rng.uniform(1.0, 6.0), LineJoin(int(rng.integers(3))), 4.0,
+                                    LineCap(int(rng.integers(3))))
+                if rng.uniform() < 0.5:
+                    path = Path(path.kind, path.pts, path.subpath_off, np.zeros_like(path.closed))
+                grp.stroke(path, random_paint(rng, 0.0, 0.0, 2 * r, linear_colors), style, tr)
+            else:
+                grp.fill(path, random_paint(rng, 0.0, 0.0, 2 * r, linear_colors), tr, FillRule.NonZero)
         mode = g % 4
         node = grp
         if mode in (2, 3):

@@ -35,6 +35,10 @@ def oracle_tree(sc):
         return ("opacity", oracle_tree(sc.children[0]), sc.params["opacity"])
     if sc.kind == "transform":
         return ("transform", oracle_tree(sc.children[0]), sc.params["tr"])
+    if sc.kind == "stroke":
+        st = sc.params["style"]
+        return ("stroke", sc.params["path"], sc.params["tr"],
+                (st.width, int(st.line_join), st.miter_limit, int(st.line_cap)), oracle_paint(sc.params["paint"]))
     return ("clip", oracle_tree(sc.children[0]), sc.params["path"], int(sc.params["units"]), int(sc.params["rule"]))
 
 

@@ -95,3 +95,28 @@ def test_invalid_trees_are_rejected(R):
     assert call([(_ffi.NODE_FILL, 0), (_ffi.NODE_FILL, 0)]) == 2   # nodes after the root's subtree
     assert call([(9, 0)]) == 2
     assert call([(_ffi.NODE_OPACITY, 0)]) == 2       # opacity without its child
+
+
+@pytest.mark.parametrize("join,cap", [(0, 0), (1, 1), (2, 2)])
+def test_strokes_match_oracle(R, join, cap):
+    """Stroke nodes (the outline filled NonZero): open and closed paths with
+    lines, quads, cubics and arcs, under an opacity layer and a clip."""
+    from rasterize_gb300 import LineCap, LineJoin, PathBuilder, StrokeStyle
+    rng = np.random.default_rng(20 + join)
+    root = Scene()
+    for t in range(6):
+        b = PathBuilder().move_to(tuple(rng.uniform(10, 118, 2)))
+        for _ in range(5):
+            k = rng.integers(4)
+            p = [tuple(rng.uniform(10, 118, 2)) for _ in range(3)]
+            [lambda: b.line_to(p[0]), lambda: b.quad_to(p[0], p[1]), lambda: b.cubic_to(*p),
+             lambda: b.arc_to((20.0, 12.0), 30.0, bool(t % 2), True, p[0])][k]()
+        if t % 2:
+            b.close()
+        style = StrokeStyle(float(rng.uniform(1.0, 8.0)), LineJoin(join), 4.0, LineCap(cap))
+        root.stroke(b.build(), LinColor(*rng.uniform(0, 1, 3), 1.0), style)
+    layered = Scene().add(root.opacity(0.7)).add(
+        root.clip(W.contour(rng, 16, 40.0, center=(64.0, 64.0))).transform(Transform.new_translate(5, 3)))
+    bg = (0.0, 0.0, 0.0, 1.0)
+    for sc in (root, layered):
+        assert_close(R.render_scene(sc, 128, 128, bg=bg), oracle_scene_tree(sc, 128, 128, bg=bg))
