@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -185,6 +186,27 @@ void parallel_for(int64_t n, int64_t min_per_thread, F fn) {
         if (lo < hi) th.emplace_back(fn, lo, hi);
     }
     fn((int64_t)0, std::min(n, chunk));
+    for (auto& x : th) x.join();
+}
+
+// fn(i) for i in [0, n) on up to 16 host threads taking one item at a time
+// (items of very different cost).
+template <typename F>
+void parallel_each(int64_t n, F fn) {
+    const int64_t hw = std::max<int64_t>(1, (int64_t)std::thread::hardware_concurrency());
+    const int64_t t = std::min<int64_t>({hw, 16, n});
+    std::atomic<int64_t> next{0};
+    auto work = [&]() {
+        for (int64_t i = next.fetch_add(1); i < n; i = next.fetch_add(1)) fn(i);
+    };
+    if (t <= 1) {
+        work();
+        return;
+    }
+    std::vector<std::thread> th;
+    th.reserve((size_t)t - 1);
+    for (int64_t i = 1; i < t; ++i) th.emplace_back(work);
+    work();
     for (auto& x : th) x.join();
 }
 
@@ -1503,6 +1525,11 @@ struct SceneTree {
     HostScene base;                   // staged segment arrays
     std::vector<uint32_t> fsub;       // entry e: staged subpaths [fsub[e], fsub[e + 1])
     std::vector<PNode> P;
+    // Fill and Stroke nodes' path bboxes under their ancestors' transforms,
+    // computed in parallel before build_rec
+    std::vector<OptBox> node_bbox;
+    std::vector<rzhost::Xf> node_tr;
+    std::vector<uint8_t> node_cached;
 };
 
 // Checks the pre-order node array and records every subtree's end.
@@ -1601,6 +1628,43 @@ OptBox scene_bbox(const SceneTree& T, uint32_t i, const rzhost::Xf& tr) {
     }
 }
 
+// The transforms build_rec will see at every Fill and Stroke node (only
+// Transform nodes change it), and those nodes' path bboxes, in parallel.
+void precompute_bboxes(SceneTree& T) {
+    T.node_bbox.assign(T.n, OptBox{});
+    T.node_tr.assign(T.n, kIdentity);
+    T.node_cached.assign(T.n, 0);
+    std::vector<uint32_t> leaves;
+    std::vector<std::pair<uint32_t, rzhost::Xf>> stack;
+    if (T.n) stack.push_back({0u, kIdentity});
+    while (!stack.empty()) {
+        const uint32_t i = stack.back().first;
+        const rzhost::Xf tr = stack.back().second;
+        stack.pop_back();
+        const rz_scene_node& nd = T.nodes[i];
+        if (nd.kind == RZ_NODE_FILL || nd.kind == RZ_NODE_STROKE) {
+            T.node_tr[i] = tr;
+            leaves.push_back(i);
+        } else if (nd.kind == RZ_NODE_GROUP) {
+            uint32_t c = i + 1;
+            for (uint32_t k = 0; k < nd.arg; ++k, c = T.end[c]) stack.push_back({c, tr});
+        } else if (nd.kind == RZ_NODE_TRANSFORM) {
+            stack.push_back({i + 1, rzhost::xf_mul(tr, node_tr(nd))});
+        } else {
+            stack.push_back({i + 1, tr});
+        }
+    }
+    parallel_for((int64_t)leaves.size(), 4, [&](int64_t a, int64_t b) {
+        for (int64_t j = a; j < b; ++j) {
+            const uint32_t i = leaves[j];
+            const rz_scene_node& nd = T.nodes[i];
+            const uint32_t e = nd.kind == RZ_NODE_FILL ? nd.arg : T.stroke_of[i];
+            T.node_bbox[i] = entry_bbox(T, e, T.node_tr[i]);
+            T.node_cached[i] = 1;
+        }
+    });
+}
+
 // Pipeline::build_rec (src/scene.rs:268-357); -1 for None.  Children are
 // allocated before their parent, so the root is the last node.
 int build_rec(SceneTree& T, uint32_t i, const OptBox& view, const rzhost::Xf& tr) {
@@ -1612,7 +1676,8 @@ int build_rec(SceneTree& T, uint32_t i, const OptBox& view, const rzhost::Xf& tr
         case RZ_NODE_STROKE: {
             // a Stroke is the Fill of its outline, NonZero (src/scene.rs:297-306)
             const uint32_t e = nd.kind == RZ_NODE_FILL ? nd.arg : T.stroke_of[i];
-            const OptBox b = view_apply(view, entry_bbox(T, e, tr));
+            const bool cached = T.node_cached[i] && std::memcmp(T.node_tr[i].m, tr.m, sizeof(tr.m)) == 0;
+            const OptBox b = view_apply(view, cached ? T.node_bbox[i] : entry_bbox(T, e, tr));
             if (!b.ok) return -1;
             p.kind = RZ_NODE_FILL;
             p.bbox = b.b;
@@ -1672,65 +1737,71 @@ int build_rec(SceneTree& T, uint32_t i, const OptBox& view, const rzhost::Xf& tr
     return (int)T.P.size() - 1;
 }
 
-// A layer: a rectangle of the canvas grid with its device pixels, and the
-// fills queued for it (flushed through the line pipeline before anything
-// reads the layer).
-struct LayerState {
+// The render of a scene tree is planned on the host, then launched without a
+// host round trip per layer: every fill of every layer (and every clip mask)
+// is flattened and binned by one pass of the line pipeline, and the plan's
+// operations -- layer initialisation, composites of a layer's fills, masks,
+// composes -- run in order on the stream.  Layers live in per-depth pools,
+// sized for the largest layer at each depth before anything is launched.
+struct TreeOp {
+    enum Kind { kFillColor, kClear, kComposite, kMask, kCompose } kind;
+    int depth = 0;          // target: 0 the canvas, d >= 1 layer_pool[d]; kMask / kClear of a mask: mask_pool[d]
+    bool mask_target = false;
+    int32_t w = 0, h = 0;   // target size
+    uint32_t f0 = 0, f1 = 0;  // kComposite / kMask: fills [f0, f1) of the plan's scene
+    int max_clip = 1;
+    // kCompose: src layer at depth + 1 onto the target, mask at mask_pool[depth] when has_mask
+    bool has_mask = false, scale = false;
+    float opacity = 1.0f;
+    int32_t drect[4] = {0, 0, 0, 0}, srect[4] = {0, 0, 0, 0}, mrect[4] = {0, 0, 0, 0};
+    int x0 = 0, y0 = 0, x1 = 0, y1 = 0;
+    float color[4] = {0, 0, 0, 0};
+};
+
+struct PlanLayer {
     int32_t x = 0, y = 0, w = 0, h = 0;
-    float* buf = nullptr;
-    HostScene hs;
+    int depth = 0;
+    uint32_t batch0 = 0;  // first fill of the layer's pending composite
+};
+
+struct TreePlan {
+    HostScene hs;  // every fill of the render (layers' fills and masks)
+    std::vector<TreeOp> ops;
+    std::vector<uint64_t> layer_bytes, mask_bytes;  // per depth
 };
 
 // Layer::new (src/scene.rs:483-501): floor of min, ceil of max.
-void layer_rect(const rzhost::Box& b, LayerState& L) {
+void layer_rect(const rzhost::Box& b, PlanLayer& L) {
     L.x = (int32_t)std::floor(b.x0);
     L.y = (int32_t)std::floor(b.y0);
     L.w = std::max<int32_t>((int32_t)std::ceil(b.x1) - L.x, 0);
     L.h = std::max<int32_t>((int32_t)std::ceil(b.y1) - L.y, 0);
 }
 
-void layer_begin(const SceneTree& T, LayerState& L) {
-    L.hs = HostScene{};
-    L.hs.kind = T.base.kind;
-    L.hs.pts = T.base.pts;
-    L.hs.sub_off = T.base.sub_off;
-    L.hs.n_seg = T.base.n_seg;
-    L.hs.n_sub = T.base.n_sub;
-    L.hs.band_rows = choose_band_rows(std::max(L.w, 1), std::max(L.h, 1), true);
+void need(std::vector<uint64_t>& v, int depth, uint64_t bytes) {
+    if ((int)v.size() <= depth) v.resize(depth + 1, 0);
+    v[depth] = std::max(v[depth], bytes);
 }
 
-rz_status layer_flush(rz_ctx* ctx, LayerState& L, double flatness) {
-    if (L.hs.fills.empty()) return RZ_OK;
-    rz_status st = run_pipeline(ctx, L.hs, flatness, L.buf, L.w, L.w, L.h, nullptr, true);
-    const int band_rows = L.hs.band_rows;
-    L.hs.fills.clear();
-    L.hs.paints.clear();
-    L.hs.n_slots = L.hs.n_entries = 0;
-    L.hs.max_clip = 1;
-    L.hs.band_rows = band_rows;
-    return st;
+// The fills queued for L since its last composite become one composite.
+void plan_flush(TreePlan& P, PlanLayer& L) {
+    const uint32_t n = (uint32_t)P.hs.fills.size();
+    if (n > L.batch0) {
+        TreeOp op{};
+        op.kind = TreeOp::kComposite;
+        op.depth = L.depth;
+        op.w = L.w;
+        op.h = L.h;
+        op.f0 = L.batch0;
+        op.f1 = n;
+        for (uint32_t f = L.batch0; f < n; ++f) op.max_clip = std::max(op.max_clip, P.hs.fills[f].clip_width);
+        P.ops.push_back(op);
+    }
+    L.batch0 = n;
 }
 
-rz_status render_rec(rz_ctx* ctx, SceneTree& T, int pid, LayerState& L, int depth, double flatness);
-
-// Pipeline::render (src/scene.rs:384-395) of a child node into a fresh
-// transparent layer at nesting depth `depth`, flushed.
-rz_status render_child(rz_ctx* ctx, SceneTree& T, int pid, LayerState& C, int depth, double flatness) {
-    layer_rect(T.P[pid].bbox, C);
-    if ((int)ctx->layer_pool.size() <= depth) ctx->layer_pool.resize(depth + 1);
-    const uint64_t n = (uint64_t)C.w * (uint64_t)C.h;
-    RZ_CUDA(ctx->layer_pool[depth].ensure(n * 16 + 16));
-    C.buf = (float*)ctx->layer_pool[depth].p;
-    if (n) RZ_CUDA(cudaMemsetAsync(C.buf, 0, n * 16, ctx->stream));
-    layer_begin(T, C);
-    if (n == 0) return RZ_OK;
-    rz_status st = render_rec(ctx, T, pid, C, depth, flatness);
-    if (st) return st;
-    return layer_flush(ctx, C, flatness);
-}
-
-// Pipeline::render_rec (src/scene.rs:397-458).
-rz_status render_rec(rz_ctx* ctx, SceneTree& T, int pid, LayerState& L, int depth, double flatness) {
+// Pipeline::render_rec (src/scene.rs:397-458) as a plan.
+void plan_rec(const SceneTree& T, TreePlan& P, int pid, PlanLayer& L) {
     const PNode& p = T.P[pid];
     if (p.kind == RZ_NODE_FILL) {
         // the fill's view of the layer (max bounds are exclusive: max + 1) and the align transform
@@ -1745,7 +1816,7 @@ rz_status render_rec(rz_ctx* ctx, SceneTree& T, int pid, LayerState& L, int dept
         col_min = std::min<long>(col_min, L.w);
         col_max = std::max(std::min<long>(col_max, L.w), col_min);
         const int vw = (int)(col_max - col_min), vh = (int)(row_max - row_min);
-        if (vw <= 0 || vh <= 0) return RZ_OK;
+        if (vw <= 0 || vh <= 0) return;
         const rzhost::Xf align{{1.0, 0.0, -std::floor(p.bbox.x0), 0.0, 1.0, -std::floor(p.bbox.y0)}};
         const rzhost::Xf tr_fill = rzhost::xf_mul(rzhost::xf_mul(align, p.tr), entry_tr(T, p.entry));
         const rz_paint& paint = T.sc->paints[T.E[p.entry].paint];
@@ -1756,59 +1827,160 @@ rz_status render_rec(rz_ctx* ctx, SceneTree& T, int pid, LayerState& L, int dept
                                        kIdentity, ubox);
         rz::PaintDev pd;
         prepare_paint(paint, tr_fill, have_u, ubox, pd);
-        if (pd.kind < 0) return RZ_OK;
-        L.hs.paints.push_back(pd);
-        add_fill(L.hs, T.fsub[p.entry], T.fsub[p.entry + 1], (int)col_min, (int)row_min, vw, vh, vw, tr_fill,
-                 T.E[p.entry].rule, (int)L.hs.paints.size() - 1);
-        return RZ_OK;
+        if (pd.kind < 0) return;
+        P.hs.paints.push_back(pd);
+        add_fill(P.hs, T.fsub[p.entry], T.fsub[p.entry + 1], (int)col_min, (int)row_min, vw, vh, vw, tr_fill,
+                 T.E[p.entry].rule, (int)P.hs.paints.size() - 1);
+        return;
     }
     if (p.kind == RZ_NODE_GROUP) {
-        for (int c : p.children) {
-            rz_status st = render_rec(ctx, T, c, L, depth, flatness);
-            if (st) return st;
-        }
-        return RZ_OK;
+        for (int c : p.children) plan_rec(T, P, c, L);
+        return;
     }
-    // Opacity and Clip: the child renders into its own layer, then composes onto L
-    rz_status st = layer_flush(ctx, L, flatness);
-    if (st) return st;
-    LayerState C;
-    st = render_child(ctx, T, p.children[0], C, depth + 1, flatness);
-    if (st) return st;
-    const int32_t drect[4] = {L.x, L.y, L.w, L.h}, srect[4] = {C.x, C.y, C.w, C.h};
-    const int x0 = std::max(L.x, C.x), x1 = std::min(L.x + L.w, C.x + C.w);
-    const int y0 = std::max(L.y, C.y), y1 = std::min(L.y + L.h, C.y + C.h);
+    // Opacity and Clip: the child renders into a fresh layer of its own
+    // (Pipeline::render, :384-395), then composes onto L
+    plan_flush(P, L);
+    PlanLayer C;
+    layer_rect(T.P[p.children[0]].bbox, C);
+    C.depth = L.depth + 1;
+    const uint64_t nc = (uint64_t)C.w * (uint64_t)C.h;
+    if (nc) {
+        need(P.layer_bytes, C.depth, nc * 16);
+        TreeOp clear{};
+        clear.kind = TreeOp::kClear;
+        clear.depth = C.depth;
+        clear.w = C.w;
+        clear.h = C.h;
+        P.ops.push_back(clear);
+        C.batch0 = (uint32_t)P.hs.fills.size();
+        plan_rec(T, P, p.children[0], C);
+        plan_flush(P, C);
+    }
+    TreeOp op{};
+    op.kind = TreeOp::kCompose;
+    op.depth = L.depth;
+    op.drect[0] = L.x, op.drect[1] = L.y, op.drect[2] = L.w, op.drect[3] = L.h;
+    op.srect[0] = C.x, op.srect[1] = C.y, op.srect[2] = C.w, op.srect[3] = C.h;
+    op.x0 = std::max(L.x, C.x), op.x1 = std::min(L.x + L.w, C.x + C.w);
+    op.y0 = std::max(L.y, C.y), op.y1 = std::min(L.y + L.h, C.y + C.h);
     if (p.kind == RZ_NODE_OPACITY) {
-        RZ_CUDA(rz::launch_layer_compose(L.buf, drect, C.buf, srect, nullptr, drect, p.opacity, true, x0, y0, x1, y1,
-                                         ctx->stream));
-        return RZ_OK;
+        op.scale = true;
+        op.opacity = p.opacity;
+    } else {
+        // Clip: the clip path's mask over the clip node's bbox (Path::mask, mask semantics)
+        PlanLayer M;
+        layer_rect(p.bbox, M);
+        const uint64_t nm = (uint64_t)M.w * (uint64_t)M.h;
+        need(P.mask_bytes, L.depth, nm * 4 + 16);
+        op.has_mask = true;
+        op.mrect[0] = M.x, op.mrect[1] = M.y, op.mrect[2] = M.w, op.mrect[3] = M.h;
+        if (nm) {
+            TreeOp clear{};
+            clear.kind = TreeOp::kClear;
+            clear.depth = L.depth;
+            clear.mask_target = true;
+            clear.w = M.w;
+            clear.h = M.h;
+            P.ops.push_back(clear);
+            const rzhost::Xf align{{1.0, 0.0, -(double)M.x, 0.0, 1.0, -(double)M.y}};
+            const rzhost::Xf t = rzhost::xf_mul(rzhost::xf_mul(align, p.clip_tr), entry_tr(T, p.entry));
+            TreeOp mk{};
+            mk.kind = TreeOp::kMask;
+            mk.depth = L.depth;
+            mk.mask_target = true;
+            mk.w = M.w;
+            mk.h = M.h;
+            mk.f0 = (uint32_t)P.hs.fills.size();
+            add_fill(P.hs, T.fsub[p.entry], T.fsub[p.entry + 1], 0, 0, M.w, M.h, M.w - 1, t, T.E[p.entry].rule, -1);
+            mk.f1 = (uint32_t)P.hs.fills.size();
+            mk.max_clip = std::max(1, M.w - 1);
+            if (mk.f1 > mk.f0) P.ops.push_back(mk);
+        }
     }
-    // Clip: the clip path's mask over the clip node's bbox (Path::mask, mask semantics)
-    LayerState M;
-    layer_rect(p.bbox, M);
-    const uint64_t nm = (uint64_t)M.w * (uint64_t)M.h;
-    if ((int)ctx->mask_pool.size() <= depth) ctx->mask_pool.resize(depth + 1);
-    RZ_CUDA(ctx->mask_pool[depth].ensure(nm * 4 + 16));
-    float* mask = (float*)ctx->mask_pool[depth].p;
-    if (nm) {
-        RZ_CUDA(cudaMemsetAsync(mask, 0, nm * 4, ctx->stream));
-        HostScene mh;
-        mh.kind = T.base.kind;
-        mh.pts = T.base.pts;
-        mh.sub_off = T.base.sub_off;
-        mh.n_seg = T.base.n_seg;
-        mh.n_sub = T.base.n_sub;
-        mh.band_rows = choose_band_rows(M.w, M.h, false);
-        const rzhost::Xf align{{1.0, 0.0, -(double)M.x, 0.0, 1.0, -(double)M.y}};
-        const rzhost::Xf t = rzhost::xf_mul(rzhost::xf_mul(align, p.clip_tr), entry_tr(T, p.entry));
-        add_fill(mh, T.fsub[p.entry], T.fsub[p.entry + 1], 0, 0, M.w, M.h, M.w - 1, t, T.E[p.entry].rule, -1);
-        st = run_pipeline(ctx, mh, flatness, mask, M.w, M.w, M.h, nullptr, false);
+    if (nc) P.ops.push_back(op);
+    L.batch0 = (uint32_t)P.hs.fills.size();  // fills queued meanwhile belong to the child and the mask
+}
+
+// Launches the plan: one flatten + bin of every fill, then the operations.
+rz_status run_plan(rz_ctx* ctx, TreePlan& P, double flatness, float* canvas, int W, int H) {
+    Trace tr("scene_tree_plan");
+    HostScene& hs = P.hs;
+    for (size_t d = 0; d < P.layer_bytes.size(); ++d) {
+        if ((int)ctx->layer_pool.size() <= (int)d) ctx->layer_pool.resize(d + 1);
+        if (P.layer_bytes[d]) RZ_CUDA(ctx->layer_pool[d].ensure(P.layer_bytes[d] + 16));
+    }
+    for (size_t d = 0; d < P.mask_bytes.size(); ++d) {
+        if ((int)ctx->mask_pool.size() <= (int)d) ctx->mask_pool.resize(d + 1);
+        if (P.mask_bytes[d]) RZ_CUDA(ctx->mask_pool[d].ensure(P.mask_bytes[d]));
+    }
+    rz::SceneDev S{};
+    S.kind = (const uint8_t*)ctx->d_kind.p;
+    S.pts = (const double*)ctx->d_pts.p;
+    S.sub_off = (const uint32_t*)ctx->d_sub.p;
+    S.n_fills = (uint32_t)hs.fills.size();
+    S.n_slots = hs.n_slots;
+    S.n_segments = hs.n_seg;
+    S.n_subpaths = hs.n_sub;
+    S.task_depth = hs.task_depth;
+    S.thr64 = 16.0 * flatness * flatness;
+    S.thr32 = (float)S.thr64;
+    S.band_rows = hs.band_rows;
+    RZ_CUDA(ctx->d_ctrl.ensure(64));
+    RZ_CUDA(cudaMemsetAsync(ctx->d_ctrl.p, 0, 64, ctx->stream));
+    S.err = (int32_t*)ctx->d_ctrl.p;
+    S.counters = (int32_t*)ctx->d_ctrl.p + 4;
+    const rz::PaintDev* paints = nullptr;
+    if (!hs.fills.empty()) {
+        if (hs.paints.empty()) hs.paints.resize(1);
+        RZ_CUDA(ctx->p_paints.ensure(hs.paints.size() * sizeof(rz::PaintDev)));
+        RZ_CUDA(cudaMemcpyAsync(ctx->p_paints.p, hs.paints.data(), hs.paints.size() * sizeof(rz::PaintDev),
+                                cudaMemcpyHostToDevice, ctx->stream));
+        paints = (const rz::PaintDev*)ctx->p_paints.p;
+        rz_status st = build_lines(ctx, hs, S, tr, nullptr);
         if (st) return st;
     }
-    const int32_t mrect[4] = {M.x, M.y, M.w, M.h};
-    RZ_CUDA(rz::launch_layer_compose(L.buf, drect, C.buf, srect, mask, mrect, 1.0f, false, x0, y0, x1, y1,
-                                     ctx->stream));
-    return RZ_OK;
+    auto target = [&](const TreeOp& op) -> float* {
+        if (op.mask_target) return (float*)ctx->mask_pool[op.depth].p;
+        return op.depth == 0 ? canvas : (float*)ctx->layer_pool[op.depth].p;
+    };
+    for (const TreeOp& op : P.ops) {
+        switch (op.kind) {
+            case TreeOp::kFillColor:
+                RZ_CUDA(rz::launch_layer_fill(target(op), (uint64_t)op.w * op.h, op.color, ctx->stream));
+                break;
+            case TreeOp::kClear:
+                RZ_CUDA(cudaMemsetAsync(target(op), 0, (uint64_t)op.w * op.h * (op.mask_target ? 4 : 16),
+                                        ctx->stream));
+                break;
+            case TreeOp::kComposite:
+            case TreeOp::kMask: {
+                rz::SceneDev C = S;
+                C.fills = S.fills + op.f0;
+                C.n_fills = op.f1 - op.f0;
+                C.paints = op.kind == TreeOp::kComposite ? paints : nullptr;
+                C.canvas = target(op);
+                C.canvas_stride = op.w;
+                C.canvas_w = op.w;
+                C.canvas_h = op.h;
+                C.n_bands = (op.h + hs.band_rows - 1) / hs.band_rows;
+                C.load_canvas = op.kind == TreeOp::kComposite ? 1 : 0;
+                int cov_stride = 0;
+                const int smem = rz::composite_smem_bytes(op.w, hs.band_rows, op.max_clip, op.kind == TreeOp::kComposite,
+                                                          &cov_stride);
+                if (C.n_bands) RZ_CUDA(rz::launch_composite(C, cov_stride, smem, ctx->stream));
+                break;
+            }
+            case TreeOp::kCompose: {
+                const float* mask = op.has_mask ? (const float*)ctx->mask_pool[op.depth].p : nullptr;
+                RZ_CUDA(rz::launch_layer_compose(target(op), op.drect, (const float*)ctx->layer_pool[op.depth + 1].p,
+                                                 op.srect, mask, op.mrect, op.opacity, op.scale, op.x0, op.y0, op.x1,
+                                                 op.y1, ctx->stream));
+                break;
+            }
+        }
+    }
+    tr.gpu_mark(ctx->stream, "layers");
+    return read_error(ctx);
 }
 
 // Scene-table checks shared by the flat and tree renders.
@@ -2156,20 +2328,44 @@ rz_status rz_render_scene_tree(rz_ctx* ctx, const rz_scene* scene, const rz_scen
         else ms.push_back(0);
         mfs.assign(scene->fill_subpath_off, scene->fill_subpath_off + F + 1);
         if (!F) mfs.assign(1, 0);
-        for (uint32_t i = 0; i < n_nodes; ++i) {
-            const rz_scene_node& nd = nodes[i];
-            if (nd.kind != RZ_NODE_STROKE) continue;
-            const rz_stroke_style style{nd.width, nd.miter_limit, nd.line_join, nd.line_cap};
+        // every Stroke node's outline, computed in parallel, then appended in node order
+        std::vector<uint32_t> sn;
+        for (uint32_t i = 0; i < n_nodes; ++i)
+            if (nodes[i].kind == RZ_NODE_STROKE) sn.push_back(i);
+        struct Outline {
+            std::vector<uint8_t> k;
+            std::vector<double> p;
             std::vector<uint32_t> ends;
+            rz_status st = RZ_OK;
+        };
+        std::vector<Outline> outl(sn.size());
+        // the largest outline first, so no thread is left with one at the end
+        std::stable_sort(sn.begin(), sn.end(), [&](uint32_t a, uint32_t b) {
+            const uint32_t* fo = scene->fill_subpath_off;
+            auto segs = [&](uint32_t i) { return scene->subpath_off[fo[nodes[i].arg + 1]] - scene->subpath_off[fo[nodes[i].arg]]; };
+            return segs(a) > segs(b);
+        });
+        parallel_each((int64_t)sn.size(), [&](int64_t j) {
+            const rz_scene_node& nd = nodes[sn[j]];
+            const rz_stroke_style style{nd.width, nd.miter_limit, nd.line_join, nd.line_cap};
+            outl[j].st = stroke_subpaths(scene->seg_kind, scene->seg_pts, scene->subpath_off, scene->subpath_closed,
+                                         scene->fill_subpath_off[nd.arg], scene->fill_subpath_off[nd.arg + 1], style,
+                                         outl[j].k, outl[j].p, outl[j].ends);
+        });
+        // appended in node order
+        std::vector<size_t> order(sn.size());
+        for (size_t j = 0; j < sn.size(); ++j) order[j] = j;
+        std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return sn[a] < sn[b]; });
+        for (size_t j : order) {
+            if (outl[j].st) return fail(ctx, outl[j].st, "scene tree: cannot stroke a path");
             const size_t base = mk.size();
-            st = stroke_subpaths(scene->seg_kind, scene->seg_pts, scene->subpath_off, scene->subpath_closed,
-                                 scene->fill_subpath_off[nd.arg], scene->fill_subpath_off[nd.arg + 1], style, mk, mp,
-                                 ends);
-            if (st) return fail(ctx, st, "scene tree: cannot stroke a path");
-            for (uint32_t e : ends) ms.push_back((uint32_t)base + e);
+            mk.insert(mk.end(), outl[j].k.begin(), outl[j].k.end());
+            mp.insert(mp.end(), outl[j].p.begin(), outl[j].p.end());
+            for (uint32_t e : outl[j].ends) ms.push_back((uint32_t)base + e);
             mfs.push_back((uint32_t)ms.size() - 1);
-            T.stroke_of[i] = (uint32_t)T.E.size();
-            T.E.push_back(TreeEntry{T.E[nd.arg].own, RZ_FILL_NONZERO, T.E[nd.arg].paint});
+            const uint32_t e0 = nodes[sn[j]].arg;
+            T.stroke_of[sn[j]] = (uint32_t)T.E.size();
+            T.E.push_back(TreeEntry{T.E[e0].own, RZ_FILL_NONZERO, T.E[e0].paint});
         }
         if (mk.size() > 0xffffffffull || ms.size() > 0xffffffffull)
             return fail(ctx, RZ_ERR_INVALID, "scene tree: stroke outlines too large");
@@ -2184,33 +2380,47 @@ rz_status rz_render_scene_tree(rz_ctx* ctx, const rz_scene* scene, const rz_scen
     // Pipeline::build with view = the canvas, tr = identity (src/scene.rs:186-199)
     const int W = (int)width, H = (int)height;
     int root = -1;
-    if (n_nodes) root = build_rec(T, 0, OptBox{true, rzhost::Box{0.0, 0.0, (double)W, (double)H}}, kIdentity);
+    if (n_nodes) {
+        precompute_bboxes(T);
+        root = build_rec(T, 0, OptBox{true, rzhost::Box{0.0, 0.0, (double)W, (double)H}}, kIdentity);
+    }
     tr.mark("build");
     // the root layer is the view: Layer::new(view, bg)
     const uint64_t n = (uint64_t)W * (uint64_t)H;
     if (n == 0) return RZ_OK;
     RZ_CUDA(ctx->p_canvas.ensure(n * 16 + 16));
-    LayerState R;
+    TreePlan P;
+    P.hs.kind = T.base.kind;
+    P.hs.pts = T.base.pts;
+    P.hs.sub_off = T.base.sub_off;
+    P.hs.n_seg = T.base.n_seg;
+    P.hs.n_sub = T.base.n_sub;
+    P.hs.band_rows = choose_band_rows(W, H, true);
+    PlanLayer R;
     R.w = W;
     R.h = H;
-    R.buf = (float*)ctx->p_canvas.p;
-    const float zero[4] = {0.f, 0.f, 0.f, 0.f};
-    RZ_CUDA(rz::launch_layer_fill(R.buf, n, bg ? bg : zero, ctx->stream));
-    layer_begin(T, R);
+    TreeOp init{};
+    init.kind = TreeOp::kFillColor;
+    init.w = W;
+    init.h = H;
+    if (bg) std::memcpy(init.color, bg, sizeof(init.color));
+    P.ops.push_back(init);
     if (root >= 0) {
-        st = render_rec(ctx, T, root, R, 0, flatness);
-        if (st) return st;
-        st = layer_flush(ctx, R, flatness);
-        if (st) return st;
+        plan_rec(T, P, root, R);
+        plan_flush(P, R);
     }
+    tr.mark("plan");
+    float* const canvas_dev = (float*)ctx->p_canvas.p;
+    st = run_plan(ctx, P, flatness, canvas_dev, W, H);
+    if (st) return st;
     tr.mark("render");
     if (canvas) {
-        st = copy_out_bytes(ctx, canvas, R.buf, n * 16);
+        st = copy_out_bytes(ctx, canvas, canvas_dev, n * 16);
         if (st) return st;
     }
     if (rgba8) {
         RZ_CUDA(ctx->p_rgba8.ensure(n * 4 + 16));
-        RZ_CUDA(rz::launch_encode_rgba8(R.buf, (uint8_t*)ctx->p_rgba8.p, n, ctx->stream));
+        RZ_CUDA(rz::launch_encode_rgba8(canvas_dev, (uint8_t*)ctx->p_rgba8.p, n, ctx->stream));
         st = copy_out_bytes(ctx, rgba8, ctx->p_rgba8.p, n * 4);
         if (st) return st;
     }

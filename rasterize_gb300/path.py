@@ -128,18 +128,20 @@ class Path:
                          self.closed.ctypes.data if self.closed.size else None, self.n_segments, self.n_subpaths)
         st = _ffi.RzStrokeStyle(style.width, style.miter_limit, int(style.line_join), int(style.line_cap))
         ns, nsub = ctypes.c_uint32(0), ctypes.c_uint32(0)
-        rc = lib.rz_stroke_path(ctypes.byref(ps), ctypes.byref(st), None, None, 0, None, 0, ctypes.byref(ns),
-                                ctypes.byref(nsub))
+        cap_s, cap_p = 16 * self.n_segments + 64, 2 * self.n_subpaths + 2  # usually enough: one call
+        while True:
+            kind = np.zeros(cap_s, dtype=np.uint8)
+            pts = np.zeros((cap_s, 8), dtype=np.float64)
+            sub = np.zeros(cap_p, dtype=np.uint32)
+            rc = lib.rz_stroke_path(ctypes.byref(ps), ctypes.byref(st), kind.ctypes.data, pts.ctypes.data, cap_s,
+                                    sub.ctypes.data, cap_p, ctypes.byref(ns), ctypes.byref(nsub))
+            if rc != 7:  # RZ_ERR_CAPACITY: grow to the sizes it reported
+                break
+            cap_s, cap_p = ns.value, nsub.value + 1
         if rc != 0:
             raise _ffi.RasterizeError(rc, "rz_stroke_path failed")
-        kind = np.zeros(ns.value, dtype=np.uint8)
-        pts = np.zeros((ns.value, 8), dtype=np.float64)
-        sub = np.zeros(nsub.value + 1, dtype=np.uint32)
-        rc = lib.rz_stroke_path(ctypes.byref(ps), ctypes.byref(st), kind.ctypes.data, pts.ctypes.data, ns.value,
-                                sub.ctypes.data, nsub.value + 1, ctypes.byref(ns), ctypes.byref(nsub))
-        if rc != 0:
-            raise _ffi.RasterizeError(rc, "rz_stroke_path failed")
-        return Path(kind, pts, sub, np.ones(nsub.value, dtype=np.uint8))
+        n = ns.value
+        return Path(kind[:n], pts[:n], sub[:nsub.value + 1], np.ones(nsub.value, dtype=np.uint8))
 
     def has_arcs(self) -> bool:
         return bool(np.any(self.kind == SEG_ARC))

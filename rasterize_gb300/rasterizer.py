@@ -207,10 +207,17 @@ class Scene:
     view = canvas: a Group of Fills goes through ``rz_render_scene``, anything
     else through ``rz_render_scene_tree``."""
 
+    _version = 0  # bumped by every mutation of any Scene: packed trees are reused only while it is unchanged
+
     def __init__(self, kind: str = "group", children=None, **params):
         self.kind = kind
         self.children = list(children or [])  # fills as (path, tr, rule, paint) tuples, or Scenes
         self.params = params
+        self._packed = None
+        self._tree = None
+
+    def _touch(self):
+        Scene._version += 1
         self._packed = None
 
     # ---- builders
@@ -219,7 +226,7 @@ class Scene:
         if self.kind != "group":
             raise TypeError("fill() appends to a group")
         self.children.append((path, tr or Transform.identity(), FillRule(fill_rule), paint))
-        self._packed = None
+        self._touch()
         return self
 
     def stroke(self, path: Path, paint, style, tr: Transform | None = None):
@@ -228,7 +235,7 @@ class Scene:
         if self.kind != "group":
             raise TypeError("stroke() appends to a group")
         self.children.append(Scene("stroke", path=path, paint=paint, style=style, tr=tr or Transform.identity()))
-        self._packed = None
+        self._touch()
         return self
 
     def add(self, child: "Scene"):
@@ -236,7 +243,7 @@ class Scene:
         if self.kind != "group":
             raise TypeError("add() appends to a group")
         self.children.append(child)
-        self._packed = None
+        self._touch()
         return self
 
     @staticmethod
@@ -543,8 +550,11 @@ class GpuRasterizer(Rasterizer):
                 self.ctx.check(lib.rz_render_scene_rgba8(self.ctx.ptr, ctypes.byref(s), self.flatness, bg_p,
                                                          rgba8.ctypes.data, width, height))
             return
-        entries, nodes, n_nodes = scene.entries_and_nodes()
-        s, keep = _pack_entries(entries)
+        if scene._tree is None or scene._tree[0] != Scene._version:
+            entries, nodes, n_nodes = scene.entries_and_nodes()
+            s, keep = _pack_entries(entries)
+            scene._tree = (Scene._version, s, keep, nodes, n_nodes)
+        _, s, keep, nodes, n_nodes = scene._tree
         self.ctx.check(lib.rz_render_scene_tree(self.ctx.ptr, ctypes.byref(s), ctypes.addressof(nodes), n_nodes,
                                                 self.flatness, bg_p,
                                                 canvas.ctypes.data if canvas is not None else None,
