@@ -71,18 +71,33 @@ __device__ __forceinline__ Band diff_band(const DiffDev& D, const FillDev& f, fl
 }
 
 
-// Accumulates the lines of (fill, band) entry e into the band, which the
-// previous scan left cleared.  Barriers before (the previous scan is done with
-// the band) and after.
-__device__ void diff_accumulate(const DiffDev& D, uint32_t e, const Band& B) {
-    const SceneDev& S = D.S;
-    __syncthreads();
-    const uint32_t n = S.entry_count[e], start = S.entry_start[e];
-    for (uint32_t j = threadIdx.x; j < n; j += kDiffThreads) {
-        const uint32_t l = S.pairs[start + j];
-        accumulate_vtx(B, line_vtx(S.lines[2ull * l], B.y0), line_vtx(S.lines[2ull * l + 1], B.y0));
+
+// Marks a superset of the accumulation words that accumulate_vtx writes for
+// the line a -> b: in every band row the line reaches (rows widened by 0.01),
+// its x range there clamped to [0, width] like the x rules, one word more on
+// each side and the carry word after it.
+__device__ void diff_mark(const Band& B, const VtxQ& a, const VtxQ& b, uint32_t* bits, int wpr) {
+    const float ax = (float)a.col + a.fx, bx = (float)b.col + b.fx;
+    const float ay = (float)a.row + a.fy, by = (float)b.row + b.fy;
+    if (ay == by) return;  // no signed height
+    const float ylo = fminf(ay, by), yhi = fmaxf(ay, by);
+    const int r0 = max((int)floorf(ylo - 0.01f), 0), r1 = min((int)floorf(yhi + 0.01f), B.bh - 1);
+    const float inv = 1.f / (by - ay), dx = bx - ax;
+    const int cmax = B.width_i + 2;
+    for (int r = r0; r <= r1; ++r) {
+        const float t0 = fminf(fmaxf(((float)r - 0.01f - ay) * inv, 0.f), 1.f);
+        const float t1 = fminf(fmaxf(((float)r + 1.01f - ay) * inv, 0.f), 1.f);
+        const float x0 = fmaf(t0, dx, ax), x1 = fmaf(t1, dx, ax);
+        const float xl = fminf(fmaxf(fminf(x0, x1), 0.f), B.width_f);
+        const float xh = fminf(fmaxf(fmaxf(x0, x1), 0.f), B.width_f);
+        const int c0 = max((int)floorf(xl) - 1, 0), c1 = min((int)floorf(xh) + 2, cmax);
+        uint32_t* row = bits + r * wpr;
+        for (int w = c0 >> 5; w <= (c1 >> 5); ++w) {
+            const int lo = max(c0 - (w << 5), 0), hi = min(c1 - (w << 5), 31);
+            const uint32_t upto = hi == 31 ? 0xffffffffu : ((1u << (hi + 1)) - 1u);
+            atomicOr(&row[w], upto & ~((1u << lo) - 1u));
+        }
     }
-    __syncthreads();
 }
 
 // Clears the band words of a row past the scanned columns (lines write up to
@@ -94,47 +109,55 @@ __device__ __forceinline__ void clear_row_tail(int4* row4, int width, int stride
 // ---------------------------------------------------------------------------
 // Forward
 // ---------------------------------------------------------------------------
-// Row prefix of the band (clearing it as it reads), fill rule, and
+// Row prefix of one band row (clearing it as it reads), fill rule, and
 // A += a alpha (1 - A) for the pixels the fill does not skip (|alpha| < 1e-6,
-// src/rasterize.rs:347-349).  One warp per row, 4 pixels per lane.
-__device__ void diff_scan_blend(const Band& B, int width, int rule, float alpha, float* A) {
-    const int lane = threadIdx.x & 31;
-    for (int r = threadIdx.x >> 5; r < B.bh; r += kDiffThreads / 32) {
-        int4* row4 = reinterpret_cast<int4*>(B.acc + r * B.stride);
-        uint32_t carry = 0;
-        for (int x0 = 0; x0 < width; x0 += 128) {
-            const int x = x0 + 4 * lane;
-            int4 v = make_int4(0, 0, 0, 0);
-            if (x < width) {
-                v = row4[x >> 2];
-                row4[x >> 2] = make_int4(0, 0, 0, 0);
-            }
-            const uint32_t a0 = (uint32_t)v.x;
-            const uint32_t a1 = a0 + (x + 1 < width ? (uint32_t)v.y : 0u);
-            const uint32_t a2 = a1 + (x + 2 < width ? (uint32_t)v.z : 0u);
-            const uint32_t a3 = a2 + (x + 3 < width ? (uint32_t)v.w : 0u);
-            uint32_t incl = a3;
-            #pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                const uint32_t o = __shfl_up_sync(0xffffffffu, incl, off);
-                if (lane >= off) incl += o;
-            }
-            const uint32_t base = carry + incl - a3;
-            carry += __shfl_sync(0xffffffffu, incl, 31);
-            const uint32_t wv[4] = {base + a0, base + a1, base + a2, base + a3};
-            #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                if (x + i >= width) break;
-                const float al = alpha_from_winding_fix(rule, (int32_t)wv[i]);
-                if (al < 1e-6f) continue;
-                float& d = A[r * width + x + i];
-                d = fmaf(alpha * al, 1.f - d, d);
-            }
+// src/rasterize.rs:347-349).  One warp, 4 pixels per lane.
+__device__ void diff_scan_blend_row(float* crow, int stride, int width, int rule, float alpha, float* Arow, int lane) {
+    int4* row4 = reinterpret_cast<int4*>(crow);
+    uint32_t carry = 0;
+    for (int x0 = 0; x0 < width; x0 += 128) {
+        const int x = x0 + 4 * lane;
+        int4 v = make_int4(0, 0, 0, 0);
+        if (x < width) {
+            v = row4[x >> 2];
+            row4[x >> 2] = make_int4(0, 0, 0, 0);
         }
-        clear_row_tail(row4, width, B.stride, lane);
+        const uint32_t a0 = (uint32_t)v.x;
+        const uint32_t a1 = a0 + (x + 1 < width ? (uint32_t)v.y : 0u);
+        const uint32_t a2 = a1 + (x + 2 < width ? (uint32_t)v.z : 0u);
+        const uint32_t a3 = a2 + (x + 3 < width ? (uint32_t)v.w : 0u);
+        uint32_t incl = a3;
+        #pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t o = __shfl_up_sync(0xffffffffu, incl, off);
+            if (lane >= off) incl += o;
+        }
+        const uint32_t base = carry + incl - a3;
+        carry += __shfl_sync(0xffffffffu, incl, 31);
+        const uint32_t wv[4] = {base + a0, base + a1, base + a2, base + a3};
+        #pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            if (x + i >= width) break;
+            const float al = alpha_from_winding_fix(rule, (int32_t)wv[i]);
+            if (al < 1e-6f) continue;
+            float& d = Arow[x + i];
+            d = fmaf(alpha * al, 1.f - d, d);
+        }
     }
+    clear_row_tail(row4, width, stride, lane);
 }
 
+// Whether the line a -> b (rows relative to a one-row band) can write the
+// row: it has a signed height and reaches [-0.01, 1.01].
+__device__ __forceinline__ bool line_reaches_row(const VtxQ& a, const VtxQ& b) {
+    const float ay = (float)a.row + a.fy, by = (float)b.row + b.fy;
+    return ay != by && fminf(ay, by) < 1.01f && fmaxf(ay, by) > -0.01f;
+}
+
+// One warp per band row, with no block barrier after the start: rows are
+// independent (a line writes only its own rows' words), so each warp takes
+// every path's lines that reach its row, accumulates them into its row
+// (int32 shared atomics), then scans and blends the row.
 __global__ void __launch_bounds__(kDiffThreads, 4) k_diff_forward(DiffDev D, int cov_stride) {
     extern __shared__ float4 sm4[];
     float* cov = reinterpret_cast<float*>(sm4);
@@ -146,17 +169,34 @@ __global__ void __launch_bounds__(kDiffThreads, 4) k_diff_forward(DiffDev D, int
     const int img = row_base / D.height;
     for (int i = threadIdx.x; i < rows * D.width; i += kDiffThreads) A[i] = 0.f;
     for (int i = threadIdx.x; i < (rows * cov_stride) >> 2; i += kDiffThreads) sm4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp >= rows) return;
+    float* crow = cov + warp * cov_stride;
+    float* Arow = A + warp * D.width;
+    const int row = row_base + warp;
     for (int p = 0; p < D.paths; ++p) {
         const FillDev& f = S.fills[img * D.paths + p];
         const uint32_t e = f.entry0 + (band - f.band0);
-        if (S.entry_count[e] == 0) continue;  // no line in the band: no coverage
-        const Band B = diff_band(D, f, cov, row_base, rows);
-        diff_accumulate(D, e, B);
-        diff_scan_blend(B, D.width, D.rule, D.alpha, A);
+        const uint32_t n = S.entry_count[e];
+        if (n == 0) continue;  // no line in the band: no coverage
+        const Band B = diff_band(D, f, crow, row, 1);
+        const uint32_t start = S.entry_start[e];
+        bool any = false;
+        for (uint32_t j = lane; j < n; j += 32) {
+            const uint32_t l = S.pairs[start + j];
+            const VtxQ a = line_vtx(S.lines[2ull * l], B.y0), b = line_vtx(S.lines[2ull * l + 1], B.y0);
+            if (!line_reaches_row(a, b)) continue;
+            any = true;
+            accumulate_vtx(B, a, b);
+        }
+        if (!__any_sync(0xffffffffu, any)) continue;  // no crossing in this row: the winding is 0 along it
+        __syncwarp();
+        diff_scan_blend_row(crow, cov_stride, D.width, D.rule, D.alpha, Arow, lane);
+        __syncwarp();
     }
-    __syncthreads();
-    float* out = D.out + (uint64_t)row_base * D.width;  // canvas rows are image rows
-    for (int i = threadIdx.x; i < rows * D.width; i += kDiffThreads) out[i] = A[i];
+    float* out = D.out + (uint64_t)row * D.width;  // canvas rows are image rows
+    for (int i = lane; i < D.width; i += 32) out[i] = Arow[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -195,7 +235,7 @@ __device__ __forceinline__ Dual dlerp(const Dual& a, const Dual& b, const Dual& 
 // where a line of the path crosses it, and those pixels are among the
 // accumulation words the lines write.  Every other pixel has an integer
 // winding, so its dalpha/dw is 0.  `bits` marks a superset of the written
-// words.  After diff_sparse_rows, each marked word of the band holds g there
+// words.  After diff_sparse_row, each marked word of the row holds g there
 // (as float bits) and P the inclusive prefix of g along the row; tot[r] is the
 // row's sum.
 struct CellView {
@@ -224,48 +264,6 @@ struct CellView {
         }
     }
 };
-
-// Marks a superset of the accumulation words that accumulate_vtx writes for
-// the line a -> b: in every band row the line reaches (rows widened by 0.01),
-// its x range there clamped to [0, width] like the x rules, one word more on
-// each side and the carry word after it.
-__device__ void diff_mark(const Band& B, const VtxQ& a, const VtxQ& b, uint32_t* bits, int wpr) {
-    const float ax = (float)a.col + a.fx, bx = (float)b.col + b.fx;
-    const float ay = (float)a.row + a.fy, by = (float)b.row + b.fy;
-    if (ay == by) return;  // no signed height
-    const float ylo = fminf(ay, by), yhi = fmaxf(ay, by);
-    const int r0 = max((int)floorf(ylo - 0.01f), 0), r1 = min((int)floorf(yhi + 0.01f), B.bh - 1);
-    const float inv = 1.f / (by - ay), dx = bx - ax;
-    const int cmax = B.width_i + 2;
-    for (int r = r0; r <= r1; ++r) {
-        const float t0 = fminf(fmaxf(((float)r - 0.01f - ay) * inv, 0.f), 1.f);
-        const float t1 = fminf(fmaxf(((float)r + 1.01f - ay) * inv, 0.f), 1.f);
-        const float x0 = fmaf(t0, dx, ax), x1 = fmaf(t1, dx, ax);
-        const float xl = fminf(fmaxf(fminf(x0, x1), 0.f), B.width_f);
-        const float xh = fminf(fmaxf(fmaxf(x0, x1), 0.f), B.width_f);
-        const int c0 = max((int)floorf(xl) - 1, 0), c1 = min((int)floorf(xh) + 2, cmax);
-        uint32_t* row = bits + r * wpr;
-        for (int w = c0 >> 5; w <= (c1 >> 5); ++w) {
-            const int lo = max(c0 - (w << 5), 0), hi = min(c1 - (w << 5), 31);
-            const uint32_t upto = hi == 31 ? 0xffffffffu : ((1u << (hi + 1)) - 1u);
-            atomicOr(&row[w], upto & ~((1u << lo) - 1u));
-        }
-    }
-}
-
-// diff_accumulate, marking the words it writes.
-__device__ void diff_accumulate_marked(const DiffDev& D, uint32_t e, const Band& B, uint32_t* bits, int wpr) {
-    const SceneDev& S = D.S;
-    __syncthreads();
-    const uint32_t n = S.entry_count[e], start = S.entry_start[e];
-    for (uint32_t j = threadIdx.x; j < n; j += kDiffThreads) {
-        const uint32_t l = S.pairs[start + j];
-        const VtxQ a = line_vtx(S.lines[2ull * l], B.y0), b = line_vtx(S.lines[2ull * l + 1], B.y0);
-        accumulate_vtx(B, a, b);
-        diff_mark(B, a, b, bits, wpr);
-    }
-    __syncthreads();
-}
 
 // Mean of W_r over [lo, hi] (x relative to column c0) and its derivatives,
 // W_r(X) = G[k+1] + (k + 1 - X) g[k] on [k, k+1).
@@ -377,89 +375,74 @@ __device__ void diff_line(float ax, float ay, float bx, float by, int rows, int 
     }
 }
 
-// Sparse row pass, one warp per row, over the marked words in increasing
+// Sparse pass over one row (one warp), over the marked words in increasing
 // order (32 at a time, skipping empty bitmask words): the exact integer
 // windings there (the prefix of the marked words; the others are 0),
 // g = dL/dA * a (1 - A) / (1 - a alpha) * dalpha/dw, and the inclusive prefix
-// P of g.  g overwrites the coverage word, P goes to its own array.
-__device__ void diff_sparse_rows(const DiffDev& D, const Band& B, int row_base, const uint32_t* bits, float* cov,
-                                 float* P, float* tot) {
-    const int lane = threadIdx.x & 31;
-    const int wpr = (B.stride + 31) >> 5, W = D.width;
-    for (int r = threadIdx.x >> 5; r < B.bh; r += kDiffThreads / 32) {
-        const uint32_t* brow = bits + r * wpr;
-        int32_t* crow = reinterpret_cast<int32_t*>(cov + r * B.stride);
-        float* prow = P + r * B.stride;
-        const float* Arow = D.image + (uint64_t)(row_base + r) * W;
-        const float* dlrow = D.dl_dimage + (uint64_t)(row_base + r) * W;
-        uint32_t wcarry = 0;
-        float gcarry = 0.f;
-        for (int w0 = 0; w0 < wpr; w0 += 32) {
-            const uint32_t mine = w0 + lane < wpr ? brow[w0 + lane] : 0u;
-            uint32_t nz = __ballot_sync(0xffffffffu, mine != 0u);
-            while (nz) {
-                const int j = __ffs(nz) - 1;
-                nz &= nz - 1u;
-                const uint32_t word = __shfl_sync(0xffffffffu, mine, j);
-                const int x = ((w0 + j) << 5) + lane;
-                const bool set = (word >> lane) & 1u;
-                const uint32_t d = set ? (uint32_t)crow[x] : 0u;
-                uint32_t wi = d;
-                #pragma unroll
-                for (int off = 1; off < 32; off <<= 1) {
-                    const uint32_t o = __shfl_up_sync(0xffffffffu, wi, off);
-                    if (lane >= off) wi += o;
-                }
-                const int32_t wn = (int32_t)(wcarry + wi);  // winding at pixel x
-                wcarry += __shfl_sync(0xffffffffu, wi, 31);
-                float gv = 0.f;
-                if (set && x < W) {
-                    const float al = alpha_from_winding_fix(D.rule, wn);
-                    if (al >= 1e-6f) {  // pixels the forward skips have no slope
-                        float da = 0.f;
-                        if (D.rule == 1) {
-                            const int32_t fo = (int32_t)(((uint32_t)wn + (1u << 22)) & ((1u << 23) - 1u)) - (1 << 22);
-                            da = fo > 0 ? 1.f : -1.f;
-                        } else if (al < 1.f) {
-                            da = wn > 0 ? 1.f : -1.f;
-                        }
-                        if (da != 0.f) gv = dlrow[x] * D.alpha * (1.f - Arow[x]) / (1.f - D.alpha * al) * da;
-                    }
-                }
-                float gi = gv;
-                #pragma unroll
-                for (int off = 1; off < 32; off <<= 1) {
-                    const float o = __shfl_up_sync(0xffffffffu, gi, off);
-                    if (lane >= off) gi += o;
-                }
-                if (set) {
-                    crow[x] = __float_as_int(gv);
-                    prow[x] = gcarry + gi;
-                }
-                gcarry += __shfl_sync(0xffffffffu, gi, 31);
+// P of g.  g overwrites the coverage word, P goes to its own row; *tot gets
+// the row's sum.
+__device__ void diff_sparse_row(const DiffDev& D, int wpr, int row, const uint32_t* brow, float* cov_row,
+                                float* prow, float* tot, int lane) {
+    const int W = D.width;
+    int32_t* crow = reinterpret_cast<int32_t*>(cov_row);
+    const float* Arow = D.image + (uint64_t)row * W;
+    const float* dlrow = D.dl_dimage + (uint64_t)row * W;
+    uint32_t wcarry = 0;
+    float gcarry = 0.f;
+    for (int w0 = 0; w0 < wpr; w0 += 32) {
+        const uint32_t mine = w0 + lane < wpr ? brow[w0 + lane] : 0u;
+        uint32_t nz = __ballot_sync(0xffffffffu, mine != 0u);
+        while (nz) {
+            const int j = __ffs(nz) - 1;
+            nz &= nz - 1u;
+            const uint32_t word = __shfl_sync(0xffffffffu, mine, j);
+            const int x = ((w0 + j) << 5) + lane;
+            const bool set = (word >> lane) & 1u;
+            const uint32_t d = set ? (uint32_t)crow[x] : 0u;
+            uint32_t wi = d;
+            #pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t o = __shfl_up_sync(0xffffffffu, wi, off);
+                if (lane >= off) wi += o;
             }
+            const int32_t wn = (int32_t)(wcarry + wi);  // winding at pixel x
+            wcarry += __shfl_sync(0xffffffffu, wi, 31);
+            float gv = 0.f;
+            if (set && x < W) {
+                const float al = alpha_from_winding_fix(D.rule, wn);
+                if (al >= 1e-6f) {  // pixels the forward skips have no slope
+                    float da = 0.f;
+                    if (D.rule == 1) {
+                        const int32_t fo = (int32_t)(((uint32_t)wn + (1u << 22)) & ((1u << 23) - 1u)) - (1 << 22);
+                        da = fo > 0 ? 1.f : -1.f;
+                    } else if (al < 1.f) {
+                        da = wn > 0 ? 1.f : -1.f;
+                    }
+                    if (da != 0.f) gv = dlrow[x] * D.alpha * (1.f - Arow[x]) / (1.f - D.alpha * al) * da;
+                }
+            }
+            float gi = gv;
+            #pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const float o = __shfl_up_sync(0xffffffffu, gi, off);
+                if (lane >= off) gi += o;
+            }
+            if (set) {
+                crow[x] = __float_as_int(gv);
+                prow[x] = gcarry + gi;
+            }
+            gcarry += __shfl_sync(0xffffffffu, gi, 31);
         }
-        if (lane == 0) tot[r] = gcarry;
     }
+    if (lane == 0) *tot = gcarry;
 }
 
-// Clears the marked words of the band and the bitmask.
-__device__ void diff_sparse_clear(const Band& B, uint32_t* bits, float* cov) {
-    const int wpr = (B.stride + 31) >> 5;
-    for (int i = threadIdx.x; i < B.bh * wpr; i += kDiffThreads) {
-        uint32_t word = bits[i];
-        if (!word) continue;
-        bits[i] = 0u;
-        const int r = i / wpr, x0 = (i - r * wpr) << 5;
-        float* row = cov + r * B.stride + x0;
-        while (word) {
-            row[__ffs(word) - 1] = 0.f;
-            word &= word - 1u;
-        }
-    }
-}
-
-// 3 CTAs per SM (<= 85 registers): the kernel is latency-bound, resident warps hide it
+// 3 CTAs per SM (<= 85 registers).  One warp per band row with no block
+// barrier after the start (rows are independent, and so are paths given the
+// forward image): for each path the warp accumulates the lines that reach its
+// row, marking the words they write, runs the sparse row pass, differentiates
+// its row's share of every line and chains it to the control points, then
+// clears the marked words.
 __global__ void __launch_bounds__(kDiffThreads, 3) k_diff_backward(DiffDev D, int cov_stride) {
     extern __shared__ float4 sm4[];
     const SceneDev& S = D.S;
@@ -475,26 +458,45 @@ __global__ void __launch_bounds__(kDiffThreads, 3) k_diff_backward(DiffDev D, in
     float2* out = reinterpret_cast<float2*>(D.out);
     for (int i = threadIdx.x; i < rows * cov_stride; i += kDiffThreads) cov[i] = 0.f;
     for (int i = threadIdx.x; i < rows * wpr; i += kDiffThreads) bits[i] = 0u;
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp >= rows) return;
+    float* crow = cov + warp * cov_stride;
+    float* prow = P + warp * cov_stride;
+    uint32_t* brow = bits + warp * wpr;
+    const int row = row_base + warp;
     for (int p = 0; p < D.paths; ++p) {
         const uint32_t fi = (uint32_t)(img * D.paths + p);
         const FillDev& f = S.fills[fi];
         const uint32_t e = f.entry0 + (band - f.band0);
         const uint32_t n = S.entry_count[e];
         if (n == 0) continue;  // no line in the band: zero coverage and no line to move
-        const Band B = diff_band(D, f, cov, row_base, rows);
-        diff_accumulate_marked(D, e, B, bits, wpr);  // also waits for the previous path's clear
-        diff_sparse_rows(D, B, row_base, bits, cov, P, tot);
-        __syncthreads();
-        const CellView V{bits, cov, P, tot, wpr, cov_stride, D.width};
+        const Band B = diff_band(D, f, crow, row, 1);
         const uint32_t start = S.entry_start[e];
-        for (uint32_t j = threadIdx.x; j < n; j += kDiffThreads) {
+        bool any = false;
+        for (uint32_t j = lane; j < n; j += 32) {
+            const uint32_t l = S.pairs[start + j];
+            const VtxQ a = line_vtx(S.lines[2ull * l], B.y0), b = line_vtx(S.lines[2ull * l + 1], B.y0);
+            if (!line_reaches_row(a, b)) continue;
+            any = true;
+            accumulate_vtx(B, a, b);
+            diff_mark(B, a, b, brow, wpr);
+        }
+        if (!__any_sync(0xffffffffu, any)) continue;  // nothing written in this row, nothing to move
+        __syncwarp();
+        diff_sparse_row(D, wpr, row, brow, crow, prow, tot + warp, lane);
+        __syncwarp();
+        const CellView V{brow, crow, prow, tot + warp, wpr, cov_stride, D.width};
+        for (uint32_t j = lane; j < n; j += 32) {
             const uint32_t l = S.pairs[start + j];
             const uint2 code = S.leaf[l];
             if (code.x == 0xffffffffu) continue;  // a closing line (zero length here)
             const VtxQ a = line_vtx(S.lines[2ull * l], B.y0), b = line_vtx(S.lines[2ull * l + 1], B.y0);
+            const float ay = (float)a.row + a.fy, by = (float)b.row + b.fy;
+            if (!(fminf(ay, by) < 1.0f && fmaxf(ay, by) >= 0.0f)) continue;  // no share of this row
             const int c0 = a.col;
             float d4[4] = {0.f, 0.f, 0.f, 0.f};
-            diff_line(a.fx, (float)a.row + a.fy, (float)(b.col - c0) + b.fx, (float)b.row + b.fy, rows, c0, V, d4);
+            diff_line(a.fx, ay, (float)(b.col - c0) + b.fx, by, 1, c0, V, d4);
             if (d4[0] == 0.f && d4[1] == 0.f && d4[2] == 0.f && d4[3] == 0.f) continue;
             // chain to the control points: Bernstein weights at the frozen tree's parameters
             const uint32_t seg = code.x;
@@ -514,8 +516,19 @@ __global__ void __launch_bounds__(kDiffThreads, 3) k_diff_backward(DiffDev D, in
                 atomicAdd(&o[idx[q]].y, d4[1] * b0[q] + d4[3] * b1[q]);
             }
         }
-        __syncthreads();
-        diff_sparse_clear(B, bits, cov);
+        __syncwarp();
+        // clear the marked words and the bitmask
+        for (int w = lane; w < wpr; w += 32) {
+            uint32_t word = brow[w];
+            if (!word) continue;
+            brow[w] = 0u;
+            float* c = crow + (w << 5);
+            while (word) {
+                c[__ffs(word) - 1] = 0.f;
+                word &= word - 1u;
+            }
+        }
+        __syncwarp();
     }
 }
 
