@@ -58,17 +58,6 @@ __global__ void k_diff_segments(const float* __restrict__ ctrl, uint32_t n_paths
 // ---------------------------------------------------------------------------
 constexpr int kDiffThreads = 256;
 
-__device__ __forceinline__ Band diff_band(const DiffDev& D, const FillDev& f, float* cov, int row_base, int rows) {
-    Band B;
-    B.acc = cov;
-    B.stride = band_stride(f.clip_width);
-    B.bh = rows;
-    B.y0 = row_base - f.row0;
-    B.img_h = f.height;
-    B.width_f = (float)f.clip_width;
-    B.width_i = f.clip_width;
-    return B;
-}
 
 
 
@@ -147,6 +136,36 @@ __device__ void diff_scan_blend_row(float* crow, int stride, int width, int rule
     clear_row_tail(row4, width, stride, lane);
 }
 
+// The band's line list of paths p0 + lane (one per lane, 32 at a time):
+// every lane loads its path's (fill, band) entry at once instead of one path
+// after the other.  n = 0 for paths past the image's last.
+__device__ __forceinline__ void path_entries(const DiffDev& D, int img, int band, int p0, int lane, uint32_t& n,
+                                             uint32_t& start) {
+    n = 0;
+    start = 0;
+    const int p = p0 + lane;
+    if (p < D.paths) {
+        const FillDev& f = D.S.fills[img * D.paths + p];
+        const uint32_t e = f.entry0 + (band - f.band0);
+        n = D.S.entry_count[e];
+        start = D.S.entry_start[e];
+    }
+}
+
+// The one-row band of image row `row` for the differentiable batch: every
+// path's fill is the whole image (view W x H at canvas row img * H, clip W).
+__device__ __forceinline__ Band diff_row_band(const DiffDev& D, float* crow, int row, int img) {
+    Band B;
+    B.acc = crow;
+    B.stride = band_stride(D.width);
+    B.bh = 1;
+    B.y0 = row - img * D.height;
+    B.img_h = D.height;
+    B.width_f = (float)D.width;
+    B.width_i = D.width;
+    return B;
+}
+
 // Whether the line a -> b (rows relative to a one-row band) can write the
 // row: it has a signed height and reaches [-0.01, 1.01].
 __device__ __forceinline__ bool line_reaches_row(const VtxQ& a, const VtxQ& b) {
@@ -175,13 +194,15 @@ __global__ void __launch_bounds__(kDiffThreads, 4) k_diff_forward(DiffDev D, int
     float* crow = cov + warp * cov_stride;
     float* Arow = A + warp * D.width;
     const int row = row_base + warp;
-    for (int p = 0; p < D.paths; ++p) {
-        const FillDev& f = S.fills[img * D.paths + p];
-        const uint32_t e = f.entry0 + (band - f.band0);
-        const uint32_t n = S.entry_count[e];
-        if (n == 0) continue;  // no line in the band: no coverage
-        const Band B = diff_band(D, f, crow, row, 1);
-        const uint32_t start = S.entry_start[e];
+    const Band B = diff_row_band(D, crow, row, img);
+    for (int p0 = 0; p0 < D.paths; p0 += 32) {
+        uint32_t my_n, my_start;
+        path_entries(D, img, band, p0, lane, my_n, my_start);
+        uint32_t todo = __ballot_sync(0xffffffffu, my_n != 0);  // paths with no line in the band add nothing
+      while (todo) {
+        const int q = __ffs(todo) - 1;
+        todo &= todo - 1u;
+        const uint32_t n = __shfl_sync(0xffffffffu, my_n, q), start = __shfl_sync(0xffffffffu, my_start, q);
         bool any = false;
         for (uint32_t j = lane; j < n; j += 32) {
             const uint32_t l = S.pairs[start + j];
@@ -194,6 +215,7 @@ __global__ void __launch_bounds__(kDiffThreads, 4) k_diff_forward(DiffDev D, int
         __syncwarp();
         diff_scan_blend_row(crow, cov_stride, D.width, D.rule, D.alpha, Arow, lane);
         __syncwarp();
+      }
     }
     float* out = D.out + (uint64_t)row * D.width;  // canvas rows are image rows
     for (int i = lane; i < D.width; i += 32) out[i] = Arow[i];
@@ -465,14 +487,15 @@ __global__ void __launch_bounds__(kDiffThreads, 3) k_diff_backward(DiffDev D, in
     float* prow = P + warp * cov_stride;
     uint32_t* brow = bits + warp * wpr;
     const int row = row_base + warp;
-    for (int p = 0; p < D.paths; ++p) {
-        const uint32_t fi = (uint32_t)(img * D.paths + p);
-        const FillDev& f = S.fills[fi];
-        const uint32_t e = f.entry0 + (band - f.band0);
-        const uint32_t n = S.entry_count[e];
-        if (n == 0) continue;  // no line in the band: zero coverage and no line to move
-        const Band B = diff_band(D, f, crow, row, 1);
-        const uint32_t start = S.entry_start[e];
+    const Band B = diff_row_band(D, crow, row, img);
+    for (int p0 = 0; p0 < D.paths; p0 += 32) {
+        uint32_t my_n, my_start;
+        path_entries(D, img, band, p0, lane, my_n, my_start);
+        uint32_t todo = __ballot_sync(0xffffffffu, my_n != 0);  // no line in the band: nothing to move
+      while (todo) {
+        const int q = __ffs(todo) - 1;
+        todo &= todo - 1u;
+        const uint32_t n = __shfl_sync(0xffffffffu, my_n, q), start = __shfl_sync(0xffffffffu, my_start, q);
         bool any = false;
         for (uint32_t j = lane; j < n; j += 32) {
             const uint32_t l = S.pairs[start + j];
@@ -529,6 +552,7 @@ __global__ void __launch_bounds__(kDiffThreads, 3) k_diff_backward(DiffDev D, in
             }
         }
         __syncwarp();
+      }
     }
 }
 
