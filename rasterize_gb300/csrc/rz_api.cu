@@ -13,7 +13,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <condition_variable>
 #include <cstring>
+#include <deque>
+#include <functional>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -168,8 +171,98 @@ struct Trace {
     }
 };
 
+// A persistent pool of host threads (up to 15 workers besides the caller),
+// started on first use, so the host-side parallel loops of every call do not
+// pay for thread creation.  run(n, fn) calls fn(i) for every i in [0, n):
+// the caller and whichever workers are free take items one at a time, and it
+// returns when all are done and no worker still holds the job.  Jobs from
+// several threads queue; a worker-run item may start a job of its own (its
+// caller works through it, so nothing waits on a busy pool).
+struct PoolJob {
+    std::function<void(int64_t)> fn;
+    int64_t n = 0;
+    std::atomic<int64_t> next{0};
+    std::atomic<int64_t> done{0};
+    int refs = 0;  // workers inside the job (guarded by the pool's mutex)
+};
+
+class HostPool {
+  public:
+    static HostPool& get() {
+        static HostPool pool;
+        return pool;
+    }
+    void run(int64_t n, std::function<void(int64_t)> fn) {
+        if (n <= 0) return;
+        if (workers_.empty() || n == 1) {
+            for (int64_t i = 0; i < n; ++i) fn(i);
+            return;
+        }
+        PoolJob job;
+        job.fn = std::move(fn);
+        job.n = n;
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            queue_.push_back(&job);
+        }
+        work_.notify_all();
+        for (int64_t i = job.next.fetch_add(1); i < n; i = job.next.fetch_add(1)) {
+            job.fn(i);
+            job.done.fetch_add(1);
+        }
+        std::unique_lock<std::mutex> lk(mu_);
+        for (auto it = queue_.begin(); it != queue_.end(); ++it)
+            if (*it == &job) {
+                queue_.erase(it);
+                break;
+            }
+        finished_.wait(lk, [&] { return job.done.load() == n && job.refs == 0; });
+    }
+    ~HostPool() {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+        }
+        work_.notify_all();
+        for (auto& t : workers_) t.join();
+    }
+
+  private:
+    HostPool() {
+        const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+        for (int i = 1; i < std::min(hw, 16); ++i) workers_.emplace_back([this] { loop(); });
+    }
+    void loop() {
+        for (;;) {
+            PoolJob* j = nullptr;
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                work_.wait(lk, [&] { return stop_ || !queue_.empty(); });
+                if (stop_) return;
+                j = queue_.front();
+                ++j->refs;
+            }
+            for (int64_t i = j->next.fetch_add(1); i < j->n; i = j->next.fetch_add(1)) {
+                j->fn(i);
+                j->done.fetch_add(1);
+            }
+            {
+                std::lock_guard<std::mutex> lk(mu_);
+                if (!queue_.empty() && queue_.front() == j) queue_.pop_front();
+                --j->refs;
+            }
+            finished_.notify_all();
+        }
+    }
+    std::mutex mu_;
+    std::condition_variable work_, finished_;
+    std::deque<PoolJob*> queue_;
+    std::vector<std::thread> workers_;
+    bool stop_ = false;
+};
+
 // Runs fn(lo, hi) over [0, n) split across the host cores (up to 16
-// threads); small ranges run on the calling thread.
+// chunks); small ranges run on the calling thread.
 template <class F>
 void parallel_for(int64_t n, int64_t min_per_thread, F fn) {
     const int64_t hw = std::max<int64_t>(1, (int64_t)std::thread::hardware_concurrency());
@@ -178,36 +271,18 @@ void parallel_for(int64_t n, int64_t min_per_thread, F fn) {
         fn((int64_t)0, n);
         return;
     }
-    std::vector<std::thread> th;
-    th.reserve((size_t)t - 1);
     const int64_t chunk = (n + t - 1) / t;
-    for (int64_t i = 1; i < t; ++i) {
+    HostPool::get().run(t, [&](int64_t i) {
         const int64_t lo = i * chunk, hi = std::min(n, lo + chunk);
-        if (lo < hi) th.emplace_back(fn, lo, hi);
-    }
-    fn((int64_t)0, std::min(n, chunk));
-    for (auto& x : th) x.join();
+        if (lo < hi) fn(lo, hi);
+    });
 }
 
-// fn(i) for i in [0, n) on up to 16 host threads taking one item at a time
-// (items of very different cost).
+// fn(i) for i in [0, n) on the pool, one item at a time (items of very
+// different cost).
 template <typename F>
 void parallel_each(int64_t n, F fn) {
-    const int64_t hw = std::max<int64_t>(1, (int64_t)std::thread::hardware_concurrency());
-    const int64_t t = std::min<int64_t>({hw, 16, n});
-    std::atomic<int64_t> next{0};
-    auto work = [&]() {
-        for (int64_t i = next.fetch_add(1); i < n; i = next.fetch_add(1)) fn(i);
-    };
-    if (t <= 1) {
-        work();
-        return;
-    }
-    std::vector<std::thread> th;
-    th.reserve((size_t)t - 1);
-    for (int64_t i = 1; i < t; ++i) th.emplace_back(work);
-    work();
-    for (auto& x : th) x.join();
+    HostPool::get().run(n, [&](int64_t i) { fn(i); });
 }
 
 // Device address of page-locked host memory the GPU can write directly
