@@ -497,9 +497,15 @@ rz_status stage_host(rz_ctx* ctx, const uint8_t* kind, const double* pts, uint32
     RZ_CUDA(cudaStreamSynchronize(ctx->stream));
     char* h = (char*)ctx->h_stage.p;
     size_t o = 0;
-    auto put = [&](const void* src, size_t n) {
+    auto put = [&](const void* src, size_t n) {  // large arrays are copied by all host threads
         char* dst = h + o;
-        if (n) std::memcpy(dst, src, n);
+        if (n) {
+            const int64_t chunks = (int64_t)((n + (1u << 20) - 1) >> 20);
+            parallel_for(chunks, 2, [&](int64_t c0, int64_t c1) {
+                const size_t b0 = (size_t)c0 << 20, b1 = std::min(n, (size_t)c1 << 20);
+                std::memcpy(dst + b0, (const char*)src + b0, b1 - b0);
+            });
+        }
         o += al(n);
         return dst;
     };
