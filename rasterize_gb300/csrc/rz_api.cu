@@ -28,6 +28,7 @@
 #include "rz_host_stroke.cpp.inc"
 #include "rz_kernels.cuh"
 #include "rz_pipeline.cuh"
+#include "rz_stroke.cuh"
 
 namespace rz {
 cudaError_t init_kernels();
@@ -127,6 +128,9 @@ struct rz_ctx {
     DevBuf p_rgba8, p_encode_in;
     // scene-tree layers by nesting depth: colour layers and clip masks
     std::vector<DevBuf> layer_pool, mask_pool;
+    // the device stroker's unit table, counts and offsets, its compact offset
+    // pieces, and the merged segment arrays it builds (swapped with d_kind / d_pts)
+    DevBuf s_units, s_styles, s_counts, s_off, s_fin, s_tmpk, s_tmpp, s_kind, s_pts;
     // batch tuning (rz_tune_batch / rz_set_tuning): band height cap, resident CTAs per SM (0 = occupancy)
     int tune_rows_cap = 256;
     int tune_ctas = 0;
@@ -420,6 +424,9 @@ void rz_destroy(rz_ctx* c) {
                       &c->p_pairs,  &c->p_scan,    &c->p_canvas,  &c->p_leaf,    &c->d_loss,    &c->p_rgba8,
                       &c->p_encode_in};
     for (DevBuf* b : bufs) b->release();
+    for (DevBuf* b : {&c->s_units, &c->s_styles, &c->s_counts, &c->s_off, &c->s_fin, &c->s_tmpk, &c->s_tmpp,
+                      &c->s_kind, &c->s_pts})
+        b->release();
     for (DevBuf& b : c->layer_pool) b.release();
     for (DevBuf& b : c->mask_pool) b.release();
     c->h_stage.release();
@@ -1611,7 +1618,22 @@ struct SceneTree {
     std::vector<OptBox> node_bbox;
     std::vector<rzhost::Xf> node_tr;
     std::vector<uint8_t> node_cached;
+    // stroke outlines (made on the device): host copies for bboxes, their own
+    // subpath offsets (okind / opts local), entry j's outline subpaths
+    // [ofsub[j], ofsub[j + 1]); the merged subpath table the pipeline reads
+    std::vector<uint8_t> okind;
+    std::vector<double> opts;
+    std::vector<uint32_t> osub, ofsub, merged_sub;
+    uint32_t outline_sub0 = 0;
 };
+
+// Entry e's subpaths in the subpath table the pipeline reads.
+uint32_t ent_sub0(const SceneTree& T, uint32_t e) {
+    return e < T.sc->n_fills ? T.fsub[e] : T.outline_sub0 + T.ofsub[e - T.sc->n_fills];
+}
+uint32_t ent_sub1(const SceneTree& T, uint32_t e) {
+    return e < T.sc->n_fills ? T.fsub[e + 1] : T.outline_sub0 + T.ofsub[e - T.sc->n_fills + 1];
+}
 
 // Checks the pre-order node array and records every subtree's end.
 rz_status parse_tree(rz_ctx* ctx, SceneTree& T, uint32_t i, int depth, uint32_t& out_end) {
@@ -1659,10 +1681,19 @@ rz_status parse_tree(rz_ctx* ctx, SceneTree& T, uint32_t i, int depth, uint32_t&
 rzhost::Xf entry_tr(const SceneTree& T, uint32_t f) { return T.E[f].own; }
 
 // Path::bbox(tr) of fill entry f (its own transform applied first)
+// Path::bbox(tr) of entry f's path as it is (a stroke outline's from the
+// host copy of the outlines).
+bool entry_path_bbox(const SceneTree& T, uint32_t f, const rzhost::Xf& tr, rzhost::Box& out) {
+    if (f < T.sc->n_fills)
+        return rzhost::path_bbox(T.base.kind, T.base.pts, T.base.sub_off, T.fsub[f], T.fsub[f + 1], tr, out);
+    const uint32_t j = f - T.sc->n_fills;
+    return rzhost::path_bbox(T.okind.data(), T.opts.data(), T.osub.data(), T.ofsub[j], T.ofsub[j + 1], tr, out);
+}
+
+// Path::bbox(tr) of fill entry f (its own transform applied first)
 OptBox entry_bbox(const SceneTree& T, uint32_t f, const rzhost::Xf& tr) {
     OptBox r;
-    r.ok = rzhost::path_bbox(T.base.kind, T.base.pts, T.base.sub_off, T.fsub[f], T.fsub[f + 1],
-                             rzhost::xf_mul(tr, entry_tr(T, f)), r.b);
+    r.ok = entry_path_bbox(T, f, rzhost::xf_mul(tr, entry_tr(T, f)), r.b);
     return r;
 }
 
@@ -1903,14 +1934,12 @@ void plan_rec(const SceneTree& T, TreePlan& P, int pid, PlanLayer& L) {
         const rz_paint& paint = T.sc->paints[T.E[p.entry].paint];
         rzhost::Box ubox{};
         bool have_u = false;
-        if (paint.units == RZ_UNITS_BOUNDING_BOX)
-            have_u = rzhost::path_bbox(T.base.kind, T.base.pts, T.base.sub_off, T.fsub[p.entry], T.fsub[p.entry + 1],
-                                       kIdentity, ubox);
+        if (paint.units == RZ_UNITS_BOUNDING_BOX) have_u = entry_path_bbox(T, p.entry, kIdentity, ubox);
         rz::PaintDev pd;
         prepare_paint(paint, tr_fill, have_u, ubox, pd);
         if (pd.kind < 0) return;
         P.hs.paints.push_back(pd);
-        add_fill(P.hs, T.fsub[p.entry], T.fsub[p.entry + 1], (int)col_min, (int)row_min, vw, vh, vw, tr_fill,
+        add_fill(P.hs, ent_sub0(T, p.entry), ent_sub1(T, p.entry), (int)col_min, (int)row_min, vw, vh, vw, tr_fill,
                  T.E[p.entry].rule, (int)P.hs.paints.size() - 1);
         return;
     }
@@ -2062,6 +2091,171 @@ rz_status run_plan(rz_ctx* ctx, TreePlan& P, double flatness, float* canvas, int
     }
     tr.gpu_mark(ctx->stream, "layers");
     return read_error(ctx);
+}
+
+// Every Stroke node's outline on the device (rz_stroke.cu), appended to the
+// staged segments; each outline becomes one more fill entry (NonZero, the
+// stroked entry's paint and own transform).  The host lays out the units of
+// every outline subpath, turns the kernels' counts into offsets and keeps a
+// copy of the outlines for the bounding boxes.
+rz_status stroke_on_device(rz_ctx* ctx, SceneTree& T, const rz_scene* scene, const rz_scene_node* nodes,
+                           uint32_t n_nodes) {
+    Trace tr("stroke_on_device");
+    std::vector<rz::StrokeStyleDev> styles;
+    struct List {
+        uint32_t u0, u1;  // units [u0, u1)
+        uint32_t entry;   // outline entry (local index)
+    };
+    std::vector<uint32_t> stroke_nodes;
+    for (uint32_t i = 0; i < n_nodes; ++i) {
+        const rz_scene_node& nd = nodes[i];
+        if (nd.kind != RZ_NODE_STROKE) continue;
+        stroke_nodes.push_back(i);
+        styles.push_back(rz::StrokeStyleDev{nd.width, nd.miter_limit, nd.line_join, nd.line_cap});
+    }
+    // every input subpath of every Stroke node: 4 m units from `base` (built on the device)
+    std::vector<rz::StrokeSub> subs;
+    std::vector<List> lists;
+    uint64_t n_units = 0;
+    for (uint32_t j = 0; j < stroke_nodes.size(); ++j) {
+        const rz_scene_node& nd = nodes[stroke_nodes[j]];
+        for (uint32_t sp = T.fsub[nd.arg]; sp < T.fsub[nd.arg + 1]; ++sp) {
+            const uint32_t s0 = T.base.sub_off[sp], s1 = T.base.sub_off[sp + 1];
+            if (s1 <= s0) continue;
+            const uint32_t in_sp = ctx->expanded ? ctx->x_submap[sp] : sp;
+            const uint32_t closed = scene->subpath_closed && scene->subpath_closed[in_sp] ? 1u : 0u;
+            const uint32_t m = s1 - s0;
+            subs.push_back(rz::StrokeSub{n_units, s0, m, closed, j});
+            if (closed) {
+                lists.push_back({(uint32_t)n_units, (uint32_t)(n_units + 2 * m), j});
+                lists.push_back({(uint32_t)(n_units + 2 * m), (uint32_t)(n_units + 4 * m), j});
+            } else {
+                lists.push_back({(uint32_t)n_units, (uint32_t)(n_units + 4 * m), j});
+            }
+            n_units += 4ull * m;
+        }
+    }
+    if (n_units >= 0xffffffffull) return fail(ctx, RZ_ERR_INVALID, "scene tree: too many stroked segments");
+    const uint32_t nu = (uint32_t)n_units;
+    // device buffers of the context (kept between calls)
+    DevBuf &d_units = ctx->s_units, &d_styles = ctx->s_styles, &d_counts = ctx->s_counts, &d_off = ctx->s_off,
+           &d_fin = ctx->s_fin, &d_tmpk = ctx->s_tmpk, &d_tmpp = ctx->s_tmpp, &d_kind = ctx->s_kind,
+           &d_pts = ctx->s_pts;
+    RZ_CUDA(d_units.ensure((size_t)nu * sizeof(rz::StrokeUnit) + subs.size() * sizeof(rz::StrokeSub) + 32));
+    RZ_CUDA(d_styles.ensure(styles.size() * sizeof(rz::StrokeStyleDev) + 16));
+    RZ_CUDA(d_counts.ensure((size_t)nu * 4 + 16));
+    RZ_CUDA(d_off.ensure((size_t)nu * 8 + 16));
+    RZ_CUDA(d_fin.ensure((size_t)nu * 8 + 16));
+    rz::StrokeUnit* units_dev = (rz::StrokeUnit*)d_units.p;
+    rz::StrokeSub* subs_dev = (rz::StrokeSub*)((char*)d_units.p + (((size_t)nu * sizeof(rz::StrokeUnit) + 15) & ~(size_t)15));
+    RZ_CUDA(cudaMemcpyAsync(subs_dev, subs.data(), subs.size() * sizeof(rz::StrokeSub), cudaMemcpyHostToDevice,
+                            ctx->stream));
+    RZ_CUDA(rz::launch_stroke_units(subs_dev, (uint32_t)subs.size(), units_dev, nu, ctx->stream));
+    RZ_CUDA(cudaMemcpyAsync(d_styles.p, styles.data(), styles.size() * sizeof(rz::StrokeStyleDev),
+                            cudaMemcpyHostToDevice, ctx->stream));
+    rz::StrokeArgs A{};
+    A.units = (const rz::StrokeUnit*)d_units.p;
+    A.n_units = nu;
+    A.styles = (const rz::StrokeStyleDev*)d_styles.p;
+    A.kind = (const uint8_t*)ctx->d_kind.p;
+    A.pts = (const double*)ctx->d_pts.p;
+    A.counts = (uint32_t*)d_counts.p;
+    A.off_start = (const uint64_t*)d_off.p;
+    A.fin_start = (const uint64_t*)d_fin.p;
+    // offsets: one pass into kStrokeOffsetMax slots per OFFSET unit when that
+    // buffer stays under 4 GiB, else counted first and packed
+    std::vector<uint32_t> counts(nu);
+    std::vector<uint64_t> start(nu);
+    const uint64_t n_offset_units = n_units / 2;  // one OFFSET unit in two
+    A.strided = n_offset_units * rz::kStrokeOffsetMax * 65 <= (4ull << 30);
+    tr.mark("units");
+    uint64_t n_off = 0;
+    if (A.strided) {
+        for (const rz::StrokeSub& sb : subs)  // OFFSET units: even positions of each subpath's way out and back
+            for (uint64_t i = 0; i < 4ull * sb.m; ++i) {
+                start[sb.base + i] = n_off;
+                if (!(i & 1u)) n_off += rz::kStrokeOffsetMax;
+            }
+    } else {
+        RZ_CUDA(rz::launch_stroke(A, 0, ctx->stream));
+        RZ_CUDA(cudaMemcpyAsync(counts.data(), d_counts.p, (size_t)nu * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+        for (const rz::StrokeSub& sb : subs)
+            for (uint64_t i = 0; i < 4ull * sb.m; ++i) {
+                start[sb.base + i] = n_off;
+                if (!(i & 1u)) n_off += counts[sb.base + i];
+            }
+    }
+    RZ_CUDA(cudaMemcpyAsync(d_off.p, start.data(), (size_t)nu * 8, cudaMemcpyHostToDevice, ctx->stream));
+    RZ_CUDA(d_tmpk.ensure(n_off + 16));
+    RZ_CUDA(d_tmpp.ensure(n_off * 64 + 16));
+    A.tmp_kind = (uint8_t*)d_tmpk.p;
+    A.tmp_pts = (double*)d_tmpp.p;
+    RZ_CUDA(rz::launch_stroke(A, 1, ctx->stream));
+    // joins, caps and closes: count, lay out the whole outline
+    RZ_CUDA(rz::launch_stroke(A, 2, ctx->stream));
+    RZ_CUDA(cudaMemcpyAsync(counts.data(), d_counts.p, (size_t)nu * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+    tr.mark("offset_emit_join_count");
+    uint64_t n_out = 0;
+    for (uint32_t u = 0; u < nu; ++u) {
+        start[u] = n_out;
+        n_out += counts[u];
+    }
+    const uint64_t n_seg = T.base.n_seg;
+    if (n_seg + n_out > 0xfffffff0ull) return fail(ctx, RZ_ERR_INVALID, "scene tree: stroke outlines too large");
+    RZ_CUDA(cudaMemcpyAsync(d_fin.p, start.data(), (size_t)nu * 8, cudaMemcpyHostToDevice, ctx->stream));
+    // the merged segment arrays: the staged segments, then the outlines
+    RZ_CUDA(d_kind.ensure(n_seg + n_out + 16));
+    RZ_CUDA(d_pts.ensure((n_seg + n_out) * 64 + 64));
+    if (n_seg) {
+        RZ_CUDA(cudaMemcpyAsync(d_kind.p, ctx->d_kind.p, n_seg, cudaMemcpyDeviceToDevice, ctx->stream));
+        RZ_CUDA(cudaMemcpyAsync(d_pts.p, ctx->d_pts.p, n_seg * 64, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    A.out_kind = (uint8_t*)d_kind.p + n_seg;
+    A.out_pts = (double*)d_pts.p + 8 * n_seg;
+    RZ_CUDA(rz::launch_stroke(A, 3, ctx->stream));
+    RZ_CUDA(rz::launch_stroke(A, 4, ctx->stream));
+    tr.gpu_mark(ctx->stream, "join_emit_gather");
+    // host copy of the outlines (bounding boxes) and the subpath tables
+    T.okind.resize(n_out);
+    T.opts.resize(n_out * 8);
+    if (n_out) {
+        RZ_CUDA(cudaMemcpyAsync(T.okind.data(), A.out_kind, n_out, cudaMemcpyDeviceToHost, ctx->stream));
+        RZ_CUDA(cudaMemcpyAsync(T.opts.data(), A.out_pts, n_out * 64, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    // Path::push drops empty lists; every list is one closed outline subpath of its node's entry
+    T.osub.assign(1, 0);
+    T.ofsub.assign(stroke_nodes.size() + 1, 0);
+    size_t li = 0;
+    for (uint32_t j = 0; j < stroke_nodes.size(); ++j) {
+        T.ofsub[j] = (uint32_t)T.osub.size() - 1;
+        for (; li < lists.size() && lists[li].entry == j; ++li) {
+            const uint64_t end = lists[li].u1 == nu ? n_out : start[lists[li].u1];
+            if (end > start[lists[li].u0]) T.osub.push_back((uint32_t)end);
+        }
+    }
+    T.ofsub[stroke_nodes.size()] = (uint32_t)T.osub.size() - 1;
+    // merged subpath table: the staged one, then the outlines' (segment indices after the staged ones)
+    const uint32_t n_sub = T.base.n_sub;
+    T.merged_sub.assign(T.base.sub_off, T.base.sub_off + n_sub + 1);
+    for (size_t k = 1; k < T.osub.size(); ++k) T.merged_sub.push_back((uint32_t)(n_seg + T.osub[k]));
+    for (uint32_t j = 0; j < stroke_nodes.size(); ++j) {
+        const uint32_t i = stroke_nodes[j];
+        T.stroke_of[i] = (uint32_t)T.E.size();
+        T.E.push_back(TreeEntry{T.E[nodes[i].arg].own, RZ_FILL_NONZERO, T.E[nodes[i].arg].paint});
+    }
+    T.outline_sub0 = n_sub;  // outline entry j: merged subpaths n_sub + [ofsub[j], ofsub[j + 1])
+    RZ_CUDA(ctx->d_sub.ensure(T.merged_sub.size() * 4 + 16));
+    RZ_CUDA(cudaMemcpyAsync(ctx->d_sub.p, T.merged_sub.data(), T.merged_sub.size() * 4, cudaMemcpyHostToDevice,
+                            ctx->stream));
+    RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+    std::swap(ctx->d_kind, d_kind);  // the staged-only arrays become next call's merged buffers
+    std::swap(ctx->d_pts, d_pts);
+    T.base.sub_off = T.merged_sub.data();
+    T.base.n_seg = (uint32_t)(n_seg + n_out);
+    T.base.n_sub = (uint32_t)T.merged_sub.size() - 1;
+    return RZ_OK;
 }
 
 // Scene-table checks shared by the flat and tree renders.
@@ -2395,67 +2589,12 @@ rz_status rz_render_scene_tree(rz_ctx* ctx, const rz_scene* scene, const rz_scen
         T.E[f].paint = scene->fill_paint[f];
     }
     T.stroke_of.assign(n_nodes, 0);
-    std::vector<uint8_t> mk;
-    std::vector<double> mp;
-    std::vector<uint32_t> ms, mfs;
+    st = stage_scene_segments(ctx, scene->seg_kind, scene->seg_pts, scene->n_segments, scene->subpath_off,
+                              scene->n_subpaths, scene->fill_subpath_off, F, T.base, T.fsub);
+    if (st) return st;
     bool strokes = false;
     for (uint32_t i = 0; i < n_nodes; ++i) strokes = strokes || nodes[i].kind == RZ_NODE_STROKE;
-    if (strokes) {
-        const uint32_t S0 = F ? scene->fill_subpath_off[F] : 0;
-        const uint32_t seg_end = scene->n_subpaths ? scene->subpath_off[S0] : 0;
-        mk.assign(scene->seg_kind, scene->seg_kind + seg_end);
-        mp.assign(scene->seg_pts, scene->seg_pts + 8ull * seg_end);
-        if (scene->n_subpaths) ms.assign(scene->subpath_off, scene->subpath_off + S0 + 1);
-        else ms.push_back(0);
-        mfs.assign(scene->fill_subpath_off, scene->fill_subpath_off + F + 1);
-        if (!F) mfs.assign(1, 0);
-        // every Stroke node's outline, computed in parallel, then appended in node order
-        std::vector<uint32_t> sn;
-        for (uint32_t i = 0; i < n_nodes; ++i)
-            if (nodes[i].kind == RZ_NODE_STROKE) sn.push_back(i);
-        struct Outline {
-            std::vector<uint8_t> k;
-            std::vector<double> p;
-            std::vector<uint32_t> ends;
-            rz_status st = RZ_OK;
-        };
-        std::vector<Outline> outl(sn.size());
-        // the largest outline first, so no thread is left with one at the end
-        std::stable_sort(sn.begin(), sn.end(), [&](uint32_t a, uint32_t b) {
-            const uint32_t* fo = scene->fill_subpath_off;
-            auto segs = [&](uint32_t i) { return scene->subpath_off[fo[nodes[i].arg + 1]] - scene->subpath_off[fo[nodes[i].arg]]; };
-            return segs(a) > segs(b);
-        });
-        parallel_each((int64_t)sn.size(), [&](int64_t j) {
-            const rz_scene_node& nd = nodes[sn[j]];
-            const rz_stroke_style style{nd.width, nd.miter_limit, nd.line_join, nd.line_cap};
-            outl[j].st = stroke_subpaths(scene->seg_kind, scene->seg_pts, scene->subpath_off, scene->subpath_closed,
-                                         scene->fill_subpath_off[nd.arg], scene->fill_subpath_off[nd.arg + 1], style,
-                                         outl[j].k, outl[j].p, outl[j].ends);
-        });
-        // appended in node order
-        std::vector<size_t> order(sn.size());
-        for (size_t j = 0; j < sn.size(); ++j) order[j] = j;
-        std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return sn[a] < sn[b]; });
-        for (size_t j : order) {
-            if (outl[j].st) return fail(ctx, outl[j].st, "scene tree: cannot stroke a path");
-            const size_t base = mk.size();
-            mk.insert(mk.end(), outl[j].k.begin(), outl[j].k.end());
-            mp.insert(mp.end(), outl[j].p.begin(), outl[j].p.end());
-            for (uint32_t e : outl[j].ends) ms.push_back((uint32_t)base + e);
-            mfs.push_back((uint32_t)ms.size() - 1);
-            const uint32_t e0 = nodes[sn[j]].arg;
-            T.stroke_of[sn[j]] = (uint32_t)T.E.size();
-            T.E.push_back(TreeEntry{T.E[e0].own, RZ_FILL_NONZERO, T.E[e0].paint});
-        }
-        if (mk.size() > 0xffffffffull || ms.size() > 0xffffffffull)
-            return fail(ctx, RZ_ERR_INVALID, "scene tree: stroke outlines too large");
-        st = stage_scene_segments(ctx, mk.data(), mp.data(), (uint32_t)mk.size(), ms.data(), (uint32_t)ms.size() - 1,
-                                  mfs.data(), (uint32_t)T.E.size(), T.base, T.fsub);
-    } else {
-        st = stage_scene_segments(ctx, scene->seg_kind, scene->seg_pts, scene->n_segments, scene->subpath_off,
-                                  scene->n_subpaths, scene->fill_subpath_off, F, T.base, T.fsub);
-    }
+    if (strokes) st = stroke_on_device(ctx, T, scene, nodes, n_nodes);
     if (st) return st;
     tr.mark("stage_segments");
     // Pipeline::build with view = the canvas, tr = identity (src/scene.rs:186-199)
