@@ -1299,7 +1299,8 @@ struct HostScene {
 int choose_band_rows(int canvas_w, int canvas_h, bool paint_mode) {
     const int stride = rz::band_stride(canvas_w);
     const int per_row = 4 * stride + (paint_mode ? 16 * canvas_w : 0);
-    int rows = std::max(1, (paint_mode ? 96 * 1024 : 64 * 1024) / per_row);
+    // coverage only: tall bands (one CTA per SM) amortise a long line's binary64 set-up per band
+    int rows = std::max(1, (paint_mode ? 96 * 1024 : 200 * 1024) / per_row);
     rows = std::min(rows, 64);
     return std::max(1, std::min(rows, std::max(canvas_h, 1)));
 }
