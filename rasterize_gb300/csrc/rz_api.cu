@@ -1545,742 +1545,7 @@ rz_status stroke_subpaths(const uint8_t* kind, const double* pts, const uint32_t
     return RZ_OK;
 }
 
-// ---------------------------------------------------------------------------
-// Scene trees: Pipeline::build_rec / render_rec and Layer (src/scene.rs:222-565)
-// ---------------------------------------------------------------------------
-// A pipeline node (src/scene.rs:222-246): the node's rendering bbox and
-// transform; FILL and CLIP name a fill entry of the scene (CLIP: its path and
-// rule), OPACITY and CLIP have one child.
-struct PNode {
-    int kind = 0;
-    rzhost::Box bbox{};
-    rzhost::Xf tr{};
-    uint32_t entry = 0;
-    std::vector<int> children;
-    float opacity = 1.0f;
-    rzhost::Xf clip_tr{};
-};
-
-struct OptBox {
-    bool ok = false;
-    rzhost::Box b{};
-};
-
-const rzhost::Xf kIdentity{{1, 0, 0, 0, 1, 0}};
-
-// BBox::intersect (src/geometry.rs:648-657 with range_intersect :677-688)
-OptBox box_intersect(const rzhost::Box& a, const rzhost::Box& o) {
-    OptBox r;
-    if (a.x0 > o.x1 || o.x0 > a.x1 || a.y0 > o.y1 || o.y0 > a.y1) return r;
-    r.ok = true;
-    r.b = rzhost::box_new(rzhost::P2{std::fmax(a.x0, o.x0), std::fmax(a.y0, o.y0)},
-                          rzhost::P2{std::fmin(a.x1, o.x1), std::fmin(a.y1, o.y1)});
-    return r;
-}
-
-// BBox::union (src/geometry.rs:636-638)
-rzhost::Box box_union(const rzhost::Box& a, const rzhost::Box& o) {
-    return rzhost::box_extend(rzhost::box_extend(a, rzhost::P2{o.x0, o.y0}), rzhost::P2{o.x1, o.y1});
-}
-
-// BBox::unit_transform (src/geometry.rs:662-664): translate(x, y).pre_scale(w, h)
-rzhost::Xf unit_transform(const rzhost::Box& b) {
-    const rzhost::Xf t{{1, 0, b.x0, 0, 1, b.y0}}, s{{b.x1 - b.x0, 0, 0, 0, b.y1 - b.y0, 0}};
-    return rzhost::xf_mul(t, s);
-}
-
-// view_apply (src/scene.rs:276-282)
-OptBox view_apply(const OptBox& view, const OptBox& bbox) {
-    if (!view.ok) return bbox;
-    if (!bbox.ok) return OptBox{};
-    return box_intersect(view.b, bbox.b);
-}
-
-// A fill entry of the tree: the scene's fill entries, then one per Stroke
-// node holding its outline (filled NonZero with the stroked entry's paint).
-struct TreeEntry {
-    rzhost::Xf own;   // the entry's own transform
-    int rule;
-    uint32_t paint;
-};
-
-struct SceneTree {
-    const rz_scene* sc = nullptr;
-    const rz_scene_node* nodes = nullptr;
-    uint32_t n = 0;
-    std::vector<uint32_t> end;        // end[i]: the index after node i's subtree
-    std::vector<TreeEntry> E;
-    std::vector<uint32_t> stroke_of;  // Stroke node -> its outline's entry
-    HostScene base;                   // staged segment arrays
-    std::vector<uint32_t> fsub;       // entry e: staged subpaths [fsub[e], fsub[e + 1])
-    std::vector<PNode> P;
-    // Fill and Stroke nodes' path bboxes under their ancestors' transforms,
-    // computed in parallel before build_rec
-    std::vector<OptBox> node_bbox;
-    std::vector<rzhost::Xf> node_tr;
-    std::vector<uint8_t> node_cached;
-    // stroke outlines (made on the device): host copies for bboxes, their own
-    // subpath offsets (okind / opts local), entry j's outline subpaths
-    // [ofsub[j], ofsub[j + 1]); the merged subpath table the pipeline reads
-    std::vector<uint8_t> okind;
-    std::vector<double> opts;
-    std::vector<uint32_t> osub, ofsub, merged_sub;
-    uint32_t outline_sub0 = 0;
-};
-
-// Entry e's subpaths in the subpath table the pipeline reads.
-uint32_t ent_sub0(const SceneTree& T, uint32_t e) {
-    return e < T.sc->n_fills ? T.fsub[e] : T.outline_sub0 + T.ofsub[e - T.sc->n_fills];
-}
-uint32_t ent_sub1(const SceneTree& T, uint32_t e) {
-    return e < T.sc->n_fills ? T.fsub[e + 1] : T.outline_sub0 + T.ofsub[e - T.sc->n_fills + 1];
-}
-
-// Checks the pre-order node array and records every subtree's end.
-rz_status parse_tree(rz_ctx* ctx, SceneTree& T, uint32_t i, int depth, uint32_t& out_end) {
-    if (i >= T.n) return fail(ctx, RZ_ERR_INVALID, "scene tree: a node's children run past n_nodes");
-    if (depth > 256) return fail(ctx, RZ_ERR_INVALID, "scene tree deeper than 256");
-    const rz_scene_node& nd = T.nodes[i];
-    uint32_t e = i + 1;
-    switch (nd.kind) {
-        case RZ_NODE_FILL:
-            if (nd.arg >= T.sc->n_fills) return fail(ctx, RZ_ERR_INVALID, "scene tree: fill entry out of range");
-            break;
-        case RZ_NODE_STROKE:
-            if (nd.arg >= T.sc->n_fills) return fail(ctx, RZ_ERR_INVALID, "scene tree: stroke entry out of range");
-            if (!(nd.width >= 0.0) || !std::isfinite(nd.width) || std::isnan(nd.miter_limit) ||
-                nd.line_join < RZ_JOIN_MITER || nd.line_join > RZ_JOIN_ROUND || nd.line_cap < RZ_CAP_BUTT ||
-                nd.line_cap > RZ_CAP_ROUND)
-                return fail(ctx, RZ_ERR_INVALID, "scene tree: bad stroke style");
-            break;
-        case RZ_NODE_GROUP:
-            for (uint32_t c = 0; c < nd.arg; ++c) {
-                rz_status st = parse_tree(ctx, T, e, depth + 1, e);
-                if (st) return st;
-            }
-            break;
-        case RZ_NODE_CLIP:
-            if (nd.arg >= T.sc->n_fills) return fail(ctx, RZ_ERR_INVALID, "scene tree: clip entry out of range");
-            if (nd.units != RZ_UNITS_USER_SPACE && nd.units != RZ_UNITS_BOUNDING_BOX)
-                return fail(ctx, RZ_ERR_INVALID, "scene tree: bad clip units");
-            // fallthrough: one child
-        case RZ_NODE_TRANSFORM:
-        case RZ_NODE_OPACITY: {
-            if (nd.kind == RZ_NODE_OPACITY && std::isnan(nd.opacity))
-                return fail(ctx, RZ_ERR_INVALID, "scene tree: opacity is NaN");
-            rz_status st = parse_tree(ctx, T, e, depth + 1, e);
-            if (st) return st;
-            break;
-        }
-        default: return fail(ctx, RZ_ERR_INVALID, "scene tree: unknown node kind");
-    }
-    T.end[i] = e;
-    out_end = e;
-    return RZ_OK;
-}
-
-rzhost::Xf entry_tr(const SceneTree& T, uint32_t f) { return T.E[f].own; }
-
-// Path::bbox(tr) of fill entry f (its own transform applied first)
-// Path::bbox(tr) of entry f's path as it is (a stroke outline's from the
-// host copy of the outlines).
-bool entry_path_bbox(const SceneTree& T, uint32_t f, const rzhost::Xf& tr, rzhost::Box& out) {
-    if (f < T.sc->n_fills)
-        return rzhost::path_bbox(T.base.kind, T.base.pts, T.base.sub_off, T.fsub[f], T.fsub[f + 1], tr, out);
-    const uint32_t j = f - T.sc->n_fills;
-    return rzhost::path_bbox(T.okind.data(), T.opts.data(), T.osub.data(), T.ofsub[j], T.ofsub[j + 1], tr, out);
-}
-
-// Path::bbox(tr) of fill entry f (its own transform applied first)
-OptBox entry_bbox(const SceneTree& T, uint32_t f, const rzhost::Xf& tr) {
-    OptBox r;
-    r.ok = entry_path_bbox(T, f, rzhost::xf_mul(tr, entry_tr(T, f)), r.b);
-    return r;
-}
-
-rzhost::Xf node_tr(const rz_scene_node& nd) {
-    rzhost::Xf t;
-    std::memcpy(t.m, nd.tr, sizeof(t.m));
-    return t;
-}
-
-// Scene::bbox (src/scene.rs:153-182)
-OptBox scene_bbox(const SceneTree& T, uint32_t i, const rzhost::Xf& tr) {
-    const rz_scene_node& nd = T.nodes[i];
-    switch (nd.kind) {
-        case RZ_NODE_FILL: return entry_bbox(T, nd.arg, tr);
-        case RZ_NODE_STROKE: return entry_bbox(T, nd.arg, tr);  // not including the stroke width
-        case RZ_NODE_GROUP: {
-            OptBox acc;
-            uint32_t c = i + 1;
-            for (uint32_t k = 0; k < nd.arg; ++k, c = T.end[c]) {
-                const OptBox cb = scene_bbox(T, c, tr);
-                if (acc.ok) {
-                    if (cb.ok) acc.b = box_union(acc.b, cb.b);
-                } else {
-                    acc = cb;
-                }
-            }
-            return acc;
-        }
-        case RZ_NODE_TRANSFORM: return scene_bbox(T, i + 1, rzhost::xf_mul(tr, node_tr(nd)));
-        case RZ_NODE_OPACITY: return scene_bbox(T, i + 1, tr);
-        default: {  // CLIP
-            rzhost::Xf clip_tr = tr;
-            if (nd.units == RZ_UNITS_BOUNDING_BOX) {
-                const OptBox cb = scene_bbox(T, i + 1, kIdentity);
-                if (!cb.ok) return OptBox{};
-                clip_tr = rzhost::xf_mul(tr, unit_transform(cb.b));
-            }
-            const OptBox child = scene_bbox(T, i + 1, tr);
-            if (!child.ok) return OptBox{};
-            const OptBox clip = entry_bbox(T, nd.arg, clip_tr);
-            if (!clip.ok) return OptBox{};
-            return box_intersect(child.b, clip.b);
-        }
-    }
-}
-
-// The transforms build_rec will see at every Fill and Stroke node (only
-// Transform nodes change it), and those nodes' path bboxes, in parallel.
-void precompute_bboxes(SceneTree& T) {
-    T.node_bbox.assign(T.n, OptBox{});
-    T.node_tr.assign(T.n, kIdentity);
-    T.node_cached.assign(T.n, 0);
-    std::vector<uint32_t> leaves;
-    std::vector<std::pair<uint32_t, rzhost::Xf>> stack;
-    if (T.n) stack.push_back({0u, kIdentity});
-    while (!stack.empty()) {
-        const uint32_t i = stack.back().first;
-        const rzhost::Xf tr = stack.back().second;
-        stack.pop_back();
-        const rz_scene_node& nd = T.nodes[i];
-        if (nd.kind == RZ_NODE_FILL || nd.kind == RZ_NODE_STROKE) {
-            T.node_tr[i] = tr;
-            leaves.push_back(i);
-        } else if (nd.kind == RZ_NODE_GROUP) {
-            uint32_t c = i + 1;
-            for (uint32_t k = 0; k < nd.arg; ++k, c = T.end[c]) stack.push_back({c, tr});
-        } else if (nd.kind == RZ_NODE_TRANSFORM) {
-            stack.push_back({i + 1, rzhost::xf_mul(tr, node_tr(nd))});
-        } else {
-            stack.push_back({i + 1, tr});
-        }
-    }
-    parallel_for((int64_t)leaves.size(), 4, [&](int64_t a, int64_t b) {
-        for (int64_t j = a; j < b; ++j) {
-            const uint32_t i = leaves[j];
-            const rz_scene_node& nd = T.nodes[i];
-            const uint32_t e = nd.kind == RZ_NODE_FILL ? nd.arg : T.stroke_of[i];
-            T.node_bbox[i] = entry_bbox(T, e, T.node_tr[i]);
-            T.node_cached[i] = 1;
-        }
-    });
-}
-
-// Pipeline::build_rec (src/scene.rs:268-357); -1 for None.  Children are
-// allocated before their parent, so the root is the last node.
-int build_rec(SceneTree& T, uint32_t i, const OptBox& view, const rzhost::Xf& tr) {
-    const rz_scene_node& nd = T.nodes[i];
-    PNode p;
-    p.tr = tr;
-    switch (nd.kind) {
-        case RZ_NODE_FILL:
-        case RZ_NODE_STROKE: {
-            // a Stroke is the Fill of its outline, NonZero (src/scene.rs:297-306)
-            const uint32_t e = nd.kind == RZ_NODE_FILL ? nd.arg : T.stroke_of[i];
-            const bool cached = T.node_cached[i] && std::memcmp(T.node_tr[i].m, tr.m, sizeof(tr.m)) == 0;
-            const OptBox b = view_apply(view, cached ? T.node_bbox[i] : entry_bbox(T, e, tr));
-            if (!b.ok) return -1;
-            p.kind = RZ_NODE_FILL;
-            p.bbox = b.b;
-            p.entry = e;
-            break;
-        }
-        case RZ_NODE_GROUP: {
-            OptBox acc;
-            uint32_t c = i + 1;
-            for (uint32_t k = 0; k < nd.arg; ++k, c = T.end[c]) {
-                const int id = build_rec(T, c, view, tr);
-                if (id < 0) continue;
-                p.children.push_back(id);
-                // fold(None, |acc, bbox| Some(bbox.union_opt(acc)))
-                acc.b = acc.ok ? box_union(T.P[id].bbox, acc.b) : T.P[id].bbox;
-                acc.ok = true;
-            }
-            if (!acc.ok) return -1;
-            p.kind = RZ_NODE_GROUP;
-            p.bbox = acc.b;
-            break;
-        }
-        case RZ_NODE_CLIP: {
-            rzhost::Xf clip_tr = tr;
-            if (nd.units == RZ_UNITS_BOUNDING_BOX) {
-                const OptBox cb = scene_bbox(T, i + 1, kIdentity);
-                if (!cb.ok) return -1;
-                clip_tr = rzhost::xf_mul(tr, unit_transform(cb.b));
-            }
-            const OptBox clip_bbox = view_apply(view, entry_bbox(T, nd.arg, clip_tr));
-            if (!clip_bbox.ok) return -1;
-            const int cid = build_rec(T, i + 1, clip_bbox, tr);
-            if (cid < 0) return -1;
-            const OptBox b = box_intersect(clip_bbox.b, T.P[cid].bbox);
-            if (!b.ok) return -1;
-            p.kind = RZ_NODE_CLIP;
-            p.bbox = b.b;
-            p.children.push_back(cid);
-            p.entry = nd.arg;
-            p.clip_tr = clip_tr;
-            break;
-        }
-        case RZ_NODE_OPACITY: {
-            const int cid = build_rec(T, i + 1, view, tr);
-            if (cid < 0) return -1;
-            p.kind = RZ_NODE_OPACITY;
-            p.bbox = T.P[cid].bbox;
-            p.children.push_back(cid);
-            // Scene::opacity clamps to [0, 1]; render_rec uses it as f32
-            p.opacity = (float)std::fmin(std::fmax(nd.opacity, 0.0), 1.0);
-            break;
-        }
-        default:  // TRANSFORM
-            return build_rec(T, i + 1, view, rzhost::xf_mul(tr, node_tr(nd)));
-    }
-    T.P.push_back(std::move(p));
-    return (int)T.P.size() - 1;
-}
-
-// The render of a scene tree is planned on the host, then launched without a
-// host round trip per layer: every fill of every layer (and every clip mask)
-// is flattened and binned by one pass of the line pipeline, and the plan's
-// operations -- layer initialisation, composites of a layer's fills, masks,
-// composes -- run in order on the stream.  Layers live in per-depth pools,
-// sized for the largest layer at each depth before anything is launched.
-struct TreeOp {
-    enum Kind { kFillColor, kClear, kComposite, kMask, kCompose } kind;
-    int depth = 0;          // target: 0 the canvas, d >= 1 layer_pool[d]; kMask / kClear of a mask: mask_pool[d]
-    bool mask_target = false;
-    int32_t w = 0, h = 0;   // target size
-    uint32_t f0 = 0, f1 = 0;  // kComposite / kMask: fills [f0, f1) of the plan's scene
-    int max_clip = 1;
-    // kCompose: src layer at depth + 1 onto the target, mask at mask_pool[depth] when has_mask
-    bool has_mask = false, scale = false;
-    float opacity = 1.0f;
-    int32_t drect[4] = {0, 0, 0, 0}, srect[4] = {0, 0, 0, 0}, mrect[4] = {0, 0, 0, 0};
-    int x0 = 0, y0 = 0, x1 = 0, y1 = 0;
-    float color[4] = {0, 0, 0, 0};
-};
-
-struct PlanLayer {
-    int32_t x = 0, y = 0, w = 0, h = 0;
-    int depth = 0;
-    uint32_t batch0 = 0;  // first fill of the layer's pending composite
-};
-
-struct TreePlan {
-    HostScene hs;  // every fill of the render (layers' fills and masks)
-    std::vector<TreeOp> ops;
-    std::vector<uint64_t> layer_bytes, mask_bytes;  // per depth
-};
-
-// Layer::new (src/scene.rs:483-501): floor of min, ceil of max.
-void layer_rect(const rzhost::Box& b, PlanLayer& L) {
-    L.x = (int32_t)std::floor(b.x0);
-    L.y = (int32_t)std::floor(b.y0);
-    L.w = std::max<int32_t>((int32_t)std::ceil(b.x1) - L.x, 0);
-    L.h = std::max<int32_t>((int32_t)std::ceil(b.y1) - L.y, 0);
-}
-
-void need(std::vector<uint64_t>& v, int depth, uint64_t bytes) {
-    if ((int)v.size() <= depth) v.resize(depth + 1, 0);
-    v[depth] = std::max(v[depth], bytes);
-}
-
-// The fills queued for L since its last composite become one composite.
-void plan_flush(TreePlan& P, PlanLayer& L) {
-    const uint32_t n = (uint32_t)P.hs.fills.size();
-    if (n > L.batch0) {
-        TreeOp op{};
-        op.kind = TreeOp::kComposite;
-        op.depth = L.depth;
-        op.w = L.w;
-        op.h = L.h;
-        op.f0 = L.batch0;
-        op.f1 = n;
-        for (uint32_t f = L.batch0; f < n; ++f) op.max_clip = std::max(op.max_clip, P.hs.fills[f].clip_width);
-        P.ops.push_back(op);
-    }
-    L.batch0 = n;
-}
-
-// Pipeline::render_rec (src/scene.rs:397-458) as a plan.
-void plan_rec(const SceneTree& T, TreePlan& P, int pid, PlanLayer& L) {
-    const PNode& p = T.P[pid];
-    if (p.kind == RZ_NODE_FILL) {
-        // the fill's view of the layer (max bounds are exclusive: max + 1) and the align transform
-        long col_min = (long)std::floor(p.bbox.x0) - L.x, col_max = (long)std::ceil(p.bbox.x1) - L.x + 1;
-        long row_min = (long)std::floor(p.bbox.y0) - L.y, row_max = (long)std::ceil(p.bbox.y1) - L.y + 1;
-        if (col_min < 0) col_min = L.w;  // `as usize` wraps; view_shape clamps (src/image.rs:588-605)
-        if (row_min < 0) row_min = L.h;
-        if (col_max < 0) col_max = L.w;
-        if (row_max < 0) row_max = L.h;
-        row_min = std::min<long>(row_min, L.h);
-        row_max = std::max(std::min<long>(row_max, L.h), row_min);
-        col_min = std::min<long>(col_min, L.w);
-        col_max = std::max(std::min<long>(col_max, L.w), col_min);
-        const int vw = (int)(col_max - col_min), vh = (int)(row_max - row_min);
-        if (vw <= 0 || vh <= 0) return;
-        const rzhost::Xf align{{1.0, 0.0, -std::floor(p.bbox.x0), 0.0, 1.0, -std::floor(p.bbox.y0)}};
-        const rzhost::Xf tr_fill = rzhost::xf_mul(rzhost::xf_mul(align, p.tr), entry_tr(T, p.entry));
-        const rz_paint& paint = T.sc->paints[T.E[p.entry].paint];
-        rzhost::Box ubox{};
-        bool have_u = false;
-        if (paint.units == RZ_UNITS_BOUNDING_BOX) have_u = entry_path_bbox(T, p.entry, kIdentity, ubox);
-        rz::PaintDev pd;
-        prepare_paint(paint, tr_fill, have_u, ubox, pd);
-        if (pd.kind < 0) return;
-        P.hs.paints.push_back(pd);
-        add_fill(P.hs, ent_sub0(T, p.entry), ent_sub1(T, p.entry), (int)col_min, (int)row_min, vw, vh, vw, tr_fill,
-                 T.E[p.entry].rule, (int)P.hs.paints.size() - 1);
-        return;
-    }
-    if (p.kind == RZ_NODE_GROUP) {
-        for (int c : p.children) plan_rec(T, P, c, L);
-        return;
-    }
-    // Opacity and Clip: the child renders into a fresh layer of its own
-    // (Pipeline::render, :384-395), then composes onto L
-    plan_flush(P, L);
-    PlanLayer C;
-    layer_rect(T.P[p.children[0]].bbox, C);
-    C.depth = L.depth + 1;
-    const uint64_t nc = (uint64_t)C.w * (uint64_t)C.h;
-    if (nc) {
-        need(P.layer_bytes, C.depth, nc * 16);
-        TreeOp clear{};
-        clear.kind = TreeOp::kClear;
-        clear.depth = C.depth;
-        clear.w = C.w;
-        clear.h = C.h;
-        P.ops.push_back(clear);
-        C.batch0 = (uint32_t)P.hs.fills.size();
-        plan_rec(T, P, p.children[0], C);
-        plan_flush(P, C);
-    }
-    TreeOp op{};
-    op.kind = TreeOp::kCompose;
-    op.depth = L.depth;
-    op.drect[0] = L.x, op.drect[1] = L.y, op.drect[2] = L.w, op.drect[3] = L.h;
-    op.srect[0] = C.x, op.srect[1] = C.y, op.srect[2] = C.w, op.srect[3] = C.h;
-    op.x0 = std::max(L.x, C.x), op.x1 = std::min(L.x + L.w, C.x + C.w);
-    op.y0 = std::max(L.y, C.y), op.y1 = std::min(L.y + L.h, C.y + C.h);
-    if (p.kind == RZ_NODE_OPACITY) {
-        op.scale = true;
-        op.opacity = p.opacity;
-    } else {
-        // Clip: the clip path's mask over the clip node's bbox (Path::mask, mask semantics)
-        PlanLayer M;
-        layer_rect(p.bbox, M);
-        const uint64_t nm = (uint64_t)M.w * (uint64_t)M.h;
-        need(P.mask_bytes, L.depth, nm * 4 + 16);
-        op.has_mask = true;
-        op.mrect[0] = M.x, op.mrect[1] = M.y, op.mrect[2] = M.w, op.mrect[3] = M.h;
-        if (nm) {
-            TreeOp clear{};
-            clear.kind = TreeOp::kClear;
-            clear.depth = L.depth;
-            clear.mask_target = true;
-            clear.w = M.w;
-            clear.h = M.h;
-            P.ops.push_back(clear);
-            const rzhost::Xf align{{1.0, 0.0, -(double)M.x, 0.0, 1.0, -(double)M.y}};
-            const rzhost::Xf t = rzhost::xf_mul(rzhost::xf_mul(align, p.clip_tr), entry_tr(T, p.entry));
-            TreeOp mk{};
-            mk.kind = TreeOp::kMask;
-            mk.depth = L.depth;
-            mk.mask_target = true;
-            mk.w = M.w;
-            mk.h = M.h;
-            mk.f0 = (uint32_t)P.hs.fills.size();
-            add_fill(P.hs, T.fsub[p.entry], T.fsub[p.entry + 1], 0, 0, M.w, M.h, M.w - 1, t, T.E[p.entry].rule, -1);
-            mk.f1 = (uint32_t)P.hs.fills.size();
-            mk.max_clip = std::max(1, M.w - 1);
-            if (mk.f1 > mk.f0) P.ops.push_back(mk);
-        }
-    }
-    if (nc) P.ops.push_back(op);
-    L.batch0 = (uint32_t)P.hs.fills.size();  // fills queued meanwhile belong to the child and the mask
-}
-
-// Launches the plan: one flatten + bin of every fill, then the operations.
-rz_status run_plan(rz_ctx* ctx, TreePlan& P, double flatness, float* canvas, int W, int H) {
-    Trace tr("scene_tree_plan");
-    HostScene& hs = P.hs;
-    for (size_t d = 0; d < P.layer_bytes.size(); ++d) {
-        if ((int)ctx->layer_pool.size() <= (int)d) ctx->layer_pool.resize(d + 1);
-        if (P.layer_bytes[d]) RZ_CUDA(ctx->layer_pool[d].ensure(P.layer_bytes[d] + 16));
-    }
-    for (size_t d = 0; d < P.mask_bytes.size(); ++d) {
-        if ((int)ctx->mask_pool.size() <= (int)d) ctx->mask_pool.resize(d + 1);
-        if (P.mask_bytes[d]) RZ_CUDA(ctx->mask_pool[d].ensure(P.mask_bytes[d]));
-    }
-    rz::SceneDev S{};
-    S.kind = (const uint8_t*)ctx->d_kind.p;
-    S.pts = (const double*)ctx->d_pts.p;
-    S.sub_off = (const uint32_t*)ctx->d_sub.p;
-    S.n_fills = (uint32_t)hs.fills.size();
-    S.n_slots = hs.n_slots;
-    S.n_segments = hs.n_seg;
-    S.n_subpaths = hs.n_sub;
-    S.task_depth = hs.task_depth;
-    S.thr64 = 16.0 * flatness * flatness;
-    S.thr32 = (float)S.thr64;
-    S.band_rows = hs.band_rows;
-    RZ_CUDA(ctx->d_ctrl.ensure(64));
-    RZ_CUDA(cudaMemsetAsync(ctx->d_ctrl.p, 0, 64, ctx->stream));
-    S.err = (int32_t*)ctx->d_ctrl.p;
-    S.counters = (int32_t*)ctx->d_ctrl.p + 4;
-    const rz::PaintDev* paints = nullptr;
-    if (!hs.fills.empty()) {
-        if (hs.paints.empty()) hs.paints.resize(1);
-        RZ_CUDA(ctx->p_paints.ensure(hs.paints.size() * sizeof(rz::PaintDev)));
-        RZ_CUDA(cudaMemcpyAsync(ctx->p_paints.p, hs.paints.data(), hs.paints.size() * sizeof(rz::PaintDev),
-                                cudaMemcpyHostToDevice, ctx->stream));
-        paints = (const rz::PaintDev*)ctx->p_paints.p;
-        rz_status st = build_lines(ctx, hs, S, tr, nullptr);
-        if (st) return st;
-    }
-    auto target = [&](const TreeOp& op) -> float* {
-        if (op.mask_target) return (float*)ctx->mask_pool[op.depth].p;
-        return op.depth == 0 ? canvas : (float*)ctx->layer_pool[op.depth].p;
-    };
-    for (const TreeOp& op : P.ops) {
-        switch (op.kind) {
-            case TreeOp::kFillColor:
-                RZ_CUDA(rz::launch_layer_fill(target(op), (uint64_t)op.w * op.h, op.color, ctx->stream));
-                break;
-            case TreeOp::kClear:
-                RZ_CUDA(cudaMemsetAsync(target(op), 0, (uint64_t)op.w * op.h * (op.mask_target ? 4 : 16),
-                                        ctx->stream));
-                break;
-            case TreeOp::kComposite:
-            case TreeOp::kMask: {
-                rz::SceneDev C = S;
-                C.fills = S.fills + op.f0;
-                C.n_fills = op.f1 - op.f0;
-                C.paints = op.kind == TreeOp::kComposite ? paints : nullptr;
-                C.canvas = target(op);
-                C.canvas_stride = op.w;
-                C.canvas_w = op.w;
-                C.canvas_h = op.h;
-                C.n_bands = (op.h + hs.band_rows - 1) / hs.band_rows;
-                C.load_canvas = op.kind == TreeOp::kComposite ? 1 : 0;
-                int cov_stride = 0;
-                const int smem = rz::composite_smem_bytes(op.w, hs.band_rows, op.max_clip, op.kind == TreeOp::kComposite,
-                                                          &cov_stride);
-                if (C.n_bands) RZ_CUDA(rz::launch_composite(C, cov_stride, smem, ctx->stream));
-                break;
-            }
-            case TreeOp::kCompose: {
-                const float* mask = op.has_mask ? (const float*)ctx->mask_pool[op.depth].p : nullptr;
-                RZ_CUDA(rz::launch_layer_compose(target(op), op.drect, (const float*)ctx->layer_pool[op.depth + 1].p,
-                                                 op.srect, mask, op.mrect, op.opacity, op.scale, op.x0, op.y0, op.x1,
-                                                 op.y1, ctx->stream));
-                break;
-            }
-        }
-    }
-    tr.gpu_mark(ctx->stream, "layers");
-    return read_error(ctx);
-}
-
-// Every Stroke node's outline on the device (rz_stroke.cu), appended to the
-// staged segments; each outline becomes one more fill entry (NonZero, the
-// stroked entry's paint and own transform).  The host lays out the units of
-// every outline subpath, turns the kernels' counts into offsets and keeps a
-// copy of the outlines for the bounding boxes.
-rz_status stroke_on_device(rz_ctx* ctx, SceneTree& T, const rz_scene* scene, const rz_scene_node* nodes,
-                           uint32_t n_nodes) {
-    Trace tr("stroke_on_device");
-    std::vector<rz::StrokeStyleDev> styles;
-    struct List {
-        uint32_t u0, u1;  // units [u0, u1)
-        uint32_t entry;   // outline entry (local index)
-    };
-    std::vector<uint32_t> stroke_nodes;
-    for (uint32_t i = 0; i < n_nodes; ++i) {
-        const rz_scene_node& nd = nodes[i];
-        if (nd.kind != RZ_NODE_STROKE) continue;
-        stroke_nodes.push_back(i);
-        styles.push_back(rz::StrokeStyleDev{nd.width, nd.miter_limit, nd.line_join, nd.line_cap});
-    }
-    // every input subpath of every Stroke node: 4 m units from `base` (built on the device)
-    std::vector<rz::StrokeSub> subs;
-    std::vector<List> lists;
-    uint64_t n_units = 0;
-    for (uint32_t j = 0; j < stroke_nodes.size(); ++j) {
-        const rz_scene_node& nd = nodes[stroke_nodes[j]];
-        for (uint32_t sp = T.fsub[nd.arg]; sp < T.fsub[nd.arg + 1]; ++sp) {
-            const uint32_t s0 = T.base.sub_off[sp], s1 = T.base.sub_off[sp + 1];
-            if (s1 <= s0) continue;
-            const uint32_t in_sp = ctx->expanded ? ctx->x_submap[sp] : sp;
-            const uint32_t closed = scene->subpath_closed && scene->subpath_closed[in_sp] ? 1u : 0u;
-            const uint32_t m = s1 - s0;
-            subs.push_back(rz::StrokeSub{n_units, s0, m, closed, j});
-            if (closed) {
-                lists.push_back({(uint32_t)n_units, (uint32_t)(n_units + 2 * m), j});
-                lists.push_back({(uint32_t)(n_units + 2 * m), (uint32_t)(n_units + 4 * m), j});
-            } else {
-                lists.push_back({(uint32_t)n_units, (uint32_t)(n_units + 4 * m), j});
-            }
-            n_units += 4ull * m;
-        }
-    }
-    if (n_units >= 0xffffffffull) return fail(ctx, RZ_ERR_INVALID, "scene tree: too many stroked segments");
-    const uint32_t nu = (uint32_t)n_units;
-    // device buffers of the context (kept between calls)
-    DevBuf &d_units = ctx->s_units, &d_styles = ctx->s_styles, &d_counts = ctx->s_counts, &d_off = ctx->s_off,
-           &d_fin = ctx->s_fin, &d_tmpk = ctx->s_tmpk, &d_tmpp = ctx->s_tmpp, &d_kind = ctx->s_kind,
-           &d_pts = ctx->s_pts;
-    RZ_CUDA(d_units.ensure((size_t)nu * sizeof(rz::StrokeUnit) + subs.size() * sizeof(rz::StrokeSub) + 32));
-    RZ_CUDA(d_styles.ensure(styles.size() * sizeof(rz::StrokeStyleDev) + 16));
-    RZ_CUDA(d_counts.ensure((size_t)nu * 4 + 16));
-    RZ_CUDA(d_off.ensure((size_t)nu * 8 + 16));
-    RZ_CUDA(d_fin.ensure((size_t)nu * 8 + 16));
-    rz::StrokeUnit* units_dev = (rz::StrokeUnit*)d_units.p;
-    rz::StrokeSub* subs_dev = (rz::StrokeSub*)((char*)d_units.p + (((size_t)nu * sizeof(rz::StrokeUnit) + 15) & ~(size_t)15));
-    RZ_CUDA(cudaMemcpyAsync(subs_dev, subs.data(), subs.size() * sizeof(rz::StrokeSub), cudaMemcpyHostToDevice,
-                            ctx->stream));
-    RZ_CUDA(rz::launch_stroke_units(subs_dev, (uint32_t)subs.size(), units_dev, nu, ctx->stream));
-    RZ_CUDA(cudaMemcpyAsync(d_styles.p, styles.data(), styles.size() * sizeof(rz::StrokeStyleDev),
-                            cudaMemcpyHostToDevice, ctx->stream));
-    rz::StrokeArgs A{};
-    A.units = (const rz::StrokeUnit*)d_units.p;
-    A.n_units = nu;
-    A.styles = (const rz::StrokeStyleDev*)d_styles.p;
-    A.kind = (const uint8_t*)ctx->d_kind.p;
-    A.pts = (const double*)ctx->d_pts.p;
-    A.counts = (uint32_t*)d_counts.p;
-    A.off_start = (const uint64_t*)d_off.p;
-    A.fin_start = (const uint64_t*)d_fin.p;
-    // offsets: one pass into kStrokeOffsetMax slots per OFFSET unit when that
-    // buffer stays under 4 GiB, else counted first and packed
-    std::vector<uint32_t> counts(nu);
-    std::vector<uint64_t> start(nu);
-    const uint64_t n_offset_units = n_units / 2;  // one OFFSET unit in two
-    A.strided = n_offset_units * rz::kStrokeOffsetMax * 65 <= (4ull << 30);
-    tr.mark("units");
-    uint64_t n_off = 0;
-    if (A.strided) {
-        for (const rz::StrokeSub& sb : subs)  // OFFSET units: even positions of each subpath's way out and back
-            for (uint64_t i = 0; i < 4ull * sb.m; ++i) {
-                start[sb.base + i] = n_off;
-                if (!(i & 1u)) n_off += rz::kStrokeOffsetMax;
-            }
-    } else {
-        RZ_CUDA(rz::launch_stroke(A, 0, ctx->stream));
-        RZ_CUDA(cudaMemcpyAsync(counts.data(), d_counts.p, (size_t)nu * 4, cudaMemcpyDeviceToHost, ctx->stream));
-        RZ_CUDA(cudaStreamSynchronize(ctx->stream));
-        for (const rz::StrokeSub& sb : subs)
-            for (uint64_t i = 0; i < 4ull * sb.m; ++i) {
-                start[sb.base + i] = n_off;
-                if (!(i & 1u)) n_off += counts[sb.base + i];
-            }
-    }
-    RZ_CUDA(cudaMemcpyAsync(d_off.p, start.data(), (size_t)nu * 8, cudaMemcpyHostToDevice, ctx->stream));
-    RZ_CUDA(d_tmpk.ensure(n_off + 16));
-    RZ_CUDA(d_tmpp.ensure(n_off * 64 + 16));
-    A.tmp_kind = (uint8_t*)d_tmpk.p;
-    A.tmp_pts = (double*)d_tmpp.p;
-    RZ_CUDA(rz::launch_stroke(A, 1, ctx->stream));
-    // joins, caps and closes: count, lay out the whole outline
-    RZ_CUDA(rz::launch_stroke(A, 2, ctx->stream));
-    RZ_CUDA(cudaMemcpyAsync(counts.data(), d_counts.p, (size_t)nu * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    RZ_CUDA(cudaStreamSynchronize(ctx->stream));
-    tr.mark("offset_emit_join_count");
-    uint64_t n_out = 0;
-    for (uint32_t u = 0; u < nu; ++u) {
-        start[u] = n_out;
-        n_out += counts[u];
-    }
-    const uint64_t n_seg = T.base.n_seg;
-    if (n_seg + n_out > 0xfffffff0ull) return fail(ctx, RZ_ERR_INVALID, "scene tree: stroke outlines too large");
-    RZ_CUDA(cudaMemcpyAsync(d_fin.p, start.data(), (size_t)nu * 8, cudaMemcpyHostToDevice, ctx->stream));
-    // the merged segment arrays: the staged segments, then the outlines
-    RZ_CUDA(d_kind.ensure(n_seg + n_out + 16));
-    RZ_CUDA(d_pts.ensure((n_seg + n_out) * 64 + 64));
-    if (n_seg) {
-        RZ_CUDA(cudaMemcpyAsync(d_kind.p, ctx->d_kind.p, n_seg, cudaMemcpyDeviceToDevice, ctx->stream));
-        RZ_CUDA(cudaMemcpyAsync(d_pts.p, ctx->d_pts.p, n_seg * 64, cudaMemcpyDeviceToDevice, ctx->stream));
-    }
-    A.out_kind = (uint8_t*)d_kind.p + n_seg;
-    A.out_pts = (double*)d_pts.p + 8 * n_seg;
-    RZ_CUDA(rz::launch_stroke(A, 3, ctx->stream));
-    RZ_CUDA(rz::launch_stroke(A, 4, ctx->stream));
-    tr.gpu_mark(ctx->stream, "join_emit_gather");
-    // host copy of the outlines (bounding boxes) and the subpath tables
-    T.okind.resize(n_out);
-    T.opts.resize(n_out * 8);
-    if (n_out) {
-        RZ_CUDA(cudaMemcpyAsync(T.okind.data(), A.out_kind, n_out, cudaMemcpyDeviceToHost, ctx->stream));
-        RZ_CUDA(cudaMemcpyAsync(T.opts.data(), A.out_pts, n_out * 64, cudaMemcpyDeviceToHost, ctx->stream));
-    }
-    // Path::push drops empty lists; every list is one closed outline subpath of its node's entry
-    T.osub.assign(1, 0);
-    T.ofsub.assign(stroke_nodes.size() + 1, 0);
-    size_t li = 0;
-    for (uint32_t j = 0; j < stroke_nodes.size(); ++j) {
-        T.ofsub[j] = (uint32_t)T.osub.size() - 1;
-        for (; li < lists.size() && lists[li].entry == j; ++li) {
-            const uint64_t end = lists[li].u1 == nu ? n_out : start[lists[li].u1];
-            if (end > start[lists[li].u0]) T.osub.push_back((uint32_t)end);
-        }
-    }
-    T.ofsub[stroke_nodes.size()] = (uint32_t)T.osub.size() - 1;
-    // merged subpath table: the staged one, then the outlines' (segment indices after the staged ones)
-    const uint32_t n_sub = T.base.n_sub;
-    T.merged_sub.assign(T.base.sub_off, T.base.sub_off + n_sub + 1);
-    for (size_t k = 1; k < T.osub.size(); ++k) T.merged_sub.push_back((uint32_t)(n_seg + T.osub[k]));
-    for (uint32_t j = 0; j < stroke_nodes.size(); ++j) {
-        const uint32_t i = stroke_nodes[j];
-        T.stroke_of[i] = (uint32_t)T.E.size();
-        T.E.push_back(TreeEntry{T.E[nodes[i].arg].own, RZ_FILL_NONZERO, T.E[nodes[i].arg].paint});
-    }
-    T.outline_sub0 = n_sub;  // outline entry j: merged subpaths n_sub + [ofsub[j], ofsub[j + 1])
-    RZ_CUDA(ctx->d_sub.ensure(T.merged_sub.size() * 4 + 16));
-    RZ_CUDA(cudaMemcpyAsync(ctx->d_sub.p, T.merged_sub.data(), T.merged_sub.size() * 4, cudaMemcpyHostToDevice,
-                            ctx->stream));
-    RZ_CUDA(cudaStreamSynchronize(ctx->stream));
-    std::swap(ctx->d_kind, d_kind);  // the staged-only arrays become next call's merged buffers
-    std::swap(ctx->d_pts, d_pts);
-    T.base.sub_off = T.merged_sub.data();
-    T.base.n_seg = (uint32_t)(n_seg + n_out);
-    T.base.n_sub = (uint32_t)T.merged_sub.size() - 1;
-    return RZ_OK;
-}
-
-// Scene-table checks shared by the flat and tree renders.
-rz_status check_scene(rz_ctx* ctx, const rz_scene* scene, double flatness, uint32_t width, uint32_t height) {
-    if (!scene || (scene->n_fills && (!scene->fill_subpath_off || !scene->fill_paint || !scene->paints)))
-        return fail(ctx, RZ_ERR_INVALID, "null argument");
-    if (!valid_flatness(flatness)) return fail(ctx, RZ_ERR_INVALID, "flatness must be > 0 and finite");
-    if (width > 16383 || height > 16383) return fail(ctx, RZ_ERR_INVALID, "canvas too large");
-    if ((scene->n_segments && (!scene->seg_kind || !scene->seg_pts)) || (scene->n_subpaths && !scene->subpath_off))
-        return fail(ctx, RZ_ERR_INVALID, "null segment arrays");
-    const uint32_t F = scene->n_fills;
-    for (uint32_t f = 0; f < F; ++f) {
-        if (scene->fill_subpath_off[f] > scene->fill_subpath_off[f + 1] || scene->fill_paint[f] >= scene->n_paints)
-            return fail(ctx, RZ_ERR_INVALID, "bad fill table");
-    }
-    if (F && scene->fill_subpath_off[F] > scene->n_subpaths) return fail(ctx, RZ_ERR_INVALID, "bad fill_subpath_off");
-    for (uint32_t i = 0; i < scene->n_subpaths; ++i)
-        if (scene->subpath_off[i] > scene->subpath_off[i + 1]) return fail(ctx, RZ_ERR_INVALID, "subpath_off decreasing");
-    if (scene->n_subpaths && scene->subpath_off[scene->n_subpaths] > scene->n_segments)
-        return fail(ctx, RZ_ERR_INVALID, "subpath_off exceeds n_segments");
-    for (uint32_t p = 0; p < scene->n_paints; ++p)
-        if (scene->paints[p].n_stops > (uint32_t)rz::kMaxStops) return fail(ctx, RZ_ERR_INVALID, "more than 16 stops");
-    return RZ_OK;
-}
+#include "rz_scene_tree.cpp.inc"
 
 }  // namespace
 
@@ -2697,161 +1962,7 @@ rz_status rz_encode_mask_rgba8(rz_ctx* ctx, const void* mask, int32_t elem_size,
 
 }  // extern "C"
 
-// ---------------------------------------------------------------------------
-// Differentiable batch (rz_diff.cu)
-// ---------------------------------------------------------------------------
-namespace {
-
-rz_status diff_check(rz_ctx* ctx, const rz_diff_batch* b, double flatness) {
-    if (!b || !b->ctrl) return fail(ctx, RZ_ERR_INVALID, "null argument");
-    if (!valid_flatness(flatness)) return fail(ctx, RZ_ERR_INVALID, "flatness must be > 0 and finite");
-    if (b->width == 0 || b->height == 0 || b->width > 16383 || b->height > 16383)
-        return fail(ctx, RZ_ERR_INVALID, "image size must be 1..16383");
-    if (b->segs_per_path == 0 || b->segs_per_path > (1u << 20)) return fail(ctx, RZ_ERR_INVALID, "bad segs_per_path");
-    if (b->fill_rule != RZ_FILL_NONZERO && b->fill_rule != RZ_FILL_EVENODD) return fail(ctx, RZ_ERR_INVALID, "bad fill rule");
-    if (!(b->paint_alpha > 0.f && b->paint_alpha < 1.f)) return fail(ctx, RZ_ERR_INVALID, "paint_alpha must be in (0, 1)");
-    const uint64_t paths = (uint64_t)b->n_images * b->paths_per_image;
-    if (paths * b->segs_per_path >= (1ull << 31)) return fail(ctx, RZ_ERR_INVALID, "batch too large");
-    if ((uint64_t)b->n_images * b->height >= (1ull << 30)) return fail(ctx, RZ_ERR_INVALID, "batch too large");
-    return RZ_OK;
-}
-
-// Band height: the largest of 8, 4, 2, 1 rows that divides the image height
-// and keeps the kernel's shared memory within 72 KiB (3 CTAs per SM).  Each
-// call bins its own lines, so the forward and the adjoint choose separately.
-int diff_band_rows(int width, int height, bool backward) {
-    for (int r = 8; r > 1; r >>= 1) {
-        int cs = 0;
-        if (height % r == 0 && rz::diff_smem_bytes(width, r, backward, &cs) <= 72 * 1024) return r;
-    }
-    return 1;
-}
-
-// Segments on the device, one fill per path (images stacked in one canvas),
-// lines flattened and binned with their tree nodes.
-rz_status diff_prepare(rz_ctx* ctx, const rz_diff_batch* b, double flatness, rz::DiffDev& D, int& cov_stride,
-                       int& smem, bool backward, Trace& tr) {
-    const uint32_t P = b->paths_per_image, segs = b->segs_per_path;
-    const uint32_t n_paths = b->n_images * P;
-    const uint32_t n_seg = n_paths * segs;
-    RZ_CUDA(ctx->d_kind.ensure((size_t)n_seg + 1));
-    RZ_CUDA(ctx->d_pts.ensure((size_t)n_seg * 64 + 8));
-    RZ_CUDA(ctx->d_sub.ensure(((size_t)n_paths + 1) * 4));
-    std::vector<uint32_t> sub(n_paths + 1);
-    for (uint32_t p = 0; p <= n_paths; ++p) sub[p] = p * segs;
-    RZ_CUDA(cudaMemcpyAsync(ctx->d_sub.p, sub.data(), sub.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
-    RZ_CUDA(rz::launch_diff_segments(b->ctrl, n_paths, (int)segs, (uint8_t*)ctx->d_kind.p, (double*)ctx->d_pts.p,
-                                     ctx->stream));
-    HostScene hs;
-    hs.sub_off = sub.data();
-    hs.n_seg = n_seg;
-    hs.n_sub = n_paths;
-    const int W = (int)b->width, H = (int)b->height;
-    hs.band_rows = diff_band_rows(W, H, backward);
-    hs.task_depth = 2;  // cubics spanning the canvas: hundreds of leaves each
-    const rzhost::Xf id{{1, 0, 0, 0, 1, 0}};
-    for (uint32_t p = 0; p < n_paths; ++p)
-        add_fill(hs, p, p + 1, 0, (int)(p / P) * H, W, H, W, id, b->fill_rule, 0);  // fill semantics: clip at W
-    rz::SceneDev& S = D.S;
-    S = rz::SceneDev{};
-    S.kind = (const uint8_t*)ctx->d_kind.p;
-    S.pts = (const double*)ctx->d_pts.p;
-    S.sub_off = (const uint32_t*)ctx->d_sub.p;
-    S.n_fills = (uint32_t)hs.fills.size();
-    S.n_slots = hs.n_slots;
-    S.n_segments = hs.n_seg;
-    S.n_subpaths = hs.n_sub;
-    S.task_depth = hs.task_depth;
-    S.thr64 = 16.0 * flatness * flatness;
-    S.thr32 = (float)S.thr64;
-    S.canvas_w = W;
-    S.canvas_h = (int32_t)(b->n_images * b->height);
-    S.band_rows = hs.band_rows;
-    S.n_bands = S.canvas_h / hs.band_rows;
-    RZ_CUDA(ctx->d_ctrl.ensure(64));
-    RZ_CUDA(cudaMemsetAsync(ctx->d_ctrl.p, 0, 64, ctx->stream));
-    S.err = (int32_t*)ctx->d_ctrl.p;
-    S.counters = (int32_t*)ctx->d_ctrl.p + 4;
-    tr.gpu_mark(ctx->stream, "segments");
-    rz_status st = build_lines(ctx, hs, S, tr, &ctx->p_leaf);
-    if (st) return st;
-    D.paths = (int32_t)P;
-    D.segs = (int32_t)segs;
-    D.width = W;
-    D.height = H;
-    D.rule = b->fill_rule;
-    D.alpha = b->paint_alpha;
-    D.ctrl = b->ctrl;
-    smem = rz::diff_smem_bytes(W, hs.band_rows, backward, &cov_stride);
-    return RZ_OK;
-}
-
-}  // namespace
-
-extern "C" {
-
-rz_status rz_diff_forward(rz_ctx* ctx, const rz_diff_batch* batch, double flatness, float* image) {
-    if (!ctx) return RZ_ERR_INVALID;
-    std::lock_guard<std::mutex> lock(ctx->mu);
-    rz_status st = diff_check(ctx, batch, flatness);
-    if (st) return st;
-    if (!image) return fail(ctx, RZ_ERR_INVALID, "null image");
-    if (batch->n_images == 0) return RZ_OK;
-    RZ_CUDA(cudaSetDevice(ctx->device));
-    Trace tr("rz_diff_forward");
-    rz::DiffDev D{};
-    int cov_stride = 0, smem = 0;
-    if (batch->paths_per_image == 0) {
-        RZ_CUDA(cudaMemsetAsync(image, 0, (size_t)batch->n_images * batch->width * batch->height * 4, ctx->stream));
-        return read_error(ctx);
-    }
-    st = diff_prepare(ctx, batch, flatness, D, cov_stride, smem, false, tr);
-    if (st) return st;
-    D.out = image;
-    RZ_CUDA(rz::launch_diff(D, false, cov_stride, smem, ctx->stream));
-    tr.gpu_mark(ctx->stream, "composite");
-    return read_error(ctx);
-}
-
-rz_status rz_l2_loss(rz_ctx* ctx, const float* image, const float* target, uint64_t n, double* loss,
-                     float* dl_dimage) {
-    if (!ctx) return RZ_ERR_INVALID;
-    std::lock_guard<std::mutex> lock(ctx->mu);
-    if (!image || !target || !loss) return fail(ctx, RZ_ERR_INVALID, "null argument");
-    RZ_CUDA(cudaSetDevice(ctx->device));
-    RZ_CUDA(ctx->d_loss.ensure(16));
-    RZ_CUDA(cudaMemsetAsync(ctx->d_loss.p, 0, 8, ctx->stream));
-    RZ_CUDA(rz::launch_l2_loss(image, target, n, (double*)ctx->d_loss.p, dl_dimage, ctx->num_sms, ctx->stream));
-    RZ_CUDA(cudaMemcpyAsync(loss, ctx->d_loss.p, 8, cudaMemcpyDeviceToHost, ctx->stream));
-    RZ_CUDA(cudaStreamSynchronize(ctx->stream));
-    return RZ_OK;
-}
-
-rz_status rasterize_backward(rz_ctx* ctx, const rz_diff_batch* batch, double flatness, const float* image,
-                             const float* dl_dimage, float* dl_dctrl) {
-    if (!ctx) return RZ_ERR_INVALID;
-    std::lock_guard<std::mutex> lock(ctx->mu);
-    rz_status st = diff_check(ctx, batch, flatness);
-    if (st) return st;
-    if (!image || !dl_dimage || !dl_dctrl) return fail(ctx, RZ_ERR_INVALID, "null argument");
-    const uint64_t n_ctrl = (uint64_t)batch->n_images * batch->paths_per_image * batch->segs_per_path * 3 * 2;
-    RZ_CUDA(cudaSetDevice(ctx->device));
-    RZ_CUDA(cudaMemsetAsync(dl_dctrl, 0, n_ctrl * 4, ctx->stream));
-    if (n_ctrl == 0) return read_error(ctx);
-    Trace tr("rasterize_backward");
-    rz::DiffDev D{};
-    int cov_stride = 0, smem = 0;
-    st = diff_prepare(ctx, batch, flatness, D, cov_stride, smem, true, tr);
-    if (st) return st;
-    D.image = image;
-    D.dl_dimage = dl_dimage;
-    D.out = dl_dctrl;
-    RZ_CUDA(rz::launch_diff(D, true, cov_stride, smem, ctx->stream));
-    tr.gpu_mark(ctx->stream, "adjoint");
-    return read_error(ctx);
-}
-
-}  // extern "C"
+#include "rz_diff_api.cpp.inc"
 
 // ---------------------------------------------------------------------------
 // Batch autotuner
