@@ -633,10 +633,10 @@ def main():
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": "k_mask_bands", "algorithmic_bytes_per_launch": int(algo_bytes),
-                     "kernel_ms": round(kernel_ms, 4)},
+                     "kernel": "k_mask_bands (with its k_band_records pass: one plan launch)",
+                     "algorithmic_bytes_per_launch": int(algo_bytes), "kernel_ms": round(kernel_ms, 4)},
         "cpu_baseline": cpu,
-        "gpu_launches": args.steps,
+        "gpu_launches": 2 * args.steps,  # k_band_records + k_mask_bands per plan launch
         "clocks": clk,
         "configs": configs,
         "tuning": {k: tuning[k] for k in ("band_rows_cap", "ctas_per_sm", "ms", "cached")},

@@ -36,6 +36,8 @@ cudaError_t launch_mask_bands(const BatchDev& b, const WorkItem* items, int n_it
                               cudaStream_t stream);
 int mask_bands_occupancy();
 int band_floats();
+uint64_t band_record_bytes();
+cudaError_t launch_band_records(const BatchDev& b, cudaStream_t stream);
 cudaError_t launch_flatten_counts(const BatchDev& b, uint32_t n_segments, uint32_t n_subpaths, uint32_t* counts,
                                   cudaStream_t stream);
 cudaError_t launch_flatten_count(const SceneDev& S, cudaStream_t st);
@@ -126,6 +128,7 @@ struct rz_ctx {
     DevBuf p_leaf, d_loss;
     // output encode (sRGB8 RGBA) and its input staging
     DevBuf p_rgba8, p_encode_in;
+    DevBuf p_recs;  // slot records of the band kernel
     // scene-tree layers by nesting depth: colour layers and clip masks
     std::vector<DevBuf> layer_pool, mask_pool;
     // the device stroker's unit table, counts and offsets, its compact offset
@@ -422,7 +425,7 @@ void rz_destroy(rz_ctx* c) {
                       &c->d_masks,  &c->d_items,   &c->d_out,     &c->d_ctrl,    &c->d_counts,  &c->p_fills,
                       &c->p_paints, &c->p_slots,   &c->p_lines,   &c->p_ecount,  &c->p_estart,  &c->p_ecursor,
                       &c->p_pairs,  &c->p_scan,    &c->p_canvas,  &c->p_leaf,    &c->d_loss,    &c->p_rgba8,
-                      &c->p_encode_in};
+                      &c->p_encode_in, &c->p_recs};
     for (DevBuf* b : bufs) b->release();
     for (DevBuf* b : {&c->s_units, &c->s_styles, &c->s_counts, &c->s_off, &c->s_fin, &c->s_tmpk, &c->s_tmpp,
                       &c->s_kind, &c->s_pts})
@@ -674,9 +677,28 @@ rz_status run_lines(rz_ctx* ctx, const rz::BatchDev& b, const std::vector<rz::Fi
     return RZ_OK;
 }
 
-rz_status run_bands(rz_ctx* ctx, const rz::BatchDev& b, const Items& items, bool per_path) {
+// Slot records of a batch (k_band_records) in `buf`, when the batch has any
+// and the buffer can hold them; otherwise the band kernel builds them per band.
+rz::BatchDev with_records(const rz::BatchDev& b, uint32_t n_paths, DevBuf& buf) {
+    rz::BatchDev r = b;
+    r.n_paths = n_paths;
+    r.recs = nullptr;
+    const uint64_t n = (uint64_t)b.n_segments + b.n_subpaths;
+    if (n == 0 || n_paths >= (1u << 30)) return r;
+    if (buf.ensure(n * rz::band_record_bytes()) != cudaSuccess) {
+        (void)cudaGetLastError();  // out of memory: per-band records
+        return r;
+    }
+    r.recs = (const rz::SlotRec*)buf.p;
+    return r;
+}
+
+rz_status run_bands(rz_ctx* ctx, const rz::BatchDev& b_in, const Items& items, bool per_path) {
     int32_t* queue = (int32_t*)ctx->d_ctrl.p + 8;
     const rz::WorkItem* d_items = (const rz::WorkItem*)ctx->d_items.p;
+    if (items.items.empty()) return RZ_OK;
+    const rz::BatchDev b = with_records(b_in, (uint32_t)(items.path_first.size() - 1), ctx->p_recs);
+    RZ_CUDA(rz::launch_band_records(b, ctx->stream));
     if (!per_path) {
         const int n = (int)items.items.size();
         if (n == 0) return RZ_OK;
@@ -982,7 +1004,7 @@ struct rz_batch_plan {
     rz_ctx* ctx = nullptr;
     rz::BatchDev b{};
     Items items;
-    DevBuf d_masks, d_items, d_ctrl;
+    DevBuf d_masks, d_items, d_ctrl, d_recs;
     // lines kernel: fills, line offsets, scan scratch, lines
     bool lines = false;
     DevBuf d_fills, d_slots, d_scan, d_lines;
@@ -1090,6 +1112,7 @@ rz_batch_plan* rz_batch_plan_create(rz_ctx* ctx, const rz_path_batch* batch, dou
     set_thresholds(b, flatness);
     const int n = (int)plan->items.items.size();
     plan->grid = batch_grid(ctx, n, plan->lines);
+    if (!plan->lines && n > 0) b = with_records(b, P, plan->d_recs);
     int32_t* queue = ctrl + 8;
     rz::SceneDev S{};
     if (plan->lines) {
@@ -1133,9 +1156,11 @@ rz_batch_plan* rz_batch_plan_create(rz_ctx* ctx, const rz_path_batch* batch, dou
             if (plan->lines)
                 rz::launch_mask_lines(S, (const rz::MaskDev*)plan->d_masks.p, (const rz::WorkItem*)plan->d_items.p, n,
                                       queue, out, plan->grid, plan->capture_stream);
-            else
+            else {
+                rz::launch_band_records(b, plan->capture_stream);
                 rz::launch_mask_bands(b, (const rz::WorkItem*)plan->d_items.p, n, queue, plan->grid,
                                       plan->capture_stream);
+            }
         }
         e = cudaStreamEndCapture(plan->capture_stream, &plan->graph);
     }
@@ -1187,6 +1212,7 @@ void rz_batch_plan_destroy(rz_batch_plan* plan) {
     plan->d_masks.release();
     plan->d_items.release();
     plan->d_ctrl.release();
+    plan->d_recs.release();
     plan->d_fills.release();
     plan->d_slots.release();
     plan->d_scan.release();

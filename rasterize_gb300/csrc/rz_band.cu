@@ -146,6 +146,55 @@ __device__ inline void drain_leaf(const Band& B, const SegRec* recs, const LeafC
     accumulate_vtx(B, rec_vtx(r, c.k, c.d, B.y0), rec_vtx(r, c.k + 1u, c.d, B.y0));
 }
 
+// Kinds of an input slot after the transform (slot_points).
+enum : int { SLOT_EMPTY = 0, SLOT_FIX = 1, SLOT_ARC = 2, SLOT_BIG = 3, SLOT_NAN = 4 };
+
+// Input slot `idx`: segment idx (closing == false) or the closing line of
+// subpath idx, Line(subpath.end(), subpath.start()) (src/path.rs:776-786),
+// transformed by trm.  SLOT_FIX: F is the 16.16 copy of the binary64 points
+// sx, sy; SLOT_BIG: a point lies beyond the 16.16 range; SLOT_ARC: a raw arc
+// (device-memory input); SLOT_EMPTY: a subpath without segments.
+__device__ __forceinline__ int slot_points(const BatchDev& b, uint32_t idx, bool closing, const double* trm,
+                                           FixSeg& F, double (&sx)[4], double (&sy)[4], uint32_t& src) {
+    F.kind = SEG_LINE;
+    src = 0xffffffffu;  // input segment (binary64 re-decisions); none for closing lines
+    int npts = 0;
+    if (!closing) {
+        const int kind = b.kind[idx];
+        if (kind == SEG_ARC) return SLOT_ARC;
+        F.kind = kind;
+        npts = seg_npts(kind);
+        const double2* p2 = reinterpret_cast<const double2*>(b.pts + 8ull * idx);
+        #pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const double2 q = __ldg(p2 + j);
+            sx[j] = q.x;
+            sy[j] = q.y;
+        }
+        src = idx;
+    } else {
+        const uint32_t s1 = min(b.sub_off[idx + 1], b.n_segments);
+        const uint32_t s0 = b.sub_off[idx];
+        if (s1 > s0 && subpath_point(b, s0, s1, false, sx[0], sy[0]) && subpath_point(b, s0, s1, true, sx[1], sy[1]))
+            npts = 2;
+    }
+    if (!npts) return SLOT_EMPTY;
+    bool nan = false, fits = true;
+    #pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (j < npts) {
+            if (trm) tr_apply64(trm, sx[j], sy[j], sx[j], sy[j]);
+            nan |= is_nan_bits(sx[j]) || is_nan_bits(sy[j]);
+            fits &= d2fix(sx[j], F.x[j]) & d2fix(sy[j], F.y[j]);
+        } else {
+            F.x[j] = F.y[j] = 0;
+            sx[j] = sy[j] = 0.0;
+        }
+    }
+    if (nan) return SLOT_NAN;
+    return fits ? SLOT_FIX : SLOT_BIG;
+}
+
 // Loads input segment slot i of a work item (segments, then one closing line
 // per subpath), transforms it and, when it lies in the fixed-point range and
 // its hull meets the band's rows, writes its record and decision
@@ -155,70 +204,134 @@ __device__ inline void drain_leaf(const Band& B, const SegRec* recs, const LeafC
 static __device__ __noinline__ bool band_load(const BatchDev& b, const Band& B, uint32_t seg0, uint32_t n_seg,
                                               uint32_t sub0, uint32_t i, const double* trm, SegRec& rec,
                                               SlotCoef& coef, int& fallbacks) {
-    bool active = false;
+    const bool closing = i >= n_seg;
+    const uint32_t idx = closing ? sub0 + (i - n_seg) : seg0 + i;
     FixSeg F;
-    F.kind = SEG_LINE;
-    uint32_t src = 0xffffffffu;  // input segment (binary64 re-decisions); none for closing lines
     double sx[4], sy[4];
-    int npts = 0;
-    if (i < n_seg) {
-        const uint32_t g = seg0 + i;
-        const int kind = b.kind[g];
-        const double2* p2 = reinterpret_cast<const double2*>(b.pts + 8ull * g);
-        if (kind == SEG_ARC) {
-            band_arc(b, B, g, trm, fallbacks);  // device-memory input with raw arcs
-        } else {
-            F.kind = kind;
-            npts = seg_npts(kind);
-            #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const double2 q = __ldg(p2 + j);
-                sx[j] = q.x;
-                sy[j] = q.y;
-            }
-            src = g;
-        }
-    } else {
-        // closing line Line(subpath.end(), subpath.start()).transform(tr) (src/path.rs:776-786)
-        const uint32_t sp = sub0 + (i - n_seg);
-        const uint32_t s1 = min(b.sub_off[sp + 1], b.n_segments);
-        const uint32_t s0 = b.sub_off[sp];
-        if (s1 > s0 && subpath_point(b, s0, s1, false, sx[0], sy[0]) &&
-            subpath_point(b, s0, s1, true, sx[1], sy[1])) {
-            F.kind = SEG_LINE;
-            npts = 2;
-        }
-    }
-    if (npts) {
-        bool nan = false, fits = true;
+    uint32_t src;
+    const int kind = slot_points(b, idx, closing, trm, F, sx, sy, src);
+    if (kind == SLOT_ARC) {
+        band_arc(b, B, idx, trm, fallbacks);  // device-memory input with raw arcs
+    } else if (kind == SLOT_NAN) {
+        set_err(b.err, ERR_NAN);  // the reference panics on NaN (src/path.rs:765-767)
+    } else if (kind == SLOT_BIG) {
+        Seg64 S;  // beyond the fixed-point range: binary64 walk
+        S.kind = F.kind;
         #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            if (j < npts) {
-                if (trm) tr_apply64(trm, sx[j], sy[j], sx[j], sy[j]);
-                nan |= is_nan_bits(sx[j]) || is_nan_bits(sy[j]);
-                fits &= d2fix(sx[j], F.x[j]) & d2fix(sy[j], F.y[j]);
-            } else {
-                F.x[j] = F.y[j] = 0;
-                sx[j] = sy[j] = 0.0;
+        for (int j = 0; j < 4; ++j) { S.x[j] = sx[j]; S.y[j] = sy[j]; }
+        band_segment(b, B, S, fallbacks);
+    } else if (kind == SLOT_FIX && hull_meets_rows(F, B.y0, B.bh)) {
+        make_record(F, sx, sy, rec);
+        rec.src = src;
+        coef.c = rec_flat(rec, coef.qerr);
+        return true;
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------------------
+// Slot records
+//
+// A path's segments are the same for every band of its mask, so their
+// records are built once per launch by k_band_records (one thread per slot,
+// no barriers) instead of once per band.  Record j < n_segments is segment
+// j, record n_segments + s the closing line of subpath s.  A band copies the
+// 96-byte records of its path into shared memory and keeps those whose hull
+// meets its rows.  Slots the fixed-point route cannot take (arcs, segments
+// beyond 16.16, NaN) are marked slow and go through band_load as before;
+// so are records built with another path's transform (offsets that put a
+// segment into two paths).
+// ---------------------------------------------------------------------------
+struct __align__(16) SlotRec {
+    SegRec rec;          // bytes 0-59
+    uint32_t tag;        // state << 30 | owning path (kAnyPath: no transforms)
+    SlotCoef coef;       // bytes 64-87
+    int32_t ymin, ymax;  // control hull rows, 16.16
+};
+static_assert(sizeof(SegRec) == 60 && sizeof(SlotCoef) == 24 && sizeof(SlotRec) == 96, "record layout");
+
+constexpr uint32_t kAnyPath = 0x3fffffffu;
+enum : uint32_t { REC_FIX = 0, REC_EMPTY = 1, REC_SLOW = 2 };
+
+// Largest k < n with a[k] <= v (0 when there is none): the range of a
+// non-decreasing offset array that holds v.
+__device__ __forceinline__ uint32_t last_le(const uint32_t* a, uint32_t n, uint32_t v) {
+    uint32_t lo = 0, hi = n;  // answer in [lo, hi)
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (a[mid] <= v) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256) k_band_records(BatchDev b, SlotRec* __restrict__ out) {
+    const uint32_t j = blockIdx.x * 256u + threadIdx.x;
+    if ((uint64_t)j >= (uint64_t)b.n_segments + b.n_subpaths) return;
+    const bool closing = j >= b.n_segments;
+    const uint32_t idx = closing ? j - b.n_segments : j;
+    uint32_t owner = kAnyPath;
+    const double* trm = nullptr;
+    if (b.tr && b.n_paths) {
+        const uint32_t sub = closing ? idx : last_le(b.sub_off, b.n_subpaths + 1, idx);
+        owner = min(last_le(b.path_sub, b.n_paths + 1, sub), b.n_paths - 1);
+        trm = b.tr + 6ull * owner;
+    }
+    SlotRec r;
+    FixSeg F;
+    double sx[4], sy[4];
+    uint32_t src;
+    const int kind = slot_points(b, idx, closing, trm, F, sx, sy, src);
+    uint32_t state = REC_SLOW;
+    int32_t ymin = 0, ymax = 0;
+    if (kind == SLOT_EMPTY) {
+        state = REC_EMPTY;
+    } else if (kind == SLOT_FIX) {
+        state = REC_FIX;
+        make_record(F, sx, sy, r.rec);
+        r.rec.src = src;
+        r.coef.c = rec_flat(r.rec, r.coef.qerr);
+        ymin = ymax = F.y[0];
+        #pragma unroll
+        for (int i = 1; i < 4; ++i) {
+            if (i < seg_npts(F.kind)) {
+                ymin = min(ymin, F.y[i]);
+                ymax = max(ymax, F.y[i]);
             }
         }
-        if (nan) {  // the reference panics on NaN (src/path.rs:765-767)
-            set_err(b.err, ERR_NAN);
-        } else if (!fits) {
-            // beyond the fixed-point range: binary64 walk
-            Seg64 S;
-            S.kind = F.kind;
-            #pragma unroll
-            for (int j = 0; j < 4; ++j) { S.x[j] = sx[j]; S.y[j] = sy[j]; }
-            band_segment(b, B, S, fallbacks);
-        } else {
-            active = hull_meets_rows(F, B.y0, B.bh);
-            if (active) make_record(F, sx, sy, rec);
-            rec.src = src;
-            if (active) coef.c = rec_flat(rec, coef.qerr);
-        }
     }
-    return active;
+    if (state != REC_FIX) {
+        r.rec = SegRec{};
+        r.coef = SlotCoef{};
+    }
+    r.tag = state << 30 | owner;
+    r.ymin = ymin;
+    r.ymax = ymax;
+    out[j] = r;
+}
+
+// Slot i of a work item from its record: 1 when the record is taken (its hull
+// meets the band), 0 when the slot adds nothing to the band, -1 when the slot
+// must go through band_load.
+__device__ __forceinline__ int band_take(const BatchDev& b, const Band& B, uint32_t path, uint32_t seg0,
+                                         uint32_t n_seg, uint32_t sub0, uint32_t i, SegRec& rec, SlotCoef& coef) {
+    const uint32_t ri = i < n_seg ? seg0 + i : b.n_segments + sub0 + (i - n_seg);
+    const int4* q = reinterpret_cast<const int4*>(b.recs + ri);
+    const int4 c0 = __ldg(q), c1 = __ldg(q + 1), c2 = __ldg(q + 2), c3 = __ldg(q + 3), c4 = __ldg(q + 4),
+               c5 = __ldg(q + 5);
+    const uint32_t tag = (uint32_t)c3.w, owner = tag & kAnyPath, state = tag >> 30;
+    if ((owner != kAnyPath && owner != path) || state == REC_SLOW) return -1;
+    if (state != REC_FIX) return 0;
+    const int32_t oy = B.y0 << 16;  // the test of hull_meets_rows
+    if (c5.w < oy - 65536 || c5.z > oy + ((B.bh + 1) << 16)) return 0;
+    int* r = reinterpret_cast<int*>(&rec);
+    r[0] = c0.x; r[1] = c0.y; r[2] = c0.z; r[3] = c0.w;
+    r[4] = c1.x; r[5] = c1.y; r[6] = c1.z; r[7] = c1.w;
+    r[8] = c2.x; r[9] = c2.y; r[10] = c2.z; r[11] = c2.w;
+    r[12] = c3.x; r[13] = c3.y; r[14] = c3.z;
+    int* c = reinterpret_cast<int*>(&coef);
+    c[0] = c4.x; c[1] = c4.y; c[2] = c4.z; c[3] = c4.w;
+    c[4] = c5.x; c[5] = c5.y;
+    return 1;
 }
 
 // queue != nullptr: persistent CTAs pull items from the queue head;
@@ -270,8 +383,12 @@ __global__ void __launch_bounds__(kThreads, 3) k_mask_bands(BatchDev b, const Wo
         const double* trm = b.tr ? b.tr + 6ull * wi.path : nullptr;
         for (uint32_t base = 0; base < n_seg + n_close; base += kThreads) {
             const uint32_t i = base + tid;
-            const bool active = i < n_seg + n_close &&
-                                band_load(b, B, seg0, n_seg, sub0, i, trm, recs[tid], coefs[tid], fallbacks);
+            bool active = false;
+            if (i < n_seg + n_close) {
+                const int t = b.recs ? band_take(b, B, wi.path, seg0, n_seg, sub0, i, recs[tid], coefs[tid]) : -1;
+                active = t > 0 || (t < 0 && band_load(b, B, seg0, n_seg, sub0, i, trm, recs[tid], coefs[tid],
+                                                      fallbacks));
+            }
             // ---- breadth-first over the top levels of every tree, all threads together
             if (tid == 0) { s_nlevel[0] = 0; s_nlevel[1] = 0; s_task = kThreads; }
             __syncthreads();
@@ -384,6 +501,14 @@ cudaError_t init_kernels() {
 }
 
 int band_floats() { return kBandFloats; }
+uint64_t band_record_bytes() { return sizeof(SlotRec); }
+
+cudaError_t launch_band_records(const BatchDev& b, cudaStream_t stream) {
+    const uint64_t n = (uint64_t)b.n_segments + b.n_subpaths;
+    if (n == 0 || !b.recs) return cudaSuccess;
+    k_band_records<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(b, const_cast<SlotRec*>(b.recs));
+    return cudaGetLastError();
+}
 int band_smem_bytes() { return kSmemBytes; }
 
 cudaError_t launch_mask_bands(const BatchDev& b, const WorkItem* items, int n_items, int32_t* queue, int grid,

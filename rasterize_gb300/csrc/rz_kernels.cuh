@@ -13,6 +13,8 @@ struct MaskDev {
     int32_t clip_width;  // the reference's `width`: width-1 (mask) or width (mask_iter)
 };
 
+struct SlotRec;  // per-slot segment record of the band kernel (rz_band.cu)
+
 struct BatchDev {
     const uint8_t* kind;        // [n_segments]
     const double* pts;          // [n_segments * 8]
@@ -28,6 +30,8 @@ struct BatchDev {
     float thr32;
     uint32_t n_segments;        // array extents: offsets are clamped to them
     uint32_t n_subpaths;
+    uint32_t n_paths;           // extent of path_sub / tr (record pass)
+    const SlotRec* recs;        // [n_segments + n_subpaths] built by k_band_records, or null (built per band)
 };
 
 // A band of rows of one path's mask: the unit of work of the band kernel.
