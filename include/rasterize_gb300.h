@@ -146,7 +146,10 @@ RZ_API rz_status rz_mask_iter(rz_ctx* ctx, const rz_path* path, const double tr[
 
 /* Renders every path of `batch` into its own f32 mask in `out` (mask
  * semantics as rz_mask; out has out_len elements, host or device memory per
- * batch->memory).  One persistent-kernel launch for the whole batch. */
+ * batch->memory).  One persistent-kernel launch for the whole batch; a large
+ * host batch with page-locked `out` is rendered in chunks of paths whose
+ * uploads and downloads overlap the rendering.  Elements of a host `out` that
+ * no mask covers (row padding, gaps between masks) may be overwritten. */
 RZ_API rz_status rz_mask_batch(rz_ctx* ctx, const rz_path_batch* batch, double flatness, float* out,
                         uint64_t out_len);
 

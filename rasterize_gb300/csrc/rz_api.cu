@@ -38,6 +38,8 @@ int mask_bands_occupancy();
 int band_floats();
 uint64_t band_record_bytes();
 cudaError_t launch_band_records(const BatchDev& b, cudaStream_t stream);
+cudaError_t launch_band_records(const BatchDev& b, uint32_t seg_lo, uint32_t seg_hi, uint32_t sub_lo, uint32_t sub_hi,
+                                cudaStream_t stream);
 cudaError_t launch_flatten_counts(const BatchDev& b, uint32_t n_segments, uint32_t n_subpaths, uint32_t* counts,
                                   cudaStream_t stream);
 cudaError_t launch_flatten_count(const SceneDev& S, cudaStream_t st);
@@ -139,11 +141,15 @@ struct rz_ctx {
     int tune_ctas = 0;
     std::string device_name;
     HostBuf h_stage, h_out;
+    HostBuf h_plan;  // page-locked mask descriptors and work items of chunked batches
     // host-side arc expansion scratch
     std::vector<uint8_t> x_kind;
     std::vector<double> x_pts;
     std::vector<uint32_t> x_sub, x_psub, x_segmap, x_submap;
     bool expanded = false;  // the last stage_host expanded arcs
+    // chunked host batches: upload and download streams, and their events
+    cudaStream_t s_in = nullptr, s_out = nullptr;
+    std::vector<cudaEvent_t> pipe_ev;
 };
 
 namespace {
@@ -346,6 +352,31 @@ struct Items {
     std::vector<int> path_first;  // first item of each path (items grouped by path)
 };
 
+// Items [0, n) by decreasing band area on a log scale (16 buckets per
+// octave), by a stable counting sort: linear time, and path order within a
+// bucket.  Persistent CTAs then pick the longest items first (LPT order).
+void lpt_sort(rz::WorkItem* items, size_t n, const std::vector<rz::MaskDev>& masks) {
+    constexpr int kBuckets = 32 * 16;
+    if (n < 2) return;
+    thread_local std::vector<uint16_t> key;
+    thread_local std::vector<uint32_t> start;
+    thread_local std::vector<rz::WorkItem> sorted;
+    key.resize(n);
+    start.assign(kBuckets + 1, 0);
+    sorted.resize(n);
+    for (size_t i = 0; i < n; ++i) {
+        const rz::WorkItem& w = items[i];
+        const uint32_t area = std::max<uint32_t>(1u, (uint32_t)w.rows * (uint32_t)masks[w.path].width);
+        const int lz = 31 - __builtin_clz(area);
+        const int frac = (int)(((uint64_t)area << (31 - lz)) >> 27) & 15;  // next 4 bits below the leading one
+        key[i] = (uint16_t)(kBuckets - 1 - std::min(kBuckets - 1, lz * 16 + frac));
+        ++start[key[i] + 1];
+    }
+    for (int k = 0; k < kBuckets; ++k) start[k + 1] += start[k];
+    for (size_t i = 0; i < n; ++i) sorted[start[key[i]]++] = items[i];
+    std::copy(sorted.begin(), sorted.begin() + n, items);
+}
+
 // Work items sorted by decreasing band area so the persistent CTAs pick the
 // longest items first (LPT order); `grouped` keeps path order instead.
 void build_items(const std::vector<rz::MaskDev>& masks, bool grouped, Items& out, int rows_cap = 256,
@@ -366,26 +397,7 @@ void build_items(const std::vector<rz::MaskDev>& masks, bool grouped, Items& out
         }
     }
     out.path_first[masks.size()] = (int)out.items.size();
-    if (!grouped) {
-        // Decreasing band area on a log scale (16 buckets per octave), by a
-        // stable counting sort: linear time, and path order within a bucket.
-        constexpr int kBuckets = 32 * 16;
-        const size_t n = out.items.size();
-        std::vector<uint16_t> key(n);
-        std::vector<uint32_t> start(kBuckets + 1, 0);
-        for (size_t i = 0; i < n; ++i) {
-            const rz::WorkItem& w = out.items[i];
-            const uint32_t area = std::max<uint32_t>(1u, (uint32_t)w.rows * (uint32_t)masks[w.path].width);
-            const int lz = 31 - __builtin_clz(area);
-            const int frac = (int)(((uint64_t)area << (31 - lz)) >> 27) & 15;  // next 4 bits below the leading one
-            key[i] = (uint16_t)(kBuckets - 1 - std::min(kBuckets - 1, lz * 16 + frac));
-            ++start[key[i] + 1];
-        }
-        for (int k = 0; k < kBuckets; ++k) start[k + 1] += start[k];
-        std::vector<rz::WorkItem> sorted(n);
-        for (size_t i = 0; i < n; ++i) sorted[start[key[i]]++] = out.items[i];
-        out.items.swap(sorted);
-    }
+    if (!grouped) lpt_sort(out.items.data(), out.items.size(), masks);
 }
 
 }  // namespace
@@ -433,7 +445,11 @@ void rz_destroy(rz_ctx* c) {
     for (DevBuf& b : c->layer_pool) b.release();
     for (DevBuf& b : c->mask_pool) b.release();
     c->h_stage.release();
+    c->h_plan.release();
     c->h_out.release();
+    if (c->s_in) cudaStreamSynchronize(c->s_in), cudaStreamDestroy(c->s_in);
+    if (c->s_out) cudaStreamSynchronize(c->s_out), cudaStreamDestroy(c->s_out);
+    for (cudaEvent_t e : c->pipe_ev) cudaEventDestroy(e);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
 }
@@ -471,7 +487,8 @@ struct Staged {
 // pinned staging buffer, one async copy per array).
 rz_status stage_host(rz_ctx* ctx, const uint8_t* kind, const double* pts, uint32_t n_seg, const uint32_t* sub_off,
                      uint32_t n_sub, const uint32_t* path_sub, uint32_t n_paths, const double* tr,
-                     const uint8_t* rule, rz::BatchDev& b) {
+                     const uint8_t* rule, rz::BatchDev& b, const char** defer_kind = nullptr,
+                     const char** defer_pts = nullptr) {
     // arcs are converted to cubics on the host, as PathBuilder::arc_to does
     const bool has_arc = n_seg && std::memchr(kind, RZ_SEG_ARC, n_seg) != nullptr;
     ctx->expanded = has_arc;
@@ -529,8 +546,13 @@ rz_status stage_host(rz_ctx* ctx, const uint8_t* kind, const double* pts, uint32
     RZ_CUDA(ctx->d_pts.ensure(sz_pts + 8));
     RZ_CUDA(ctx->d_sub.ensure(sz_sub));
     RZ_CUDA(ctx->d_psub.ensure(sz_psub));
-    if (sz_kind) RZ_CUDA(cudaMemcpyAsync(ctx->d_kind.p, hk, sz_kind, cudaMemcpyHostToDevice, ctx->stream));
-    if (sz_pts) RZ_CUDA(cudaMemcpyAsync(ctx->d_pts.p, hp, sz_pts, cudaMemcpyHostToDevice, ctx->stream));
+    if (defer_kind && defer_pts) {  // the caller uploads the segments in chunks
+        *defer_kind = hk;
+        *defer_pts = hp;
+    } else {
+        if (sz_kind) RZ_CUDA(cudaMemcpyAsync(ctx->d_kind.p, hk, sz_kind, cudaMemcpyHostToDevice, ctx->stream));
+        if (sz_pts) RZ_CUDA(cudaMemcpyAsync(ctx->d_pts.p, hp, sz_pts, cudaMemcpyHostToDevice, ctx->stream));
+    }
     RZ_CUDA(cudaMemcpyAsync(ctx->d_sub.p, hs, sz_sub, cudaMemcpyHostToDevice, ctx->stream));
     RZ_CUDA(cudaMemcpyAsync(ctx->d_psub.p, hq, sz_psub, cudaMemcpyHostToDevice, ctx->stream));
     b.n_segments = n_seg;
@@ -560,12 +582,12 @@ rz_status stage_plan(rz_ctx* ctx, const std::vector<rz::MaskDev>& masks, const I
     const size_t sz_i = std::max<size_t>(items.items.size(), 1) * sizeof(rz::WorkItem);
     RZ_CUDA(ctx->d_masks.ensure(sz_m + 16));
     RZ_CUDA(ctx->d_items.ensure(sz_i));
-    RZ_CUDA(ctx->d_ctrl.ensure(64));
+    RZ_CUDA(ctx->d_ctrl.ensure(256));
     if (sz_m) RZ_CUDA(cudaMemcpyAsync(ctx->d_masks.p, masks.data(), sz_m, cudaMemcpyHostToDevice, ctx->stream));
     if (!items.items.empty())
         RZ_CUDA(cudaMemcpyAsync(ctx->d_items.p, items.items.data(), items.items.size() * sizeof(rz::WorkItem),
                                 cudaMemcpyHostToDevice, ctx->stream));
-    RZ_CUDA(cudaMemsetAsync(ctx->d_ctrl.p, 0, 64, ctx->stream));
+    RZ_CUDA(cudaMemsetAsync(ctx->d_ctrl.p, 0, 256, ctx->stream));  // error word, counters, queue heads
     // pageable sources above: the copies complete before the call returns
     int32_t* ctrl = (int32_t*)ctx->d_ctrl.p;
     b.masks = (const rz::MaskDev*)ctx->d_masks.p;
@@ -712,6 +734,164 @@ rz_status run_bands(rz_ctx* ctx, const rz::BatchDev& b_in, const Items& items, b
             RZ_CUDA(rz::launch_mask_bands(b, d_items + f, n, nullptr, n, ctx->stream));
         }
     }
+    return RZ_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Host batches with page-locked output, in chunks of paths.  Three streams
+// carry a chunk each: its segments up (s_in), its records and band kernel
+// (the context stream), its masks down (s_out), so the host link moves one
+// chunk's inputs and another's masks while the SMs render a third.  The masks
+// are rendered into device memory and leave in one copy per chunk: the span
+// from the chunk's first mask element to its last, padding included.
+// ---------------------------------------------------------------------------
+struct PipeChunk {
+    uint32_t p_lo, p_hi;          // paths
+    size_t item_lo, item_hi;      // work items (LPT order within the chunk)
+    uint64_t out_lo, out_hi;      // output elements copied back
+};
+
+constexpr uint64_t kPipeChunkBytes = 32ull << 20;  // output bytes per chunk
+constexpr int kPipeMaxChunks = 16;                 // queue heads in the control words
+
+// Chunks of about equal pixel counts; none when the batch is too small to gain
+// from overlap or its masks are laid out so that the chunks' spans overlap.
+std::vector<PipeChunk> pipe_chunks(const std::vector<rz::MaskDev>& masks, uint64_t out_len) {
+    std::vector<PipeChunk> chunks;
+    const uint64_t bytes = out_len * 4;
+    if (masks.size() < 2 || bytes < 2 * kPipeChunkBytes) return chunks;
+    const int K = (int)std::min<uint64_t>(kPipeMaxChunks, bytes / kPipeChunkBytes);
+    uint64_t total = 0;
+    for (const rz::MaskDev& m : masks)
+        if (m.width > 0 && m.height > 0) total += (uint64_t)m.width * m.height;
+    if (total == 0) return chunks;
+    uint64_t acc = 0, spans = 0;
+    uint32_t p_lo = 0;
+    for (uint32_t p = 0; p < masks.size(); ++p) {
+        const rz::MaskDev& m = masks[p];
+        if (m.width > 0 && m.height > 0) acc += (uint64_t)m.width * m.height;
+        const bool last = p + 1 == masks.size();
+        if (!last && acc * K < total * (chunks.size() + 1)) continue;
+        PipeChunk c{p_lo, p + 1, 0, 0, ~0ull, 0};
+        for (uint32_t q = p_lo; q <= p; ++q) {
+            const rz::MaskDev& n = masks[q];
+            if (n.width <= 0 || n.height <= 0) continue;
+            c.out_lo = std::min<uint64_t>(c.out_lo, n.offset);
+            c.out_hi = std::max<uint64_t>(c.out_hi, n.offset + (uint64_t)(n.height - 1) * n.row_stride + n.width);
+        }
+        if (c.out_hi > c.out_lo) {
+            spans += c.out_hi - c.out_lo;
+            chunks.push_back(c);
+        } else if (!chunks.empty()) {
+            chunks.back().p_hi = p + 1;  // no pixels: joins the chunk before
+        } else {
+            continue;  // leading paths without pixels join the first chunk
+        }
+        p_lo = p + 1;
+    }
+    if (chunks.size() < 2 || spans > out_len + out_len / 8) chunks.clear();  // interleaved layouts: one launch
+    if (!chunks.empty()) chunks.front().p_lo = 0;
+    return chunks;
+}
+
+rz_status pipe_streams(rz_ctx* ctx, size_t n_events) {
+    if (!ctx->s_in) RZ_CUDA(cudaStreamCreateWithFlags(&ctx->s_in, cudaStreamNonBlocking));
+    if (!ctx->s_out) RZ_CUDA(cudaStreamCreateWithFlags(&ctx->s_out, cudaStreamNonBlocking));
+    while (ctx->pipe_ev.size() < n_events) {
+        cudaEvent_t e;
+        RZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->pipe_ev.push_back(e);
+    }
+    return RZ_OK;
+}
+
+// Uploads the segments of each chunk (host sources hk / hp), renders it and
+// copies its masks into the page-locked `out`.  b: the small arrays staged,
+// the segment buffers allocated; hsub / hpsub: host copies of the offsets.
+// A chunk's work list is built, sorted and uploaded just before its launch,
+// so the first chunk renders while the host prepares the others.
+rz_status run_pipelined(rz_ctx* ctx, rz::BatchDev b, const std::vector<rz::MaskDev>& masks,
+                        std::vector<PipeChunk>& chunks, const uint32_t* hsub, const uint32_t* hpsub,
+                        const char* hk, const char* hp, float* out, uint64_t out_len, Trace& tr) {
+    const size_t K = chunks.size(), P = masks.size();
+    rz_status st = pipe_streams(ctx, 2 * K + 1);
+    if (st) return st;
+    cudaEvent_t* ev_in = ctx->pipe_ev.data();
+    cudaEvent_t* ev_done = ev_in + K;
+    cudaEvent_t ev_out = ev_in[2 * K];
+    // band heights and the first item of every path
+    std::vector<int> rows(P, 0);
+    std::vector<size_t> first(P + 1, 0);
+    for (size_t p = 0; p < P; ++p) {
+        const rz::MaskDev& m = masks[p];
+        size_t n = 0;
+        if (m.width > 0 && m.height > 0) {
+            rows[p] = band_rows(m.clip_width, m.height, ctx->tune_rows_cap);
+            n = (size_t)((m.height + rows[p] - 1) / rows[p]);
+        }
+        first[p + 1] = first[p] + n;
+    }
+    const size_t n_items = first[P];
+    const size_t sz_m = P * sizeof(rz::MaskDev), sz_i = std::max<size_t>(n_items, 1) * sizeof(rz::WorkItem);
+    RZ_CUDA(ctx->d_masks.ensure(sz_m + 16));
+    RZ_CUDA(ctx->d_items.ensure(sz_i));
+    RZ_CUDA(ctx->d_ctrl.ensure(256));
+    RZ_CUDA(ctx->d_out.ensure(out_len * 4 + 16));
+    RZ_CUDA(ctx->h_plan.ensure(sz_m + sz_i + 64));
+    b.out = (float*)ctx->d_out.p;
+    b.masks = (const rz::MaskDev*)ctx->d_masks.p;
+    int32_t* ctrl = (int32_t*)ctx->d_ctrl.p;
+    b.err = ctrl;
+    b.counters = ctrl + 4;
+    const rz::BatchDev br = with_records(b, (uint32_t)P, ctx->p_recs);
+    char* hplan = (char*)ctx->h_plan.p;
+    std::memcpy(hplan, masks.data(), sz_m);
+    rz::WorkItem* h_items = (rz::WorkItem*)(hplan + ((sz_m + 15) & ~(size_t)15));
+    RZ_CUDA(cudaMemsetAsync(ctrl, 0, 256, ctx->stream));  // error word, counters, queue heads
+    RZ_CUDA(cudaEventRecord(ev_out, ctx->stream));
+    RZ_CUDA(cudaStreamWaitEvent(ctx->s_in, ev_out, 0));  // the small arrays, then everything on s_in
+    RZ_CUDA(cudaMemcpyAsync(ctx->d_masks.p, hplan, sz_m, cudaMemcpyHostToDevice, ctx->s_in));
+    tr.mark("prepare");
+    rz::WorkItem* d_items = (rz::WorkItem*)ctx->d_items.p;
+    int32_t* queues = ctrl + 16;
+    for (size_t k = 0; k < K; ++k) {
+        PipeChunk& c = chunks[k];
+        c.item_lo = first[c.p_lo];
+        c.item_hi = first[c.p_hi];
+        rz::WorkItem* it = h_items + c.item_lo;
+        for (uint32_t p = c.p_lo; p < c.p_hi; ++p) {
+            const rz::MaskDev& m = masks[p];
+            for (int y = 0, i = 0; y < m.height && rows[p] > 0; y += rows[p], ++i) {
+                rz::WorkItem& w = h_items[first[p] + i];
+                w.path = p;
+                w.y0 = (uint16_t)y;
+                w.rows = (uint16_t)std::min(rows[p], m.height - y);
+            }
+        }
+        const size_t n = c.item_hi - c.item_lo;
+        lpt_sort(it, n, masks);
+        // one upload queue in chunk order: the chunk's work list, then its segments
+        if (n) RZ_CUDA(cudaMemcpyAsync(d_items + c.item_lo, it, n * sizeof(rz::WorkItem), cudaMemcpyHostToDevice,
+                                       ctx->s_in));
+        const uint32_t s0 = hsub[hpsub[c.p_lo]], s1 = hsub[hpsub[c.p_hi]];
+        if (s1 > s0) {
+            RZ_CUDA(cudaMemcpyAsync((uint8_t*)ctx->d_kind.p + s0, hk + s0, s1 - s0, cudaMemcpyHostToDevice, ctx->s_in));
+            RZ_CUDA(cudaMemcpyAsync((char*)ctx->d_pts.p + 64ull * s0, hp + 64ull * s0, 64ull * (s1 - s0),
+                                    cudaMemcpyHostToDevice, ctx->s_in));
+        }
+        RZ_CUDA(cudaEventRecord(ev_in[k], ctx->s_in));
+        RZ_CUDA(cudaStreamWaitEvent(ctx->stream, ev_in[k], 0));
+        RZ_CUDA(rz::launch_band_records(br, hsub[hpsub[c.p_lo]], hsub[hpsub[c.p_hi]], hpsub[c.p_lo], hpsub[c.p_hi],
+                                        ctx->stream));
+        if (n) RZ_CUDA(rz::launch_mask_bands(br, d_items + c.item_lo, (int)n, queues + k, batch_grid(ctx, (int)n),
+                                             ctx->stream));
+        RZ_CUDA(cudaEventRecord(ev_done[k], ctx->stream));
+        RZ_CUDA(cudaStreamWaitEvent(ctx->s_out, ev_done[k], 0));
+        RZ_CUDA(cudaMemcpyAsync(out + c.out_lo, b.out + c.out_lo, (c.out_hi - c.out_lo) * 4, cudaMemcpyDeviceToHost,
+                                ctx->s_out));
+    }
+    RZ_CUDA(cudaEventRecord(ev_out, ctx->s_out));
+    RZ_CUDA(cudaStreamWaitEvent(ctx->stream, ev_out, 0));  // the call's stream covers every copy
     return RZ_OK;
 }
 
@@ -898,10 +1078,26 @@ static rz_status mask_batch_impl(rz_ctx* ctx, const rz_path_batch* batch, double
         if (batch->subpath_off[batch->n_subpaths] > batch->n_segments)
             return fail(ctx, RZ_ERR_INVALID, "subpath_off exceeds n_segments");
         tr.mark("validate");
+        // page-locked output of a large batch: chunks of paths, uploads and downloads overlapped with rendering
+        std::vector<PipeChunk> chunks;
+        if (!per_path && !use_lines_kernel() && mapped_host(out)) chunks = pipe_chunks(masks, out_len);
+        const char *hk = nullptr, *hp = nullptr;
         st = stage_host(ctx, batch->seg_kind, batch->seg_pts, batch->n_segments, batch->subpath_off,
-                        batch->n_subpaths, batch->path_subpath_off, P, batch->transforms, batch->fill_rules, b);
+                        batch->n_subpaths, batch->path_subpath_off, P, batch->transforms, batch->fill_rules, b,
+                        chunks.empty() ? nullptr : &hk, chunks.empty() ? nullptr : &hp);
         if (st) return st;
         tr.mark("stage_inputs");
+        if (!chunks.empty()) {
+            set_thresholds(b, flatness);
+            const uint32_t* hsub = ctx->expanded ? ctx->x_sub.data() : batch->subpath_off;
+            const uint32_t* hpsub = ctx->expanded ? ctx->x_psub.data() : batch->path_subpath_off;
+            st = run_pipelined(ctx, b, masks, chunks, hsub, hpsub, hk, hp, out, out_len, tr);
+            if (st) return st;
+            tr.mark("enqueue");
+            st = read_error(ctx);
+            tr.mark("sync");
+            return st;
+        }
     } else {
         b.kind = batch->seg_kind;
         b.pts = batch->seg_pts;
@@ -928,6 +1124,7 @@ static rz_status mask_batch_impl(rz_ctx* ctx, const rz_path_batch* batch, double
     } else {
         b.out = direct_out ? (float*)direct_out : out;
     }
+    b.flat_out = direct_out ? 1 : 0;
     tr.mark("stage_plan");
     if (lines) {
         std::vector<rz::FillDev> fills;
@@ -1106,6 +1303,7 @@ rz_batch_plan* rz_batch_plan_create(rz_ctx* ctx, const rz_path_batch* batch, dou
     b.n_subpaths = batch->n_subpaths;
     b.masks = (const rz::MaskDev*)plan->d_masks.p;
     b.out = out;
+    b.flat_out = mapped_host(out) ? 1 : 0;  // page-locked host output: whole-line spans
     int32_t* ctrl = (int32_t*)plan->d_ctrl.p;
     b.err = ctrl;
     b.counters = ctrl + 4;

@@ -264,11 +264,15 @@ __device__ __forceinline__ uint32_t last_le(const uint32_t* a, uint32_t n, uint3
     return lo;
 }
 
-__global__ void __launch_bounds__(256) k_band_records(BatchDev b, SlotRec* __restrict__ out) {
-    const uint32_t j = blockIdx.x * 256u + threadIdx.x;
-    if ((uint64_t)j >= (uint64_t)b.n_segments + b.n_subpaths) return;
-    const bool closing = j >= b.n_segments;
-    const uint32_t idx = closing ? j - b.n_segments : j;
+// Records of segments [seg_lo, seg_lo + n_seg) and of the closing lines of
+// subpaths [sub_lo, sub_lo + n_sub).
+__global__ void __launch_bounds__(256) k_band_records(BatchDev b, SlotRec* __restrict__ out, uint32_t seg_lo,
+                                                      uint32_t n_seg, uint32_t sub_lo, uint32_t n_sub) {
+    const uint32_t t = blockIdx.x * 256u + threadIdx.x;
+    if ((uint64_t)t >= (uint64_t)n_seg + n_sub) return;
+    const bool closing = t >= n_seg;
+    const uint32_t idx = closing ? sub_lo + (t - n_seg) : seg_lo + t;
+    const uint32_t j = closing ? b.n_segments + idx : idx;
     uint32_t owner = kAnyPath;
     const double* trm = nullptr;
     if (b.tr && b.n_paths) {
@@ -487,8 +491,15 @@ __global__ void __launch_bounds__(kThreads, 3) k_mask_bands(BatchDev b, const Wo
         __syncthreads();
 
         const int rule = b.rule ? b.rule[wi.path] : 0;
-        MaskStore st{b.out, m.offset, (int64_t)m.row_stride, B.y0, m.width};
-        band_scan<kThreads>(B, m.width, rule, st);
+        if (b.flat_out && m.row_stride == m.width) {
+            // staged in shared memory, then one contiguous span per band
+            band_scan<kThreads>(B, m.width, rule, SmemStore{acc, B.stride});
+            __syncthreads();
+            band_flush<kThreads>(acc, B.stride, B.bh, m.width, b.out + m.offset + (uint64_t)B.y0 * (uint64_t)m.width);
+        } else {
+            MaskStore st{b.out, m.offset, (int64_t)m.row_stride, B.y0, m.width};
+            band_scan<kThreads>(B, m.width, rule, st);
+        }
         __syncthreads();
     }
     if (fallbacks) atomicAdd(&b.counters[1], fallbacks);
@@ -503,11 +514,21 @@ cudaError_t init_kernels() {
 int band_floats() { return kBandFloats; }
 uint64_t band_record_bytes() { return sizeof(SlotRec); }
 
-cudaError_t launch_band_records(const BatchDev& b, cudaStream_t stream) {
-    const uint64_t n = (uint64_t)b.n_segments + b.n_subpaths;
+// Records of segments [seg_lo, seg_hi) and closing lines of subpaths [sub_lo, sub_hi).
+cudaError_t launch_band_records(const BatchDev& b, uint32_t seg_lo, uint32_t seg_hi, uint32_t sub_lo, uint32_t sub_hi,
+                                cudaStream_t stream) {
+    seg_hi = min(seg_hi, b.n_segments);
+    sub_hi = min(sub_hi, b.n_subpaths);
+    const uint32_t n_seg = seg_hi > seg_lo ? seg_hi - seg_lo : 0, n_sub = sub_hi > sub_lo ? sub_hi - sub_lo : 0;
+    const uint64_t n = (uint64_t)n_seg + n_sub;
     if (n == 0 || !b.recs) return cudaSuccess;
-    k_band_records<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(b, const_cast<SlotRec*>(b.recs));
+    k_band_records<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(b, const_cast<SlotRec*>(b.recs), seg_lo, n_seg,
+                                                                     sub_lo, n_sub);
     return cudaGetLastError();
+}
+
+cudaError_t launch_band_records(const BatchDev& b, cudaStream_t stream) {
+    return launch_band_records(b, 0, b.n_segments, 0, b.n_subpaths, stream);
 }
 int band_smem_bytes() { return kSmemBytes; }
 

@@ -684,6 +684,52 @@ struct MaskStore {
     }
 };
 
+// Staging epilogue of the row scan: the alphas replace the row's accumulation
+// words in shared memory (each lane reads its 4 words before it writes them).
+struct SmemStore {
+    float* acc;
+    int stride;
+    __device__ __forceinline__ void operator()(int r, int x0, const float (&a)[kScanChunk]) const {
+        *reinterpret_cast<float4*>(acc + r * stride + x0) = make_float4(a[0], a[1], a[2], a[3]);
+    }
+};
+
+// Streams a staged band (rows x width alphas at `stride` in shared memory) to
+// a mask whose rows are packed (row stride == width): one contiguous span of
+// rows * width floats, written with aligned 16-byte stores, so every 128-byte
+// line inside the span is written whole by one warp instruction.  Over a
+// host link (page-locked output) partial lines cost a transaction each.
+template <int THREADS>
+__device__ void band_flush(const float* acc, int stride, int rows, int width, float* dst) {
+    const uint32_t n = (uint32_t)rows * (uint32_t)width;
+    const uint32_t head = min((uint32_t)(((16u - ((uint32_t)reinterpret_cast<uintptr_t>(dst) & 15u)) & 15u) >> 2), n);
+    const uint32_t n4 = (n - head) >> 2;
+    const uint32_t tid = threadIdx.x;
+    if (tid < head) {
+        const uint32_t r = tid / (uint32_t)width;
+        dst[tid] = acc[r * stride + (tid - r * width)];
+    }
+    float4* d4 = reinterpret_cast<float4*>(dst + head);
+    for (uint32_t j = tid; j < n4; j += THREADS) {
+        const uint32_t i = head + 4u * j;
+        uint32_t r = i / (uint32_t)width, c = i - r * (uint32_t)width;
+        float v[4];
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            v[k] = acc[r * stride + c];
+            if (++c == (uint32_t)width) {
+                c = 0;
+                ++r;
+            }
+        }
+        __stcs(d4 + j, make_float4(v[0], v[1], v[2], v[3]));
+    }
+    for (uint32_t i = head + 4u * n4 + tid; i < n; i += THREADS) {
+        const uint32_t r = i / (uint32_t)width;
+        dst[i] = acc[r * stride + (i - r * width)];
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Segment records shared by the band kernel and the line pipeline
 // ---------------------------------------------------------------------------

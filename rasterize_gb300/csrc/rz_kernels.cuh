@@ -31,6 +31,7 @@ struct BatchDev {
     uint32_t n_segments;        // array extents: offsets are clamped to them
     uint32_t n_subpaths;
     uint32_t n_paths;           // extent of path_sub / tr (record pass)
+    int32_t flat_out;           // packed masks are written as one span per band (page-locked host output)
     const SlotRec* recs;        // [n_segments + n_subpaths] built by k_band_records, or null (built per band)
 };
 

@@ -209,6 +209,43 @@ def test_batch_into_page_locked_host_memory(R):
         assert np.array_equal(batch.mask(pinned, i), batch.mask(staged, i))
 
 
+def _arc_glyph(w, h):
+    cx, cy, r = w / 2, h / 2, 0.4 * min(w, h)
+    b = PathBuilder()
+    b.move_to((cx - r, cy)).arc_to((r, 0.7 * r), 0.3, False, True, (cx + r, cy))
+    b.arc_to((r, 0.5 * r), 0.0, True, True, (cx - r, cy)).close()
+    return b.build()
+
+
+@pytest.mark.parametrize("with_arcs", [False, True])
+def test_large_batch_in_chunks_into_page_locked_memory(R, with_arcs):
+    """A host batch above 64 MB of masks with page-locked output is rendered in
+    chunks of paths (uploads, band kernels and downloads on three streams);
+    its masks equal the one-launch path's bit for bit, with transforms, both
+    fill rules and (expanded on the host) arcs."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(41)
+    paths, sizes, _ = W.glyph_batch(seed=43, n=1700)
+    trs, rules = [], []
+    for i, (w, h) in enumerate(sizes):
+        if with_arcs and i % 37 == 5:
+            paths[i] = _arc_glyph(w, h)
+        a = rng.uniform(-0.3, 0.3)
+        c = (w / 2, h / 2)
+        trs.append(Transform.new_translate(*c) * Transform.new_rotate(a) * Transform.new_translate(-c[0], -c[1]))
+        rules.append(FillRule(i % 2))
+    batch = MaskBatch(paths, sizes, transforms=trs, fill_rules=rules)
+    assert batch.out_len * 4 >= 64 << 20
+    one = R.mask_batch(batch)  # pageable output: one launch
+    pinned = torch.full((batch.out_len,), -7.0, dtype=torch.float32).pin_memory().numpy()
+    R.mask_batch(batch, out=pinned)
+    for i in range(len(paths)):
+        assert np.array_equal(batch.mask(pinned, i), batch.mask(one, i)), i
+    for i in range(0, len(paths), 97):
+        w, h = sizes[i]
+        assert_close(batch.mask(pinned, i), O.mask(paths[i], trs[i], rules[i], w, h))
+
+
 def test_batch_with_transforms_and_rules(R):
     rng = np.random.default_rng(5)
     paths, sizes, _ = W.glyph_batch(seed=11, n=40, side_range=(16, 300))
