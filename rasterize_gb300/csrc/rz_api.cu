@@ -133,15 +133,20 @@ struct rz_ctx {
     DevBuf p_recs;  // slot records of the band kernel
     // scene-tree layers by nesting depth: colour layers and clip masks
     std::vector<DevBuf> layer_pool, mask_pool;
+    // concurrent scene-tree layers: one arena for every layer and mask, a stream pool, events
+    DevBuf layer_arena;
+    std::vector<cudaStream_t> tree_streams;
+    std::vector<cudaEvent_t> tree_events;
     // the device stroker's unit table, counts and offsets, its compact offset
     // pieces, and the merged segment arrays it builds (swapped with d_kind / d_pts)
-    DevBuf s_units, s_styles, s_counts, s_off, s_fin, s_tmpk, s_tmpp, s_kind, s_pts;
+    DevBuf s_units, s_styles, s_counts, s_off, s_fin, s_tmpk, s_tmpp, s_kind, s_pts, s_order;
     // batch tuning (rz_tune_batch / rz_set_tuning): band height cap, resident CTAs per SM (0 = occupancy)
     int tune_rows_cap = 256;
     int tune_ctas = 0;
     std::string device_name;
     HostBuf h_stage, h_out;
-    HostBuf h_plan;  // page-locked mask descriptors and work items of chunked batches
+    HostBuf h_plan;   // page-locked mask descriptors and work items of chunked batches
+    HostBuf h_order;  // page-locked launch order of the device stroker's OFFSET units
     // host-side arc expansion scratch
     std::vector<uint8_t> x_kind;
     std::vector<double> x_pts;
@@ -439,13 +444,17 @@ void rz_destroy(rz_ctx* c) {
                       &c->p_pairs,  &c->p_scan,    &c->p_canvas,  &c->p_leaf,    &c->d_loss,    &c->p_rgba8,
                       &c->p_encode_in, &c->p_recs};
     for (DevBuf* b : bufs) b->release();
-    for (DevBuf* b : {&c->s_units, &c->s_styles, &c->s_counts, &c->s_off, &c->s_fin, &c->s_tmpk, &c->s_tmpp,
+    for (DevBuf* b : {&c->s_units, &c->s_styles, &c->s_counts, &c->s_off, &c->s_fin, &c->s_tmpk, &c->s_tmpp, &c->s_order,
                       &c->s_kind, &c->s_pts})
         b->release();
+    for (cudaStream_t s : c->tree_streams) cudaStreamSynchronize(s), cudaStreamDestroy(s);
+    for (cudaEvent_t e : c->tree_events) cudaEventDestroy(e);
+    c->layer_arena.release();
     for (DevBuf& b : c->layer_pool) b.release();
     for (DevBuf& b : c->mask_pool) b.release();
     c->h_stage.release();
     c->h_plan.release();
+    c->h_order.release();
     c->h_out.release();
     if (c->s_in) cudaStreamSynchronize(c->s_in), cudaStreamDestroy(c->s_in);
     if (c->s_out) cudaStreamSynchronize(c->s_out), cudaStreamDestroy(c->s_out);
@@ -2092,6 +2101,7 @@ rz_status rz_render_scene_tree(rz_ctx* ctx, const rz_scene* scene, const rz_scen
     int root = -1;
     if (n_nodes) {
         precompute_bboxes(T);
+        tr.mark("bboxes");
         root = build_rec(T, 0, OptBox{true, rzhost::Box{0.0, 0.0, (double)W, (double)H}}, kIdentity);
     }
     tr.mark("build");

@@ -441,8 +441,16 @@ __device__ __forceinline__ void write_piece(uint8_t* kind, double* pts, uint64_t
 constexpr int kOffsetMax = kStrokeOffsetMax;
 
 // OFFSET units: counts (emit == false) or pieces at off_start[u] (emit).
+// With an order list, consecutive threads take OFFSET units of the same
+// segment kind: the binary64 work of a warp then follows one code path for
+// longer (GB300's FP64 pipe pays for every warp instruction, however few of
+// its lanes are active).
 __global__ void k_stroke_offsets(StrokeArgs A, bool emit) {
-    const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (A.order) {
+        if (u >= A.n_order) return;
+        u = A.order[u];
+    }
     if (u >= A.n_units) return;
     const StrokeUnit un = A.units[u];
     if (un.type != STROKE_OFFSET) return;
@@ -602,9 +610,10 @@ cudaError_t launch_stroke_units(const StrokeSub* subs, uint32_t n_subs, StrokeUn
 cudaError_t launch_stroke(const StrokeArgs& A, int phase, cudaStream_t st) {
     if (A.n_units == 0) return cudaSuccess;
     const unsigned grid = (A.n_units + 127) / 128;
+    const unsigned grid_off = A.order ? (A.n_order + 127) / 128 : grid;
     switch (phase) {
-        case 0: k_stroke_offsets<<<grid, 128, 0, st>>>(A, false); break;
-        case 1: k_stroke_offsets<<<grid, 128, 0, st>>>(A, true); break;
+        case 0: if (grid_off) k_stroke_offsets<<<grid_off, 128, 0, st>>>(A, false); break;
+        case 1: if (grid_off) k_stroke_offsets<<<grid_off, 128, 0, st>>>(A, true); break;
         case 2: k_stroke_joins<<<grid, 128, 0, st>>>(A, false); break;
         case 3: k_stroke_joins<<<grid, 128, 0, st>>>(A, true); break;
         default: k_stroke_gather<<<grid, 128, 0, st>>>(A); break;

@@ -52,6 +52,8 @@ struct StrokeArgs {
     uint8_t* out_kind;     // the outline
     double* out_pts;
     int32_t strided;       // OFFSET pieces at kStrokeOffsetMax slots per unit (counts written by the emit pass)
+    const uint32_t* order; // OFFSET units in launch order (cubics, then quads, then lines), or null: every unit
+    uint32_t n_order;
 };
 
 constexpr int kStrokeOffsetMax = 36;  // 8 pieces of a cubic and 7 Round joins of up to 4 cubics
