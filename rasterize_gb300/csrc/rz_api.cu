@@ -763,13 +763,15 @@ struct PipeChunk {
 constexpr uint64_t kPipeChunkBytes = 32ull << 20;  // output bytes per chunk
 constexpr int kPipeMaxChunks = 16;                 // queue heads in the control words
 
-// Chunks of about equal pixel counts; none when the batch is too small to gain
+// Chunks of about equal pixel counts, the first and the last of half that
+// size (the first download waits for the first chunk's render, the last
+// render's download ends the call); none when the batch is too small to gain
 // from overlap or its masks are laid out so that the chunks' spans overlap.
 std::vector<PipeChunk> pipe_chunks(const std::vector<rz::MaskDev>& masks, uint64_t out_len) {
     std::vector<PipeChunk> chunks;
     const uint64_t bytes = out_len * 4;
     if (masks.size() < 2 || bytes < 2 * kPipeChunkBytes) return chunks;
-    const int K = (int)std::min<uint64_t>(kPipeMaxChunks, bytes / kPipeChunkBytes);
+    const int K = (int)std::min<uint64_t>(kPipeMaxChunks - 1, bytes / kPipeChunkBytes);
     uint64_t total = 0;
     for (const rz::MaskDev& m : masks)
         if (m.width > 0 && m.height > 0) total += (uint64_t)m.width * m.height;
@@ -780,7 +782,7 @@ std::vector<PipeChunk> pipe_chunks(const std::vector<rz::MaskDev>& masks, uint64
         const rz::MaskDev& m = masks[p];
         if (m.width > 0 && m.height > 0) acc += (uint64_t)m.width * m.height;
         const bool last = p + 1 == masks.size();
-        if (!last && acc * K < total * (chunks.size() + 1)) continue;
+        if (!last && acc * 2 * K < total * (2 * chunks.size() + 1)) continue;
         PipeChunk c{p_lo, p + 1, 0, 0, ~0ull, 0};
         for (uint32_t q = p_lo; q <= p; ++q) {
             const rz::MaskDev& n = masks[q];
