@@ -104,6 +104,7 @@ __device__ __forceinline__ void clear_row_tail(int4* row4, int width, int stride
 __device__ void diff_scan_blend_row(float* crow, int stride, int width, int rule, float alpha, float* Arow, int lane) {
     int4* row4 = reinterpret_cast<int4*>(crow);
     uint32_t carry = 0;
+    const bool vec = (width & 3) == 0;  // rows of A are 16-byte aligned: whole float4 chunks
     for (int x0 = 0; x0 < width; x0 += 128) {
         const int x = x0 + 4 * lane;
         int4 v = make_int4(0, 0, 0, 0);
@@ -124,6 +125,18 @@ __device__ void diff_scan_blend_row(float* crow, int stride, int width, int rule
         const uint32_t base = carry + incl - a3;
         carry += __shfl_sync(0xffffffffu, incl, 31);
         const uint32_t wv[4] = {base + a0, base + a1, base + a2, base + a3};
+        if (vec && x < width) {
+            // four pixels at once; an alpha below 1e-6 leaves the pixel as it is (fma with 0 is exact)
+            float4 dv = *reinterpret_cast<const float4*>(Arow + x);
+            float* d = reinterpret_cast<float*>(&dv);
+            #pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float al = alpha_from_winding_fix(rule, (int32_t)wv[i]);
+                d[i] = fmaf(al < 1e-6f ? 0.f : alpha * al, 1.f - d[i], d[i]);
+            }
+            *reinterpret_cast<float4*>(Arow + x) = dv;
+            continue;
+        }
         #pragma unroll
         for (int i = 0; i < 4; ++i) {
             if (x + i >= width) break;
