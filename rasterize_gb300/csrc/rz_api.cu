@@ -808,6 +808,9 @@ std::vector<PipeChunk> pipe_chunks(const std::vector<rz::MaskDev>& masks, uint64
 rz_status pipe_streams(rz_ctx* ctx, size_t n_events) {
     if (!ctx->s_in) RZ_CUDA(cudaStreamCreateWithFlags(&ctx->s_in, cudaStreamNonBlocking));
     if (!ctx->s_out) RZ_CUDA(cudaStreamCreateWithFlags(&ctx->s_out, cudaStreamNonBlocking));
+    // a call that failed half-way may have left copies queued: none may touch the buffers of this one
+    RZ_CUDA(cudaStreamSynchronize(ctx->s_in));
+    RZ_CUDA(cudaStreamSynchronize(ctx->s_out));
     while (ctx->pipe_ev.size() < n_events) {
         cudaEvent_t e;
         RZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));

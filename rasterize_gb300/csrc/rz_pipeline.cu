@@ -10,6 +10,8 @@
 // applies the fill rule and blends the fill's paint source-over into an RGBA
 // band kept in shared memory (Rasterizer::fill + Pipeline::render_rec,
 // src/rasterize.rs:69-115, src/scene.rs:407-435).
+#include <atomic>
+
 #include "rz_color.cuh"
 #include "rz_device.cuh"
 #include "rz_kernels.cuh"
@@ -641,12 +643,24 @@ int composite_smem_bytes(int canvas_w, int band_rows, int max_clip_width, bool p
     return 4 * band_rows * stride + (paint_mode ? 16 * band_rows * canvas_w : 0);
 }
 
+// The shared-memory attribute is per device: the largest size set so far on
+// each device (contexts on several GPUs, host threads calling at once).
+constexpr int kMaxAttrDevices = 64;
+static std::atomic<int> g_composite_smem[kMaxAttrDevices];
+
 cudaError_t launch_composite(const SceneDev& S, int cov_stride, int smem, cudaStream_t st) {
-    static int configured = 0;
-    if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_composite, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::atomic<int>* configured = dev >= 0 && dev < kMaxAttrDevices ? &g_composite_smem[dev] : nullptr;
+    if (!configured || smem > configured->load()) {
+        e = cudaFuncSetAttribute(k_composite, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
-        configured = smem;
+        if (configured) {
+            int cur = configured->load();
+            while (smem > cur && !configured->compare_exchange_weak(cur, smem)) {
+            }
+        }
     }
     k_composite<<<S.n_bands, kCompThreads, smem, st>>>(S, cov_stride);
     return cudaGetLastError();
