@@ -424,50 +424,58 @@ __device__ void diff_sparse_row(const DiffDev& D, int wpr, int row, const uint32
     const float* dlrow = D.dl_dimage + (uint64_t)row * W;
     uint32_t wcarry = 0;
     float gcarry = 0.f;
+    // Lane j owns the 32-pixel group w0 + j and walks its marked pixels in
+    // order; only the groups' totals go through warp scans (two per 1024
+    // pixels instead of two per marked group).
     for (int w0 = 0; w0 < wpr; w0 += 32) {
         const uint32_t mine = w0 + lane < wpr ? brow[w0 + lane] : 0u;
-        uint32_t nz = __ballot_sync(0xffffffffu, mine != 0u);
-        while (nz) {
-            const int j = __ffs(nz) - 1;
-            nz &= nz - 1u;
-            const uint32_t word = __shfl_sync(0xffffffffu, mine, j);
-            const int x = ((w0 + j) << 5) + lane;
-            const bool set = (word >> lane) & 1u;
-            const uint32_t d = set ? (uint32_t)crow[x] : 0u;
-            uint32_t wi = d;
-            #pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                const uint32_t o = __shfl_up_sync(0xffffffffu, wi, off);
-                if (lane >= off) wi += o;
-            }
-            const int32_t wn = (int32_t)(wcarry + wi);  // winding at pixel x
-            wcarry += __shfl_sync(0xffffffffu, wi, 31);
+        if (!__any_sync(0xffffffffu, mine != 0u)) continue;
+        const int xb = (w0 + lane) << 5;
+        // the group's winding change, then the winding before it
+        uint32_t dsum = 0;
+        for (uint32_t m = mine; m; m &= m - 1u) dsum += (uint32_t)crow[xb + __ffs(m) - 1];
+        uint32_t wi = dsum;
+        #pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t o = __shfl_up_sync(0xffffffffu, wi, off);
+            if (lane >= off) wi += o;
+        }
+        uint32_t wn = wcarry + wi - dsum;
+        wcarry += __shfl_sync(0xffffffffu, wi, 31);
+        // g at every marked pixel and its prefix within the group
+        float gsum = 0.f;
+        for (uint32_t m = mine; m; m &= m - 1u) {
+            const int x = xb + __ffs(m) - 1;
+            wn += (uint32_t)crow[x];  // winding at pixel x
             float gv = 0.f;
-            if (set && x < W) {
-                const float al = alpha_from_winding_fix(D.rule, wn);
+            if (x < W) {
+                const float al = alpha_from_winding_fix(D.rule, (int32_t)wn);
                 if (al >= 1e-6f) {  // pixels the forward skips have no slope
                     float da = 0.f;
                     if (D.rule == 1) {
-                        const int32_t fo = (int32_t)(((uint32_t)wn + (1u << 22)) & ((1u << 23) - 1u)) - (1 << 22);
+                        const int32_t fo =
+                            (int32_t)(((uint32_t)wn + (1u << 22)) & ((1u << 23) - 1u)) - (1 << 22);
                         da = fo > 0 ? 1.f : -1.f;
                     } else if (al < 1.f) {
-                        da = wn > 0 ? 1.f : -1.f;
+                        da = (int32_t)wn > 0 ? 1.f : -1.f;
                     }
                     if (da != 0.f) gv = dlrow[x] * D.alpha * (1.f - Arow[x]) / (1.f - D.alpha * al) * da;
                 }
             }
-            float gi = gv;
-            #pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                const float o = __shfl_up_sync(0xffffffffu, gi, off);
-                if (lane >= off) gi += o;
-            }
-            if (set) {
-                crow[x] = __float_as_int(gv);
-                prow[x] = gcarry + gi;
-            }
-            gcarry += __shfl_sync(0xffffffffu, gi, 31);
+            gsum += gv;
+            crow[x] = __float_as_int(gv);
+            prow[x] = gsum;
         }
+        float gi = gsum;
+        #pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const float o = __shfl_up_sync(0xffffffffu, gi, off);
+            if (lane >= off) gi += o;
+        }
+        const float gbase = gcarry + (gi - gsum);
+        gcarry += __shfl_sync(0xffffffffu, gi, 31);
+        if (gbase != 0.f)
+            for (uint32_t m = mine; m; m &= m - 1u) prow[xb + __ffs(m) - 1] += gbase;
     }
     if (lane == 0) *tot = gcarry;
 }
