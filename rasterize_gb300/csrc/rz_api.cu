@@ -147,6 +147,7 @@ struct rz_ctx {
     HostBuf h_stage, h_out;
     HostBuf h_plan;   // page-locked mask descriptors and work items of chunked batches
     HostBuf h_order;  // page-locked launch order of the device stroker's OFFSET units
+    HostBuf h_outline;  // page-locked host copy of the stroke outlines (their bounding boxes)
     // host-side arc expansion scratch
     std::vector<uint8_t> x_kind;
     std::vector<double> x_pts;
@@ -455,6 +456,7 @@ void rz_destroy(rz_ctx* c) {
     c->h_stage.release();
     c->h_plan.release();
     c->h_order.release();
+    c->h_outline.release();
     c->h_out.release();
     if (c->s_in) cudaStreamSynchronize(c->s_in), cudaStreamDestroy(c->s_in);
     if (c->s_out) cudaStreamSynchronize(c->s_out), cudaStreamDestroy(c->s_out);
