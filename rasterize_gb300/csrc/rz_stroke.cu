@@ -13,12 +13,13 @@
 //   CAPEND   the cap from the last piece of an open subpath's list to its
 //            first piece.
 // Every unit's pieces depend only on its own segment and its neighbours'
-// end pieces, so one thread per unit computes them: OFFSET units first (into
-// kStrokeOffsetMax slots each, or counted and then packed when those slots
-// would be too large), then the other units, which read the neighbours'
-// pieces, are counted; the host turns the counts into the outline's layout,
-// and the other units' pieces and the OFFSET pieces land in place.  hypot and
-// the arc's transcendental functions are CUDA's binary64 ones.
+// end pieces.  OFFSET units come first: the curves' split trees level by level
+// and their leaves one thread each, then one thread per unit assembles its
+// pieces (into kStrokeOffsetMax slots each, or counted and then packed when
+// those slots would be too large); then one thread per other unit, reading
+// the neighbours' pieces, counts its own; the host turns the counts into the
+// outline's layout, and the other units' pieces and the OFFSET pieces land in
+// place.  hypot and the arc's transcendental functions are CUDA's binary64 ones.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -345,68 +346,6 @@ __device__ void scap(const SSeg& self, const SSeg& other, double width, int cap,
     }
 }
 
-// Segment::offset of one segment (src/curve.rs:275-277, 515-517, 825-827):
-// quads split with split_at(0.5), cubics with Cubic::split, up to depth 3,
-// depth first; a cubic's consecutive pieces that do not meet get a Round join.
-__device__ void soffset(const SSeg& s, double dist, Sink& out) {
-    if (s.kind == 0) {
-        SLn l;
-        if (loffset(SLn{s.p[0], s.p[1]}, dist, l)) out.push(sline(l.a, l.b));
-        return;
-    }
-    SSeg stack[4];
-    int depth[4];
-    int sp = 0;
-    stack[0] = s;
-    depth[0] = 0;
-    bool have_last = false;
-    SSeg last{};
-    while (sp >= 0) {
-        const SSeg c = stack[sp];
-        const int d = depth[sp];
-        --sp;
-        const bool split = s.kind == 1 ? qsplit_needed(c) : csplit_needed(c);
-        if (split && d < 3) {
-            SSeg a = c, b = c;
-            const SP* p = c.p;
-            if (s.kind == 1) {
-                const double t = 0.5, t1 = t, t_1 = ds(1.0, t), t2 = dm(t1, t1), t_2 = dm(t_1, t_1);
-                const double w1 = dm(dm(2.0, t1), t_1);
-                const SP mid{da(da(dm(t_2, p[0].x), dm(w1, p[1].x)), dm(t2, p[2].x)),
-                             da(da(dm(t_2, p[0].y), dm(w1, p[1].y)), dm(t2, p[2].y))};
-                a.p[1] = SP{da(dm(t_1, p[0].x), dm(t, p[1].x)), da(dm(t_1, p[0].y), dm(t, p[1].y))};
-                a.p[2] = mid;
-                b.p[0] = mid;
-                b.p[1] = SP{da(dm(t_1, p[1].x), dm(t, p[2].x)), da(dm(t_1, p[1].y), dm(t, p[2].y))};
-            } else {
-                const SP mid{da(da(da(dm(0.125, p[0].x), dm(0.375, p[1].x)), dm(0.375, p[2].x)), dm(0.125, p[3].x)),
-                             da(da(da(dm(0.125, p[0].y), dm(0.375, p[1].y)), dm(0.375, p[2].y)), dm(0.125, p[3].y))};
-                a.p[1] = SP{da(dm(0.5, p[0].x), dm(0.5, p[1].x)), da(dm(0.5, p[0].y), dm(0.5, p[1].y))};
-                a.p[2] = SP{da(da(dm(0.25, p[0].x), dm(0.5, p[1].x)), dm(0.25, p[2].x)),
-                            da(da(dm(0.25, p[0].y), dm(0.5, p[1].y)), dm(0.25, p[2].y))};
-                a.p[3] = mid;
-                b.p[0] = mid;
-                b.p[1] = SP{da(da(dm(0.25, p[1].x), dm(0.5, p[2].x)), dm(0.25, p[3].x)),
-                            da(da(dm(0.25, p[1].y), dm(0.5, p[2].y)), dm(0.25, p[3].y))};
-                b.p[2] = SP{da(dm(0.5, p[2].x), dm(0.5, p[3].x)), da(dm(0.5, p[2].y), dm(0.5, p[3].y))};
-            }
-            // depth first, the first half first: at most one pending second half per level
-            stack[++sp] = b;
-            depth[sp] = d + 1;
-            stack[++sp] = a;
-            depth[sp] = d + 1;
-            continue;
-        }
-        SSeg r = c;
-        if (!polyoffset(r.p, slast(r.kind) + 1, dist)) continue;
-        if (s.kind == 2 && have_last && !pclose(send(last), sstart(r)))
-            sjoin(last, r, dm(dist, 2.0), STROKE_JOIN_ROUND, 0.0, out);
-        out.push(r);
-        have_last = true;
-        last = r;
-    }
-}
-
 __device__ SSeg load_sseg(const uint8_t* kind, const double* pts, uint32_t g, bool reversed) {
     SSeg s;
     const int k = kind[g];
@@ -438,30 +377,144 @@ __device__ __forceinline__ void write_piece(uint8_t* kind, double* pts, uint64_t
     }
 }
 
-constexpr int kOffsetMax = kStrokeOffsetMax;
-
-// OFFSET units: counts (emit == false) or pieces at off_start[u] (emit).
-// With an order list, consecutive threads take OFFSET units of the same
-// segment kind: the binary64 work of a warp then follows one code path for
-// longer (GB300's FP64 pipe pays for every warp instruction, however few of
-// its lanes are active).
-__global__ void k_stroke_offsets(StrokeArgs A, bool emit) {
-    uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (A.order) {
-        if (u >= A.n_order) return;
-        u = A.order[u];
+// ---------------------------------------------------------------------------
+// Segment::offset (src/curve.rs:275-277, 515-517, 825-827), node-parallel.
+// The reference splits a quad (split_at(0.5)) or a cubic (Cubic::split) while
+// quad/cubic_offset_should_split says so, up to depth 3, depth first, offsets
+// each leaf's control polygon and puts a Round join between consecutive pieces
+// of a cubic that do not meet.  GB300's FP64 pipe is paid per warp
+// instruction, so a thread per segment walking its own tree (lanes at
+// different nodes doing different work) wastes most of it.  Here every kernel
+// gives its threads the same work: the split decision of one node (levels 0,
+// 1, 2; a node at depth 3 is always a leaf), the offset of one leaf, then the
+// assembly of one unit's pieces in depth-first order (position k << (3 - d))
+// with the joins between them.  Each node's operations and their order are
+// the reference's, so the pieces are the same.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ SSeg node_seg(const StrokeNode& n) {
+    SSeg s;
+    s.kind = n.kind;
+    for (int j = 0; j < 4; ++j) s.p[j] = SP{n.p[2 * j], n.p[2 * j + 1]};
+    return s;
+}
+__device__ __forceinline__ void put_node(StrokeNode* list, uint32_t* counter, uint32_t t, uint32_t k, int d,
+                                         const SSeg& s) {
+    StrokeNode& n = list[atomicAdd(counter, 1u)];
+    n.t = t;
+    n.k = k;
+    n.d = d;
+    n.kind = s.kind;
+    for (int j = 0; j < 4; ++j) {
+        n.p[2 * j] = s.p[j].x;
+        n.p[2 * j + 1] = s.p[j].y;
     }
-    if (u >= A.n_units) return;
+}
+
+// Split decision of one node: two children into `out` (depth 3 children go to
+// the leaves), or the node itself into the leaves.
+__device__ void node_step(const StrokeNodes& N, const StrokeNode& n, StrokeNode* out, uint32_t* out_count) {
+    const SSeg c = node_seg(n);
+    const bool split = c.kind == 1 ? qsplit_needed(c) : csplit_needed(c);
+    if (!split) {
+        put_node(N.leaves, N.counters + 2, n.t, n.k, n.d, c);
+        return;
+    }
+    SSeg a = c, b = c;
+    const SP* p = c.p;
+    if (c.kind == 1) {
+        const double t = 0.5, t1 = t, t_1 = ds(1.0, t), t2 = dm(t1, t1), t_2 = dm(t_1, t_1);
+        const double w1 = dm(dm(2.0, t1), t_1);
+        const SP mid{da(da(dm(t_2, p[0].x), dm(w1, p[1].x)), dm(t2, p[2].x)),
+                     da(da(dm(t_2, p[0].y), dm(w1, p[1].y)), dm(t2, p[2].y))};
+        a.p[1] = SP{da(dm(t_1, p[0].x), dm(t, p[1].x)), da(dm(t_1, p[0].y), dm(t, p[1].y))};
+        a.p[2] = mid;
+        b.p[0] = mid;
+        b.p[1] = SP{da(dm(t_1, p[1].x), dm(t, p[2].x)), da(dm(t_1, p[1].y), dm(t, p[2].y))};
+    } else {
+        const SP mid{da(da(da(dm(0.125, p[0].x), dm(0.375, p[1].x)), dm(0.375, p[2].x)), dm(0.125, p[3].x)),
+                     da(da(da(dm(0.125, p[0].y), dm(0.375, p[1].y)), dm(0.375, p[2].y)), dm(0.125, p[3].y))};
+        a.p[1] = SP{da(dm(0.5, p[0].x), dm(0.5, p[1].x)), da(dm(0.5, p[0].y), dm(0.5, p[1].y))};
+        a.p[2] = SP{da(da(dm(0.25, p[0].x), dm(0.5, p[1].x)), dm(0.25, p[2].x)),
+                    da(da(dm(0.25, p[0].y), dm(0.5, p[1].y)), dm(0.25, p[2].y))};
+        a.p[3] = mid;
+        b.p[0] = mid;
+        b.p[1] = SP{da(da(dm(0.25, p[1].x), dm(0.5, p[2].x)), dm(0.25, p[3].x)),
+                    da(da(dm(0.25, p[1].y), dm(0.5, p[2].y)), dm(0.25, p[3].y))};
+        b.p[2] = SP{da(dm(0.5, p[2].x), dm(0.5, p[3].x)), da(dm(0.5, p[2].y), dm(0.5, p[3].y))};
+    }
+    StrokeNode* dst = n.d + 1 == 3 ? N.leaves : out;
+    uint32_t* cnt = n.d + 1 == 3 ? N.counters + 2 : out_count;
+    put_node(dst, cnt, n.t, 2 * n.k, n.d + 1, a);
+    put_node(dst, cnt, n.t, 2 * n.k + 1, n.d + 1, b);
+}
+
+__global__ void k_stroke_roots(StrokeArgs A, StrokeNodes N) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N.n_curves) return;
+    const StrokeUnit un = A.units[A.order[t]];
+    const SSeg s = load_sseg(A.kind, A.pts, un.seg, un.aux != 0);
+    StrokeNode n;
+    n.t = t;
+    n.k = 0;
+    n.d = 0;
+    n.kind = s.kind;
+    for (int j = 0; j < 4; ++j) {
+        n.p[2 * j] = s.p[j].x;
+        n.p[2 * j + 1] = s.p[j].y;
+    }
+    node_step(N, n, N.list[0], N.counters + 0);
+}
+
+__global__ void k_stroke_level(StrokeNodes N, int in) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N.counters[in]) return;
+    node_step(N, N.list[in][i], N.list[in ^ 1], N.counters + (in ^ 1));
+}
+
+// One leaf: polyline_offset of its control polygon (src/curve.rs:1302-1352).
+__global__ void k_stroke_leaves(StrokeArgs A, StrokeNodes N) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N.counters[2]) return;
+    const StrokeNode& n = N.leaves[i];
+    const StrokeUnit un = A.units[A.order[n.t]];
+    const double dist = A.styles[un.style].width / 2.0;
+    SSeg r = node_seg(n);
+    if (!polyoffset(r.p, slast(r.kind) + 1, dist)) return;
+    const uint64_t slot = 8ull * n.t + (n.k << (3 - n.d));
+    write_piece(N.piece_kind, N.piece_pts, slot, r);
+    atomicOr(N.valid + n.t, 1u << (n.k << (3 - n.d)));
+}
+
+// One OFFSET unit of the order list: a line's offset, or a curve's pieces in
+// order with a Round join between consecutive pieces that do not meet.
+__global__ void k_stroke_assemble(StrokeArgs A, StrokeNodes N, bool emit) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.n_order) return;
+    const uint32_t u = A.order[t];
     const StrokeUnit un = A.units[u];
-    if (un.type != STROKE_OFFSET) return;
-    const StrokeStyleDev st = A.styles[un.style];
-    SSeg buf[kOffsetMax];
-    Sink sink{buf, kOffsetMax, 0};
-    soffset(load_sseg(A.kind, A.pts, un.seg, un.aux != 0), st.width / 2.0, sink);
-    if (!emit || A.strided) A.counts[u] = (uint32_t)sink.n;  // strided: one pass, kOffsetMax slots a unit
+    const double dist = A.styles[un.style].width / 2.0;
+    SSeg buf[kStrokeOffsetMax];
+    Sink sink{buf, kStrokeOffsetMax, 0};
+    if (t >= N.n_curves) {
+        const SSeg s = load_sseg(A.kind, A.pts, un.seg, un.aux != 0);
+        SLn l;
+        if (loffset(SLn{s.p[0], s.p[1]}, dist, l)) sink.push(sline(l.a, l.b));
+    } else {
+        bool have_last = false;
+        SSeg last{};
+        for (uint32_t m = N.valid[t]; m; m &= m - 1u) {
+            const SSeg r = read_piece(N.piece_kind, N.piece_pts, 8ull * t + (__ffs(m) - 1));
+            if (r.kind == 2 && have_last && !pclose(send(last), sstart(r)))
+                sjoin(last, r, dm(dist, 2.0), STROKE_JOIN_ROUND, 0.0, sink);
+            sink.push(r);
+            have_last = true;
+            last = r;
+        }
+    }
+    if (!emit || A.strided) A.counts[u] = (uint32_t)sink.n;
     if (!emit) return;
     const uint64_t o = A.off_start[u];
-    for (int i = 0; i < sink.n && i < kOffsetMax; ++i) write_piece(A.tmp_kind, A.tmp_pts, o + i, buf[i]);
+    for (int i = 0; i < sink.n && i < kStrokeOffsetMax; ++i) write_piece(A.tmp_kind, A.tmp_pts, o + i, buf[i]);
 }
 
 // The nearest non-empty OFFSET unit in [lo, hi) from the end (last) or from the start.
@@ -607,16 +660,30 @@ cudaError_t launch_stroke_units(const StrokeSub* subs, uint32_t n_subs, StrokeUn
     return cudaGetLastError();
 }
 
+cudaError_t launch_stroke_nodes(const StrokeArgs& A, const StrokeNodes& N, cudaStream_t st) {
+    const uint32_t n = N.n_curves;
+    if (n == 0) return cudaSuccess;
+    k_stroke_roots<<<(n + 127) / 128, 128, 0, st>>>(A, N);
+    k_stroke_level<<<(2 * n + 127) / 128, 128, 0, st>>>(N, 0);  // depth 1 -> depth 2 nodes in list[1]
+    k_stroke_level<<<(4 * n + 127) / 128, 128, 0, st>>>(N, 1);  // depth 2 -> depth 3, all leaves
+    k_stroke_leaves<<<(8 * n + 127) / 128, 128, 0, st>>>(A, N);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stroke_assemble(const StrokeArgs& A, const StrokeNodes& N, bool emit, cudaStream_t st) {
+    if (A.n_order == 0) return cudaSuccess;
+    k_stroke_assemble<<<(A.n_order + 127) / 128, 128, 0, st>>>(A, N, emit);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_stroke(const StrokeArgs& A, int phase, cudaStream_t st) {
     if (A.n_units == 0) return cudaSuccess;
     const unsigned grid = (A.n_units + 127) / 128;
-    const unsigned grid_off = A.order ? (A.n_order + 127) / 128 : grid;
     switch (phase) {
-        case 0: if (grid_off) k_stroke_offsets<<<grid_off, 128, 0, st>>>(A, false); break;
-        case 1: if (grid_off) k_stroke_offsets<<<grid_off, 128, 0, st>>>(A, true); break;
         case 2: k_stroke_joins<<<grid, 128, 0, st>>>(A, false); break;
         case 3: k_stroke_joins<<<grid, 128, 0, st>>>(A, true); break;
-        default: k_stroke_gather<<<grid, 128, 0, st>>>(A); break;
+        case 4: k_stroke_gather<<<grid, 128, 0, st>>>(A); break;
+        default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
 }

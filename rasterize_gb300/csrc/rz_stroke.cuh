@@ -58,7 +58,35 @@ struct StrokeArgs {
 
 constexpr int kStrokeOffsetMax = 36;  // 8 pieces of a cubic and 7 Round joins of up to 4 cubics
 
-// phase 0 / 1: OFFSET counts / pieces; 2 / 3: the other units' counts / pieces; 4: gather.
+// A node of a curve's offset split tree (Segment::offset splits at 1/2 up to
+// depth 3): curve t of the order list, depth d, index k, its control points.
+struct StrokeNode {
+    uint32_t t, k;
+    int32_t d, kind;  // kind: 1 quad, 2 cubic
+    double p[8];
+};
+
+// Scratch of the node-parallel offsets of the first n_curves entries of
+// A.order (the quads and cubics): two node lists, the leaf list, their
+// counters, and every leaf's offset piece at position k << (3 - d) of its curve.
+struct StrokeNodes {
+    StrokeNode* list[2];    // depth 1 (capacity 2 n_curves) and depth 2 (4 n_curves) nodes
+    StrokeNode* leaves;     // capacity 8 n_curves
+    uint32_t* counters;     // [0] list[0], [1] list[1], [2] leaves
+    uint8_t* piece_kind;    // [n_curves * 8]
+    double* piece_pts;      // [n_curves * 8 * 8]
+    uint32_t* valid;        // [n_curves]: positions holding a piece
+    uint32_t n_curves;
+};
+
+// The offsets of every OFFSET unit in A.order: the curves' split trees level by
+// level (one thread per node), one thread per leaf for its offset, then one
+// thread per unit assembles its pieces in order with the Round joins between
+// them: counts (emit false) or counts and pieces at off_start (emit true).
+// N's counters must be zero.
+cudaError_t launch_stroke_nodes(const StrokeArgs& A, const StrokeNodes& N, cudaStream_t st);
+cudaError_t launch_stroke_assemble(const StrokeArgs& A, const StrokeNodes& N, bool emit, cudaStream_t st);
+// phase 2 / 3: the JOIN, CAP, CLOSE and CAPEND units' counts / pieces; 4: gather.
 cudaError_t launch_stroke(const StrokeArgs& A, int phase, cudaStream_t st);
 // The unit table of n_subs subpaths (n_units = the sum of their 4 m).
 cudaError_t launch_stroke_units(const StrokeSub* subs, uint32_t n_subs, StrokeUnit* units, uint64_t n_units,
