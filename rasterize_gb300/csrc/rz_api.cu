@@ -139,7 +139,7 @@ struct rz_ctx {
     std::vector<cudaEvent_t> tree_events;
     // the device stroker's unit table, counts and offsets, its compact offset
     // pieces, and the merged segment arrays it builds (swapped with d_kind / d_pts)
-    DevBuf s_units, s_styles, s_counts, s_off, s_fin, s_tmpk, s_tmpp, s_kind, s_pts, s_order, s_nodes, s_pieces;
+    DevBuf s_units, s_styles, s_counts, s_off, s_fin, s_tmpk, s_tmpp, s_kind, s_pts, s_order, s_nodes, s_pieces, s_joins;
     // batch tuning (rz_tune_batch / rz_set_tuning): band height cap, resident CTAs per SM (0 = occupancy)
     int tune_rows_cap = 256;
     int tune_ctas = 0;
@@ -445,7 +445,7 @@ void rz_destroy(rz_ctx* c) {
                       &c->p_pairs,  &c->p_scan,    &c->p_canvas,  &c->p_leaf,    &c->d_loss,    &c->p_rgba8,
                       &c->p_encode_in, &c->p_recs};
     for (DevBuf* b : bufs) b->release();
-    for (DevBuf* b : {&c->s_units, &c->s_styles, &c->s_counts, &c->s_off, &c->s_fin, &c->s_tmpk, &c->s_tmpp, &c->s_order, &c->s_nodes, &c->s_pieces,
+    for (DevBuf* b : {&c->s_units, &c->s_styles, &c->s_counts, &c->s_off, &c->s_fin, &c->s_tmpk, &c->s_tmpp, &c->s_order, &c->s_nodes, &c->s_pieces, &c->s_joins,
                       &c->s_kind, &c->s_pts})
         b->release();
     for (cudaStream_t s : c->tree_streams) cudaStreamSynchronize(s), cudaStreamDestroy(s);

@@ -529,12 +529,23 @@ __device__ int find_offset(const StrokeArgs& A, uint32_t lo, uint32_t hi, bool l
     return -1;
 }
 
-// JOIN / CAP / CLOSE / CAPEND units: counts, or pieces at fin_start[u] of the output.
+// JOIN / CAP / CLOSE / CAPEND units (the odd units): counts, or pieces at
+// fin_start[u] of the output.  With a join buffer the counting pass keeps the
+// pieces and the emitting pass only copies them.
 __global__ void k_stroke_joins(StrokeArgs A, bool emit) {
-    const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t u = 2 * t + 1;
     if (u >= A.n_units) return;
     const StrokeUnit un = A.units[u];
     if (un.type == STROKE_OFFSET) return;
+    if (emit && A.join_kind) {
+        const uint64_t o = A.fin_start[u];
+        for (uint32_t i = 0; i < A.counts[u] && i < 9; ++i) {
+            A.out_kind[o + i] = A.join_kind[9ull * t + i];
+            for (int j = 0; j < 8; ++j) A.out_pts[8 * (o + i) + j] = A.join_pts[8 * (9ull * t + i) + j];
+        }
+        return;
+    }
     const StrokeStyleDev st = A.styles[un.style];
     SSeg buf[9];
     Sink sink{buf, 9, 0};
@@ -575,6 +586,8 @@ __global__ void k_stroke_joins(StrokeArgs A, bool emit) {
     }
     if (!emit) {
         A.counts[u] = (uint32_t)sink.n;
+        if (A.join_kind)
+            for (int i = 0; i < sink.n && i < 9; ++i) write_piece(A.join_kind, A.join_pts, 9ull * t + i, buf[i]);
         return;
     }
     const uint64_t o = A.fin_start[u];
@@ -679,9 +692,10 @@ cudaError_t launch_stroke_assemble(const StrokeArgs& A, const StrokeNodes& N, bo
 cudaError_t launch_stroke(const StrokeArgs& A, int phase, cudaStream_t st) {
     if (A.n_units == 0) return cudaSuccess;
     const unsigned grid = (A.n_units + 127) / 128;
+    const unsigned grid_odd = (A.n_units / 2 + 127) / 128;  // the non-OFFSET units are the odd ones
     switch (phase) {
-        case 2: k_stroke_joins<<<grid, 128, 0, st>>>(A, false); break;
-        case 3: k_stroke_joins<<<grid, 128, 0, st>>>(A, true); break;
+        case 2: if (grid_odd) k_stroke_joins<<<grid_odd, 128, 0, st>>>(A, false); break;
+        case 3: if (grid_odd) k_stroke_joins<<<grid_odd, 128, 0, st>>>(A, true); break;
         case 4: k_stroke_gather<<<grid, 128, 0, st>>>(A); break;
         default: return cudaErrorInvalidValue;
     }

@@ -54,6 +54,8 @@ struct StrokeArgs {
     int32_t strided;       // OFFSET pieces at kStrokeOffsetMax slots per unit (counts written by the emit pass)
     const uint32_t* order; // OFFSET units in launch order (cubics, then quads, then lines), or null: every unit
     uint32_t n_order;
+    uint8_t* join_kind;    // the other (odd) units' pieces, 9 slots each, kept by the counting pass, or null
+    double* join_pts;
 };
 
 constexpr int kStrokeOffsetMax = 36;  // 8 pieces of a cubic and 7 Round joins of up to 4 cubics
