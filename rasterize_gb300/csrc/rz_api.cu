@@ -996,6 +996,7 @@ rz_status rz_mask(rz_ctx* ctx, const rz_path* path, const double tr[6], int32_t 
     if (!tr || !img) return fail(ctx, RZ_ERR_INVALID, "null argument");
     if (shape.width == 0 || shape.height == 0) return RZ_OK;
     rz_status st;
+    Trace trc("rz_mask");
     if (use_pipeline(path, shape.width, shape.height)) {
         st = check_path(ctx, path);
         if (st) return st;
@@ -1008,11 +1009,13 @@ rz_status rz_mask(rz_ctx* ctx, const rz_path* path, const double tr[6], int32_t 
         st = render_single(ctx, path, tr, fill_rule, flatness, shape.width, shape.height, false);
     }
     if (st) return st;
+    trc.gpu_mark(ctx->stream, "render");
     const size_t n = shape.width * shape.height;
     RZ_CUDA(ctx->h_out.ensure(n * 4));
     RZ_CUDA(cudaMemcpyAsync(ctx->h_out.p, ctx->d_out.p, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
     st = read_error(ctx);
     if (st) return st;
+    trc.mark("download");
     const float* src = (const float*)ctx->h_out.p;
     parallel_for((int64_t)shape.height, 64, [&](int64_t y0, int64_t y1) {
         for (int64_t y = y0; y < y1; ++y) {
@@ -1025,6 +1028,7 @@ rz_status rz_mask(rz_ctx* ctx, const rz_path* path, const double tr[6], int32_t 
             }
         }
     });
+    trc.mark("to_f64");
     return RZ_OK;
 }
 
