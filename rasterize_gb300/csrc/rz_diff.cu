@@ -101,49 +101,71 @@ __device__ __forceinline__ void clear_row_tail(int4* row4, int width, int stride
 // Row prefix of one band row (clearing it as it reads), fill rule, and
 // A += a alpha (1 - A) for the pixels the fill does not skip (|alpha| < 1e-6,
 // src/rasterize.rs:347-349).  One warp, 4 pixels per lane.
+// One 128-pixel step of the blend: windings base + a_i of the lane's 4 pixels.
+__device__ __forceinline__ void diff_blend4(float* Arow, int x, int width, bool vec, int rule, float alpha,
+                                            uint32_t base, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3) {
+    const uint32_t wv[4] = {base + a0, base + a1, base + a2, base + a3};
+    if (vec && x < width) {
+        // four pixels at once; an alpha below 1e-6 leaves the pixel as it is (fma with 0 is exact)
+        float4 dv = *reinterpret_cast<const float4*>(Arow + x);
+        float* d = reinterpret_cast<float*>(&dv);
+        #pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const float al = alpha_from_winding_fix(rule, (int32_t)wv[i]);
+            d[i] = fmaf(al < 1e-6f ? 0.f : alpha * al, 1.f - d[i], d[i]);
+        }
+        *reinterpret_cast<float4*>(Arow + x) = dv;
+        return;
+    }
+    #pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        if (x + i >= width) break;
+        const float al = alpha_from_winding_fix(rule, (int32_t)wv[i]);
+        if (al < 1e-6f) continue;
+        float& d = Arow[x + i];
+        d = fmaf(alpha * al, 1.f - d, d);
+    }
+}
+
+// Row prefix over kScanSteps 128-pixel steps at a time: the steps' warp
+// scans are independent, so their shuffles interleave instead of forming one
+// dependent chain per step; the carry then runs over the steps in order.
+constexpr int kScanSteps = 4;
+
 __device__ void diff_scan_blend_row(float* crow, int stride, int width, int rule, float alpha, float* Arow, int lane) {
     int4* row4 = reinterpret_cast<int4*>(crow);
     uint32_t carry = 0;
     const bool vec = (width & 3) == 0;  // rows of A are 16-byte aligned: whole float4 chunks
-    for (int x0 = 0; x0 < width; x0 += 128) {
-        const int x = x0 + 4 * lane;
-        int4 v = make_int4(0, 0, 0, 0);
-        if (x < width) {
-            v = row4[x >> 2];
-            row4[x >> 2] = make_int4(0, 0, 0, 0);
+    for (int x0 = 0; x0 < width; x0 += 128 * kScanSteps) {
+        uint32_t a0[kScanSteps], a1[kScanSteps], a2[kScanSteps], a3[kScanSteps], incl[kScanSteps];
+        #pragma unroll
+        for (int g = 0; g < kScanSteps; ++g) {
+            const int x = x0 + 128 * g + 4 * lane;
+            int4 v = make_int4(0, 0, 0, 0);
+            if (x < width) {
+                v = row4[x >> 2];
+                row4[x >> 2] = make_int4(0, 0, 0, 0);
+            }
+            a0[g] = (uint32_t)v.x;
+            a1[g] = a0[g] + (x + 1 < width ? (uint32_t)v.y : 0u);
+            a2[g] = a1[g] + (x + 2 < width ? (uint32_t)v.z : 0u);
+            a3[g] = a2[g] + (x + 3 < width ? (uint32_t)v.w : 0u);
+            incl[g] = a3[g];
         }
-        const uint32_t a0 = (uint32_t)v.x;
-        const uint32_t a1 = a0 + (x + 1 < width ? (uint32_t)v.y : 0u);
-        const uint32_t a2 = a1 + (x + 2 < width ? (uint32_t)v.z : 0u);
-        const uint32_t a3 = a2 + (x + 3 < width ? (uint32_t)v.w : 0u);
-        uint32_t incl = a3;
         #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
-            const uint32_t o = __shfl_up_sync(0xffffffffu, incl, off);
-            if (lane >= off) incl += o;
-        }
-        const uint32_t base = carry + incl - a3;
-        carry += __shfl_sync(0xffffffffu, incl, 31);
-        const uint32_t wv[4] = {base + a0, base + a1, base + a2, base + a3};
-        if (vec && x < width) {
-            // four pixels at once; an alpha below 1e-6 leaves the pixel as it is (fma with 0 is exact)
-            float4 dv = *reinterpret_cast<const float4*>(Arow + x);
-            float* d = reinterpret_cast<float*>(&dv);
             #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const float al = alpha_from_winding_fix(rule, (int32_t)wv[i]);
-                d[i] = fmaf(al < 1e-6f ? 0.f : alpha * al, 1.f - d[i], d[i]);
+            for (int g = 0; g < kScanSteps; ++g) {
+                const uint32_t o = __shfl_up_sync(0xffffffffu, incl[g], off);
+                if (lane >= off) incl[g] += o;
             }
-            *reinterpret_cast<float4*>(Arow + x) = dv;
-            continue;
         }
         #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            if (x + i >= width) break;
-            const float al = alpha_from_winding_fix(rule, (int32_t)wv[i]);
-            if (al < 1e-6f) continue;
-            float& d = Arow[x + i];
-            d = fmaf(alpha * al, 1.f - d, d);
+        for (int g = 0; g < kScanSteps; ++g) {
+            const uint32_t base = carry + incl[g] - a3[g];
+            carry += __shfl_sync(0xffffffffu, incl[g], 31);
+            if (x0 + 128 * g < width)
+                diff_blend4(Arow, x0 + 128 * g + 4 * lane, width, vec, rule, alpha, base, a0[g], a1[g], a2[g], a3[g]);
         }
     }
     clear_row_tail(row4, width, stride, lane);
