@@ -110,6 +110,24 @@ def test_invalid_trees_are_rejected(R):
     assert call([(_ffi.NODE_OPACITY, 0)]) == 2       # opacity without its child
 
 
+def test_line_only_strokes_match_oracle(R):
+    """Stroke nodes whose paths hold only lines: the device stroker's curve
+    stages have nothing to do and every offset is a line's."""
+    from rasterize_gb300 import LineCap, LineJoin, PathBuilder, StrokeStyle
+    rng = np.random.default_rng(77)
+    root = Scene()
+    for t in range(5):
+        b = PathBuilder().move_to(tuple(rng.uniform(10, 118, 2)))
+        for _ in range(6):
+            b.line_to(tuple(rng.uniform(10, 118, 2)))
+        if t % 2:
+            b.close()
+        style = StrokeStyle(float(rng.uniform(1.0, 6.0)), LineJoin(t % 3), 4.0, LineCap(t % 3))
+        root.stroke(b.build(), LinColor(*rng.uniform(0, 1, 3), 1.0), style)
+    bg = (0.0, 0.0, 0.0, 1.0)
+    assert_close(R.render_scene(root, 128, 128, bg=bg), oracle_scene_tree(root, 128, 128, bg=bg))
+
+
 @pytest.mark.parametrize("join,cap", [(0, 0), (1, 1), (2, 2)])
 def test_strokes_match_oracle(R, join, cap):
     """Stroke nodes (the outline filled NonZero): open and closed paths with

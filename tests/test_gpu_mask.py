@@ -226,9 +226,11 @@ def test_large_batch_in_chunks_into_page_locked_memory(R, with_arcs):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(41)
     paths, sizes, _ = W.glyph_batch(seed=43, n=1700)
+    # a few empty masks, the first one among them: chunks skip or absorb them
+    sizes = [(0, 0) if i % 61 == 0 else (w, 0) if i % 89 == 3 else (w, h) for i, (w, h) in enumerate(sizes)]
     trs, rules = [], []
     for i, (w, h) in enumerate(sizes):
-        if with_arcs and i % 37 == 5:
+        if with_arcs and i % 37 == 5 and w and h:
             paths[i] = _arc_glyph(w, h)
         a = rng.uniform(-0.3, 0.3)
         c = (w / 2, h / 2)
@@ -241,9 +243,10 @@ def test_large_batch_in_chunks_into_page_locked_memory(R, with_arcs):
     R.mask_batch(batch, out=pinned)
     for i in range(len(paths)):
         assert np.array_equal(batch.mask(pinned, i), batch.mask(one, i)), i
-    for i in range(0, len(paths), 97):
+    for i in range(1, len(paths), 97):
         w, h = sizes[i]
-        assert_close(batch.mask(pinned, i), O.mask(paths[i], trs[i], rules[i], w, h))
+        if w and h:
+            assert_close(batch.mask(pinned, i), O.mask(paths[i], trs[i], rules[i], w, h))
 
 
 def test_batch_with_transforms_and_rules(R):
