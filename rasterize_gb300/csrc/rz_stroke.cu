@@ -255,12 +255,30 @@ __device__ bool csplit_needed(const SSeg& c) {
 }
 
 // Pieces go to `out` (up to `cap`, then only counted).
+// Pieces go to `out` (up to `cap`, then only counted), or, with gkind set,
+// straight to pieces gbase, gbase + 1, ... of a global piece array (no
+// thread-local buffer: a large one lives in local memory).
 struct Sink {
     SSeg* out;
     int cap;
     int n;
+    uint8_t* gkind = nullptr;
+    double* gpts = nullptr;
+    uint64_t gbase = 0;
     __device__ void push(const SSeg& s) {
-        if (out && n < cap) out[n] = s;
+        if (n < cap) {
+            if (gkind) {
+                const uint64_t i = gbase + (uint64_t)n;
+                gkind[i] = (uint8_t)s.kind;
+                const int last = s.kind == 0 ? 1 : (s.kind == 1 ? 2 : 3);
+                for (int j = 0; j < 4; ++j) {
+                    gpts[8 * i + 2 * j] = j <= last ? s.p[j].x : 0.0;
+                    gpts[8 * i + 2 * j + 1] = j <= last ? s.p[j].y : 0.0;
+                }
+            } else if (out) {
+                out[n] = s;
+            }
+        }
         ++n;
     }
 };
@@ -493,8 +511,12 @@ __global__ void k_stroke_assemble(StrokeArgs A, StrokeNodes N, bool emit) {
     const uint32_t u = A.order[t];
     const StrokeUnit un = A.units[u];
     const double dist = A.styles[un.style].width / 2.0;
-    SSeg buf[kStrokeOffsetMax];
-    Sink sink{buf, kStrokeOffsetMax, 0};
+    Sink sink{nullptr, emit ? kStrokeOffsetMax : 0, 0};
+    if (emit) {
+        sink.gkind = A.tmp_kind;
+        sink.gpts = A.tmp_pts;
+        sink.gbase = A.off_start[u];
+    }
     if (t >= N.n_curves) {
         const SSeg s = load_sseg(A.kind, A.pts, un.seg, un.aux != 0);
         SLn l;
@@ -512,9 +534,6 @@ __global__ void k_stroke_assemble(StrokeArgs A, StrokeNodes N, bool emit) {
         }
     }
     if (!emit || A.strided) A.counts[u] = (uint32_t)sink.n;
-    if (!emit) return;
-    const uint64_t o = A.off_start[u];
-    for (int i = 0; i < sink.n && i < kStrokeOffsetMax; ++i) write_piece(A.tmp_kind, A.tmp_pts, o + i, buf[i]);
 }
 
 // The nearest non-empty OFFSET unit in [lo, hi) from the end (last) or from the start.
@@ -547,8 +566,19 @@ __global__ void k_stroke_joins(StrokeArgs A, bool emit) {
         return;
     }
     const StrokeStyleDev st = A.styles[un.style];
-    SSeg buf[9];
-    Sink sink{buf, 9, 0};
+    // counting: into the join buffer when there is one; emitting: into the outline
+    Sink sink{nullptr, 9, 0};
+    if (!emit && A.join_kind) {
+        sink.gkind = A.join_kind;
+        sink.gpts = A.join_pts;
+        sink.gbase = 9ull * t;
+    } else if (emit) {
+        sink.gkind = A.out_kind;
+        sink.gpts = A.out_pts;
+        sink.gbase = A.fin_start[u];
+    } else {
+        sink.cap = 0;
+    }
     if (un.type == STROKE_JOIN || un.type == STROKE_JOIN_CAP) {
         // joins the last piece before it to the first piece of the OFFSET unit after it
         if (A.counts[u + 1]) {
@@ -584,14 +614,7 @@ __global__ void k_stroke_joins(StrokeArgs A, bool emit) {
             }
         }
     }
-    if (!emit) {
-        A.counts[u] = (uint32_t)sink.n;
-        if (A.join_kind)
-            for (int i = 0; i < sink.n && i < 9; ++i) write_piece(A.join_kind, A.join_pts, 9ull * t + i, buf[i]);
-        return;
-    }
-    const uint64_t o = A.fin_start[u];
-    for (int i = 0; i < sink.n && i < 9; ++i) write_piece(A.out_kind, A.out_pts, o + i, buf[i]);
+    if (!emit) A.counts[u] = (uint32_t)sink.n;
 }
 
 // OFFSET units' pieces from the compact buffer to their place in the output.
