@@ -499,7 +499,10 @@ struct Staged {
 rz_status stage_host(rz_ctx* ctx, const uint8_t* kind, const double* pts, uint32_t n_seg, const uint32_t* sub_off,
                      uint32_t n_sub, const uint32_t* path_sub, uint32_t n_paths, const double* tr,
                      const uint8_t* rule, rz::BatchDev& b, const char** defer_kind = nullptr,
-                     const char** defer_pts = nullptr) {
+                     const char** defer_pts = nullptr, Trace* trace = nullptr) {
+    auto mark = [&](const char* phase) {
+        if (trace) trace->mark(phase);
+    };
     // arcs are converted to cubics on the host, as PathBuilder::arc_to does
     const bool has_arc = n_seg && std::memchr(kind, RZ_SEG_ARC, n_seg) != nullptr;
     ctx->expanded = has_arc;
@@ -528,11 +531,14 @@ rz_status stage_host(rz_ctx* ctx, const uint8_t* kind, const double* pts, uint32
         }
         return a.type == cudaMemoryTypeHost;
     };
+    mark("arc_scan");
     const bool direct = pinned(kind) && pinned(pts);
+    mark("pinned_check");
     const size_t total = (direct ? 0 : al(sz_kind) + al(sz_pts)) + al(sz_sub) + al(sz_psub) + al(sz_tr) + al(sz_rule);
     RZ_CUDA(ctx->h_stage.ensure(total));
     // wait for earlier copies out of the staging buffer before overwriting it
     RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+    mark("stage_sync");
     char* h = (char*)ctx->h_stage.p;
     size_t o = 0;
     auto put = [&](const void* src, size_t n) {  // large arrays are copied by all host threads
@@ -553,6 +559,7 @@ rz_status stage_host(rz_ctx* ctx, const uint8_t* kind, const double* pts, uint32
     char* hq = put(path_sub, sz_psub);
     char* ht = tr ? put(tr, sz_tr) : nullptr;
     char* hr = rule ? put(rule, sz_rule) : nullptr;
+    mark("put");
     RZ_CUDA(ctx->d_kind.ensure(sz_kind + 1));
     RZ_CUDA(ctx->d_pts.ensure(sz_pts + 8));
     RZ_CUDA(ctx->d_sub.ensure(sz_sub));
@@ -1102,9 +1109,10 @@ static rz_status mask_batch_impl(rz_ctx* ctx, const rz_path_batch* batch, double
         std::vector<PipeChunk> chunks;
         if (!per_path && !use_lines_kernel() && mapped_host(out)) chunks = pipe_chunks(masks, out_len);
         const char *hk = nullptr, *hp = nullptr;
+        tr.mark("chunks");
         st = stage_host(ctx, batch->seg_kind, batch->seg_pts, batch->n_segments, batch->subpath_off,
                         batch->n_subpaths, batch->path_subpath_off, P, batch->transforms, batch->fill_rules, b,
-                        chunks.empty() ? nullptr : &hk, chunks.empty() ? nullptr : &hp);
+                        chunks.empty() ? nullptr : &hk, chunks.empty() ? nullptr : &hp, &tr);
         if (st) return st;
         tr.mark("stage_inputs");
         if (!chunks.empty()) {
