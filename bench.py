@@ -40,11 +40,13 @@ WORKLOAD = "glyph_batch: 10000 closed glyphs, 10-400 segs (70% cubic/30% quad), 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--glyphs", type=int, default=10000)
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="bounded CPU baseline sample")
+    ap.add_argument("--load-seconds", type=float, default=1.0,
+                    help="back-to-back launches just before the timed region, under the clock sampler")
     ap.add_argument("--no-per-path", action="store_true")
     ap.add_argument("--no-configs", action="store_true", help="skip the C1/C2/C4/C5 legs")
     ap.add_argument("--workload", default="glyphs", choices=["glyphs", "small_path", "large_path", "scene", "diff", "encode", "scene_tree"],
@@ -73,6 +75,11 @@ class ClockSampler:
         self.gpu = gpu_index
         self.proc = None
         self.lines = []
+        self.first = 0
+
+    def mark(self):
+        """Samples before this call (the sampler's own start-up) are left out."""
+        self.first = len(self.lines)
 
     def start(self):
         try:
@@ -98,7 +105,7 @@ class ClockSampler:
             self.proc.kill()
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in self.lines[self.first:]:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -169,15 +176,26 @@ def _oracle_init(n):
 
 
 def _oracle_chunk(args):
-    """Worker: renders glyphs start, start + stride, ... with the binary64 oracle; returns pixels."""
-    start, stride = args
+    """Worker: renders glyphs start, start + stride, ... with the binary64
+    oracle's SignedDifferenceRasterizer (rasterizer "sd") or
+    ActiveEdgeRasterizer ("ae"); returns pixels."""
+    start, stride = args[:2]
+    rasterizer = args[2] if len(args) > 2 else "sd"
     O, tr = _WORKER["O"], _WORKER["id"]
+    fn = O.mask if rasterizer == "sd" else O.mask_ae
     px = 0
     for i in range(start, len(_WORKER["paths"]), stride):
         w, h = _WORKER["sizes"][i]
-        O.mask(_WORKER["paths"][i], tr, _WORKER["rules"][i], w, h)
+        fn(_WORKER["paths"][i], tr, _WORKER["rules"][i], w, h)
         px += w * h
     return px
+
+
+def headline_config(n_glyphs, segments, pixels, world):
+    """The `config` of the headline line, the same for both arms."""
+    return {"workload": WORKLOAD, "glyphs": n_glyphs, "segments": segments, "pixels_per_step": pixels,
+            "flatness": 0.05, "parallelism": "replicas" if world > 1 else "single",
+            "l2": "masks written per step (%.0f MB) exceed the 129 MB L2" % (pixels * 4 / 1e6)}
 
 
 def cpu_baseline_single(paths, sizes, rules, seconds, gpu_masks=None):
@@ -467,28 +485,40 @@ def run_reference(args, rank, world):
     O.build()
     cores = os.cpu_count() or 1
     from rasterize_gb300 import workloads as W
-    _, sizes, _ = W.glyph_batch(seed=2, n=args.glyphs)
+    paths, sizes, _ = W.glyph_batch(seed=2, n=args.glyphs)
     px_step = sum(w * h for w, h in sizes)
+    segments = sum(p.n_segments for p in paths)
     ctx = mp.get_context("spawn")
-    times = []
-    with ctx.Pool(cores, initializer=_oracle_init, initargs=(args.glyphs,)) as pool:
-        pool.map(_oracle_chunk, [(c, cores) for c in range(cores)])  # every worker has built its batch
-        for s in range(args.warmup + args.steps):
+
+    def timed(pool, rasterizer, steps, warmup):
+        times = []
+        for s in range(warmup + steps):
             t = time.perf_counter()
-            done = sum(pool.map(_oracle_chunk, [(c, cores) for c in range(cores)], chunksize=1))
+            done = sum(pool.map(_oracle_chunk, [(c, cores, rasterizer) for c in range(cores)], chunksize=1))
             dt = time.perf_counter() - t
             assert done == px_step
-            if s >= args.warmup:
+            if s >= warmup:
                 times.append(dt)
-    dt = sum(times) / len(times)
+        return sum(times) / len(times)
+
+    with ctx.Pool(cores, initializer=_oracle_init, initargs=(args.glyphs,)) as pool:
+        pool.map(_oracle_chunk, [(c, cores) for c in range(cores)])  # every worker has built its batch
+        dt = timed(pool, "sd", args.steps, args.warmup)
+        # the reference's other CPU rasterizer, on the same batch and cores (fewer steps: it is slower)
+        ae_steps = max(1, min(args.steps, 3))
+        dt_ae = timed(pool, "ae", ae_steps, 1)
     value = px_step / dt / 1e6
     out = {"metric": METRIC, "value": round(value, 3), "unit": "Mpx/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
-           "config": {"workload": WORKLOAD, "glyphs": args.glyphs, "pixels_per_step": px_step},
+           "config": headline_config(args.glyphs, segments, px_step, world),
            "cpu_baseline": {"value": round(value, 3), "unit": "Mpx/s", "cores": cores, "kind": "port",
                             "sample": "the whole batch (%d glyphs, %.2f Mpx) per step, interleaved over a spawn "
                                       "pool of %d processes" % (args.glyphs, px_step / 1e6, cores)},
+           "rasterizer": "SignedDifferenceRasterizer (src/rasterize.rs:279-507), binary64 port",
+           "active_edge": {"value": round(px_step / dt_ae / 1e6, 3), "unit": "Mpx/s", "steps": ae_steps,
+                           "ms_per_step": round(dt_ae * 1e3, 3), "cores": cores, "kind": "port",
+                           "rasterizer": "ActiveEdgeRasterizer (src/rasterize.rs:517-937), binary64 port"},
            "e2e": {"value": round(value, 3), "unit": "Mpx/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -555,6 +585,17 @@ def main():
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
+    clocks.mark()
+    # the sampler's period (200 ms) is far longer than a step: keep the GPU under the same load for
+    # --load-seconds before the timed region so the clock record describes this workload, not idle time
+    t_load = time.perf_counter()
+    load_launches = 0
+    while time.perf_counter() - t_load < args.load_seconds:
+        for _ in range(64):
+            plan.launch()
+        load_launches += 64
+        torch.cuda.synchronize(dev)
+    load_s = time.perf_counter() - t_load
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
@@ -566,6 +607,8 @@ def main():
     t_end.record(stream)
     torch.cuda.synchronize(dev)
     clk = clocks.stop()
+    clk["window"] = "%d back-to-back plan launches (%.2f s) just before the timed region, then the timed region" % (
+        load_launches, load_s)
     plan.status()
     total_ms = max_over_ranks(t_start.elapsed_time(t_end), dev)
     launch_ms = [a.elapsed_time(b) for a, b in ev]
@@ -620,9 +663,7 @@ def main():
         "metric": METRIC, "value": round(value, 2), "unit": "Mpx/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded glyph outlines)",
-        "config": {"workload": WORKLOAD, "glyphs": len(paths), "segments": batch.n_segments,
-                   "pixels_per_step": px, "flatness": 0.05, "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "masks written per step (%.0f MB) exceed the 129 MB L2" % (px * 4 / 1e6)},
+        "config": headline_config(len(paths), batch.n_segments, px, world),
         "segments_per_s": round(batch.n_segments * world / (ms_per_step / 1e3), 1),
         "masks_per_s": round(len(paths) * world / (ms_per_step / 1e3), 1),
         "per_path": per_path,

@@ -2,10 +2,10 @@
  * rasterize_gb300.h -- C ABI of the GB300 (sm_103a) rasterizer library.
  *
  * Drop-in boundary for the `Rasterizer` trait of aslpavel/rasterize v0.6.7
- * (src/rasterize.rs:44-101): a Rust `GpuRasterizer` (source in INTEGRATION.md)
- * packs its `Path` (src/path.rs:228-233) into `rz_path`, calls these entry
- * points and keeps the crate's `Path` / `Transform` / `FillRule` / `ImageMut`
- * API unchanged.  Every entry point returns a status; nothing traps or
+ * (src/rasterize.rs:44-101): a Rust `GpuRasterizer` shim (an `extern "C"`
+ * block over these declarations plus a `Rasterizer` impl) packs its `Path`
+ * (src/path.rs:228-233) into `rz_path`, calls these entry points and keeps
+ * the crate's `Path` / `Transform` / `FillRule` / `ImageMut` API unchanged.  Every entry point returns a status; nothing traps or
  * panics.  All functions are callable from any host thread; calls on one
  * context are serialised on the context's stream.
  */
@@ -35,7 +35,6 @@ typedef int32_t rz_status;
 #define RZ_ERR_DEPTH 5        /* a curve needs more than 22 bisection levels */
 #define RZ_ERR_ARC 6          /* an arc has no finite cubic count (the reference never terminates) */
 #define RZ_ERR_CAPACITY 7     /* an internal buffer limit was exceeded */
-#define RZ_ERR_SPIN 8         /* a bounded device wait gave up */
 
 /* ---- enums mirroring the reference ------------------------------------- */
 #define RZ_SEG_LINE 0  /* Segment::Line  src/curve.rs:905-909 */
@@ -351,7 +350,9 @@ RZ_API void rz_batch_plan_destroy(rz_batch_plan* plan);
  * 16384 paths and 65536 row bands per call, larger batches return
  * RZ_ERR_CAPACITY.  The first call on a device does a one-time set-up; make
  * it before any stream capture.  Calls share the array and must not overlap
- * on the GPU.  Returns after the work has finished (it reads the error word). */
+ * on the GPU; within one process they are serialised by a process-wide lock,
+ * across devices too.  The call is synchronous: it returns after its work has
+ * finished (it reads the error word). */
 RZ_API rz_status rz_mask_batch_noalloc(const rz_path_batch* batch, double flatness, float* out, uint64_t out_len,
                                        void* stream);
 

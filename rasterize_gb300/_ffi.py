@@ -17,7 +17,7 @@ HEADER = os.path.join(os.path.dirname(HERE), "include", "rasterize_gb300.h")
 
 RZ_OK = 0
 STATUS_NAMES = {0: "RZ_OK", 1: "RZ_ERR_NAN", 2: "RZ_ERR_INVALID", 3: "RZ_ERR_CUDA", 4: "RZ_ERR_NO_DEVICE",
-                5: "RZ_ERR_DEPTH", 6: "RZ_ERR_ARC", 7: "RZ_ERR_CAPACITY", 8: "RZ_ERR_SPIN"}
+                5: "RZ_ERR_DEPTH", 6: "RZ_ERR_ARC", 7: "RZ_ERR_CAPACITY"}
 RZ_MEM_HOST, RZ_MEM_DEVICE = 0, 1
 
 

@@ -4,11 +4,12 @@
 // Work items are (path, band of rows); a CTA pulls items from a device queue
 // (an atomic head counter), so thousands of uneven paths balance across the
 // 152 SMs.  Per item the CTA clears a shared-memory accumulation band
-// (rows x (clip_width + 3) floats), every thread walks the bisection trees of
+// (rows x (clip_width + 3) words), every thread walks the bisection trees of
 // a strided subset of the path's segments (skipping segments whose control
 // hull misses the band), accumulates signed area differences with shared
-// atomics, and finally one warp per row runs a two-sum compensated prefix
-// scan, applies the fill rule and streams the row to HBM with float4 stores.
+// int32 fixed-point atomics, and finally one warp per row runs an exact
+// integer prefix scan, applies the fill rule and streams the row to HBM with
+// float4 stores.
 // Nothing but the masks themselves is written to global memory.
 #include "rz_arc.cuh"
 #include "rz_device.cuh"

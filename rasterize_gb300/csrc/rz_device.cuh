@@ -14,9 +14,9 @@
 // Coverage (src/rasterize.rs:365-507): lines are clipped with the reference's
 // own x rules (drop x > width, fully-right lines become vertical at
 // width - 0.001, x < 0 parts become vertical at x = 0), then their signed
-// area differences are accumulated in shared memory per row band; a warp
-// scan with two-sum compensation turns differences into winding numbers and
-// the fill rule into alpha.
+// area differences are accumulated as int32 fixed point in shared memory per
+// row band; an exact integer warp scan turns differences into winding numbers
+// and the fill rule into alpha.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>

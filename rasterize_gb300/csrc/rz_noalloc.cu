@@ -18,13 +18,16 @@
 //
 // All calls share the one array, which keeps the last call's contents: the
 // queue head, error word and counters are cleared at the start of every call,
-// and calls whose work overlaps on the GPU (two streams, or two host threads)
-// race on the array.  The first call on a device performs a one-time set-up
+// and calls whose work overlaps on the GPU race on the array.  Inside one
+// process the calls are serialised: each holds a process-wide lock on the
+// host staging arrays until its work has finished, so a call on a second GPU
+// waits for a call on the first.  The first call on a device performs a one-time set-up
 // with that device current (the array's device address and the kernel's
 // shared-memory attribute); make that first call before any stream capture.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <mutex>
 
 #include "../../include/rasterize_gb300.h"
@@ -91,7 +94,7 @@ extern "C" {
 RZ_API rz_status rz_mask_batch_noalloc(const rz_path_batch* batch, double flatness, float* out, uint64_t out_len,
                                        void* stream) {
     if (!batch || !out || !batch->masks || batch->memory != RZ_MEM_DEVICE) return RZ_ERR_INVALID;
-    if (!(flatness > 0.0) || !(16.0 * flatness * flatness > 0.0) || flatness != flatness) return RZ_ERR_INVALID;
+    if (!std::isfinite(flatness) || !(16.0 * flatness * flatness > 0.0)) return RZ_ERR_INVALID;  // as rz_mask_batch
     const uint32_t P = batch->n_paths;
     if (P > (uint32_t)kMaxPaths) return RZ_ERR_CAPACITY;
     int device = 0;
@@ -167,7 +170,10 @@ RZ_API rz_status rz_mask_batch_noalloc(const rz_path_batch* batch, double flatne
     int32_t code = 0;
     if (cudaMemcpyAsync(&code, ctrl, sizeof(code), cudaMemcpyDeviceToHost, s) != cudaSuccess) return RZ_ERR_CUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess) return RZ_ERR_CUDA;
-    return code;  // device error words use the RZ_ERR_* values
+    // the kernel writes RZ_ERR_NAN, RZ_ERR_DEPTH or RZ_ERR_ARC; any other word is reported as a capacity error,
+    // the way the context entry points map it
+    if (code == RZ_OK || code == RZ_ERR_NAN || code == RZ_ERR_DEPTH || code == RZ_ERR_ARC) return code;
+    return RZ_ERR_CAPACITY;
 }
 
 }  // extern "C"

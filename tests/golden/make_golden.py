@@ -1,7 +1,7 @@
 """Extracts the reference's own test fixtures into reference_fixtures.json.
 
-Run in a checkout that has the reference crate mounted (default
-/root/reference); the GPU host never runs this.  It copies, as data:
+Usage: ``python make_golden.py <reference checkout>`` (the directory that
+holds the reference crate's src/ and data/); the GPU host never runs this.  It copies, as data:
 
 * the SVG path strings of the reference's unit tests (SQUIRREL in
   src/path.rs, the star/boxes path of test_fill_rule and the 9x4 polygon of
@@ -17,7 +17,6 @@ import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_fixtures.json")
 
 
@@ -33,6 +32,10 @@ def raw_in_fn(src, fn, idx=0):
 
 
 def main():
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <reference checkout>")
+    global REF
+    REF = sys.argv[1]
     path_rs = open(os.path.join(REF, "src/path.rs")).read()
     rast_rs = open(os.path.join(REF, "src/rasterize.rs")).read()
     fx = {
