@@ -55,30 +55,44 @@ def test_noalloc_matches_mask_batch():
             assert np.array_equal(a, e), "call %d, path %d: max difference %.3g" % (call, i, float(np.abs(a - e).max()))
 
 
-def test_noalloc_rejects_oversized_batch():
-    pytest.importorskip("torch")
+def _small_device_batch(torch, n, seed):
+    """A real device-memory batch: whatever the entry point does with it stays in bounds."""
     from rasterize_gb300 import MaskBatch, _ffi
     from rasterize_gb300 import workloads as W
 
-    paths, sizes, _ = W.glyph_batch(seed=22, n=2)
+    dev = torch.device("cuda", 0)
+    paths, sizes, _ = W.glyph_batch(seed=seed, n=n)
     batch = MaskBatch(paths, sizes)
-    s = batch.struct(_ffi.RZ_MEM_DEVICE, dict(kind=1, pts=1, sub_off=1, path_sub=1))
+    keep = dict(kind=torch.from_numpy(batch.kind).to(dev), pts=torch.from_numpy(batch.pts.reshape(-1)).to(dev),
+                sub_off=torch.from_numpy(batch.sub_off.view(np.int32)).to(dev),
+                path_sub=torch.from_numpy(batch.path_sub.view(np.int32)).to(dev),
+                out=torch.zeros(max(batch.out_len, 1), dtype=torch.float32, device=dev))
+    s = batch.struct(_ffi.RZ_MEM_DEVICE, {k: v.data_ptr() for k, v in keep.items()})
+    return batch, s, keep
+
+
+def test_noalloc_rejects_oversized_batch():
+    torch = pytest.importorskip("torch")
+    from rasterize_gb300 import _ffi
+
+    batch, s, keep = _small_device_batch(torch, 2, 22)
     s.n_paths = 16385  # beyond the static scratch; rejected before any memory is touched
-    big = (_ffi.RzMaskDesc * 16385)()
+    big = (_ffi.RzMaskDesc * 16385)()  # zero-size masks: nothing to render even if it were accepted
     s.masks = ctypes.addressof(big)
     lib = _ffi.load()
-    assert lib.rz_mask_batch_noalloc(ctypes.byref(s), 0.05, 1, 1 << 40, None) == 7  # RZ_ERR_CAPACITY
+    st = lib.rz_mask_batch_noalloc(ctypes.byref(s), 0.05, keep["out"].data_ptr(), batch.out_len, None)
+    torch.cuda.synchronize()
+    assert st == 7  # RZ_ERR_CAPACITY
 
 
 def test_noalloc_rejects_bad_flatness():
-    """Flatness must be finite and positive, as for rz_mask_batch."""
-    pytest.importorskip("torch")
-    from rasterize_gb300 import MaskBatch, _ffi
-    from rasterize_gb300 import workloads as W
+    """Flatness must make 16 f^2 finite and positive, as for rz_mask_batch."""
+    torch = pytest.importorskip("torch")
+    from rasterize_gb300 import _ffi
 
-    paths, sizes, _ = W.glyph_batch(seed=22, n=2)
-    batch = MaskBatch(paths, sizes)
-    s = batch.struct(_ffi.RZ_MEM_DEVICE, dict(kind=1, pts=1, sub_off=1, path_sub=1))
+    batch, s, keep = _small_device_batch(torch, 2, 22)
     lib = _ffi.load()
-    for f in (float("inf"), float("nan"), 0.0, -0.05, 1e-200):
-        assert lib.rz_mask_batch_noalloc(ctypes.byref(s), f, 1, batch.out_len, None) == 2, f  # RZ_ERR_INVALID
+    for f in (float("inf"), float("-inf"), float("nan"), 0.0, 1e-200):
+        st = lib.rz_mask_batch_noalloc(ctypes.byref(s), f, keep["out"].data_ptr(), batch.out_len, None)
+        assert st == 2, (f, st)  # RZ_ERR_INVALID
+    torch.cuda.synchronize()
