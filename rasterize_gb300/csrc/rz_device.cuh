@@ -228,7 +228,9 @@ __device__ inline int decide_fp32(int kind, const FlatCoef& c, int d, uint32_t k
         const float q = qerr * (1.f + tv);
         const float bx = (fabsf(c.a2x) + fabsf(c.a3x) * tv) * e21 + ms + q;
         const float by = (fabsf(c.a2y) + fabsf(c.a3y) * tv) * e21 + ms + q;
-        const float wx = sqrtf(gx), wy = sqrtf(gy);
+        // sqrt(gx) without a square root: gx is the larger square, so its root is the larger |w| (widened by
+        // 2^-22 to cover the rounding of the square and of a correctly rounded root)
+        const float wx = fmaxf(fabsf(wux), fabsf(wvx)) * 1.00000024f, wy = fmaxf(fabsf(wuy), fabsf(wvy)) * 1.00000024f;
         E = (2.f * wx + bx) * bx + (2.f * wy + by) * by + G * e19;
     } else {
         G = c.a2x * c.a2x + c.a2y * c.a2y;
@@ -352,7 +354,7 @@ __device__ __forceinline__ void accumulate_row(const Band& B, int r, int xb, flo
         sadd(row + x0i + 1, d - c0);
         return;
     }
-    const float s = 1.f / (xhi - xlo);
+    const float s = __fdividef(1.f, xhi - xlo);  // xhi - xlo > 1: the hardware reciprocal, within 2 ulp
     const float x0f = xlo - x0_floor;
     const float x1f = xhi - x1_ceil + 1.f;
     const float a0 = 0.5f * s * (1.f - x0f) * (1.f - x0f);  // share of the first pixel
@@ -396,9 +398,13 @@ __device__ inline void accumulate_piece(const Band& B, int xb, float x0, int32_t
     const int32_t qa_all = max(q0, row_lo << COV_SHIFT);
     const int32_t qb_all = min(q1, row_hi << COV_SHIFT);
     if (!(qa_all < qb_all)) return;
-    const float dxq = (x1 - x0) / (float)(q1 - q0);  // px per fixed-point unit of height
     const int r0 = qa_all >> COV_SHIFT;
     const int r1 = (qb_all + COV_ONE - 1) >> COV_SHIFT;
+    if (r1 == r0 + 1 && qa_all == q0 && qb_all == q1) {  // one row, unclipped: the ends are the crossings
+        accumulate_row(B, r0, xb, x0, x1, dir * (q1 - q0));
+        return;
+    }
+    const float dxq = __fdividef(x1 - x0, (float)(q1 - q0));  // px per fixed-point unit of height (within 2 ulp)
     for (int r = r0; r < r1; ++r) {
         const int32_t qa = max(qa_all, r << COV_SHIFT);
         const int32_t qb = min(qb_all, (r + 1) << COV_SHIFT);
@@ -410,8 +416,11 @@ __device__ inline void accumulate_piece(const Band& B, int xb, float x0, int32_t
 }
 
 // A long piece: x absolute in binary64, y band-relative in fixed point.  The
-// row crossings are interpolated in binary64 and every row is handed to the
-// FP32 distribution relative to its own integer column.
+// x of the row boundaries is stepped in 64-bit fixed point (2^-40 px: after
+// 16384 rows the accumulated step error is below 1e-8 px), so the rows cost
+// integer instructions; only the set-up is binary64.  Every row is handed to
+// the FP32 distribution relative to its own integer column.
+constexpr int kLongFrac = 40;
 static __device__ __noinline__ void accumulate_piece_long(const Band& B, double x0, int32_t q0, double x1,
                                                           int32_t q1) {
     if (q0 == q1) return;
@@ -429,14 +438,27 @@ static __device__ __noinline__ void accumulate_piece_long(const Band& B, double 
     const double dxq = (x1 - x0) / (double)(q1 - q0);
     const int r0 = qa_all >> COV_SHIFT;
     const int r1 = (qb_all + COV_ONE - 1) >> COV_SHIFT;
+    const double one = 1099511627776.0;  // 2^40
+    // x at the top of row r0 + 1 and the step per row, in units of 2^-40 px
+    long long xb_fix = __double2ll_rn((x0 + (double)(((r0 + 1) << COV_SHIFT) - q0) * dxq) * one);
+    const long long step = __double2ll_rn(dxq * (double)COV_ONE * one);
+    const long long x1_fix = __double2ll_rn(x1 * one);
+    long long xa_fix = qa_all == q0 ? __double2ll_rn(x0 * one) : __double2ll_rn((x0 + (double)(qa_all - q0) * dxq) * one);
     for (int r = r0; r < r1; ++r) {
         const int32_t qa = max(qa_all, r << COV_SHIFT);
         const int32_t qb = min(qb_all, (r + 1) << COV_SHIFT);
-        if (!(qa < qb)) continue;
-        const double xa = qa == q0 ? x0 : x0 + (double)(qa - q0) * dxq;
-        const double xn = qb == q1 ? x1 : x0 + (double)(qb - q0) * dxq;
-        const int col = (int)floor(fmin(xa, xn));
-        accumulate_row(B, r, col, (float)(xa - col), (float)(xn - col), dir * (qb - qa));
+        const long long xn_fix = qb == q1 ? x1_fix
+                                          : (qb == qb_all ? __double2ll_rn((x0 + (double)(qb - q0) * dxq) * one) : xb_fix);
+        if (qa < qb) {
+            const long long lo = min(xa_fix, xn_fix);
+            const long long col = lo >> kLongFrac;  // floor
+            const long long base = col << kLongFrac;
+            const float fa = (float)(xa_fix - base) * (1.0f / 1099511627776.0f);
+            const float fn = (float)(xn_fix - base) * (1.0f / 1099511627776.0f);
+            accumulate_row(B, r, (int)col, fa, fn, dir * (qb - qa));
+        }
+        xa_fix = xn_fix;
+        xb_fix += step;
     }
 }
 
@@ -633,17 +655,24 @@ __device__ inline bool clip_y64(double lo, double hi, double (&x)[2], double (&y
 // ---------------------------------------------------------------------------
 constexpr int kScanChunk = 4;
 
-template <int THREADS, class Epi>
+// CLEAR: every word the band's writes can reach (columns [0, width + 2),
+// the reference's two spill columns included) is zeroed as it is read, so the
+// band is clear for the next work item without a separate pass.
+template <int THREADS, class Epi, bool CLEAR = false>
 __device__ void band_scan(const Band& B, int width, int rule, const Epi& epi) {
     const int lane = threadIdx.x & 31;
+    const int span = CLEAR ? width + 2 : width;  // stride >= width + 2, a multiple of 16
     for (int r = threadIdx.x >> 5; r < B.bh; r += THREADS / 32) {
-        const int4* row4 = reinterpret_cast<const int4*>(B.acc + r * B.stride);
+        int4* row4 = reinterpret_cast<int4*>(B.acc + r * B.stride);
         uint32_t carry = 0;  // unsigned: the winding wraps by design
-        for (int x0 = 0; x0 < width; x0 += 32 * kScanChunk) {
+        for (int x0 = 0; x0 < span; x0 += 32 * kScanChunk) {
             const int x = x0 + kScanChunk * lane;
             int4 v = make_int4(0, 0, 0, 0);
-            if (x < width) v = row4[x >> 2];
-            const uint32_t a0 = (uint32_t)v.x;
+            if (x < span) {
+                v = row4[x >> 2];
+                if (CLEAR) row4[x >> 2] = make_int4(0, 0, 0, 0);
+            }
+            const uint32_t a0 = x < width ? (uint32_t)v.x : 0u;
             const uint32_t a1 = a0 + (x + 1 < width ? (uint32_t)v.y : 0u);
             const uint32_t a2 = a1 + (x + 2 < width ? (uint32_t)v.z : 0u);
             const uint32_t a3 = a2 + (x + 3 < width ? (uint32_t)v.w : 0u);
