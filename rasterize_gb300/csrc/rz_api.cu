@@ -26,6 +26,7 @@
 #include "rz_host_arc.cpp.inc"
 #include "rz_host_scene.cpp.inc"
 #include "rz_host_stroke.cpp.inc"
+#include "rz_glyph.cuh"
 #include "rz_kernels.cuh"
 #include "rz_pipeline.cuh"
 #include "rz_stroke.cuh"
@@ -131,6 +132,8 @@ struct rz_ctx {
     // output encode (sRGB8 RGBA) and its input staging
     DevBuf p_rgba8, p_encode_in;
     DevBuf p_recs;  // slot records of the band kernel
+    // glyph pipeline of the tuner: records, coefficients, chain offsets, tree codes, path flags, vertices, scan scratch
+    DevBuf g_recs, g_coef, g_chain, g_code, g_pflags, g_vtx, g_scan;
     // scene-tree layers by nesting depth: colour layers and clip masks
     std::vector<DevBuf> layer_pool, mask_pool;
     // concurrent scene-tree layers: one arena for every layer and mask, a stream pool, events
@@ -424,7 +427,8 @@ rz_ctx* rz_create(int device, rz_status* status) {
     if (cudaSetDevice(device) != cudaSuccess ||
         cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
-        rz::init_kernels() != cudaSuccess || rz::init_lines_kernel() != cudaSuccess) {
+        rz::init_kernels() != cudaSuccess || rz::init_lines_kernel() != cudaSuccess ||
+        rz::init_glyph_kernels() != cudaSuccess) {
         cudaGetLastError();
         delete c;
         if (status) *status = RZ_ERR_NO_DEVICE;
@@ -443,7 +447,8 @@ void rz_destroy(rz_ctx* c) {
                       &c->d_masks,  &c->d_items,   &c->d_out,     &c->d_ctrl,    &c->d_counts,  &c->p_fills,
                       &c->p_paints, &c->p_slots,   &c->p_lines,   &c->p_ecount,  &c->p_estart,  &c->p_ecursor,
                       &c->p_pairs,  &c->p_scan,    &c->p_canvas,  &c->p_leaf,    &c->d_loss,    &c->p_rgba8,
-                      &c->p_encode_in, &c->p_recs};
+                      &c->p_encode_in, &c->p_recs,  &c->g_recs,    &c->g_coef,    &c->g_chain,   &c->g_code,
+                      &c->g_pflags, &c->g_vtx,     &c->g_scan};
     for (DevBuf* b : bufs) b->release();
     for (DevBuf* b : {&c->s_units, &c->s_styles, &c->s_counts, &c->s_off, &c->s_fin, &c->s_tmpk, &c->s_tmpp, &c->s_order, &c->s_nodes, &c->s_pieces, &c->s_joins,
                       &c->s_kind, &c->s_pts})
@@ -631,6 +636,81 @@ int batch_grid(rz_ctx* ctx, int n_items, bool lines = false) {
 bool use_lines_kernel() {
     const char* e = std::getenv("RZ_BATCH_KERNEL");
     return e && std::strcmp(e, "lines") == 0;
+}
+
+// The glyph pipeline (rz_glyph.cu: records, walk, emit, cover) is the default
+// for batch plans; RZ_BATCH_KERNEL=bands selects the band kernel instead.
+bool use_glyph_pipeline() {
+    const char* e = std::getenv("RZ_BATCH_KERNEL");
+    return !(e && (std::strcmp(e, "bands") == 0 || std::strcmp(e, "lines") == 0));
+}
+
+// Subpath offsets non-decreasing within the segments, path offsets
+// non-decreasing within the subpaths: every slot belongs to one path.
+bool offsets_monotone(const uint32_t* sub, uint32_t n_sub, uint32_t n_seg, const uint32_t* psub, uint32_t n_paths) {
+    for (uint32_t i = 0; i < n_sub; ++i)
+        if (sub[i] > sub[i + 1]) return false;
+    if (sub[n_sub] > n_seg) return false;
+    for (uint32_t p = 0; p < n_paths; ++p)
+        if (psub[p] > psub[p + 1]) return false;
+    return psub[n_paths] <= n_sub;
+}
+
+int glyph_grid(rz_ctx* ctx, int n_items) {
+    const int occ = std::max(1, rz::glyph_cover_occupancy());
+    const int per_sm = ctx->tune_ctas > 0 ? std::min(ctx->tune_ctas, occ) : occ;
+    return std::max(1, std::min(n_items, ctx->num_sms * per_sm));
+}
+
+// Records, walks, chain offsets and vertices of a batch on `st` (the path
+// flags cleared first).
+cudaError_t glyph_enqueue_flatten(const rz::GlyphDev& g, uint32_t* scan_tmp, uint32_t n_paths, cudaStream_t st) {
+    const uint64_t n = (uint64_t)g.b.n_segments + g.b.n_subpaths;
+    cudaError_t e = cudaSuccess;
+    if (n_paths) e = cudaMemsetAsync(g.path_flags, 0, (size_t)n_paths * 4, st);
+    if (e == cudaSuccess) e = rz::launch_glyph_walk(g, st);
+    if (e == cudaSuccess) e = rz::scan_u32(g.chain, n + 1, scan_tmp, st);
+    if (e == cudaSuccess) e = rz::launch_glyph_emit(g, st);
+    return e;
+}
+
+// Buffers of the glyph pipeline for batch `b` (device memory), sized by one
+// walk + scan on `st`; the vertex buffer gets an eighth of slack for inputs
+// rewritten between launches (more is reported as ERR_CAPACITY).
+cudaError_t glyph_setup(const rz::BatchDev& b, rz::GlyphDev& g, DevBuf& recs, DevBuf& coefs, DevBuf& chain,
+                        DevBuf& code, DevBuf& pflags, DevBuf& vtx, DevBuf& scan, cudaStream_t st) {
+    const uint64_t n = (uint64_t)b.n_segments + b.n_subpaths;
+    cudaError_t e = recs.ensure(std::max<uint64_t>(n, 1) * sizeof(rz::GlyphRec));
+    if (e == cudaSuccess) e = coefs.ensure(std::max<uint64_t>(n, 1) * sizeof(rz::GlyphCoef));
+    if (e == cudaSuccess) e = chain.ensure((n + 1) * 4);
+    if (e == cudaSuccess) e = code.ensure(std::max<uint64_t>(n, 1) * 8);
+    if (e == cudaSuccess) e = pflags.ensure(std::max<uint64_t>(b.n_paths, 1) * 4);
+    if (e == cudaSuccess) e = scan.ensure(rz::scan_temp_words(n + 1) * 4 + 64);
+    if (e == cudaSuccess) e = cudaMemsetAsync(chain.p, 0, (n + 1) * 4, st);
+    if (e != cudaSuccess) return e;
+    g = rz::GlyphDev{};
+    g.b = b;
+    g.recs = (rz::GlyphRec*)recs.p;
+    g.coefs = (rz::GlyphCoef*)coefs.p;
+    g.chain = (uint32_t*)chain.p;
+    g.code = (unsigned long long*)code.p;
+    g.path_flags = (uint32_t*)pflags.p;
+    g.vtx = nullptr;
+    g.vtx_cap = 0;  // the sizing pass emits nothing
+    if (b.n_paths) e = cudaMemsetAsync(g.path_flags, 0, (size_t)b.n_paths * 4, st);
+    if (e == cudaSuccess) e = rz::launch_glyph_walk(g, st);
+    if (e == cudaSuccess) e = rz::scan_u32(g.chain, n + 1, (uint32_t*)scan.p, st);
+    uint32_t total = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&total, g.chain + n, 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return e;
+    const uint64_t want = std::min<uint64_t>((uint64_t)total + total / 8 + 1024, 0xffffffffull);
+    e = vtx.ensure(want * sizeof(int4));
+    if (e != cudaSuccess) return e;
+    g.vtx = (int4*)vtx.p;
+    g.vtx_cap = (uint32_t)std::min<uint64_t>(vtx.cap / sizeof(int4), 0xffffffffull);
+    // the sizing pass may have recorded errors (NaN, depth) and re-decisions: the first launch counts them again
+    return cudaMemsetAsync(b.err, 0, 32, st);
 }
 
 // Fills of a batch from host copies of its offsets, rules and transforms.
@@ -1233,6 +1313,10 @@ struct rz_batch_plan {
     // lines kernel: fills, line offsets, scan scratch, lines
     bool lines = false;
     DevBuf d_fills, d_slots, d_scan, d_lines;
+    // glyph pipeline: records, coefficients, chain lengths / offsets, tree codes, path flags, vertices
+    bool glyph = false;
+    rz::GlyphDev g{};
+    DevBuf d_grecs, d_gcoef, d_chain, d_code, d_pflags, d_vtx;
     int grid = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -1303,7 +1387,21 @@ rz_batch_plan* rz_batch_plan_create(rz_ctx* ctx, const rz_path_batch* batch, dou
         ok = ok && h_sub[batch->n_subpaths] <= batch->n_segments;
         plan->lines = ok;
     }
-    build_items(masks, false, plan->items, ctx->tune_rows_cap, plan->lines ? rz::lines_band_floats() : 0);
+    if (!plan->lines && P > 0 && use_glyph_pipeline()) {
+        // the glyph pipeline needs non-decreasing subpath and path offsets (every slot in one path)
+        h_sub.resize((size_t)batch->n_subpaths + 1);
+        h_psub.resize((size_t)P + 1);
+        cudaError_t ce = cudaMemcpy(h_sub.data(), batch->subpath_off, h_sub.size() * 4, cudaMemcpyDeviceToHost);
+        if (ce == cudaSuccess)
+            ce = cudaMemcpy(h_psub.data(), batch->path_subpath_off, h_psub.size() * 4, cudaMemcpyDeviceToHost);
+        if (ce != cudaSuccess) {
+            delete plan;
+            return bail(cuda_fail(ctx, ce, "plan: reading the batch offsets"));
+        }
+        plan->glyph = offsets_monotone(h_sub.data(), batch->n_subpaths, batch->n_segments, h_psub.data(), P);
+    }
+    build_items(masks, false, plan->items, ctx->tune_rows_cap,
+                plan->lines ? rz::lines_band_floats() : (plan->glyph ? rz::kGlyphBandFloats : 0));
     const size_t sz_m = std::max<size_t>(masks.size(), 1) * sizeof(rz::MaskDev);
     const size_t sz_i = std::max<size_t>(plan->items.items.size(), 1) * sizeof(rz::WorkItem);
     cudaError_t e = plan->d_masks.ensure(sz_m);
@@ -1337,8 +1435,17 @@ rz_batch_plan* rz_batch_plan_create(rz_ctx* ctx, const rz_path_batch* batch, dou
     b.counters = ctrl + 4;
     set_thresholds(b, flatness);
     const int n = (int)plan->items.items.size();
-    plan->grid = batch_grid(ctx, n, plan->lines);
-    if (!plan->lines && n > 0) b = with_records(b, P, plan->d_recs);
+    plan->grid = plan->glyph ? glyph_grid(ctx, n) : batch_grid(ctx, n, plan->lines);
+    if (!plan->lines && !plan->glyph && n > 0) b = with_records(b, P, plan->d_recs);
+    if (plan->glyph) {
+        b.n_paths = P;
+        e = glyph_setup(b, plan->g, plan->d_grecs, plan->d_gcoef, plan->d_chain, plan->d_code, plan->d_pflags,
+                        plan->d_vtx, plan->d_scan, plan->capture_stream);
+        if (e != cudaSuccess) {
+            rz_batch_plan_destroy(plan);
+            return bail(cuda_fail(ctx, e, "plan: glyph pipeline buffers"));
+        }
+    }
     int32_t* queue = ctrl + 8;
     rz::SceneDev S{};
     if (plan->lines) {
@@ -1377,9 +1484,13 @@ rz_batch_plan* rz_batch_plan_create(rz_ctx* ctx, const rz_path_batch* batch, dou
             lines_count(ctx, S, (uint32_t*)plan->d_scan.p, plan->capture_stream);
             rz::launch_flatten_emit(S, plan->capture_stream);
         }
+        if (plan->glyph) glyph_enqueue_flatten(plan->g, (uint32_t*)plan->d_scan.p, P, plan->capture_stream);
         cudaMemsetAsync(queue, 0, 4, plan->capture_stream);
         if (n > 0) {
-            if (plan->lines)
+            if (plan->glyph)
+                rz::launch_glyph_cover(plan->g, (const rz::WorkItem*)plan->d_items.p, n, queue, plan->grid,
+                                       plan->capture_stream);
+            else if (plan->lines)
                 rz::launch_mask_lines(S, (const rz::MaskDev*)plan->d_masks.p, (const rz::WorkItem*)plan->d_items.p, n,
                                       queue, out, plan->grid, plan->capture_stream);
             else {
@@ -1443,6 +1554,12 @@ void rz_batch_plan_destroy(rz_batch_plan* plan) {
     plan->d_slots.release();
     plan->d_scan.release();
     plan->d_lines.release();
+    plan->d_grecs.release();
+    plan->d_gcoef.release();
+    plan->d_chain.release();
+    plan->d_code.release();
+    plan->d_pflags.release();
+    plan->d_vtx.release();
     delete plan;
 }
 
@@ -2220,6 +2337,85 @@ rz_status rz_encode_mask_rgba8(rz_ctx* ctx, const void* mask, int32_t elem_size,
 // ---------------------------------------------------------------------------
 // Batch autotuner
 // ---------------------------------------------------------------------------
+namespace {
+
+// The tuner's candidates for the glyph pipeline: band-height cap (the work
+// item's shape) x resident cover CTAs per SM, each timed as one full pass
+// (records, walk, scan, emit, cover) on the caller's batch; median of 3
+// after a warm-up.
+rz_status tune_glyph(rz_ctx* ctx, const std::vector<rz::MaskDev>& masks, rz::BatchDev b, rz_tune_result* result) {
+    const uint32_t P = (uint32_t)masks.size();
+    const int occ = std::max(1, rz::glyph_cover_occupancy());
+    const int caps[5] = {16, 32, 64, 128, 256};
+    const int saved_cap = ctx->tune_rows_cap, saved_ctas = ctx->tune_ctas;
+    std::memset(result, 0, sizeof(*result));
+    result->ms = 1e30f;
+    Items items;
+    build_items(masks, false, items, 256, rz::kGlyphBandFloats);
+    rz_status st = stage_plan(ctx, masks, items, b);
+    if (st) return st;
+    b.n_paths = P;
+    rz::GlyphDev g{};
+    RZ_CUDA(glyph_setup(b, g, ctx->g_recs, ctx->g_coef, ctx->g_chain, ctx->g_code, ctx->g_pflags, ctx->g_vtx,
+                        ctx->g_scan, ctx->stream));
+    cudaEvent_t e0, e1;
+    RZ_CUDA(cudaEventCreate(&e0));
+    RZ_CUDA(cudaEventCreate(&e1));
+    int32_t* queue = (int32_t*)ctx->d_ctrl.p + 8;
+    for (int ci = 0; ci < 5 && st == RZ_OK; ++ci) {
+        build_items(masks, false, items, caps[ci], rz::kGlyphBandFloats);
+        const int n = (int)items.items.size();
+        if (ctx->d_items.ensure(std::max(n, 1) * sizeof(rz::WorkItem)) != cudaSuccess ||
+            cudaMemcpyAsync(ctx->d_items.p, items.items.data(), n * sizeof(rz::WorkItem), cudaMemcpyHostToDevice,
+                            ctx->stream) != cudaSuccess) {
+            st = RZ_ERR_CUDA;
+            break;
+        }
+        for (int per_sm = occ; per_sm >= std::max(1, occ - 2) && st == RZ_OK; --per_sm) {
+            const int grid = std::max(1, std::min(n, ctx->num_sms * per_sm));
+            float t[3] = {0.f, 0.f, 0.f};
+            for (int rep = 0; rep < 4 && st == RZ_OK; ++rep) {
+                cudaError_t e = cudaEventRecord(e0, ctx->stream);
+                if (e == cudaSuccess) e = glyph_enqueue_flatten(g, (uint32_t*)ctx->g_scan.p, P, ctx->stream);
+                if (e == cudaSuccess) e = cudaMemsetAsync(queue, 0, 4, ctx->stream);
+                if (e == cudaSuccess)
+                    e = rz::launch_glyph_cover(g, (const rz::WorkItem*)ctx->d_items.p, n, queue, grid, ctx->stream);
+                if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->stream);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                if (e != cudaSuccess) {
+                    st = RZ_ERR_CUDA;
+                    break;
+                }
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (rep > 0) t[rep - 1] = ms;  // the first launch warms up
+            }
+            if (st) break;
+            st = read_error(ctx);
+            if (st) break;
+            std::sort(t, t + 3);
+            if (result->n_entries < 16) result->entries[result->n_entries++] = rz_tune_entry{caps[ci], per_sm, t[1]};
+            if (t[1] < result->ms) {
+                result->ms = t[1];
+                result->band_rows_cap = caps[ci];
+                result->ctas_per_sm = per_sm;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st) {
+        ctx->tune_rows_cap = saved_cap;
+        ctx->tune_ctas = saved_ctas;
+        return st == RZ_ERR_CUDA ? fail(ctx, st, "tuning launch failed") : st;
+    }
+    ctx->tune_rows_cap = result->band_rows_cap;
+    ctx->tune_ctas = result->ctas_per_sm;
+    return RZ_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char* rz_device_name(rz_ctx* ctx) {
@@ -2276,6 +2472,15 @@ rz_status rz_tune_batch(rz_ctx* ctx, const rz_path_batch* batch, double flatness
     b.n_subpaths = batch->n_subpaths;
     b.out = out;
     set_thresholds(b, flatness);
+    // the kernel batch plans of this batch will use: the glyph pipeline when its offsets allow it
+    bool glyph = false;
+    if (P > 0 && use_glyph_pipeline()) {
+        std::vector<uint32_t> h_sub((size_t)batch->n_subpaths + 1), h_psub((size_t)P + 1);
+        RZ_CUDA(cudaMemcpy(h_sub.data(), batch->subpath_off, h_sub.size() * 4, cudaMemcpyDeviceToHost));
+        RZ_CUDA(cudaMemcpy(h_psub.data(), batch->path_subpath_off, h_psub.size() * 4, cudaMemcpyDeviceToHost));
+        glyph = offsets_monotone(h_sub.data(), batch->n_subpaths, batch->n_segments, h_psub.data(), P);
+    }
+    if (glyph) return tune_glyph(ctx, masks, b, result);
     const int occ = std::max(1, rz::mask_bands_occupancy());
     const int caps[5] = {16, 32, 64, 128, 256};
     const int saved_cap = ctx->tune_rows_cap, saved_ctas = ctx->tune_ctas;

@@ -388,11 +388,12 @@ def _pack_entries(entries):
 
 
 def _tune_key(device: str, batch: "MaskBatch", flatness: float) -> str:
-    """GPU + batch shape (paths, segments and pixels to two significant digits, flatness)."""
+    """GPU + batch kernel + batch shape (paths, segments and pixels to two significant digits, flatness)."""
     def sig2(v):
         return "%.1e" % float(v) if v else "0"
-    return "%s|paths=%s|segs=%s|px=%s|f=%g" % (device, sig2(len(batch.paths)), sig2(batch.n_segments),
-                                               sig2(batch.pixels), flatness)
+    kernel = os.environ.get("RZ_BATCH_KERNEL") or "glyph"
+    return "%s|%s|paths=%s|segs=%s|px=%s|f=%g" % (device, kernel, sig2(len(batch.paths)), sig2(batch.n_segments),
+                                                  sig2(batch.pixels), flatness)
 
 
 class DiffBatch:
