@@ -59,32 +59,64 @@ def test_forward_loss_and_gradient_match_oracle(R, rule, margin):
     assert gerr.max() <= 2e-3 * scale, (gerr.max(), scale)
 
 
-def test_gradient_matches_finite_differences(R):
-    """Central differences of the GPU loss at +-1e-3 px on random coordinates."""
-    rng = np.random.default_rng(7)
-    n, P, S, w, h = 1, 8, 8, 128, 96
-    ctrl, target = W.diff_batch(seed=2, n_images=n, paths=P, segs=S, size=96)
-    ctrl[..., 0] *= w / 96.0
-    target[..., 0] *= w / 96.0
-    T = oracle_images(target, n, P, S, w, h, FillRule.NonZero).astype(np.float32)
-    _, _, grad = run(R, ctrl, T, n, P, S, w, h, FillRule.NonZero)
+def _fd_setup(seed=2, P=8, S=8, w=128, h=96):
+    ctrl, target = W.diff_batch(seed=seed, n_images=1, paths=P, segs=S, size=h)
+    ctrl[..., 0] *= w / float(h)
+    target[..., 0] *= w / float(h)
+    T = oracle_images(target, 1, P, S, w, h, FillRule.NonZero).astype(np.float32)
+    return ctrl, T, P, S, w, h
+
+
+def _coords(rng, P, S, n=100):
+    return [(int(rng.integers(P)), int(rng.integers(3 * S)), int(rng.integers(2))) for _ in range(n)]
+
+
+def test_adjoint_matches_f64_finite_differences(R):
+    """The GPU adjoint against central differences (h = 1e-3 px) of the
+    reference's binary64 forward (the oracle) with the bisection tree held at
+    the unperturbed control points, as the adjoint holds it: at most 1e-3
+    relative error on 100 random coordinates (relative to max(|fd|, 1e-2))."""
+    ctrl, T, P, S, w, h = _fd_setup()
+    _, _, grad = run(R, ctrl, T, 1, P, S, w, h, FillRule.NonZero)
+    c64 = ctrl[0].astype(np.float64)
+    T64 = T[0].astype(np.float64)
+    worst = 0.0
+    for p, j, c in _coords(np.random.default_rng(7), P, S):
+        cp, cm = c64.copy(), c64.copy()
+        cp[p, j, c] += 1e-3
+        cm[p, j, c] -= 1e-3
+        lp = float(((O.diff_forward(cp, P, S, w, h, frozen=c64) - T64) ** 2).sum())
+        lm = float(((O.diff_forward(cm, P, S, w, h, frozen=c64) - T64) ** 2).sum())
+        fd = (lp - lm) / 2e-3
+        worst = max(worst, abs(float(grad[0, p, j, c]) - fd) / max(abs(fd), 1e-2))
+    assert worst <= 1e-3, worst
+
+
+def test_gradient_matches_gpu_finite_differences(R):
+    """Central differences (h = 1e-3 px) of the GPU's own FP32 forward.  The
+    forward quantises coverage to 2^-22 per winding unit, so a 1e-3 px step
+    resolves the loss derivative only to a few 1e-4 (the FD noise, not the
+    adjoint: against the binary64 forward the adjoint matches to 1e-4, see
+    the test above).  Bar: every coordinate within 1e-3 of the gradient's
+    scale (max |d loss / d ctrl|), the median within 1e-3 relative."""
+    ctrl, T, P, S, w, h = _fd_setup()
+    _, _, grad = run(R, ctrl, T, 1, P, S, w, h, FillRule.NonZero)
+    scale = float(np.abs(grad).max())
     hstep = np.float32(1e-3)
-    ok = 0
-    for _ in range(40):
-        p, j, c = rng.integers(P), rng.integers(3 * S), rng.integers(2)
+    errs, rels = [], []
+    for p, j, c in _coords(np.random.default_rng(8), P, S, 60):
         cp, cm = ctrl.copy(), ctrl.copy()
         cp[0, p, j, c] += hstep
         cm[0, p, j, c] -= hstep
-        dp = float(cp[0, p, j, c]) - float(ctrl[0, p, j, c])
-        dm = float(ctrl[0, p, j, c]) - float(cm[0, p, j, c])
-        lp = run(R, cp, T, n, P, S, w, h, FillRule.NonZero)[1]
-        lm = run(R, cm, T, n, P, S, w, h, FillRule.NonZero)[1]
-        fd = (lp - lm) / (dp + dm)
+        dsum = float(cp[0, p, j, c]) - float(cm[0, p, j, c])
+        lp = run(R, cp, T, 1, P, S, w, h, FillRule.NonZero)[1]
+        lm = run(R, cm, T, 1, P, S, w, h, FillRule.NonZero)[1]
+        fd = (lp - lm) / dsum
         an = float(grad[0, p, j, c])
-        if abs(an - fd) <= 2e-2 * max(abs(fd), 0.05):
-            ok += 1
-    # a re-decided tree node under the perturbation changes the loss by a step: allow a few
-    assert ok >= 36, ok
+        errs.append(abs(an - fd))
+        rels.append(abs(an - fd) / max(abs(fd), 1e-2))
+    assert max(errs) <= 1e-3 * scale, (max(errs), scale)
+    assert float(np.median(rels)) <= 1e-3, float(np.median(rels))
 
 
 def test_empty_and_invalid(R):
