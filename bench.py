@@ -49,7 +49,7 @@ def parse():
                     help="back-to-back launches just before the timed region, under the clock sampler")
     ap.add_argument("--no-per-path", action="store_true")
     ap.add_argument("--no-configs", action="store_true", help="skip the C1/C2/C4/C5 legs")
-    ap.add_argument("--workload", default="glyphs", choices=["glyphs", "small_path", "large_path", "scene", "diff", "encode", "scene_tree"],
+    ap.add_argument("--workload", default="glyphs", choices=["glyphs", "small_path", "large_path", "scene", "diff", "encode", "scene_tree", "link"],
                     help="glyphs: the headline line; the others run one configuration leg alone")
     ap.add_argument("--diff-images", type=int, default=64, help="images of the diff workload")
     ap.add_argument("--fd-coords", type=int, default=100, help="finite-difference coordinates of the diff workload")
@@ -539,6 +539,64 @@ def fd_f64(ctrl0, target0, paths, segs, size, coords, an):
             "note": "relative to max(|fd|, 1e-2); image 0, tree held at the unperturbed control points"}
 
 
+def run_link(size_mb=476):
+    """Host link: page-locked buffers of the C3 masks' size placed on each NUMA
+    node that has CPUs (process-level placement: the memory policy of this
+    process while the buffer is allocated and first touched), device->host and
+    host->device copy bandwidth (best of 5, CUDA events), and where the GPU
+    and this process sit (sysfs, nvidia-smi topo)."""
+    import ctypes
+    import glob
+    import torch
+    out = {}
+    nodes = sorted(int(p.rsplit("node", 1)[1]) for p in glob.glob("/sys/devices/system/node/node[0-9]*"))
+    cpus = {n: open("/sys/devices/system/node/node%d/cpulist" % n).read().strip() for n in nodes}
+    out["numa_nodes"] = cpus
+    out["process_cpus"] = len(os.sched_getaffinity(0))
+    try:
+        pci = subprocess.run(["nvidia-smi", "--query-gpu=pci.bus_id", "--format=csv,noheader"], capture_output=True,
+                             text=True, timeout=30).stdout.strip().splitlines()[0].lower()
+        node_file = "/sys/bus/pci/devices/%s/numa_node" % pci[4:]
+        out["gpu_pci"] = pci
+        out["gpu_numa_node"] = open(node_file).read().strip() if os.path.exists(node_file) else None
+    except Exception as e:  # noqa: BLE001 - informational only
+        out["gpu_numa_node"] = "unknown (%s)" % e
+    libc = ctypes.CDLL("libc.so.6", use_errno=True)
+    nr = 237 if os.uname().machine == "aarch64" else 238  # set_mempolicy
+
+    def policy(node):
+        if node is None:
+            return libc.syscall(nr, 0, None, 0)
+        mask = ctypes.c_ulong(1 << node)
+        return libc.syscall(nr, 2, ctypes.byref(mask), 64)  # MPOL_BIND
+
+    n = size_mb * (1 << 20) // 4
+    dev = torch.full((n,), 1.0, dtype=torch.float32, device="cuda")
+    res = {}
+    for node in [None] + [m for m in nodes if cpus[m]]:
+        if node is not None and policy(node) != 0:
+            res[str(node)] = "set_mempolicy failed (errno %d)" % ctypes.get_errno()
+            continue
+        host = torch.empty(n, dtype=torch.float32).pin_memory()
+        host.fill_(0.0)
+        policy(None)
+        torch.cuda.synchronize()
+        d2h, h2d = [], []
+        for _ in range(5):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(); host.copy_(dev, non_blocking=True); b.record(); torch.cuda.synchronize()
+            d2h.append(a.elapsed_time(b))
+            a.record(); dev.copy_(host, non_blocking=True); b.record(); torch.cuda.synchronize()
+            h2d.append(a.elapsed_time(b))
+        gb = n * 4 / 1e9
+        res["default" if node is None else str(node)] = {"d2h_gbs": round(gb / (min(d2h) / 1e3), 1),
+                                                          "h2d_gbs": round(gb / (min(h2d) / 1e3), 1)}
+        del host
+    out["bandwidth"] = res
+    out["bytes"] = n * 4
+    return out
+
+
 def run_reference(args, rank, world):
     """The reference's algorithm (the binary64 oracle port: the Rust crate has
     no toolchain here) on every host core: one process per core, each
@@ -610,7 +668,8 @@ def main():
                "scene": lambda: run_scene(R, stream, n=args.scene_fills),
                "diff": lambda: run_diff(R, stream, n_images=args.diff_images, fd_coords=args.fd_coords),
                "encode": lambda: run_encode(R, stream),
-               "scene_tree": lambda: run_scene_tree(R, stream)}[args.workload]()
+               "scene_tree": lambda: run_scene_tree(R, stream),
+               "link": lambda: run_link()}[args.workload]()
         if rank == 0:
             print(json.dumps({"metric": METRIC, "workload": args.workload, "n_gpus": world, **leg}))
         return
