@@ -133,7 +133,7 @@ struct rz_ctx {
     DevBuf p_rgba8, p_encode_in;
     DevBuf p_recs;  // slot records of the band kernel
     // glyph pipeline of the tuner: records, coefficients, chain offsets, tree codes, path flags, vertices, scan scratch
-    DevBuf g_recs, g_coef, g_chain, g_code, g_pflags, g_vtx, g_scan;
+    DevBuf g_recs, g_coef, g_chain, g_code, g_pflags, g_vtx, g_scan, g_paths;
     // scene-tree layers by nesting depth: colour layers and clip masks
     std::vector<DevBuf> layer_pool, mask_pool;
     // concurrent scene-tree layers: one arena for every layer and mask, a stream pool, events
@@ -448,7 +448,7 @@ void rz_destroy(rz_ctx* c) {
                       &c->p_paints, &c->p_slots,   &c->p_lines,   &c->p_ecount,  &c->p_estart,  &c->p_ecursor,
                       &c->p_pairs,  &c->p_scan,    &c->p_canvas,  &c->p_leaf,    &c->d_loss,    &c->p_rgba8,
                       &c->p_encode_in, &c->p_recs,  &c->g_recs,    &c->g_coef,    &c->g_chain,   &c->g_code,
-                      &c->g_pflags, &c->g_vtx,     &c->g_scan};
+                      &c->g_pflags, &c->g_vtx,     &c->g_scan,    &c->g_paths};
     for (DevBuf* b : bufs) b->release();
     for (DevBuf* b : {&c->s_units, &c->s_styles, &c->s_counts, &c->s_off, &c->s_fin, &c->s_tmpk, &c->s_tmpp, &c->s_order, &c->s_nodes, &c->s_pieces, &c->s_joins,
                       &c->s_kind, &c->s_pts})
@@ -678,9 +678,10 @@ cudaError_t glyph_enqueue_flatten(const rz::GlyphDev& g, uint32_t* scan_tmp, uin
 // walk + scan on `st`; the vertex buffer gets an eighth of slack for inputs
 // rewritten between launches (more is reported as ERR_CAPACITY).
 cudaError_t glyph_setup(const rz::BatchDev& b, rz::GlyphDev& g, DevBuf& recs, DevBuf& coefs, DevBuf& chain,
-                        DevBuf& code, DevBuf& pflags, DevBuf& vtx, DevBuf& scan, cudaStream_t st) {
+                        DevBuf& code, DevBuf& pflags, DevBuf& vtx, DevBuf& scan, DevBuf& paths, cudaStream_t st) {
     const uint64_t n = (uint64_t)b.n_segments + b.n_subpaths;
     cudaError_t e = recs.ensure(std::max<uint64_t>(n, 1) * sizeof(rz::GlyphRec));
+    if (e == cudaSuccess) e = paths.ensure(std::max<uint64_t>(b.n_paths, 1) * rz::glyph_path_bytes());
     if (e == cudaSuccess) e = coefs.ensure(std::max<uint64_t>(n, 1) * sizeof(rz::GlyphCoef));
     if (e == cudaSuccess) e = chain.ensure((n + 1) * 4);
     if (e == cudaSuccess) e = code.ensure(std::max<uint64_t>(n, 1) * 8);
@@ -695,6 +696,7 @@ cudaError_t glyph_setup(const rz::BatchDev& b, rz::GlyphDev& g, DevBuf& recs, De
     g.chain = (uint32_t*)chain.p;
     g.code = (unsigned long long*)code.p;
     g.path_flags = (uint32_t*)pflags.p;
+    g.paths = paths.p;
     g.vtx = nullptr;
     g.vtx_cap = 0;  // the sizing pass emits nothing
     if (b.n_paths) e = cudaMemsetAsync(g.path_flags, 0, (size_t)b.n_paths * 4, st);
@@ -1316,7 +1318,7 @@ struct rz_batch_plan {
     // glyph pipeline: records, coefficients, chain lengths / offsets, tree codes, path flags, vertices
     bool glyph = false;
     rz::GlyphDev g{};
-    DevBuf d_grecs, d_gcoef, d_chain, d_code, d_pflags, d_vtx;
+    DevBuf d_grecs, d_gcoef, d_chain, d_code, d_pflags, d_vtx, d_gpaths;
     int grid = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -1440,7 +1442,7 @@ rz_batch_plan* rz_batch_plan_create(rz_ctx* ctx, const rz_path_batch* batch, dou
     if (plan->glyph) {
         b.n_paths = P;
         e = glyph_setup(b, plan->g, plan->d_grecs, plan->d_gcoef, plan->d_chain, plan->d_code, plan->d_pflags,
-                        plan->d_vtx, plan->d_scan, plan->capture_stream);
+                        plan->d_vtx, plan->d_scan, plan->d_gpaths, plan->capture_stream);
         if (e != cudaSuccess) {
             rz_batch_plan_destroy(plan);
             return bail(cuda_fail(ctx, e, "plan: glyph pipeline buffers"));
@@ -1560,6 +1562,7 @@ void rz_batch_plan_destroy(rz_batch_plan* plan) {
     plan->d_code.release();
     plan->d_pflags.release();
     plan->d_vtx.release();
+    plan->d_gpaths.release();
     delete plan;
 }
 
@@ -2357,7 +2360,7 @@ rz_status tune_glyph(rz_ctx* ctx, const std::vector<rz::MaskDev>& masks, rz::Bat
     b.n_paths = P;
     rz::GlyphDev g{};
     RZ_CUDA(glyph_setup(b, g, ctx->g_recs, ctx->g_coef, ctx->g_chain, ctx->g_code, ctx->g_pflags, ctx->g_vtx,
-                        ctx->g_scan, ctx->stream));
+                        ctx->g_scan, ctx->g_paths, ctx->stream));
     cudaEvent_t e0, e1;
     RZ_CUDA(cudaEventCreate(&e0));
     RZ_CUDA(cudaEventCreate(&e1));

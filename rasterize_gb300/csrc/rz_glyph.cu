@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(256) k_glyph_records(GlyphDev g) {
 // Each lane walks the trees of kWalkPerLane slots one after the other in one
 // flat loop (a lane that finishes a tree starts its next slot while the other
 // lanes keep deciding), so the warp's lanes stay busy however uneven the
-// trees.
+// trees.  The next slot's record is loaded while the current tree is walked.
 constexpr int kWalkPerLane = 4;
 
 __global__ void __launch_bounds__(256) k_glyph_walk(GlyphDev g) {
@@ -114,30 +114,50 @@ __global__ void __launch_bounds__(256) k_glyph_walk(GlyphDev g) {
     const uint32_t warp = (blockIdx.x * 256u + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
     const uint32_t first = warp * 32u * kWalkPerLane + lane;
     int fallbacks = 0;
-    int s = -1;            // index of the lane's current slot in its list
-    uint32_t j = 0;        // current slot
-    bool walking = false;  // a tree is being walked
-    SegRec rec;
+    int s = 0;            // index in the lane's list of the slot held in `next`
+    uint32_t j = 0;       // slot being walked
+    bool walking = false;
+    SegRec rec, nrec;
+    GlyphCoef nc{};
+    uint32_t ntag = REC_EMPTY << 30;
     FlatCoef fc;
     float qerr = 0.f;
     const double* trm = nullptr;
     int d = 0, pos = 0;
     uint32_t k = 0, leaves = 0;
     unsigned long long code = 0;
+    if (first < n) {
+        const GlyphRec gr = g.recs[first];
+        nrec = gr.rec;
+        ntag = gr.tag;
+        nc = g.coefs[first];
+    }
     for (;;) {
         if (!walking) {
-            // the lane's next slot; slots that are not fixed-point records have empty chains
+            // take the prefetched slot and prefetch the one after it; slots that are not fixed-point
+            // records have empty chains
             for (;;) {
-                ++s;
+                if (s >= kWalkPerLane) break;
                 j = first + 32u * (uint32_t)s;
-                if (s >= kWalkPerLane || j >= n) break;
-                const GlyphRec gr = g.recs[j];
-                if ((gr.tag >> 30) == REC_FIX) {
-                    rec = gr.rec;
-                    const GlyphCoef c = g.coefs[j];
+                if (j >= n) {
+                    s = kWalkPerLane;
+                    break;
+                }
+                const uint32_t tag = ntag;
+                rec = nrec;
+                const GlyphCoef c = nc;
+                ++s;
+                const uint32_t jn = first + 32u * (uint32_t)s;
+                if (s < kWalkPerLane && jn < n) {
+                    const GlyphRec gr = g.recs[jn];
+                    nrec = gr.rec;
+                    ntag = gr.tag;
+                    nc = g.coefs[jn];
+                }
+                if ((tag >> 30) == REC_FIX) {
                     fc = flat_of(c);
                     qerr = c.qerr;
-                    const uint32_t owner = gr.tag & kAnyPath;
+                    const uint32_t owner = tag & kAnyPath;
                     trm = (b.tr && owner != kAnyPath) ? b.tr + 6ull * owner : nullptr;
                     walking = true;
                     d = 0;
@@ -307,14 +327,48 @@ __global__ void __launch_bounds__(256) k_glyph_emit(GlyphDev g) {
 
 constexpr int kCoverThreads = 256;
 
-template <bool FLAT>
-__device__ __forceinline__ void cover_finish(const Band& B, const MaskDev& m, int rule, float* out, float* acc) {
+// What a cover work item needs of its path, gathered once per launch by
+// k_glyph_paths so an item starts with two loads instead of a chain of five.
+struct __align__(16) GlyphPath {
+    uint32_t vs0, vs1;    // vertex range of the segments' chains
+    uint32_t vc0, vc1;    // vertex range of the closing lines' chains
+    uint32_t seg0, seg1;  // segment range (the binary64 slow path)
+    uint32_t sub0, sub1;  // subpath range
+    uint32_t flags;       // bit 0: slots the fixed-point route cannot take; bits 8-15: fill rule
+    uint32_t pad[3];
+};
+
+__global__ void __launch_bounds__(256) k_glyph_paths(GlyphDev g, GlyphPath* __restrict__ out) {
+    const uint32_t p = blockIdx.x * 256u + threadIdx.x;
+    const BatchDev& b = g.b;
+    if (p >= b.n_paths) return;
+    // ranges are clamped to the arrays so malformed offsets cannot read out of bounds
+    const uint32_t sub1 = min(b.path_sub[p + 1], b.n_subpaths);
+    const uint32_t sub0 = min(b.path_sub[p], sub1);
+    const uint32_t seg1 = min(b.sub_off[sub1], b.n_segments);
+    const uint32_t seg0 = min(b.sub_off[sub0], seg1);
+    GlyphPath q;
+    q.vs0 = min(g.chain[seg0], g.vtx_cap);
+    q.vs1 = min(g.chain[seg1], g.vtx_cap);
+    q.vc0 = min(g.chain[b.n_segments + sub0], g.vtx_cap);
+    q.vc1 = min(g.chain[b.n_segments + sub1], g.vtx_cap);
+    q.seg0 = seg0;
+    q.seg1 = seg1;
+    q.sub0 = sub0;
+    q.sub1 = sub1;
+    q.flags = (g.path_flags[p] & 1u) | ((uint32_t)(b.rule ? b.rule[p] : 0) << 8);
+    q.pad[0] = q.pad[1] = q.pad[2] = 0;
+    out[p] = q;
+}
+
+template <bool FLAT, int RULE>
+__device__ __forceinline__ void cover_finish(const Band& B, const MaskDev& m, float* out, float* acc) {
     if (!FLAT) {
         MaskStore st{out, m.offset, (int64_t)m.row_stride, B.y0, m.width};
-        band_scan<kCoverThreads, MaskStore, true>(B, m.width, rule, st);
+        band_scan8<kCoverThreads, RULE>(B, m.width, st);
     } else {
         // page-locked host output: staged in shared memory, then one contiguous span per band
-        band_scan<kCoverThreads>(B, m.width, rule, SmemStore{acc, B.stride});
+        band_scan<kCoverThreads>(B, m.width, RULE, SmemStore{acc, B.stride});
         __syncthreads();
         band_flush<kCoverThreads>(acc, B.stride, B.bh, m.width, out + m.offset + (uint64_t)B.y0 * (uint64_t)m.width);
         __syncthreads();
@@ -340,22 +394,50 @@ __device__ __forceinline__ void cover_range(const GlyphDev& g, const Band& B, ui
     }
 }
 
+// The item a CTA works on, staged in shared memory: the next one is fetched
+// by thread 0 while the block works on the current one.
+struct CoverItem {
+    WorkItem wi;
+    int32_t valid;
+    int32_t pad;
+    MaskDev m;
+    GlyphPath p;
+};
+
+__device__ __forceinline__ void fetch_item(const GlyphDev& g, const WorkItem* items, int n_items, int32_t* queue,
+                                           const GlyphPath* paths, CoverItem& dst) {
+    const int it = atomicAdd(queue, 1);
+    if (it >= n_items) {
+        dst.valid = 0;
+        return;
+    }
+    const WorkItem wi = items[it];
+    dst.wi = wi;
+    dst.m = g.b.masks[wi.path];
+    dst.p = paths[wi.path];
+    dst.valid = 1;
+}
+
 template <bool FLAT>
-__global__ void __launch_bounds__(kCoverThreads, 4) k_glyph_cover(GlyphDev g, const WorkItem* __restrict__ items,
-                                                                 int n_items, int32_t* queue) {
+__global__ void __launch_bounds__(kCoverThreads, 4) k_glyph_cover(GlyphDev g, const GlyphPath* __restrict__ paths,
+                                                                 const WorkItem* __restrict__ items, int n_items,
+                                                                 int32_t* queue) {
     extern __shared__ float4 smg4[];
     float* acc = reinterpret_cast<float*>(smg4);
-    __shared__ int s_item;
+    __shared__ CoverItem s_it[2];
     const BatchDev& b = g.b;
     for (int i = threadIdx.x; i < kGlyphBandFloats / 4; i += kCoverThreads) smg4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (threadIdx.x == 0) fetch_item(g, items, n_items, queue, paths, s_it[0]);
+    __syncthreads();
     int fallbacks = 0;
-    for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(queue, 1);
-        __syncthreads();  // the item is known; the previous item's scan has cleared the band
-        const int it = s_item;
-        if (it >= n_items) break;
-        const WorkItem wi = items[it];
-        const MaskDev m = b.masks[wi.path];
+    for (int cur = 0;; cur ^= 1) {
+        const CoverItem& ci = s_it[cur];
+        if (!ci.valid) break;
+        const WorkItem wi = ci.wi;
+        const MaskDev m = ci.m;
+        const GlyphPath q = ci.p;
+        // the next item's loads overlap this item's work
+        if (threadIdx.x == 0) fetch_item(g, items, n_items, queue, paths, s_it[cur ^ 1]);
         Band B;
         B.acc = acc;
         B.stride = band_stride(m.clip_width);
@@ -364,27 +446,24 @@ __global__ void __launch_bounds__(kCoverThreads, 4) k_glyph_cover(GlyphDev g, co
         B.img_h = m.height;
         B.width_f = (float)m.clip_width;
         B.width_i = m.clip_width;
-        // ranges are clamped to the arrays so malformed offsets cannot read out of bounds
-        const uint32_t sub1 = min(b.path_sub[wi.path + 1], b.n_subpaths);
-        const uint32_t sub0 = min(b.path_sub[wi.path], sub1);
-        const uint32_t seg1 = min(b.sub_off[sub1], b.n_segments);
-        const uint32_t seg0 = min(b.sub_off[sub0], seg1);
-        cover_range(g, B, min(g.chain[seg0], g.vtx_cap), min(g.chain[seg1], g.vtx_cap));
-        cover_range(g, B, min(g.chain[b.n_segments + sub0], g.vtx_cap), min(g.chain[b.n_segments + sub1], g.vtx_cap));
-        if (g.path_flags[wi.path] & 1u) {
+        cover_range(g, B, q.vs0, q.vs1);
+        cover_range(g, B, q.vc0, q.vc1);
+        if (q.flags & 1u) {
             // slots of this path the fixed-point route cannot take: binary64 per band
-            const uint32_t n_seg = seg1 - seg0, n_close = sub1 - sub0;
+            const uint32_t n_seg = q.seg1 - q.seg0, n_close = q.sub1 - q.sub0;
             const double* trm = b.tr ? b.tr + 6ull * wi.path : nullptr;
             for (uint32_t i = threadIdx.x; i < n_seg + n_close; i += kCoverThreads) {
-                const uint32_t j = i < n_seg ? seg0 + i : b.n_segments + sub0 + (i - n_seg);
+                const uint32_t j = i < n_seg ? q.seg0 + i : b.n_segments + q.sub0 + (i - n_seg);
                 if ((g.recs[j].tag >> 30) != REC_SLOW) continue;
                 SegRec rec;
                 SlotCoef coef;
-                band_load(b, B, seg0, n_seg, sub0, i, trm, rec, coef, fallbacks);  // never a fixed-point slot here
+                band_load(b, B, q.seg0, n_seg, q.sub0, i, trm, rec, coef, fallbacks);  // never a fixed-point slot here
             }
         }
         __syncthreads();
-        cover_finish<FLAT>(B, m, b.rule ? b.rule[wi.path] : 0, b.out, acc);
+        if ((q.flags >> 8) & 1u) cover_finish<FLAT, 1>(B, m, b.out, acc);
+        else cover_finish<FLAT, 0>(B, m, b.out, acc);
+        __syncthreads();  // the band is clear and the next item is staged
     }
     if (fallbacks) atomicAdd(&b.counters[1], fallbacks);
 }
@@ -406,6 +485,8 @@ int glyph_cover_occupancy() {
     return blocks;
 }
 
+uint64_t glyph_path_bytes() { return sizeof(GlyphPath); }
+
 // Records and tree walks of every slot.
 cudaError_t launch_glyph_walk(const GlyphDev& g, cudaStream_t st) {
     const uint64_t n = (uint64_t)g.b.n_segments + g.b.n_subpaths;
@@ -418,20 +499,29 @@ cudaError_t launch_glyph_walk(const GlyphDev& g, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// Chain vertices, then the per-path descriptors of the cover items.
 cudaError_t launch_glyph_emit(const GlyphDev& g, cudaStream_t st) {
     const uint64_t n = (uint64_t)g.b.n_segments + g.b.n_subpaths;
-    if (n == 0) return cudaSuccess;
-    k_glyph_emit<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g);
-    return cudaGetLastError();
+    if (n) {
+        k_glyph_emit<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (g.b.n_paths && g.paths) {
+        k_glyph_paths<<<(g.b.n_paths + 255) / 256, 256, 0, st>>>(g, reinterpret_cast<GlyphPath*>(g.paths));
+        return cudaGetLastError();
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_glyph_cover(const GlyphDev& g, const WorkItem* items, int n_items, int32_t* queue, int grid,
                                cudaStream_t st) {
     if (n_items <= 0) return cudaSuccess;
+    const GlyphPath* paths = reinterpret_cast<const GlyphPath*>(g.paths);
     if (g.b.flat_out)
-        k_glyph_cover<true><<<grid, kCoverThreads, kGlyphBandBytes, st>>>(g, items, n_items, queue);
+        k_glyph_cover<true><<<grid, kCoverThreads, kGlyphBandBytes, st>>>(g, paths, items, n_items, queue);
     else
-        k_glyph_cover<false><<<grid, kCoverThreads, kGlyphBandBytes, st>>>(g, items, n_items, queue);
+        k_glyph_cover<false><<<grid, kCoverThreads, kGlyphBandBytes, st>>>(g, paths, items, n_items, queue);
     return cudaGetLastError();
 }
 

@@ -33,10 +33,12 @@ struct GlyphDev {
     uint32_t* path_flags;      // [n_paths] bit 0: the path has slots the fixed-point route cannot take
     int4* vtx;                 // [vtx_cap] chain vertices
     uint32_t vtx_cap;
+    void* paths;               // [n_paths] per-path descriptors of the cover items (glyph_path_bytes() each)
 };
 
 cudaError_t init_glyph_kernels();
 int glyph_cover_occupancy();
+uint64_t glyph_path_bytes();
 cudaError_t launch_glyph_walk(const GlyphDev& g, cudaStream_t st);
 cudaError_t launch_glyph_emit(const GlyphDev& g, cudaStream_t st);
 cudaError_t launch_glyph_cover(const GlyphDev& g, const WorkItem* items, int n_items, int32_t* queue, int grid,
