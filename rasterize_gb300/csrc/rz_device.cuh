@@ -217,27 +217,22 @@ __device__ inline int decide_fp32(int kind, const FlatCoef& c, int d, uint32_t k
     const float td = thr32 * pow2f(4 * d);     // thr * 16^d, exact power-of-two scaling
     const float ms = c.mag * pow2f(2 * d - 40);  // chain error grows like 4^d in w units
     const float e21 = pow2f(-21), e19 = pow2f(-19);
-    float G, E;
-    if (kind == SEG_CUBIC) {
-        const float tu = h * (float)(3u * k + 1u);
-        const float tv = h * (float)(3u * k + 2u);
-        const float wux = fmaf(c.a3x, tu, c.a2x), wvx = fmaf(c.a3x, tv, c.a2x);
-        const float wuy = fmaf(c.a3y, tu, c.a2y), wvy = fmaf(c.a3y, tv, c.a2y);
-        const float gx = fmaxf(wux * wux, wvx * wvx), gy = fmaxf(wuy * wuy, wvy * wvy);
-        G = gx + gy;
-        const float q = qerr * (1.f + tv);
-        const float bx = (fabsf(c.a2x) + fabsf(c.a3x) * tv) * e21 + ms + q;
-        const float by = (fabsf(c.a2y) + fabsf(c.a3y) * tv) * e21 + ms + q;
-        // sqrt(gx) without a square root: gx is the larger square, so its root is the larger |w| (widened by
-        // 2^-22 to cover the rounding of the square and of a correctly rounded root)
-        const float wx = fmaxf(fabsf(wux), fabsf(wvx)) * 1.00000024f, wy = fmaxf(fabsf(wuy), fabsf(wvy)) * 1.00000024f;
-        E = (2.f * wx + bx) * bx + (2.f * wy + by) * by + G * e19;
-    } else {
-        G = c.a2x * c.a2x + c.a2y * c.a2y;
-        const float bx = fabsf(c.a2x) * e21 + ms + qerr;
-        const float by = fabsf(c.a2y) * e21 + ms + qerr;
-        E = (2.f * fabsf(c.a2x) + bx) * bx + (2.f * fabsf(c.a2y) + by) * by + G * e19;
-    }
+    // One formula for cubics and quads (a quad's a3 is 0: u = v and G = |a2|^2, the reference's quad
+    // flatness), so a warp that mixes the two kinds does not diverge here.
+    (void)kind;
+    const float tu = h * (float)(3u * k + 1u);
+    const float tv = h * (float)(3u * k + 2u);
+    const float wux = fmaf(c.a3x, tu, c.a2x), wvx = fmaf(c.a3x, tv, c.a2x);
+    const float wuy = fmaf(c.a3y, tu, c.a2y), wvy = fmaf(c.a3y, tv, c.a2y);
+    const float gx = fmaxf(wux * wux, wvx * wvx), gy = fmaxf(wuy * wuy, wvy * wvy);
+    const float G = gx + gy;
+    const float q = qerr * (1.f + tv);
+    const float bx = (fabsf(c.a2x) + fabsf(c.a3x) * tv) * e21 + ms + q;
+    const float by = (fabsf(c.a2y) + fabsf(c.a3y) * tv) * e21 + ms + q;
+    // sqrt(gx) without a square root: gx is the larger square, so its root is the larger |w| (widened by
+    // 2^-22 to cover the rounding of the square and of a correctly rounded root)
+    const float wx = fmaxf(fabsf(wux), fabsf(wvx)) * 1.00000024f, wy = fmaxf(fabsf(wuy), fabsf(wvy)) * 1.00000024f;
+    const float E = (2.f * wx + bx) * bx + (2.f * wy + by) * by + G * e19;
     if (isfinite(G) && isfinite(E) && isfinite(td)) {
         if (G + E < td) return 1;
         if (G - E >= td) return 0;
