@@ -132,6 +132,7 @@ struct rz_ctx {
     // output encode (sRGB8 RGBA) and its input staging
     DevBuf p_rgba8, p_encode_in;
     DevBuf p_recs;  // slot records of the band kernel
+    DevBuf p_tasks;  // first flatten task of each slot (adaptive subtree tasks)
     // glyph pipeline of the tuner: records, coefficients, chain offsets, tree codes, path flags, vertices, scan scratch
     DevBuf g_recs, g_coef, g_chain, g_code, g_pflags, g_vtx, g_scan, g_paths;
     // scene-tree layers by nesting depth: colour layers and clip masks
@@ -448,7 +449,7 @@ void rz_destroy(rz_ctx* c) {
                       &c->p_paints, &c->p_slots,   &c->p_lines,   &c->p_ecount,  &c->p_estart,  &c->p_ecursor,
                       &c->p_pairs,  &c->p_scan,    &c->p_canvas,  &c->p_leaf,    &c->d_loss,    &c->p_rgba8,
                       &c->p_encode_in, &c->p_recs,  &c->g_recs,    &c->g_coef,    &c->g_chain,   &c->g_code,
-                      &c->g_pflags, &c->g_vtx,     &c->g_scan,    &c->g_paths};
+                      &c->g_pflags, &c->g_vtx,     &c->g_scan,    &c->g_paths,   &c->p_tasks};
     for (DevBuf* b : bufs) b->release();
     for (DevBuf* b : {&c->s_units, &c->s_styles, &c->s_counts, &c->s_off, &c->s_fin, &c->s_tmpk, &c->s_tmpp, &c->s_order, &c->s_nodes, &c->s_pieces, &c->s_joins,
                       &c->s_kind, &c->s_pts})
@@ -1686,7 +1687,54 @@ struct HostScene {
     uint32_t n_slots = 0, n_entries = 0;
     int band_rows = 1, n_bands = 0, max_clip = 1;
     int task_depth = 0;  // flatten tasks per slot = 2^task_depth (2 for large segments)
+    std::vector<uint32_t> task_off;  // or per slot: first task (2^k tasks each), then the total
 };
+
+// Flatten tasks per slot from each segment's root flatness (the reference's
+// formula on the transformed control points): a curve whose tree is about D
+// levels deep gets 2^(D - 3) subtree tasks (at most 1024), so every task walks
+// about 8 leaves however long the curve.  Closing lines and lines get one.
+void adaptive_tasks(HostScene& hs, double flatness) {
+    const double thr = 16.0 * flatness * flatness;
+    hs.task_off.assign((size_t)hs.n_slots + 1, 0);
+    uint32_t acc = 0;
+    for (const rz::FillDev& f : hs.fills) {
+        const uint32_t nseg = f.seg1 - f.seg0, nslot = nseg + (f.sub1 - f.sub0);
+        for (uint32_t i = 0; i < nslot; ++i) {
+            int depth = 0;
+            if (i < nseg) {
+                const uint32_t g = f.seg0 + i;
+                const int kind = hs.kind[g];
+                if (kind == RZ_SEG_QUAD || kind == RZ_SEG_CUBIC) {
+                    const double* p = hs.pts + 8ull * g;
+                    double x[4], y[4];
+                    for (int q = 0; q < 4; ++q) {
+                        x[q] = f.tr[0] * p[2 * q] + f.tr[1] * p[2 * q + 1] + f.tr[2];
+                        y[q] = f.tr[3] * p[2 * q] + f.tr[4] * p[2 * q + 1] + f.tr[5];
+                    }
+                    double fl;
+                    if (kind == RZ_SEG_QUAD) {
+                        const double ux = 2 * x[1] - x[0] - x[2], uy = 2 * y[1] - y[0] - y[2];
+                        fl = ux * ux + uy * uy;
+                    } else {
+                        const double ux = 3 * x[1] - 2 * x[0] - x[3], uy = 3 * y[1] - 2 * y[0] - y[3];
+                        const double vx = 3 * x[2] - x[0] - 2 * x[3], vy = 3 * y[2] - y[0] - 2 * y[3];
+                        fl = std::max(ux * ux, vx * vx) + std::max(uy * uy, vy * vy);
+                    }
+                    int d = 0;
+                    while (d < 22 && std::isfinite(fl) && fl >= thr) {
+                        fl /= 16.0;
+                        ++d;
+                    }
+                    depth = std::min(10, std::max(0, d - 3));
+                }
+            }
+            hs.task_off[f.slot0 + i] = acc;
+            acc += 1u << depth;
+        }
+    }
+    hs.task_off[hs.n_slots] = acc;
+}
 
 int choose_band_rows(int canvas_w, int canvas_h, bool paint_mode) {
     const int stride = rz::band_stride(canvas_w);
@@ -1733,7 +1781,14 @@ rz_status build_lines(rz_ctx* ctx, HostScene& hs, rz::SceneDev& S, Trace& tr, De
                             cudaMemcpyHostToDevice, ctx->stream));
     S.fills = (const rz::FillDev*)ctx->p_fills.p;
     // 1) lines per slot, 2) offsets (one extra element receives the total)
-    const uint64_t ns = rz::slot_tasks(hs.n_slots, hs.task_depth) + 1;
+    if (!hs.task_off.empty()) {
+        RZ_CUDA(ctx->p_tasks.ensure(hs.task_off.size() * 4));
+        RZ_CUDA(cudaMemcpyAsync(ctx->p_tasks.p, hs.task_off.data(), hs.task_off.size() * 4, cudaMemcpyHostToDevice,
+                                ctx->stream));
+        S.task_off = (const uint32_t*)ctx->p_tasks.p;
+        S.n_tasks = hs.task_off.back();
+    }
+    const uint64_t ns = rz::scene_tasks(S) + 1;
     RZ_CUDA(ctx->p_slots.ensure(ns * 4));
     S.slot_count = (uint32_t*)ctx->p_slots.p;
     RZ_CUDA(cudaMemsetAsync(S.slot_count, 0, ns * 4, ctx->stream));
@@ -1744,8 +1799,7 @@ rz_status build_lines(rz_ctx* ctx, HostScene& hs, rz::SceneDev& S, Trace& tr, De
     RZ_CUDA(ctx->p_scan.ensure(rz::scan_temp_words(std::max(ns, ne)) * 4 + 64));
     RZ_CUDA(rz::scan_u32(S.slot_count, ns, (uint32_t*)ctx->p_scan.p, ctx->stream));
     uint32_t n_lines = 0;
-    RZ_CUDA(cudaMemcpyAsync(&n_lines, S.slot_count + rz::slot_tasks(hs.n_slots, hs.task_depth), 4, cudaMemcpyDeviceToHost,
-                            ctx->stream));
+    RZ_CUDA(cudaMemcpyAsync(&n_lines, S.slot_count + (ns - 1), 4, cudaMemcpyDeviceToHost, ctx->stream));
     RZ_CUDA(cudaStreamSynchronize(ctx->stream));
     rz_status st = read_error(ctx);
     if (st) return st;
@@ -1894,10 +1948,10 @@ rz_status mask_pipeline(rz_ctx* ctx, const rz_path* path, const double tr[6], in
                                         path->n_subpaths, psub, 1, hs, fsub);
     if (st) return st;
     hs.band_rows = choose_band_rows((int)width, (int)height, false);
-    hs.task_depth = 4;  // a path this large has long segments: 16 subtree tasks each
     rzhost::Xf t;
     std::memcpy(t.m, tr, sizeof(t.m));
     add_fill(hs, fsub[0], fsub[1], 0, 0, (int)width, (int)height, (int)width - 1, t, rule, -1);
+    adaptive_tasks(hs, flatness);  // a path this large has long segments: subtree tasks by their depth
     RZ_CUDA(ctx->d_out.ensure(width * height * 4 + 16));
     RZ_CUDA(cudaMemsetAsync(ctx->d_out.p, 0, width * height * 4, ctx->stream));
     return run_pipeline(ctx, hs, flatness, (float*)ctx->d_out.p, (int64_t)width, (int)width, (int)height, nullptr,

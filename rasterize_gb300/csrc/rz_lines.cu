@@ -47,8 +47,8 @@ __global__ void __launch_bounds__(kLinesThreads, 4) k_mask_lines(SceneDev S, con
         __syncthreads();
         // the path's lines: its slots are contiguous, slot_count holds their line offsets
         const uint32_t nslot = (f.seg1 - f.seg0) + (f.sub1 - f.sub0);
-        const uint32_t l0 = S.slot_count[slot_tasks(f.slot0, S.task_depth)];
-        const uint32_t l1 = min(S.slot_count[slot_tasks(f.slot0 + nslot, S.task_depth)], S.line_cap);
+        const uint32_t l0 = S.slot_count[task_first(S, f.slot0)];
+        const uint32_t l1 = min(S.slot_count[task_first(S, f.slot0 + nslot)], S.line_cap);
         // anchors are within a few px of the exact ends: a margin of 8 rows keeps every line that reaches the band
         const int32_t ylo = (B.y0 - 8) * 65536, yhi = (B.y0 + B.bh + 8) * 65536;
         for (uint32_t l = l0 + tid; l < l1; l += kLinesThreads) {

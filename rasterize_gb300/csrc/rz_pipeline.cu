@@ -116,9 +116,8 @@ __device__ __forceinline__ int slot_decide(const SceneDev& S, const FillDev& f, 
 // leaf above the task depth belongs to the first task under it.  Returns
 // false on a tree deeper than MAX_DEPTH.
 template <class Emit>
-__device__ bool walk_task(const SceneDev& S, const FillDev& f, const SlotState& st, uint32_t j, int& fallbacks,
-                          Emit& emit) {
-    const int td = S.task_depth;
+__device__ bool walk_task(const SceneDev& S, const FillDev& f, const SlotState& st, uint32_t j, int td,
+                          int& fallbacks, Emit& emit) {
     for (int d = 0; d < td; ++d) {
         const int up = td - d;
         if (slot_decide(S, f, st, d, j >> up, fallbacks)) {
@@ -152,10 +151,30 @@ struct CountLeaves {
 
 // A leaf is one line, or two (the reference's x rules split it) when the
 // slot's coordinates are beyond the 16.16 range.
+// Slot s, subtree index j and subtree depth td of flatten task t.
+__device__ __forceinline__ void task_slot(const SceneDev& S, uint64_t t, uint32_t& s, uint32_t& j, int& td) {
+    if (S.task_off) {
+        uint32_t lo = 0, hi = S.n_slots;  // largest s with task_off[s] <= t (every slot has a task)
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (S.task_off[mid] <= t) lo = mid; else hi = mid;
+        }
+        s = lo;
+        j = (uint32_t)(t - S.task_off[lo]);
+        td = __ffs(S.task_off[lo + 1] - S.task_off[lo]) - 1;
+    } else {
+        s = (uint32_t)(t >> S.task_depth);
+        j = (uint32_t)(t & ((1u << S.task_depth) - 1u));
+        td = S.task_depth;
+    }
+}
+
 __global__ void k_flatten_count(SceneDev S) {
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= slot_tasks(S.n_slots, S.task_depth)) return;
-    const uint32_t s = (uint32_t)(t >> S.task_depth), j = (uint32_t)(t & ((1u << S.task_depth) - 1u));
+    if (t >= scene_tasks(S)) return;
+    uint32_t s, j;
+    int td;
+    task_slot(S, t, s, j, td);
     const FillDev& f = S.fills[fill_of_slot(S, s)];
     SlotState st;
     load_slot(S, f, s, st);
@@ -163,7 +182,7 @@ __global__ void k_flatten_count(SceneDev S) {
     int fallbacks = 0;
     if (st.ok) {
         CountLeaves c;
-        if (!walk_task(S, f, st, j, fallbacks, c)) pset_err(S.err, ERR_DEPTH);
+        if (!walk_task(S, f, st, j, td, fallbacks, c)) pset_err(S.err, ERR_DEPTH);
         n = st.fits ? c.n : 2u * c.n;
     }
     S.slot_count[t] = n;
@@ -275,15 +294,17 @@ struct EmitLines {
 
 __global__ void k_flatten_emit(SceneDev S) {
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= slot_tasks(S.n_slots, S.task_depth)) return;
-    const uint32_t s = (uint32_t)(t >> S.task_depth), j = (uint32_t)(t & ((1u << S.task_depth) - 1u));
+    if (t >= scene_tasks(S)) return;
+    uint32_t s, j;
+    int td;
+    task_slot(S, t, s, j, td);
     const FillDev& f = S.fills[fill_of_slot(S, s)];
     SlotState st;
     load_slot(S, f, s, st);
     if (!st.ok) return;
     int fallbacks = 0;
     EmitLines e{&S, &f, &st, S.slot_count[t]};
-    walk_task(S, f, st, j, fallbacks, e);
+    walk_task(S, f, st, j, td, fallbacks, e);
 }
 
 // Fill owning line l (slot_count holds the line offsets of the flatten tasks).
@@ -292,7 +313,7 @@ __device__ __forceinline__ uint32_t fill_of_line(const SceneDev& S, uint32_t l) 
     while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) >> 1;
         const uint32_t first =
-            S.fills[mid].slot0 < S.n_slots ? S.slot_count[slot_tasks(S.fills[mid].slot0, S.task_depth)] : S.n_lines;
+            S.fills[mid].slot0 < S.n_slots ? S.slot_count[task_first(S, S.fills[mid].slot0)] : S.n_lines;
         if (first <= l) lo = mid; else hi = mid;
     }
     return lo;
@@ -617,14 +638,14 @@ __global__ void __launch_bounds__(kCompThreads) k_composite(SceneDev S, int cov_
 // launchers (declared in rz_api.cu)
 // ---------------------------------------------------------------------------
 cudaError_t launch_flatten_count(const SceneDev& S, cudaStream_t st) {
-    const uint64_t n = slot_tasks(S.n_slots, S.task_depth);
+    const uint64_t n = scene_tasks(S);
     if (n == 0) return cudaSuccess;
     k_flatten_count<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(S);
     return cudaGetLastError();
 }
 
 cudaError_t launch_flatten_emit(const SceneDev& S, cudaStream_t st) {
-    const uint64_t n = slot_tasks(S.n_slots, S.task_depth);
+    const uint64_t n = scene_tasks(S);
     if (n == 0) return cudaSuccess;
     k_flatten_emit<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(S);
     return cudaGetLastError();

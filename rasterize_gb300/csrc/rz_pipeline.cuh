@@ -58,6 +58,8 @@ struct PaintDev {
     float col[kMaxStops][4];
 };
 
+struct SceneDev;
+
 struct SceneDev {
     const uint8_t* kind;
     const double* pts;
@@ -68,7 +70,9 @@ struct SceneDev {
     uint32_t n_slots;
     uint32_t n_segments;
     uint32_t n_subpaths;
-    int32_t task_depth;      // flatten tasks per slot = 2^task_depth
+    int32_t task_depth;      // flatten tasks per slot = 2^task_depth (when task_off is null)
+    const uint32_t* task_off;  // [n_slots + 1] first task of each slot (2^k tasks each), or null
+    uint32_t n_tasks;        // tasks in total when task_off is set
     double thr64;
     float thr32;
     int32_t canvas_w, canvas_h;
@@ -107,5 +111,17 @@ struct DiffDev {
     const float* dl_dimage;
     float* out;          // forward: images; backward: d loss / d ctrl
 };
+
+}  // namespace rz
+
+namespace rz {
+
+// First flatten task of slot `slot`, and the number of tasks of a scene.
+__device__ __forceinline__ uint64_t task_first(const SceneDev& S, uint32_t slot) {
+    return S.task_off ? (uint64_t)S.task_off[slot] : ((uint64_t)slot << S.task_depth);
+}
+__host__ __device__ inline uint64_t scene_tasks(const SceneDev& S) {
+    return S.task_off ? (uint64_t)S.n_tasks : slot_tasks(S.n_slots, S.task_depth);
+}
 
 }  // namespace rz
