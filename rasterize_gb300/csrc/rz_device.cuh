@@ -586,6 +586,25 @@ __device__ __forceinline__ float alpha_from_winding_fix(int rule, int32_t w) {
     return v >= 1.f ? 1.f : (v < 1e-6f ? 0.f : v);
 }
 
+// alpha_from_winding_fix with a rule known at compile time, in integer
+// instructions and one FP32 add: for 0 <= m <= 2^22 the bits 0x3f800000 +
+// 2m are the float 1 + m 2^-22 exactly, so subtracting 1 gives m 2^-22
+// exactly (the same value the conversion route rounds to).  NonZero keeps
+// the 1e-6 cut-off: m 2^-22 < 1e-6 exactly when m <= 4.
+template <int RULE>
+__device__ __forceinline__ float alpha_fix(uint32_t w) {
+    uint32_t m;
+    if (RULE == 1) {
+        const int32_t r = (int32_t)((w + (1u << 22)) & ((1u << 23) - 1u));
+        m = (uint32_t)abs(r - (1 << 22));
+    } else {
+        const uint32_t a = (int32_t)w < 0 ? 0u - w : w;
+        m = min(a, 1u << 22);
+        m = m <= 4u ? 0u : m;
+    }
+    return __int_as_float((int32_t)(0x3f800000u + (m << 1))) - 1.0f;
+}
+
 // The x rules of signed_difference_line (src/rasterize.rs:372-393) on a
 // binary64 line: the part beyond `width` is dropped (a line entirely beyond
 // becomes vertical at width - 0.001), then split_at_zero_x
@@ -690,27 +709,28 @@ __device__ void band_scan(const Band& B, int width, int rule, const Epi& epi) {
     }
 }
 
-// The same row scan with 8 pixels a lane (two 16-byte loads, 256 columns per
-// warp step) for a rule known at compile time (RULE: 0 NonZero, 1 EvenOdd),
-// clearing the words it reads (columns [0, width + 2)).  Bit-identical to
-// band_scan; epi receives 4 alphas at a time.
-template <int THREADS, int RULE, class Epi>
-__device__ void band_scan8(const Band& B, int width, const Epi& epi) {
+// The row scan of a mask band with 8 pixels a lane (two 16-byte loads, 256
+// columns per warp step) for a fill rule known at compile time (RULE: 0
+// NonZero, 1 EvenOdd), clearing the words it reads (columns [0, width + 2))
+// and streaming the alphas to mask rows `out + (y0 + r) * row_stride`.
+// Bit-identical to band_scan with MaskStore.
+template <int THREADS, int RULE>
+__device__ void band_scan8(const Band& B, int width, float* out, int64_t row_stride, int y0) {
     const int lane = threadIdx.x & 31;
     const int span = width + 2;  // stride >= width + 2, a multiple of 16
     for (int r = threadIdx.x >> 5; r < B.bh; r += THREADS / 32) {
         int4* row4 = reinterpret_cast<int4*>(B.acc + r * B.stride);
+        float* o = out + (int64_t)(y0 + r) * row_stride;
+        const bool aligned = (reinterpret_cast<uintptr_t>(o) & 15u) == 0;
         uint32_t carry = 0;  // unsigned: the winding wraps by design
         for (int x0 = 0; x0 < span; x0 += 256) {
             const int x = x0 + 8 * lane;
             int4 v = make_int4(0, 0, 0, 0), u = make_int4(0, 0, 0, 0);
             if (x < span) {
                 v = row4[x >> 2];
+                u = row4[(x >> 2) + 1];  // x + 8 <= stride
                 row4[x >> 2] = make_int4(0, 0, 0, 0);
-                if (x + 4 < span) {
-                    u = row4[(x >> 2) + 1];
-                    row4[(x >> 2) + 1] = make_int4(0, 0, 0, 0);
-                }
+                row4[(x >> 2) + 1] = make_int4(0, 0, 0, 0);
             }
             uint32_t a[8];
             if (x + 8 <= width) {
@@ -735,20 +755,21 @@ __device__ void band_scan8(const Band& B, int width, const Epi& epi) {
             uint32_t incl = a[7];
             #pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
-                const uint32_t o = __shfl_up_sync(0xffffffffu, incl, off);
-                if (lane >= off) incl += o;
+                const uint32_t t = __shfl_up_sync(0xffffffffu, incl, off);
+                if (lane >= off) incl += t;
             }
             const uint32_t base = carry + incl - a[7];
             carry += __shfl_sync(0xffffffffu, incl, 31);
+            float al[8];
             #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                if (x + 4 * h < width) {
-                    const float al[kScanChunk] = {alpha_from_winding_fix(RULE, (int32_t)(base + a[4 * h])),
-                                                  alpha_from_winding_fix(RULE, (int32_t)(base + a[4 * h + 1])),
-                                                  alpha_from_winding_fix(RULE, (int32_t)(base + a[4 * h + 2])),
-                                                  alpha_from_winding_fix(RULE, (int32_t)(base + a[4 * h + 3]))};
-                    epi(r, x + 4 * h, al);
-                }
+            for (int i = 0; i < 8; ++i) al[i] = alpha_fix<RULE>(base + a[i]);
+            if (aligned && x + 8 <= width) {
+                __stcs(reinterpret_cast<float4*>(o + x), make_float4(al[0], al[1], al[2], al[3]));
+                __stcs(reinterpret_cast<float4*>(o + x + 4), make_float4(al[4], al[5], al[6], al[7]));
+            } else if (x < width) {
+                #pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    if (x + i < width) o[x + i] = al[i];
             }
         }
     }

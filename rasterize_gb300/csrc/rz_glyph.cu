@@ -364,8 +364,7 @@ __global__ void __launch_bounds__(256) k_glyph_paths(GlyphDev g, GlyphPath* __re
 template <bool FLAT, int RULE>
 __device__ __forceinline__ void cover_finish(const Band& B, const MaskDev& m, float* out, float* acc) {
     if (!FLAT) {
-        MaskStore st{out, m.offset, (int64_t)m.row_stride, B.y0, m.width};
-        band_scan8<kCoverThreads, RULE>(B, m.width, st);
+        band_scan8<kCoverThreads, RULE>(B, m.width, out + m.offset, (int64_t)m.row_stride, B.y0);
     } else {
         // page-locked host output: staged in shared memory, then one contiguous span per band
         band_scan<kCoverThreads>(B, m.width, RULE, SmemStore{acc, B.stride});
@@ -380,17 +379,40 @@ __device__ __forceinline__ void cover_finish(const Band& B, const MaskDev& m, fl
 
 // Lines of vertex range [v0, v1) that reach the band.  A vertex's row word
 // is the row of its anchor; the FP32 fraction can reach several rows beyond
-// it, so the test uses floor(row + fy).
+// it, so the test uses floor(row + fy).  Each thread takes kLineBatch lines
+// a step and issues all their loads before it uses any.
+#ifndef RZ_COVER_BATCH
+#define RZ_COVER_BATCH 1
+#endif
+#ifndef RZ_COVER_MIN_BLOCKS
+#define RZ_COVER_MIN_BLOCKS 4
+#endif
+constexpr int kLineBatch = RZ_COVER_BATCH;
+
+__device__ __forceinline__ void cover_line(const Band& B, const int4& a, const int4& c) {
+    if (vtx_end(a)) return;
+    const VtxQ va = unpack_vtx(a, 0), vc = unpack_vtx(c, 0);
+    const int ra = va.row + __float2int_rd(va.fy), rc = vc.row + __float2int_rd(vc.fy);
+    if (max(ra, rc) < B.y0 - 1 || min(ra, rc) > B.y0 + B.bh) return;
+    accumulate_vtx(B, unpack_vtx(a, B.y0), unpack_vtx(c, B.y0));
+}
+
 __device__ __forceinline__ void cover_range(const GlyphDev& g, const Band& B, uint32_t v0, uint32_t v1) {
-    const int lo = B.y0 - 1, hi = B.y0 + B.bh;
-    for (uint32_t i = v0 + threadIdx.x; i + 1 < v1; i += kCoverThreads) {
-        const int4 a = g.vtx[i];
-        if (vtx_end(a)) continue;
-        const int4 c = g.vtx[i + 1];
-        const VtxQ va = unpack_vtx(a, 0), vc = unpack_vtx(c, 0);
-        const int ra = va.row + __float2int_rd(va.fy), rc = vc.row + __float2int_rd(vc.fy);
-        if (max(ra, rc) < lo || min(ra, rc) > hi) continue;
-        accumulate_vtx(B, unpack_vtx(a, B.y0), unpack_vtx(c, B.y0));
+    if (v1 <= v0 + 1) return;
+    const uint32_t n = v1 - 1 - v0;  // line i runs from vertex v0 + i to v0 + i + 1
+    for (uint32_t i0 = threadIdx.x; i0 < n; i0 += kCoverThreads * kLineBatch) {
+        int4 a[kLineBatch], c[kLineBatch];
+        #pragma unroll
+        for (int q = 0; q < kLineBatch; ++q) {
+            const uint32_t i = i0 + q * kCoverThreads;
+            if (i < n) {
+                a[q] = g.vtx[v0 + i];
+                c[q] = g.vtx[v0 + i + 1];
+            }
+        }
+        #pragma unroll
+        for (int q = 0; q < kLineBatch; ++q)
+            if (i0 + q * kCoverThreads < n) cover_line(B, a[q], c[q]);
     }
 }
 
@@ -419,7 +441,7 @@ __device__ __forceinline__ void fetch_item(const GlyphDev& g, const WorkItem* it
 }
 
 template <bool FLAT>
-__global__ void __launch_bounds__(kCoverThreads, 4) k_glyph_cover(GlyphDev g, const GlyphPath* __restrict__ paths,
+__global__ void __launch_bounds__(kCoverThreads, RZ_COVER_MIN_BLOCKS) k_glyph_cover(GlyphDev g, const GlyphPath* __restrict__ paths,
                                                                  const WorkItem* __restrict__ items, int n_items,
                                                                  int32_t* queue) {
     extern __shared__ float4 smg4[];
