@@ -679,8 +679,7 @@ cudaError_t glyph_enqueue_flatten(const rz::GlyphDev& g, uint32_t* scan_tmp, uin
 // walk + scan on `st`; the vertex buffer gets an eighth of slack for inputs
 // rewritten between launches (more is reported as ERR_CAPACITY).
 cudaError_t glyph_setup(const rz::BatchDev& b, rz::GlyphDev& g, DevBuf& recs, DevBuf& coefs, DevBuf& chain,
-                        DevBuf& code, DevBuf& pflags, DevBuf& vtx, DevBuf& scan, DevBuf& paths, cudaStream_t st,
-                        bool replay = true) {
+                        DevBuf& code, DevBuf& pflags, DevBuf& vtx, DevBuf& scan, DevBuf& paths, cudaStream_t st) {
     const uint64_t n = (uint64_t)b.n_segments + b.n_subpaths;
     cudaError_t e = recs.ensure(std::max<uint64_t>(n, 1) * sizeof(rz::GlyphRec));
     if (e == cudaSuccess) e = paths.ensure(std::max<uint64_t>(b.n_paths, 1) * rz::glyph_path_bytes());
@@ -713,27 +712,11 @@ cudaError_t glyph_setup(const rz::BatchDev& b, rz::GlyphDev& g, DevBuf& recs, De
     if (e != cudaSuccess) return e;
     g.vtx = (int4*)vtx.p;
     g.vtx_cap = (uint32_t)std::min<uint64_t>(vtx.cap / sizeof(int4), 0xffffffffull);
-    // the sizing pass may have recorded errors (NaN, depth) and re-decisions: a replayed pass (batch plans)
-    // counts them again; a one-shot render keeps them and goes on from the computed offsets
-    return replay ? cudaMemsetAsync(b.err, 0, 32, st) : cudaSuccess;
+    // the sizing pass may have recorded errors (NaN, depth) and re-decisions: the first launch counts them again
+    return cudaMemsetAsync(b.err, 0, 32, st);
 }
 
-// One-shot render of a staged batch (inputs, masks, items built with
-// kGlyphBandFloats) through the glyph pipeline on the context's stream: one
-// sizing synchronisation, then emit and cover.
-rz_status run_glyph(rz_ctx* ctx, rz::BatchDev b, uint32_t n_paths, const Items& items) {
-    const int n = (int)items.items.size();
-    if (n == 0) return RZ_OK;
-    b.n_paths = n_paths;
-    rz::GlyphDev g{};
-    RZ_CUDA(glyph_setup(b, g, ctx->g_recs, ctx->g_coef, ctx->g_chain, ctx->g_code, ctx->g_pflags, ctx->g_vtx,
-                        ctx->g_scan, ctx->g_paths, ctx->stream, false));
-    RZ_CUDA(rz::launch_glyph_emit(g, ctx->stream));
-    int32_t* queue = (int32_t*)ctx->d_ctrl.p + 8;
-    RZ_CUDA(cudaMemsetAsync(queue, 0, 4, ctx->stream));
-    RZ_CUDA(rz::launch_glyph_cover(g, (const rz::WorkItem*)ctx->d_items.p, n, queue, glyph_grid(ctx, n), ctx->stream));
-    return RZ_OK;
-}
+
 
 // Fills of a batch from host copies of its offsets, rules and transforms.
 uint32_t lines_fills(const std::vector<rz::MaskDev>& masks, const uint32_t* sub_off, const uint32_t* path_sub,
@@ -1068,20 +1051,22 @@ rz_status render_single(rz_ctx* ctx, const rz_path* path, const double tr[6], in
     masks[0].row_stride = (int32_t)width;
     masks[0].clip_width = (int32_t)(iter_semantics ? width : width - 1);
     Items items;
-    const bool glyph = use_glyph_pipeline();
-    build_items(masks, false, items, ctx->tune_rows_cap, glyph ? rz::kGlyphBandFloats : 0);
+    build_items(masks, false, items);
     st = stage_plan(ctx, masks, items, b);
     if (st) return st;
     RZ_CUDA(ctx->d_out.ensure(width * height * 4 + 16));
     b.out = (float*)ctx->d_out.p;
     set_thresholds(b, flatness);
-    st = glyph ? run_glyph(ctx, b, 1, items) : run_bands(ctx, b, items, false);
+    st = run_bands(ctx, b, items, false);
     if (st) return st;
     return RZ_OK;
 }
 
 }  // namespace
 
+#ifndef RZ_PIPELINE_MIN
+#define RZ_PIPELINE_MIN 2000000
+#endif
 namespace {
 rz_status mask_pipeline(rz_ctx* ctx, const rz_path* path, const double tr[6], int32_t rule, double flatness,
                         uint64_t width, uint64_t height);
@@ -1093,7 +1078,7 @@ bool use_pipeline(const rz_path* path, uint64_t width, uint64_t height) {
     if (!path) return false;
     const int rows = band_rows((int)width - 1, (int)height);
     const uint64_t bands = (height + rows - 1) / rows;
-    return bands * ((uint64_t)path->n_segments + path->n_subpaths) > 2000000ull;
+    return bands * ((uint64_t)path->n_segments + path->n_subpaths) > (uint64_t)RZ_PIPELINE_MIN;
 }
 }  // namespace
 

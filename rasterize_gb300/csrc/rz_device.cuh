@@ -25,7 +25,10 @@ namespace rz {
 
 enum : int { SEG_LINE = 0, SEG_QUAD = 1, SEG_CUBIC = 2, SEG_ARC = 3 };
 enum : int { ERR_NAN = 1, ERR_DEPTH = 5, ERR_ARC = 6, ERR_CAPACITY = 7 };
-constexpr int MAX_DEPTH = 22;  // 3k+2 < 2^24 keeps the node parameter exact in FP32
+constexpr int MAX_DEPTH = 22;
+#ifndef RZ_ANCHOR_PX
+#define RZ_ANCHOR_PX 2
+#endif  // 3k+2 < 2^24 keeps the node parameter exact in FP32
 
 // binary64 without contraction: the reference's Rust code never fuses a*b+c
 __device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
@@ -972,13 +975,14 @@ __device__ inline void make_record(const FixSeg& s, const double (&sx)[4], const
     r.kind = (int16_t)s.kind;
     float c1x, c1y, c2x, c2y, c3x, c3y;
     rec_coefs(r, s.kind, c1x, c1y, c2x, c2y, c3x, c3y);
-    // Anchor level: sub-curves over 2^-a of the parameter span stay below ~2 px,
-    // so the FP32 remainder keeps ~1e-7 px.  Lines need no anchors (t is 0 or 1).
-    // a <= 9 keeps the integer evaluation below 2^62.
+    // Anchor level: sub-curves over 2^-a of the parameter span stay below
+    // RZ_ANCHOR_PX px, so the FP32 remainder keeps ~RZ_ANCHOR_PX x 1e-7 px.
+    // Lines need no anchors (t is 0 or 1).  a <= 9 keeps the integer
+    // evaluation below 2^62.
     const float ext = fmaxf(fabsf(c1x) + fabsf(c2x) + fabsf(c3x), fabsf(c1y) + fabsf(c2y) + fabsf(c3y));
     int a = 0;
     if (s.kind != SEG_LINE) {
-        while (a < 9 && ext * pow2f(-a) > 2.f) ++a;
+        while (a < 9 && ext * pow2f(-a) > (float)RZ_ANCHOR_PX) ++a;
     }
     r.mag = (float)mx * FIX_ONE_INV;
     r.anchor = (int8_t)a;
