@@ -383,7 +383,7 @@ constexpr int kShortLine = 32;
 // Walks its rows like signed_difference_line (src/rasterize.rs:405-469); the
 // row crossings are interpolated from the exact fixed-point heights, so their
 // x error stays below ~kShortLine * 2^-23 px.
-__device__ inline void accumulate_piece(const Band& B, int xb, float x0, int32_t q0, float x1, int32_t q1) {
+__device__ __forceinline__ void accumulate_piece(const Band& B, int xb, float x0, int32_t q0, float x1, int32_t q1) {
     if (q0 == q1) return;  // no signed coverage (the reference skips |dy| < EPSILON)
     int dir = 1;
     if (q0 > q1) {
@@ -529,6 +529,22 @@ struct VtxQ {
 // Line between two vertices.  Short lines away from the x rules stay in FP32
 // with exact fixed-point heights; the rest take the binary64 route, which
 // quantises the same vertex to the same height.
+// The FP32 route of accumulate_vtx alone: false when the line needs the
+// binary64 route (long, or near the x rules' columns), which the caller then
+// takes outside its hot loop.
+__device__ __forceinline__ bool accumulate_vtx_short(const Band& B, const VtxQ& a, const VtxQ& b) {
+    const int dc = b.col - a.col, dr = b.row - a.row;
+    if (abs(dc) >= kShortLine || abs(dr) >= kShortLine) return false;
+    if (a.row < -kShortLine - 4 || a.row > B.bh + kShortLine + 4) return true;  // wholly above or below
+    const float x0 = a.fx, x1 = (float)dc + b.fx;
+    const float xlo = (float)a.col + fminf(x0, x1), xhi = (float)a.col + fmaxf(x0, x1);
+    if (!(xlo > 0.01f && xhi < B.width_f - 0.01f)) return false;
+    const int32_t q0 = a.row * COV_ONE + __float2int_rn(a.fy * COV_ONE_F);
+    const int32_t q1 = b.row * COV_ONE + __float2int_rn(b.fy * COV_ONE_F);
+    accumulate_piece(B, a.col, x0, q0, x1, q1);
+    return true;
+}
+
 __device__ __forceinline__ void accumulate_vtx(const Band& B, const VtxQ& a, const VtxQ& b) {
     const int dc = b.col - a.col, dr = b.row - a.row;
     if (abs(dc) < kShortLine && abs(dr) < kShortLine) {

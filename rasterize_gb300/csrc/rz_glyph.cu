@@ -389,17 +389,21 @@ __device__ __forceinline__ void cover_finish(const Band& B, const MaskDev& m, fl
 #endif
 constexpr int kLineBatch = RZ_COVER_BATCH;
 
-__device__ __forceinline__ void cover_line(const Band& B, const int4& a, const int4& c) {
-    if (vtx_end(a)) return;
+// Line from packed vertices a -> c: false when it needs the binary64 route.
+__device__ __forceinline__ bool cover_line(const Band& B, const int4& a, const int4& c) {
+    if (vtx_end(a)) return true;
     const VtxQ va = unpack_vtx(a, 0), vc = unpack_vtx(c, 0);
     const int ra = va.row + __float2int_rd(va.fy), rc = vc.row + __float2int_rd(vc.fy);
-    if (max(ra, rc) < B.y0 - 1 || min(ra, rc) > B.y0 + B.bh) return;
-    accumulate_vtx(B, unpack_vtx(a, B.y0), unpack_vtx(c, B.y0));
+    if (max(ra, rc) < B.y0 - 1 || min(ra, rc) > B.y0 + B.bh) return true;
+    return accumulate_vtx_short(B, unpack_vtx(a, B.y0), unpack_vtx(c, B.y0));
 }
 
+// The lines of vertex range [v0, v1); those that need the binary64 route are
+// taken after the loop, so the loop holds no call and its loads can batch.
 __device__ __forceinline__ void cover_range(const GlyphDev& g, const Band& B, uint32_t v0, uint32_t v1) {
     if (v1 <= v0 + 1) return;
     const uint32_t n = v1 - 1 - v0;  // line i runs from vertex v0 + i to v0 + i + 1
+    uint32_t slow = 0;               // bit q: line i0 + q * kCoverThreads of the current step
     for (uint32_t i0 = threadIdx.x; i0 < n; i0 += kCoverThreads * kLineBatch) {
         int4 a[kLineBatch], c[kLineBatch];
         #pragma unroll
@@ -412,7 +416,15 @@ __device__ __forceinline__ void cover_range(const GlyphDev& g, const Band& B, ui
         }
         #pragma unroll
         for (int q = 0; q < kLineBatch; ++q)
-            if (i0 + q * kCoverThreads < n) cover_line(B, a[q], c[q]);
+            if (i0 + q * kCoverThreads < n && !cover_line(B, a[q], c[q])) slow |= 1u << q;
+        if (slow) {
+            for (int q = 0; q < kLineBatch; ++q) {
+                if (!((slow >> q) & 1u)) continue;
+                const uint32_t i = i0 + q * kCoverThreads;
+                accumulate_vtx(B, unpack_vtx(g.vtx[v0 + i], B.y0), unpack_vtx(g.vtx[v0 + i + 1], B.y0));
+            }
+            slow = 0;
+        }
     }
 }
 

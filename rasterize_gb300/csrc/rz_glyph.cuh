@@ -9,7 +9,10 @@
 namespace rz {
 
 // Shared-memory band of one k_glyph_cover CTA (4 CTAs per SM).
-constexpr int kGlyphBandBytes = 48 * 1024;
+#ifndef RZ_GLYPH_BAND_KB
+#define RZ_GLYPH_BAND_KB 48
+#endif
+constexpr int kGlyphBandBytes = RZ_GLYPH_BAND_KB * 1024;
 constexpr int kGlyphBandFloats = kGlyphBandBytes / 4;
 
 // Per-slot record kept between the passes.
