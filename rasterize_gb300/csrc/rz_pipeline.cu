@@ -204,15 +204,6 @@ __device__ __forceinline__ bool line_rows(const SceneDev& S, const FillDev& f, i
     return r0 < r1;
 }
 
-// Lines per (fill, band) of one local-frame line.
-__device__ __forceinline__ void count_bands(const SceneDev& S, const FillDev& f, int4 l) {
-    int r0, r1;
-    if (!line_rows(S, f, l.y, l.w, r0, r1)) return;
-    const int b0 = (r0 + f.row0) / S.band_rows, b1 = (r1 - 1 + f.row0) / S.band_rows;
-    for (int b = max(b0, f.band0); b <= min(b1, f.band0 + f.nbands - 1); ++b)
-        atomicAdd(&S.entry_count[f.entry0 + (b - f.band0)], 1u);
-}
-
 __device__ __forceinline__ int32_t fix_add(int32_t a, float d) { return a + __float2int_rn(d * 65536.0f); }
 
 // A line end point: exact 16.16 anchor plus FP32 remainder (px).
@@ -234,9 +225,29 @@ struct EmitLines {
         S->lines[2ull * out] = a;
         S->lines[2ull * out + 1] = b;
         ++out;
-        if (S->entry_count)
-            count_bands(*S, *f, make_int4(fix_add(a.x, __int_as_float(a.z)), fix_add(a.y, __int_as_float(a.w)),
-                                          fix_add(b.x, __int_as_float(b.z)), fix_add(b.y, __int_as_float(b.w))));
+        if (S->entry_count) {
+            // consecutive lines of a walk mostly fall in one band: their counts are added once per run
+            int r0, r1;
+            if (!line_rows(*S, *f, fix_add(a.y, __int_as_float(a.w)), fix_add(b.y, __int_as_float(b.w)), r0, r1))
+                return;
+            const int b0 = max((r0 + f->row0) / S->band_rows, f->band0);
+            const int b1 = min((r1 - 1 + f->row0) / S->band_rows, f->band0 + f->nbands - 1);
+            if (b0 == b1) {
+                const uint32_t e = f->entry0 + (b0 - f->band0);
+                if (e != pend_e) {
+                    flush();
+                    pend_e = e;
+                }
+                ++pend_n;
+            } else {
+                for (int bb = b0; bb <= b1; ++bb) atomicAdd(&S->entry_count[f->entry0 + (bb - f->band0)], 1u);
+            }
+        }
+    }
+    uint32_t pend_e = 0xffffffffu, pend_n = 0;  // a run of lines counted in one (fill, band) entry
+    __device__ void flush() {
+        if (pend_n) atomicAdd(&S->entry_count[pend_e], pend_n);
+        pend_n = 0;
     }
     __device__ void operator()(int d, uint32_t k) {
         const uint32_t first = out;
@@ -305,6 +316,7 @@ __global__ void k_flatten_emit(SceneDev S) {
     int fallbacks = 0;
     EmitLines e{&S, &f, &st, S.slot_count[t]};
     walk_task(S, f, st, j, td, fallbacks, e);
+    e.flush();
 }
 
 // Fill owning line l (slot_count holds the line offsets of the flatten tasks).
@@ -319,18 +331,38 @@ __device__ __forceinline__ uint32_t fill_of_line(const SceneDev& S, uint32_t l) 
     return lo;
 }
 
+// Consecutive lines mostly fall in one (fill, band) entry: the lanes of a
+// warp with the same single entry take their list slots with one atomic.
 __global__ void k_bin_scatter(SceneDev S) {
     const uint32_t l = blockIdx.x * blockDim.x + threadIdx.x;
-    if (l >= S.n_lines) return;
-    const FillDev& f = S.fills[fill_of_line(S, l)];
-    const int4 a = S.lines[2ull * l], b = S.lines[2ull * l + 1];
-    const int32_t ya = fix_add(a.y, __int_as_float(a.w)), yb = fix_add(b.y, __int_as_float(b.w));
-    int r0, r1;
-    if (!line_rows(S, f, ya, yb, r0, r1)) return;
-    const int b0 = (r0 + f.row0) / S.band_rows, b1 = (r1 - 1 + f.row0) / S.band_rows;
-    for (int b = max(b0, f.band0); b <= min(b1, f.band0 + f.nbands - 1); ++b) {
-        const uint32_t e = f.entry0 + (b - f.band0);
-        S.pairs[S.entry_start[e] + atomicAdd(&S.entry_cursor[e], 1u)] = l;
+    const int lane = threadIdx.x & 31;
+    int b0 = 0, b1 = -1;
+    const FillDev* f = nullptr;
+    if (l < S.n_lines) {
+        f = &S.fills[fill_of_line(S, l)];
+        const int4 a = S.lines[2ull * l], b = S.lines[2ull * l + 1];
+        const int32_t ya = fix_add(a.y, __int_as_float(a.w)), yb = fix_add(b.y, __int_as_float(b.w));
+        int r0, r1;
+        if (line_rows(S, *f, ya, yb, r0, r1)) {
+            b0 = max((r0 + f->row0) / S.band_rows, f->band0);
+            b1 = min((r1 - 1 + f->row0) / S.band_rows, f->band0 + f->nbands - 1);
+        }
+    }
+    // one entry: aggregated per warp; none: a key no other lane has; several: one atomic per entry below
+    const long long key = b0 == b1 ? (long long)(f->entry0 + (b0 - f->band0)) : -1 - (long long)threadIdx.x;
+    const unsigned same = __match_any_sync(0xffffffffu, key);
+    if (b0 == b1) {
+        const uint32_t e = (uint32_t)key;
+        const int leader = __ffs(same) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&S.entry_cursor[e], (uint32_t)__popc(same));
+        base = __shfl_sync(same, base, leader);
+        S.pairs[S.entry_start[e] + base + __popc(same & ((1u << lane) - 1u))] = l;
+    } else {
+        for (int bb = b0; bb <= b1; ++bb) {
+            const uint32_t e = f->entry0 + (bb - f->band0);
+            S.pairs[S.entry_start[e] + atomicAdd(&S.entry_cursor[e], 1u)] = l;
+        }
     }
 }
 
@@ -653,7 +685,7 @@ cudaError_t launch_flatten_emit(const SceneDev& S, cudaStream_t st) {
 
 cudaError_t launch_bin_scatter(const SceneDev& S, cudaStream_t st) {
     if (S.n_lines == 0) return cudaSuccess;
-    k_bin_scatter<<<(S.n_lines + 255) / 256, 256, 0, st>>>(S);
+    k_bin_scatter<<<(S.n_lines + 255) / 256, 256, 0, st>>>(S);  // whole warps: every lane reaches the match
     return cudaGetLastError();
 }
 
