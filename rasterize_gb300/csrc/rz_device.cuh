@@ -413,39 +413,39 @@ __device__ __forceinline__ void accumulate_piece(const Band& B, int xb, float x0
     }
 }
 
-// A long piece: x absolute in binary64, y band-relative (not clipped: rows
-// are clamped to the band in 64-bit fixed point, COV_ONE per row).  The x of
-// the row boundaries is stepped in 64-bit fixed point (2^-40 px: after 16384
-// rows the accumulated step error is below 1e-8 px), so the rows cost integer
-// instructions; the set-up is one binary64 division and a few products.
-// Every row is handed to the FP32 distribution relative to its own column.
+// A long piece: x absolute in binary64, y band-relative in fixed point
+// (already clipped to the band's rows, so q fits in 32 bits), with its slope
+// dxdy in px per row.  The x of the row boundaries is stepped in 64-bit fixed
+// point (2^-40 px: after 16384 rows the accumulated step error is below
+// 1e-8 px), so the rows cost integer instructions.  Every row is handed to the
+// FP32 distribution relative to its own integer column.
 constexpr int kLongFrac = 40;
-static __device__ __noinline__ void accumulate_piece_long(const Band& B, double x0, double y0, double x1, double y1) {
-    long long q0 = __double2ll_rn(y0 * 4194304.0), q1 = __double2ll_rn(y1 * 4194304.0);
-    if (q0 == q1) return;  // no signed coverage
+static __device__ __noinline__ void accumulate_piece_long(const Band& B, double x0, int32_t q0, double x1,
+                                                          int32_t q1, double dxdy) {
+    if (q0 == q1) return;
     int dir = 1;
     if (q0 > q1) {
         const double t = x0; x0 = x1; x1 = t;
-        const long long u = q0; q0 = q1; q1 = u;
+        const int32_t u = q0; q0 = q1; q1 = u;
         dir = -1;
     }
     const int row_lo = max(0, -B.y0);
     const int row_hi = min(B.bh, B.img_h - B.y0);
-    const long long qa_all = max(q0, (long long)row_lo << COV_SHIFT);
-    const long long qb_all = min(q1, (long long)row_hi << COV_SHIFT);
+    const int32_t qa_all = max(q0, row_lo << COV_SHIFT);
+    const int32_t qb_all = min(q1, row_hi << COV_SHIFT);
     if (!(qa_all < qb_all)) return;
-    const double dxq = (x1 - x0) / (double)(q1 - q0);
-    const int r0 = (int)(qa_all >> COV_SHIFT);
-    const int r1 = (int)((qb_all + COV_ONE - 1) >> COV_SHIFT);
+    const double dxq = dxdy * (1.0 / 4194304.0);  // px per fixed-point unit of height (exact scaling)
+    const int r0 = qa_all >> COV_SHIFT;
+    const int r1 = (qb_all + COV_ONE - 1) >> COV_SHIFT;
     const double one = 1099511627776.0;  // 2^40
     // x at the top of row r0 + 1 and the step per row, in units of 2^-40 px
-    long long xb_fix = __double2ll_rn((x0 + (double)(((long long)(r0 + 1) << COV_SHIFT) - q0) * dxq) * one);
-    const long long step = __double2ll_rn(dxq * (double)COV_ONE * one);
+    long long xb_fix = __double2ll_rn((x0 + (double)(((r0 + 1) << COV_SHIFT) - q0) * dxq) * one);
+    const long long step = __double2ll_rn(dxdy * one);
     const long long x1_fix = __double2ll_rn(x1 * one);
     long long xa_fix = qa_all == q0 ? __double2ll_rn(x0 * one) : __double2ll_rn((x0 + (double)(qa_all - q0) * dxq) * one);
     for (int r = r0; r < r1; ++r) {
-        const long long qa = max(qa_all, (long long)r << COV_SHIFT);
-        const long long qb = min(qb_all, (long long)(r + 1) << COV_SHIFT);
+        const int32_t qa = max(qa_all, r << COV_SHIFT);
+        const int32_t qb = min(qb_all, (r + 1) << COV_SHIFT);
         const long long xn_fix = qb == q1 ? x1_fix
                                           : (qb == qb_all ? __double2ll_rn((x0 + (double)(qb - q0) * dxq) * one) : xb_fix);
         if (qa < qb) {
@@ -454,7 +454,7 @@ static __device__ __noinline__ void accumulate_piece_long(const Band& B, double 
             const long long base = col << kLongFrac;
             const float fa = (float)(xa_fix - base) * (1.0f / 1099511627776.0f);
             const float fn = (float)(xn_fix - base) * (1.0f / 1099511627776.0f);
-            accumulate_row(B, r, (int)col, fa, fn, dir * (int)(qb - qa));
+            accumulate_row(B, r, (int)col, fa, fn, dir * (qb - qa));
         }
         xa_fix = xn_fix;
         xb_fix += step;
@@ -462,22 +462,29 @@ static __device__ __noinline__ void accumulate_piece_long(const Band& B, double 
 }
 
 // Piece of a line after the x rules, in binary64 (x absolute, y relative to
-// the band).  Short pieces (at most kShortLine px each way) are quantised
-// (COV_ONE per row) and distributed in FP32; long ones take the fixed-point
-// row stepping.  Either way the rows are clamped to the band exactly, so
-// nothing is clipped in binary64.
+// the band).  Clips it to the band's rows (a pure geometric clip, so the area
+// inside is unchanged; one binary64 division for the slope, which the long
+// route reuses), quantises y (COV_ONE per row) and dispatches it: short pieces
+// to the FP32 distribution, long ones to the fixed-point row stepping.
 __device__ inline void accumulate_piece64(const Band& B, double x0, double y0, double x1, double y1) {
     if (y0 == y1) return;
     const double lo = fmax(-1.0, -(double)B.y0 - 1.0);
     const double hi = (double)min(B.bh, B.img_h - B.y0) + 1.0;
     const double ymin = fmin(y0, y1), ymax = fmax(y0, y1);
     if (ymax <= lo || ymin >= hi) return;
-    if (fabs(x1 - x0) <= (double)kShortLine && ymax - ymin <= (double)kShortLine) {
-        const int32_t q0 = __double2int_rn(y0 * 4194304.0), q1 = __double2int_rn(y1 * 4194304.0);
+    const double dxdy = (x1 - x0) / (y1 - y0);
+    if (ymin < lo || ymax > hi) {
+        if (y0 < lo) { x0 = x0 + (lo - y0) * dxdy; y0 = lo; }
+        else if (y0 > hi) { x0 = x0 + (hi - y0) * dxdy; y0 = hi; }
+        if (y1 < lo) { x1 = x0 + (lo - y0) * dxdy; y1 = lo; }
+        else if (y1 > hi) { x1 = x0 + (hi - y0) * dxdy; y1 = hi; }
+    }
+    const int32_t q0 = __double2int_rn(y0 * 4194304.0), q1 = __double2int_rn(y1 * 4194304.0);
+    if (fabs(x1 - x0) <= (double)kShortLine && abs(q1 - q0) <= (kShortLine << COV_SHIFT)) {
         const int xb = (int)floor(fmin(x0, x1));
         accumulate_piece(B, xb, (float)(x0 - xb), q0, (float)(x1 - xb), q1);
     } else {
-        accumulate_piece_long(B, x0, y0, x1, y1);
+        accumulate_piece_long(B, x0, q0, x1, q1, dxdy);
     }
 }
 
