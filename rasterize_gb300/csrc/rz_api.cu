@@ -1721,13 +1721,26 @@ void adaptive_tasks(HostScene& hs, double flatness) {
     hs.task_off[hs.n_slots] = acc;
 }
 
-int choose_band_rows(int canvas_w, int canvas_h, bool paint_mode) {
+int choose_band_rows(int canvas_w, int canvas_h, bool paint_mode, int num_sms) {
     const int stride = rz::band_stride(canvas_w);
     const int per_row = 4 * stride + (paint_mode ? 16 * canvas_w : 0);
-    // coverage only: tall bands (one CTA per SM) amortise a long line's binary64 set-up per band
-    int rows = std::max(1, (paint_mode ? 96 * 1024 : 200 * 1024) / per_row);
-    rows = std::min(rows, 64);
-    return std::max(1, std::min(rows, std::max(canvas_h, 1)));
+    // coverage only: tall bands (one CTA per SM) amortise a line's per-band set-up; with paint, two CTAs per SM
+    const int rmax = std::max(1, std::min(std::min((paint_mode ? 96 * 1024 : 208 * 1024) / per_row, 64),
+                                          std::max(canvas_h, 1)));
+    const int64_t slots = (int64_t)std::max(num_sms, 1) * (paint_mode ? 2 : 1);
+    // the band kernel runs in waves of `slots` bands: the height whose waves cost least, counting each band's
+    // rows plus a fixed share for the lines that cross its edges
+    int best = rmax;
+    int64_t best_cost = INT64_MAX;
+    for (int r = rmax; r >= std::max(1, rmax / 2); --r) {
+        const int64_t bands = (canvas_h + r - 1) / r;
+        const int64_t cost = (bands + slots - 1) / slots * (r + 4);
+        if (cost < best_cost) {
+            best_cost = cost;
+            best = r;
+        }
+    }
+    return best;
 }
 
 // Adds one fill (its view, transform, paint, slots and bands) to `hs`.
@@ -1932,7 +1945,7 @@ rz_status mask_pipeline(rz_ctx* ctx, const rz_path* path, const double tr[6], in
     rz_status st = stage_scene_segments(ctx, path->seg_kind, path->seg_pts, path->n_segments, path->subpath_off,
                                         path->n_subpaths, psub, 1, hs, fsub);
     if (st) return st;
-    hs.band_rows = choose_band_rows((int)width, (int)height, false);
+    hs.band_rows = choose_band_rows((int)width, (int)height, false, ctx->num_sms);
     rzhost::Xf t;
     std::memcpy(t.m, tr, sizeof(t.m));
     add_fill(hs, fsub[0], fsub[1], 0, 0, (int)width, (int)height, (int)width - 1, t, rule, -1);
@@ -2001,7 +2014,7 @@ rz_status rz_fill(rz_ctx* ctx, const rz_path* path, const double tr[6], int32_t 
                               path->n_subpaths, psub, 1, hs, fsub);
     if (st) return st;
     const int W = (int)shape.width, H = (int)shape.height;
-    hs.band_rows = choose_band_rows(W, H, true);
+    hs.band_rows = choose_band_rows(W, H, true, ctx->num_sms);
     rzhost::Xf t;
     std::memcpy(t.m, tr, sizeof(t.m));
     rzhost::Box bb0{};
@@ -2056,7 +2069,7 @@ static rz_status render_scene_impl(rz_ctx* ctx, const rz_scene* scene, double fl
     if (st) return st;
     tr.mark("stage_segments");
     const int W = (int)width, H = (int)height;
-    hs.band_rows = choose_band_rows(W, H, true);
+    hs.band_rows = choose_band_rows(W, H, true, ctx->num_sms);
     const rzhost::Xf id{{1, 0, 0, 0, 1, 0}};
     // tight bounding boxes of every fill (transformed; untransformed only for
     // BoundingBox paint units), computed in parallel
@@ -2313,7 +2326,7 @@ rz_status rz_render_scene_tree(rz_ctx* ctx, const rz_scene* scene, const rz_scen
     P.hs.sub_off = T.base.sub_off;
     P.hs.n_seg = T.base.n_seg;
     P.hs.n_sub = T.base.n_sub;
-    P.hs.band_rows = choose_band_rows(W, H, true);
+    P.hs.band_rows = choose_band_rows(W, H, true, ctx->num_sms);
     PlanLayer R;
     R.w = W;
     R.h = H;

@@ -736,10 +736,69 @@ __device__ void band_scan(const Band& B, int width, int rule, const Epi& epi) {
 // NonZero, 1 EvenOdd), clearing the words it reads (columns [0, width + 2))
 // and streaming the alphas to mask rows `out + (y0 + r) * row_stride`.
 // Bit-identical to band_scan with MaskStore.
+// Rows of at most 128 columns are scanned several to a warp: L lanes (a power
+// of two, 8 columns each) per row, the warp scan segmented to L lanes.  The
+// sums are the same integers in the same wrap-around arithmetic.
+template <int THREADS, int RULE>
+__device__ void band_scan8_narrow(const Band& B, int width, float* out, int64_t row_stride, int y0) {
+    const int lane = threadIdx.x & 31;
+    const int span = width + 2;  // <= 128
+    const int lg = span <= 8 ? 0 : 32 - __clz((span + 7) / 8 - 1);  // log2 L
+    const int L = 1 << lg;
+    const int sl = lane & (L - 1);
+    const int per_warp = 32 >> lg;
+    const int x = 8 * sl;
+    for (int r0 = (threadIdx.x >> 5) * per_warp; r0 < B.bh; r0 += (THREADS / 32) * per_warp) {
+        const int r = r0 + (lane >> lg);
+        const bool live = r < B.bh;
+        int4 v = make_int4(0, 0, 0, 0), u = make_int4(0, 0, 0, 0);
+        if (live && x < span) {
+            int4* row4 = reinterpret_cast<int4*>(B.acc + r * B.stride);
+            v = row4[x >> 2];
+            u = row4[(x >> 2) + 1];  // x + 8 <= stride
+            row4[x >> 2] = make_int4(0, 0, 0, 0);
+            row4[(x >> 2) + 1] = make_int4(0, 0, 0, 0);
+        }
+        const uint32_t w8[8] = {(uint32_t)v.x, (uint32_t)v.y, (uint32_t)v.z, (uint32_t)v.w,
+                                (uint32_t)u.x, (uint32_t)u.y, (uint32_t)u.z, (uint32_t)u.w};
+        uint32_t a[8];
+        uint32_t run = 0;
+        #pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            run += x + i < width ? w8[i] : 0u;
+            a[i] = run;
+        }
+        uint32_t incl = a[7];
+        for (int off = 1; off < L; off <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, off, L);
+            if (sl >= off) incl += t;
+        }
+        const uint32_t base = incl - a[7];
+        if (live && x < width) {
+            float* o = out + (int64_t)(y0 + r) * row_stride;
+            float al[8];
+            #pragma unroll
+            for (int i = 0; i < 8; ++i) al[i] = alpha_fix<RULE>(base + a[i]);
+            if ((reinterpret_cast<uintptr_t>(o) & 15u) == 0 && x + 8 <= width) {
+                __stcs(reinterpret_cast<float4*>(o + x), make_float4(al[0], al[1], al[2], al[3]));
+                __stcs(reinterpret_cast<float4*>(o + x + 4), make_float4(al[4], al[5], al[6], al[7]));
+            } else {
+                #pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    if (x + i < width) o[x + i] = al[i];
+            }
+        }
+    }
+}
+
 template <int THREADS, int RULE>
 __device__ void band_scan8(const Band& B, int width, float* out, int64_t row_stride, int y0) {
     const int lane = threadIdx.x & 31;
     const int span = width + 2;  // stride >= width + 2, a multiple of 16
+    if (span <= 128) {
+        band_scan8_narrow<THREADS, RULE>(B, width, out, row_stride, y0);
+        return;
+    }
     for (int r = threadIdx.x >> 5; r < B.bh; r += THREADS / 32) {
         int4* row4 = reinterpret_cast<int4*>(B.acc + r * B.stride);
         float* o = out + (int64_t)(y0 + r) * row_stride;

@@ -105,9 +105,13 @@ __device__ void load_slot(const SceneDev& S, const FillDev& f, uint32_t s, SlotS
     }
 }
 
+// FITS: the slot is inside the 16.16 range (a fixed-point record), known at
+// compile time so a walk over records keeps nothing of the binary64 segment live.
+template <int FITS>  // 1 record, 0 binary64 segment, -1 either (st.fits)
 __device__ __forceinline__ int slot_decide(const SceneDev& S, const FillDev& f, const SlotState& st, int d, uint32_t k,
                                            int& fallbacks) {
-    if (st.fits) return decide_node(st.r, st.c, st.qerr, d, k, S.thr32, S.thr64, S.pts, f.tr, fallbacks);
+    if (FITS == 1 || (FITS < 0 && st.fits))
+        return decide_node(st.r, st.c, st.qerr, d, k, S.thr32, S.thr64, S.pts, f.tr, fallbacks);
     const FlatCoef c = flat_coef(st.g);
     return node_is_leaf(st.g, c, d, k, S.thr64, S.thr32, fallbacks);
 }
@@ -115,12 +119,12 @@ __device__ __forceinline__ int slot_decide(const SceneDev& S, const FillDev& f, 
 // Leaves of task j of the slot's tree, in order; `emit(d, k)` per leaf.  A
 // leaf above the task depth belongs to the first task under it.  Returns
 // false on a tree deeper than MAX_DEPTH.
-template <class Emit>
+template <int FITS = -1, class Emit>
 __device__ bool walk_task(const SceneDev& S, const FillDev& f, const SlotState& st, uint32_t j, int td,
                           int& fallbacks, Emit& emit) {
     for (int d = 0; d < td; ++d) {
         const int up = td - d;
-        if (slot_decide(S, f, st, d, j >> up, fallbacks)) {
+        if (slot_decide<FITS>(S, f, st, d, j >> up, fallbacks)) {
             if ((j & ((1u << up) - 1u)) == 0u) emit(d, j >> up);
             return true;
         }
@@ -128,7 +132,7 @@ __device__ bool walk_task(const SceneDev& S, const FillDev& f, const SlotState& 
     int d = td;
     uint32_t k = j;
     for (;;) {
-        if (!slot_decide(S, f, st, d, k, fallbacks)) {
+        if (!slot_decide<FITS>(S, f, st, d, k, fallbacks)) {
             if (d >= MAX_DEPTH) return false;
             ++d;
             k <<= 1;
@@ -211,117 +215,197 @@ __device__ __forceinline__ int4 end_point(int32_t ax, int32_t ay, float dx, floa
     return make_int4(ax, ay, __float_as_int(dx), __float_as_int(dy));
 }
 
-struct EmitLines {
-    const SceneDev* S;
-    const FillDev* f;
-    const SlotState* st;
-    uint32_t out;
-    __device__ void write(int4 a, int4 b) {
-        if (out >= S->line_cap) {  // the geometry changed since the buffer was sized: report, never overrun
-            pset_err(S->err, ERR_CAPACITY);
-            ++out;
-            return;
-        }
-        S->lines[2ull * out] = a;
-        S->lines[2ull * out + 1] = b;
-        ++out;
-        if (S->entry_count) {
-            // consecutive lines of a walk mostly fall in one band: their counts are added once per run
-            int r0, r1;
-            if (!line_rows(*S, *f, fix_add(a.y, __int_as_float(a.w)), fix_add(b.y, __int_as_float(b.w)), r0, r1))
-                return;
-            const int b0 = max((r0 + f->row0) / S->band_rows, f->band0);
-            const int b1 = min((r1 - 1 + f->row0) / S->band_rows, f->band0 + f->nbands - 1);
-            if (b0 == b1) {
-                const uint32_t e = f->entry0 + (b0 - f->band0);
-                if (e != pend_e) {
-                    flush();
-                    pend_e = e;
-                }
-                ++pend_n;
-            } else {
-                for (int bb = b0; bb <= b1; ++bb) atomicAdd(&S->entry_count[f->entry0 + (bb - f->band0)], 1u);
+// A leaf of a segment beyond the 16.16 range: the reference's x rules
+// (src/rasterize.rs:372-393) and a pure y clip in binary64, then anchors +
+// remainders.  Up to two lines (e[0], e[1]) and (e[2], e[3]); returns how many
+// slots the leaf takes (2), unused ones hold a degenerate line (never binned).
+static __device__ __noinline__ int emit_big_leaf(const Seg64 g, int d, uint32_t k, int clip_width, int height,
+                                                  int4 (&e)[4]) {
+    const VertexCoef v = vertex_coef(g);
+    double x0, y0, x1, y1;
+    vertex_big(v, k, d, 0.0, x0, y0);
+    vertex_big(v, k + 1u, d, 0.0, x1, y1);
+    double px[2][2], py[2][2];
+    const int np = clip_line_x64((double)clip_width, x0, y0, x1, y1, px, py);
+    #pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        e[2 * i] = e[2 * i + 1] = make_int4(0, 0, 0, 0);
+        if (i < np && clip_y64(-1.0, (double)height + 1.0, px[i], py[i])) {
+            int32_t a, b2, c, f;
+            if (d2fix(px[i][0], a) & d2fix(py[i][0], b2) & d2fix(px[i][1], c) & d2fix(py[i][1], f)) {
+                const double u = 1.0 / 65536.0;
+                e[2 * i] = end_point(a, b2, (float)(px[i][0] - a * u), (float)(py[i][0] - b2 * u));
+                e[2 * i + 1] = end_point(c, f, (float)(px[i][1] - c * u), (float)(py[i][1] - f * u));
             }
         }
     }
+    return np;
+}
+
+// The lines of a walk, written from line offset `out` on, with their
+// per-(fill, band) counts.  Holds copies of what it needs, so nothing of the
+// kernel's parameters or the slot state has to live in local memory.
+template <bool FITS>
+struct EmitLines {
+    int4* lines;
+    uint2* leaf;
+    uint32_t* entry_count;
+    int32_t* err;
+    uint32_t line_cap;
+    int band_rows, row0, height, clip_width, band0, nbands;
+    uint32_t entry0;
+    uint32_t out;
+    uint32_t src;
+    const SlotState& st;
+    uint32_t* hist = nullptr;  // the block's counts of entries [hist_e0, hist_e0 + n) in shared memory, or null
+    uint32_t hist_e0 = 0;
     uint32_t pend_e = 0xffffffffu, pend_n = 0;  // a run of lines counted in one (fill, band) entry
-    __device__ void flush() {
-        if (pend_n) atomicAdd(&S->entry_count[pend_e], pend_n);
+
+    __device__ __forceinline__ EmitLines(const SceneDev& S, const FillDev& f, const SlotState& st, uint32_t first)
+        : lines(S.lines), leaf(S.leaf), entry_count(S.entry_count), err(S.err), line_cap(S.line_cap),
+          band_rows(S.band_rows), row0(f.row0), height(f.height), clip_width(f.clip_width), band0(f.band0),
+          nbands(f.nbands), entry0(f.entry0), out(first), src(st.src), st(st) {}
+
+    __device__ __forceinline__ void flush() {
+        if (pend_n) atomicAdd(&entry_count[pend_e], pend_n);
         pend_n = 0;
     }
-    __device__ void operator()(int d, uint32_t k) {
+    __device__ __forceinline__ void count(int4 a, int4 b) {
+        const int32_t ya = fix_add(a.y, __int_as_float(a.w)), yb = fix_add(b.y, __int_as_float(b.w));
+        const int32_t ylo = min(ya, yb), yhi = max(ya, yb);
+        if (ylo == yhi && !leaf) return;  // line_rows: no signed coverage
+        const int r0 = max((ylo - 1) >> 16, 0);
+        const int r1 = min((yhi + 1 + 65535) >> 16, height);
+        if (r0 >= r1) return;
+        const int b0 = max((r0 + row0) / band_rows, band0);
+        const int b1 = min((r1 - 1 + row0) / band_rows, band0 + nbands - 1);
+        if (hist) {
+            for (int bb = b0; bb <= b1; ++bb) atomicAdd(&hist[entry0 + (bb - band0) - hist_e0], 1u);
+            return;
+        }
+        if (b0 == b1) {
+            // consecutive lines of a walk mostly fall in one band: their counts are added once per run
+            const uint32_t e = entry0 + (b0 - band0);
+            if (e != pend_e) {
+                flush();
+                pend_e = e;
+            }
+            ++pend_n;
+        } else {
+            for (int bb = b0; bb <= b1; ++bb) atomicAdd(&entry_count[entry0 + (bb - band0)], 1u);
+        }
+    }
+    __device__ __forceinline__ void write(int4 a, int4 b, bool binned) {
+        if (out >= line_cap) {  // the geometry changed since the buffer was sized: report, never overrun
+            if (binned) atomicCAS(err, 0, ERR_CAPACITY);
+            ++out;
+            return;
+        }
+        lines[2ull * out] = a;
+        lines[2ull * out + 1] = b;
+        ++out;
+        if (binned && entry_count) count(a, b);
+    }
+    __device__ __forceinline__ void operator()(int d, uint32_t k) {
         const uint32_t first = out;
-        emit(d, k);
-        if (S->leaf) {
-            const uint2 code = make_uint2(st->src, ((uint32_t)d << 27) | k);
-            for (uint32_t i = first; i < out && i < S->line_cap; ++i) S->leaf[i] = code;
+        if (FITS) {
+            // integer pixel of the vertex as the 16.16 anchor, its fraction as the remainder
+            const uint32_t t0 = k << (MAX_DEPTH - d), t1 = (k + 1u) << (MAX_DEPTH - d);
+            const VtxQ a = t0 == prev_t ? prev : rec_vtx(st.r, k, d, 0);
+            const VtxQ b = rec_vtx(st.r, k + 1u, d, 0);
+            prev_t = t1;
+            prev = b;
+            write(end_point(a.col << 16, a.row << 16, a.fx, a.fy), end_point(b.col << 16, b.row << 16, b.fx, b.fy),
+                  true);
+        } else {
+            int4 e[4];
+            const int np = emit_big_leaf(st.g, d, k, clip_width, height, e);
+            write(e[0], e[1], np > 0);
+            write(e[2], e[3], np > 1);
+        }
+        if (leaf) {
+            const uint2 code = make_uint2(src, ((uint32_t)d << 27) | k);
+            for (uint32_t i = first; i < out && i < line_cap; ++i) leaf[i] = code;
         }
     }
     // the last leaf's end vertex, as t * 2^MAX_DEPTH: the next leaf of the walk starts there
     uint32_t prev_t = 0xffffffffu;
     VtxQ prev;
-    __device__ void emit(int d, uint32_t k) {
-        if (st->fits) {
-            // integer pixel of the vertex as the 16.16 anchor, its fraction as the remainder
-            const uint32_t t0 = k << (MAX_DEPTH - d), t1 = (k + 1u) << (MAX_DEPTH - d);
-            const VtxQ a = t0 == prev_t ? prev : rec_vtx(st->r, k, d, 0);
-            const VtxQ b = rec_vtx(st->r, k + 1u, d, 0);
-            prev_t = t1;
-            prev = b;
-            write(end_point(a.col << 16, a.row << 16, a.fx, a.fy), end_point(b.col << 16, b.row << 16, b.fx, b.fy));
-        } else {
-            // beyond the 16.16 range: the reference's x rules (src/rasterize.rs:372-393)
-            // and a pure y clip in binary64, then anchors + remainders
-            const Seg64& g = st->g;
-            const VertexCoef v = vertex_coef(g);
-            double x0, y0, x1, y1;
-            vertex_big(v, k, d, 0.0, x0, y0);
-            vertex_big(v, k + 1u, d, 0.0, x1, y1);
-            double px[2][2], py[2][2];
-            const int np = clip_line_x64((double)f->clip_width, x0, y0, x1, y1, px, py);
-            for (int i = 0; i < 2; ++i) {
-                int4 e0 = make_int4(0, 0, 0, 0), e1 = make_int4(0, 0, 0, 0);
-                if (i < np && clip_y64(-1.0, (double)f->height + 1.0, px[i], py[i])) {
-                    int32_t a, b2, c, e;
-                    if (d2fix(px[i][0], a) & d2fix(py[i][0], b2) & d2fix(px[i][1], c) & d2fix(py[i][1], e)) {
-                        const double u = 1.0 / 65536.0;
-                        e0 = end_point(a, b2, (float)(px[i][0] - a * u), (float)(py[i][0] - b2 * u));
-                        e1 = end_point(c, e, (float)(px[i][1] - c * u), (float)(py[i][1] - e * u));
-                    }
-                }
-                if (i < np) {
-                    write(e0, e1);
-                } else if (out < S->line_cap) {
-                    S->lines[2ull * out] = e0;  // unused slot: a degenerate line, never binned
-                    S->lines[2ull * out + 1] = e1;
-                    ++out;
-                } else {
-                    ++out;
-                }
-            }
-        }
-    }
 };
 
-__global__ void k_flatten_emit(SceneDev S) {
-    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= scene_tasks(S)) return;
-    uint32_t s, j;
-    int td;
-    task_slot(S, t, s, j, td);
-    const FillDev& f = S.fills[fill_of_slot(S, s)];
+// A flatten task of a slot beyond the 16.16 range, out of line so the record
+// walk keeps no binary64 state (the scene by value: the copy is made on this
+// rare path only).
+static __device__ __noinline__ void emit_task_big(const SceneDev S, uint32_t fill, uint32_t s, uint32_t j, int td,
+                                                  uint32_t first) {
+    const FillDev& f = S.fills[fill];
     SlotState st;
     load_slot(S, f, s, st);
-    if (!st.ok) return;
     int fallbacks = 0;
-    EmitLines e{&S, &f, &st, S.slot_count[t]};
-    walk_task(S, f, st, j, td, fallbacks, e);
+    EmitLines<false> e(S, f, st, first);
+    walk_task<0>(S, f, st, j, td, fallbacks, e);
     e.flush();
 }
 
-// Fill owning line l (slot_count holds the line offsets of the flatten tasks).
-__device__ __forceinline__ uint32_t fill_of_line(const SceneDev& S, uint32_t l) {
-    uint32_t lo = 0, hi = S.n_fills;
+// Entries (fill, band) a block of flatten tasks or of lines can reach when
+// its fills' entries span at most kHistEntries: counted in shared memory and
+// added to the global counters once per block.  Every line of a walk lands in
+// a few neighbouring bands, and one global atomic per line and band would
+// serialise on the few cache lines that hold a fill's counters.
+constexpr int kHistEntries = 2048;
+constexpr int kEmitThreads = 128;
+
+__global__ void __launch_bounds__(kEmitThreads) k_flatten_emit(SceneDev S) {
+    __shared__ uint32_t s_hist[kHistEntries];
+    __shared__ uint32_t s_e0, s_n;
+    const uint64_t nt = scene_tasks(S);
+    const uint64_t t0 = (uint64_t)blockIdx.x * kEmitThreads;
+    const uint64_t t = t0 + threadIdx.x;
+    if (threadIdx.x == 0) {
+        uint32_t sa, sb, j;
+        int td;
+        task_slot(S, t0, sa, j, td);
+        task_slot(S, min(t0 + kEmitThreads, nt) - 1, sb, j, td);
+        const FillDev& fa = S.fills[fill_of_slot(S, sa)];
+        const FillDev& fb = S.fills[fill_of_slot(S, sb)];
+        const uint32_t e1 = fb.entry0 + (uint32_t)fb.nbands;
+        s_e0 = fa.entry0;
+        s_n = S.entry_count && e1 - fa.entry0 <= (uint32_t)kHistEntries ? e1 - fa.entry0 : 0u;
+    }
+    __syncthreads();
+    const uint32_t hn = s_n, he0 = s_e0;
+    for (uint32_t i = threadIdx.x; i < hn; i += kEmitThreads) s_hist[i] = 0u;
+    __syncthreads();
+    if (t < nt) {
+        uint32_t s, j;
+        int td;
+        task_slot(S, t, s, j, td);
+        const uint32_t fill = fill_of_slot(S, s);
+        const FillDev& f = S.fills[fill];
+        SlotState st;
+        load_slot(S, f, s, st);
+        if (st.ok && !st.fits) {
+            emit_task_big(S, fill, s, j, td, S.slot_count[t]);
+        } else if (st.ok) {
+            int fallbacks = 0;
+            EmitLines<true> e(S, f, st, S.slot_count[t]);
+            if (hn) {
+                e.hist = s_hist;
+                e.hist_e0 = he0;
+            }
+            walk_task<1>(S, f, st, j, td, fallbacks, e);
+            e.flush();
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < hn; i += kEmitThreads)
+        if (s_hist[i]) atomicAdd(&S.entry_count[he0 + i], s_hist[i]);
+}
+
+// Fill owning line l among fills [lo, hi) (slot_count holds the line offsets
+// of the flatten tasks).
+__device__ __forceinline__ uint32_t fill_of_line(const SceneDev& S, uint32_t l, uint32_t lo = 0, uint32_t hi = 0) {
+    if (hi == 0) hi = S.n_fills;
     while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) >> 1;
         const uint32_t first =
@@ -331,22 +415,30 @@ __device__ __forceinline__ uint32_t fill_of_line(const SceneDev& S, uint32_t l) 
     return lo;
 }
 
-// Consecutive lines mostly fall in one (fill, band) entry: the lanes of a
-// warp with the same single entry take their list slots with one atomic.
-__global__ void k_bin_scatter(SceneDev S) {
-    const uint32_t l = blockIdx.x * blockDim.x + threadIdx.x;
+// Bands [b0, b1] of the fill's bands that line l reaches (b0 > b1: none).
+__device__ __forceinline__ void line_bands(const SceneDev& S, const FillDev& f, uint32_t l, int& b0, int& b1) {
+    b0 = 0;
+    b1 = -1;
+    const int4 a = S.lines[2ull * l], b = S.lines[2ull * l + 1];
+    const int32_t ya = fix_add(a.y, __int_as_float(a.w)), yb = fix_add(b.y, __int_as_float(b.w));
+    int r0, r1;
+    if (line_rows(S, f, ya, yb, r0, r1)) {
+        b0 = max((r0 + f.row0) / S.band_rows, f.band0);
+        b1 = min((r1 - 1 + f.row0) / S.band_rows, f.band0 + f.nbands - 1);
+    }
+}
+
+// Line l into its (fill, band) lists with global atomics; called by all 32
+// lanes of a warp (l >= n_lines: no line).  Consecutive lines mostly fall in
+// one entry: the lanes with the same single entry take their slots with one
+// atomic.
+__device__ void bin_line_global(const SceneDev& S, uint32_t l) {
     const int lane = threadIdx.x & 31;
     int b0 = 0, b1 = -1;
     const FillDev* f = nullptr;
     if (l < S.n_lines) {
         f = &S.fills[fill_of_line(S, l)];
-        const int4 a = S.lines[2ull * l], b = S.lines[2ull * l + 1];
-        const int32_t ya = fix_add(a.y, __int_as_float(a.w)), yb = fix_add(b.y, __int_as_float(b.w));
-        int r0, r1;
-        if (line_rows(S, *f, ya, yb, r0, r1)) {
-            b0 = max((r0 + f->row0) / S.band_rows, f->band0);
-            b1 = min((r1 - 1 + f->row0) / S.band_rows, f->band0 + f->nbands - 1);
-        }
+        line_bands(S, *f, l, b0, b1);
     }
     // one entry: aggregated per warp; none: a key no other lane has; several: one atomic per entry below
     const long long key = b0 == b1 ? (long long)(f->entry0 + (b0 - f->band0)) : -1 - (long long)threadIdx.x;
@@ -362,6 +454,59 @@ __global__ void k_bin_scatter(SceneDev S) {
         for (int bb = b0; bb <= b1; ++bb) {
             const uint32_t e = f->entry0 + (bb - f->band0);
             S.pairs[S.entry_start[e] + atomicAdd(&S.entry_cursor[e], 1u)] = l;
+        }
+    }
+}
+
+// A block takes kBinLines consecutive lines.  When their fills' entries fit
+// the shared histogram: count per entry in shared memory, reserve each
+// entry's slots with one global atomic, then place the lines with shared
+// atomics (the order inside a list is free: coverage sums are exact).
+constexpr int kBinThreads = 256;
+constexpr int kBinLines = 4 * kBinThreads;
+
+__global__ void __launch_bounds__(kBinThreads) k_bin_scatter(SceneDev S) {
+    __shared__ uint32_t s_cnt[kHistEntries];
+    __shared__ uint32_t s_base[kHistEntries];
+    __shared__ uint32_t s_e0, s_n, s_fa, s_fb;
+    const uint32_t l0 = blockIdx.x * kBinLines;
+    const uint32_t l1 = min(l0 + kBinLines, S.n_lines);
+    if (threadIdx.x == 0) {
+        const uint32_t fa = fill_of_line(S, l0), fb = fill_of_line(S, l1 - 1);
+        const uint32_t e0 = S.fills[fa].entry0, e1 = S.fills[fb].entry0 + (uint32_t)S.fills[fb].nbands;
+        s_e0 = e0;
+        s_n = e1 - e0 <= (uint32_t)kHistEntries ? e1 - e0 : 0u;
+        s_fa = fa;
+        s_fb = fb + 1;
+    }
+    __syncthreads();
+    const uint32_t n = s_n, e0 = s_e0, fa = s_fa, fb = s_fb;
+    if (n == 0) {
+        for (uint32_t l = l0 + threadIdx.x; l < l0 + kBinLines; l += kBinThreads) bin_line_global(S, l < l1 ? l : S.n_lines);
+        return;
+    }
+    for (uint32_t i = threadIdx.x; i < n; i += kBinThreads) s_cnt[i] = 0u;
+    __syncthreads();
+    for (uint32_t l = l0 + threadIdx.x; l < l1; l += kBinThreads) {
+        const FillDev& f = S.fills[fill_of_line(S, l, fa, fb)];
+        int b0, b1;
+        line_bands(S, f, l, b0, b1);
+        for (int bb = b0; bb <= b1; ++bb) atomicAdd(&s_cnt[f.entry0 + (bb - f.band0) - e0], 1u);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += kBinThreads) {
+        const uint32_t c = s_cnt[i];
+        if (c) s_base[i] = S.entry_start[e0 + i] + atomicAdd(&S.entry_cursor[e0 + i], c);
+        s_cnt[i] = 0u;
+    }
+    __syncthreads();
+    for (uint32_t l = l0 + threadIdx.x; l < l1; l += kBinThreads) {
+        const FillDev& f = S.fills[fill_of_line(S, l, fa, fb)];
+        int b0, b1;
+        line_bands(S, f, l, b0, b1);
+        for (int bb = b0; bb <= b1; ++bb) {
+            const uint32_t i = f.entry0 + (bb - f.band0) - e0;
+            S.pairs[s_base[i] + atomicAdd(&s_cnt[i], 1u)] = l;
         }
     }
 }
@@ -547,7 +692,6 @@ __device__ float4 paint_at(const PaintDev& p, float px, float py) {
 // Composite
 // ---------------------------------------------------------------------------
 
-constexpr int kCompThreads = 256;
 
 struct BlendEpi {
     float4* rgba;        // band colour, canvas_w per row
@@ -587,9 +731,21 @@ struct AlphaEpi {  // coverage-only fills write the mask
 };
 
 // smem: coverage band (band_rows x cov_stride words) | RGBA band (band_rows x canvas_w float4)
-__global__ void __launch_bounds__(kCompThreads) k_composite(SceneDev S, int cov_stride) {
+// The binary64 route of accumulate_vtx for line l.
+static __device__ __noinline__ void composite_slow_line(const SceneDev& S, const Band& B, uint32_t l) {
+    const VtxQ a = line_vtx(S.lines[2ull * l], B.y0), b = line_vtx(S.lines[2ull * l + 1], B.y0);
+    accumulate_line64(B, (double)a.col + (double)a.fx, (double)a.row + (double)a.fy, (double)b.col + (double)b.fx,
+                      (double)b.row + (double)b.fy);
+}
+
+// THREADS: 512 for masks (one CTA per SM), 256 with paint (two CTAs per SM,
+// so one CTA blends while the other accumulates).
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) k_composite(SceneDev S, int cov_stride) {
     extern __shared__ float4 sm4[];
     __shared__ PaintDev s_paint;
+    __shared__ uint32_t s_slow[THREADS / 32][64];  // per warp: at most 31 queued + 32 new
+    const int lane = threadIdx.x & 31;
     float* cov = reinterpret_cast<float*>(sm4);
     const bool paint_mode = S.paints != nullptr;
     float4* rgba = reinterpret_cast<float4*>(cov + S.band_rows * cov_stride);
@@ -598,7 +754,7 @@ __global__ void __launch_bounds__(kCompThreads) k_composite(SceneDev S, int cov_
     const int rows = min(S.band_rows, S.canvas_h - row_base);
     if (rows <= 0) return;
     if (paint_mode) {
-        for (int i = threadIdx.x; i < rows * S.canvas_w; i += kCompThreads) {
+        for (int i = threadIdx.x; i < rows * S.canvas_w; i += THREADS) {
             const int r = i / S.canvas_w, x = i - r * S.canvas_w;
             float4 v;
             if (S.load_canvas) {
@@ -630,24 +786,44 @@ __global__ void __launch_bounds__(kCompThreads) k_composite(SceneDev S, int cov_
             // the fill's paint record in shared memory: read by every covered pixel
             const uint32_t* src = reinterpret_cast<const uint32_t*>(S.paints + f.paint);
             uint32_t* dst = reinterpret_cast<uint32_t*>(&s_paint);
-            for (int i = threadIdx.x; i < (int)(sizeof(PaintDev) / 4); i += kCompThreads) dst[i] = src[i];
+            for (int i = threadIdx.x; i < (int)(sizeof(PaintDev) / 4); i += THREADS) dst[i] = src[i];
         }
         const int n4 = (rows * B.stride) >> 2;
-        for (int i = threadIdx.x; i < n4; i += kCompThreads) sm4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int i = threadIdx.x; i < n4; i += THREADS) sm4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         __syncthreads();
         const uint32_t start = S.entry_start[e];
-        for (uint32_t j = threadIdx.x; j < n; j += kCompThreads) {
-            const uint32_t l = S.pairs[start + j];
-            const int4 a = S.lines[2ull * l], b = S.lines[2ull * l + 1];
-            accumulate_vtx(B, line_vtx(a, B.y0), line_vtx(b, B.y0));
+        // Lines that need the binary64 route (long, or at the x rules) are queued per warp and taken 32 at a
+        // time, so the slow route runs with full warps instead of a few lanes of every step.
+        uint32_t* q = s_slow[threadIdx.x >> 5];
+        int nq = 0;
+        for (uint32_t j0 = threadIdx.x & ~31u; j0 < n; j0 += THREADS) {
+            const uint32_t j = j0 + lane;
+            uint32_t l = 0;
+            bool slow = false;
+            if (j < n) {
+                l = S.pairs[start + j];
+                const int4 a = S.lines[2ull * l], b = S.lines[2ull * l + 1];
+                slow = !accumulate_vtx_short(B, line_vtx(a, B.y0), line_vtx(b, B.y0));
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, slow);
+            if (slow) q[nq + __popc(m & ((1u << lane) - 1u))] = l;
+            nq += __popc(m);
+            if (nq >= 32) {
+                __syncwarp();
+                nq -= 32;
+                composite_slow_line(S, B, q[nq + lane]);
+                __syncwarp();
+            }
         }
+        __syncwarp();
+        if (lane < nq) composite_slow_line(S, B, q[lane]);
         __syncthreads();
         if (paint_mode) {
             BlendEpi epi{rgba, S.canvas_w, f.col0, B.y0, f.width, &s_paint};
-            band_scan<kCompThreads>(B, f.width, f.rule, epi);
+            band_scan<THREADS>(B, f.width, f.rule, epi);
         } else {
             AlphaEpi epi{S.canvas, S.canvas_stride, row_base, f.col0, f.width};
-            band_scan<kCompThreads>(B, f.width, f.rule, epi);
+            band_scan<THREADS>(B, f.width, f.rule, epi);
         }
     }
     if (paint_mode) {
@@ -655,10 +831,10 @@ __global__ void __launch_bounds__(kCompThreads) k_composite(SceneDev S, int cov_
         if (S.rgba8) {
             // fused output encode: From<LinColor> for RGBA per pixel, 4 bytes out instead of 16
             uint32_t* o = S.rgba8 + (int64_t)row_base * S.canvas_w;
-            for (int i = threadIdx.x; i < rows * S.canvas_w; i += kCompThreads)
+            for (int i = threadIdx.x; i < rows * S.canvas_w; i += THREADS)
                 __stcs(o + i, encode_lin_rgba8(rgba[i]));
         } else {
-            for (int i = threadIdx.x; i < rows * S.canvas_w; i += kCompThreads) {
+            for (int i = threadIdx.x; i < rows * S.canvas_w; i += THREADS) {
                 const int r = i / S.canvas_w, x = i - r * S.canvas_w;
                 reinterpret_cast<float4*>(S.canvas)[(int64_t)(row_base + r) * S.canvas_stride + x] = rgba[i];
             }
@@ -679,13 +855,13 @@ cudaError_t launch_flatten_count(const SceneDev& S, cudaStream_t st) {
 cudaError_t launch_flatten_emit(const SceneDev& S, cudaStream_t st) {
     const uint64_t n = scene_tasks(S);
     if (n == 0) return cudaSuccess;
-    k_flatten_emit<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(S);
+    k_flatten_emit<<<(unsigned)((n + kEmitThreads - 1) / kEmitThreads), kEmitThreads, 0, st>>>(S);
     return cudaGetLastError();
 }
 
 cudaError_t launch_bin_scatter(const SceneDev& S, cudaStream_t st) {
     if (S.n_lines == 0) return cudaSuccess;
-    k_bin_scatter<<<(S.n_lines + 255) / 256, 256, 0, st>>>(S);  // whole warps: every lane reaches the match
+    k_bin_scatter<<<(S.n_lines + kBinLines - 1) / kBinLines, kBinThreads, 0, st>>>(S);
     return cudaGetLastError();
 }
 
@@ -696,18 +872,20 @@ int composite_smem_bytes(int canvas_w, int band_rows, int max_clip_width, bool p
     return 4 * band_rows * stride + (paint_mode ? 16 * band_rows * canvas_w : 0);
 }
 
-// The shared-memory attribute is per device: the largest size set so far on
-// each device (contexts on several GPUs, host threads calling at once).
+// The shared-memory attribute is per device and kernel: the largest size set
+// so far on each device (contexts on several GPUs, host threads calling at once).
 constexpr int kMaxAttrDevices = 64;
-static std::atomic<int> g_composite_smem[kMaxAttrDevices];
+static std::atomic<int> g_composite_smem[2][kMaxAttrDevices];
 
-cudaError_t launch_composite(const SceneDev& S, int cov_stride, int smem, cudaStream_t st) {
+template <int THREADS>
+static cudaError_t launch_composite_t(const SceneDev& S, int cov_stride, int smem, cudaStream_t st,
+                                      std::atomic<int>* attr) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    std::atomic<int>* configured = dev >= 0 && dev < kMaxAttrDevices ? &g_composite_smem[dev] : nullptr;
+    std::atomic<int>* configured = dev >= 0 && dev < kMaxAttrDevices ? &attr[dev] : nullptr;
     if (!configured || smem > configured->load()) {
-        e = cudaFuncSetAttribute(k_composite, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        e = cudaFuncSetAttribute(k_composite<THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
         if (configured) {
             int cur = configured->load();
@@ -715,8 +893,13 @@ cudaError_t launch_composite(const SceneDev& S, int cov_stride, int smem, cudaSt
             }
         }
     }
-    k_composite<<<S.n_bands, kCompThreads, smem, st>>>(S, cov_stride);
+    k_composite<THREADS><<<S.n_bands, THREADS, smem, st>>>(S, cov_stride);
     return cudaGetLastError();
+}
+
+cudaError_t launch_composite(const SceneDev& S, int cov_stride, int smem, cudaStream_t st) {
+    if (S.paints) return launch_composite_t<256>(S, cov_stride, smem, st, g_composite_smem[0]);
+    return launch_composite_t<512>(S, cov_stride, smem, st, g_composite_smem[1]);
 }
 
 }  // namespace rz
