@@ -513,8 +513,12 @@ rz_status stage_host(rz_ctx* ctx, const uint8_t* kind, const double* pts, uint32
     const bool has_arc = n_seg && std::memchr(kind, RZ_SEG_ARC, n_seg) != nullptr;
     ctx->expanded = has_arc;
     if (has_arc) {
+        auto pfor = [](int64_t n, const auto& fn) {
+            if (n > 1) parallel_each(n, fn);
+            else if (n == 1) fn(0);
+        };
         if (!rzhost::expand_batch(kind, pts, sub_off, path_sub, n_paths, ctx->x_kind, ctx->x_pts, ctx->x_sub,
-                                  ctx->x_psub, ctx->x_segmap, ctx->x_submap))
+                                  ctx->x_psub, ctx->x_segmap, ctx->x_submap, pfor))
             return fail(ctx, RZ_ERR_ARC, "an arc has no finite cubic count");
         kind = ctx->x_kind.data();
         pts = ctx->x_pts.data();
@@ -1038,11 +1042,12 @@ rz_status render_single(rz_ctx* ctx, const rz_path* path, const double tr[6], in
     if (rule != RZ_FILL_NONZERO && rule != RZ_FILL_EVENODD) return fail(ctx, RZ_ERR_INVALID, "bad fill rule");
     if (width > 16383 || height > 16383) return fail(ctx, RZ_ERR_INVALID, "image too large (max 16383 x 16383)");
     RZ_CUDA(cudaSetDevice(ctx->device));
+    Trace trc("render_single");
     rz::BatchDev b{};
     const uint32_t path_sub[2] = {0, path->n_subpaths};
     const uint8_t r8 = (uint8_t)rule;
     st = stage_host(ctx, path->seg_kind, path->seg_pts, path->n_segments, path->subpath_off, path->n_subpaths,
-                    path_sub, 1, tr, &r8, b);
+                    path_sub, 1, tr, &r8, b, nullptr, nullptr, &trc);
     if (st) return st;
     std::vector<rz::MaskDev> masks(1);
     masks[0].offset = 0;
@@ -1054,18 +1059,23 @@ rz_status render_single(rz_ctx* ctx, const rz_path* path, const double tr[6], in
     build_items(masks, false, items);
     st = stage_plan(ctx, masks, items, b);
     if (st) return st;
+    trc.mark("plan");
     RZ_CUDA(ctx->d_out.ensure(width * height * 4 + 16));
     b.out = (float*)ctx->d_out.p;
     set_thresholds(b, flatness);
     st = run_bands(ctx, b, items, false);
     if (st) return st;
+    trc.gpu_mark(ctx->stream, "bands");
     return RZ_OK;
 }
 
 }  // namespace
 
+// Segment x band products above this take the line pipeline: a 200-cubic
+// path over a 512^2 mask (31 bands, 6,231) renders in 0.19 ms there against
+// 0.30 ms of band kernel (31 CTAs re-walking every tree).
 #ifndef RZ_PIPELINE_MIN
-#define RZ_PIPELINE_MIN 2000000
+#define RZ_PIPELINE_MIN 4000
 #endif
 namespace {
 rz_status mask_pipeline(rz_ctx* ctx, const rz_path* path, const double tr[6], int32_t rule, double flatness,
@@ -1682,41 +1692,48 @@ struct HostScene {
 void adaptive_tasks(HostScene& hs, double flatness) {
     const double thr = 16.0 * flatness * flatness;
     hs.task_off.assign((size_t)hs.n_slots + 1, 0);
-    uint32_t acc = 0;
     for (const rz::FillDev& f : hs.fills) {
         const uint32_t nseg = f.seg1 - f.seg0, nslot = nseg + (f.sub1 - f.sub0);
-        for (uint32_t i = 0; i < nslot; ++i) {
-            int depth = 0;
-            if (i < nseg) {
-                const uint32_t g = f.seg0 + i;
-                const int kind = hs.kind[g];
-                if (kind == RZ_SEG_QUAD || kind == RZ_SEG_CUBIC) {
-                    const double* p = hs.pts + 8ull * g;
-                    double x[4], y[4];
-                    for (int q = 0; q < 4; ++q) {
-                        x[q] = f.tr[0] * p[2 * q] + f.tr[1] * p[2 * q + 1] + f.tr[2];
-                        y[q] = f.tr[3] * p[2 * q] + f.tr[4] * p[2 * q + 1] + f.tr[5];
+        // per slot: the log2 of its task count (slots of different fills never overlap)
+        parallel_for((int64_t)nslot, 2048, [&](int64_t i0, int64_t i1) {
+            for (int64_t i = i0; i < i1; ++i) {
+                int depth = 0;
+                if (i < (int64_t)nseg) {
+                    const uint32_t g = f.seg0 + (uint32_t)i;
+                    const int kind = hs.kind[g];
+                    if (kind == RZ_SEG_QUAD || kind == RZ_SEG_CUBIC) {
+                        const double* p = hs.pts + 8ull * g;
+                        double x[4], y[4];
+                        for (int q = 0; q < 4; ++q) {
+                            x[q] = f.tr[0] * p[2 * q] + f.tr[1] * p[2 * q + 1] + f.tr[2];
+                            y[q] = f.tr[3] * p[2 * q] + f.tr[4] * p[2 * q + 1] + f.tr[5];
+                        }
+                        double fl;
+                        if (kind == RZ_SEG_QUAD) {
+                            const double ux = 2 * x[1] - x[0] - x[2], uy = 2 * y[1] - y[0] - y[2];
+                            fl = ux * ux + uy * uy;
+                        } else {
+                            const double ux = 3 * x[1] - 2 * x[0] - x[3], uy = 3 * y[1] - 2 * y[0] - y[3];
+                            const double vx = 3 * x[2] - x[0] - 2 * x[3], vy = 3 * y[2] - y[0] - 2 * y[3];
+                            fl = std::max(ux * ux, vx * vx) + std::max(uy * uy, vy * vy);
+                        }
+                        int d = 0;
+                        while (d < 22 && std::isfinite(fl) && fl >= thr) {
+                            fl /= 16.0;
+                            ++d;
+                        }
+                        depth = std::min(10, std::max(0, d - 3));
                     }
-                    double fl;
-                    if (kind == RZ_SEG_QUAD) {
-                        const double ux = 2 * x[1] - x[0] - x[2], uy = 2 * y[1] - y[0] - y[2];
-                        fl = ux * ux + uy * uy;
-                    } else {
-                        const double ux = 3 * x[1] - 2 * x[0] - x[3], uy = 3 * y[1] - 2 * y[0] - y[3];
-                        const double vx = 3 * x[2] - x[0] - 2 * x[3], vy = 3 * y[2] - y[0] - 2 * y[3];
-                        fl = std::max(ux * ux, vx * vx) + std::max(uy * uy, vy * vy);
-                    }
-                    int d = 0;
-                    while (d < 22 && std::isfinite(fl) && fl >= thr) {
-                        fl /= 16.0;
-                        ++d;
-                    }
-                    depth = std::min(10, std::max(0, d - 3));
                 }
+                hs.task_off[f.slot0 + i] = (uint32_t)depth;
             }
-            hs.task_off[f.slot0 + i] = acc;
-            acc += 1u << depth;
-        }
+        });
+    }
+    uint32_t acc = 0;  // depths -> first task of each slot
+    for (uint32_t s = 0; s < hs.n_slots; ++s) {
+        const uint32_t depth = hs.task_off[s];
+        hs.task_off[s] = acc;
+        acc += 1u << depth;
     }
     hs.task_off[hs.n_slots] = acc;
 }
@@ -1732,7 +1749,7 @@ int choose_band_rows(int canvas_w, int canvas_h, bool paint_mode, int num_sms) {
     // rows plus a fixed share for the lines that cross its edges
     int best = rmax;
     int64_t best_cost = INT64_MAX;
-    for (int r = rmax; r >= std::max(1, rmax / 2); --r) {
+    for (int r = rmax; r >= 1; --r) {
         const int64_t bands = (canvas_h + r - 1) / r;
         const int64_t cost = (bands + slots - 1) / slots * (r + 4);
         if (cost < best_cost) {
@@ -1773,7 +1790,12 @@ void add_fill(HostScene& hs, uint32_t sub0, uint32_t sub1, int col0, int row0, i
 // Flatten + bin on the device (pipeline steps 1-5): every fill's lines, the
 // per-(fill, band) counts and starts, and the band lists.  `leaf` (device,
 // may be null) receives each line's segment and tree node.
-rz_status build_lines(rz_ctx* ctx, HostScene& hs, rz::SceneDev& S, Trace& tr, DevBuf* leaf) {
+// speculative: the lines and lists go into the buffers as they are and the
+// counts stay on the device (no host round trip between the passes); a
+// buffer too small shows as RZ_ERR_CAPACITY once the composite has run, and
+// the caller then sizes the buffers from the device counts and runs again.
+rz_status build_lines(rz_ctx* ctx, HostScene& hs, rz::SceneDev& S, Trace& tr, DevBuf* leaf,
+                      bool speculative = false) {
     RZ_CUDA(ctx->p_fills.ensure(hs.fills.size() * sizeof(rz::FillDev)));
     RZ_CUDA(cudaMemcpyAsync(ctx->p_fills.p, hs.fills.data(), hs.fills.size() * sizeof(rz::FillDev),
                             cudaMemcpyHostToDevice, ctx->stream));
@@ -1796,20 +1818,29 @@ rz_status build_lines(rz_ctx* ctx, HostScene& hs, rz::SceneDev& S, Trace& tr, De
     const uint64_t ne = (uint64_t)hs.n_entries + 1;
     RZ_CUDA(ctx->p_scan.ensure(rz::scan_temp_words(std::max(ns, ne)) * 4 + 64));
     RZ_CUDA(rz::scan_u32(S.slot_count, ns, (uint32_t*)ctx->p_scan.p, ctx->stream));
-    uint32_t n_lines = 0;
-    RZ_CUDA(cudaMemcpyAsync(&n_lines, S.slot_count + (ns - 1), 4, cudaMemcpyDeviceToHost, ctx->stream));
-    RZ_CUDA(cudaStreamSynchronize(ctx->stream));
-    rz_status st = read_error(ctx);
-    if (st) return st;
-    if (leaf) {
-        RZ_CUDA(leaf->ensure((uint64_t)std::max(n_lines, 1u) * sizeof(uint2)));
-        S.leaf = (uint2*)leaf->p;
+    if (speculative) {
+        constexpr size_t kMinLines = 1u << 16;
+        RZ_CUDA(ctx->p_lines.ensure(kMinLines * 2 * sizeof(int4)));
+        const uint64_t cap = std::min<uint64_t>(ctx->p_lines.cap / (2 * sizeof(int4)), 0xffffffffull);
+        S.line_cap = (uint32_t)cap;
+        S.n_lines = (uint32_t)cap;  // launch bound; the count is read on the device
+        S.n_lines_dev = S.slot_count + (ns - 1);
+    } else {
+        uint32_t n_lines = 0;
+        RZ_CUDA(cudaMemcpyAsync(&n_lines, S.slot_count + (ns - 1), 4, cudaMemcpyDeviceToHost, ctx->stream));
+        RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+        rz_status st = read_error(ctx);
+        if (st) return st;
+        if (leaf) {
+            RZ_CUDA(leaf->ensure((uint64_t)std::max(n_lines, 1u) * sizeof(uint2)));
+            S.leaf = (uint2*)leaf->p;
+        }
+        S.n_lines = n_lines;
+        S.line_cap = n_lines;
+        RZ_CUDA(ctx->p_lines.ensure((uint64_t)std::max(n_lines, 1u) * 2 * sizeof(int4)));
     }
-    S.n_lines = n_lines;
     // 3) lines + per-(fill, band) counts
-    RZ_CUDA(ctx->p_lines.ensure((uint64_t)std::max(n_lines, 1u) * 2 * sizeof(int4)));
     S.lines = (int4*)ctx->p_lines.p;
-    S.line_cap = n_lines;
     RZ_CUDA(ctx->p_ecount.ensure(ne * 4));
     RZ_CUDA(ctx->p_estart.ensure(ne * 4));
     RZ_CUDA(ctx->p_ecursor.ensure(ne * 4));
@@ -1823,15 +1854,33 @@ rz_status build_lines(rz_ctx* ctx, HostScene& hs, rz::SceneDev& S, Trace& tr, De
     // 4) list starts per (fill, band)
     RZ_CUDA(cudaMemcpyAsync(S.entry_start, S.entry_count, ne * 4, cudaMemcpyDeviceToDevice, ctx->stream));
     RZ_CUDA(rz::scan_u32(S.entry_start, ne, (uint32_t*)ctx->p_scan.p, ctx->stream));
-    uint32_t n_pairs = 0;
-    RZ_CUDA(cudaMemcpyAsync(&n_pairs, S.entry_start + hs.n_entries, 4, cudaMemcpyDeviceToHost, ctx->stream));
-    RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (speculative) {
+        constexpr size_t kMinPairs = 1u << 18;
+        RZ_CUDA(ctx->p_pairs.ensure(kMinPairs * 4));
+    } else {
+        uint32_t n_pairs = 0;
+        RZ_CUDA(cudaMemcpyAsync(&n_pairs, S.entry_start + hs.n_entries, 4, cudaMemcpyDeviceToHost, ctx->stream));
+        RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+        RZ_CUDA(ctx->p_pairs.ensure((uint64_t)std::max(n_pairs, 1u) * 4));
+    }
     // 5) line lists
-    RZ_CUDA(ctx->p_pairs.ensure((uint64_t)std::max(n_pairs, 1u) * 4));
     S.pairs = (uint32_t*)ctx->p_pairs.p;
+    S.pair_cap = (uint32_t)std::min<uint64_t>(ctx->p_pairs.cap / 4, 0xffffffffull);
     tr.gpu_mark(ctx->stream, "entry_scan");
     RZ_CUDA(rz::launch_bin_scatter(S, ctx->stream));
     tr.gpu_mark(ctx->stream, "bin_scatter");
+    return RZ_OK;
+}
+
+// After a speculative pass that ran out of room: the buffers sized from the
+// device's counts (the lines' total and the lists' total).
+rz_status grow_line_buffers(rz_ctx* ctx, const rz::SceneDev& S, uint32_t n_entries) {
+    uint32_t n_lines = 0, n_pairs = 0;
+    RZ_CUDA(cudaMemcpyAsync(&n_lines, S.n_lines_dev, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    RZ_CUDA(cudaMemcpyAsync(&n_pairs, S.entry_start + n_entries, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+    RZ_CUDA(ctx->p_lines.ensure((uint64_t)std::max(n_lines, 1u) * 2 * sizeof(int4)));
+    RZ_CUDA(ctx->p_pairs.ensure((uint64_t)std::max(n_pairs, 1u) * 4));
     return RZ_OK;
 }
 
@@ -1883,20 +1932,37 @@ rz_status run_pipeline(rz_ctx* ctx, HostScene& hs, double flatness, float* canva
                                 cudaMemcpyHostToDevice, ctx->stream));
         S.paints = (const rz::PaintDev*)ctx->p_paints.p;
     }
-    rz_status st = build_lines(ctx, hs, S, tr, nullptr);
+    // the composite writes every pixel from bg (or leaves untouched mask bands zero): a pass
+    // that ran out of list room can run again; over a loaded canvas the buffers are sized first
+    const bool speculative = !load_canvas;
+    rz::SceneDev S0 = S;
+    rz_status st = build_lines(ctx, hs, S, tr, nullptr, speculative);
     if (st) return st;
     // 6) composite
     RZ_CUDA(rz::launch_composite(S, cov_stride, smem, ctx->stream));
     tr.gpu_mark(ctx->stream, "composite");
-    return read_error(ctx);
+    st = read_error(ctx);
+    if (st == RZ_ERR_CAPACITY && speculative) {
+        st = grow_line_buffers(ctx, S, hs.n_entries);
+        if (st) return st;
+        S = S0;
+        RZ_CUDA(cudaMemsetAsync(ctx->d_ctrl.p, 0, 64, ctx->stream));
+        ctx->last_error.clear();
+        st = build_lines(ctx, hs, S, tr, nullptr, false);
+        if (st) return st;
+        RZ_CUDA(rz::launch_composite(S, cov_stride, smem, ctx->stream));
+        st = read_error(ctx);
+    }
+    return st;
 }
 
 // Segments of `hs` staged into the context's device buffers (arcs expanded).
 rz_status stage_scene_segments(rz_ctx* ctx, const uint8_t* kind, const double* pts, uint32_t n_seg,
                                const uint32_t* sub_off, uint32_t n_sub, const uint32_t* fill_sub, uint32_t n_fills,
-                               HostScene& hs, std::vector<uint32_t>& fill_sub_out) {
+                               HostScene& hs, std::vector<uint32_t>& fill_sub_out, Trace* trace = nullptr) {
     rz::BatchDev b{};
-    rz_status st = stage_host(ctx, kind, pts, n_seg, sub_off, n_sub, fill_sub, n_fills, nullptr, nullptr, b);
+    rz_status st =
+        stage_host(ctx, kind, pts, n_seg, sub_off, n_sub, fill_sub, n_fills, nullptr, nullptr, b, nullptr, nullptr, trace);
     if (st) return st;
     if (ctx->expanded) {
         hs.kind = ctx->x_kind.data();
@@ -1939,17 +2005,19 @@ rz_status copy_out_bytes(rz_ctx* ctx, void* dst, const void* src_dev, uint64_t b
 // Renders one large path as a mask with the line pipeline (mask semantics).
 rz_status mask_pipeline(rz_ctx* ctx, const rz_path* path, const double tr[6], int32_t rule, double flatness,
                         uint64_t width, uint64_t height) {
+    Trace trc("mask_pipeline host");
     HostScene hs;
     std::vector<uint32_t> fsub;
     const uint32_t psub[2] = {0, path->n_subpaths};
     rz_status st = stage_scene_segments(ctx, path->seg_kind, path->seg_pts, path->n_segments, path->subpath_off,
-                                        path->n_subpaths, psub, 1, hs, fsub);
+                                        path->n_subpaths, psub, 1, hs, fsub, &trc);
     if (st) return st;
     hs.band_rows = choose_band_rows((int)width, (int)height, false, ctx->num_sms);
     rzhost::Xf t;
     std::memcpy(t.m, tr, sizeof(t.m));
     add_fill(hs, fsub[0], fsub[1], 0, 0, (int)width, (int)height, (int)width - 1, t, rule, -1);
     adaptive_tasks(hs, flatness);  // a path this large has long segments: subtree tasks by their depth
+    trc.mark("tasks");
     RZ_CUDA(ctx->d_out.ensure(width * height * 4 + 16));
     RZ_CUDA(cudaMemsetAsync(ctx->d_out.p, 0, width * height * 4, ctx->stream));
     return run_pipeline(ctx, hs, flatness, (float*)ctx->d_out.p, (int64_t)width, (int)width, (int)height, nullptr,

@@ -402,6 +402,11 @@ __global__ void __launch_bounds__(kEmitThreads) k_flatten_emit(SceneDev S) {
         if (s_hist[i]) atomicAdd(&S.entry_count[he0 + i], s_hist[i]);
 }
 
+// Lines of the scene (at most the buffer's capacity when counted on the device).
+__device__ __forceinline__ uint32_t scene_lines(const SceneDev& S) {
+    return S.n_lines_dev ? min(*S.n_lines_dev, S.line_cap) : S.n_lines;
+}
+
 // Fill owning line l among fills [lo, hi) (slot_count holds the line offsets
 // of the flatten tasks).
 __device__ __forceinline__ uint32_t fill_of_line(const SceneDev& S, uint32_t l, uint32_t lo = 0, uint32_t hi = 0) {
@@ -409,7 +414,7 @@ __device__ __forceinline__ uint32_t fill_of_line(const SceneDev& S, uint32_t l, 
     while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) >> 1;
         const uint32_t first =
-            S.fills[mid].slot0 < S.n_slots ? S.slot_count[task_first(S, S.fills[mid].slot0)] : S.n_lines;
+            S.fills[mid].slot0 < S.n_slots ? S.slot_count[task_first(S, S.fills[mid].slot0)] : scene_lines(S);
         if (first <= l) lo = mid; else hi = mid;
     }
     return lo;
@@ -432,11 +437,18 @@ __device__ __forceinline__ void line_bands(const SceneDev& S, const FillDev& f, 
 // lanes of a warp (l >= n_lines: no line).  Consecutive lines mostly fall in
 // one entry: the lanes with the same single entry take their slots with one
 // atomic.
-__device__ void bin_line_global(const SceneDev& S, uint32_t l) {
+// A list slot beyond the buffer (sized before the lines were counted) is
+// reported as ERR_CAPACITY and not written.
+__device__ __forceinline__ void put_pair(const SceneDev& S, uint32_t i, uint32_t l) {
+    if (i < S.pair_cap) S.pairs[i] = l;
+    else pset_err(S.err, ERR_CAPACITY);
+}
+
+__device__ void bin_line_global(const SceneDev& S, uint32_t l, uint32_t n_lines) {
     const int lane = threadIdx.x & 31;
     int b0 = 0, b1 = -1;
     const FillDev* f = nullptr;
-    if (l < S.n_lines) {
+    if (l < n_lines) {
         f = &S.fills[fill_of_line(S, l)];
         line_bands(S, *f, l, b0, b1);
     }
@@ -449,11 +461,11 @@ __device__ void bin_line_global(const SceneDev& S, uint32_t l) {
         uint32_t base = 0;
         if (lane == leader) base = atomicAdd(&S.entry_cursor[e], (uint32_t)__popc(same));
         base = __shfl_sync(same, base, leader);
-        S.pairs[S.entry_start[e] + base + __popc(same & ((1u << lane) - 1u))] = l;
+        put_pair(S, S.entry_start[e] + base + __popc(same & ((1u << lane) - 1u)), l);
     } else {
         for (int bb = b0; bb <= b1; ++bb) {
             const uint32_t e = f->entry0 + (bb - f->band0);
-            S.pairs[S.entry_start[e] + atomicAdd(&S.entry_cursor[e], 1u)] = l;
+            put_pair(S, S.entry_start[e] + atomicAdd(&S.entry_cursor[e], 1u), l);
         }
     }
 }
@@ -469,8 +481,10 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_scatter(SceneDev S) {
     __shared__ uint32_t s_cnt[kHistEntries];
     __shared__ uint32_t s_base[kHistEntries];
     __shared__ uint32_t s_e0, s_n, s_fa, s_fb;
+    const uint32_t n_lines = scene_lines(S);
     const uint32_t l0 = blockIdx.x * kBinLines;
-    const uint32_t l1 = min(l0 + kBinLines, S.n_lines);
+    if (l0 >= n_lines) return;  // the grid covers the buffer's capacity
+    const uint32_t l1 = min(l0 + kBinLines, n_lines);
     if (threadIdx.x == 0) {
         const uint32_t fa = fill_of_line(S, l0), fb = fill_of_line(S, l1 - 1);
         const uint32_t e0 = S.fills[fa].entry0, e1 = S.fills[fb].entry0 + (uint32_t)S.fills[fb].nbands;
@@ -482,7 +496,7 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_scatter(SceneDev S) {
     __syncthreads();
     const uint32_t n = s_n, e0 = s_e0, fa = s_fa, fb = s_fb;
     if (n == 0) {
-        for (uint32_t l = l0 + threadIdx.x; l < l0 + kBinLines; l += kBinThreads) bin_line_global(S, l < l1 ? l : S.n_lines);
+        for (uint32_t l = l0 + threadIdx.x; l < l0 + kBinLines; l += kBinThreads) bin_line_global(S, l < l1 ? l : n_lines, n_lines);
         return;
     }
     for (uint32_t i = threadIdx.x; i < n; i += kBinThreads) s_cnt[i] = 0u;
@@ -506,7 +520,7 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_scatter(SceneDev S) {
         line_bands(S, f, l, b0, b1);
         for (int bb = b0; bb <= b1; ++bb) {
             const uint32_t i = f.entry0 + (bb - f.band0) - e0;
-            S.pairs[s_base[i] + atomicAdd(&s_cnt[i], 1u)] = l;
+            put_pair(S, s_base[i] + atomicAdd(&s_cnt[i], 1u), l);
         }
     }
 }
@@ -800,8 +814,9 @@ __global__ void __launch_bounds__(THREADS) k_composite(SceneDev S, int cov_strid
             const uint32_t j = j0 + lane;
             uint32_t l = 0;
             bool slow = false;
-            if (j < n) {
-                l = S.pairs[start + j];
+            // slots and lines beyond the buffers (reported by the earlier passes) are skipped
+            if (j < n && start + j < S.pair_cap) l = S.pairs[start + j];
+            if (j < n && start + j < S.pair_cap && l < S.line_cap) {
                 const int4 a = S.lines[2ull * l], b = S.lines[2ull * l + 1];
                 slow = !accumulate_vtx_short(B, line_vtx(a, B.y0), line_vtx(b, B.y0));
             }

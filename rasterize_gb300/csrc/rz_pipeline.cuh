@@ -81,8 +81,10 @@ struct SceneDev {
     // pipeline buffers
     uint32_t* slot_count;    // [tasks + 1] lines per flatten task, then its exclusive prefix (line offsets)
     int4* lines;             // [2 * n_lines] per end point: exact 16.16 anchor (x, y), FP32 remainder (dx, dy)
-    uint32_t n_lines;
+    uint32_t n_lines;        // lines, or (n_lines_dev set) an upper bound for launch sizes
+    const uint32_t* n_lines_dev;  // non-null: the line count in device memory (sized without a host round trip)
     uint32_t line_cap;       // lines the buffer holds (the emit pass reports more as ERR_CAPACITY)
+    uint32_t pair_cap;       // (line, band) pairs the list buffer holds (the scatter reports more)
     uint32_t* entry_count;   // [n_entries]
     uint32_t* entry_start;   // [n_entries] exclusive prefix of entry_count
     uint32_t* entry_cursor;  // [n_entries]

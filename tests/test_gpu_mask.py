@@ -277,3 +277,20 @@ def test_lines_kernel_matches_band_kernel(R, monkeypatch):
     for i in range(0, 200, 9):
         w, h = sizes[i]
         assert_close(batch.mask(lines, i), O.mask(paths[i], Transform.identity(), rules[i], w, h))
+
+
+def test_pipeline_line_buffers_grow():
+    """The line pipeline sizes its buffers without a host round trip: a fresh
+    context starts small, so its first large path runs out of room, is
+    re-rendered with buffers sized from the device's counts, and every later
+    call (large or small) renders the same masks."""
+    R2 = GpuRasterizer()
+    path, rule, _ = W.large_path(seed=4, n_segments=5000, size=1024)
+    ref = O.mask(path, Transform.identity(), rule, 1024, 1024)
+    first = gpu_mask(R2, path, Transform.identity(), rule, 1024, 1024)
+    assert_close(first, ref)
+    assert np.array_equal(gpu_mask(R2, path, Transform.identity(), rule, 1024, 1024), first)
+    small, srule, (w, h) = W.small_path(seed=0)
+    assert_close(gpu_mask(R2, small, Transform.identity(), srule, w, h),
+                 O.mask(small, Transform.identity(), srule, w, h))
+    assert np.array_equal(gpu_mask(R2, path, Transform.identity(), rule, 1024, 1024), first)
