@@ -1740,9 +1740,9 @@ void adaptive_tasks(HostScene& hs, double flatness) {
 
 int choose_band_rows(int canvas_w, int canvas_h, bool paint_mode, int num_sms) {
     const int stride = rz::band_stride(canvas_w);
-    const int per_row = 4 * stride + (paint_mode ? 16 * canvas_w : 0);
+    const int per_row = 4 * stride;  // the coverage band (colours stay in the canvas)
     // coverage only: tall bands (one CTA per SM) amortise a line's per-band set-up; with paint, two CTAs per SM
-    const int rmax = std::max(1, std::min(std::min((paint_mode ? 96 * 1024 : 208 * 1024) / per_row, 64),
+    const int rmax = std::max(1, std::min(std::min((paint_mode ? 100 * 1024 : 208 * 1024) / per_row, 64),
                                           std::max(canvas_h, 1)));
     const int64_t slots = (int64_t)std::max(num_sms, 1) * (paint_mode ? 2 : 1);
     // the band kernel runs in waves of `slots` bands: the height whose waves cost least, counting each band's

@@ -708,9 +708,9 @@ __device__ float4 paint_at(const PaintDev& p, float px, float py) {
 
 
 struct BlendEpi {
-    float4* rgba;        // band colour, canvas_w per row
-    int canvas_w;
-    int col0;            // canvas column of local x = 0
+    float4* rgba;        // the canvas at the band's first row and the view's first column
+    int64_t stride;      // pixels between canvas rows
+    int col0;            // canvas column of local x = 0 (already in rgba)
     int y0_local;        // local row of band row 0
     int width;           // view width
     const PaintDev* paint;
@@ -722,7 +722,7 @@ struct BlendEpi {
             const float al = a[i];
             if (fabsf(al) < 1e-6f) continue;  // mask_iter skips these pixels (src/rasterize.rs:347-349)
             const float4 c = paint_at(*paint, (float)x + 0.5f, (float)(y0_local + r) + 0.5f);
-            float4& d = rgba[r * canvas_w + col0 + x];
+            float4& d = rgba[r * stride + x];
             // dst.blend_over(color.with_alpha(alpha)) = src + dst * (1 - src.a) (src/color.rs:342-349)
             const float4 s = make_float4(c.x * al, c.y * al, c.z * al, c.w * al);
             const float inv = 1.f - s.w;
@@ -744,7 +744,7 @@ struct AlphaEpi {  // coverage-only fills write the mask
     }
 };
 
-// smem: coverage band (band_rows x cov_stride words) | RGBA band (band_rows x canvas_w float4)
+// smem: the coverage band (band_rows x cov_stride words)
 // The binary64 route of accumulate_vtx for line l.
 static __device__ __noinline__ void composite_slow_line(const SceneDev& S, const Band& B, uint32_t l) {
     const VtxQ a = line_vtx(S.lines[2ull * l], B.y0), b = line_vtx(S.lines[2ull * l + 1], B.y0);
@@ -753,7 +753,10 @@ static __device__ __noinline__ void composite_slow_line(const SceneDev& S, const
 }
 
 // THREADS: 512 for masks (one CTA per SM), 256 with paint (two CTAs per SM,
-// so one CTA blends while the other accumulates).
+// so one CTA blends while the other accumulates).  With paint the band's
+// colours stay in the canvas itself (L2-resident while the band is worked
+// on): only the coverage band takes shared memory, so bands are tall and the
+// per-fill work of a band covers many rows.
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS) k_composite(SceneDev S, int cov_stride) {
     extern __shared__ float4 sm4[];
@@ -762,23 +765,16 @@ __global__ void __launch_bounds__(THREADS) k_composite(SceneDev S, int cov_strid
     const int lane = threadIdx.x & 31;
     float* cov = reinterpret_cast<float*>(sm4);
     const bool paint_mode = S.paints != nullptr;
-    float4* rgba = reinterpret_cast<float4*>(cov + S.band_rows * cov_stride);
     const int band = blockIdx.x;
     const int row_base = band * S.band_rows;
     const int rows = min(S.band_rows, S.canvas_h - row_base);
     if (rows <= 0) return;
-    if (paint_mode) {
+    float4* canvas4 = reinterpret_cast<float4*>(S.canvas) + (int64_t)row_base * S.canvas_stride;
+    if (paint_mode && !S.load_canvas) {
+        const float4 v = S.bg ? make_float4(S.bg[0], S.bg[1], S.bg[2], S.bg[3]) : make_float4(0.f, 0.f, 0.f, 0.f);
         for (int i = threadIdx.x; i < rows * S.canvas_w; i += THREADS) {
             const int r = i / S.canvas_w, x = i - r * S.canvas_w;
-            float4 v;
-            if (S.load_canvas) {
-                v = reinterpret_cast<const float4*>(S.canvas)[(int64_t)(row_base + r) * S.canvas_stride + x];
-            } else if (S.bg) {
-                v = make_float4(S.bg[0], S.bg[1], S.bg[2], S.bg[3]);
-            } else {
-                v = make_float4(0.f, 0.f, 0.f, 0.f);
-            }
-            rgba[i] = v;
+            canvas4[(int64_t)r * S.canvas_stride + x] = v;
         }
     }
     for (uint32_t fi = 0; fi < S.n_fills; ++fi) {
@@ -834,25 +830,20 @@ __global__ void __launch_bounds__(THREADS) k_composite(SceneDev S, int cov_strid
         if (lane < nq) composite_slow_line(S, B, q[lane]);
         __syncthreads();
         if (paint_mode) {
-            BlendEpi epi{rgba, S.canvas_w, f.col0, B.y0, f.width, &s_paint};
+            BlendEpi epi{canvas4 + f.col0, S.canvas_stride, f.col0, B.y0, f.width, &s_paint};
             band_scan<THREADS>(B, f.width, f.rule, epi);
         } else {
             AlphaEpi epi{S.canvas, S.canvas_stride, row_base, f.col0, f.width};
             band_scan<THREADS>(B, f.width, f.rule, epi);
         }
     }
-    if (paint_mode) {
-        __syncthreads();
-        if (S.rgba8) {
-            // fused output encode: From<LinColor> for RGBA per pixel, 4 bytes out instead of 16
-            uint32_t* o = S.rgba8 + (int64_t)row_base * S.canvas_w;
-            for (int i = threadIdx.x; i < rows * S.canvas_w; i += THREADS)
-                __stcs(o + i, encode_lin_rgba8(rgba[i]));
-        } else {
-            for (int i = threadIdx.x; i < rows * S.canvas_w; i += THREADS) {
-                const int r = i / S.canvas_w, x = i - r * S.canvas_w;
-                reinterpret_cast<float4*>(S.canvas)[(int64_t)(row_base + r) * S.canvas_stride + x] = rgba[i];
-            }
+    if (paint_mode && S.rgba8) {
+        __syncthreads();  // the block's blends are visible to the block
+        // fused output encode: From<LinColor> for RGBA per pixel, 4 bytes out instead of 16
+        uint32_t* o = S.rgba8 + (int64_t)row_base * S.canvas_w;
+        for (int i = threadIdx.x; i < rows * S.canvas_w; i += THREADS) {
+            const int r = i / S.canvas_w, x = i - r * S.canvas_w;
+            __stcs(o + i, encode_lin_rgba8(canvas4[(int64_t)r * S.canvas_stride + x]));
         }
     }
 }
@@ -884,7 +875,9 @@ cudaError_t launch_bin_scatter(const SceneDev& S, cudaStream_t st) {
 int composite_smem_bytes(int canvas_w, int band_rows, int max_clip_width, bool paint_mode, int* cov_stride) {
     const int stride = band_stride(max_clip_width);
     *cov_stride = stride;
-    return 4 * band_rows * stride + (paint_mode ? 16 * band_rows * canvas_w : 0);
+    (void)canvas_w;
+    (void)paint_mode;
+    return 4 * band_rows * stride;
 }
 
 // The shared-memory attribute is per device and kernel: the largest size set
