@@ -2,8 +2,9 @@
 //
 // The images are stacked into one tall canvas (image i owns canvas rows
 // [i H, (i + 1) H)) so the line pipeline flattens every path once and bins
-// its lines by (path, band of R rows); R divides H, so a band belongs to one
-// image.  One CTA per band then:
+// its lines by (path, row).  One CTA per band of R rows (R divides H, so a
+// band belongs to one image; one warp per row, which reads only its row's
+// lists) then:
 //
 //   forward   for the paths of its image in order: signed area of the path's
 //             lines in shared memory (exact fixed point), row prefix, fill
@@ -171,9 +172,10 @@ __device__ void diff_scan_blend_row(float* crow, int stride, int width, int rule
     clear_row_tail(row4, width, stride, lane);
 }
 
-// The band's line list of paths p0 + lane (one per lane, 32 at a time):
-// every lane loads its path's (fill, band) entry at once instead of one path
-// after the other.  n = 0 for paths past the image's last.
+// The line lists of canvas row `band` (lists are binned per row) of paths
+// p0 + lane (one per lane, 32 at a time): every lane loads its path's
+// (fill, row) entry at once instead of one path after the other.  n = 0 for
+// paths past the image's last.
 __device__ __forceinline__ void path_entries(const DiffDev& D, int img, int band, int p0, int lane, uint32_t& n,
                                              uint32_t& start) {
     n = 0;
@@ -216,10 +218,9 @@ __global__ void __launch_bounds__(kDiffThreads, 4) k_diff_forward(DiffDev D, int
     extern __shared__ float4 sm4[];
     float* cov = reinterpret_cast<float*>(sm4);
     const SceneDev& S = D.S;
-    const int rows = S.band_rows;
+    const int rows = D.cta_rows;
     float* A = cov + rows * cov_stride;
-    const int band = blockIdx.x;
-    const int row_base = band * rows;
+    const int row_base = blockIdx.x * rows;
     const int img = row_base / D.height;
     for (int i = threadIdx.x; i < rows * D.width; i += kDiffThreads) A[i] = 0.f;
     for (int i = threadIdx.x; i < (rows * cov_stride) >> 2; i += kDiffThreads) sm4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -232,8 +233,8 @@ __global__ void __launch_bounds__(kDiffThreads, 4) k_diff_forward(DiffDev D, int
     const Band B = diff_row_band(D, crow, row, img);
     for (int p0 = 0; p0 < D.paths; p0 += 32) {
         uint32_t my_n, my_start;
-        path_entries(D, img, band, p0, lane, my_n, my_start);
-        uint32_t todo = __ballot_sync(0xffffffffu, my_n != 0);  // paths with no line in the band add nothing
+        path_entries(D, img, row, p0, lane, my_n, my_start);  // lists are binned per row
+        uint32_t todo = __ballot_sync(0xffffffffu, my_n != 0);  // paths with no line in the row add nothing
       while (todo) {
         const int q = __ffs(todo) - 1;
         todo &= todo - 1u;
@@ -511,14 +512,13 @@ __device__ void diff_sparse_row(const DiffDev& D, int wpr, int row, const uint32
 __global__ void __launch_bounds__(kDiffThreads, 3) k_diff_backward(DiffDev D, int cov_stride) {
     extern __shared__ float4 sm4[];
     const SceneDev& S = D.S;
-    const int rows = S.band_rows;
+    const int rows = D.cta_rows;
     const int wpr = (cov_stride + 31) >> 5;
     float* cov = reinterpret_cast<float*>(sm4);  // coverage words, then g
     float* P = cov + rows * cov_stride;
     float* tot = P + rows * cov_stride;
     uint32_t* bits = reinterpret_cast<uint32_t*>(tot + 8);
-    const int band = blockIdx.x;
-    const int row_base = band * rows;
+    const int row_base = blockIdx.x * rows;
     const int img = row_base / D.height;
     float2* out = reinterpret_cast<float2*>(D.out);
     for (int i = threadIdx.x; i < rows * cov_stride; i += kDiffThreads) cov[i] = 0.f;
@@ -533,8 +533,8 @@ __global__ void __launch_bounds__(kDiffThreads, 3) k_diff_backward(DiffDev D, in
     const Band B = diff_row_band(D, crow, row, img);
     for (int p0 = 0; p0 < D.paths; p0 += 32) {
         uint32_t my_n, my_start;
-        path_entries(D, img, band, p0, lane, my_n, my_start);
-        uint32_t todo = __ballot_sync(0xffffffffu, my_n != 0);  // no line in the band: nothing to move
+        path_entries(D, img, row, p0, lane, my_n, my_start);  // lists are binned per row
+        uint32_t todo = __ballot_sync(0xffffffffu, my_n != 0);  // no line in the row: nothing to move
       while (todo) {
         const int q = __ffs(todo) - 1;
         todo &= todo - 1u;
@@ -647,11 +647,11 @@ cudaError_t launch_diff(const DiffDev& D, bool backward, int cov_stride, int sme
     if (backward) {
         cudaError_t e = cudaFuncSetAttribute(k_diff_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
-        k_diff_backward<<<D.S.n_bands, kDiffThreads, smem, st>>>(D, cov_stride);
+        k_diff_backward<<<D.S.canvas_h / D.cta_rows, kDiffThreads, smem, st>>>(D, cov_stride);
     } else {
         cudaError_t e = cudaFuncSetAttribute(k_diff_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
-        k_diff_forward<<<D.S.n_bands, kDiffThreads, smem, st>>>(D, cov_stride);
+        k_diff_forward<<<D.S.canvas_h / D.cta_rows, kDiffThreads, smem, st>>>(D, cov_stride);
     }
     return cudaGetLastError();
 }

@@ -102,7 +102,8 @@ struct SceneDev {
 
 // Differentiable batch (rz_diff.cu): images stacked in one canvas, one fill per path.
 struct DiffDev {
-    SceneDev S;
+    SceneDev S;          // lines binned per row (S.band_rows = 1)
+    int32_t cta_rows;    // rows of a CTA (one warp each); divides the image height
     int32_t paths;       // per image
     int32_t segs;        // per path
     int32_t width, height;
