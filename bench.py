@@ -7,11 +7,11 @@ Workload (default, ``glyphs``): 10,000 independent closed glyph outlines,
 and flatness 0.05 (synthetic, seeded; ~1.07 M segments, ~118 Mpx per step).
 One step = one pass of flatten + coverage + fill rule over the whole batch.
 
-* ``value``      Mpx/s with inputs resident in HBM: the batch plan (one
-  persistent-kernel launch replayed from a CUDA graph) launched back to back.
+* ``value``      Mpx/s with inputs resident in HBM: the batch plan (the glyph
+  pipeline's kernels replayed from a CUDA graph) launched back to back.
 * ``e2e``        the same metric through the C ABI with host buffers
   (``rz_mask_batch``, pinned inputs in, masks back to pinned host memory).
-* ``roofline``   the band kernel against the measured HBM copy bandwidth.
+* ``roofline``   one plan launch against the measured HBM copy bandwidth.
 * ``cpu_baseline``  the CPU f64 oracle on a bounded sample, 1 thread.
 
 ``--impl reference`` times the reference's CPU algorithm (the oracle port,
@@ -160,9 +160,9 @@ def scan_launches(n):
 
 
 def plan_kernels(batch):
-    """Our kernels in one glyph-pipeline plan launch: records, walk, the chain-offset scan, emit, cover."""
+    """Our kernels in one glyph-pipeline plan launch: records, walk, the chain-offset scan, emit, paths, cover."""
     slots = batch.n_segments + len(batch.sub_off) - 1
-    return 4 + scan_launches(slots + 1)
+    return 5 + scan_launches(slots + 1)
 
 
 def make_workload(n):
