@@ -433,9 +433,11 @@ __device__ void diff_line(float ax, float ay, float bx, float by, int rows, int 
     }
 }
 
-// Sparse pass over one row (one warp), over the marked words in increasing
-// order (32 at a time, skipping empty bitmask words): the exact integer
-// windings there (the prefix of the marked words; the others are 0),
+// Sparse pass over one row (one warp): the marked pixels in increasing order,
+// 32 at a time, one per lane (lane i takes the marked pixel of rank c + i: its
+// 32-word block by a search over the words' prefix counts, its bit by a
+// select within the word).  Warp scans give the exact integer windings there
+// (the prefix of the marked words; the others are 0),
 // g = dL/dA * a (1 - A) / (1 - a alpha) * dalpha/dw, and the inclusive prefix
 // P of g.  g overwrites the coverage word, P goes to its own row; *tot gets
 // the row's sum.
@@ -447,37 +449,56 @@ __device__ void diff_sparse_row(const DiffDev& D, int wpr, int row, const uint32
     const float* dlrow = D.dl_dimage + (uint64_t)row * W;
     uint32_t wcarry = 0;
     float gcarry = 0.f;
-    // Lane j owns the 32-pixel group w0 + j and walks its marked pixels in
-    // order; only the groups' totals go through warp scans (two per 1024
-    // pixels instead of two per marked group).
     for (int w0 = 0; w0 < wpr; w0 += 32) {
         const uint32_t mine = w0 + lane < wpr ? brow[w0 + lane] : 0u;
-        if (!__any_sync(0xffffffffu, mine != 0u)) continue;
-        const int xb = (w0 + lane) << 5;
-        // the group's winding change, then the winding before it
-        uint32_t dsum = 0;
-        for (uint32_t m = mine; m; m &= m - 1u) dsum += (uint32_t)crow[xb + __ffs(m) - 1];
-        uint32_t wi = dsum;
+        const int cnt = __popc(mine);
+        int incl = cnt;  // marked pixels in words w0 .. w0 + lane
         #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
-            const uint32_t o = __shfl_up_sync(0xffffffffu, wi, off);
-            if (lane >= off) wi += o;
+            const int o = __shfl_up_sync(0xffffffffu, incl, off);
+            if (lane >= off) incl += o;
         }
-        uint32_t wn = wcarry + wi - dsum;
-        wcarry += __shfl_sync(0xffffffffu, wi, 31);
-        // g at every marked pixel and its prefix within the group
-        float gsum = 0.f;
-        for (uint32_t m = mine; m; m &= m - 1u) {
-            const int x = xb + __ffs(m) - 1;
-            wn += (uint32_t)crow[x];  // winding at pixel x
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        const int excl = incl - cnt;
+        for (int c = 0; c < total; c += 32) {
+            const int r = c + lane;
+            // the word holding rank r: the number of words whose inclusive count is <= r
+            int j = 0;
+            #pragma unroll
+            for (int step = 16; step >= 1; step >>= 1) {
+                const int v = __shfl_sync(0xffffffffu, incl, j + step - 1);
+                if (v <= r) j += step;
+            }
+            j = min(j, 31);
+            const uint32_t wbits = __shfl_sync(0xffffffffu, mine, j);
+            int k = r - __shfl_sync(0xffffffffu, excl, j);  // rank within the word
+            int pos = 0;
+            #pragma unroll
+            for (int w = 16; w >= 1; w >>= 1) {
+                const int in = __popc((wbits >> pos) & ((1u << w) - 1u));
+                if (k >= in) {
+                    k -= in;
+                    pos += w;
+                }
+            }
+            const bool live = r < total;
+            const int x = ((w0 + j) << 5) + pos;
+            const uint32_t dep = live ? (uint32_t)crow[x] : 0u;
+            uint32_t wi = dep;
+            #pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t o = __shfl_up_sync(0xffffffffu, wi, off);
+                if (lane >= off) wi += o;
+            }
+            const uint32_t wn = wcarry + wi;  // winding at pixel x
+            wcarry += __shfl_sync(0xffffffffu, wi, 31);
             float gv = 0.f;
-            if (x < W) {
+            if (live && x < W) {
                 const float al = alpha_from_winding_fix(D.rule, (int32_t)wn);
                 if (al >= 1e-6f) {  // pixels the forward skips have no slope
                     float da = 0.f;
                     if (D.rule == 1) {
-                        const int32_t fo =
-                            (int32_t)(((uint32_t)wn + (1u << 22)) & ((1u << 23) - 1u)) - (1 << 22);
+                        const int32_t fo = (int32_t)((wn + (1u << 22)) & ((1u << 23) - 1u)) - (1 << 22);
                         da = fo > 0 ? 1.f : -1.f;
                     } else if (al < 1.f) {
                         da = (int32_t)wn > 0 ? 1.f : -1.f;
@@ -485,20 +506,18 @@ __device__ void diff_sparse_row(const DiffDev& D, int wpr, int row, const uint32
                     if (da != 0.f) gv = dlrow[x] * D.alpha * (1.f - Arow[x]) / (1.f - D.alpha * al) * da;
                 }
             }
-            gsum += gv;
-            crow[x] = __float_as_int(gv);
-            prow[x] = gsum;
+            float gi = gv;
+            #pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const float o = __shfl_up_sync(0xffffffffu, gi, off);
+                if (lane >= off) gi += o;
+            }
+            if (live) {
+                crow[x] = __float_as_int(gv);
+                prow[x] = gcarry + gi;
+            }
+            gcarry += __shfl_sync(0xffffffffu, gi, 31);
         }
-        float gi = gsum;
-        #pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            const float o = __shfl_up_sync(0xffffffffu, gi, off);
-            if (lane >= off) gi += o;
-        }
-        const float gbase = gcarry + (gi - gsum);
-        gcarry += __shfl_sync(0xffffffffu, gi, 31);
-        if (gbase != 0.f)
-            for (uint32_t m = mine; m; m &= m - 1u) prow[xb + __ffs(m) - 1] += gbase;
     }
     if (lane == 0) *tot = gcarry;
 }
