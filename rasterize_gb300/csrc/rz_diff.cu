@@ -72,7 +72,7 @@ __device__ void diff_mark(const Band& B, const VtxQ& a, const VtxQ& b, uint32_t*
     if (ay == by) return;  // no signed height
     const float ylo = fminf(ay, by), yhi = fmaxf(ay, by);
     const int r0 = max((int)floorf(ylo - 0.01f), 0), r1 = min((int)floorf(yhi + 0.01f), B.bh - 1);
-    const float inv = 1.f / (by - ay), dx = bx - ax;
+    const float inv = __fdividef(1.f, by - ay), dx = bx - ax;  // |by - ay| > 0: the marks are widened anyway
     const int cmax = B.width_i + 2;
     for (int r = r0; r <= r1; ++r) {
         const float t0 = fminf(fmaxf(((float)r - 0.01f - ay) * inv, 0.f), 1.f);
@@ -277,10 +277,12 @@ __device__ __forceinline__ Dual dmul(const Dual& a, const Dual& b) {
     for (int k = 0; k < 4; ++k) r.d[k] = fmaf(a.d[k], b.v, a.v * b.d[k]);
     return r;
 }
+// One hardware reciprocal (within 2 ulp) per quotient: the derivatives do not
+// need the correctly rounded division.
 __device__ __forceinline__ Dual ddiv(const Dual& a, const Dual& b) {
     Dual r;
-    r.v = a.v / b.v;
-    const float inv = 1.f / b.v;
+    const float inv = __fdividef(1.f, b.v);
+    r.v = a.v * inv;
     #pragma unroll
     for (int k = 0; k < 4; ++k) r.d[k] = (a.d[k] - r.v * b.d[k]) * inv;
     return r;
@@ -354,7 +356,7 @@ __device__ void diff_row_mean(const CellView& V, int r, int c0, float lo, float 
         shi -= gk * 0.5f * ((b - lo) * (b - lo) - (a - lo) * (a - lo));
         slo -= gk * 0.5f * ((hi - a) * (hi - a) - (hi - b) * (hi - b));
     }
-    const float inv = 1.f / D;
+    const float inv = __fdividef(1.f, D);  // D >= 1e-6
     I = sI * inv;
     dhi = shi * inv * inv;
     dlo = slo * inv * inv;
@@ -503,7 +505,8 @@ __device__ void diff_sparse_row(const DiffDev& D, int wpr, int row, const uint32
                     } else if (al < 1.f) {
                         da = (int32_t)wn > 0 ? 1.f : -1.f;
                     }
-                    if (da != 0.f) gv = dlrow[x] * D.alpha * (1.f - Arow[x]) / (1.f - D.alpha * al) * da;
+                    // 1 - a alpha lies in [1 - a, 1]: the hardware quotient (within 2 ulp) is enough
+                    if (da != 0.f) gv = __fdividef(dlrow[x] * D.alpha * (1.f - Arow[x]), 1.f - D.alpha * al) * da;
                 }
             }
             float gi = gv;
