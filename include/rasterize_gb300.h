@@ -323,11 +323,15 @@ RZ_API rz_status rz_write_image(const uint8_t* rgba8, uint32_t width, uint32_t h
 
 /* ---- batch plans: resident work list + CUDA graph replay ---------------- */
 /* A plan fixes one device-memory batch (batch->memory == RZ_MEM_DEVICE), its
- * output buffer and flatness.  Creating it uploads the work list (bands of
- * rows, longest first) and mask descriptors once; each launch replays a
- * captured CUDA graph (queue reset + one persistent-kernel launch) on the
- * context's stream without any host synchronisation.  The input arrays may be
- * rewritten between launches (same sizes). */
+ * output buffer and flatness.  Creating it sizes the plan's buffers (one pass
+ * over the trees and a host round trip), uploads the work list (bands of rows,
+ * longest first) and mask descriptors once and captures a CUDA graph; each
+ * launch replays the graph (queue reset, record pass, tree walk, vertex offsets,
+ * vertex emission, persistent cover kernel; with RZ_BATCH_KERNEL=bands the
+ * record pass and the band kernel) on the context's stream without any host
+ * synchronisation.  The input arrays may be rewritten between launches (same
+ * sizes); geometry that outgrows the sized buffers is reported as
+ * RZ_ERR_CAPACITY by rz_batch_plan_status, never written past them. */
 typedef struct rz_batch_plan rz_batch_plan;
 RZ_API rz_batch_plan* rz_batch_plan_create(rz_ctx* ctx, const rz_path_batch* batch, double flatness, float* out,
                                            uint64_t out_len, rz_status* status);
@@ -348,11 +352,11 @@ RZ_API void rz_batch_plan_destroy(rz_batch_plan* plan);
  * no pinned or heap allocation and no rz_ctx.  The kernel's scratch is one
  * static 896 KiB device array per GPU (held until the process exits): at most
  * 16384 paths and 65536 row bands per call, larger batches return
- * RZ_ERR_CAPACITY.  The first call on a device does a one-time set-up; make
- * it before any stream capture.  Calls share the array and must not overlap
- * on the GPU; within one process they are serialised by a process-wide lock,
- * across devices too.  The call is synchronous: it returns after its work has
- * finished (it reads the error word). */
+ * RZ_ERR_CAPACITY.  The first call on a device does a one-time set-up.  Calls
+ * share the array and must not overlap on the GPU; within one process they are
+ * serialised by a process-wide lock, across devices too.  The call is
+ * synchronous: it returns after its work has finished (it reads the error
+ * word), so it cannot be captured into a CUDA graph. */
 RZ_API rz_status rz_mask_batch_noalloc(const rz_path_batch* batch, double flatness, float* out, uint64_t out_len,
                                        void* stream);
 
