@@ -759,15 +759,16 @@ __device__ void band_scan8_narrow(const Band& B, int width, float* out, int64_t 
             row4[x >> 2] = make_int4(0, 0, 0, 0);
             row4[(x >> 2) + 1] = make_int4(0, 0, 0, 0);
         }
-        const uint32_t w8[8] = {(uint32_t)v.x, (uint32_t)v.y, (uint32_t)v.z, (uint32_t)v.w,
-                                (uint32_t)u.x, (uint32_t)u.y, (uint32_t)u.z, (uint32_t)u.w};
+        // the spill columns only reach prefixes at or past width, which are not stored
         uint32_t a[8];
-        uint32_t run = 0;
-        #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            run += x + i < width ? w8[i] : 0u;
-            a[i] = run;
-        }
+        a[0] = (uint32_t)v.x;
+        a[1] = a[0] + (uint32_t)v.y;
+        a[2] = a[1] + (uint32_t)v.z;
+        a[3] = a[2] + (uint32_t)v.w;
+        a[4] = a[3] + (uint32_t)u.x;
+        a[5] = a[4] + (uint32_t)u.y;
+        a[6] = a[5] + (uint32_t)u.z;
+        a[7] = a[6] + (uint32_t)u.w;
         uint32_t incl = a[7];
         for (int off = 1; off < L; off <<= 1) {
             const uint32_t t = __shfl_up_sync(0xffffffffu, incl, off, L);
@@ -813,26 +814,16 @@ __device__ void band_scan8(const Band& B, int width, float* out, int64_t row_str
                 row4[x >> 2] = make_int4(0, 0, 0, 0);
                 row4[(x >> 2) + 1] = make_int4(0, 0, 0, 0);
             }
+            // the spill columns (width, width + 1) only reach prefixes at or past width, which are not stored
             uint32_t a[8];
-            if (x + 8 <= width) {
-                a[0] = (uint32_t)v.x;
-                a[1] = a[0] + (uint32_t)v.y;
-                a[2] = a[1] + (uint32_t)v.z;
-                a[3] = a[2] + (uint32_t)v.w;
-                a[4] = a[3] + (uint32_t)u.x;
-                a[5] = a[4] + (uint32_t)u.y;
-                a[6] = a[5] + (uint32_t)u.z;
-                a[7] = a[6] + (uint32_t)u.w;
-            } else {
-                const uint32_t w8[8] = {(uint32_t)v.x, (uint32_t)v.y, (uint32_t)v.z, (uint32_t)v.w,
-                                        (uint32_t)u.x, (uint32_t)u.y, (uint32_t)u.z, (uint32_t)u.w};
-                uint32_t run = 0;
-                #pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    run += x + i < width ? w8[i] : 0u;
-                    a[i] = run;
-                }
-            }
+            a[0] = (uint32_t)v.x;
+            a[1] = a[0] + (uint32_t)v.y;
+            a[2] = a[1] + (uint32_t)v.z;
+            a[3] = a[2] + (uint32_t)v.w;
+            a[4] = a[3] + (uint32_t)u.x;
+            a[5] = a[4] + (uint32_t)u.y;
+            a[6] = a[5] + (uint32_t)u.z;
+            a[7] = a[6] + (uint32_t)u.w;
             uint32_t incl = a[7];
             #pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
