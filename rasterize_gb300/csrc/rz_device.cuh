@@ -336,15 +336,19 @@ __device__ __forceinline__ void sadd(float* p, int v) { atomicAdd(reinterpret_ca
 // difference of the rounded cumulative shares, so every pixel is within one
 // fixed-point unit of the exact share however long the span, and the row
 // receives exactly `d` (the row prefix telescopes).
+// INSIDE: the caller has checked that the line stays more than 0.01 px inside
+// (0, width), so the clamps to the image's columns cannot change anything and
+// are left out.
+template <bool INSIDE = false>
 __device__ __forceinline__ void accumulate_row(const Band& B, int r, int xb, float xa, float xn, int d) {
     const float df = (float)d;
     const float xlo = fminf(xa, xn), xhi = fmaxf(xa, xn);
-    const float x0_floor = fmaxf(floorf(xlo), -(float)xb);
+    const float x0_floor = INSIDE ? floorf(xlo) : fmaxf(floorf(xlo), -(float)xb);
     int x0i = (int)x0_floor;
-    const float x1_ceil = fminf(ceilf(xhi), B.width_f - (float)xb);  // the reference's `width`, relative
+    const float x1_ceil = INSIDE ? ceilf(xhi) : fminf(ceilf(xhi), B.width_f - (float)xb);  // the reference's `width`
     const int x1i = (int)x1_ceil;
     float* row = B.acc + r * B.stride + xb;
-    x0i = min(x0i, B.width_i + 1 - xb);
+    if (!INSIDE) x0i = min(x0i, B.width_i + 1 - xb);
     if (x1i <= x0i + 1) {
         const float xmf = 0.5f * (xa + xn) - x0_floor;
         const int c0 = __float2int_rn(df * (1.f - xmf));
@@ -383,6 +387,7 @@ constexpr int kShortLine = 32;
 // Walks its rows like signed_difference_line (src/rasterize.rs:405-469); the
 // row crossings are interpolated from the exact fixed-point heights, so their
 // x error stays below ~kShortLine * 2^-23 px.
+template <bool INSIDE = false>
 __device__ __forceinline__ void accumulate_piece(const Band& B, int xb, float x0, int32_t q0, float x1, int32_t q1) {
     if (q0 == q1) return;  // no signed coverage (the reference skips |dy| < EPSILON)
     int dir = 1;
@@ -399,7 +404,7 @@ __device__ __forceinline__ void accumulate_piece(const Band& B, int xb, float x0
     const int r0 = qa_all >> COV_SHIFT;
     const int r1 = (qb_all + COV_ONE - 1) >> COV_SHIFT;
     if (r1 == r0 + 1 && qa_all == q0 && qb_all == q1) {  // one row, unclipped: the ends are the crossings
-        accumulate_row(B, r0, xb, x0, x1, dir * (q1 - q0));
+        accumulate_row<INSIDE>(B, r0, xb, x0, x1, dir * (q1 - q0));
         return;
     }
     const float dxq = __fdividef(x1 - x0, (float)(q1 - q0));  // px per fixed-point unit of height (within 2 ulp)
@@ -409,7 +414,7 @@ __device__ __forceinline__ void accumulate_piece(const Band& B, int xb, float x0
         if (!(qa < qb)) continue;
         const float xa = qa == q0 ? x0 : fmaf((float)(qa - q0), dxq, x0);
         const float xn = qb == q1 ? x1 : fmaf((float)(qb - q0), dxq, x0);
-        accumulate_row(B, r, xb, xa, xn, dir * (qb - qa));
+        accumulate_row<INSIDE>(B, r, xb, xa, xn, dir * (qb - qa));
     }
 }
 
@@ -544,7 +549,7 @@ __device__ __forceinline__ bool accumulate_vtx_short(const Band& B, const VtxQ& 
     if (!(xlo > 0.01f && xhi < B.width_f - 0.01f)) return false;
     const int32_t q0 = a.row * COV_ONE + __float2int_rn(a.fy * COV_ONE_F);
     const int32_t q1 = b.row * COV_ONE + __float2int_rn(b.fy * COV_ONE_F);
-    accumulate_piece(B, a.col, x0, q0, x1, q1);
+    accumulate_piece<true>(B, a.col, x0, q0, x1, q1);
     return true;
 }
 
@@ -558,7 +563,7 @@ __device__ __forceinline__ void accumulate_vtx(const Band& B, const VtxQ& a, con
         if (xlo > 0.01f && xhi < B.width_f - 0.01f) {
             const int32_t q0 = a.row * COV_ONE + __float2int_rn(a.fy * COV_ONE_F);
             const int32_t q1 = b.row * COV_ONE + __float2int_rn(b.fy * COV_ONE_F);
-            accumulate_piece(B, a.col, x0, q0, x1, q1);
+            accumulate_piece<true>(B, a.col, x0, q0, x1, q1);
             return;
         }
     }
