@@ -328,7 +328,12 @@ struct Band {
     int width_i;
 };
 
-__device__ __forceinline__ void sadd(float* p, int v) { atomicAdd(reinterpret_cast<int*>(p), v); }
+// Adds v to an accumulation word.  Bands always live in shared memory: a
+// reduction on the shared window (no return value, no generic-address check).
+__device__ __forceinline__ void sadd(float* p, int v) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("red.shared.add.s32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
 
 // Signed height `d` (fixed point) of one row, spread over the pixels the line
 // covers between xa and xn (FP32, relative to integer column xb) as in
