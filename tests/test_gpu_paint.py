@@ -109,3 +109,22 @@ def test_large_path_pipeline(R):
     R.mask(path, Transform.identity(), img, rule)
     ref = O.mask(path, Transform.identity(), rule, 1024, 1024)
     assert_close(img, ref, TOL)
+
+
+def test_scene_many_tall_fills(R):
+    """300 thin fills nearly as tall as the canvas, a few lines each: the line blocks of the flatten and
+    scatter passes span more (fill, band) entries than their shared-memory histograms hold, so the global
+    counting route runs; the canvas must still match the oracle."""
+    from rasterize_gb300 import Scene
+    rng = np.random.default_rng(21)
+    sc = Scene()
+    for i in range(300):
+        x = rng.uniform(2, 1000)
+        y0, y1 = rng.uniform(0, 20), rng.uniform(990, 1020)
+        w = rng.uniform(0.5, 4.0)
+        p = PathBuilder().move_to((x, y0)).line_to((x + w, y0 + 3)).line_to((x + w, y1)).line_to((x, y1 - 2)).close().build()
+        sc.fill(p, LinColor(rng.uniform(0, 1), rng.uniform(0, 1), rng.uniform(0, 1), rng.uniform(0.2, 1.0)))
+    bg = (0.0, 0.0, 0.0, 1.0)
+    gpu = R.render_scene(sc, 1024, 1024, bg=bg)
+    ref = oracle_scene(sc, 1024, 1024, bg=bg)
+    assert_close(gpu, ref, COLOR_TOL)
