@@ -368,17 +368,20 @@ RZ_API rz_status rz_flatten_counts(rz_ctx* ctx, const rz_path* path, const doubl
                             uint32_t* counts, uint64_t cap, uint64_t* n_counts);
 
 /* ------------------------------------------------------------------------
- * Batch autotuner.  Times the persistent batch kernel on the caller's
- * device-memory batch (rendering into `out`) for every candidate band-height
- * cap (16, 32, 64, 128, 256 rows: the work-item shape) and resident CTAs per
- * SM (the occupancy limit and one less), keeps the fastest in the context for
- * later rz_mask_batch / rz_batch_plan_create calls, and reports every entry.
- * rz_set_tuning applies a stored choice (0, 0 restores the defaults).
+ * Batch autotuner.  Times the batch kernels on the caller's device-memory
+ * batch (rendering into `out`) for every candidate band-height cap (16, 32,
+ * 64, 128, 256 rows: the work-item shape) and resident CTAs per SM (the
+ * occupancy limit and one or two less), then, for the glyph pipeline, the
+ * slots each lane of the tree walk takes (1, 2, 4, 8: 32 to 256 segments per
+ * warp) at the fastest shape; keeps the fastest in the context for later
+ * rz_mask_batch / rz_batch_plan_create calls, and reports every entry.
+ * rz_set_tuning applies a stored choice (0, 0, 0 restores the defaults).
  * ------------------------------------------------------------------------ */
 typedef struct rz_tune_entry {
     int32_t band_rows_cap;
     int32_t ctas_per_sm;
-    float ms;  /* median of 3 launches, CUDA events */
+    float ms;            /* median of 3 launches, CUDA events */
+    int32_t walk_slots;  /* slots per lane of the glyph pipeline's tree walk (32 per warp times that); 0: n/a */
 } rz_tune_entry;
 
 typedef struct rz_tune_result {
@@ -386,12 +389,14 @@ typedef struct rz_tune_result {
     int32_t ctas_per_sm;
     float ms;
     uint32_t n_entries;
-    rz_tune_entry entries[16];
+    rz_tune_entry entries[24];
+    int32_t walk_slots;
 } rz_tune_result;
 
 RZ_API rz_status rz_tune_batch(rz_ctx* ctx, const rz_path_batch* batch, double flatness, float* out, uint64_t out_len,
                                rz_tune_result* result);
-RZ_API rz_status rz_set_tuning(rz_ctx* ctx, int32_t band_rows_cap, int32_t ctas_per_sm);
+/* walk_slots 0 keeps the default (4). */
+RZ_API rz_status rz_set_tuning(rz_ctx* ctx, int32_t band_rows_cap, int32_t ctas_per_sm, int32_t walk_slots);
 /* Name of the context's GPU (for keying stored tunings). */
 RZ_API const char* rz_device_name(rz_ctx* ctx);
 

@@ -87,12 +87,13 @@ class RzDiffBatch(ctypes.Structure):
 
 
 class RzTuneEntry(ctypes.Structure):
-    _fields_ = [("band_rows_cap", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("ms", ctypes.c_float)]
+    _fields_ = [("band_rows_cap", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("ms", ctypes.c_float),
+                ("walk_slots", ctypes.c_int32)]
 
 
 class RzTuneResult(ctypes.Structure):
     _fields_ = [("band_rows_cap", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("ms", ctypes.c_float),
-                ("n_entries", ctypes.c_uint32), ("entries", RzTuneEntry * 16)]
+                ("n_entries", ctypes.c_uint32), ("entries", RzTuneEntry * 24), ("walk_slots", ctypes.c_int32)]
 
 
 _lock = threading.Lock()
@@ -142,7 +143,7 @@ _SIGNATURES = {
     "rasterize_backward": (ctypes.c_int32, [P, ctypes.POINTER(RzDiffBatch), ctypes.c_double, P, P, P]),
     "rz_tune_batch": (ctypes.c_int32, [P, ctypes.POINTER(RzPathBatch), ctypes.c_double, P, ctypes.c_uint64,
                                        ctypes.POINTER(RzTuneResult)]),
-    "rz_set_tuning": (ctypes.c_int32, [P, ctypes.c_int32, ctypes.c_int32]),
+    "rz_set_tuning": (ctypes.c_int32, [P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     "rz_device_name": (ctypes.c_char_p, [P]),
 }
 

@@ -147,6 +147,7 @@ struct rz_ctx {
     // batch tuning (rz_tune_batch / rz_set_tuning): band height cap, resident CTAs per SM (0 = occupancy)
     int tune_rows_cap = 256;
     int tune_ctas = 0;
+    int tune_walk = 0;  // slots per lane of the glyph tree walk (0: the default)
     std::string device_name;
     HostBuf h_stage, h_out;
     HostBuf h_plan;   // page-locked mask descriptors and work items of chunked batches
@@ -696,6 +697,7 @@ cudaError_t glyph_setup(const rz::BatchDev& b, rz::GlyphDev& g, DevBuf& recs, De
     if (e != cudaSuccess) return e;
     g = rz::GlyphDev{};
     g.b = b;
+    g.walk_slots = rz::kWalkSlotsDefault;
     g.recs = (rz::GlyphRec*)recs.p;
     g.coefs = (rz::GlyphCoef*)coefs.p;
     g.chain = (uint32_t*)chain.p;
@@ -1463,6 +1465,7 @@ rz_batch_plan* rz_batch_plan_create(rz_ctx* ctx, const rz_path_batch* batch, dou
             rz_batch_plan_destroy(plan);
             return bail(cuda_fail(ctx, e, "plan: glyph pipeline buffers"));
         }
+        if (ctx->tune_walk > 0) plan->g.walk_slots = ctx->tune_walk;
     }
     int32_t* queue = ctrl + 8;
     rz::SceneDev S{};
@@ -2537,11 +2540,55 @@ rz_status tune_glyph(rz_ctx* ctx, const std::vector<rz::MaskDev>& masks, rz::Bat
             st = read_error(ctx);
             if (st) break;
             std::sort(t, t + 3);
-            if (result->n_entries < 16) result->entries[result->n_entries++] = rz_tune_entry{caps[ci], per_sm, t[1]};
+            if (result->n_entries < 24)
+                result->entries[result->n_entries++] = rz_tune_entry{caps[ci], per_sm, t[1], rz::kWalkSlotsDefault};
             if (t[1] < result->ms) {
                 result->ms = t[1];
                 result->band_rows_cap = caps[ci];
                 result->ctas_per_sm = per_sm;
+            }
+        }
+    }
+    // slots per lane of the tree walk (32 times that per warp), at the chosen band shape
+    result->walk_slots = rz::kWalkSlotsDefault;
+    if (st == RZ_OK) {
+        build_items(masks, false, items, result->band_rows_cap, rz::kGlyphBandFloats);
+        const int n = (int)items.items.size();
+        if (ctx->d_items.ensure(std::max(n, 1) * sizeof(rz::WorkItem)) != cudaSuccess ||
+            cudaMemcpyAsync(ctx->d_items.p, items.items.data(), n * sizeof(rz::WorkItem), cudaMemcpyHostToDevice,
+                            ctx->stream) != cudaSuccess)
+            st = RZ_ERR_CUDA;
+        const int grid = std::max(1, std::min(n, ctx->num_sms * result->ctas_per_sm));
+        const int slots[3] = {1, 2, 8};  // 4, the default, was timed above
+        for (int si = 0; si < 3 && st == RZ_OK; ++si) {
+            g.walk_slots = slots[si];
+            float t[3] = {0.f, 0.f, 0.f};
+            for (int rep = 0; rep < 4 && st == RZ_OK; ++rep) {
+                cudaError_t e = cudaEventRecord(e0, ctx->stream);
+                if (e == cudaSuccess) e = glyph_enqueue_flatten(g, (uint32_t*)ctx->g_scan.p, P, ctx->stream);
+                if (e == cudaSuccess) e = cudaMemsetAsync(queue, 0, 4, ctx->stream);
+                if (e == cudaSuccess)
+                    e = rz::launch_glyph_cover(g, (const rz::WorkItem*)ctx->d_items.p, n, queue, grid, ctx->stream);
+                if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->stream);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                if (e != cudaSuccess) {
+                    st = RZ_ERR_CUDA;
+                    break;
+                }
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (rep > 0) t[rep - 1] = ms;  // the first launch warms up
+            }
+            if (st) break;
+            st = read_error(ctx);
+            if (st) break;
+            std::sort(t, t + 3);
+            if (result->n_entries < 24)
+                result->entries[result->n_entries++] =
+                    rz_tune_entry{result->band_rows_cap, result->ctas_per_sm, t[1], slots[si]};
+            if (t[1] < result->ms) {
+                result->ms = t[1];
+                result->walk_slots = slots[si];
             }
         }
     }
@@ -2554,6 +2601,7 @@ rz_status tune_glyph(rz_ctx* ctx, const std::vector<rz::MaskDev>& masks, rz::Bat
     }
     ctx->tune_rows_cap = result->band_rows_cap;
     ctx->tune_ctas = result->ctas_per_sm;
+    ctx->tune_walk = result->walk_slots;
     return RZ_OK;
 }
 
@@ -2572,13 +2620,15 @@ const char* rz_device_name(rz_ctx* ctx) {
     return ctx->device_name.c_str();
 }
 
-rz_status rz_set_tuning(rz_ctx* ctx, int32_t band_rows_cap, int32_t ctas_per_sm) {
+rz_status rz_set_tuning(rz_ctx* ctx, int32_t band_rows_cap, int32_t ctas_per_sm, int32_t walk_slots) {
     if (!ctx) return RZ_ERR_INVALID;
     std::lock_guard<std::mutex> lock(ctx->mu);
-    if (band_rows_cap < 0 || band_rows_cap > 256 || ctas_per_sm < 0 || ctas_per_sm > 32)
-        return fail(ctx, RZ_ERR_INVALID, "band_rows_cap must be 0..256 and ctas_per_sm 0..32");
+    if (band_rows_cap < 0 || band_rows_cap > 256 || ctas_per_sm < 0 || ctas_per_sm > 32 || walk_slots < 0 ||
+        walk_slots > 16)
+        return fail(ctx, RZ_ERR_INVALID, "band_rows_cap must be 0..256, ctas_per_sm 0..32 and walk_slots 0..16");
     ctx->tune_rows_cap = band_rows_cap ? band_rows_cap : 256;
     ctx->tune_ctas = ctas_per_sm;
+    ctx->tune_walk = walk_slots;
     return RZ_OK;
 }
 
@@ -2659,7 +2709,7 @@ rz_status rz_tune_batch(rz_ctx* ctx, const rz_path_batch* batch, double flatness
             st = read_error(ctx);
             if (st) break;
             std::sort(t, t + 3);
-            if (result->n_entries < 16) result->entries[result->n_entries++] = rz_tune_entry{caps[ci], per_sm, t[1]};
+            if (result->n_entries < 24) result->entries[result->n_entries++] = rz_tune_entry{caps[ci], per_sm, t[1], 0};
             if (t[1] < result->ms) {
                 result->ms = t[1];
                 result->band_rows_cap = caps[ci];

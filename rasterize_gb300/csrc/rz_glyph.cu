@@ -102,17 +102,18 @@ __global__ void __launch_bounds__(256) k_glyph_records(GlyphDev g) {
     }
 }
 
-// Each lane walks the trees of kWalkPerLane slots one after the other in one
+// Each lane walks the trees of g.walk_slots slots one after the other in one
 // flat loop (a lane that finishes a tree starts its next slot while the other
 // lanes keep deciding), so the warp's lanes stay busy however uneven the
 // trees.  The next slot's record is loaded while the current tree is walked.
-constexpr int kWalkPerLane = 4;
+// The number of slots per lane (segments per warp / 32) is tuned per batch.
 
 __global__ void __launch_bounds__(256) k_glyph_walk(GlyphDev g) {
     const BatchDev& b = g.b;
     const uint32_t n = b.n_segments + b.n_subpaths;
     const uint32_t warp = (blockIdx.x * 256u + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
-    const uint32_t first = warp * 32u * kWalkPerLane + lane;
+    const int per_lane = g.walk_slots;
+    const uint32_t first = warp * 32u * (uint32_t)per_lane + lane;
     int fallbacks = 0;
     int s = 0;            // index in the lane's list of the slot held in `next`
     uint32_t j = 0;       // slot being walked
@@ -137,10 +138,10 @@ __global__ void __launch_bounds__(256) k_glyph_walk(GlyphDev g) {
             // take the prefetched slot and prefetch the one after it; slots that are not fixed-point
             // records have empty chains
             for (;;) {
-                if (s >= kWalkPerLane) break;
+                if (s >= per_lane) break;
                 j = first + 32u * (uint32_t)s;
                 if (j >= n) {
-                    s = kWalkPerLane;
+                    s = per_lane;
                     break;
                 }
                 const uint32_t tag = ntag;
@@ -148,7 +149,7 @@ __global__ void __launch_bounds__(256) k_glyph_walk(GlyphDev g) {
                 const GlyphCoef c = nc;
                 ++s;
                 const uint32_t jn = first + 32u * (uint32_t)s;
-                if (s < kWalkPerLane && jn < n) {
+                if (s < per_lane && jn < n) {
                     const GlyphRec gr = g.recs[jn];
                     nrec = gr.rec;
                     ntag = gr.tag;
@@ -528,7 +529,7 @@ cudaError_t launch_glyph_walk(const GlyphDev& g, cudaStream_t st) {
     k_glyph_records<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    const uint64_t per_block = 256ull * kWalkPerLane;
+    const uint64_t per_block = 256ull * (uint64_t)g.walk_slots;
     k_glyph_walk<<<(unsigned)((n + per_block - 1) / per_block), 256, 0, st>>>(g);
     return cudaGetLastError();
 }

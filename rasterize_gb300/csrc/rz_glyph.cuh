@@ -37,7 +37,10 @@ struct GlyphDev {
     int4* vtx;                 // [vtx_cap] chain vertices
     uint32_t vtx_cap;
     void* paths;               // [n_paths] per-path descriptors of the cover items (glyph_path_bytes() each)
+    int32_t walk_slots;        // slots each lane of the tree walk takes (1..16; 32 of them per warp)
 };
+
+constexpr int kWalkSlotsDefault = 4;
 
 cudaError_t init_glyph_kernels();
 int glyph_cover_occupancy();

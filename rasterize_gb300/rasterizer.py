@@ -627,14 +627,17 @@ class GpuRasterizer(Rasterizer):
             table = {}
         if not retune and key in table:
             e = table[key]
-            self.ctx.check(lib.rz_set_tuning(self.ctx.ptr, int(e["band_rows_cap"]), int(e["ctas_per_sm"])))
+            self.ctx.check(lib.rz_set_tuning(self.ctx.ptr, int(e["band_rows_cap"]), int(e["ctas_per_sm"]),
+                                             int(e.get("walk_slots", 0))))
             return dict(e, cached=True)
         s = batch.struct(_ffi.RZ_MEM_DEVICE, device_ptrs)
         res = _ffi.RzTuneResult()
         self.ctx.check(lib.rz_tune_batch(self.ctx.ptr, ctypes.byref(s), self.flatness, out_ptr, batch.out_len,
                                          ctypes.byref(res)))
-        entry = {"band_rows_cap": res.band_rows_cap, "ctas_per_sm": res.ctas_per_sm, "ms": res.ms,
-                 "candidates": [[e.band_rows_cap, e.ctas_per_sm, e.ms] for e in res.entries[:res.n_entries]]}
+        entry = {"band_rows_cap": res.band_rows_cap, "ctas_per_sm": res.ctas_per_sm, "walk_slots": res.walk_slots,
+                 "ms": res.ms,
+                 "candidates": [[e.band_rows_cap, e.ctas_per_sm, e.walk_slots, e.ms]
+                                for e in res.entries[:res.n_entries]]}
         table[key] = entry
         try:
             os.makedirs(os.path.dirname(path), exist_ok=True)
@@ -646,8 +649,9 @@ class GpuRasterizer(Rasterizer):
             pass
         return dict(entry, cached=False)
 
-    def set_tuning(self, band_rows_cap: int = 0, ctas_per_sm: int = 0) -> None:
-        self.ctx.check(self.ctx.lib.rz_set_tuning(self.ctx.ptr, int(band_rows_cap), int(ctas_per_sm)))
+    def set_tuning(self, band_rows_cap: int = 0, ctas_per_sm: int = 0, walk_slots: int = 0) -> None:
+        self.ctx.check(self.ctx.lib.rz_set_tuning(self.ctx.ptr, int(band_rows_cap), int(ctas_per_sm),
+                                                  int(walk_slots)))
 
     # ---- differentiable batch (device pointers)
     def diff_forward(self, batch: DiffBatch, image_ptr: int) -> None:

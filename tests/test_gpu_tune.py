@@ -36,6 +36,9 @@ def test_tune_applies_and_caches(tmp_path):
     assert not res["cached"] and res["ms"] > 0
     assert [res["band_rows_cap"], res["ctas_per_sm"]] in [c[:2] for c in res["candidates"]]
     assert len(res["candidates"]) >= 5
+    # the glyph pipeline's walk: slots per lane tried at the chosen band shape
+    assert res["walk_slots"] in (1, 2, 4, 8)
+    assert {c[2] for c in res["candidates"]} >= {1, 2, 4, 8}
     out.zero_()
     R.mask_batch_device(batch, ptrs, out.data_ptr())  # under the tuned shape
     torch.cuda.synchronize()
@@ -52,5 +55,30 @@ def test_set_tuning_rejects_bad_values():
     R = GpuRasterizer()
     with pytest.raises(RasterizeError):
         R.set_tuning(1000, 0)
-    R.set_tuning(32, 2)
+    with pytest.raises(RasterizeError):
+        R.set_tuning(0, 0, 17)
+    R.set_tuning(32, 2, 2)
     R.set_tuning(0, 0)
+
+
+def test_walk_slots_render_the_same():
+    """Slots per lane of the glyph pipeline's tree walk only change which lane walks which tree: plans made
+    under every setting render the same masks, bit for bit."""
+    R = GpuRasterizer()
+    batch, ptrs, out, _keep = device_batch(n=500, seed=17)
+    results = []
+    try:
+        for w in (0, 1, 2, 8, 16):
+            R.set_tuning(0, 0, w)
+            out.fill_(-1.0)
+            plan = R.plan(batch, ptrs, out.data_ptr())
+            try:
+                plan.launch()
+                plan.status()
+            finally:
+                plan.close()
+            results.append(out.cpu().numpy().copy())
+    finally:
+        R.set_tuning(0, 0)
+    for r in results[1:]:
+        assert np.array_equal(r, results[0])
