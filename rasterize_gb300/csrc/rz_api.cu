@@ -1741,13 +1741,20 @@ void adaptive_tasks(HostScene& hs, double flatness) {
     hs.task_off[hs.n_slots] = acc;
 }
 
+// CTAs per SM of the paint composite: its blends wait on L2 round trips, so
+// more resident warps hide them (at the cost of shorter bands).
+#ifndef RZ_PAINT_CTAS
+#define RZ_PAINT_CTAS 3
+#endif
+
 int choose_band_rows(int canvas_w, int canvas_h, bool paint_mode, int num_sms) {
     const int stride = rz::band_stride(canvas_w);
     const int per_row = 4 * stride;  // the coverage band (colours stay in the canvas)
-    // coverage only: tall bands (one CTA per SM) amortise a line's per-band set-up; with paint, two CTAs per SM
-    const int rmax = std::max(1, std::min(std::min((paint_mode ? 100 * 1024 : 208 * 1024) / per_row, 64),
-                                          std::max(canvas_h, 1)));
-    const int64_t slots = (int64_t)std::max(num_sms, 1) * (paint_mode ? 2 : 1);
+    // coverage only: tall bands (one CTA per SM) amortise a line's per-band set-up; with paint, RZ_PAINT_CTAS
+    // CTAs per SM
+    const int budget = paint_mode ? 200 * 1024 / RZ_PAINT_CTAS : 208 * 1024;
+    const int rmax = std::max(1, std::min(std::min(budget / per_row, 64), std::max(canvas_h, 1)));
+    const int64_t slots = (int64_t)std::max(num_sms, 1) * (paint_mode ? RZ_PAINT_CTAS : 1);
     // the band kernel runs in waves of `slots` bands: the height whose waves cost least, counting each band's
     // rows plus a fixed share for the lines that cross its edges
     int best = rmax;

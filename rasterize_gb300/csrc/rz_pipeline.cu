@@ -752,8 +752,8 @@ static __device__ __noinline__ void composite_slow_line(const SceneDev& S, const
                       (double)b.row + (double)b.fy);
 }
 
-// THREADS: 512 for masks (one CTA per SM), 256 with paint (two CTAs per SM,
-// so one CTA blends while the other accumulates).  With paint the band's
+// THREADS: 512 for masks (one CTA per SM), 256 with paint (three CTAs per SM:
+// while one CTA's blends wait on L2, the others accumulate or blend).  With paint the band's
 // colours stay in the canvas itself (L2-resident while the band is worked
 // on): only the coverage band takes shared memory, so bands are tall and the
 // per-fill work of a band covers many rows.
