@@ -215,6 +215,10 @@ __device__ inline FlatCoef flat_coef(const Seg64& s) {
 // 1 = leaf, 0 = split, -1 = too close to call (re-decide in binary64).
 // qerr bounds |a2 - a2_true| and |a3 - a3_true| (px) when the coefficients
 // come from rounded inputs.
+// FINITE: the coefficients are known to be finite and bounded (fixed-point
+// records: |a2|, |a3| < 2^18 px, so G and E stay finite; an infinite td only
+// says what the exact comparison says), and the checks are left out.
+template <bool FINITE = false>
 __device__ inline int decide_fp32(int kind, const FlatCoef& c, int d, uint32_t k, float thr32, float qerr) {
     const float h = pow2f(-d);
     const float td = thr32 * pow2f(4 * d);     // thr * 16^d, exact power-of-two scaling
@@ -236,7 +240,7 @@ __device__ inline int decide_fp32(int kind, const FlatCoef& c, int d, uint32_t k
     // 2^-22 to cover the rounding of the square and of a correctly rounded root)
     const float wx = fmaxf(fabsf(wux), fabsf(wvx)) * 1.00000024f, wy = fmaxf(fabsf(wuy), fabsf(wvy)) * 1.00000024f;
     const float E = (2.f * wx + bx) * bx + (2.f * wy + by) * by + G * e19;
-    if (isfinite(G) && isfinite(E) && isfinite(td)) {
+    if (FINITE || (isfinite(G) && isfinite(E) && isfinite(td))) {
         if (G + E < td) return 1;
         if (G - E >= td) return 0;
     }
@@ -1152,7 +1156,7 @@ __device__ __forceinline__ int decide_node(const SegRec& r, const FlatCoef& c, f
                                            float thr32, double thr64, const double* pts, const double* trm,
                                            int& fallbacks) {
     if (r.kind == SEG_LINE) return 1;
-    const int v = decide_fp32(r.kind, c, d, k, thr32, qerr);
+    const int v = decide_fp32<true>(r.kind, c, d, k, thr32, qerr);
     if (v >= 0) return v;
     Seg64 S;
     S.kind = r.kind;
