@@ -805,7 +805,8 @@ def main():
         "gpu_launches": plan_kernels(batch) * args.steps,
         "clocks": clk,
         "configs": configs,
-        "tuning": {k: tuning[k] for k in ("band_rows_cap", "ctas_per_sm", "ms", "cached", "candidates") if k in tuning},
+        "tuning": {k: tuning[k] for k in ("band_rows_cap", "ctas_per_sm", "walk_slots", "ms", "cached", "candidates")
+                   if k in tuning},
     }
     print(json.dumps(out))
 
