@@ -65,8 +65,9 @@ constexpr int kDiffThreads = 256;
 // Marks a superset of the accumulation words that accumulate_vtx writes for
 // the line a -> b: in every band row the line reaches (rows widened by 0.01),
 // its x range there clamped to [0, width] like the x rules, one word more on
-// each side and the carry word after it.
-__device__ void diff_mark(const Band& B, const VtxQ& a, const VtxQ& b, uint32_t* bits, int wpr) {
+// each side and the carry word after it.  Widens [lo, hi] to the marked
+// columns.
+__device__ void diff_mark(const Band& B, const VtxQ& a, const VtxQ& b, uint32_t* bits, int wpr, int& lo, int& hi) {
     const float ax = (float)a.col + a.fx, bx = (float)b.col + b.fx;
     const float ay = (float)a.row + a.fy, by = (float)b.row + b.fy;
     if (ay == by) return;  // no signed height
@@ -81,6 +82,8 @@ __device__ void diff_mark(const Band& B, const VtxQ& a, const VtxQ& b, uint32_t*
         const float xl = fminf(fmaxf(fminf(x0, x1), 0.f), B.width_f);
         const float xh = fminf(fmaxf(fmaxf(x0, x1), 0.f), B.width_f);
         const int c0 = max((int)floorf(xl) - 1, 0), c1 = min((int)floorf(xh) + 2, cmax);
+        lo = min(lo, c0);
+        hi = max(hi, c1);
         uint32_t* row = bits + r * wpr;
         for (int w = c0 >> 5; w <= (c1 >> 5); ++w) {
             const int lo = max(c0 - (w << 5), 0), hi = min(c1 - (w << 5), 31);
@@ -90,30 +93,34 @@ __device__ void diff_mark(const Band& B, const VtxQ& a, const VtxQ& b, uint32_t*
     }
 }
 
-// Clears the band words of a row past the scanned columns (lines write up to
-// column width + 1).
-__device__ __forceinline__ void clear_row_tail(int4* row4, int width, int stride, int lane) {
-    for (int c = ((width + 3) & ~3) + 4 * lane; c < stride; c += 128) row4[c >> 2] = make_int4(0, 0, 0, 0);
-}
-
 // ---------------------------------------------------------------------------
 // Forward
 // ---------------------------------------------------------------------------
-// Row prefix of one band row (clearing it as it reads), fill rule, and
+// Widens [lo, hi] to the columns the accumulation of the line a -> b can
+// write in its band row: the line's x range clamped to [0, width] like the x
+// rules, one column more on the left and two on the right (the pixel after
+// the last covered one takes the rest of the row's height; FP32 rounding of
+// the ends stays far below a column).
+__device__ __forceinline__ void line_cols(const Band& B, const VtxQ& a, const VtxQ& b, int& lo, int& hi) {
+    const float ax = (float)a.col + a.fx, bx = (float)b.col + b.fx;
+    const float xl = fminf(fmaxf(fminf(ax, bx), 0.f), B.width_f);
+    const float xh = fminf(fmaxf(fmaxf(ax, bx), 0.f), B.width_f);
+    lo = min(lo, max((int)floorf(xl) - 1, 0));
+    hi = max(hi, min((int)floorf(xh) + 2, B.width_i + 2));
+}
+
 // A += a alpha (1 - A) for the pixels the fill does not skip (|alpha| < 1e-6,
-// src/rasterize.rs:347-349).  One warp, 4 pixels per lane.
-// One 128-pixel step of the blend: windings base + a_i of the lane's 4 pixels.
-__device__ __forceinline__ void diff_blend4(float* Arow, int x, int width, bool vec, int rule, float alpha,
-                                            uint32_t base, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3) {
-    const uint32_t wv[4] = {base + a0, base + a1, base + a2, base + a3};
+// src/rasterize.rs:347-349): the lane's 4 pixels at x, windings w[0..3].
+template <int RULE>
+__device__ __forceinline__ void diff_blend4(float* Arow, int x, int width, bool vec, float alpha, const uint32_t (&w)[4]) {
     if (vec && x < width) {
-        // four pixels at once; an alpha below 1e-6 leaves the pixel as it is (fma with 0 is exact)
+        // four pixels at once; a skipped pixel takes fma(0, 1 - A, A) = A exactly
         float4 dv = *reinterpret_cast<const float4*>(Arow + x);
         float* d = reinterpret_cast<float*>(&dv);
         #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            const float al = alpha_from_winding_fix(rule, (int32_t)wv[i]);
-            d[i] = fmaf(al < 1e-6f ? 0.f : alpha * al, 1.f - d[i], d[i]);
+            const float al = alpha_fix<RULE>(w[i]);  // NonZero: 0 below 1e-6 already
+            d[i] = fmaf(RULE == 1 && al < 1e-6f ? 0.f : alpha * al, 1.f - d[i], d[i]);
         }
         *reinterpret_cast<float4*>(Arow + x) = dv;
         return;
@@ -121,55 +128,82 @@ __device__ __forceinline__ void diff_blend4(float* Arow, int x, int width, bool 
     #pragma unroll
     for (int i = 0; i < 4; ++i) {
         if (x + i >= width) break;
-        const float al = alpha_from_winding_fix(rule, (int32_t)wv[i]);
+        const float al = alpha_fix<RULE>(w[i]);
         if (al < 1e-6f) continue;
         float& d = Arow[x + i];
         d = fmaf(alpha * al, 1.f - d, d);
     }
 }
 
-// Row prefix over kScanSteps 128-pixel steps at a time: the steps' warp
-// scans are independent, so their shuffles interleave instead of forming one
+// STEPS 128-pixel steps of the row prefix from column x0 (clearing the words
+// it reads below x_end), the fill rule and the blend.  The steps' warp scans
+// are independent, so their shuffles interleave instead of forming one
 // dependent chain per step; the carry then runs over the steps in order.
-constexpr int kScanSteps = 4;
+// Columns at or past `width` (lines write up to width + 2) are cleared but
+// take no part in the prefix.
+template <int RULE, int STEPS>
+__device__ __forceinline__ void diff_scan_steps(int4* row4, int x0, int x_end, int width, bool vec, float alpha,
+                                                float* Arow, uint32_t& carry, int lane) {
+    uint32_t a[STEPS][4], incl[STEPS];
+    #pragma unroll
+    for (int g = 0; g < STEPS; ++g) {
+        const int x = x0 + 128 * g + 4 * lane;
+        int4 v = make_int4(0, 0, 0, 0);
+        if (x < x_end) {
+            v = row4[x >> 2];
+            row4[x >> 2] = make_int4(0, 0, 0, 0);
+        }
+        a[g][0] = x < width ? (uint32_t)v.x : 0u;
+        a[g][1] = a[g][0] + (x + 1 < width ? (uint32_t)v.y : 0u);
+        a[g][2] = a[g][1] + (x + 2 < width ? (uint32_t)v.z : 0u);
+        a[g][3] = a[g][2] + (x + 3 < width ? (uint32_t)v.w : 0u);
+        incl[g] = a[g][3];
+    }
+    #pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        #pragma unroll
+        for (int g = 0; g < STEPS; ++g) {
+            const uint32_t o = __shfl_up_sync(0xffffffffu, incl[g], off);
+            if (lane >= off) incl[g] += o;
+        }
+    }
+    #pragma unroll
+    for (int g = 0; g < STEPS; ++g) {
+        const uint32_t base = carry + incl[g] - a[g][3];
+        carry += __shfl_sync(0xffffffffu, incl[g], 31);
+        const uint32_t w[4] = {base + a[g][0], base + a[g][1], base + a[g][2], base + a[g][3]};
+        diff_blend4<RULE>(Arow, x0 + 128 * g + 4 * lane, width, vec, alpha, w);
+    }
+}
 
-__device__ void diff_scan_blend_row(float* crow, int stride, int width, int rule, float alpha, float* Arow, int lane) {
+// Row prefix of one band row over the columns [lo, hi] that the path's lines
+// wrote (clearing them as it reads), fill rule and blend.  The winding is 0
+// before lo (nothing to blend) and constant after hi: the rest of the row
+// takes one alpha, blended only if the fill keeps it.  One warp, 4 pixels per
+// lane per step.
+template <int RULE>
+__device__ void diff_scan_blend_span(float* crow, int width, float alpha, float* Arow, int lo, int hi, int lane) {
     int4* row4 = reinterpret_cast<int4*>(crow);
     uint32_t carry = 0;
     const bool vec = (width & 3) == 0;  // rows of A are 16-byte aligned: whole float4 chunks
-    for (int x0 = 0; x0 < width; x0 += 128 * kScanSteps) {
-        uint32_t a0[kScanSteps], a1[kScanSteps], a2[kScanSteps], a3[kScanSteps], incl[kScanSteps];
-        #pragma unroll
-        for (int g = 0; g < kScanSteps; ++g) {
-            const int x = x0 + 128 * g + 4 * lane;
-            int4 v = make_int4(0, 0, 0, 0);
-            if (x < width) {
-                v = row4[x >> 2];
-                row4[x >> 2] = make_int4(0, 0, 0, 0);
-            }
-            a0[g] = (uint32_t)v.x;
-            a1[g] = a0[g] + (x + 1 < width ? (uint32_t)v.y : 0u);
-            a2[g] = a1[g] + (x + 2 < width ? (uint32_t)v.z : 0u);
-            a3[g] = a2[g] + (x + 3 < width ? (uint32_t)v.w : 0u);
-            incl[g] = a3[g];
-        }
-        #pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            #pragma unroll
-            for (int g = 0; g < kScanSteps; ++g) {
-                const uint32_t o = __shfl_up_sync(0xffffffffu, incl[g], off);
-                if (lane >= off) incl[g] += o;
-            }
-        }
-        #pragma unroll
-        for (int g = 0; g < kScanSteps; ++g) {
-            const uint32_t base = carry + incl[g] - a3[g];
-            carry += __shfl_sync(0xffffffffu, incl[g], 31);
-            if (x0 + 128 * g < width)
-                diff_blend4(Arow, x0 + 128 * g + 4 * lane, width, vec, rule, alpha, base, a0[g], a1[g], a2[g], a3[g]);
-        }
+    const int x_end = hi + 1;           // < the row stride (width + 3 at least)
+    int x0 = lo & ~3;
+    while (x_end - x0 > 384) {
+        diff_scan_steps<RULE, 4>(row4, x0, x_end, width, vec, alpha, Arow, carry, lane);
+        x0 += 512;
     }
-    clear_row_tail(row4, width, stride, lane);
+    if (x_end - x0 > 128) {
+        diff_scan_steps<RULE, 2>(row4, x0, x_end, width, vec, alpha, Arow, carry, lane);
+        x0 += 256;
+    }
+    if (x_end - x0 > 0) {
+        diff_scan_steps<RULE, 1>(row4, x0, x_end, width, vec, alpha, Arow, carry, lane);
+        x0 += 128;
+    }
+    if (x0 >= width) return;
+    const float al = alpha_fix<RULE>(carry);
+    if (al < 1e-6f) return;
+    for (int x = x0 + lane; x < width; x += 32) Arow[x] = fmaf(alpha * al, 1.f - Arow[x], Arow[x]);
 }
 
 // The line lists of canvas row `band` (lists are binned per row) of paths
@@ -213,8 +247,9 @@ __device__ __forceinline__ bool line_reaches_row(const VtxQ& a, const VtxQ& b) {
 // One warp per band row, with no block barrier after the start: rows are
 // independent (a line writes only its own rows' words), so each warp takes
 // every path's lines that reach its row, accumulates them into its row
-// (int32 shared atomics), then scans and blends the row.
-__global__ void __launch_bounds__(kDiffThreads, 4) k_diff_forward(DiffDev D, int cov_stride) {
+// (int32 shared atomics), then scans and blends the columns they wrote.
+template <int RULE>
+__global__ void __launch_bounds__(kDiffThreads, 3) k_diff_forward(DiffDev D, int cov_stride) {
     extern __shared__ float4 sm4[];
     float* cov = reinterpret_cast<float*>(sm4);
     const SceneDev& S = D.S;
@@ -239,17 +274,19 @@ __global__ void __launch_bounds__(kDiffThreads, 4) k_diff_forward(DiffDev D, int
         const int q = __ffs(todo) - 1;
         todo &= todo - 1u;
         const uint32_t n = __shfl_sync(0xffffffffu, my_n, q), start = __shfl_sync(0xffffffffu, my_start, q);
-        bool any = false;
+        int lo = D.width + 2, hi = -1;  // the columns written
         for (uint32_t j = lane; j < n; j += 32) {
             const uint32_t l = S.pairs[start + j];
             const VtxQ a = line_vtx(S.lines[2ull * l], B.y0), b = line_vtx(S.lines[2ull * l + 1], B.y0);
             if (!line_reaches_row(a, b)) continue;
-            any = true;
+            line_cols(B, a, b, lo, hi);
             accumulate_vtx(B, a, b);
         }
-        if (!__any_sync(0xffffffffu, any)) continue;  // no crossing in this row: the winding is 0 along it
+        hi = __reduce_max_sync(0xffffffffu, hi);
+        if (hi < 0) continue;  // no crossing in this row: the winding is 0 along it
+        lo = __reduce_min_sync(0xffffffffu, lo);
         __syncwarp();
-        diff_scan_blend_row(crow, cov_stride, D.width, D.rule, D.alpha, Arow, lane);
+        diff_scan_blend_span<RULE>(crow, D.width, D.alpha, Arow, lo, hi, lane);
         __syncwarp();
       }
     }
@@ -435,7 +472,8 @@ __device__ void diff_line(float ax, float ay, float bx, float by, int rows, int 
     }
 }
 
-// Sparse pass over one row (one warp): the marked pixels in increasing order,
+// Sparse pass over the words wlo..whi of one row (one warp; no other word
+// holds a mark): the marked pixels in increasing order,
 // 32 at a time, one per lane (lane i takes the marked pixel of rank c + i: its
 // 32-word block by a search over the words' prefix counts, its bit by a
 // select within the word).  Warp scans give the exact integer windings there
@@ -443,7 +481,8 @@ __device__ void diff_line(float ax, float ay, float bx, float by, int rows, int 
 // g = dL/dA * a (1 - A) / (1 - a alpha) * dalpha/dw, and the inclusive prefix
 // P of g.  g overwrites the coverage word, P goes to its own row; *tot gets
 // the row's sum.
-__device__ void diff_sparse_row(const DiffDev& D, int wpr, int row, const uint32_t* brow, float* cov_row,
+template <int RULE>
+__device__ void diff_sparse_row(const DiffDev& D, int wlo, int whi, int row, const uint32_t* brow, float* cov_row,
                                 float* prow, float* tot, int lane) {
     const int W = D.width;
     int32_t* crow = reinterpret_cast<int32_t*>(cov_row);
@@ -451,8 +490,8 @@ __device__ void diff_sparse_row(const DiffDev& D, int wpr, int row, const uint32
     const float* dlrow = D.dl_dimage + (uint64_t)row * W;
     uint32_t wcarry = 0;
     float gcarry = 0.f;
-    for (int w0 = 0; w0 < wpr; w0 += 32) {
-        const uint32_t mine = w0 + lane < wpr ? brow[w0 + lane] : 0u;
+    for (int w0 = wlo; w0 <= whi; w0 += 32) {
+        const uint32_t mine = w0 + lane <= whi ? brow[w0 + lane] : 0u;
         const int cnt = __popc(mine);
         int incl = cnt;  // marked pixels in words w0 .. w0 + lane
         #pragma unroll
@@ -496,10 +535,10 @@ __device__ void diff_sparse_row(const DiffDev& D, int wpr, int row, const uint32
             wcarry += __shfl_sync(0xffffffffu, wi, 31);
             float gv = 0.f;
             if (live && x < W) {
-                const float al = alpha_from_winding_fix(D.rule, (int32_t)wn);
+                const float al = alpha_fix<RULE>(wn);
                 if (al >= 1e-6f) {  // pixels the forward skips have no slope
                     float da = 0.f;
-                    if (D.rule == 1) {
+                    if (RULE == 1) {
                         const int32_t fo = (int32_t)((wn + (1u << 22)) & ((1u << 23) - 1u)) - (1 << 22);
                         da = fo > 0 ? 1.f : -1.f;
                     } else if (al < 1.f) {
@@ -531,6 +570,7 @@ __device__ void diff_sparse_row(const DiffDev& D, int wpr, int row, const uint32
 // row, marking the words they write, runs the sparse row pass, differentiates
 // its row's share of every line and chains it to the control points, then
 // clears the marked words.
+template <int RULE>
 __global__ void __launch_bounds__(kDiffThreads, 3) k_diff_backward(DiffDev D, int cov_stride) {
     extern __shared__ float4 sm4[];
     const SceneDev& S = D.S;
@@ -561,18 +601,21 @@ __global__ void __launch_bounds__(kDiffThreads, 3) k_diff_backward(DiffDev D, in
         const int q = __ffs(todo) - 1;
         todo &= todo - 1u;
         const uint32_t n = __shfl_sync(0xffffffffu, my_n, q), start = __shfl_sync(0xffffffffu, my_start, q);
-        bool any = false;
+        int lo = D.width + 2, hi = -1;  // the marked columns
         for (uint32_t j = lane; j < n; j += 32) {
             const uint32_t l = S.pairs[start + j];
             const VtxQ a = line_vtx(S.lines[2ull * l], B.y0), b = line_vtx(S.lines[2ull * l + 1], B.y0);
             if (!line_reaches_row(a, b)) continue;
-            any = true;
             accumulate_vtx(B, a, b);
-            diff_mark(B, a, b, brow, wpr);
+            diff_mark(B, a, b, brow, wpr, lo, hi);
         }
-        if (!__any_sync(0xffffffffu, any)) continue;  // nothing written in this row, nothing to move
+        // nothing marked: nothing written in this row, g is 0 along it and no line moves the loss
+        hi = __reduce_max_sync(0xffffffffu, hi);
+        if (hi < 0) continue;
+        lo = __reduce_min_sync(0xffffffffu, lo);
+        const int wlo = lo >> 5, whi = hi >> 5;
         __syncwarp();
-        diff_sparse_row(D, wpr, row, brow, crow, prow, tot + warp, lane);
+        diff_sparse_row<RULE>(D, wlo, whi, row, brow, crow, prow, tot + warp, lane);
         __syncwarp();
         const CellView V{brow, crow, prow, tot + warp, wpr, cov_stride, D.width};
         for (uint32_t j = lane; j < n; j += 32) {
@@ -599,23 +642,15 @@ __global__ void __launch_bounds__(kDiffThreads, 3) k_diff_backward(DiffDev D, in
             const float b1[4] = {u1 * u1 * u1, 3.f * t1 * u1 * u1, 3.f * t1 * t1 * u1, t1 * t1 * t1};
             float2* o = out + path * 3ull * D.segs;
             #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                atomicAdd(&o[idx[q]].x, d4[0] * b0[q] + d4[2] * b1[q]);
-                atomicAdd(&o[idx[q]].y, d4[1] * b0[q] + d4[3] * b1[q]);
-            }
+            for (int q = 0; q < 4; ++q)
+                atomicAdd(&o[idx[q]], make_float2(d4[0] * b0[q] + d4[2] * b1[q], d4[1] * b0[q] + d4[3] * b1[q]));
         }
         __syncwarp();
-        // clear the marked words and the bitmask
-        for (int w = lane; w < wpr; w += 32) {
-            uint32_t word = brow[w];
-            if (!word) continue;
-            brow[w] = 0u;
-            float* c = crow + (w << 5);
-            while (word) {
-                c[__ffs(word) - 1] = 0.f;
-                word &= word - 1u;
-            }
-        }
+        // clear the words wlo..whi (every marked pixel, so every written one) and their bitmask words
+        float4* c4 = reinterpret_cast<float4*>(crow);
+        const int e4 = min((whi + 1) << 3, cov_stride >> 2);
+        for (int i = (wlo << 3) + lane; i < e4; i += 32) c4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int w = wlo + lane; w <= whi; w += 32) brow[w] = 0u;
         __syncwarp();
       }
     }
@@ -667,13 +702,15 @@ cudaError_t launch_diff_segments(const float* ctrl, uint32_t n_paths, int segs, 
 
 cudaError_t launch_diff(const DiffDev& D, bool backward, int cov_stride, int smem, cudaStream_t st) {
     if (backward) {
-        cudaError_t e = cudaFuncSetAttribute(k_diff_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        auto kern = D.rule == 1 ? k_diff_backward<1> : k_diff_backward<0>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
-        k_diff_backward<<<D.S.canvas_h / D.cta_rows, kDiffThreads, smem, st>>>(D, cov_stride);
+        kern<<<D.S.canvas_h / D.cta_rows, kDiffThreads, smem, st>>>(D, cov_stride);
     } else {
-        cudaError_t e = cudaFuncSetAttribute(k_diff_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        auto kern = D.rule == 1 ? k_diff_forward<1> : k_diff_forward<0>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
-        k_diff_forward<<<D.S.canvas_h / D.cta_rows, kDiffThreads, smem, st>>>(D, cov_stride);
+        kern<<<D.S.canvas_h / D.cta_rows, kDiffThreads, smem, st>>>(D, cov_stride);
     }
     return cudaGetLastError();
 }

@@ -39,9 +39,12 @@ def oracle_images(ctrl, n, P, S, w, h, rule, alpha=0.5):
                      for i in range(n)])
 
 
-@pytest.mark.parametrize("rule,margin", [(FillRule.NonZero, 0.0), (FillRule.EvenOdd, 0.0), (FillRule.NonZero, 15.0)])
-def test_forward_loss_and_gradient_match_oracle(R, rule, margin):
-    n, P, S, w, h = 3, 6, 8, 96, 72
+@pytest.mark.parametrize("rule,margin,w", [(FillRule.NonZero, 0.0, 96), (FillRule.EvenOdd, 0.0, 96),
+                                           (FillRule.NonZero, 15.0, 96), (FillRule.EvenOdd, 15.0, 101)])
+def test_forward_loss_and_gradient_match_oracle(R, rule, margin, w):
+    """Paths inside the image and crossing all four edges; a width that is not
+    a multiple of 4 (the row scan's ragged end, lines written past it)."""
+    n, P, S, h = 3, 6, 8, 72
     ctrl, _ = W.diff_batch(seed=1, n_images=n, paths=P, segs=S, size=72, margin=margin)
     ctrl[..., 0] *= w / 72.0
     target_imgs = oracle_images(ctrl + np.float32(1.5), n, P, S, w, h, rule)
