@@ -382,6 +382,13 @@ __device__ void diff_row_mean(const CellView& V, int r, int c0, float lo, float 
         return;
     }
     const int k0 = (int)floorf(lo), k1 = min((int)floorf(hi), W - 1 - c0);
+    if (k1 == k0 || hi <= (float)(k0 + 1)) {  // one pixel: the mean in closed form
+        float gk, Gk1;
+        V.at(r, k0 + c0, gk, Gk1);
+        I = Gk1 + ((float)(k0 + 1) - 0.5f * (lo + hi)) * gk;
+        dlo = dhi = -0.5f * gk;
+        return;
+    }
     float sI = 0.f, slo = 0.f, shi = 0.f;
     for (int k = k0; k <= k1; ++k) {
         const float a = fmaxf(lo, (float)k), b = fminf(hi, (float)(k + 1));
@@ -399,15 +406,14 @@ __device__ void diff_row_mean(const CellView& V, int r, int c0, float lo, float 
     dlo = slo * inv * inv;
 }
 
-// d(sum over the band's pixels of g * winding contribution of the piece p -> q)/d(line ends);
-// x relative to column c0, y relative to band row 0.
-__device__ void diff_piece(Dual px, Dual py, Dual qx, Dual qy, int rows, int c0, const CellView& V, float (&out)[4]) {
+// d(sum over the row's pixels of g * winding contribution of the piece p -> q)/d(line ends);
+// x relative to column c0, y relative to the row (which is y in [0, 1)).
+__device__ void diff_piece(Dual px, Dual py, Dual qx, Dual qy, int c0, const CellView& V, float (&out)[4]) {
     if (py.v == qy.v) {
         // horizontal: no coverage, but moving an end vertically brings coverage in
-        const int r = (int)floorf(py.v);
-        if (r < 0 || r >= rows) return;
+        if (!(py.v >= 0.f && py.v < 1.f)) return;
         float I, dlo, dhi;
-        diff_row_mean(V, r, c0, fminf(px.v, qx.v), fmaxf(px.v, qx.v), I, dlo, dhi);
+        diff_row_mean(V, 0, c0, fminf(px.v, qx.v), fmaxf(px.v, qx.v), I, dlo, dhi);
         #pragma unroll
         for (int k = 0; k < 4; ++k) out[k] += I * (qy.d[k] - py.d[k]);
         return;
@@ -418,32 +424,99 @@ __device__ void diff_piece(Dual px, Dual py, Dual qx, Dual qy, int rows, int c0,
         t = py; py = qy; qy = t;
         dir = -1.f;
     }
-    const Dual kx = ddiv(dsub(qx, px), dsub(qy, py));  // dx/dy
-    const int r0 = max((int)floorf(py.v), 0), r1 = min((int)ceilf(qy.v), rows);
-    for (int r = r0; r < r1; ++r) {
-        const bool start_in = py.v >= (float)r, end_in = qy.v <= (float)(r + 1);
-        const Dual sa = start_in ? py : dconst((float)r);
-        const Dual sb = end_in ? qy : dconst((float)(r + 1));
-        if (!(sb.v > sa.v)) continue;
-        const Dual xa = start_in ? px : dadd(px, dmul(dsub(sa, py), kx));
-        const Dual xn = end_in ? qx : dadd(px, dmul(dsub(sb, py), kx));
-        const Dual h = dsub(sb, sa);
-        const bool ord = xa.v <= xn.v;
-        const Dual& lo = ord ? xa : xn;
-        const Dual& hi = ord ? xn : xa;
-        float I, dlo, dhi;
-        diff_row_mean(V, r, c0, lo.v, hi.v, I, dlo, dhi);
-        #pragma unroll
-        for (int k = 0; k < 4; ++k) out[k] += dir * (I * h.d[k] + h.v * (dlo * lo.d[k] + dhi * hi.d[k]));
+    if (!(py.v < 1.f && qy.v > 0.f)) return;  // the piece misses the row
+    const bool start_in = py.v >= 0.f, end_in = qy.v <= 1.f;
+    const Dual sa = start_in ? py : dconst(0.f);
+    const Dual sb = end_in ? qy : dconst(1.f);
+    if (!(sb.v > sa.v)) return;
+    Dual xa = px, xn = qx;  // x where the piece enters and leaves the row
+    if (!start_in || !end_in) {
+        const Dual kx = ddiv(dsub(qx, px), dsub(qy, py));  // dx/dy
+        if (!start_in) xa = dadd(px, dmul(dsub(sa, py), kx));
+        if (!end_in) xn = dadd(px, dmul(dsub(sb, py), kx));
     }
+    const Dual h = dsub(sb, sa);
+    const bool ord = xa.v <= xn.v;
+    const Dual& lo = ord ? xa : xn;
+    const Dual& hi = ord ? xn : xa;
+    float I, dlo, dhi;
+    diff_row_mean(V, 0, c0, lo.v, hi.v, I, dlo, dhi);
+    #pragma unroll
+    for (int k = 0; k < 4; ++k) out[k] += dir * (I * h.d[k] + h.v * (dlo * lo.d[k] + dhi * hi.d[k]));
+}
+
+// diff_piece for a line that no x rule changes (both ends in [0, width]),
+// with the gradient of F = dir h I(lo, hi) taken in reverse mode through
+// the row clip: the same quantities as the dual numbers in a few scalar
+// operations.  (ax, ay) -> (bx, by), x relative to column c0, y relative to
+// the row.
+__device__ __forceinline__ void diff_piece_inside(float ax, float ay, float bx, float by, int c0, const CellView& V,
+                                                  float (&out)[4]) {
+    float I, dlo, dhi;
+    if (ay == by) {
+        // horizontal: no coverage, but moving an end vertically brings coverage in
+        if (!(ay >= 0.f && ay < 1.f)) return;
+        diff_row_mean(V, 0, c0, fminf(ax, bx), fmaxf(ax, bx), I, dlo, dhi);
+        out[1] -= I;
+        out[3] += I;
+        return;
+    }
+    const bool down = ay < by;  // p -> q runs down the rows
+    const float px = down ? ax : bx, py = down ? ay : by, qx = down ? bx : ax, qy = down ? by : ay;
+    if (!(py < 1.f && qy > 0.f)) return;  // the piece misses the row
+    const bool start_in = py >= 0.f, end_in = qy <= 1.f;
+    const float sa = start_in ? py : 0.f, sb = end_in ? qy : 1.f;
+    if (!(sb > sa)) return;
+    float xa = px, xn = qx, inv = 0.f, kx = 0.f;  // x where the piece enters and leaves the row
+    if (!start_in || !end_in) {
+        inv = __fdividef(1.f, qy - py);
+        kx = (qx - px) * inv;  // dx/dy
+        if (!start_in) xa = px + (sa - py) * kx;
+        if (!end_in) xn = px + (sb - py) * kx;
+    }
+    const float h = sb - sa;
+    const bool ord = xa <= xn;
+    diff_row_mean(V, 0, c0, ord ? xa : xn, ord ? xn : xa, I, dlo, dhi);
+    const float dir = down ? 1.f : -1.f;
+    const float gh = dir * I;                           // dF/dh
+    const float gxa = dir * h * (ord ? dlo : dhi);      // dF/dxa
+    const float gxn = dir * h * (ord ? dhi : dlo);      // dF/dxn
+    float gpx = 0.f, gpy = 0.f, gqx = 0.f, gqy = 0.f;
+    if (start_in) {  // xa = px, h = sb - py
+        gpx += gxa;
+        gpy -= gh;
+    } else {  // xa = px + u kx, u = sa - py, kx = (qx - px) / (qy - py)
+        const float u = (sa - py) * inv, t = gxa * u;
+        gpx += gxa - t;
+        gpy += t * kx - gxa * kx;
+        gqx += t;
+        gqy -= t * kx;
+    }
+    if (end_in) {  // xn = qx, h = qy - sa
+        gqx += gxn;
+        gqy += gh;
+    } else {  // xn = px + v kx, v = sb - py
+        const float v = (sb - py) * inv, t = gxn * v;
+        gpx += gxn - t;
+        gpy += t * kx - gxn * kx;
+        gqx += t;
+        gqy -= t * kx;
+    }
+    out[0] += down ? gpx : gqx;
+    out[1] += down ? gpy : gqy;
+    out[2] += down ? gqx : gpx;
+    out[3] += down ? gqy : gpy;
 }
 
 // The reference's x rules on dual numbers (width = W, relative to column c0), then the pieces.
-__device__ void diff_line(float ax, float ay, float bx, float by, int rows, int c0, const CellView& V,
-                          float (&out)[4]) {
+__device__ void diff_line(float ax, float ay, float bx, float by, int c0, const CellView& V, float (&out)[4]) {
     Dual x0{ax, {1.f, 0.f, 0.f, 0.f}}, y0{ay, {0.f, 1.f, 0.f, 0.f}};
     Dual x1{bx, {0.f, 0.f, 1.f, 0.f}}, y1{by, {0.f, 0.f, 0.f, 1.f}};
     const float width = (float)(V.W - c0), zero = (float)(-c0);
+    if (ax <= width && bx <= width && ax >= zero && bx >= zero) {  // no x rule applies: most lines
+        diff_piece_inside(ax, ay, bx, by, c0, V, out);
+        return;
+    }
     if (x0.v > width || x1.v > width) {
         if (x0.v > width && x1.v > width) {
             x0 = dconst(width - 0.001f);
@@ -456,18 +529,18 @@ __device__ void diff_line(float ax, float ay, float bx, float by, int rows, int 
         }
     }
     if (x0.v >= zero && x1.v >= zero) {
-        diff_piece(x0, y0, x1, y1, rows, c0, V, out);
+        diff_piece(x0, y0, x1, y1, c0, V, out);
     } else if (x0.v <= zero && x1.v <= zero) {
-        diff_piece(dconst(zero), y0, dconst(zero), y1, rows, c0, V, out);
+        diff_piece(dconst(zero), y0, dconst(zero), y1, c0, V, out);
     } else {
         const Dual t = ddiv(dsub(x0, dconst(zero)), dsub(x0, x1));
         const Dual mx = dlerp(x0, x1, t), my = dlerp(y0, y1, t);
         if (x0.v < zero) {
-            diff_piece(mx, my, x1, y1, rows, c0, V, out);
-            diff_piece(dconst(zero), y0, mx, my, rows, c0, V, out);
+            diff_piece(mx, my, x1, y1, c0, V, out);
+            diff_piece(dconst(zero), y0, mx, my, c0, V, out);
         } else {
-            diff_piece(x0, y0, mx, my, rows, c0, V, out);
-            diff_piece(mx, my, dconst(zero), y1, rows, c0, V, out);
+            diff_piece(x0, y0, mx, my, c0, V, out);
+            diff_piece(mx, my, dconst(zero), y1, c0, V, out);
         }
     }
 }
@@ -618,6 +691,9 @@ __global__ void __launch_bounds__(kDiffThreads, 3) k_diff_backward(DiffDev D, in
         diff_sparse_row<RULE>(D, wlo, whi, row, brow, crow, prow, tot + warp, lane);
         __syncwarp();
         const CellView V{brow, crow, prow, tot + warp, wpr, cov_stride, D.width};
+        // the lists hold the lines of path p0 + q of the image: segments path_seg0 .. path_seg1 - 1
+        const uint32_t path_seg0 = ((uint32_t)img * (uint32_t)D.paths + (uint32_t)(p0 + q)) * (uint32_t)D.segs;
+        const uint32_t path_seg1 = path_seg0 + (uint32_t)D.segs;
         for (uint32_t j = lane; j < n; j += 32) {
             const uint32_t l = S.pairs[start + j];
             const uint2 code = S.leaf[l];
@@ -627,23 +703,23 @@ __global__ void __launch_bounds__(kDiffThreads, 3) k_diff_backward(DiffDev D, in
             if (!(fminf(ay, by) < 1.0f && fmaxf(ay, by) >= 0.0f)) continue;  // no share of this row
             const int c0 = a.col;
             float d4[4] = {0.f, 0.f, 0.f, 0.f};
-            diff_line(a.fx, ay, (float)(b.col - c0) + b.fx, by, 1, c0, V, d4);
+            diff_line(a.fx, ay, (float)(b.col - c0) + b.fx, by, c0, V, d4);
             if (d4[0] == 0.f && d4[1] == 0.f && d4[2] == 0.f && d4[3] == 0.f) continue;
             // chain to the control points: Bernstein weights at the frozen tree's parameters
+            // (segment seg of the path: control points 3 seg .. 3 seg + 2, then the next segment's first)
             const uint32_t seg = code.x;
             const int d = (int)(code.y >> 27);
             const uint32_t k = code.y & ((1u << 27) - 1u);
             const float t0 = (float)k * pow2f(-d), t1 = (float)(k + 1u) * pow2f(-d);
-            const uint64_t path = seg / (uint32_t)D.segs;
-            const int s = (int)(seg - path * (uint32_t)D.segs);
-            const int idx[4] = {3 * s, 3 * s + 1, 3 * s + 2, 3 * ((s + 1) % D.segs)};
+            const bool last = seg + 1u == path_seg1;
             const float u0 = 1.f - t0, u1 = 1.f - t1;
             const float b0[4] = {u0 * u0 * u0, 3.f * t0 * u0 * u0, 3.f * t0 * t0 * u0, t0 * t0 * t0};
             const float b1[4] = {u1 * u1 * u1, 3.f * t1 * u1 * u1, 3.f * t1 * t1 * u1, t1 * t1 * t1};
-            float2* o = out + path * 3ull * D.segs;
+            float2* o = out + 3ull * seg;
+            float2* o3 = last ? out + 3ull * path_seg0 : o + 3;
             #pragma unroll
             for (int q = 0; q < 4; ++q)
-                atomicAdd(&o[idx[q]], make_float2(d4[0] * b0[q] + d4[2] * b1[q], d4[1] * b0[q] + d4[3] * b1[q]));
+                atomicAdd(q < 3 ? o + q : o3, make_float2(d4[0] * b0[q] + d4[2] * b1[q], d4[1] * b0[q] + d4[3] * b1[q]));
         }
         __syncwarp();
         // clear the words wlo..whi (every marked pixel, so every written one) and their bitmask words
