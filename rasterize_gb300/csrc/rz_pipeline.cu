@@ -279,8 +279,12 @@ struct EmitLines {
         if (r0 >= r1) return;
         const int b0 = max((r0 + row0) / band_rows, band0);
         const int b1 = min((r1 - 1 + row0) / band_rows, band0 + nbands - 1);
+        if (b0 > b1) return;
         if (hist) {
-            for (int bb = b0; bb <= b1; ++bb) atomicAdd(&hist[entry0 + (bb - band0) - hist_e0], 1u);
+            // difference-coded: +1 at the first band, -1 after the last (prefix-summed once per block)
+            const uint32_t i0 = entry0 + (b0 - band0) - hist_e0;
+            atomicAdd(&hist[i0], 1u);
+            atomicAdd(&hist[i0 + (uint32_t)(b1 - b0) + 1u], 0xffffffffu);
             return;
         }
         if (b0 == b1) {
@@ -351,12 +355,49 @@ static __device__ __noinline__ void emit_task_big(const SceneDev S, uint32_t fil
 // its fills' entries span at most kHistEntries: counted in shared memory and
 // added to the global counters once per block.  Every line of a walk lands in
 // a few neighbouring bands, and one global atomic per line and band would
-// serialise on the few cache lines that hold a fill's counters.
+// serialise on the few cache lines that hold a fill's counters.  A line's
+// bands are consecutive entries, so it is counted as a difference (two
+// shared atomics however many bands it crosses) and the block prefix-sums
+// the window before adding it.
 constexpr int kHistEntries = 2048;
 constexpr int kEmitThreads = 128;
 
+// In-place inclusive prefix of h[0, n) (n <= kHistEntries) by the THREADS
+// threads of the block, each over its own run of consecutive entries.
+// Starts and ends with a block barrier.
+template <int THREADS>
+__device__ void block_prefix_hist(uint32_t* h, uint32_t n) {
+    constexpr int PER = kHistEntries / THREADS;
+    __shared__ uint32_t s_warp[THREADS / 32];
+    __syncthreads();
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t base = (uint32_t)t * PER;
+    uint32_t v[PER], sum = 0;
+    #pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        v[i] = base + i < n ? h[base + i] : 0u;
+        sum += v[i];
+    }
+    uint32_t incl = sum;
+    #pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t o = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += o;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    uint32_t run = incl - sum;
+    for (int w = 0; w < warp; ++w) run += s_warp[w];
+    #pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        run += v[i];
+        if (base + i < n) h[base + i] = run;
+    }
+    __syncthreads();
+}
+
 __global__ void __launch_bounds__(kEmitThreads) k_flatten_emit(SceneDev S) {
-    __shared__ uint32_t s_hist[kHistEntries];
+    __shared__ uint32_t s_hist[kHistEntries + 1];  // one past the window: a difference's end
     __shared__ uint32_t s_e0, s_n;
     const uint64_t nt = scene_tasks(S);
     const uint64_t t0 = (uint64_t)blockIdx.x * kEmitThreads;
@@ -374,7 +415,7 @@ __global__ void __launch_bounds__(kEmitThreads) k_flatten_emit(SceneDev S) {
     }
     __syncthreads();
     const uint32_t hn = s_n, he0 = s_e0;
-    for (uint32_t i = threadIdx.x; i < hn; i += kEmitThreads) s_hist[i] = 0u;
+    for (uint32_t i = threadIdx.x; i <= hn; i += kEmitThreads) s_hist[i] = 0u;
     __syncthreads();
     if (t < nt) {
         uint32_t s, j;
@@ -397,7 +438,8 @@ __global__ void __launch_bounds__(kEmitThreads) k_flatten_emit(SceneDev S) {
             e.flush();
         }
     }
-    __syncthreads();
+    if (hn == 0) return;  // (uniform over the block)
+    block_prefix_hist<kEmitThreads>(s_hist, hn);
     for (uint32_t i = threadIdx.x; i < hn; i += kEmitThreads)
         if (s_hist[i]) atomicAdd(&S.entry_count[he0 + i], s_hist[i]);
 }
@@ -478,7 +520,7 @@ constexpr int kBinThreads = 256;
 constexpr int kBinLines = 4 * kBinThreads;
 
 __global__ void __launch_bounds__(kBinThreads) k_bin_scatter(SceneDev S) {
-    __shared__ uint32_t s_cnt[kHistEntries];
+    __shared__ uint32_t s_cnt[kHistEntries + 1];  // one past the window: a difference's end
     __shared__ uint32_t s_base[kHistEntries];
     __shared__ uint32_t s_e0, s_n, s_fa, s_fb;
     const uint32_t n_lines = scene_lines(S);
@@ -499,15 +541,18 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_scatter(SceneDev S) {
         for (uint32_t l = l0 + threadIdx.x; l < l0 + kBinLines; l += kBinThreads) bin_line_global(S, l < l1 ? l : n_lines, n_lines);
         return;
     }
-    for (uint32_t i = threadIdx.x; i < n; i += kBinThreads) s_cnt[i] = 0u;
+    for (uint32_t i = threadIdx.x; i <= n; i += kBinThreads) s_cnt[i] = 0u;
     __syncthreads();
     for (uint32_t l = l0 + threadIdx.x; l < l1; l += kBinThreads) {
         const FillDev& f = S.fills[fill_of_line(S, l, fa, fb)];
         int b0, b1;
         line_bands(S, f, l, b0, b1);
-        for (int bb = b0; bb <= b1; ++bb) atomicAdd(&s_cnt[f.entry0 + (bb - f.band0) - e0], 1u);
+        if (b0 > b1) continue;
+        const uint32_t i0 = f.entry0 + (b0 - f.band0) - e0;  // difference-coded, as in the emit
+        atomicAdd(&s_cnt[i0], 1u);
+        atomicAdd(&s_cnt[i0 + (uint32_t)(b1 - b0) + 1u], 0xffffffffu);
     }
-    __syncthreads();
+    block_prefix_hist<kBinThreads>(s_cnt, n);
     for (uint32_t i = threadIdx.x; i < n; i += kBinThreads) {
         const uint32_t c = s_cnt[i];
         if (c) s_base[i] = S.entry_start[e0 + i] + atomicAdd(&S.entry_cursor[e0 + i], c);
