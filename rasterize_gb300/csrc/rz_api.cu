@@ -55,7 +55,8 @@ int mask_lines_occupancy();
 cudaError_t launch_mask_lines(const SceneDev& S, const MaskDev* masks, const WorkItem* items, int n_items,
                               int32_t* queue, float* out, int grid, cudaStream_t st);
 int diff_smem_bytes(int width, int band_rows, bool backward, int* cov_stride);
-cudaError_t launch_diff_segments(const float* ctrl, uint32_t n_paths, int segs, uint8_t* kind, double* pts,
+cudaError_t launch_diff_segments(const float* ctrl, uint32_t n_paths, uint32_t paths_per_image, int segs, int width,
+                                 int height, int rule, uint8_t* kind, double* pts, uint32_t* sub_off, FillDev* fills,
                                  cudaStream_t st);
 cudaError_t launch_diff(const DiffDev& D, bool backward, int cov_stride, int smem, cudaStream_t st);
 cudaError_t launch_l2_loss(const float* A, const float* T, uint64_t n, double* loss, float* dl, int num_sms,
@@ -1677,6 +1678,8 @@ void prepare_paint(const rz_paint& in, const rzhost::Xf& tr, bool have_bbox, con
 
 struct HostScene {
     std::vector<rz::FillDev> fills;
+    // or the fills already built on the device (ctx->p_fills, n_dev_fills of them): nothing to upload
+    uint32_t n_dev_fills = 0;
     std::vector<rz::PaintDev> paints;
     const uint8_t* kind = nullptr;
     const double* pts = nullptr;
@@ -1806,9 +1809,11 @@ void add_fill(HostScene& hs, uint32_t sub0, uint32_t sub1, int col0, int row0, i
 // the caller then sizes the buffers from the device counts and runs again.
 rz_status build_lines(rz_ctx* ctx, HostScene& hs, rz::SceneDev& S, Trace& tr, DevBuf* leaf,
                       bool speculative = false) {
-    RZ_CUDA(ctx->p_fills.ensure(hs.fills.size() * sizeof(rz::FillDev)));
-    RZ_CUDA(cudaMemcpyAsync(ctx->p_fills.p, hs.fills.data(), hs.fills.size() * sizeof(rz::FillDev),
-                            cudaMemcpyHostToDevice, ctx->stream));
+    if (!hs.n_dev_fills) {
+        RZ_CUDA(ctx->p_fills.ensure(hs.fills.size() * sizeof(rz::FillDev)));
+        RZ_CUDA(cudaMemcpyAsync(ctx->p_fills.p, hs.fills.data(), hs.fills.size() * sizeof(rz::FillDev),
+                                cudaMemcpyHostToDevice, ctx->stream));
+    }
     S.fills = (const rz::FillDev*)ctx->p_fills.p;
     // 1) lines per slot, 2) offsets (one extra element receives the total)
     if (!hs.task_off.empty()) {

@@ -35,11 +35,38 @@
 namespace rz {
 
 // ---------------------------------------------------------------------------
-// FP32 control points -> the pipeline's binary64 cubic segments
+// FP32 control points -> the pipeline's binary64 cubic segments, and the
+// scene around them: path p is subpath p (segments p segs .. (p + 1) segs - 1)
+// and fill p, whose view is its image (W x H at canvas row (p / P) H, clip
+// column W), one (fill, row) entry per image row.
 // ---------------------------------------------------------------------------
-__global__ void k_diff_segments(const float* __restrict__ ctrl, uint32_t n_paths, int segs, uint8_t* kind,
-                                double* pts) {
+__global__ void k_diff_segments(const float* __restrict__ ctrl, uint32_t n_paths, uint32_t paths_per_image, int segs,
+                                int width, int height, int rule, uint8_t* kind, double* pts, uint32_t* sub_off,
+                                FillDev* fills) {
     const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g <= n_paths) sub_off[g] = (uint32_t)g * (uint32_t)segs;
+    if (g < n_paths) {
+        const uint32_t p = (uint32_t)g;
+        FillDev f{};
+        f.sub0 = p;
+        f.sub1 = p + 1u;
+        f.seg0 = p * (uint32_t)segs;
+        f.seg1 = f.seg0 + (uint32_t)segs;
+        f.slot0 = p * (uint32_t)(segs + 1);  // the segments, then the closing line
+        f.entry0 = p * (uint32_t)height;
+        f.col0 = 0;
+        f.row0 = (int32_t)(p / paths_per_image) * height;
+        f.width = width;
+        f.height = height;
+        f.clip_width = width;
+        f.band0 = f.row0;  // one-row bands
+        f.nbands = height;
+        f.rule = rule;
+        f.paint = 0;
+        f.tr[0] = 1.0;
+        f.tr[4] = 1.0;
+        fills[p] = f;
+    }
     if (g >= (uint64_t)n_paths * segs) return;
     const uint64_t p = g / segs;
     const int s = (int)(g - p * segs);
@@ -768,11 +795,12 @@ int diff_smem_bytes(int width, int band_rows, bool backward, int* cov_stride) {
     return 8 * band_rows * stride + 32 + 4 * band_rows * ((stride + 31) >> 5);
 }
 
-cudaError_t launch_diff_segments(const float* ctrl, uint32_t n_paths, int segs, uint8_t* kind, double* pts,
+cudaError_t launch_diff_segments(const float* ctrl, uint32_t n_paths, uint32_t paths_per_image, int segs, int width,
+                                 int height, int rule, uint8_t* kind, double* pts, uint32_t* sub_off, FillDev* fills,
                                  cudaStream_t st) {
-    const uint64_t n = (uint64_t)n_paths * segs;
-    if (n == 0) return cudaSuccess;
-    k_diff_segments<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(ctrl, n_paths, segs, kind, pts);
+    const uint64_t n = std::max<uint64_t>((uint64_t)n_paths * segs, (uint64_t)n_paths + 1);
+    k_diff_segments<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(ctrl, n_paths, paths_per_image, segs, width, height,
+                                                                   rule, kind, pts, sub_off, fills);
     return cudaGetLastError();
 }
 

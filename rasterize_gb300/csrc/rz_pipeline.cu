@@ -356,7 +356,7 @@ static __device__ __noinline__ void emit_task_big(const SceneDev S, uint32_t fil
 // added to the global counters once per block.  Every line of a walk lands in
 // a few neighbouring bands, and one global atomic per line and band would
 // serialise on the few cache lines that hold a fill's counters.  A line's
-// bands are consecutive entries, so it is counted as a difference (two
+// bands are consecutive entries, so the emit counts it as a difference (two
 // shared atomics however many bands it crosses) and the block prefix-sums
 // the window before adding it.
 constexpr int kHistEntries = 2048;
@@ -520,7 +520,7 @@ constexpr int kBinThreads = 256;
 constexpr int kBinLines = 4 * kBinThreads;
 
 __global__ void __launch_bounds__(kBinThreads) k_bin_scatter(SceneDev S) {
-    __shared__ uint32_t s_cnt[kHistEntries + 1];  // one past the window: a difference's end
+    __shared__ uint32_t s_cnt[kHistEntries];
     __shared__ uint32_t s_base[kHistEntries];
     __shared__ uint32_t s_e0, s_n, s_fa, s_fb;
     const uint32_t n_lines = scene_lines(S);
@@ -541,18 +541,17 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_scatter(SceneDev S) {
         for (uint32_t l = l0 + threadIdx.x; l < l0 + kBinLines; l += kBinThreads) bin_line_global(S, l < l1 ? l : n_lines, n_lines);
         return;
     }
-    for (uint32_t i = threadIdx.x; i <= n; i += kBinThreads) s_cnt[i] = 0u;
+    for (uint32_t i = threadIdx.x; i < n; i += kBinThreads) s_cnt[i] = 0u;
     __syncthreads();
+    // (the placement below takes one shared atomic per line and band anyway: a difference-coded count here
+    // measured no faster)
     for (uint32_t l = l0 + threadIdx.x; l < l1; l += kBinThreads) {
         const FillDev& f = S.fills[fill_of_line(S, l, fa, fb)];
         int b0, b1;
         line_bands(S, f, l, b0, b1);
-        if (b0 > b1) continue;
-        const uint32_t i0 = f.entry0 + (b0 - f.band0) - e0;  // difference-coded, as in the emit
-        atomicAdd(&s_cnt[i0], 1u);
-        atomicAdd(&s_cnt[i0 + (uint32_t)(b1 - b0) + 1u], 0xffffffffu);
+        for (int bb = b0; bb <= b1; ++bb) atomicAdd(&s_cnt[f.entry0 + (bb - f.band0) - e0], 1u);
     }
-    block_prefix_hist<kBinThreads>(s_cnt, n);
+    __syncthreads();
     for (uint32_t i = threadIdx.x; i < n; i += kBinThreads) {
         const uint32_t c = s_cnt[i];
         if (c) s_base[i] = S.entry_start[e0 + i] + atomicAdd(&S.entry_cursor[e0 + i], c);
