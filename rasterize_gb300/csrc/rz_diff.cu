@@ -572,11 +572,31 @@ __device__ void diff_line(float ax, float ay, float bx, float by, int c0, const 
     }
 }
 
+// g = dL/dA * a (1 - A) / (1 - a alpha) * dalpha/dw at pixel x of the row,
+// winding wn (0 where the forward skips the pixel or the fill has no slope).
+template <int RULE>
+__device__ __forceinline__ float diff_g(const DiffDev& D, uint32_t wn, int x, int W, const float* dlrow,
+                                        const float* Arow) {
+    if (x >= W) return 0.f;
+    const float al = alpha_fix<RULE>(wn);
+    if (al < 1e-6f) return 0.f;  // pixels the forward skips have no slope
+    float da = 0.f;
+    if (RULE == 1) {
+        const int32_t fo = (int32_t)((wn + (1u << 22)) & ((1u << 23) - 1u)) - (1 << 22);
+        da = fo > 0 ? 1.f : -1.f;
+    } else if (al < 1.f) {
+        da = (int32_t)wn > 0 ? 1.f : -1.f;
+    }
+    if (da == 0.f) return 0.f;
+    // 1 - a alpha lies in [1 - a, 1]: the hardware quotient (within 2 ulp) is enough
+    return __fdividef(dlrow[x] * D.alpha * (1.f - Arow[x]), 1.f - D.alpha * al) * da;
+}
+
 // Sparse pass over the words wlo..whi of one row (one warp; no other word
-// holds a mark): the marked pixels in increasing order,
-// 32 at a time, one per lane (lane i takes the marked pixel of rank c + i: its
-// 32-word block by a search over the words' prefix counts, its bit by a
-// select within the word).  Warp scans give the exact integer windings there
+// holds a mark): the marked pixels in increasing order, 64 at a time, two
+// per lane (lane i takes the marked pixels of ranks c + 2i and c + 2i + 1:
+// the first's 32-word block by a search over the words' prefix counts and its
+// bit by a select within the word, the second the next mark after it).  Warp scans give the exact integer windings there
 // (the prefix of the marked words; the others are 0),
 // g = dL/dA * a (1 - A) / (1 - a alpha) * dalpha/dw, and the inclusive prefix
 // P of g.  g overwrites the coverage word, P goes to its own row; *tot gets
@@ -601,8 +621,9 @@ __device__ void diff_sparse_row(const DiffDev& D, int wlo, int whi, int row, con
         }
         const int total = __shfl_sync(0xffffffffu, incl, 31);
         const int excl = incl - cnt;
-        for (int c = 0; c < total; c += 32) {
-            const int r = c + lane;
+        const uint32_t nonempty = __ballot_sync(0xffffffffu, mine != 0u);
+        for (int c = 0; c < total; c += 64) {
+            const int r = c + 2 * lane;  // this lane's ranks: r and r + 1
             // the word holding rank r: the number of words whose inclusive count is <= r
             int j = 0;
             #pragma unroll
@@ -622,41 +643,41 @@ __device__ void diff_sparse_row(const DiffDev& D, int wlo, int whi, int row, con
                     pos += w;
                 }
             }
-            const bool live = r < total;
-            const int x = ((w0 + j) << 5) + pos;
-            const uint32_t dep = live ? (uint32_t)crow[x] : 0u;
-            uint32_t wi = dep;
+            // rank r + 1: the next mark of the same word, else the first mark of the next marked word
+            const uint32_t above = pos == 31 ? 0u : wbits & (0xfffffffeu << pos);
+            const uint32_t later = j == 31 ? 0u : nonempty & (0xfffffffeu << j);
+            const int j2 = later ? __ffs(later) - 1 : j;
+            const uint32_t wbits2 = __shfl_sync(0xffffffffu, mine, j2);
+            const bool live0 = r < total, live1 = r + 1 < total;
+            const int x0 = ((w0 + j) << 5) + pos;
+            const int x1 = above ? ((w0 + j) << 5) + __ffs(above) - 1 : ((w0 + j2) << 5) + __ffs(wbits2) - 1;
+            const uint32_t d0 = live0 ? (uint32_t)crow[x0] : 0u, d1 = live1 ? (uint32_t)crow[x1] : 0u;
+            uint32_t wi = d0 + d1;
             #pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
                 const uint32_t o = __shfl_up_sync(0xffffffffu, wi, off);
                 if (lane >= off) wi += o;
             }
-            const uint32_t wn = wcarry + wi;  // winding at pixel x
+            // windings at x0 and x1 (exact: integer prefix)
+            const uint32_t wn1 = wcarry + wi, wn0 = wn1 - d1;
             wcarry += __shfl_sync(0xffffffffu, wi, 31);
-            float gv = 0.f;
-            if (live && x < W) {
-                const float al = alpha_fix<RULE>(wn);
-                if (al >= 1e-6f) {  // pixels the forward skips have no slope
-                    float da = 0.f;
-                    if (RULE == 1) {
-                        const int32_t fo = (int32_t)((wn + (1u << 22)) & ((1u << 23) - 1u)) - (1 << 22);
-                        da = fo > 0 ? 1.f : -1.f;
-                    } else if (al < 1.f) {
-                        da = (int32_t)wn > 0 ? 1.f : -1.f;
-                    }
-                    // 1 - a alpha lies in [1 - a, 1]: the hardware quotient (within 2 ulp) is enough
-                    if (da != 0.f) gv = __fdividef(dlrow[x] * D.alpha * (1.f - Arow[x]), 1.f - D.alpha * al) * da;
-                }
-            }
-            float gi = gv;
+            const float g0 = live0 ? diff_g<RULE>(D, wn0, x0, W, dlrow, Arow) : 0.f;
+            const float g1 = live1 ? diff_g<RULE>(D, wn1, x1, W, dlrow, Arow) : 0.f;
+            float gi = g0 + g1;
             #pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
                 const float o = __shfl_up_sync(0xffffffffu, gi, off);
                 if (lane >= off) gi += o;
             }
-            if (live) {
-                crow[x] = __float_as_int(gv);
-                prow[x] = gcarry + gi;
+            const float gex = __shfl_up_sync(0xffffffffu, gi, 1);
+            const float p0 = gcarry + (lane ? gex : 0.f) + g0;
+            if (live0) {
+                crow[x0] = __float_as_int(g0);
+                prow[x0] = p0;
+            }
+            if (live1) {
+                crow[x1] = __float_as_int(g1);
+                prow[x1] = p0 + g1;
             }
             gcarry += __shfl_sync(0xffffffffu, gi, 31);
         }
