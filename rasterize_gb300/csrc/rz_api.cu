@@ -45,6 +45,7 @@ cudaError_t launch_flatten_counts(const BatchDev& b, uint32_t n_segments, uint32
                                   cudaStream_t stream);
 cudaError_t launch_flatten_count(const SceneDev& S, cudaStream_t st);
 cudaError_t launch_flatten_emit(const SceneDev& S, cudaStream_t st);
+cudaError_t launch_flatten_emit_alloc(const SceneDev& S, uint32_t* n_lines, cudaStream_t st);
 cudaError_t launch_bin_scatter(const SceneDev& S, cudaStream_t st);
 int composite_smem_bytes(int canvas_w, int band_rows, int max_clip_width, bool paint_mode, int* cov_stride);
 cudaError_t launch_composite(const SceneDev& S, int cov_stride, int smem, cudaStream_t st);
@@ -1125,7 +1126,7 @@ rz_status rz_mask(rz_ctx* ctx, const rz_path* path, const double tr[6], int32_t 
     if (st) return st;
     trc.mark("download");
     const float* src = (const float*)ctx->h_out.p;
-    parallel_for((int64_t)shape.height, 64, [&](int64_t y0, int64_t y1) {
+    parallel_for((int64_t)shape.height, 32, [&](int64_t y0, int64_t y1) {
         for (int64_t y = y0; y < y1; ++y) {
             const float* s = src + (uint64_t)y * shape.width;
             double* d = img + shape.start + (uint64_t)y * shape.row_stride;
@@ -1901,6 +1902,57 @@ rz_status grow_line_buffers(rz_ctx* ctx, const rz::SceneDev& S, uint32_t n_entri
 
 // Flatten + bin + composite on the device.  canvas: device buffer (RGBA
 // pixels when paints are given, else an f32 mask), stride in pixels.
+// A mask of one small fill (at most ~64 K lines expected, times its bands at most ~8 M): every band
+// reading every line costs less than the offsets scan, the per-band counts and lists and their launches.
+bool small_scene(const HostScene& hs, const rz::SceneDev& S) {
+    if (hs.fills.size() != 1) return false;
+    const uint64_t tasks = hs.task_off.empty() ? ((uint64_t)hs.n_slots << hs.task_depth) : hs.task_off.back();
+    const uint64_t est_lines = 8 * tasks;  // subtree tasks are sized to about 8 leaves each
+    return est_lines <= (1u << 16) && est_lines * (uint64_t)S.n_bands <= (1u << 23);
+}
+
+// The small-scene route: one pass flattens every task into lines it reserves on a device counter, then the
+// composite gives every band every line.  A line buffer too small shows as RZ_ERR_CAPACITY: it is sized from
+// the counter and the two launches run again.
+rz_status run_small(rz_ctx* ctx, HostScene& hs, rz::SceneDev& S, int cov_stride, int smem, Trace& tr) {
+    RZ_CUDA(ctx->p_fills.ensure(hs.fills.size() * sizeof(rz::FillDev)));
+    RZ_CUDA(cudaMemcpyAsync(ctx->p_fills.p, hs.fills.data(), hs.fills.size() * sizeof(rz::FillDev),
+                            cudaMemcpyHostToDevice, ctx->stream));
+    S.fills = (const rz::FillDev*)ctx->p_fills.p;
+    if (!hs.task_off.empty()) {
+        RZ_CUDA(ctx->p_tasks.ensure(hs.task_off.size() * 4));
+        RZ_CUDA(cudaMemcpyAsync(ctx->p_tasks.p, hs.task_off.data(), hs.task_off.size() * 4, cudaMemcpyHostToDevice,
+                                ctx->stream));
+        S.task_off = (const uint32_t*)ctx->p_tasks.p;
+        S.n_tasks = hs.task_off.back();
+    }
+    uint32_t* counter = (uint32_t*)ctx->d_ctrl.p + 15;  // zeroed with the control words
+    constexpr size_t kMinLines = 1u << 16;
+    RZ_CUDA(ctx->p_lines.ensure(kMinLines * 2 * sizeof(int4)));
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        const uint64_t cap = std::min<uint64_t>(ctx->p_lines.cap / (2 * sizeof(int4)), 0xffffffffull);
+        S.lines = (int4*)ctx->p_lines.p;
+        S.line_cap = (uint32_t)cap;
+        S.n_lines = (uint32_t)cap;
+        S.n_lines_dev = counter;
+        S.pairs = nullptr;  // every band takes every line
+        tr.gpu_mark(ctx->stream, "upload");
+        RZ_CUDA(rz::launch_flatten_emit_alloc(S, counter, ctx->stream));
+        tr.gpu_mark(ctx->stream, "flatten_emit_alloc");
+        RZ_CUDA(rz::launch_composite(S, cov_stride, smem, ctx->stream));
+        tr.gpu_mark(ctx->stream, "composite");
+        rz_status st = read_error(ctx);
+        if (st != RZ_ERR_CAPACITY || attempt) return st;
+        uint32_t n_lines = 0;
+        RZ_CUDA(cudaMemcpyAsync(&n_lines, counter, 4, cudaMemcpyDeviceToHost, ctx->stream));
+        RZ_CUDA(cudaStreamSynchronize(ctx->stream));
+        RZ_CUDA(ctx->p_lines.ensure((uint64_t)n_lines * 2 * sizeof(int4)));
+        RZ_CUDA(cudaMemsetAsync(ctx->d_ctrl.p, 0, 64, ctx->stream));
+        ctx->last_error.clear();
+    }
+    return RZ_OK;
+}
+
 rz_status run_pipeline(rz_ctx* ctx, HostScene& hs, double flatness, float* canvas, int64_t canvas_stride, int canvas_w,
                        int canvas_h, const float* bg_dev, bool load_canvas, uint32_t* rgba8 = nullptr) {
     Trace tr("pipeline");
@@ -1947,6 +1999,7 @@ rz_status run_pipeline(rz_ctx* ctx, HostScene& hs, double flatness, float* canva
                                 cudaMemcpyHostToDevice, ctx->stream));
         S.paints = (const rz::PaintDev*)ctx->p_paints.p;
     }
+    if (!paint_mode && !load_canvas && small_scene(hs, S)) return run_small(ctx, hs, S, cov_stride, smem, tr);
     // the composite writes every pixel from bg (or leaves untouched mask bands zero): a pass
     // that ran out of list room can run again; over a loaded canvas the buffers are sized first
     const bool speculative = !load_canvas;

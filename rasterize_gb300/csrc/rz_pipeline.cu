@@ -444,6 +444,40 @@ __global__ void __launch_bounds__(kEmitThreads) k_flatten_emit(SceneDev S) {
         if (s_hist[i]) atomicAdd(&S.entry_count[he0 + i], s_hist[i]);
 }
 
+// Small scenes in one pass: every flatten task counts its leaves, reserves
+// its lines with one atomic on *n_lines and emits them there.  No offsets
+// scan and no per-band counts: the composite then gives every band every
+// line (lines of different tasks interleave; the integer coverage does not
+// depend on their order).
+__global__ void __launch_bounds__(kEmitThreads) k_flatten_emit_alloc(SceneDev S, uint32_t* n_lines) {
+    const uint64_t t = (uint64_t)blockIdx.x * kEmitThreads + threadIdx.x;
+    if (t >= scene_tasks(S)) return;
+    uint32_t s, j;
+    int td;
+    task_slot(S, t, s, j, td);
+    const uint32_t fill = fill_of_slot(S, s);
+    const FillDev& f = S.fills[fill];
+    SlotState st;
+    load_slot(S, f, s, st);
+    if (!st.ok) return;
+    CountLeaves c;
+    int fallbacks = 0;
+    if (!walk_task(S, f, st, j, td, fallbacks, c)) {
+        pset_err(S.err, ERR_DEPTH);
+        return;
+    }
+    if (fallbacks) atomicAdd(&S.counters[1], fallbacks);
+    const uint32_t n = st.fits ? c.n : 2u * c.n;
+    if (n == 0) return;
+    const uint32_t first = atomicAdd(n_lines, n);
+    if (!st.fits) {
+        emit_task_big(S, fill, s, j, td, first);
+    } else {
+        EmitLines<true> e(S, f, st, first);
+        walk_task<1>(S, f, st, j, td, fallbacks, e);
+    }
+}
+
 // Lines of the scene (at most the buffer's capacity when counted on the device).
 __device__ __forceinline__ uint32_t scene_lines(const SceneDev& S) {
     return S.n_lines_dev ? min(*S.n_lines_dev, S.line_cap) : S.n_lines;
@@ -824,8 +858,10 @@ __global__ void __launch_bounds__(THREADS) k_composite(SceneDev S, int cov_strid
     for (uint32_t fi = 0; fi < S.n_fills; ++fi) {
         const FillDev& f = S.fills[fi];
         if (band < f.band0 || band >= f.band0 + f.nbands) continue;
+        // no lists (small scenes): every band takes every line, dropping those whose rows miss it
+        const bool all = S.pairs == nullptr;
         const uint32_t e = f.entry0 + (band - f.band0);
-        const uint32_t n = S.entry_count[e];
+        const uint32_t n = all ? scene_lines(S) : S.entry_count[e];
         if (n == 0) continue;  // full-width bands: no line, no coverage
         Band B;
         B.acc = cov;
@@ -845,20 +881,27 @@ __global__ void __launch_bounds__(THREADS) k_composite(SceneDev S, int cov_strid
         const int n4 = (rows * B.stride) >> 2;
         for (int i = threadIdx.x; i < n4; i += THREADS) sm4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         __syncthreads();
-        const uint32_t start = S.entry_start[e];
+        const uint32_t start = all ? 0u : S.entry_start[e];
         // Lines that need the binary64 route (long, or at the x rules) are queued per warp and taken 32 at a
         // time, so the slow route runs with full warps instead of a few lanes of every step.
         uint32_t* q = s_slow[threadIdx.x >> 5];
         int nq = 0;
         for (uint32_t j0 = threadIdx.x & ~31u; j0 < n; j0 += THREADS) {
             const uint32_t j = j0 + lane;
-            uint32_t l = 0;
+            uint32_t l = j;
             bool slow = false;
             // slots and lines beyond the buffers (reported by the earlier passes) are skipped
-            if (j < n && start + j < S.pair_cap) l = S.pairs[start + j];
-            if (j < n && start + j < S.pair_cap && l < S.line_cap) {
+            bool have = j < n;  // (all: n is at most the line capacity)
+            if (!all) {
+                have = have && start + j < S.pair_cap;
+                if (have) l = S.pairs[start + j];
+                have = have && l < S.line_cap;
+            }
+            if (have) {
                 const int4 a = S.lines[2ull * l], b = S.lines[2ull * l + 1];
-                slow = !accumulate_vtx_short(B, line_vtx(a, B.y0), line_vtx(b, B.y0));
+                const VtxQ va = line_vtx(a, B.y0), vb = line_vtx(b, B.y0);
+                if (!all || (min(va.row, vb.row) <= rows + 1 && max(va.row, vb.row) >= -2))
+                    slow = !accumulate_vtx_short(B, va, vb);
             }
             const unsigned m = __ballot_sync(0xffffffffu, slow);
             if (slow) q[nq + __popc(m & ((1u << lane) - 1u))] = l;
@@ -906,6 +949,13 @@ cudaError_t launch_flatten_emit(const SceneDev& S, cudaStream_t st) {
     const uint64_t n = scene_tasks(S);
     if (n == 0) return cudaSuccess;
     k_flatten_emit<<<(unsigned)((n + kEmitThreads - 1) / kEmitThreads), kEmitThreads, 0, st>>>(S);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_flatten_emit_alloc(const SceneDev& S, uint32_t* n_lines, cudaStream_t st) {
+    const uint64_t n = scene_tasks(S);
+    if (n == 0) return cudaSuccess;
+    k_flatten_emit_alloc<<<(unsigned)((n + kEmitThreads - 1) / kEmitThreads), kEmitThreads, 0, st>>>(S, n_lines);
     return cudaGetLastError();
 }
 
