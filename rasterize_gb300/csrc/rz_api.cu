@@ -1908,12 +1908,17 @@ bool small_scene(const HostScene& hs, const rz::SceneDev& S) {
     if (hs.fills.size() != 1) return false;
     const uint64_t tasks = hs.task_off.empty() ? ((uint64_t)hs.n_slots << hs.task_depth) : hs.task_off.back();
     const uint64_t est_lines = 8 * tasks;  // subtree tasks are sized to about 8 leaves each
-    return est_lines <= (1u << 16) && est_lines * (uint64_t)S.n_bands <= (1u << 23);
+    if (est_lines > (1u << 16) || est_lines * (uint64_t)S.n_bands > (1u << 23)) return false;
+    // a slot at the task cap (1024) may have a tree far deeper than the estimate
+    for (size_t s = 0; s + 1 < hs.task_off.size(); ++s)
+        if (hs.task_off[s + 1] - hs.task_off[s] >= 1024u) return false;
+    return true;
 }
 
 // The small-scene route: one pass flattens every task into lines it reserves on a device counter, then the
-// composite gives every band every line.  A line buffer too small shows as RZ_ERR_CAPACITY: it is sized from
-// the counter and the two launches run again.
+// composite gives every band every line.  RZ_ERR_CAPACITY: the trees were deeper than the estimate and there
+// were more lines than the route takes (the composite then returns at once); the caller takes the binned
+// pipeline instead (every band reading every line of a large scene would cost lines x bands).
 rz_status run_small(rz_ctx* ctx, HostScene& hs, rz::SceneDev& S, int cov_stride, int smem, Trace& tr) {
     RZ_CUDA(ctx->p_fills.ensure(hs.fills.size() * sizeof(rz::FillDev)));
     RZ_CUDA(cudaMemcpyAsync(ctx->p_fills.p, hs.fills.data(), hs.fills.size() * sizeof(rz::FillDev),
@@ -1927,30 +1932,21 @@ rz_status run_small(rz_ctx* ctx, HostScene& hs, rz::SceneDev& S, int cov_stride,
         S.n_tasks = hs.task_off.back();
     }
     uint32_t* counter = (uint32_t*)ctx->d_ctrl.p + 15;  // zeroed with the control words
-    constexpr size_t kMinLines = 1u << 16;
-    RZ_CUDA(ctx->p_lines.ensure(kMinLines * 2 * sizeof(int4)));
-    for (int attempt = 0; attempt < 2; ++attempt) {
-        const uint64_t cap = std::min<uint64_t>(ctx->p_lines.cap / (2 * sizeof(int4)), 0xffffffffull);
-        S.lines = (int4*)ctx->p_lines.p;
-        S.line_cap = (uint32_t)cap;
-        S.n_lines = (uint32_t)cap;
-        S.n_lines_dev = counter;
-        S.pairs = nullptr;  // every band takes every line
-        tr.gpu_mark(ctx->stream, "upload");
-        RZ_CUDA(rz::launch_flatten_emit_alloc(S, counter, ctx->stream));
-        tr.gpu_mark(ctx->stream, "flatten_emit_alloc");
-        RZ_CUDA(rz::launch_composite(S, cov_stride, smem, ctx->stream));
-        tr.gpu_mark(ctx->stream, "composite");
-        rz_status st = read_error(ctx);
-        if (st != RZ_ERR_CAPACITY || attempt) return st;
-        uint32_t n_lines = 0;
-        RZ_CUDA(cudaMemcpyAsync(&n_lines, counter, 4, cudaMemcpyDeviceToHost, ctx->stream));
-        RZ_CUDA(cudaStreamSynchronize(ctx->stream));
-        RZ_CUDA(ctx->p_lines.ensure((uint64_t)n_lines * 2 * sizeof(int4)));
-        RZ_CUDA(cudaMemsetAsync(ctx->d_ctrl.p, 0, 64, ctx->stream));
-        ctx->last_error.clear();
-    }
-    return RZ_OK;
+    // at most this many lines: beyond it every band reading every line costs more than the binned pipeline
+    constexpr size_t kSmallLines = 1u << 16;
+    RZ_CUDA(ctx->p_lines.ensure(kSmallLines * 2 * sizeof(int4)));
+    const uint64_t cap = kSmallLines;
+    S.lines = (int4*)ctx->p_lines.p;
+    S.line_cap = (uint32_t)cap;
+    S.n_lines = (uint32_t)cap;
+    S.n_lines_dev = counter;
+    S.pairs = nullptr;  // every band takes every line
+    tr.gpu_mark(ctx->stream, "upload");
+    RZ_CUDA(rz::launch_flatten_emit_alloc(S, counter, ctx->stream));
+    tr.gpu_mark(ctx->stream, "flatten_emit_alloc");
+    RZ_CUDA(rz::launch_composite(S, cov_stride, smem, ctx->stream));
+    tr.gpu_mark(ctx->stream, "composite");
+    return read_error(ctx);
 }
 
 rz_status run_pipeline(rz_ctx* ctx, HostScene& hs, double flatness, float* canvas, int64_t canvas_stride, int canvas_w,
@@ -1999,7 +1995,17 @@ rz_status run_pipeline(rz_ctx* ctx, HostScene& hs, double flatness, float* canva
                                 cudaMemcpyHostToDevice, ctx->stream));
         S.paints = (const rz::PaintDev*)ctx->p_paints.p;
     }
-    if (!paint_mode && !load_canvas && small_scene(hs, S)) return run_small(ctx, hs, S, cov_stride, smem, tr);
+    if (!paint_mode && !load_canvas && small_scene(hs, S)) {
+        rz::SceneDev S1 = S;
+        rz_status st = run_small(ctx, hs, S1, cov_stride, smem, tr);
+        if (st != RZ_ERR_CAPACITY) return st;
+        // more lines than the estimate: the binned pipeline below, over a cleared mask (its composite leaves
+        // bands without lines untouched)
+        RZ_CUDA(cudaMemset2DAsync(canvas, (size_t)canvas_stride * 4, 0, (size_t)canvas_w * 4, (size_t)canvas_h,
+                                  ctx->stream));
+        RZ_CUDA(cudaMemsetAsync(ctx->d_ctrl.p, 0, 64, ctx->stream));
+        ctx->last_error.clear();
+    }
     // the composite writes every pixel from bg (or leaves untouched mask bands zero): a pass
     // that ran out of list room can run again; over a loaded canvas the buffers are sized first
     const bool speculative = !load_canvas;

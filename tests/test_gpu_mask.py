@@ -279,6 +279,41 @@ def test_lines_kernel_matches_band_kernel(R, monkeypatch):
         assert_close(batch.mask(lines, i), O.mask(paths[i], Transform.identity(), rules[i], w, h))
 
 
+def _far_swinging_path():
+    """Ten cubics swinging 5e4 px left of a 512 x 512 view: beyond the 16.16
+    range (binary64 leaves, two lines each), trees 12 levels deep at flatness
+    0.005 (512 subtree tasks each, under the task cap), about 80 K lines; the
+    x < 0 parts become vertical lines on column 0.  And a 200-gon inside the
+    view."""
+    pb = PathBuilder()
+    pb.move_to((300.0, 4.0))
+    for k in range(10):
+        y0, y1 = 4.0 + 24.0 * k, 4.0 + 24.0 * (k + 1)
+        pb.cubic_to((-5.0e4, y0 + 6.0), (-5.0e4, y1 - 6.0), (300.0, y1))
+    pb.close()
+    pb.move_to((90.0, 60.0))
+    for i in range(1, 200):
+        a = 2.0 * math.pi * i / 200.0
+        pb.line_to((60.0 + 30.0 * math.cos(a), 60.0 + 30.0 * math.sin(a)))
+    pb.close()
+    return pb.build()
+
+
+def test_small_route_line_buffer_grows():
+    """A path whose task estimate is small (it takes the two-launch route for
+    small masks) but whose binary64 leaves take two line slots each: its
+    lines overflow what that route takes, so the call falls back to the
+    binned pipeline (which sizes its own buffers from the device's counts);
+    the mask matches the oracle, call after call."""
+    R2 = GpuRasterizer(flatness=0.005)
+    path = _far_swinging_path()
+    for rule in (FillRule.NonZero, FillRule.EvenOdd):
+        ref = O.mask(path, Transform.identity(), rule, 512, 512, flatness=0.005)
+        first = gpu_mask(R2, path, Transform.identity(), rule, 512, 512)
+        assert_close(first, ref)
+        assert np.array_equal(gpu_mask(R2, path, Transform.identity(), rule, 512, 512), first)
+
+
 def test_pipeline_line_buffers_grow():
     """The line pipeline sizes its buffers without a host round trip: a fresh
     context starts small, so its first large path runs out of room, is
