@@ -577,13 +577,28 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_scatter(SceneDev S) {
     }
     for (uint32_t i = threadIdx.x; i < n; i += kBinThreads) s_cnt[i] = 0u;
     __syncthreads();
-    // (the placement below takes one shared atomic per line and band anyway: a difference-coded count here
-    // measured no faster)
-    for (uint32_t l = l0 + threadIdx.x; l < l1; l += kBinThreads) {
-        const FillDev& f = S.fills[fill_of_line(S, l, fa, fb)];
-        int b0, b1;
-        line_bands(S, f, l, b0, b1);
-        for (int bb = b0; bb <= b1; ++bb) atomicAdd(&s_cnt[f.entry0 + (bb - f.band0) - e0], 1u);
+    // each thread's lines l0 + threadIdx.x + k kBinThreads: their first entry (relative to e0) and band count,
+    // kept in registers from the count to the placement
+    constexpr int kPer = kBinLines / kBinThreads;
+    uint32_t e_lo[kPer];
+    int nb[kPer];
+    #pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+        const uint32_t l = l0 + threadIdx.x + (uint32_t)k * kBinThreads;
+        e_lo[k] = 0u;
+        nb[k] = 0;
+        if (l < l1) {
+            const FillDev& f = S.fills[fill_of_line(S, l, fa, fb)];
+            int b0, b1;
+            line_bands(S, f, l, b0, b1);
+            if (b0 <= b1) {
+                e_lo[k] = f.entry0 + (uint32_t)(b0 - f.band0) - e0;
+                nb[k] = b1 - b0 + 1;
+            }
+        }
+        // (the placement below takes one shared atomic per line and band anyway: a difference-coded count
+        // here measured no faster)
+        for (int i = 0; i < nb[k]; ++i) atomicAdd(&s_cnt[e_lo[k] + i], 1u);
     }
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < n; i += kBinThreads) {
@@ -592,13 +607,12 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_scatter(SceneDev S) {
         s_cnt[i] = 0u;
     }
     __syncthreads();
-    for (uint32_t l = l0 + threadIdx.x; l < l1; l += kBinThreads) {
-        const FillDev& f = S.fills[fill_of_line(S, l, fa, fb)];
-        int b0, b1;
-        line_bands(S, f, l, b0, b1);
-        for (int bb = b0; bb <= b1; ++bb) {
-            const uint32_t i = f.entry0 + (bb - f.band0) - e0;
-            put_pair(S, s_base[i] + atomicAdd(&s_cnt[i], 1u), l);
+    #pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+        const uint32_t l = l0 + threadIdx.x + (uint32_t)k * kBinThreads;
+        for (int i = 0; i < nb[k]; ++i) {
+            const uint32_t e = e_lo[k] + (uint32_t)i;
+            put_pair(S, s_base[e] + atomicAdd(&s_cnt[e], 1u), l);
         }
     }
 }
