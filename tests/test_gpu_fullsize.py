@@ -12,12 +12,15 @@
   tree's line counts equal to the oracle's.
 * The scene composite (2,000 painted fills on a 2048 x 2048 RGBA f32 canvas)
   within 1e-4 per colour channel.
+* The differentiable batch (64 images of 1024 x 1024, 256 closed cubic paths
+  x 32 segments each): the first and last images within 1e-4 of the binary64
+  forward, their gradients within 2e-3 of the binary64 adjoint's scale.
 """
 import numpy as np
 import pytest
 
 from oracle import oracle as O
-from rasterize_gb300 import GpuRasterizer, MaskBatch, Transform
+from rasterize_gb300 import DiffBatch, GpuRasterizer, MaskBatch, Transform
 from rasterize_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -133,3 +136,40 @@ def test_scene_full_shape(R):
     ref = oracle_scene(sc, 2048, 2048, bg=bg)
     err = np.abs(gpu.astype(np.float64) - ref.astype(np.float64))
     assert err.max() <= TOL, "max %.3g mean %.3g" % (err.max(), err.mean())
+
+
+def test_diff_full_shape(R):
+    """The benchmark's differentiable batch: forward, L2 loss against targets
+    rendered from jittered control points, adjoint; images 0 and 63 and their
+    gradients against the oracle (each image's paths are independent of the
+    other images')."""
+    n, P, S, size = 64, 256, 32, 1024
+    ctrl, tctrl = W.diff_batch(seed=4, n_images=n, paths=P, segs=S, size=size)
+    dev = torch.device("cuda", 0)
+    c = torch.from_numpy(ctrl).to(dev)
+    t = torch.from_numpy(tctrl).to(dev)
+    img = torch.empty(n * size * size, dtype=torch.float32, device=dev)
+    tgt = torch.empty_like(img)
+    dl = torch.empty_like(img)
+    g = torch.empty(c.numel(), dtype=torch.float32, device=dev)
+    R.diff_forward(DiffBatch(n, P, S, size, size, t.data_ptr()), tgt.data_ptr())
+    b = DiffBatch(n, P, S, size, size, c.data_ptr())
+    R.diff_forward(b, img.data_ptr())
+    R.l2_loss(img.data_ptr(), tgt.data_ptr(), img.numel(), dl.data_ptr())
+    R.diff_backward(b, img.data_ptr(), dl.data_ptr(), g.data_ptr())
+    torch.cuda.synchronize()
+    A = img.cpu().numpy().reshape(n, size, size)
+    T = tgt.cpu().numpy().reshape(n, size, size)
+    G = g.cpu().numpy().reshape(ctrl.shape)
+    assert np.isfinite(A).all() and np.isfinite(G).all()
+    for i in (0, n - 1):
+        ref = O.diff_forward(ctrl[i].astype(np.float64), P, S, size, size)
+        err = np.abs(A[i] - ref)
+        assert err.max() <= TOL, "image %d: max %.3g mean %.3g" % (i, err.max(), err.mean())
+        ref_t = O.diff_forward(tctrl[i].astype(np.float64), P, S, size, size)
+        assert np.abs(T[i] - ref_t).max() <= TOL
+        ref_g = O.diff_backward(ctrl[i].astype(np.float64), P, S, size, size, ref,
+                                2.0 * (ref - T[i].astype(np.float64)))
+        scale = np.abs(ref_g).max()
+        gerr = np.abs(G[i] - ref_g).max()
+        assert gerr <= 2e-3 * scale, "image %d: gradient max err %.3g, scale %.3g" % (i, gerr, scale)
