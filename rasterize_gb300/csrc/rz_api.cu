@@ -1694,9 +1694,11 @@ struct HostScene {
 
 // Flatten tasks per slot from each segment's root flatness (the reference's
 // formula on the transformed control points): a curve whose tree is about D
-// levels deep gets 2^(D - 3) subtree tasks (at most 1024), so every task walks
-// about 8 leaves however long the curve.  Closing lines and lines get one.
-void adaptive_tasks(HostScene& hs, double flatness) {
+// levels deep gets 2^(D - leaf_shift) subtree tasks (at most 1024), so every
+// task walks about 2^leaf_shift leaves however long the curve (8 by default;
+// small scenes, whose few tasks leave most SMs idle, take shorter ones).
+// Closing lines and lines get one.
+void adaptive_tasks(HostScene& hs, double flatness, int leaf_shift = 3) {
     const double thr = 16.0 * flatness * flatness;
     hs.task_off.assign((size_t)hs.n_slots + 1, 0);
     for (const rz::FillDev& f : hs.fills) {
@@ -1729,7 +1731,7 @@ void adaptive_tasks(HostScene& hs, double flatness) {
                             fl /= 16.0;
                             ++d;
                         }
-                        depth = std::min(10, std::max(0, d - 3));
+                        depth = std::min(10, std::max(0, d - leaf_shift));
                     }
                 }
                 hs.task_off[f.slot0 + i] = (uint32_t)depth;
@@ -1902,6 +1904,10 @@ rz_status grow_line_buffers(rz_ctx* ctx, const rz::SceneDev& S, uint32_t n_entri
 
 // Flatten + bin + composite on the device.  canvas: device buffer (RGBA
 // pixels when paints are given, else an f32 mask), stride in pixels.
+#ifndef RZ_SMALL_LEAF_SHIFT
+#define RZ_SMALL_LEAF_SHIFT 1
+#endif
+
 // A mask of one small fill (at most ~64 K lines expected, times its bands at most ~8 M): every band
 // reading every line costs less than the offsets scan, the per-band counts and lists and their launches.
 bool small_scene(const HostScene& hs, const rz::SceneDev& S) {
@@ -1996,6 +2002,8 @@ rz_status run_pipeline(rz_ctx* ctx, HostScene& hs, double flatness, float* canva
         S.paints = (const rz::PaintDev*)ctx->p_paints.p;
     }
     if (!paint_mode && !load_canvas && small_scene(hs, S)) {
+        // a few thousand tasks fill a fraction of the SMs: shorter tasks, more of them, cut the longest walk
+        if (!hs.task_off.empty()) adaptive_tasks(hs, flatness, RZ_SMALL_LEAF_SHIFT);
         rz::SceneDev S1 = S;
         rz_status st = run_small(ctx, hs, S1, cov_stride, smem, tr);
         if (st != RZ_ERR_CAPACITY) return st;

@@ -849,8 +849,10 @@ static __device__ __noinline__ void composite_slow_line(const SceneDev& S, const
 // colours stay in the canvas itself (L2-resident while the band is worked
 // on): only the coverage band takes shared memory, so bands are tall and the
 // per-fill work of a band covers many rows.
+// Masks: one 512-thread CTA per SM (the band takes the shared memory), so up
+// to 128 registers; paint: three 256-thread CTAs per SM.
 template <int THREADS>
-__global__ void __launch_bounds__(THREADS) k_composite(SceneDev S, int cov_stride) {
+__global__ void __launch_bounds__(THREADS, THREADS == 512 ? 1 : 3) k_composite(SceneDev S, int cov_stride) {
     extern __shared__ float4 sm4[];
     __shared__ PaintDev s_paint;
     __shared__ uint32_t s_slow[THREADS / 32][64];  // per warp: at most 31 queued + 32 new
@@ -902,23 +904,7 @@ __global__ void __launch_bounds__(THREADS) k_composite(SceneDev S, int cov_strid
         // time, so the slow route runs with full warps instead of a few lanes of every step.
         uint32_t* q = s_slow[threadIdx.x >> 5];
         int nq = 0;
-        for (uint32_t j0 = threadIdx.x & ~31u; j0 < n; j0 += THREADS) {
-            const uint32_t j = j0 + lane;
-            uint32_t l = j;
-            bool slow = false;
-            // slots and lines beyond the buffers (reported by the earlier passes) are skipped
-            bool have = j < n;  // (all: n is at most the line capacity)
-            if (!all) {
-                have = have && start + j < S.pair_cap;
-                if (have) l = S.pairs[start + j];
-                have = have && l < S.line_cap;
-            }
-            if (have) {
-                const int4 a = S.lines[2ull * l], b = S.lines[2ull * l + 1];
-                const VtxQ va = line_vtx(a, B.y0), vb = line_vtx(b, B.y0);
-                if (!all || (min(va.row, vb.row) <= rows + 1 && max(va.row, vb.row) >= -2))
-                    slow = !accumulate_vtx_short(B, va, vb);
-            }
+        auto queue_slow = [&](bool slow, uint32_t l) {  // (warp-uniform call)
             const unsigned m = __ballot_sync(0xffffffffu, slow);
             if (slow) q[nq + __popc(m & ((1u << lane) - 1u))] = l;
             nq += __popc(m);
@@ -927,6 +913,46 @@ __global__ void __launch_bounds__(THREADS) k_composite(SceneDev S, int cov_strid
                 nq -= 32;
                 composite_slow_line(S, B, q[nq + lane]);
                 __syncwarp();
+            }
+        };
+        if (all) {
+            // every line of the scene (n is at most the line capacity): most miss the band, so only the two
+            // row words are read first, four lines a thread at once, and the rest of a line only if it is near
+            constexpr int kU = 4;
+            for (uint32_t j0 = threadIdx.x & ~31u; j0 < n; j0 += kU * THREADS) {
+                int32_t ya[kU], yb[kU];
+                #pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const uint32_t j = j0 + (uint32_t)u * THREADS + lane;
+                    ya[u] = yb[u] = INT32_MIN;
+                    if (j < n) {
+                        ya[u] = S.lines[2ull * j].y;
+                        yb[u] = S.lines[2ull * j + 1].y;
+                    }
+                }
+                #pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const uint32_t j = j0 + (uint32_t)u * THREADS + lane;
+                    const int ra = (ya[u] >> 16) - B.y0, rb = (yb[u] >> 16) - B.y0;
+                    bool slow = false;
+                    if (j < n && min(ra, rb) <= rows + 1 && max(ra, rb) >= -2)
+                        slow = !accumulate_vtx_short(B, line_vtx(S.lines[2ull * j], B.y0),
+                                                     line_vtx(S.lines[2ull * j + 1], B.y0));
+                    queue_slow(slow, j);
+                }
+            }
+        } else {
+            for (uint32_t j0 = threadIdx.x & ~31u; j0 < n; j0 += THREADS) {
+                const uint32_t j = j0 + lane;
+                uint32_t l = 0;
+                bool slow = false;
+                // slots and lines beyond the buffers (reported by the earlier passes) are skipped
+                if (j < n && start + j < S.pair_cap) l = S.pairs[start + j];
+                if (j < n && start + j < S.pair_cap && l < S.line_cap) {
+                    const int4 a = S.lines[2ull * l], b = S.lines[2ull * l + 1];
+                    slow = !accumulate_vtx_short(B, line_vtx(a, B.y0), line_vtx(b, B.y0));
+                }
+                queue_slow(slow, l);
             }
         }
         __syncwarp();
