@@ -62,6 +62,25 @@ def test_forward_loss_and_gradient_match_oracle(R, rule, margin, w):
     assert gerr.max() <= 2e-3 * scale, (gerr.max(), scale)
 
 
+@pytest.mark.parametrize("w,h", [(1, 5), (3, 4), (7, 6), (33, 9)])
+def test_tiny_images(R, w, h):
+    """Images narrower than one 128-pixel scan step and than a word of the
+    adjoint's bitmask (the row spans and marked words clamp at the edges),
+    heights not multiples of the 8-row CTAs."""
+    n, P, S = 2, 3, 4
+    ctrl, _ = W.diff_batch(seed=9, n_images=n, paths=P, segs=S, size=h, margin=2.0)
+    ctrl[..., 0] *= w / float(h)
+    target = oracle_images(ctrl + np.float32(0.7), n, P, S, w, h, FillRule.NonZero).astype(np.float32)
+    img, loss, grad = run(R, ctrl, target, n, P, S, w, h, FillRule.NonZero)
+    ref = oracle_images(ctrl, n, P, S, w, h, FillRule.NonZero)
+    assert np.abs(img - ref).max() <= TOL
+    ref_grad = np.stack([O.diff_backward(ctrl[i].astype(np.float64), P, S, w, h, ref[i],
+                                         2.0 * (ref[i] - target[i].astype(np.float64)))
+                         for i in range(n)])
+    scale = max(np.abs(ref_grad).max(), 1e-6)
+    assert np.abs(grad - ref_grad).max() <= 2e-3 * scale
+
+
 def _fd_setup(seed=2, P=8, S=8, w=128, h=96):
     ctrl, target = W.diff_batch(seed=seed, n_images=1, paths=P, segs=S, size=h)
     ctrl[..., 0] *= w / float(h)

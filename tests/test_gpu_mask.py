@@ -68,6 +68,19 @@ def test_small_path_config(R):
                  O.mask(path, Transform.identity(), rule, w, h))
 
 
+@pytest.mark.parametrize("seed,w,h", [(1, 512, 512), (2, 509, 257), (3, 384, 130)])
+def test_small_route_rules_and_transforms(R, seed, w, h):
+    """Single masks of a few hundred curves (the two-launch route for small
+    masks: one flatten pass into a counter-reserved line buffer, every band
+    reading every line) under a rotation and a shear, both fill rules, odd
+    mask sizes whose last band is short."""
+    path, _, _ = W.small_path(seed=seed, n_cubics=300, size=512)
+    tr = Transform.new_translate(w / 2, h / 2) * Transform.new_rotate(0.3 * seed) * Transform.new_translate(-256, -256)
+    tr = tr.pre_scale(1.0, 0.6)
+    for rule in (FillRule.NonZero, FillRule.EvenOdd):
+        assert_close(gpu_mask(R, path, tr, rule, w, h), O.mask(path, tr, rule, w, h))
+
+
 @pytest.mark.parametrize("seed", range(6))
 def test_random_paths_both_rules(R, seed):
     rng = np.random.default_rng(100 + seed)
