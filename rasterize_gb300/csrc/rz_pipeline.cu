@@ -864,7 +864,7 @@ __global__ void __launch_bounds__(THREADS, THREADS == 512 ? 1 : 3) k_composite(S
     const int rows = min(S.band_rows, S.canvas_h - row_base);
     if (rows <= 0) return;
     // no lists (small scenes): a flatten pass that failed (too many lines) leaves nothing to do here
-    if (S.pairs == nullptr && *(volatile const int32_t*)S.err != 0) return;
+    if (S.pairs == nullptr && S.err != nullptr && *(volatile const int32_t*)S.err != 0) return;
     float4* canvas4 = reinterpret_cast<float4*>(S.canvas) + (int64_t)row_base * S.canvas_stride;
     if (paint_mode && !S.load_canvas) {
         const float4 v = S.bg ? make_float4(S.bg[0], S.bg[1], S.bg[2], S.bg[3]) : make_float4(0.f, 0.f, 0.f, 0.f);
